@@ -1,0 +1,302 @@
+"""Python binding of libarap_gb300.so (the C ABI in include/arap_gpu.h).
+
+Two layers:
+
+* ``ArapContext`` -- one-to-one wrapper of the C entry points (what a cgo/JNI
+  binding would look like), numpy arrays in and out.
+* ``AsRigidAsPossibleDeformation`` -- mirrors the reference's class template
+  ``deform::AsRigidAsPossibleDeformation`` (inc/deform/arap.h:49-466) over a
+  mesh adapter: ``set_constraint`` fills a map and marks the object dirty
+  (arap.h:81-85); ``deform(n)`` re-captures the rest pose from the mesh when
+  dirty (arap.h:102-120), iterates, and writes the positions back through the
+  adapter (arap.h:133-135). Returns False where the reference returns false.
+
+There is no CPU fallback: a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libarap_gb300.so"
+
+ARAP_OK = 0
+ARAP_ERR_INVALID_ARGUMENT = 1
+ARAP_ERR_BAD_INDEX = 2
+ARAP_ERR_NOT_SPD = 3
+ARAP_ERR_OUT_OF_MEMORY = 4
+ARAP_ERR_CUDA = 5
+ARAP_ERR_TIMEOUT = 6
+ARAP_ERR_ADMISSION_REFUSED = 7
+ARAP_ERR_NO_DEVICE = 8
+ARAP_ERR_UNSUPPORTED = 9
+
+PRECISION = {"fp64": 0, "mixed": 1}
+
+# Every symbol include/arap_gpu.h declares: (restype, argtypes).
+_P = C.c_void_p
+_I32 = C.c_int32
+_I64 = C.c_int64
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+_dp = C.POINTER(C.c_double)
+SIGNATURES = {
+    "arap_status_string": (C.c_char_p, [C.c_int]),
+    "arap_last_error": (C.c_char_p, [_P]),
+    "arap_create": (C.c_int, [_I32, _I32, _ip, _I32, C.POINTER(_P)]),
+    "arap_destroy": (None, [_P]),
+    "arap_set_precision": (C.c_int, [_P, _I32, _I32]),
+    "arap_set_rest_positions": (C.c_int, [_P, _dp]),
+    "arap_set_constraints": (C.c_int, [_P, _I32, _ip, _dp]),
+    "arap_deform": (C.c_int, [_P, _I32, _dp]),
+    "arap_invalidate": (C.c_int, [_P]),
+    "arap_get_positions": (C.c_int, [_P, _dp]),
+    "arap_edge_weights_nnz": (C.c_int, [_P, _ip]),
+    "arap_get_edge_weights": (C.c_int, [_P, _ip, _ip, _dp]),
+    "arap_get_rotations": (C.c_int, [_P, _dp]),
+    "arap_get_symbolic_sizes": (C.c_int, [_P, _ip, _ip, _lp]),
+    "arap_get_symbolic": (C.c_int, [_P, _ip, _ip, _ip]),
+    "arap_analyze_pattern": (C.c_int, [_I32, _I32, _ip, _I32, _ip, _ip, _ip, _lp, _ip, _ip, _ip]),
+    "arap_get_timing": (C.c_int, [_P, _dp, _dp]),
+    "arap_get_launch_count": (C.c_int, [_P, _lp]),
+}
+
+_lib = None
+
+
+def load(path: Path | str | None = None):
+    """Loads the library (and binds every declared symbol); raises if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with build_lib.build() (no CPU fallback exists)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class ArapError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_status_name(code)}: {msg}")
+        self.code = code
+
+
+def _status_name(code: int) -> str:
+    return load().arap_status_string(code).decode()
+
+
+def _i32(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _f64(a):
+    return a.ctypes.data_as(_dp)
+
+
+class ArapContext:
+    """Thin object wrapper over one ``arap_ctx``."""
+
+    def __init__(self, n_vertices: int, faces: np.ndarray, device: int = 0):
+        self.lib = load()
+        self.V = int(n_vertices)
+        self.faces = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+        h = _P()
+        rc = self.lib.arap_create(self.V, len(self.faces), _i32(self.faces), int(device), C.byref(h))
+        if rc != ARAP_OK:
+            raise ArapError(rc, self.lib.arap_last_error(None).decode())
+        self.h = h
+
+    def _check(self, rc: int):
+        if rc != ARAP_OK:
+            raise ArapError(rc, self.lib.arap_last_error(self.h).decode())
+
+    def status(self, rc: int) -> int:
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.arap_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_precision(self, precision: str = "fp64", refine_steps: int = 2):
+        self._check(self.lib.arap_set_precision(self.h, PRECISION[precision], int(refine_steps)))
+
+    def set_rest_positions(self, xyz: np.ndarray):
+        a = np.ascontiguousarray(xyz, dtype=np.float64).reshape(self.V, 3)
+        self._check(self.lib.arap_set_rest_positions(self.h, _f64(a)))
+
+    def set_constraints(self, idx, xyz):
+        i = np.ascontiguousarray(idx, dtype=np.int32).reshape(-1)
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        self._check(self.lib.arap_set_constraints(self.h, len(i), _i32(i), _f64(x)))
+
+    def deform_rc(self, iterations: int, out: np.ndarray | None = None) -> int:
+        ptr = _f64(out) if out is not None else None
+        return self.lib.arap_deform(self.h, int(iterations), ptr)
+
+    def deform(self, iterations: int, want_output: bool = True) -> np.ndarray | None:
+        out = np.empty((self.V, 3), np.float64) if want_output else None
+        self._check(self.deform_rc(iterations, out))
+        return out
+
+    def invalidate(self):
+        self._check(self.lib.arap_invalidate(self.h))
+
+    def positions(self) -> np.ndarray:
+        out = np.empty((self.V, 3), np.float64)
+        self._check(self.lib.arap_get_positions(self.h, _f64(out)))
+        return out
+
+    def edge_weights(self):
+        nnz = C.c_int32()
+        self._check(self.lib.arap_edge_weights_nnz(self.h, C.byref(nnz)))
+        rp = np.zeros(self.V + 1, np.int32)
+        col = np.zeros(max(nnz.value, 1), np.int32)
+        val = np.zeros(max(nnz.value, 1), np.float64)
+        self._check(self.lib.arap_get_edge_weights(self.h, _i32(rp), _i32(col), _f64(val)))
+        return rp, col[: nnz.value], val[: nnz.value]
+
+    def rotations(self) -> np.ndarray:
+        out = np.empty((self.V, 3, 3), np.float64)
+        self._check(self.lib.arap_get_rotations(self.h, _f64(out)))
+        return out
+
+    def symbolic(self):
+        m, s, nz = C.c_int32(), C.c_int32(), C.c_int64()
+        self._check(self.lib.arap_get_symbolic_sizes(self.h, C.byref(m), C.byref(s), C.byref(nz)))
+        perm = np.zeros(max(m.value, 1), np.int32)
+        et = np.zeros(max(m.value, 1), np.int32)
+        bp = np.zeros(s.value + 1, np.int32)
+        self._check(self.lib.arap_get_symbolic(self.h, _i32(perm), _i32(et), _i32(bp)))
+        return {"m": m.value, "perm": perm[: m.value], "etree": et[: m.value], "block_ptr": bp,
+                "factor_nnz": nz.value}
+
+    def timing(self):
+        a, b = C.c_double(), C.c_double()
+        self._check(self.lib.arap_get_timing(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.arap_get_launch_count(self.h, C.byref(n)))
+        return n.value
+
+
+def analyze_pattern(n_vertices: int, faces: np.ndarray, constrained) -> dict:
+    """Host-only symbolic analysis (no GPU needed), see arap_analyze_pattern."""
+    lib = load()
+    f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+    c = np.ascontiguousarray(constrained, dtype=np.int32).reshape(-1)
+    V = int(n_vertices)
+    perm = np.zeros(max(V, 1), np.int32)
+    et = np.zeros(max(V, 1), np.int32)
+    bp = np.zeros(V + 1, np.int32)
+    m, s, nz = C.c_int32(), C.c_int32(), C.c_int64()
+    rc = lib.arap_analyze_pattern(V, len(f), _i32(f), len(c), _i32(c) if len(c) else None, C.byref(m),
+                                  C.byref(s), C.byref(nz), _i32(perm), _i32(et), _i32(bp))
+    if rc != ARAP_OK:
+        raise ArapError(rc, lib.arap_last_error(None).decode())
+    return {"m": m.value, "perm": perm[: m.value], "etree": et[: m.value], "block_ptr": bp[: s.value + 1],
+            "factor_nnz": nz.value}
+
+
+class ArrayMesh:
+    """Array-backed mesh adapter: the five accessors of the adapter concept
+    (inc/deform/openmesh_adapter.h:74-113) over numpy arrays."""
+
+    def __init__(self, positions: np.ndarray, faces: np.ndarray, scalar=np.float64):
+        self.scalar = scalar
+        self.positions = np.array(positions, dtype=scalar).reshape(-1, 3)
+        self.faces = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+
+    def number_of_vertices(self) -> int:
+        return len(self.positions)
+
+    def number_of_faces(self) -> int:
+        return len(self.faces)
+
+    def vertex_location(self, i, value=None):
+        if value is None:
+            return self.positions[i].copy()
+        self.positions[i] = value
+
+    def face(self, i):
+        return self.faces[i]
+
+
+class AsRigidAsPossibleDeformation:
+    """deform::AsRigidAsPossibleDeformation<Mesh, PrecisionType> on the GPU.
+
+    ``precision`` "fp64" is PrecisionType=double; "mixed" is the FP32 GPU form
+    with FP64-residual refinement (the reference's PrecisionType=float maps here)."""
+
+    def __init__(self, mesh: ArrayMesh, precision: str = "fp64", refine_steps: int = 2, device: int = 0):
+        self.mesh = mesh
+        self.precision = precision
+        self.ctx = ArapContext(mesh.number_of_vertices(), mesh.faces, device)
+        self.ctx.set_precision(precision, refine_steps)
+        self.scalar = np.float64 if precision == "fp64" else np.float32
+        self._constraints: dict[int, np.ndarray] = {}
+        self._dirty = True
+
+    def set_constraint(self, vidx: int, loc) -> None:
+        """arap.h:81-85: store loc cast to the compute scalar, mark dirty."""
+        self._constraints[int(vidx)] = np.asarray(loc, dtype=self.scalar).astype(np.float64)
+        self._dirty = True
+
+    def deform(self, iterations: int) -> bool:
+        """arap.h:101-138."""
+        ctx = self.ctx
+        if self._dirty:
+            rest = self.mesh.positions.astype(self.scalar).astype(np.float64)
+            ctx.set_rest_positions(rest)
+            if self._constraints:
+                idx = np.fromiter(self._constraints.keys(), np.int32, len(self._constraints))
+                xyz = np.stack([self._constraints[int(i)] for i in idx])
+            else:
+                idx = np.zeros(0, np.int32)
+                xyz = np.zeros((0, 3))
+            rc = ctx.lib.arap_set_constraints(ctx.h, len(idx), _i32(idx), _f64(np.ascontiguousarray(xyz)))
+            if rc != ARAP_OK:
+                return False
+        out = np.empty((ctx.V, 3), np.float64)
+        rc = ctx.deform_rc(iterations, out)
+        if rc == ARAP_ERR_NOT_SPD or rc == ARAP_ERR_BAD_INDEX:
+            return False
+        if rc != ARAP_OK:
+            raise ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+        if not self._constraints:
+            return True  # arap.h:113-114: stays dirty, no write-back
+        self._dirty = False
+        self.mesh.positions[:] = out.astype(self.mesh.scalar)
+        return True
+
+    def cotan_weights(self):
+        """PrivateAccessor<ARAP>::cotanWeights (tests/accessor.h:19-21) as a dense matrix."""
+        rp, col, val = self.ctx.edge_weights()
+        W = np.zeros((self.ctx.V, self.ctx.V))
+        for i in range(self.ctx.V):
+            W[i, col[rp[i]:rp[i + 1]]] = val[rp[i]:rp[i + 1]]
+        return W

@@ -1,0 +1,623 @@
+// arap_context.cu -- the C ABI (include/arap_gpu.h): context state, setup and
+// the local/global iteration loop of deform() (inc/deform/arap.h:101-138).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/arap_gpu.h"
+#include "arap_kernels.h"
+#include "arap_symbolic.h"
+
+namespace arapgpu {
+cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64);
+}
+
+using namespace arapgpu;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+thread_local std::string g_create_error;
+
+}  // namespace
+
+struct arap_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    std::string err;
+    Topology topo;
+    // inputs
+    bool have_rest = false;
+    std::vector<int32_t> cidx;    // sorted unique constrained vertices
+    std::vector<double> ctgt;     // 3 per constrained vertex (sorted order)
+    std::vector<uint8_t> cmask;   // V
+    int precision = ARAP_PRECISION_FP64;
+    int refine = 2;
+    bool dirty = true;
+    // symbolic cache (keyed by the constrained-vertex mask)
+    bool sym_valid = false;
+    Symbolic sym;
+    int smem_rows = 0;
+    // which precision the iteration state was set up for
+    int state_prec = -1;
+    bool have_rotations = false;
+    // device buffers
+    DevBuf faces, ent_ptr, ent_fc, hc, w_orig;
+    DevBuf rest, targets, out;
+    DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn;
+    DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd;
+    DevBuf errw, ticket, flags;
+    DevTopo dt{};
+    DevSym ds{};
+    int64_t launches = 0;
+    double setup_ms = 0.0, iter_ms = 0.0;
+};
+
+#define CK(call)                                                                       \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);             \
+            return e_ == cudaErrorMemoryAllocation ? ARAP_ERR_OUT_OF_MEMORY : ARAP_ERR_CUDA; \
+        }                                                                              \
+    } while (0)
+
+namespace {
+
+template <typename T>
+cudaError_t upload(DevBuf &buf, const std::vector<T> &v, cudaStream_t st) {
+    cudaError_t e = buf.ensure(v.size() * sizeof(T));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+int fail(arap_ctx *ctx, int code, const std::string &msg) {
+    ctx->err = msg;
+    return code;
+}
+
+// Builds (or reuses) the symbolic analysis for the current constraint mask and
+// uploads it.
+int prepare_symbolic(arap_ctx *ctx) {
+    if (ctx->sym_valid && ctx->sym.constrained == ctx->cmask) return ARAP_OK;
+    ctx->sym_valid = false;
+    std::string err;
+    bool singular = false;
+    if (!build_symbolic(ctx->topo, ctx->cmask, ctx->sym, err, singular))
+        return fail(ctx, singular ? ARAP_ERR_NOT_SPD : ARAP_ERR_CUDA, err);
+    Symbolic &s = ctx->sym;
+    cudaStream_t st = ctx->stream;
+    CK(upload(ctx->drow, s.drow, st));
+    CK(upload(ctx->dcol, s.dcol, st));
+    CK(upload(ctx->dent, s.dent, st));
+    CK(upload(ctx->oldidx, s.oldidx, st));
+    CK(upload(ctx->amap, s.amap, st));
+    CK(upload(ctx->dmap, s.dmap, st));
+    CK(upload(ctx->sn, s.sn, st));
+    CK(upload(ctx->rows, s.rows, st));
+    CK(upload(ctx->relind, s.relind, st));
+    CK(upload(ctx->child, s.child, st));
+    CK(upload(ctx->level_sn, s.level_sn, st));
+    // solve scheduling state: ticket counters and per-supernode flags start at 0
+    CK(ctx->ticket.ensure(2 * sizeof(unsigned long long)));
+    CK(ctx->flags.ensure(2 * sizeof(unsigned) * (size_t)std::max(s.S, 1)));
+    CK(cudaMemsetAsync(ctx->ticket.p, 0, 2 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
+    const int rows_needed = std::max(s.max_nrow, 1);
+    if ((size_t)rows_needed * sizeof(Vec4<double>) > 200 * 1024)
+        return fail(ctx, ARAP_ERR_UNSUPPORTED,
+                    "supernode front of " + std::to_string(s.max_nrow) + " rows exceeds the solve kernel limit");
+    if (rows_needed > ctx->smem_rows) {
+        CK(configure_solve_smem((int)(rows_needed * sizeof(Vec4<float>)), (int)(rows_needed * sizeof(Vec4<double>))));
+        ctx->smem_rows = rows_needed;
+    }
+    DevSym &d = ctx->ds;
+    d.V = s.V;
+    d.m = s.m;
+    d.S = s.S;
+    d.nnz = (int)s.dcol.size();
+    d.drow = ctx->drow.as<int32_t>();
+    d.dcol = ctx->dcol.as<int32_t>();
+    d.dent = ctx->dent.as<int32_t>();
+    d.oldidx = ctx->oldidx.as<int32_t>();
+    d.amap = ctx->amap.as<int64_t>();
+    d.dmap = ctx->dmap.as<int64_t>();
+    d.sn = ctx->sn.as<SnInfo>();
+    d.rows = ctx->rows.as<int32_t>();
+    d.relind = ctx->relind.as<int32_t>();
+    d.child = ctx->child.as<int32_t>();
+    d.level_sn = ctx->level_sn.as<int32_t>();
+    ctx->sym_valid = true;
+    return ARAP_OK;
+}
+
+template <typename T> struct PrecTag;
+template <> struct PrecTag<float> { static constexpr int value = ARAP_PRECISION_MIXED; };
+template <> struct PrecTag<double> { static constexpr int value = ARAP_PRECISION_FP64; };
+
+// Dirty-deform setup in precision T (FP64: T = double for everything; MIXED:
+// T = float for the local step, RHS, factor and solves).
+template <typename T>
+int setup_numeric(arap_ctx *ctx) {
+    const Symbolic &s = ctx->sym;
+    const DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    const int V = s.V, m = s.m;
+    const size_t nnz = s.dcol.size();
+    CK(ctx->w64.ensure(nnz * sizeof(double)));
+    if (sizeof(T) == 4) CK(ctx->w32.ensure(nnz * sizeof(float)));
+    CK(ctx->p64.ensure((size_t)V * sizeof(Vec4<double>)));
+    CK(ctx->pc64.ensure((size_t)V * sizeof(Vec4<double>)));
+    if (sizeof(T) == 4) {
+        CK(ctx->p32.ensure((size_t)V * sizeof(Vec4<float>)));
+        CK(ctx->pc32.ensure((size_t)V * sizeof(Vec4<float>)));
+    }
+    CK(ctx->R.ensure((size_t)V * 3 * sizeof(Vec4<T>)));
+    CK(ctx->diag64.ensure((size_t)std::max(m, 1) * sizeof(double)));
+    CK(ctx->bfixed.ensure((size_t)std::max(m, 1) * sizeof(Vec4<T>)));
+    CK(ctx->b.ensure((size_t)std::max(m, 1) * sizeof(Vec4<T>)));
+    CK(ctx->sol.ensure((size_t)std::max(m, 1) * sizeof(Vec4<T>)));
+    CK(ctx->uvec.ensure((size_t)std::max<int64_t>(s.uvec_size, 1) * sizeof(Vec4<T>)));
+    CK(ctx->Lval.ensure((size_t)std::max<int64_t>(s.panel_size, 1) * sizeof(T)));
+    CK(ctx->Dinv.ensure((size_t)std::max<int64_t>(s.dinv_size, 1) * sizeof(T)));
+    CK(ctx->Upd.ensure((size_t)std::max<int64_t>(s.upd_size, 1) * sizeof(T)));
+    CK(ctx->errw.ensure(sizeof(int)));
+    CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
+
+    // cotan weights (arap.h:182-239)
+    launch_edge_weights(ctx->dt, d, ctx->hc.as<double>(), ctx->w64.as<double>(),
+                        sizeof(T) == 4 ? ctx->w32.as<float>() : nullptr, ctx->w_orig.as<double>(), st);
+    // geometry, constraint snap, rotations = I
+    Vec4<T> *p_t = sizeof(T) == 4 ? ctx->p32.as<Vec4<T>>() : ctx->p64.as<Vec4<T>>();
+    Vec4<T> *pc_t = sizeof(T) == 4 ? ctx->pc32.as<Vec4<T>>() : ctx->pc64.as<Vec4<T>>();
+    launch_setup_vertices<T>(d, ctx->rest.as<double>(), ctx->targets.as<double>(), ctx->p64.as<Vec4<double>>(),
+                             ctx->pc64.as<Vec4<double>>(), p_t, pc_t, ctx->R.as<Vec4<T>>(), st);
+    ctx->launches += 2;
+    if (m > 0) {
+        CK(cudaMemsetAsync(ctx->Lval.p, 0, (size_t)s.panel_size * sizeof(T), st));
+        if (s.upd_size > 0) CK(cudaMemsetAsync(ctx->Upd.p, 0, (size_t)s.upd_size * sizeof(T), st));
+        launch_assemble<T, T>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->Lval.as<T>(),
+                              ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<T>>(), st);
+        ctx->launches += 1;
+        const int nlev = (int)s.level_ptr.size() - 1;
+        for (int l = 0; l < nlev; ++l) {
+            launch_factor_level<T>(d, s.level_ptr[l], s.level_ptr[l + 1] - s.level_ptr[l], ctx->Lval.as<T>(),
+                                   ctx->Upd.as<T>(), ctx->Dinv.as<T>(), ctx->errw.as<int>(), st);
+            ctx->launches += 1;
+        }
+    }
+    CK(cudaGetLastError());
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (herr & kErrNotSpd) return fail(ctx, ARAP_ERR_NOT_SPD, "Cholesky factorisation met a non-positive pivot");
+    ctx->state_prec = PrecTag<T>::value;
+    ctx->have_rotations = true;
+    return ARAP_OK;
+}
+
+template <typename T>
+int run_iterations(arap_ctx *ctx, int iterations);
+
+template <>
+int run_iterations<double>(arap_ctx *ctx, int iterations) {
+    const Symbolic &s = ctx->sym;
+    const DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    unsigned long long *tk = ctx->ticket.as<unsigned long long>();
+    unsigned *fl = ctx->flags.as<unsigned>();
+    for (int it = 0; it < iterations; ++it) {
+        launch_local_step<double>(d, ctx->w64.as<double>(), ctx->p64.as<Vec4<double>>(),
+                                  ctx->pc64.as<Vec4<double>>(), ctx->R.as<Vec4<double>>(), st);
+        ctx->launches += 1;
+        if (s.m == 0) continue;
+        launch_rhs<double>(d, ctx->w64.as<double>(), ctx->p64.as<Vec4<double>>(), ctx->R.as<Vec4<double>>(),
+                           ctx->bfixed.as<Vec4<double>>(), ctx->sol.as<Vec4<double>>(), st);
+        launch_solve_fwd<double>(d, ctx->Lval.as<double>(), ctx->Dinv.as<double>(), ctx->sol.as<Vec4<double>>(),
+                                 ctx->uvec.as<Vec4<double>>(), tk, fl, ctx->errw.as<int>(), ctx->smem_rows, st);
+        launch_solve_bwd<double>(d, ctx->Lval.as<double>(), ctx->Dinv.as<double>(), ctx->sol.as<Vec4<double>>(),
+                                 ctx->pc64.as<Vec4<double>>(), nullptr, 0, tk + 1, fl + s.S, ctx->errw.as<int>(),
+                                 ctx->smem_rows, st);
+        ctx->launches += 3;
+    }
+    CK(cudaGetLastError());
+    return ARAP_OK;
+}
+
+template <>
+int run_iterations<float>(arap_ctx *ctx, int iterations) {
+    const Symbolic &s = ctx->sym;
+    const DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    unsigned long long *tk = ctx->ticket.as<unsigned long long>();
+    unsigned *fl = ctx->flags.as<unsigned>();
+    for (int it = 0; it < iterations; ++it) {
+        launch_local_step<float>(d, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->pc32.as<Vec4<float>>(),
+                                 ctx->R.as<Vec4<float>>(), st);
+        ctx->launches += 1;
+        if (s.m == 0) continue;
+        launch_rhs<float>(d, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->R.as<Vec4<float>>(),
+                          ctx->bfixed.as<Vec4<float>>(), ctx->b.as<Vec4<float>>(), st);
+        ctx->launches += 1;
+        for (int r = 0; r <= ctx->refine; ++r) {
+            launch_residual(d, ctx->w64.as<double>(), ctx->diag64.as<double>(), ctx->b.as<Vec4<float>>(),
+                            ctx->pc64.as<Vec4<double>>(), ctx->sol.as<Vec4<float>>(), st);
+            launch_solve_fwd<float>(d, ctx->Lval.as<float>(), ctx->Dinv.as<float>(), ctx->sol.as<Vec4<float>>(),
+                                    ctx->uvec.as<Vec4<float>>(), tk, fl, ctx->errw.as<int>(), ctx->smem_rows, st);
+            launch_solve_bwd<float>(d, ctx->Lval.as<float>(), ctx->Dinv.as<float>(), ctx->sol.as<Vec4<float>>(),
+                                    ctx->pc64.as<Vec4<double>>(), ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S,
+                                    ctx->errw.as<int>(), ctx->smem_rows, st);
+            ctx->launches += 3;
+        }
+    }
+    CK(cudaGetLastError());
+    return ARAP_OK;
+}
+
+int check_ctx(const arap_ctx *ctx) { return ctx ? ARAP_OK : ARAP_ERR_INVALID_ARGUMENT; }
+
+}  // namespace
+
+extern "C" {
+
+const char *arap_status_string(int status) {
+    switch (status) {
+    case ARAP_OK: return "ARAP_OK";
+    case ARAP_ERR_INVALID_ARGUMENT: return "ARAP_ERR_INVALID_ARGUMENT";
+    case ARAP_ERR_BAD_INDEX: return "ARAP_ERR_BAD_INDEX";
+    case ARAP_ERR_NOT_SPD: return "ARAP_ERR_NOT_SPD";
+    case ARAP_ERR_OUT_OF_MEMORY: return "ARAP_ERR_OUT_OF_MEMORY";
+    case ARAP_ERR_CUDA: return "ARAP_ERR_CUDA";
+    case ARAP_ERR_TIMEOUT: return "ARAP_ERR_TIMEOUT";
+    case ARAP_ERR_ADMISSION_REFUSED: return "ARAP_ERR_ADMISSION_REFUSED";
+    case ARAP_ERR_NO_DEVICE: return "ARAP_ERR_NO_DEVICE";
+    case ARAP_ERR_UNSUPPORTED: return "ARAP_ERR_UNSUPPORTED";
+    default: return "ARAP_ERR_UNKNOWN";
+    }
+}
+
+const char *arap_last_error(const arap_ctx *ctx) {
+    return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+int arap_create(int32_t n_vertices, int32_t n_faces, const int32_t *faces, int32_t device, arap_ctx **out) {
+    g_create_error.clear();
+    if (!out || n_vertices < 0 || n_faces < 0 || (n_faces > 0 && !faces)) {
+        g_create_error = "arap_create: invalid argument";
+        return ARAP_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        g_create_error = "no CUDA device visible";
+        return ARAP_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= ndev) {
+        g_create_error = "device ordinal out of range";
+        return ARAP_ERR_INVALID_ARGUMENT;
+    }
+    arap_ctx *ctx = new arap_ctx();
+    ctx->device = device;
+    std::string err;
+    if (!build_topology(n_vertices, n_faces, faces, ctx->topo, err)) {
+        g_create_error = err;
+        delete ctx;
+        return ARAP_ERR_BAD_INDEX;
+    }
+    ctx->cmask.assign(n_vertices, 0);
+    auto bail = [&](cudaError_t e, const char *what) {
+        g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
+        arap_destroy(ctx);
+        return e == cudaErrorMemoryAllocation ? ARAP_ERR_OUT_OF_MEMORY : ARAP_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e, "cudaSetDevice");
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&ctx->ev2)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    const Topology &t = ctx->topo;
+    if ((e = upload(ctx->faces, t.faces, ctx->stream)) != cudaSuccess) return bail(e, "upload faces");
+    if ((e = upload(ctx->ent_ptr, t.ent_ptr, ctx->stream)) != cudaSuccess) return bail(e, "upload adjacency");
+    if ((e = upload(ctx->ent_fc, t.ent_fc, ctx->stream)) != cudaSuccess) return bail(e, "upload adjacency");
+    if ((e = ctx->hc.ensure((size_t)3 * std::max(n_faces, 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->w_orig.ensure((size_t)std::max(t.nnz(), 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->rest.ensure((size_t)3 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->targets.ensure((size_t)3 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->out.ensure((size_t)9 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return bail(e, "sync");
+    ctx->dt.V = n_vertices;
+    ctx->dt.F = n_faces;
+    ctx->dt.nnz = t.nnz();
+    ctx->dt.faces = ctx->faces.as<int32_t>();
+    ctx->dt.ent_ptr = ctx->ent_ptr.as<int32_t>();
+    ctx->dt.ent_fc = ctx->ent_fc.as<int32_t>();
+    *out = ctx;
+    return ARAP_OK;
+}
+
+void arap_destroy(arap_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    DevBuf *bufs[] = {&ctx->faces, &ctx->ent_ptr, &ctx->ent_fc, &ctx->hc, &ctx->w_orig, &ctx->rest,
+                      &ctx->targets, &ctx->out, &ctx->drow, &ctx->dcol, &ctx->dent, &ctx->oldidx,
+                      &ctx->amap, &ctx->dmap, &ctx->sn, &ctx->rows, &ctx->relind, &ctx->child,
+                      &ctx->level_sn, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
+                      &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
+                      &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->errw, &ctx->ticket,
+                      &ctx->flags};
+    for (DevBuf *b : bufs) b->release();
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev2) cudaEventDestroy(ctx->ev2);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int arap_set_precision(arap_ctx *ctx, int32_t precision, int32_t refine_steps) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (precision != ARAP_PRECISION_FP64 && precision != ARAP_PRECISION_MIXED)
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (refine_steps < 0 || refine_steps > 8) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "refine_steps outside 0..8");
+    ctx->precision = precision;
+    ctx->refine = refine_steps;
+    ctx->dirty = true;
+    return ARAP_OK;
+}
+
+int arap_set_rest_positions(arap_ctx *ctx, const double *xyz) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (!xyz && ctx->topo.V > 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "null positions");
+    cudaSetDevice(ctx->device);
+    if (ctx->topo.V > 0)
+        CK(cudaMemcpyAsync(ctx->rest.p, xyz, (size_t)3 * ctx->topo.V * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    ctx->have_rest = true;
+    ctx->dirty = true;
+    return ARAP_OK;
+}
+
+int arap_set_constraints(arap_ctx *ctx, int32_t n, const int32_t *indices, const double *xyz) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (n < 0 || (n > 0 && (!indices || !xyz))) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "invalid constraint arrays");
+    const int V = ctx->topo.V;
+    for (int i = 0; i < n; ++i)
+        if (indices[i] < 0 || indices[i] >= V)
+            return fail(ctx, ARAP_ERR_BAD_INDEX,
+                        "constraint index " + std::to_string(indices[i]) + " outside [0, " + std::to_string(V) + ")");
+    // map semantics: the last target given for a vertex wins
+    std::vector<int32_t> last(V, -1);
+    for (int i = 0; i < n; ++i) last[indices[i]] = i;
+    ctx->cidx.clear();
+    ctx->ctgt.clear();
+    std::fill(ctx->cmask.begin(), ctx->cmask.end(), 0);
+    for (int v = 0; v < V; ++v) {
+        if (last[v] < 0) continue;
+        ctx->cidx.push_back(v);
+        ctx->cmask[v] = 1;
+        const double *t = xyz + 3 * (size_t)last[v];
+        ctx->ctgt.insert(ctx->ctgt.end(), t, t + 3);
+    }
+    cudaSetDevice(ctx->device);
+    if (!ctx->ctgt.empty())
+        CK(cudaMemcpyAsync(ctx->targets.p, ctx->ctgt.data(), ctx->ctgt.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // the host vector may change on the next call
+    ctx->dirty = true;
+    return ARAP_OK;
+}
+
+int arap_invalidate(arap_ctx *ctx) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    ctx->dirty = true;
+    return ARAP_OK;
+}
+
+int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (iterations < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "negative iteration count");
+    if (!ctx->have_rest) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "rest positions not set");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    ctx->launches = 0;
+    ctx->setup_ms = ctx->iter_ms = 0.0;
+    const bool fp64 = ctx->precision == ARAP_PRECISION_FP64;
+    CK(cudaEventRecord(ctx->ev0, st));
+    if (ctx->dirty) {
+        launch_face_cots(ctx->dt, ctx->rest.as<double>(), ctx->hc.as<double>(), st);
+        ctx->launches += 1;
+        if (ctx->cidx.empty()) {
+            // arap.h:113-114: no constrained vertex -> weights only, no write-back
+            launch_edge_weights_orig(ctx->dt, ctx->hc.as<double>(), ctx->w_orig.as<double>(), st);
+            ctx->launches += 1;
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(st));
+            ctx->have_rotations = false;
+            return ARAP_OK;
+        }
+        int rc = prepare_symbolic(ctx);
+        if (rc != ARAP_OK) return rc;
+        rc = fp64 ? setup_numeric<double>(ctx) : setup_numeric<float>(ctx);
+        if (rc != ARAP_OK) return rc;
+        ctx->dirty = false;
+    }
+    CK(cudaEventRecord(ctx->ev1, st));
+    int rc = ctx->state_prec == ARAP_PRECISION_FP64 ? run_iterations<double>(ctx, iterations)
+                                                     : run_iterations<float>(ctx, iterations);
+    if (rc != ARAP_OK) return rc;
+    CK(cudaEventRecord(ctx->ev2, st));
+    if (out_xyz) {
+        launch_gather_positions(ctx->ds, ctx->pc64.as<Vec4<double>>(), ctx->out.as<double>(), st);
+        ctx->launches += 1;
+        CK(cudaMemcpyAsync(out_xyz, ctx->out.p, (size_t)3 * ctx->topo.V * sizeof(double), cudaMemcpyDeviceToHost,
+                           st));
+    }
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&b, ctx->ev1, ctx->ev2);
+    ctx->setup_ms = a;
+    ctx->iter_ms = b;
+    if (herr & kErrTimeout) {
+        // scheduling counters may be inconsistent now: rebuild them next time
+        ctx->sym_valid = false;
+        ctx->dirty = true;
+        return fail(ctx, ARAP_ERR_TIMEOUT, "a triangular-solve wait exceeded its bound");
+    }
+    return ARAP_OK;
+}
+
+int arap_get_positions(arap_ctx *ctx, double *out_xyz) {
+    if (check_ctx(ctx) || !out_xyz) return ARAP_ERR_INVALID_ARGUMENT;
+    if (!ctx->sym_valid || ctx->state_prec < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no deformed state yet");
+    CK(cudaSetDevice(ctx->device));
+    launch_gather_positions(ctx->ds, ctx->pc64.as<Vec4<double>>(), ctx->out.as<double>(), ctx->stream);
+    CK(cudaMemcpyAsync(out_xyz, ctx->out.p, (size_t)3 * ctx->topo.V * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ARAP_OK;
+}
+
+int arap_edge_weights_nnz(arap_ctx *ctx, int32_t *nnz) {
+    if (check_ctx(ctx) || !nnz) return ARAP_ERR_INVALID_ARGUMENT;
+    *nnz = ctx->topo.nnz();
+    return ARAP_OK;
+}
+
+int arap_get_edge_weights(arap_ctx *ctx, int32_t *rowptr, int32_t *col, double *val) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    const Topology &t = ctx->topo;
+    if (rowptr) std::memcpy(rowptr, t.rowptr.data(), t.rowptr.size() * sizeof(int32_t));
+    if (col && t.nnz()) std::memcpy(col, t.col.data(), t.col.size() * sizeof(int32_t));
+    if (val && t.nnz()) {
+        CK(cudaSetDevice(ctx->device));
+        CK(cudaMemcpyAsync(val, ctx->w_orig.p, (size_t)t.nnz() * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return ARAP_OK;
+}
+
+int arap_get_rotations(arap_ctx *ctx, double *R9) {
+    if (check_ctx(ctx) || !R9) return ARAP_ERR_INVALID_ARGUMENT;
+    const int V = ctx->topo.V;
+    if (!ctx->have_rotations || !ctx->sym_valid) {
+        for (int v = 0; v < V; ++v)
+            for (int a = 0; a < 9; ++a) R9[9 * v + a] = (a % 4 == 0) ? 1.0 : 0.0;
+        return ARAP_OK;
+    }
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->state_prec == ARAP_PRECISION_FP64)
+        launch_gather_rotations<double>(ctx->ds, ctx->R.as<Vec4<double>>(), ctx->out.as<double>(), ctx->stream);
+    else
+        launch_gather_rotations<float>(ctx->ds, ctx->R.as<Vec4<float>>(), ctx->out.as<double>(), ctx->stream);
+    CK(cudaMemcpyAsync(R9, ctx->out.p, (size_t)9 * V * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ARAP_OK;
+}
+
+int arap_get_symbolic_sizes(arap_ctx *ctx, int32_t *n_free, int32_t *n_blocks, int64_t *factor_nnz) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (!ctx->sym_valid) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no symbolic analysis yet");
+    if (n_free) *n_free = ctx->sym.m;
+    if (n_blocks) *n_blocks = ctx->sym.S;
+    if (factor_nnz) *factor_nnz = ctx->sym.factor_nnz;
+    return ARAP_OK;
+}
+
+int arap_get_symbolic(arap_ctx *ctx, int32_t *perm, int32_t *etree, int32_t *block_ptr) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (!ctx->sym_valid) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no symbolic analysis yet");
+    const Symbolic &s = ctx->sym;
+    if (perm && s.m) std::memcpy(perm, s.perm.data(), (size_t)s.m * sizeof(int32_t));
+    if (etree && s.m) std::memcpy(etree, s.etree.data(), (size_t)s.m * sizeof(int32_t));
+    if (block_ptr) std::memcpy(block_ptr, s.block_ptr.data(), s.block_ptr.size() * sizeof(int32_t));
+    return ARAP_OK;
+}
+
+int arap_analyze_pattern(int32_t n_vertices, int32_t n_faces, const int32_t *faces, int32_t n_constrained,
+                         const int32_t *constrained, int32_t *n_free, int32_t *n_blocks, int64_t *factor_nnz,
+                         int32_t *perm, int32_t *etree, int32_t *block_ptr) {
+    g_create_error.clear();
+    if (n_vertices < 0 || n_faces < 0 || n_constrained < 0 || (n_faces > 0 && !faces) ||
+        (n_constrained > 0 && !constrained)) {
+        g_create_error = "arap_analyze_pattern: invalid argument";
+        return ARAP_ERR_INVALID_ARGUMENT;
+    }
+    Topology topo;
+    std::string err;
+    if (!build_topology(n_vertices, n_faces, faces, topo, err)) {
+        g_create_error = err;
+        return ARAP_ERR_BAD_INDEX;
+    }
+    std::vector<uint8_t> mask(n_vertices, 0);
+    for (int i = 0; i < n_constrained; ++i) {
+        if (constrained[i] < 0 || constrained[i] >= n_vertices) {
+            g_create_error = "constraint index outside the mesh";
+            return ARAP_ERR_BAD_INDEX;
+        }
+        mask[constrained[i]] = 1;
+    }
+    Symbolic s;
+    bool singular = false;
+    if (!build_symbolic(topo, mask, s, err, singular)) {
+        g_create_error = err;
+        return singular ? ARAP_ERR_NOT_SPD : ARAP_ERR_UNSUPPORTED;
+    }
+    if (n_free) *n_free = s.m;
+    if (n_blocks) *n_blocks = s.S;
+    if (factor_nnz) *factor_nnz = s.factor_nnz;
+    if (perm && s.m) std::memcpy(perm, s.perm.data(), (size_t)s.m * sizeof(int32_t));
+    if (etree && s.m) std::memcpy(etree, s.etree.data(), (size_t)s.m * sizeof(int32_t));
+    if (block_ptr) std::memcpy(block_ptr, s.block_ptr.data(), s.block_ptr.size() * sizeof(int32_t));
+    return ARAP_OK;
+}
+
+int arap_get_timing(arap_ctx *ctx, double *setup_ms, double *iterations_ms) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (setup_ms) *setup_ms = ctx->setup_ms;
+    if (iterations_ms) *iterations_ms = ctx->iter_ms;
+    return ARAP_OK;
+}
+
+int arap_get_launch_count(arap_ctx *ctx, int64_t *launches) {
+    if (check_ctx(ctx) || !launches) return ARAP_ERR_INVALID_ARGUMENT;
+    *launches = ctx->launches;
+    return ARAP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,881 @@
+// arap_kernels.cu -- sm_103a kernels of the ARAP hot path.
+//
+// Reference: cheind/mesh-deform inc/deform/arap.h. Each kernel names the lines
+// it replaces. Layouts are described in arap_kernels.h.
+#include "arap_kernels.h"
+
+#include <cstdio>
+
+namespace arapgpu {
+
+namespace {
+
+constexpr int NB = kDiagBlock;  // diagonal block width (32)
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait until *p >= target; on expiry records kErrTimeout and returns.
+__device__ __forceinline__ void wait_flag(const unsigned *p, unsigned target, int *err) {
+    for (unsigned it = 0; it < kSpinLimit; ++it) {
+        if (ld_acquire(p) >= target) return;
+        __nanosleep(100);
+    }
+    atomicOr(err, kErrTimeout);
+}
+
+template <typename T> __device__ __forceinline__ Vec4<T> ldcg4(const Vec4<T> *p);
+template <> __device__ __forceinline__ Vec4<float> ldcg4(const Vec4<float> *p) {
+    float4 v = __ldcg(reinterpret_cast<const float4 *>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+template <> __device__ __forceinline__ Vec4<double> ldcg4(const Vec4<double> *p) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    double2 a = __ldcg(q), b = __ldcg(q + 1);
+    return {a.x, a.y, b.x, b.y};
+}
+
+template <typename T> __device__ __forceinline__ T tsqrt(T x);
+template <> __device__ __forceinline__ float tsqrt(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double tsqrt(double x) { return sqrt(x); }
+
+template <typename T> struct Eps;
+template <> struct Eps<float> { static constexpr float v = 1.1920929e-07f; };
+template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; };
+
+// ---------------------------------------------------------------------------
+// cotan weights
+
+// computeCotanWeights, arap.h:189-222, per face: the three clamped cotangents
+// times 1/2, rounded exactly as the FP64 CPU code (no fused multiply-adds).
+__global__ void k_face_cots(int F, const int32_t *__restrict__ faces, const double *__restrict__ xyz,
+                            double *__restrict__ hc) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
+    const double *v0 = xyz + 3 * (int64_t)i0, *v1 = xyz + 3 * (int64_t)i1, *v2 = xyz + 3 * (int64_t)i2;
+    double l0 = 0.0, l1 = 0.0, l2 = 0.0, d;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { d = __dsub_rn(v1[c], v0[c]); l0 = __dadd_rn(l0, __dmul_rn(d, d)); }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { d = __dsub_rn(v2[c], v1[c]); l1 = __dadd_rn(l1, __dmul_rn(d, d)); }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { d = __dsub_rn(v0[c], v2[c]); l2 = __dadd_rn(l2, __dmul_rn(d, d)); }
+    // std::max<Scalar>(1e-8, x) = (1e-8 < x) ? x : 1e-8
+    l0 = (1e-8 < l0) ? l0 : 1e-8;
+    l1 = (1e-8 < l1) ? l1 : 1e-8;
+    l2 = (1e-8 < l2) ? l2 : 1e-8;
+    l0 = __dsqrt_rn(l0);
+    l1 = __dsqrt_rn(l1);
+    l2 = __dsqrt_rn(l2);
+    const double semip = __dmul_rn(0.5, __dadd_rn(__dadd_rn(l0, l1), l2));
+    double h = __dmul_rn(__dmul_rn(__dmul_rn(semip, __dsub_rn(semip, l0)), __dsub_rn(semip, l1)),
+                         __dsub_rn(semip, l2));
+    double area = __dsqrt_rn(h);
+    area = (1e-8 < area) ? area : 1e-8;  // NaN from a negative product also gives 1e-8
+    const double denom = __ddiv_rn(1.0, __dmul_rn(4.0, area));
+    const double s0 = __dmul_rn(l0, l0), s1 = __dmul_rn(l1, l1), s2 = __dmul_rn(l2, l2);
+    double c0 = __dmul_rn(__dadd_rn(__dadd_rn(-s0, s1), s2), denom);
+    double c1 = __dmul_rn(__dadd_rn(__dsub_rn(s0, s1), s2), denom);
+    double c2 = __dmul_rn(__dsub_rn(__dadd_rn(s0, s1), s2), denom);
+    c0 = (1e-10 < c0) ? c0 : 1e-10;
+    c1 = (1e-10 < c1) ? c1 : 1e-10;
+    c2 = (1e-10 < c2) ? c2 : 1e-10;
+    hc[3 * (int64_t)f + 0] = __dmul_rn(c0, 0.5);
+    hc[3 * (int64_t)f + 1] = __dmul_rn(c1, 0.5);
+    hc[3 * (int64_t)f + 2] = __dmul_rn(c2, 0.5);
+}
+
+// setFromTriplets (arap.h:238): contributions of an edge summed in face order.
+__device__ __forceinline__ double edge_weight(const int32_t *ent_ptr, const int32_t *ent_fc, const double *hc,
+                                              int e) {
+    const int b = ent_ptr[e], t = ent_ptr[e + 1];
+    double w = hc[ent_fc[b]];
+    for (int q = b + 1; q < t; ++q) w = __dadd_rn(w, hc[ent_fc[q]]);
+    return w;
+}
+
+__global__ void k_edge_weights(int nnz, const int32_t *__restrict__ dent, const int32_t *__restrict__ ent_ptr,
+                               const int32_t *__restrict__ ent_fc, const double *__restrict__ hc,
+                               double *__restrict__ w64, float *__restrict__ w32, double *__restrict__ w_orig) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nnz) return;
+    const int o = dent[e];
+    const double w = edge_weight(ent_ptr, ent_fc, hc, o);
+    if (w64) w64[e] = w;
+    if (w32) w32[e] = (float)w;
+    if (w_orig) w_orig[o] = w;
+}
+
+__global__ void k_edge_weights_orig(int nnz, const int32_t *__restrict__ ent_ptr, const int32_t *__restrict__ ent_fc,
+                                    const double *__restrict__ hc, double *__restrict__ w_orig) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nnz) return;
+    w_orig[e] = edge_weight(ent_ptr, ent_fc, hc, e);
+}
+
+// ---------------------------------------------------------------------------
+// per-vertex setup
+
+template <typename T>
+__global__ void k_setup_vertices(int V, int m, const int32_t *__restrict__ oldidx, const double *__restrict__ rest,
+                                 const double *__restrict__ targets, Vec4<double> *p64, Vec4<double> *pc64,
+                                 Vec4<T> *p_t, Vec4<T> *pc_t, Vec4<T> *R) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= V) return;
+    const int v = oldidx[k];
+    const Vec4<double> pr = {rest[3 * (int64_t)v], rest[3 * (int64_t)v + 1], rest[3 * (int64_t)v + 2], 0.0};
+    Vec4<double> pc = pr;
+    if (k >= m) {  // constrained vertex: snapped to its target (arap.h:277-281)
+        const double *t = targets + 3 * (int64_t)(k - m);
+        pc = {t[0], t[1], t[2], 0.0};
+    }
+    p64[k] = pr;
+    pc64[k] = pc;
+    p_t[k] = {(T)pr.x, (T)pr.y, (T)pr.z, (T)0};
+    pc_t[k] = {(T)pc.x, (T)pc.y, (T)pc.z, (T)0};
+    R[3 * (int64_t)k + 0] = {(T)1, (T)0, (T)0, (T)0};
+    R[3 * (int64_t)k + 1] = {(T)0, (T)1, (T)0, (T)0};
+    R[3 * (int64_t)k + 2] = {(T)0, (T)0, (T)1, (T)0};
+}
+
+// setupLinearSystem, arap.h:310-336: L_kk = sum_j w_kj, L_lk = -w_kl for free
+// l > k (written into the supernodal panel of column k), bFixed_k = sum over
+// constrained neighbours of w_kj * c_j, all summed in adjacency order.
+template <typename TF, typename T>
+__global__ void k_assemble(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
+                           const double *__restrict__ w64, const int64_t *__restrict__ amap,
+                           const int64_t *__restrict__ dmap, const Vec4<double> *__restrict__ pc64,
+                           TF *__restrict__ Lval, double *__restrict__ diag64, Vec4<T> *__restrict__ bfixed) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    double diag = 0.0, bx = 0.0, by = 0.0, bz = 0.0;
+    for (int e = drow[k]; e < drow[k + 1]; ++e) {
+        const int l = dcol[e];
+        if (l == k) continue;
+        const double w = w64[e];
+        diag = __dadd_rn(diag, w);
+        if (l >= m) {
+            const Vec4<double> c = pc64[l];
+            bx = __dadd_rn(bx, __dmul_rn(w, c.x));
+            by = __dadd_rn(by, __dmul_rn(w, c.y));
+            bz = __dadd_rn(bz, __dmul_rn(w, c.z));
+        } else if (l > k) {
+            Lval[amap[e]] = (TF)(-w);
+        }
+    }
+    Lval[dmap[k]] = (TF)diag;
+    diag64[k] = diag;
+    bfixed[k] = {(T)bx, (T)by, (T)bz, (T)0};
+}
+
+// ---------------------------------------------------------------------------
+// multifrontal Cholesky, one CTA per supernode of a level
+
+constexpr int kFactorThreads = 256;
+constexpr int kTile = 64;
+
+template <typename TF>
+__global__ void __launch_bounds__(kFactorThreads)
+k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
+               const int32_t *__restrict__ relind, TF *__restrict__ Lval, TF *__restrict__ Upd,
+               TF *__restrict__ Dinv, int *err) {
+    __shared__ TF As[NB][kTile];
+    __shared__ TF Bs[NB][kTile];
+    __shared__ TF s_inv;
+    const int tid = threadIdx.x;
+    const SnInfo d = sn[level_sn[blockIdx.x]];
+    const int n = d.nrow, nc = d.ncol, nb = n - nc;
+    TF *P = Lval + d.panel_off;
+    TF *U = Upd + d.upd_off;
+
+    // extend-add of the children's update matrices (pull; children in order)
+    for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+        const SnInfo c = sn[child[ci]];
+        const int nbc = c.nrow - c.ncol;
+        const TF *Uc = Upd + c.upd_off;
+        const int32_t *ri = relind + c.relind_off;
+        const int64_t total = (int64_t)nbc * nbc;
+        for (int64_t t = tid; t < total; t += kFactorThreads) {
+            const int k = (int)(t / nbc), i = (int)(t - (int64_t)k * nbc);
+            if (i < k) continue;
+            const int pi = ri[i], pk = ri[k];
+            const TF v = Uc[t];
+            if (pk < nc) P[(int64_t)pk * n + pi] += v;
+            else U[(int64_t)(pk - nc) * nb + (pi - nc)] += v;
+        }
+        __syncthreads();
+    }
+
+    // blocked right-looking partial Cholesky of the front [P | U]
+    for (int j0 = 0; j0 < nc; j0 += NB) {
+        const int w = min(NB, nc - j0);
+        // (a) panel columns j0..j0+w-1, rows j0..n-1
+        for (int jj = 0; jj < w; ++jj) {
+            const int j = j0 + jj;
+            TF *Pj = P + (int64_t)j * n;
+            if (tid == 0) {
+                TF dj = Pj[j];
+                if (!(dj > (TF)0)) { atomicOr(err, kErrNotSpd); dj = (TF)1; }
+                dj = tsqrt(dj);
+                Pj[j] = dj;
+                s_inv = (TF)1 / dj;
+            }
+            __syncthreads();
+            const TF inv = s_inv;
+            for (int i = j + 1 + tid; i < n; i += kFactorThreads) Pj[i] *= inv;
+            __syncthreads();
+            const int ncols = j0 + w - j - 1, nr = n - j - 1;
+            for (int t = tid; t < ncols * nr; t += kFactorThreads) {
+                const int kk = t / nr, i = j + 1 + (t - kk * nr);
+                const int k = j + 1 + kk;
+                if (i >= k) P[(int64_t)k * n + i] -= Pj[i] * Pj[k];
+            }
+            __syncthreads();
+        }
+        // (b) inverse of the w x w diagonal block (column c by thread c)
+        if (tid < NB) {
+            const int c = tid;
+            TF x[NB];
+#pragma unroll
+            for (int i = 0; i < NB; ++i) {
+                TF v = (TF)0;
+                if (i >= c && i < w) {
+                    TF s = (i == c) ? (TF)1 : (TF)0;
+#pragma unroll
+                    for (int t = 0; t < NB; ++t)
+                        if (t >= c && t < i) s -= P[(int64_t)(j0 + t) * n + j0 + i] * x[t];
+                    v = s / P[(int64_t)(j0 + i) * n + j0 + i];
+                }
+                x[i] = v;
+            }
+            TF *D = Dinv + d.dinv_off + (int64_t)(j0 / NB) * NB * NB + (int64_t)c * NB;
+#pragma unroll
+            for (int i = 0; i < NB; ++i) D[i] = x[i];
+        }
+        // (c) trailing update F[i][k] -= sum_t L[i][j0+t] L[k][j0+t], k,i >= j0+w
+        const int c0 = j0 + w;
+        const int rem = n - c0;
+        if (rem > 0) {
+            const int ntl = (rem + kTile - 1) / kTile;
+            const int tx = tid % 16, ty = tid / 16;
+            for (int ti = 0; ti < ntl; ++ti) {
+                for (int tk = 0; tk <= ti; ++tk) {
+                    const int rb = c0 + ti * kTile, cb = c0 + tk * kTile;
+                    for (int q = tid; q < NB * kTile; q += kFactorThreads) {
+                        const int t = q / kTile, r = q % kTile;
+                        TF a = (TF)0, b = (TF)0;
+                        if (t < w) {
+                            const TF *col = P + (int64_t)(j0 + t) * n;
+                            if (rb + r < n) a = col[rb + r];
+                            if (cb + r < n) b = col[cb + r];
+                        }
+                        As[t][r] = a;
+                        Bs[t][r] = b;
+                    }
+                    __syncthreads();
+                    TF acc[4][4];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) acc[a][b] = (TF)0;
+                    for (int t = 0; t < w; ++t) {
+                        TF av[4], bv[4];
+#pragma unroll
+                        for (int a = 0; a < 4; ++a) av[a] = As[t][ty + 16 * a];
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) bv[b] = Bs[t][tx + 16 * b];
+#pragma unroll
+                        for (int a = 0; a < 4; ++a)
+#pragma unroll
+                            for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+                    }
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const int row = rb + ty + 16 * a;
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            const int colf = cb + tx + 16 * b;
+                            if (row < n && colf < n && row >= colf) {
+                                if (colf < nc) P[(int64_t)colf * n + row] -= acc[a][b];
+                                else U[(int64_t)(colf - nc) * nb + (row - nc)] -= acc[a][b];
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// local step: estimateRotations, arap.h:354-384
+
+// Classical cyclic Jacobi on a symmetric 3x3 (Golub & Van Loan, Alg. 8.5.3):
+// a -> diag(lambda), v = eigenvectors (columns).
+template <typename T>
+__device__ __forceinline__ void jacobi_eig3(T a[3][3], T v[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? (T)1 : (T)0;
+    const int sweeps = sizeof(T) == 4 ? 6 : 10;
+    for (int sw = 0; sw < sweeps; ++sw) {
+        const T off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+        const T dia = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+        if (off <= Eps<T>::v * Eps<T>::v * dia) break;
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0;
+            const int q = pq == 0 ? 1 : 2;
+            const int r = 3 - p - q;
+            const T apq = a[p][q];
+            if (apq == (T)0) continue;
+            const T theta = (a[q][q] - a[p][p]) / ((T)2 * apq);
+            T t = (T)1 / (fabs(theta) + tsqrt(theta * theta + (T)1));
+            if (theta < (T)0) t = -t;
+            const T c = (T)1 / tsqrt(t * t + (T)1);
+            const T s = t * c;
+            const T tau = s / ((T)1 + c);
+            a[p][p] -= t * apq;
+            a[q][q] += t * apq;
+            a[p][q] = a[q][p] = (T)0;
+            const T arp = a[r][p], arq = a[r][q];
+            a[r][p] = a[p][r] = arp - s * (arq + tau * arp);
+            a[r][q] = a[q][r] = arq + s * (arp - tau * arq);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const T vip = v[i][p], viq = v[i][q];
+                v[i][p] = vip - s * (viq + tau * vip);
+                v[i][q] = viq + s * (vip - tau * viq);
+            }
+        }
+    }
+}
+
+// Best rotation R = V diag(1,1,det(V U^T)) U^T for cov = U S V^T (arap.h:376-382),
+// from the eigenvectors V of cov^T cov (proper, v3 = v1 x v2) and the proper
+// left factor u1 = cov v1/|.|, u2 = Gram-Schmidt(cov v2), u3 = u1 x u2.
+template <typename T>
+__device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3]) {
+    T f2 = (T)0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) f2 += S_in[i][j] * S_in[i][j];
+    if (!(f2 > (T)0)) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) R[i][j] = (i == j) ? (T)1 : (T)0;
+        return;
+    }
+    const T sc = (T)1 / tsqrt(f2);
+    T S[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) S[i][j] = S_in[i][j] * sc;
+    T C[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) C[i][j] = S[0][i] * S[0][j] + S[1][i] * S[1][j] + S[2][i] * S[2][j];
+    T Vm[3][3];
+    jacobi_eig3(C, Vm);
+    // order eigenpairs descending
+    T lam[3] = {C[0][0], C[1][1], C[2][2]};
+    int o0 = 0, o1 = 1, o2 = 2;
+    if (lam[o1] > lam[o0]) { int t = o0; o0 = o1; o1 = t; }
+    if (lam[o2] > lam[o0]) { int t = o0; o0 = o2; o2 = t; }
+    if (lam[o2] > lam[o1]) { int t = o1; o1 = o2; o2 = t; }
+    T v1[3], v2[3], v3[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { v1[i] = Vm[i][o0]; v2[i] = Vm[i][o1]; }
+    v3[0] = v1[1] * v2[2] - v1[2] * v2[1];
+    v3[1] = v1[2] * v2[0] - v1[0] * v2[2];
+    v3[2] = v1[0] * v2[1] - v1[1] * v2[0];
+    T u1[3], u2[3], u3[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        u1[i] = S[i][0] * v1[0] + S[i][1] * v1[1] + S[i][2] * v1[2];
+        u2[i] = S[i][0] * v2[0] + S[i][1] * v2[1] + S[i][2] * v2[2];
+    }
+    const T n1 = tsqrt(u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) u1[i] /= n1;
+    const T dp = u1[0] * u2[0] + u1[1] * u2[1] + u1[2] * u2[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) u2[i] -= dp * u1[i];
+    T n2 = tsqrt(u2[0] * u2[0] + u2[1] * u2[1] + u2[2] * u2[2]);
+    if (!(n2 > (T)64 * Eps<T>::v * n1)) {
+        // rank one: any unit vector orthogonal to u1
+        int mi = 0;
+        if (fabs(u1[1]) < fabs(u1[mi])) mi = 1;
+        if (fabs(u1[2]) < fabs(u1[mi])) mi = 2;
+        T e[3] = {(T)0, (T)0, (T)0};
+        e[mi] = (T)1;
+        const T d2 = u1[mi];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) u2[i] = e[i] - d2 * u1[i];
+        n2 = tsqrt(u2[0] * u2[0] + u2[1] * u2[1] + u2[2] * u2[2]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) u2[i] /= n2;
+    u3[0] = u1[1] * u2[2] - u1[2] * u2[1];
+    u3[1] = u1[2] * u2[0] - u1[0] * u2[2];
+    u3[2] = u1[0] * u2[1] - u1[1] * u2[0];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) R[i][j] = v1[i] * u1[j] + v2[i] * u2[j] + v3[i] * u3[j];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_local_step(int V, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const T *__restrict__ w,
+             const Vec4<T> *__restrict__ p, const Vec4<T> *__restrict__ pc, Vec4<T> *__restrict__ R) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const Vec4<T> pi = p[i], ci = pc[i];
+    T S[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) S[a][b] = (T)0;
+    const int e1 = drow[i + 1];
+    for (int e = drow[i]; e < e1; ++e) {
+        const int j = dcol[e];
+        const T wj = w[e];
+        const Vec4<T> pj = p[j], cj = pc[j];
+        const T ex = wj * (pi.x - pj.x), ey = wj * (pi.y - pj.y), ez = wj * (pi.z - pj.z);
+        const T fx = ci.x - cj.x, fy = ci.y - cj.y, fz = ci.z - cj.z;
+        S[0][0] += ex * fx; S[0][1] += ex * fy; S[0][2] += ex * fz;
+        S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
+        S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
+    }
+    T Rm[3][3];
+    rotation_from_cov(S, Rm);
+    R[3 * (int64_t)i + 0] = {Rm[0][0], Rm[0][1], Rm[0][2], (T)0};
+    R[3 * (int64_t)i + 1] = {Rm[1][0], Rm[1][1], Rm[1][2], (T)0};
+    R[3 * (int64_t)i + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], (T)0};
+}
+
+// estimatePositions RHS, arap.h:395-414
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_rhs(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const T *__restrict__ w,
+      const Vec4<T> *__restrict__ p, const Vec4<T> *__restrict__ R, const Vec4<T> *__restrict__ bfixed,
+      Vec4<T> *__restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const Vec4<T> pi = p[i];
+    const Vec4<T> r0 = R[3 * (int64_t)i], r1 = R[3 * (int64_t)i + 1], r2 = R[3 * (int64_t)i + 2];
+    Vec4<T> acc = bfixed[i];
+    const int e1 = drow[i + 1];
+    for (int e = drow[i]; e < e1; ++e) {
+        const int j = dcol[e];
+        if (j == i) continue;
+        const T h = w[e] * (T)0.5;
+        const Vec4<T> pj = p[j];
+        const Vec4<T> q0 = R[3 * (int64_t)j], q1 = R[3 * (int64_t)j + 1], q2 = R[3 * (int64_t)j + 2];
+        const T dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        acc.x += ((r0.x + q0.x) * dx + (r0.y + q0.y) * dy + (r0.z + q0.z) * dz) * h;
+        acc.y += ((r1.x + q1.x) * dx + (r1.y + q1.y) * dy + (r1.z + q1.z) * dz) * h;
+        acc.z += ((r2.x + q2.x) * dx + (r2.y + q2.y) * dy + (r2.z + q2.z) * dz) * h;
+    }
+    b[i] = acc;
+}
+
+// r = b - A x in FP64 over the free vertices (A = constrained Laplacian)
+__global__ void __launch_bounds__(256)
+k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const double *__restrict__ w64,
+           const double *__restrict__ diag64, const Vec4<float> *__restrict__ b, const Vec4<double> *__restrict__ x,
+           Vec4<float> *__restrict__ r) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const Vec4<double> xi = x[i];
+    const double d = diag64[i];
+    double ax = d * xi.x, ay = d * xi.y, az = d * xi.z;
+    const int e1 = drow[i + 1];
+    for (int e = drow[i]; e < e1; ++e) {
+        const int j = dcol[e];
+        if (j == i || j >= m) continue;
+        const double wj = w64[e];
+        const Vec4<double> xj = x[j];
+        ax -= wj * xj.x;
+        ay -= wj * xj.y;
+        az -= wj * xj.z;
+    }
+    const Vec4<float> bi = b[i];
+    r[i] = {(float)((double)bi.x - ax), (float)((double)bi.y - ay), (float)((double)bi.z - az), 0.f};
+}
+
+// ---------------------------------------------------------------------------
+// supernodal triangular solves
+
+constexpr int kSolveThreads = 256;
+
+// Forward: for supernode s (children first), front f = [b(cols); 0] plus the
+// children's update vectors; y = L11^{-1} f(cols) block by block with the
+// inverted diagonal blocks; u_s = f(struct) - L21 y goes to the parent.
+template <typename T>
+__global__ void __launch_bounds__(kSolveThreads)
+k_solve_fwd(int S, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
+            const int32_t *__restrict__ relind, const T *__restrict__ Lval, const T *__restrict__ Dinv,
+            Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec, unsigned long long *ticket, unsigned *flags,
+            int *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Vec4<T> *f = reinterpret_cast<Vec4<T> *>(smem_raw);
+    __shared__ int s_task;
+    __shared__ unsigned s_epoch;
+    __shared__ Vec4<T> yblk[NB];
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        const unsigned long long t = atomicAdd(ticket, 1ull);
+        s_task = (int)(t % (unsigned long long)S);
+        s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
+    }
+    __syncthreads();
+    const int s = s_task;
+    const unsigned epoch = s_epoch;
+    const SnInfo d = sn[s];
+    const int n = d.nrow, nc = d.ncol;
+    if (tid == 0)
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
+    __syncthreads();
+    for (int i = tid; i < n; i += kSolveThreads) {
+        if (i < nc) f[i] = sol[d.first + i];
+        else f[i] = {(T)0, (T)0, (T)0, (T)0};
+    }
+    __syncthreads();
+    for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+        const SnInfo c = sn[child[ci]];
+        const int nbc = c.nrow - c.ncol;
+        const int32_t *ri = relind + c.relind_off;
+        for (int i = tid; i < nbc; i += kSolveThreads) {
+            const Vec4<T> u = ldcg4(uvec + c.uvec_off + i);
+            Vec4<T> &t = f[ri[i]];
+            t.x += u.x;
+            t.y += u.y;
+            t.z += u.z;
+        }
+        __syncthreads();
+    }
+    const T *P = Lval + d.panel_off;
+    for (int b0 = 0; b0 < nc; b0 += NB) {
+        const int w = min(NB, nc - b0);
+        if (tid < w) {
+            const T *D = Dinv + d.dinv_off + (int64_t)(b0 / NB) * NB * NB;
+            T yx = 0, yy = 0, yz = 0;
+            for (int c = 0; c <= tid; ++c) {
+                const T dv = D[c * NB + tid];
+                const Vec4<T> fc = f[b0 + c];
+                yx += dv * fc.x;
+                yy += dv * fc.y;
+                yz += dv * fc.z;
+            }
+            yblk[tid] = {yx, yy, yz, (T)0};
+        }
+        __syncthreads();
+        if (tid < w) f[b0 + tid] = yblk[tid];
+        for (int i = b0 + w + tid; i < n; i += kSolveThreads) {
+            T ax = 0, ay = 0, az = 0;
+            for (int c = 0; c < w; ++c) {
+                const T l = P[(int64_t)(b0 + c) * n + i];
+                const Vec4<T> y = yblk[c];
+                ax += l * y.x;
+                ay += l * y.y;
+                az += l * y.z;
+            }
+            Vec4<T> &t = f[i];
+            t.x -= ax;
+            t.y -= ay;
+            t.z -= az;
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < n; i += kSolveThreads) {
+        if (i < nc) sol[d.first + i] = f[i];
+        else uvec[d.uvec_off + (i - nc)] = f[i];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(flags + s, epoch);
+}
+
+// Backward: for supernode s (root first), g = [y(cols); x(struct)]; block by
+// block from the last, z = g_b - L(rows below, b)^T g(rows below), x_b = Dinv_b^T z.
+template <typename T>
+__global__ void __launch_bounds__(kSolveThreads)
+k_solve_bwd(int S, const SnInfo *__restrict__ sn, const int32_t *__restrict__ rows, const T *__restrict__ Lval,
+            const T *__restrict__ Dinv, Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64,
+            Vec4<float> *__restrict__ pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Vec4<T> *g = reinterpret_cast<Vec4<T> *>(smem_raw);
+    __shared__ int s_task;
+    __shared__ unsigned s_epoch;
+    __shared__ Vec4<T> zblk[NB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int nwarps = kSolveThreads / 32;
+    if (tid == 0) {
+        const unsigned long long t = atomicAdd(ticket, 1ull);
+        s_task = S - 1 - (int)(t % (unsigned long long)S);
+        s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
+    }
+    __syncthreads();
+    const int s = s_task;
+    const unsigned epoch = s_epoch;
+    const SnInfo d = sn[s];
+    const int n = d.nrow, nc = d.ncol;
+    if (tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
+    __syncthreads();
+    const int32_t *rs = rows + d.rows_off;
+    for (int i = tid; i < n; i += kSolveThreads) {
+        if (i < nc) g[i] = sol[d.first + i];
+        else g[i] = ldcg4(sol + rs[i - nc]);
+    }
+    __syncthreads();
+    const T *P = Lval + d.panel_off;
+    const int nblk = (nc + NB - 1) / NB;
+    for (int bi = nblk - 1; bi >= 0; --bi) {
+        const int b0 = bi * NB;
+        const int w = min(NB, nc - b0);
+        for (int r = warp; r < w; r += nwarps) {
+            const T *col = P + (int64_t)(b0 + r) * n;
+            T ax = 0, ay = 0, az = 0;
+            for (int i = b0 + w + lane; i < n; i += 32) {
+                const T l = col[i];
+                const Vec4<T> x = g[i];
+                ax += l * x.x;
+                ay += l * x.y;
+                az += l * x.z;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                ax += __shfl_xor_sync(0xffffffffu, ax, o);
+                ay += __shfl_xor_sync(0xffffffffu, ay, o);
+                az += __shfl_xor_sync(0xffffffffu, az, o);
+            }
+            if (lane == 0) {
+                const Vec4<T> gv = g[b0 + r];
+                zblk[r] = {gv.x - ax, gv.y - ay, gv.z - az, (T)0};
+            }
+        }
+        __syncthreads();
+        Vec4<T> xr = {(T)0, (T)0, (T)0, (T)0};
+        if (tid < w) {
+            const T *D = Dinv + d.dinv_off + (int64_t)bi * NB * NB + (int64_t)tid * NB;
+            for (int c = tid; c < w; ++c) {
+                const T dv = D[c];
+                const Vec4<T> z = zblk[c];
+                xr.x += dv * z.x;
+                xr.y += dv * z.y;
+                xr.z += dv * z.z;
+            }
+        }
+        __syncthreads();
+        if (tid < w) g[b0 + tid] = xr;
+        __syncthreads();
+    }
+    for (int i = tid; i < nc; i += kSolveThreads) {
+        const Vec4<T> x = g[i];
+        const int k = d.first + i;
+        sol[k] = x;
+        if (mode == 0) {
+            pc64[k] = {(double)x.x, (double)x.y, (double)x.z, 0.0};
+        } else {
+            Vec4<double> v = pc64[k];
+            v.x += (double)x.x;
+            v.y += (double)x.y;
+            v.z += (double)x.z;
+            pc64[k] = v;
+            pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(flags + s, epoch);
+}
+
+// ---------------------------------------------------------------------------
+
+__global__ void k_gather_positions(int V, const int32_t *__restrict__ oldidx, const Vec4<double> *__restrict__ pc64,
+                                   double *__restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= V) return;
+    const int v = oldidx[k];
+    const Vec4<double> x = pc64[k];
+    out[3 * (int64_t)v] = x.x;
+    out[3 * (int64_t)v + 1] = x.y;
+    out[3 * (int64_t)v + 2] = x.z;
+}
+
+template <typename T>
+__global__ void k_gather_rotations(int V, const int32_t *__restrict__ oldidx, const Vec4<T> *__restrict__ R,
+                                   double *__restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= V) return;
+    const int v = oldidx[k];
+    for (int r = 0; r < 3; ++r) {
+        const Vec4<T> q = R[3 * (int64_t)k + r];
+        out[9 * (int64_t)v + 3 * r + 0] = (double)q.x;
+        out[9 * (int64_t)v + 3 * r + 1] = (double)q.y;
+        out[9 * (int64_t)v + 3 * r + 2] = (double)q.z;
+    }
+}
+
+inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+
+void launch_face_cots(const DevTopo &t, const double *rest_xyz, double *hc, cudaStream_t st) {
+    if (t.F == 0) return;
+    k_face_cots<<<blocks_for(t.F, 256), 256, 0, st>>>(t.F, t.faces, rest_xyz, hc);
+}
+
+void launch_edge_weights(const DevTopo &t, const DevSym &s, const double *hc, double *w64, float *w32,
+                         double *w_orig, cudaStream_t st) {
+    if (s.nnz == 0) return;
+    k_edge_weights<<<blocks_for(s.nnz, 256), 256, 0, st>>>(s.nnz, s.dent, t.ent_ptr, t.ent_fc, hc, w64, w32, w_orig);
+}
+
+void launch_edge_weights_orig(const DevTopo &t, const double *hc, double *w_orig, cudaStream_t st) {
+    if (t.nnz == 0) return;
+    k_edge_weights_orig<<<blocks_for(t.nnz, 256), 256, 0, st>>>(t.nnz, t.ent_ptr, t.ent_fc, hc, w_orig);
+}
+
+template <typename T>
+void launch_setup_vertices(const DevSym &s, const double *rest_xyz, const double *targets_xyz,
+                           Vec4<double> *p64, Vec4<double> *pc64, Vec4<T> *p_t, Vec4<T> *pc_t, Vec4<T> *R,
+                           cudaStream_t st) {
+    if (s.V == 0) return;
+    k_setup_vertices<T><<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.m, s.oldidx, rest_xyz, targets_xyz, p64, pc64,
+                                                              p_t, pc_t, R);
+}
+
+template <typename TF, typename T>
+void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc64, TF *Lval, double *diag64,
+                     Vec4<T> *bfixed, cudaStream_t st) {
+    if (s.m == 0) return;
+    k_assemble<TF, T><<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, s.amap, s.dmap, pc64, Lval,
+                                                            diag64, bfixed);
+}
+
+template <typename TF>
+void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv,
+                         int *err, cudaStream_t st) {
+    if (level_count == 0) return;
+    k_factor_level<TF><<<level_count, kFactorThreads, 0, st>>>(s.level_sn + level_begin, s.sn, s.child, s.relind,
+                                                               Lval, Upd, Dinv, err);
+}
+
+template <typename T>
+void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *pc, Vec4<T> *R,
+                       cudaStream_t st) {
+    if (s.V == 0) return;
+    k_local_step<T><<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.drow, s.dcol, w, p, pc, R);
+}
+
+template <typename T>
+void launch_rhs(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *R, const Vec4<T> *bfixed,
+                Vec4<T> *b, cudaStream_t st) {
+    if (s.m == 0) return;
+    k_rhs<T><<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w, p, R, bfixed, b);
+}
+
+void launch_residual(const DevSym &s, const double *w64, const double *diag64, const Vec4<float> *b,
+                     const Vec4<double> *x64, Vec4<float> *r, cudaStream_t st) {
+    if (s.m == 0) return;
+    k_residual<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, b, x64, r);
+}
+
+template <typename T>
+void launch_solve_fwd(const DevSym &s, const T *Lval, const T *Dinv, Vec4<T> *sol, Vec4<T> *uvec,
+                      unsigned long long *ticket, unsigned *flags, int *err, int smem_rows, cudaStream_t st) {
+    if (s.S == 0) return;
+    const size_t smem = (size_t)smem_rows * sizeof(Vec4<T>);
+    k_solve_fwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, s.sn, s.child, s.relind, Lval, Dinv, sol, uvec, ticket,
+                                                     flags, err);
+}
+
+template <typename T>
+void launch_solve_bwd(const DevSym &s, const T *Lval, const T *Dinv, Vec4<T> *sol, Vec4<double> *pc64,
+                      Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
+                      int smem_rows, cudaStream_t st) {
+    if (s.S == 0) return;
+    const size_t smem = (size_t)smem_rows * sizeof(Vec4<T>);
+    k_solve_bwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, s.sn, s.rows, Lval, Dinv, sol, pc64, pc32, mode, ticket,
+                                                     flags, err);
+}
+
+void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st) {
+    if (s.V == 0) return;
+    k_gather_positions<<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.oldidx, pc64, out_xyz);
+}
+
+template <typename T>
+void launch_gather_rotations(const DevSym &s, const Vec4<T> *R, double *out9, cudaStream_t st) {
+    if (s.V == 0) return;
+    k_gather_rotations<T><<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.oldidx, R, out9);
+}
+
+// Raises the dynamic shared-memory limit of the solve kernels.
+cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64) {
+    cudaError_t e = cudaFuncSetAttribute(k_solve_fwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f32);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_solve_bwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f32);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_solve_fwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f64);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_solve_bwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f64);
+}
+
+// explicit instantiations
+template void launch_setup_vertices<float>(const DevSym &, const double *, const double *, Vec4<double> *,
+                                           Vec4<double> *, Vec4<float> *, Vec4<float> *, Vec4<float> *,
+                                           cudaStream_t);
+template void launch_setup_vertices<double>(const DevSym &, const double *, const double *, Vec4<double> *,
+                                            Vec4<double> *, Vec4<double> *, Vec4<double> *, Vec4<double> *,
+                                            cudaStream_t);
+template void launch_assemble<float, float>(const DevSym &, const double *, const Vec4<double> *, float *, double *,
+                                            Vec4<float> *, cudaStream_t);
+template void launch_assemble<double, double>(const DevSym &, const double *, const Vec4<double> *, double *,
+                                              double *, Vec4<double> *, cudaStream_t);
+template void launch_factor_level<float>(const DevSym &, int, int, float *, float *, float *, int *, cudaStream_t);
+template void launch_factor_level<double>(const DevSym &, int, int, double *, double *, double *, int *,
+                                          cudaStream_t);
+template void launch_local_step<float>(const DevSym &, const float *, const Vec4<float> *, const Vec4<float> *,
+                                       Vec4<float> *, cudaStream_t);
+template void launch_local_step<double>(const DevSym &, const double *, const Vec4<double> *, const Vec4<double> *,
+                                        Vec4<double> *, cudaStream_t);
+template void launch_rhs<float>(const DevSym &, const float *, const Vec4<float> *, const Vec4<float> *,
+                                const Vec4<float> *, Vec4<float> *, cudaStream_t);
+template void launch_rhs<double>(const DevSym &, const double *, const Vec4<double> *, const Vec4<double> *,
+                                 const Vec4<double> *, Vec4<double> *, cudaStream_t);
+template void launch_solve_fwd<float>(const DevSym &, const float *, const float *, Vec4<float> *, Vec4<float> *,
+                                      unsigned long long *, unsigned *, int *, int, cudaStream_t);
+template void launch_solve_fwd<double>(const DevSym &, const double *, const double *, Vec4<double> *,
+                                       Vec4<double> *, unsigned long long *, unsigned *, int *, int, cudaStream_t);
+template void launch_solve_bwd<float>(const DevSym &, const float *, const float *, Vec4<float> *, Vec4<double> *,
+                                      Vec4<float> *, int, unsigned long long *, unsigned *, int *, int,
+                                      cudaStream_t);
+template void launch_solve_bwd<double>(const DevSym &, const double *, const double *, Vec4<double> *,
+                                       Vec4<double> *, Vec4<float> *, int, unsigned long long *, unsigned *, int *,
+                                       int, cudaStream_t);
+template void launch_gather_rotations<float>(const DevSym &, const Vec4<float> *, double *, cudaStream_t);
+template void launch_gather_rotations<double>(const DevSym &, const Vec4<double> *, double *, cudaStream_t);
+
+}  // namespace arapgpu

@@ -1,0 +1,92 @@
+// arap_kernels.h -- launch interface of the sm_103a ARAP kernels.
+//
+// Device data layout (all arrays in device order: free vertices in
+// nested-dissection elimination order [0, m), constrained vertices [m, V) in
+// ascending vertex order):
+//   positions   V x {x,y,z,0} in Vec4<T> (16 B for float, 32 B for double)
+//   rotations   V x 3 rows of Vec4<T> (row-major R, 4th lane unused)
+//   adjacency   CSR drow/dcol with weights w (per device entry)
+//   factor      per supernode an nrow x ncol column-major panel (L11 lower
+//               triangle, then L21) and the inverses of its 32x32 diagonal blocks
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "arap_symbolic.h"
+
+namespace arapgpu {
+
+template <typename T> struct __align__(4 * sizeof(T)) Vec4 { T x, y, z, w; };
+
+// error bits written by kernels into the context's device status word
+constexpr int kErrNotSpd = 1;
+constexpr int kErrTimeout = 2;
+
+// Bound on the polls of one in-kernel wait (each poll sleeps ~100 ns).
+constexpr unsigned kSpinLimit = 1u << 24;
+
+struct DevTopo {
+    int V, F, nnz;
+    const int32_t *faces;    // 3F (original vertex ids)
+    const int32_t *ent_ptr;  // nnz+1 (original CSR entries)
+    const int32_t *ent_fc;   // face*3+k
+};
+
+struct DevSym {
+    int V, m, S, nnz;
+    const int32_t *drow, *dcol, *dent, *oldidx;
+    const int64_t *amap, *dmap;
+    const SnInfo *sn;
+    const int32_t *rows, *relind, *child, *level_sn;
+};
+
+// cotangent halves per face (computeCotanWeights arap.h:189-222), FP64
+void launch_face_cots(const DevTopo &t, const double *rest_xyz, double *hc, cudaStream_t st);
+// edge weights per device entry (w64/w32) and per original entry (w_orig); any
+// output may be null. arap.h:224-238
+void launch_edge_weights(const DevTopo &t, const DevSym &s, const double *hc, double *w64, float *w32,
+                         double *w_orig, cudaStream_t st);
+// weights per original entry only (no symbolic analysis yet)
+void launch_edge_weights_orig(const DevTopo &t, const double *hc, double *w_orig, cudaStream_t st);
+// rest / current positions in device order (initializeMeshGeometry arap.h:162-168,
+// initializeConstraints arap.h:277-281), rotations reset (arap.h:246-249)
+template <typename T>
+void launch_setup_vertices(const DevSym &s, const double *rest_xyz, const double *targets_xyz,
+                           Vec4<double> *p64, Vec4<double> *pc64, Vec4<T> *p_t, Vec4<T> *pc_t, Vec4<T> *R,
+                           cudaStream_t st);
+// constrained Laplacian into the supernodal panels + bFixed (arap.h:292-336)
+template <typename TF, typename T>
+void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc64, TF *Lval, double *diag64,
+                     Vec4<T> *bfixed, cudaStream_t st);
+// multifrontal Cholesky of one level of the supernodal tree
+template <typename TF>
+void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv,
+                         int *err, cudaStream_t st);
+// local step: covariance + rotation fit (estimateRotations arap.h:354-384)
+template <typename T>
+void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *pc, Vec4<T> *R,
+                       cudaStream_t st);
+// RHS (estimatePositions arap.h:395-414): b = bFixed + sum 1/2 w (Ri+Rj)(pi-pj)
+template <typename T>
+void launch_rhs(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *R, const Vec4<T> *bfixed,
+                Vec4<T> *b, cudaStream_t st);
+// FP64 residual of the global system: r = b - A x over the free vertices
+void launch_residual(const DevSym &s, const double *w64, const double *diag64, const Vec4<float> *b,
+                     const Vec4<double> *x64, Vec4<float> *r, cudaStream_t st);
+// supernodal triangular solves L y = b (forward) and L^T x = y (backward),
+// one launch each, supernodes scheduled by a ticket counter with bounded waits.
+// mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k and pc32[k] = float(pc64[k]).
+template <typename T>
+void launch_solve_fwd(const DevSym &s, const T *Lval, const T *Dinv, Vec4<T> *sol, Vec4<T> *uvec,
+                      unsigned long long *ticket, unsigned *flags, int *err, int smem_rows, cudaStream_t st);
+template <typename T>
+void launch_solve_bwd(const DevSym &s, const T *Lval, const T *Dinv, Vec4<T> *sol, Vec4<double> *pc64,
+                      Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
+                      int smem_rows, cudaStream_t st);
+// deformed positions back to the original vertex order as doubles (arap.h:133-135)
+void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st);
+template <typename T>
+void launch_gather_rotations(const DevSym &s, const Vec4<T> *R, double *out9, cudaStream_t st);
+
+}  // namespace arapgpu

@@ -1,0 +1,453 @@
+// arap_symbolic.cpp -- host-side symbolic analysis for the GPU ARAP solver.
+//
+// Covers the integer part of inc/deform/arap.h:
+//   - the sparsity of _edgeWeights built by computeCotanWeights (arap.h:182-239,
+//     undirectedEdge arap.h:435-440), which doubles as the one-ring adjacency;
+//   - the free-variable map (initializeFreeVariableMapping, arap.h:261-272);
+//   - the pattern of the constrained Laplacian L (setupLinearSystem, arap.h:292-336)
+//     and the symbolic part of its factorisation (SimplicialLDLT::compute,
+//     arap.h:337), here a nested-dissection ordering, the elimination tree and a
+//     supernodal partition for a multifrontal Cholesky on the GPU.
+//
+// Nested dissection (George 1973) with level-structure separators: a set of at
+// most kNdLeaf vertices is one leaf block; a disconnected set is ordered one
+// component at a time (components in order of their smallest vertex); a
+// connected set is split by the BFS level of a pseudo-peripheral vertex
+// (George & Liu) whose two sides both hold >= 4/10 of the set, smallest level
+// first, then most balanced, then lowest level; level vertices with no
+// neighbour in the next level move to the near side. Order: near side, far
+// side, separator. Every emitted leaf or separator is one supernode.
+#include "arap_symbolic.h"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+namespace arapgpu {
+
+bool build_topology(int V, int F, const int32_t *faces, Topology &topo, std::string &err) {
+    topo = Topology();
+    topo.V = V;
+    topo.F = F;
+    topo.faces.assign(faces, faces + (size_t)3 * F);
+    for (int64_t i = 0; i < (int64_t)3 * F; ++i) {
+        if (faces[i] < 0 || faces[i] >= V) {
+            err = "face index " + std::to_string(faces[i]) + " outside [0, " + std::to_string(V) + ")";
+            return false;
+        }
+    }
+    // Directed contributions in the order computeCotanWeights pushes them
+    // (arap.h:225-232): per face e0,e1,e2 as (min,max), then as (max,min).
+    struct Contrib { int32_t r, c, fc; };
+    std::vector<Contrib> t;
+    t.reserve((size_t)6 * F);
+    for (int f = 0; f < F; ++f) {
+        const int32_t v[3] = {faces[3 * f], faces[3 * f + 1], faces[3 * f + 2]};
+        int32_t a[3], b[3];
+        for (int k = 0; k < 3; ++k) {
+            int32_t x = v[k], y = v[(k + 1) % 3];
+            a[k] = std::min(x, y);
+            b[k] = std::max(x, y);
+        }
+        for (int k = 0; k < 3; ++k) t.push_back({a[k], b[k], 3 * f + k});
+        for (int k = 0; k < 3; ++k) t.push_back({b[k], a[k], 3 * f + k});
+    }
+    std::stable_sort(t.begin(), t.end(), [](const Contrib &x, const Contrib &y) {
+        return x.r != y.r ? x.r < y.r : x.c < y.c;
+    });
+    topo.rowptr.assign((size_t)V + 1, 0);
+    topo.ent_ptr.clear();
+    topo.ent_ptr.push_back(0);
+    for (size_t i = 0; i < t.size();) {
+        size_t j = i;
+        while (j < t.size() && t[j].r == t[i].r && t[j].c == t[i].c) {
+            topo.ent_fc.push_back(t[j].fc);
+            ++j;
+        }
+        topo.col.push_back(t[i].c);
+        topo.rowptr[t[i].r + 1]++;
+        topo.ent_ptr.push_back((int32_t)topo.ent_fc.size());
+        i = j;
+    }
+    for (int v = 0; v < V; ++v) topo.rowptr[v + 1] += topo.rowptr[v];
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// nested dissection
+
+namespace {
+
+struct NestedDissection {
+    const int32_t *rowptr, *col;
+    int n;
+    std::vector<int32_t> inset, seen, lev, queue;
+    int32_t stamp = 0;
+    std::vector<int32_t> *perm, *block_ptr;
+
+    void emit(const std::vector<int32_t> &S) {
+        perm->insert(perm->end(), S.begin(), S.end());
+        block_ptr->push_back((int32_t)perm->size());
+    }
+
+    // BFS inside the stamped set; neighbours visited in CSR order. Returns the
+    // number of levels, level offsets into queue in levptr.
+    int bfs(int32_t setstamp, int32_t root, std::vector<int32_t> &levptr) {
+        const int32_t bs = ++stamp;
+        int head = 0, tail = 0;
+        queue[tail++] = root;
+        seen[root] = bs;
+        lev[root] = 0;
+        levptr.clear();
+        while (head < tail) {
+            const int32_t v = queue[head];
+            if (lev[v] == (int32_t)levptr.size()) levptr.push_back(head);
+            ++head;
+            for (int32_t q = rowptr[v]; q < rowptr[v + 1]; ++q) {
+                const int32_t u = col[q];
+                if (inset[u] != setstamp || seen[u] == bs) continue;
+                seen[u] = bs;
+                lev[u] = lev[v] + 1;
+                queue[tail++] = u;
+            }
+        }
+        levptr.push_back(tail);
+        return (int)levptr.size() - 1;
+    }
+
+    void recurse(std::vector<int32_t> S) {
+        const int ns = (int)S.size();
+        if (ns <= kNdLeaf) { emit(S); return; }
+        const int32_t setstamp = ++stamp;
+        for (int32_t v : S) inset[v] = setstamp;
+        std::vector<int32_t> levptr;
+        int h = bfs(setstamp, S[0], levptr);
+        if (levptr[h] < ns) {
+            // several components, each in order of its smallest vertex
+            for (int32_t v : S) {
+                if (inset[v] != setstamp) continue;
+                const int hl = bfs(setstamp, v, levptr);
+                std::vector<int32_t> comp(queue.begin(), queue.begin() + levptr[hl]);
+                const int32_t cs = ++stamp;
+                for (int32_t u : comp) inset[u] = cs;
+                std::sort(comp.begin(), comp.end());
+                recurse(std::move(comp));
+            }
+            return;
+        }
+        // pseudo-peripheral vertex
+        int32_t root = S[0];
+        for (int it = 0; it < kNdPseudoPeripheralRounds; ++it) {
+            int32_t best = -1, bestdeg = 0;
+            for (int q = levptr[h - 1]; q < levptr[h]; ++q) {
+                const int32_t v = queue[q];
+                int32_t deg = 0;
+                for (int32_t e = rowptr[v]; e < rowptr[v + 1]; ++e) deg += (inset[col[e]] == setstamp);
+                if (best < 0 || deg < bestdeg || (deg == bestdeg && v < best)) { best = v; bestdeg = deg; }
+            }
+            std::vector<int32_t> lp2;
+            const int h2 = bfs(setstamp, best, lp2);
+            if (h2 > h) { root = best; h = h2; levptr = lp2; }
+            else break;
+        }
+        h = bfs(setstamp, root, levptr);
+        if (h < 3) { emit(S); return; }
+        int bestk = -1;
+        int64_t bsz = 0, bdiff = 0;
+        for (int k = 1; k <= h - 2; ++k) {
+            const int64_t a = levptr[k], s = levptr[k + 1] - levptr[k], b = (int64_t)ns - a - s;
+            const int64_t mn = std::min(a, b);
+            if (mn * kNdBalDen < (int64_t)kNdBalNum * ns) continue;
+            const int64_t d = a > b ? a - b : b - a;
+            if (bestk < 0 || s < bsz || (s == bsz && d < bdiff)) { bestk = k; bsz = s; bdiff = d; }
+        }
+        if (bestk < 0) {
+            bestk = h - 2;
+            for (int k = 1; k <= h - 2; ++k)
+                if (2LL * levptr[k + 1] >= ns) { bestk = k; break; }
+        }
+        const int k = bestk;
+        std::vector<int32_t> A, B, Sep;
+        A.assign(queue.begin(), queue.begin() + levptr[k]);
+        for (int q = levptr[k]; q < levptr[k + 1]; ++q) {
+            const int32_t v = queue[q];
+            bool touches = false;
+            for (int32_t e = rowptr[v]; e < rowptr[v + 1] && !touches; ++e) {
+                const int32_t u = col[e];
+                touches = (inset[u] == setstamp && lev[u] == k + 1);
+            }
+            (touches ? Sep : A).push_back(v);
+        }
+        B.assign(queue.begin() + levptr[k + 1], queue.begin() + levptr[h]);
+        std::sort(A.begin(), A.end());
+        std::sort(B.begin(), B.end());
+        std::sort(Sep.begin(), Sep.end());
+        recurse(std::move(A));
+        recurse(std::move(B));
+        emit(Sep);
+    }
+};
+
+}  // namespace
+
+void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int32_t> &perm,
+              std::vector<int32_t> &block_ptr) {
+    perm.clear();
+    block_ptr.assign(1, 0);
+    if (n <= 0) return;
+    NestedDissection nd;
+    nd.rowptr = rowptr;
+    nd.col = col;
+    nd.n = n;
+    nd.inset.assign(n, 0);
+    nd.seen.assign(n, 0);
+    nd.lev.assign(n, 0);
+    nd.queue.assign(n, 0);
+    nd.perm = &perm;
+    nd.block_ptr = &block_ptr;
+    std::vector<int32_t> S(n);
+    std::iota(S.begin(), S.end(), 0);
+    nd.recurse(std::move(S));
+}
+
+// ---------------------------------------------------------------------------
+
+bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
+                    std::string &err, bool &singular) {
+    singular = false;
+    sym = Symbolic();
+    const int V = topo.V;
+    sym.V = V;
+    sym.constrained = constrained;
+    // free-variable map (arap.h:261-272)
+    std::vector<int32_t> fidx(V, -1), fvert;
+    for (int v = 0; v < V; ++v)
+        if (!constrained[v]) { fidx[v] = (int32_t)fvert.size(); fvert.push_back(v); }
+    const int m = (int)fvert.size();
+    sym.m = m;
+    // graph of L's off-diagonal pattern over free indices (arap.h:319-330)
+    std::vector<int32_t> grow(m + 1, 0), gcol;
+    std::vector<uint8_t> touches_c(m, 0);
+    for (int a = 0; a < m; ++a) {
+        const int v = fvert[a];
+        for (int32_t q = topo.rowptr[v]; q < topo.rowptr[v + 1]; ++q) {
+            const int u = topo.col[q];
+            if (u == v) continue;
+            if (constrained[u]) { touches_c[a] = 1; continue; }
+            gcol.push_back(fidx[u]);
+        }
+        grow[a + 1] = (int32_t)gcol.size();
+    }
+    // every free component must reach a constrained vertex, else L is singular
+    {
+        std::vector<int32_t> comp(m, -1), stack;
+        for (int a = 0; a < m; ++a) {
+            if (comp[a] >= 0) continue;
+            bool anchored = false;
+            stack.assign(1, a);
+            comp[a] = a;
+            while (!stack.empty()) {
+                const int x = stack.back();
+                stack.pop_back();
+                anchored |= touches_c[x] != 0;
+                for (int32_t q = grow[x]; q < grow[x + 1]; ++q)
+                    if (comp[gcol[q]] < 0) { comp[gcol[q]] = a; stack.push_back(gcol[q]); }
+            }
+            if (!anchored) {
+                singular = true;
+                err = "free vertex " + std::to_string(fvert[a]) +
+                      " belongs to a mesh component without constrained vertices (singular Laplacian)";
+                return false;
+            }
+        }
+    }
+    nd_order(m, grow.data(), gcol.data(), sym.perm, sym.block_ptr);
+    std::vector<int32_t> iperm(m);
+    for (int k = 0; k < m; ++k) iperm[sym.perm[k]] = k;
+    // device order: free vertices in elimination order, then constrained ascending
+    sym.newidx.assign(V, -1);
+    sym.oldidx.assign(V, -1);
+    for (int a = 0; a < m; ++a) sym.newidx[fvert[a]] = iperm[a];
+    int nc = m;
+    for (int v = 0; v < V; ++v)
+        if (constrained[v]) sym.newidx[v] = nc++;
+    for (int v = 0; v < V; ++v) sym.oldidx[sym.newidx[v]] = v;
+    // adjacency in device order
+    const int nnz = topo.nnz();
+    sym.drow.assign(V + 1, 0);
+    sym.dcol.resize(nnz);
+    sym.dent.resize(nnz);
+    {
+        int32_t e = 0;
+        for (int k = 0; k < V; ++k) {
+            const int v = sym.oldidx[k];
+            for (int32_t q = topo.rowptr[v]; q < topo.rowptr[v + 1]; ++q) {
+                sym.dcol[e] = sym.newidx[topo.col[q]];
+                sym.dent[e] = q;
+                ++e;
+            }
+            sym.drow[k + 1] = e;
+        }
+    }
+    // permuted free graph: adjacency of device index k < m (neighbours < m)
+    std::vector<int32_t> prow(m + 1, 0), pcol;
+    pcol.reserve(gcol.size());
+    for (int k = 0; k < m; ++k) {
+        const int a = sym.perm[k];
+        for (int32_t q = grow[a]; q < grow[a + 1]; ++q) pcol.push_back(iperm[gcol[q]]);
+        prow[k + 1] = (int32_t)pcol.size();
+    }
+    // elimination tree (Liu, with path compression) and factor column counts
+    sym.etree.assign(m, -1);
+    {
+        std::vector<int32_t> anc(m, -1);
+        for (int k = 0; k < m; ++k) {
+            for (int32_t q = prow[k]; q < prow[k + 1]; ++q) {
+                int32_t i = pcol[q];
+                while (i != -1 && i < k) {
+                    const int32_t next = anc[i];
+                    anc[i] = k;
+                    if (next == -1) { sym.etree[i] = k; break; }
+                    i = next;
+                }
+            }
+        }
+        std::vector<int32_t> mark(m, -1);
+        int64_t nz = m;
+        for (int k = 0; k < m; ++k) {
+            mark[k] = k;
+            for (int32_t q = prow[k]; q < prow[k + 1]; ++q) {
+                int32_t i = pcol[q];
+                if (i >= k) continue;
+                while (mark[i] != k) { mark[i] = k; ++nz; i = sym.etree[i]; }
+            }
+        }
+        sym.factor_nnz = nz;
+    }
+    // supernodes = the dissection's blocks
+    const int S = (int)sym.block_ptr.size() - 1;
+    sym.S = S;
+    sym.sn.assign(S, SnInfo());
+    std::vector<int32_t> owner(m);
+    for (int s = 0; s < S; ++s)
+        for (int k = sym.block_ptr[s]; k < sym.block_ptr[s + 1]; ++k) owner[k] = s;
+    std::vector<std::vector<int32_t>> strct(S), children(S);
+    std::vector<int32_t> mark(m, -1);
+    for (int s = 0; s < S; ++s) {
+        const int f = sym.block_ptr[s], l = sym.block_ptr[s + 1];
+        std::vector<int32_t> &st = strct[s];
+        for (int k = f; k < l; ++k)
+            for (int32_t q = prow[k]; q < prow[k + 1]; ++q) {
+                const int32_t r = pcol[q];
+                if (r >= l && mark[r] != s) { mark[r] = s; st.push_back(r); }
+            }
+        for (int32_t c : children[s])
+            for (int32_t r : strct[c])
+                if (r >= l && mark[r] != s) { mark[r] = s; st.push_back(r); }
+        std::sort(st.begin(), st.end());
+        const int p = st.empty() ? -1 : owner[st[0]];
+        SnInfo &d = sym.sn[s];
+        d.first = f;
+        d.ncol = l - f;
+        d.nrow = d.ncol + (int32_t)st.size();
+        d.parent = p;
+        if (p >= 0) children[p].push_back(s);
+    }
+    // levels, offsets, struct rows, children, relative indices
+    int maxlev = 0;
+    int64_t poff = 0, doff = 0, uoff = 0, voff = 0;
+    double flops = 0.0;
+    for (int s = 0; s < S; ++s) {
+        SnInfo &d = sym.sn[s];
+        int lv = 0;
+        for (int32_t c : children[s]) lv = std::max(lv, sym.sn[c].level + 1);
+        d.level = lv;
+        maxlev = std::max(maxlev, lv);
+        const int nb = d.nrow - d.ncol;
+        d.panel_off = poff;
+        poff += (int64_t)d.nrow * d.ncol;
+        d.dinv_off = doff;
+        doff += (int64_t)((d.ncol + kDiagBlock - 1) / kDiagBlock) * kDiagBlock * kDiagBlock;
+        d.upd_off = uoff;
+        uoff += (int64_t)nb * nb;
+        d.uvec_off = voff;
+        voff += nb;
+        d.rows_off = (int32_t)sym.rows.size();
+        sym.rows.insert(sym.rows.end(), strct[s].begin(), strct[s].end());
+        d.child_begin = (int32_t)sym.child.size();
+        sym.child.insert(sym.child.end(), children[s].begin(), children[s].end());
+        d.child_end = (int32_t)sym.child.size();
+        sym.max_nrow = std::max(sym.max_nrow, (int)d.nrow);
+        sym.max_ncol = std::max(sym.max_ncol, (int)d.ncol);
+        sym.max_children = std::max(sym.max_children, (int)children[s].size());
+        const double nc_ = d.ncol, nb_ = nb;
+        flops += nc_ * nc_ * nc_ / 3.0 + nc_ * nc_ * nb_ + nc_ * nb_ * nb_;
+    }
+    sym.factor_flops = flops;
+    sym.panel_size = poff;
+    sym.dinv_size = doff;
+    sym.upd_size = uoff;
+    sym.uvec_size = voff;
+    // relind: where each struct row of s sits in its parent's front
+    for (int s = 0; s < S; ++s) {
+        SnInfo &d = sym.sn[s];
+        d.relind_off = (int32_t)sym.relind.size();
+        if (d.parent < 0) continue;
+        const SnInfo &p = sym.sn[d.parent];
+        const int32_t *prs = sym.rows.data() + p.rows_off;
+        const int pnb = p.nrow - p.ncol;
+        for (int32_t r : strct[s]) {
+            int32_t pos;
+            if (r < p.first + p.ncol) {
+                pos = r - p.first;
+            } else {
+                const int32_t *it = std::lower_bound(prs, prs + pnb, r);
+                if (it == prs + pnb || *it != r) {
+                    err = "internal: struct row missing from parent front";
+                    return false;
+                }
+                pos = p.ncol + (int32_t)(it - prs);
+            }
+            sym.relind.push_back(pos);
+        }
+    }
+    // supernodes grouped by level
+    sym.level_ptr.assign(maxlev + 2, 0);
+    for (int s = 0; s < S; ++s) sym.level_ptr[sym.sn[s].level + 1]++;
+    for (int l = 0; l <= maxlev; ++l) sym.level_ptr[l + 1] += sym.level_ptr[l];
+    sym.level_sn.assign(S, 0);
+    {
+        std::vector<int32_t> fill(sym.level_ptr.begin(), sym.level_ptr.end() - 1);
+        for (int s = 0; s < S; ++s) sym.level_sn[fill[sym.sn[s].level]++] = s;
+    }
+    if (S == 0) sym.level_ptr.assign(1, 0);
+    // assembly maps: L_kk and L_lk = -w_kl (l > k, both free) into the panels
+    sym.amap.assign(nnz, -1);
+    sym.dmap.assign(m, -1);
+    for (int k = 0; k < m; ++k) {
+        const SnInfo &d = sym.sn[owner[k]];
+        const int cidx = k - d.first;
+        const int32_t *rs = sym.rows.data() + d.rows_off;
+        const int nb = d.nrow - d.ncol;
+        sym.dmap[k] = d.panel_off + (int64_t)cidx * d.nrow + cidx;
+        for (int32_t e = sym.drow[k]; e < sym.drow[k + 1]; ++e) {
+            const int32_t l = sym.dcol[e];
+            if (l >= m || l <= k) continue;
+            int32_t pos;
+            if (l < d.first + d.ncol) {
+                pos = l - d.first;
+            } else {
+                const int32_t *it = std::lower_bound(rs, rs + nb, l);
+                if (it == rs + nb || *it != l) {
+                    err = "internal: matrix entry outside its supernode's front";
+                    return false;
+                }
+                pos = d.ncol + (int32_t)(it - rs);
+            }
+            sym.amap[e] = d.panel_off + (int64_t)cidx * d.nrow + pos;
+        }
+    }
+    return true;
+}
+
+}  // namespace arapgpu

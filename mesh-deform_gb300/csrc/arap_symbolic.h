@@ -1,0 +1,98 @@
+// arap_symbolic.h -- host-side symbolic analysis for the GPU ARAP solver.
+//
+// Everything here is integer work done once per mesh (adjacency) or once per
+// constrained-vertex set (ordering, elimination tree, supernodes, assembly
+// maps). It is deterministic: the same mesh and constraint set give the same
+// arrays on every machine.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace arapgpu {
+
+// Nested-dissection parameters (must match the oracle's ND_LEAF / ND_BAL_*).
+constexpr int kNdLeaf = 64;
+constexpr int kNdBalNum = 4;
+constexpr int kNdBalDen = 10;
+constexpr int kNdPseudoPeripheralRounds = 8;
+
+// Block width of the dense diagonal blocks inside a supernode.
+constexpr int kDiagBlock = 32;
+
+// Vertex adjacency of a triangle mesh: the sparsity pattern of _edgeWeights
+// (inc/deform/arap.h:224-238), sorted columns, one entry per undirected edge
+// direction (a face whose corners repeat contributes a self entry, as in the
+// reference). For every CSR entry, the faces that contribute to its weight, in
+// face order (setFromTriplets sums duplicates in insertion order).
+struct Topology {
+    int V = 0, F = 0;
+    std::vector<int32_t> faces;      // 3F
+    std::vector<int32_t> rowptr;     // V+1
+    std::vector<int32_t> col;        // nnz
+    std::vector<int32_t> ent_ptr;    // nnz+1
+    std::vector<int32_t> ent_fc;     // face*3 + k (k: which cotangent of the face)
+    int nnz() const { return (int)col.size(); }
+};
+
+bool build_topology(int V, int F, const int32_t *faces, Topology &topo, std::string &err);
+
+// Per-supernode description used by the kernels (plain data, copied to the device).
+struct SnInfo {
+    int32_t first;       // first column (device / elimination order)
+    int32_t ncol;        // columns in the supernode
+    int32_t nrow;        // rows of the front: ncol + |struct|
+    int32_t parent;      // parent supernode or -1
+    int64_t panel_off;   // nrow x ncol column-major panel in the factor array
+    int64_t dinv_off;    // ceil(ncol/kDiagBlock) blocks of kDiagBlock^2 inverse diagonal blocks
+    int64_t upd_off;     // nb x nb update matrix (nb = nrow - ncol)
+    int64_t uvec_off;    // nb rows of the forward-solve update vectors
+    int32_t rows_off;    // offset of the struct row list (nb entries, device indices)
+    int32_t relind_off;  // offset of this supernode's struct positions in its parent's front
+    int32_t child_begin; // children [child_begin, child_end) in the child list
+    int32_t child_end;
+    int32_t level;       // height in the supernodal tree (leaves = 0)
+    int32_t pad;
+};
+
+struct Symbolic {
+    int V = 0, m = 0;                 // vertices, free vertices
+    std::vector<uint8_t> constrained; // V
+    std::vector<int32_t> perm;        // m: free index eliminated k-th
+    std::vector<int32_t> etree;       // m: elimination tree of the permuted matrix
+    std::vector<int32_t> block_ptr;   // S+1: supernode partition of [0, m)
+    std::vector<int32_t> newidx;      // V: vertex -> device index
+    std::vector<int32_t> oldidx;      // V: device index -> vertex
+    // adjacency in device order (row k = vertex oldidx[k]; entries keep the
+    // original neighbour order)
+    std::vector<int32_t> drow, dcol;  // V+1, nnz
+    std::vector<int32_t> dent;        // nnz: original CSR entry of each device entry
+    // supernodes
+    int S = 0;
+    std::vector<SnInfo> sn;
+    std::vector<int32_t> rows;        // concatenated struct rows
+    std::vector<int32_t> relind;      // concatenated positions in the parent's front
+    std::vector<int32_t> child;       // concatenated children lists
+    std::vector<int32_t> level_ptr;   // levels+1
+    std::vector<int32_t> level_sn;    // supernodes grouped by level (leaves first)
+    int max_nrow = 0, max_ncol = 0, max_children = 0;
+    int64_t panel_size = 0, dinv_size = 0, upd_size = 0, uvec_size = 0;
+    int64_t factor_nnz = 0;           // nonzeros of the scalar factor (from the etree)
+    double factor_flops = 0.0;        // dense flops of the supernodal factorisation
+    // assembly maps into the factor array
+    std::vector<int64_t> amap;        // per device entry: destination of -w (or -1)
+    std::vector<int64_t> dmap;        // per free device row: destination of the diagonal
+};
+
+// Builds the symbolic analysis for a constrained-vertex set. Returns false and
+// sets err when the free graph has a component that touches no constrained
+// vertex (the constrained Laplacian is then singular).
+bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
+                    std::string &err, bool &singular);
+
+// Nested-dissection order of a symmetric graph (no self loops); exposed for tests.
+void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int32_t> &perm,
+              std::vector<int32_t> &block_ptr);
+
+}  // namespace arapgpu
