@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""ARAP deformation benchmark: ARAP iterations/s on one GB300.
+
+Workload (one "step"): one dirty deform of the twisted bar -- the 10x1x1 box
+surface at 0.025 spacing (67,202 vertices, 134,400 triangles), anchors x<0.2
+(2,801), handles x>9.8 (2,801) turned 90 deg about the bar axis and shifted
+(0,0.5,0) -- in the mixed-precision form, 30 local/global iterations. A dirty
+deform is what the reference does after setConstraint (inc/deform/arap.h:102-129):
+cotan weights, constrained Laplacian and its factorisation, then the iterations.
+Inputs are seeded synthetic meshes (the reference publishes no data set).
+
+value: iterations/s with the rest pose and targets already in device memory
+       (arap_invalidate + arap_deform, output left on the device), timed with
+       CUDA events on the library's stream; L2 (129 MB) is flushed before each
+       step by writing a 256 MB buffer, outside the timed events.
+e2e:   the same steps through the C ABI with host buffers: pinned rest
+       positions and targets copied in, deformed positions copied out.
+cpu_baseline: the FP64 C restatement of arap.h (the oracle) on one host core,
+       full requests of the same workload; its output also gives the error of
+       the GPU result (bbox-diagonal-relative, stated on every line).
+
+--impl reference times the reference's CPU path (the oracle restatement,
+since the reference needs Eigen and cannot be built) with one independent
+request per host thread.
+Multi-GPU: replicas only (one independent replica per rank, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "mesh-deform_gb300"
+for p in (str(ROOT), str(PKG)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "ARAP iterations/s and p50/p99 deform latency at <=1e-6 bbox-rel error vs FP64"
+UNIT = "iterations/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def workload(args):
+    import arap_workloads as W
+
+    if args.workload == "twisted_bar":
+        return W.cfg_twisted_bar(h=args.h, iterations=args.iterations, precision=args.precision)
+    if args.workload == "icosphere_l4":
+        w = W.cfg_icosphere_l4(iterations=args.iterations)
+        w.precision = args.precision
+        return w
+    if args.workload == "noisy_sphere":
+        return W.cfg_noisy_sphere(iterations=args.iterations, precision=args.precision)
+    raise SystemExit(f"unknown workload {args.workload}")
+
+
+def config_of(w, args, extra=None):
+    c = {
+        "workload": w.name,
+        "vertices": w.V,
+        "faces": w.F,
+        "constrained": int(len(w.cidx)),
+        "free": int(w.V - len(w.cidx)),
+        "iterations_per_step": w.iterations,
+        "precision": args.precision,
+        "refine_steps": args.refine,
+        "step": "dirty deform (weights + factor + iterations), one request",
+        "l2": "flushed before every step (256 MB write)",
+        "parallelism": f"replicas{args.gpus}",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_requests(w, n_requests: int, threads: int):
+    """n_requests full dirty deforms of w by the FP64 oracle, on `threads` threads.
+    Returns (seconds, last output)."""
+    from oracle import oracle as O
+
+    O.build()
+    O.load()
+
+    def one(_):
+        ok, out = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, w.iterations)
+        assert ok
+        return out
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        outs = list(ex.map(one, range(n_requests)))
+    return time.perf_counter() - t0, outs[-1]
+
+
+def run_reference(args):
+    """The reference's CPU path (oracle restatement), one request per host thread."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    w = workload(args)
+    threads = os.cpu_count() or 1
+    per_step = []
+    for s in range(args.warmup + args.steps):
+        dt, _ = cpu_oracle_requests(w, threads, threads)
+        if s >= args.warmup:
+            per_step.append(dt)
+    total = sum(per_step)
+    its = threads * w.iterations * len(per_step)
+    value = its / total
+    sample = f"{threads} concurrent dirty deform({w.iterations}) requests per step on {w.name}"
+    line = {
+        "impl": "reference",
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / len(per_step), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_of(w, args, {"precision": "fp64", "threads": threads}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "latency_ms": {"p50": 1e3 * statistics.median(per_step), "p99": 1e3 * float(np.percentile(per_step, 99))},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="twisted_bar")
+    ap.add_argument("--h", type=float, default=0.025)
+    ap.add_argument("--iterations", type=int, default=30)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--refine", type=int, default=2)
+    ap.add_argument("--cpu-requests", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    import arap_gpu as G
+    import arap_workloads as W
+
+    w = workload(args)
+    ctx = G.ArapContext(w.V, w.faces, device=local)
+    ctx.set_precision(args.precision, args.refine)
+    ctx.set_rest_positions(w.positions)
+    ctx.set_constraints(w.cidx, w.ctargets)
+    first = ctx.deform(w.iterations)  # symbolic analysis + allocation happen here, untimed
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        ctx.invalidate()
+        rc = ctx.deform_rc(w.iterations, None)
+        if rc != G.ARAP_OK:
+            raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step()
+    # ---- timed region (device-resident inputs) ----
+    ctx.set_profiling(True)
+    ctx.reset_kernel_stats()
+    clocks = ClockSampler(local)
+    launches = 0
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    clocks.start()
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+        launches += ctx.launch_count()
+    barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    kstats = ctx.kernel_stats()
+    kmodel = ctx.kernel_model()
+    ctx.set_profiling(False)
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    its_total = w.iterations * args.steps * world
+    value = its_total / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    rest_h = torch.from_numpy(np.ascontiguousarray(w.positions)).pin_memory().numpy()
+    idx_h = torch.from_numpy(np.ascontiguousarray(w.cidx, dtype=np.int32)).pin_memory().numpy()
+    tgt_h = torch.from_numpy(np.ascontiguousarray(w.ctargets)).pin_memory().numpy()
+    out_h = torch.empty((w.V, 3), dtype=torch.float64).pin_memory().numpy()
+    e2e_s = []
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.set_rest_positions(rest_h)
+        ctx.set_constraints(idx_h, tgt_h)
+        rc = ctx.deform_rc(w.iterations, out_h)
+        t1 = time.perf_counter()
+        if rc != G.ARAP_OK:
+            raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+        if k >= args.warmup:
+            e2e_s.append(t1 - t0)
+    e2e_total = sum(e2e_s)
+    if dist is not None:
+        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = its_total / e2e_total
+    h2d = w.positions.nbytes + idx_h.nbytes + tgt_h.nbytes
+    d2h = out_h.nbytes
+
+    # ---- roofline of the dominant kernel class ----
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    dom = max(kstats, key=lambda k: kstats[k][0])
+    dom_ms, dom_n = kstats[dom]
+    dom_bytes = kmodel[dom][0]
+    per_launch_ms = dom_ms / max(dom_n, 1)
+    if dom == "factor":  # model bytes cover a whole factorisation (all levels)
+        per_launch_ms = dom_ms / max(args.steps, 1)
+    achieved = dom_bytes / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "ncu_traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get(w.name, {}).get(dom)
+        except Exception:
+            traffic = None
+
+    # ---- CPU baseline (oracle, one core) + error of the GPU result ----
+    cpu = None
+    err = None
+    if rank == 0 and not args.no_cpu_baseline:
+        dt, ref = cpu_oracle_requests(w, args.cpu_requests, 1)
+        cpu = {"value": args.cpu_requests * w.iterations / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_requests} dirty deform({w.iterations}) requests of {w.name} on one thread "
+                         f"({dt:.1f} s)"}
+        err = W.bbox_rel_error(out_h, ref, w.positions)
+        err_first = W.bbox_rel_error(first, ref, w.positions)
+        log(f"error vs FP64 oracle: {err:.3e} (first deform {err_first:.3e})")
+
+    setup_ms, iter_ms = ctx.timing()
+    lat = sorted(step_ms)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": config_of(w, args),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                     "bytes_per_launch": dom_bytes, "ms_per_launch": per_launch_ms},
+        "cpu_baseline": cpu,
+        "error_vs_fp64_oracle": err,
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": float(np.percentile(lat, 99))},
+        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kstats.items()},
+        "last_step_ms": {"setup": setup_ms, "iterations": iter_ms},
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -132,6 +132,36 @@ int arap_get_timing(arap_ctx *ctx, double *setup_ms, double *iterations_ms);
 /* Number of kernel launches issued by the last arap_deform. */
 int arap_get_launch_count(arap_ctx *ctx, int64_t *launches);
 
+/* The CUDA stream (cudaStream_t) every kernel of this context runs on, so a
+   caller can order its own work or record events on it. */
+int arap_get_stream(arap_ctx *ctx, void **stream);
+
+/* Kernel classes timed by the optional per-launch profiler. */
+typedef enum arap_kernel_class {
+    ARAP_K_WEIGHTS = 0,   /* cotan weights (face cotangents + edge sums) */
+    ARAP_K_ASSEMBLE = 1,  /* vertex setup + Laplacian/bFixed assembly */
+    ARAP_K_FACTOR = 2,    /* multifrontal Cholesky levels */
+    ARAP_K_LOCAL = 3,     /* local step: covariance + rotation fit */
+    ARAP_K_RHS = 4,       /* right-hand side assembly */
+    ARAP_K_RESIDUAL = 5,  /* FP64 residual of the global system */
+    ARAP_K_SOLVE_FWD = 6, /* forward supernodal triangular solve */
+    ARAP_K_SOLVE_BWD = 7, /* backward supernodal triangular solve */
+    ARAP_K_GATHER = 8,    /* positions back to vertex order */
+    ARAP_K_NUM_CLASSES = 9
+} arap_kernel_class;
+
+/* enable != 0 brackets every launch with CUDA events on the context's stream
+   and accumulates the device time per kernel class until reset. */
+int arap_set_profiling(arap_ctx *ctx, int32_t enable);
+int arap_reset_kernel_stats(arap_ctx *ctx);
+int arap_get_kernel_stats(arap_ctx *ctx, int32_t kernel_class, double *total_ms, int64_t *launches);
+
+/* Algorithmic DRAM bytes and flops of ONE launch of a kernel class for the
+   current problem and precision (the minimum traffic: every input read once,
+   every output written once, unpadded 3-vectors; for FACTOR the sum over all
+   of its level launches). Used for roofline fractions. */
+int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, double *flops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,7 +62,14 @@ SIGNATURES = {
     "arap_analyze_pattern": (C.c_int, [_I32, _I32, _ip, _I32, _ip, _ip, _ip, _lp, _ip, _ip, _ip]),
     "arap_get_timing": (C.c_int, [_P, _dp, _dp]),
     "arap_get_launch_count": (C.c_int, [_P, _lp]),
+    "arap_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "arap_set_profiling": (C.c_int, [_P, _I32]),
+    "arap_reset_kernel_stats": (C.c_int, [_P]),
+    "arap_get_kernel_stats": (C.c_int, [_P, _I32, _dp, _lp]),
+    "arap_get_kernel_model": (C.c_int, [_P, _I32, _dp, _dp]),
 }
+
+KERNEL_CLASSES = ["weights", "assemble", "factor", "local", "rhs", "residual", "solve_fwd", "solve_bwd", "gather"]
 
 _lib = None
 
@@ -202,6 +209,33 @@ class ArapContext:
         n = C.c_int64()
         self._check(self.lib.arap_get_launch_count(self.h, C.byref(n)))
         return n.value
+
+    def stream(self) -> int:
+        p = _P()
+        self._check(self.lib.arap_get_stream(self.h, C.byref(p)))
+        return int(p.value or 0)
+
+    def set_profiling(self, enable: bool):
+        self._check(self.lib.arap_set_profiling(self.h, 1 if enable else 0))
+
+    def reset_kernel_stats(self):
+        self._check(self.lib.arap_reset_kernel_stats(self.h))
+
+    def kernel_model(self) -> dict:
+        out = {}
+        for k, name in enumerate(KERNEL_CLASSES):
+            b, f = C.c_double(), C.c_double()
+            self._check(self.lib.arap_get_kernel_model(self.h, k, C.byref(b), C.byref(f)))
+            out[name] = (b.value, f.value)
+        return out
+
+    def kernel_stats(self) -> dict:
+        out = {}
+        for k, name in enumerate(KERNEL_CLASSES):
+            ms, n = C.c_double(), C.c_int64()
+            self._check(self.lib.arap_get_kernel_stats(self.h, k, C.byref(ms), C.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
 
 
 def analyze_pattern(n_vertices: int, faces: np.ndarray, constrained) -> dict:

@@ -76,6 +76,14 @@ struct arap_ctx {
     DevSym ds{};
     int64_t launches = 0;
     double setup_ms = 0.0, iter_ms = 0.0;
+    // optional per-launch profiler
+    bool profiling = false;
+    std::vector<cudaEvent_t> evpool;
+    size_t evused = 0;
+    struct Pending { int cls; cudaEvent_t a, b; };
+    std::vector<Pending> pending;
+    double kms[ARAP_K_NUM_CLASSES] = {0};
+    int64_t kcnt[ARAP_K_NUM_CLASSES] = {0};
 };
 
 #define CK(call)                                                                       \
@@ -88,6 +96,45 @@ struct arap_ctx {
     } while (0)
 
 namespace {
+
+cudaEvent_t pool_event(arap_ctx *ctx) {
+    if (ctx->evused == ctx->evpool.size()) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        ctx->evpool.push_back(e);
+    }
+    return ctx->evpool[ctx->evused++];
+}
+
+// Brackets one launch with events when profiling is on.
+struct Prof {
+    arap_ctx *ctx;
+    int cls;
+    cudaEvent_t a = nullptr;
+    Prof(arap_ctx *c, int k) : ctx(c), cls(k) {
+        if (ctx->profiling && (a = pool_event(ctx))) cudaEventRecord(a, ctx->stream);
+    }
+    ~Prof() {
+        if (!a) return;
+        cudaEvent_t b = pool_event(ctx);
+        if (!b) return;
+        cudaEventRecord(b, ctx->stream);
+        ctx->pending.push_back({cls, a, b});
+    }
+};
+
+// Adds the device time of completed bracketed launches (stream synchronized).
+void collect_profile(arap_ctx *ctx) {
+    for (const auto &p : ctx->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            ctx->kms[p.cls] += ms;
+            ctx->kcnt[p.cls] += 1;
+        }
+    }
+    ctx->pending.clear();
+    ctx->evused = 0;
+}
 
 template <typename T>
 cudaError_t upload(DevBuf &buf, const std::vector<T> &v, cudaStream_t st) {
@@ -190,22 +237,32 @@ int setup_numeric(arap_ctx *ctx) {
     CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
 
     // cotan weights (arap.h:182-239)
-    launch_edge_weights(ctx->dt, d, ctx->hc.as<double>(), ctx->w64.as<double>(),
-                        sizeof(T) == 4 ? ctx->w32.as<float>() : nullptr, ctx->w_orig.as<double>(), st);
+    {
+        Prof pr(ctx, ARAP_K_WEIGHTS);
+        launch_edge_weights(ctx->dt, d, ctx->hc.as<double>(), ctx->w64.as<double>(),
+                            sizeof(T) == 4 ? ctx->w32.as<float>() : nullptr, ctx->w_orig.as<double>(), st);
+    }
     // geometry, constraint snap, rotations = I
     Vec4<T> *p_t = sizeof(T) == 4 ? ctx->p32.as<Vec4<T>>() : ctx->p64.as<Vec4<T>>();
     Vec4<T> *pc_t = sizeof(T) == 4 ? ctx->pc32.as<Vec4<T>>() : ctx->pc64.as<Vec4<T>>();
-    launch_setup_vertices<T>(d, ctx->rest.as<double>(), ctx->targets.as<double>(), ctx->p64.as<Vec4<double>>(),
-                             ctx->pc64.as<Vec4<double>>(), p_t, pc_t, ctx->R.as<Vec4<T>>(), st);
+    {
+        Prof pr(ctx, ARAP_K_ASSEMBLE);
+        launch_setup_vertices<T>(d, ctx->rest.as<double>(), ctx->targets.as<double>(), ctx->p64.as<Vec4<double>>(),
+                                 ctx->pc64.as<Vec4<double>>(), p_t, pc_t, ctx->R.as<Vec4<T>>(), st);
+    }
     ctx->launches += 2;
     if (m > 0) {
         CK(cudaMemsetAsync(ctx->Lval.p, 0, (size_t)s.panel_size * sizeof(T), st));
         if (s.upd_size > 0) CK(cudaMemsetAsync(ctx->Upd.p, 0, (size_t)s.upd_size * sizeof(T), st));
-        launch_assemble<T, T>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->Lval.as<T>(),
-                              ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<T>>(), st);
+        {
+            Prof pr(ctx, ARAP_K_ASSEMBLE);
+            launch_assemble<T, T>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->Lval.as<T>(),
+                                  ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<T>>(), st);
+        }
         ctx->launches += 1;
         const int nlev = (int)s.level_ptr.size() - 1;
         for (int l = 0; l < nlev; ++l) {
+            Prof pr(ctx, ARAP_K_FACTOR);
             launch_factor_level<T>(d, s.level_ptr[l], s.level_ptr[l + 1] - s.level_ptr[l], ctx->Lval.as<T>(),
                                    ctx->Upd.as<T>(), ctx->Dinv.as<T>(), ctx->errw.as<int>(), st);
             ctx->launches += 1;
@@ -232,17 +289,30 @@ int run_iterations<double>(arap_ctx *ctx, int iterations) {
     unsigned long long *tk = ctx->ticket.as<unsigned long long>();
     unsigned *fl = ctx->flags.as<unsigned>();
     for (int it = 0; it < iterations; ++it) {
-        launch_local_step<double>(d, ctx->w64.as<double>(), ctx->p64.as<Vec4<double>>(),
-                                  ctx->pc64.as<Vec4<double>>(), ctx->R.as<Vec4<double>>(), st);
+        {
+            Prof pr(ctx, ARAP_K_LOCAL);
+            launch_local_step<double>(d, ctx->w64.as<double>(), ctx->p64.as<Vec4<double>>(),
+                                      ctx->pc64.as<Vec4<double>>(), ctx->R.as<Vec4<double>>(), st);
+        }
         ctx->launches += 1;
         if (s.m == 0) continue;
-        launch_rhs<double>(d, ctx->w64.as<double>(), ctx->p64.as<Vec4<double>>(), ctx->R.as<Vec4<double>>(),
-                           ctx->bfixed.as<Vec4<double>>(), ctx->sol.as<Vec4<double>>(), st);
-        launch_solve_fwd<double>(d, ctx->Lval.as<double>(), ctx->Dinv.as<double>(), ctx->sol.as<Vec4<double>>(),
-                                 ctx->uvec.as<Vec4<double>>(), tk, fl, ctx->errw.as<int>(), ctx->smem_rows, st);
-        launch_solve_bwd<double>(d, ctx->Lval.as<double>(), ctx->Dinv.as<double>(), ctx->sol.as<Vec4<double>>(),
-                                 ctx->pc64.as<Vec4<double>>(), nullptr, 0, tk + 1, fl + s.S, ctx->errw.as<int>(),
-                                 ctx->smem_rows, st);
+        {
+            Prof pr(ctx, ARAP_K_RHS);
+            launch_rhs<double>(d, ctx->w64.as<double>(), ctx->p64.as<Vec4<double>>(), ctx->R.as<Vec4<double>>(),
+                               ctx->bfixed.as<Vec4<double>>(), ctx->sol.as<Vec4<double>>(), st);
+        }
+        {
+            Prof pr(ctx, ARAP_K_SOLVE_FWD);
+            launch_solve_fwd<double>(d, ctx->Lval.as<double>(), ctx->Dinv.as<double>(),
+                                     ctx->sol.as<Vec4<double>>(), ctx->uvec.as<Vec4<double>>(), tk, fl,
+                                     ctx->errw.as<int>(), ctx->smem_rows, st);
+        }
+        {
+            Prof pr(ctx, ARAP_K_SOLVE_BWD);
+            launch_solve_bwd<double>(d, ctx->Lval.as<double>(), ctx->Dinv.as<double>(),
+                                     ctx->sol.as<Vec4<double>>(), ctx->pc64.as<Vec4<double>>(), nullptr, 0, tk + 1,
+                                     fl + s.S, ctx->errw.as<int>(), ctx->smem_rows, st);
+        }
         ctx->launches += 3;
     }
     CK(cudaGetLastError());
@@ -257,21 +327,38 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
     unsigned long long *tk = ctx->ticket.as<unsigned long long>();
     unsigned *fl = ctx->flags.as<unsigned>();
     for (int it = 0; it < iterations; ++it) {
-        launch_local_step<float>(d, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->pc32.as<Vec4<float>>(),
-                                 ctx->R.as<Vec4<float>>(), st);
+        {
+            Prof pr(ctx, ARAP_K_LOCAL);
+            launch_local_step<float>(d, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(),
+                                     ctx->pc32.as<Vec4<float>>(), ctx->R.as<Vec4<float>>(), st);
+        }
         ctx->launches += 1;
         if (s.m == 0) continue;
-        launch_rhs<float>(d, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->R.as<Vec4<float>>(),
-                          ctx->bfixed.as<Vec4<float>>(), ctx->b.as<Vec4<float>>(), st);
+        {
+            Prof pr(ctx, ARAP_K_RHS);
+            launch_rhs<float>(d, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->R.as<Vec4<float>>(),
+                              ctx->bfixed.as<Vec4<float>>(), ctx->b.as<Vec4<float>>(), st);
+        }
         ctx->launches += 1;
         for (int r = 0; r <= ctx->refine; ++r) {
-            launch_residual(d, ctx->w64.as<double>(), ctx->diag64.as<double>(), ctx->b.as<Vec4<float>>(),
-                            ctx->pc64.as<Vec4<double>>(), ctx->sol.as<Vec4<float>>(), st);
-            launch_solve_fwd<float>(d, ctx->Lval.as<float>(), ctx->Dinv.as<float>(), ctx->sol.as<Vec4<float>>(),
-                                    ctx->uvec.as<Vec4<float>>(), tk, fl, ctx->errw.as<int>(), ctx->smem_rows, st);
-            launch_solve_bwd<float>(d, ctx->Lval.as<float>(), ctx->Dinv.as<float>(), ctx->sol.as<Vec4<float>>(),
-                                    ctx->pc64.as<Vec4<double>>(), ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S,
-                                    ctx->errw.as<int>(), ctx->smem_rows, st);
+            {
+                Prof pr(ctx, ARAP_K_RESIDUAL);
+                launch_residual(d, ctx->w64.as<double>(), ctx->diag64.as<double>(), ctx->b.as<Vec4<float>>(),
+                                ctx->pc64.as<Vec4<double>>(), ctx->sol.as<Vec4<float>>(), st);
+            }
+            {
+                Prof pr(ctx, ARAP_K_SOLVE_FWD);
+                launch_solve_fwd<float>(d, ctx->Lval.as<float>(), ctx->Dinv.as<float>(),
+                                        ctx->sol.as<Vec4<float>>(), ctx->uvec.as<Vec4<float>>(), tk, fl,
+                                        ctx->errw.as<int>(), ctx->smem_rows, st);
+            }
+            {
+                Prof pr(ctx, ARAP_K_SOLVE_BWD);
+                launch_solve_bwd<float>(d, ctx->Lval.as<float>(), ctx->Dinv.as<float>(),
+                                        ctx->sol.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(),
+                                        ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(),
+                                        ctx->smem_rows, st);
+            }
             ctx->launches += 3;
         }
     }
@@ -379,6 +466,7 @@ void arap_destroy(arap_ctx *ctx) {
                       &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->errw, &ctx->ticket,
                       &ctx->flags};
     for (DevBuf *b : bufs) b->release();
+    for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev2) cudaEventDestroy(ctx->ev2);
@@ -451,12 +539,17 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     if (!ctx->have_rest) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "rest positions not set");
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
+    CK(cudaStreamSynchronize(st));
+    collect_profile(ctx);
     ctx->launches = 0;
     ctx->setup_ms = ctx->iter_ms = 0.0;
     const bool fp64 = ctx->precision == ARAP_PRECISION_FP64;
     CK(cudaEventRecord(ctx->ev0, st));
     if (ctx->dirty) {
-        launch_face_cots(ctx->dt, ctx->rest.as<double>(), ctx->hc.as<double>(), st);
+        {
+            Prof pr(ctx, ARAP_K_WEIGHTS);
+            launch_face_cots(ctx->dt, ctx->rest.as<double>(), ctx->hc.as<double>(), st);
+        }
         ctx->launches += 1;
         if (ctx->cidx.empty()) {
             // arap.h:113-114: no constrained vertex -> weights only, no write-back
@@ -479,7 +572,10 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     if (rc != ARAP_OK) return rc;
     CK(cudaEventRecord(ctx->ev2, st));
     if (out_xyz) {
-        launch_gather_positions(ctx->ds, ctx->pc64.as<Vec4<double>>(), ctx->out.as<double>(), st);
+        {
+            Prof pr(ctx, ARAP_K_GATHER);
+            launch_gather_positions(ctx->ds, ctx->pc64.as<Vec4<double>>(), ctx->out.as<double>(), st);
+        }
         ctx->launches += 1;
         CK(cudaMemcpyAsync(out_xyz, ctx->out.p, (size_t)3 * ctx->topo.V * sizeof(double), cudaMemcpyDeviceToHost,
                            st));
@@ -487,6 +583,7 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    collect_profile(ctx);
     float a = 0.f, b = 0.f;
     cudaEventElapsedTime(&a, ctx->ev0, ctx->ev1);
     cudaEventElapsedTime(&b, ctx->ev1, ctx->ev2);
@@ -617,6 +714,96 @@ int arap_get_timing(arap_ctx *ctx, double *setup_ms, double *iterations_ms) {
 int arap_get_launch_count(arap_ctx *ctx, int64_t *launches) {
     if (check_ctx(ctx) || !launches) return ARAP_ERR_INVALID_ARGUMENT;
     *launches = ctx->launches;
+    return ARAP_OK;
+}
+
+int arap_get_stream(arap_ctx *ctx, void **stream) {
+    if (check_ctx(ctx) || !stream) return ARAP_ERR_INVALID_ARGUMENT;
+    *stream = (void *)ctx->stream;
+    return ARAP_OK;
+}
+
+int arap_set_profiling(arap_ctx *ctx, int32_t enable) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    ctx->profiling = enable != 0;
+    return ARAP_OK;
+}
+
+int arap_reset_kernel_stats(arap_ctx *ctx) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    collect_profile(ctx);
+    for (int k = 0; k < ARAP_K_NUM_CLASSES; ++k) {
+        ctx->kms[k] = 0.0;
+        ctx->kcnt[k] = 0;
+    }
+    return ARAP_OK;
+}
+
+int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, double *flops) {
+    if (check_ctx(ctx) || kernel_class < 0 || kernel_class >= ARAP_K_NUM_CLASSES) return ARAP_ERR_INVALID_ARGUMENT;
+    if (!ctx->sym_valid || ctx->state_prec < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no problem set up yet");
+    const Symbolic &s = ctx->sym;
+    const double sz = ctx->state_prec == ARAP_PRECISION_FP64 ? 8.0 : 4.0;  // scalar of the iteration
+    const double V = s.V, m = s.m, nnz = (double)s.dcol.size(), F = ctx->topo.F;
+    // panel entries below the diagonal blocks and lower-triangular entries of the
+    // inverted diagonal blocks, read once per solve sweep
+    double below = 0.0, dlow = 0.0, nbsum = 0.0;
+    for (const SnInfo &d : s.sn) {
+        for (int b0 = 0; b0 < d.ncol; b0 += kDiagBlock) {
+            const double w = std::min(kDiagBlock, d.ncol - b0);
+            below += (d.nrow - b0 - w) * w;
+            dlow += w * (w + 1) / 2;
+        }
+        nbsum += d.nrow - d.ncol;
+    }
+    double B = 0.0, FL = 0.0;
+    switch (kernel_class) {
+    case ARAP_K_WEIGHTS:  // faces + rest positions + weights out (two precisions)
+        B = F * 12 + V * 24 + F * 24 + nnz * (4 + 8 + sz);
+        FL = F * 40;
+        break;
+    case ARAP_K_ASSEMBLE:
+        B = V * (24 + 24 + 3 * sz * 2 + 9 * sz) + m * (8 + 3 * sz) + nnz * (4 + 8 + 8) + (below + dlow) * 0;
+        FL = nnz * 4;
+        break;
+    case ARAP_K_FACTOR:
+        B = (double)s.panel_size * sz * 2 + (double)s.upd_size * sz * 2 + (double)s.dinv_size * sz;
+        FL = s.factor_flops;
+        break;
+    case ARAP_K_LOCAL:  // rest + current positions, rotations out, adjacency + weights
+        B = V * (3 * sz + 3 * sz + 9 * sz) + 4 * (V + 1) + nnz * (4 + sz);
+        FL = nnz * 24 + V * 600;
+        break;
+    case ARAP_K_RHS:
+        B = m * (9 * sz + 3 * sz + 3 * sz + 3 * sz) + 4 * (m + 1) + nnz * (4 + sz);
+        FL = nnz * 24;
+        break;
+    case ARAP_K_RESIDUAL:
+        B = m * (24 + 8 + 12 + 12) + 4 * (m + 1) + nnz * (4 + 8);
+        FL = nnz * 6;
+        break;
+    case ARAP_K_SOLVE_FWD:
+    case ARAP_K_SOLVE_BWD:
+        B = (below + dlow) * sz + m * 3 * sz * 2 + nbsum * 3 * sz * 2;
+        if (kernel_class == ARAP_K_SOLVE_BWD && ctx->state_prec != ARAP_PRECISION_FP64) B += m * (24 * 2 + 12);
+        FL = (below + dlow) * 6;
+        break;
+    case ARAP_K_GATHER:
+        B = V * (24 + 24 + 4);
+        FL = 0;
+        break;
+    }
+    if (bytes) *bytes = B;
+    if (flops) *flops = FL;
+    return ARAP_OK;
+}
+
+int arap_get_kernel_stats(arap_ctx *ctx, int32_t kernel_class, double *total_ms, int64_t *launches) {
+    if (check_ctx(ctx) || kernel_class < 0 || kernel_class >= ARAP_K_NUM_CLASSES) return ARAP_ERR_INVALID_ARGUMENT;
+    if (total_ms) *total_ms = ctx->kms[kernel_class];
+    if (launches) *launches = ctx->kcnt[kernel_class];
     return ARAP_OK;
 }
 

@@ -155,8 +155,9 @@ def test_zero_iterations_snaps_targets(gpu):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_rigid_motion_is_reproduced(gpu, precision):
     """All constrained vertices moved by one rigid motion: the ARAP optimum is
-    that motion of the whole mesh (energy 0)."""
-    w = W.cfg_icosphere_l4(level=3, iterations=6)
+    that motion of the whole mesh (energy 0); 200 iterations from the rest pose
+    reach it to rounding (the FP64 CPU path gets 4e-15)."""
+    w = W.cfg_icosphere_l4(level=3, iterations=200)
     R = W.rotation_matrix([0.3, -0.5, 0.8], 0.7)
     t = np.array([0.2, -0.4, 0.1])
     tgt = w.positions[w.cidx] @ R.T + t
@@ -164,7 +165,7 @@ def test_rigid_motion_is_reproduced(gpu, precision):
         ctx.set_precision(precision, 2)
         ctx.set_rest_positions(w.positions)
         ctx.set_constraints(w.cidx, tgt)
-        out = ctx.deform(6)
+        out = ctx.deform(200)
     exp = w.positions @ R.T + t
     assert W.bbox_rel_error(out, exp, w.positions) <= (1e-9 if precision == "fp64" else 2e-6)
 
@@ -200,3 +201,22 @@ def test_all_vertices_constrained(gpu):
         ctx.set_constraints(np.arange(w.V), tgt)
         out = ctx.deform(2)
     np.testing.assert_array_equal(out, tgt)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["sphere", "bar", "plane"])
+def test_golden_fixture_deforms(gpu, name, precision):
+    """The reference's etc/ meshes with example-style constraint sets, against
+    the committed oracle outputs (tests/golden/oracle_deforms.npz)."""
+    from pathlib import Path
+
+    g = Path(__file__).resolve().parent / "golden"
+    m = np.load(g / "meshes.npz")
+    d = np.load(g / "oracle_deforms.npz")
+    v, f = m[f"{name}_v"], m[f"{name}_f"]
+    with gpu.ArapContext(len(v), f) as ctx:
+        ctx.set_precision(precision, 2)
+        ctx.set_rest_positions(v)
+        ctx.set_constraints(d[f"{name}_cidx"], d[f"{name}_targets"])
+        out = ctx.deform(int(d[f"{name}_iterations"]))
+    assert W.bbox_rel_error(out, d[f"{name}_out"], v) <= TOL[precision]
