@@ -45,6 +45,8 @@ thread_local std::string g_create_error;
 
 }  // namespace
 
+
+
 struct arap_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
