@@ -162,6 +162,30 @@ int arap_get_kernel_stats(arap_ctx *ctx, int32_t kernel_class, double *total_ms,
    of its level launches). Used for roofline fractions. */
 int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, double *flops);
 
+/* Cotan edge weights (the values of _edgeWeights, inc/deform/arap.h:182-239)
+   for callers that cannot allocate device memory when they need them: a
+   per-frame callback of an interactive viewer must not stall the device on
+   cudaMalloc, and a host application that manages all device memory through
+   its own pool forbids driver allocations. This entry point has no counterpart
+   in the reference. It allocates nothing: its only scratch, three doubles per
+   face, is a file-scope __device__ array of at most 524,288 faces (12 MiB,
+   held on every device that loads the library until the process exits).
+   All pointers are DEVICE pointers owned by the caller: faces (3*n_faces),
+   xyz (3*n_vertices doubles), the weight pattern rowptr (n_vertices+1) / col
+   (nnz, columns sorted in each row, every mesh edge present in both
+   directions -- the pattern arap_get_edge_weights returns), and the output
+   val (nnz doubles, overwritten). The kernels run on `stream` (a
+   cudaStream_t; NULL = default stream) of the calling thread's current
+   device and the call returns without waiting for them. The first call on a
+   device looks up the scratch array's device address; make that first call
+   before any stream capture. All calls on one device share the scratch array,
+   which keeps the last call's contents: calls whose kernels overlap on the GPU
+   race and must be ordered by the caller. More than 524,288 faces returns
+   ARAP_ERR_UNSUPPORTED. Values equal arap_get_edge_weights bit for bit when
+   every edge lies on at most two faces. */
+int arap_cotan_weights_static(int32_t n_vertices, int32_t n_faces, const int32_t *faces, const double *xyz,
+                              const int32_t *rowptr, const int32_t *col, int32_t nnz, double *val, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,7 @@ SIGNATURES = {
     "arap_reset_kernel_stats": (C.c_int, [_P]),
     "arap_get_kernel_stats": (C.c_int, [_P, _I32, _dp, _lp]),
     "arap_get_kernel_model": (C.c_int, [_P, _I32, _dp, _dp]),
+    "arap_cotan_weights_static": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _I32, _P, _P]),
 }
 
 KERNEL_CLASSES = ["weights", "assemble", "factor", "local", "rhs", "residual", "solve_fwd", "solve_bwd", "gather"]

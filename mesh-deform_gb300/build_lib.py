@@ -1,9 +1,10 @@
 """Builds libarap_gb300.so (the C ABI of include/arap_gpu.h) for sm_103a.
 
-Three translation units compiled in parallel, then linked with the static CUDA
+Four translation units compiled in parallel, then linked with the static CUDA
 runtime:
   csrc/arap_kernels.cu   the sm_103a kernels (nvcc)
   csrc/arap_context.cu   context state and the C ABI (nvcc)
+  csrc/arap_noalloc.cu   cotan weights with static scratch (nvcc)
   csrc/arap_symbolic.cpp host symbolic analysis (g++)
 The library is built in-tree (next to this file) and is git-ignored.
 """
@@ -30,6 +31,7 @@ GXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", f"-I{ROOT / 'include'}"]
 SOURCES = [
     ("nvcc", CSRC / "arap_kernels.cu"),
     ("nvcc", CSRC / "arap_context.cu"),
+    ("nvcc", CSRC / "arap_noalloc.cu"),
     ("g++", CSRC / "arap_symbolic.cpp"),
 ]
 HEADERS = [CSRC / "arap_kernels.h", CSRC / "arap_symbolic.h", ROOT / "include" / "arap_gpu.h"]

@@ -45,7 +45,10 @@ thread_local std::string g_create_error;
 
 }  // namespace
 
-
+namespace arapgpu {
+// Message returned by arap_last_error(NULL) for context-free entry points.
+void set_global_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace arapgpu
 
 struct arap_ctx {
     int device = 0;
