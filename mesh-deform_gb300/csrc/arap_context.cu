@@ -67,7 +67,7 @@ struct arap_ctx {
     // symbolic cache (keyed by the constrained-vertex mask)
     bool sym_valid = false;
     Symbolic sym;
-    int smem_rows = 0;
+    size_t smem_f32 = 0, smem_f64 = 0;  // dynamic shared memory the solve kernels are configured for
     // which precision the iteration state was set up for
     int state_prec = -1;
     bool have_rotations = false;
@@ -75,7 +75,7 @@ struct arap_ctx {
     DevBuf faces, ent_ptr, ent_fc, hc, w_orig;
     DevBuf rest, targets, out;
     DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn;
-    DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd;
+    DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21;
     DevBuf errw, ticket, flags;
     DevTopo dt{};
     DevSym ds{};
@@ -180,19 +180,23 @@ int prepare_symbolic(arap_ctx *ctx) {
     CK(ctx->flags.ensure(2 * sizeof(unsigned) * (size_t)std::max(s.S, 1)));
     CK(cudaMemsetAsync(ctx->ticket.p, 0, 2 * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
-    const int rows_needed = std::max(s.max_nrow, 1);
-    if ((size_t)rows_needed * sizeof(Vec4<double>) > 200 * 1024)
+    const size_t b32 = solve_smem_bytes(s.max_ldx, s.max_ld21, 4), b64 = solve_smem_bytes(s.max_ldx, s.max_ld21, 8);
+    if (b64 > 227 * 1024)
         return fail(ctx, ARAP_ERR_UNSUPPORTED,
-                    "supernode front of " + std::to_string(s.max_nrow) + " rows exceeds the solve kernel limit");
-    if (rows_needed > ctx->smem_rows) {
-        CK(configure_solve_smem((int)(rows_needed * sizeof(Vec4<float>)), (int)(rows_needed * sizeof(Vec4<double>))));
-        ctx->smem_rows = rows_needed;
+                    "supernode of " + std::to_string(s.max_ncol) + " columns and " +
+                        std::to_string(s.max_ld21) + " struct rows exceeds the solve kernel's shared memory");
+    if (b32 > ctx->smem_f32 || b64 > ctx->smem_f64) {
+        CK(configure_solve_smem((int)b32, (int)b64));
+        ctx->smem_f32 = b32;
+        ctx->smem_f64 = b64;
     }
     DevSym &d = ctx->ds;
     d.V = s.V;
     d.m = s.m;
     d.S = s.S;
     d.nnz = (int)s.dcol.size();
+    d.max_ldx = s.max_ldx;
+    d.max_ld21 = s.max_ld21;
     d.drow = ctx->drow.as<int32_t>();
     d.dcol = ctx->dcol.as<int32_t>();
     d.dent = ctx->dent.as<int32_t>();
@@ -238,6 +242,8 @@ int setup_numeric(arap_ctx *ctx) {
     CK(ctx->Lval.ensure((size_t)std::max<int64_t>(s.panel_size, 1) * sizeof(T)));
     CK(ctx->Dinv.ensure((size_t)std::max<int64_t>(s.dinv_size, 1) * sizeof(T)));
     CK(ctx->Upd.ensure((size_t)std::max<int64_t>(s.upd_size, 1) * sizeof(T)));
+    CK(ctx->Xinv.ensure((size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T)));
+    CK(ctx->L21.ensure((size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T)));
     CK(ctx->errw.ensure(sizeof(int)));
     CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
 
@@ -259,6 +265,8 @@ int setup_numeric(arap_ctx *ctx) {
     if (m > 0) {
         CK(cudaMemsetAsync(ctx->Lval.p, 0, (size_t)s.panel_size * sizeof(T), st));
         if (s.upd_size > 0) CK(cudaMemsetAsync(ctx->Upd.p, 0, (size_t)s.upd_size * sizeof(T), st));
+        CK(cudaMemsetAsync(ctx->Xinv.p, 0, (size_t)s.x_size * sizeof(T), st));
+        if (s.l21_size > 0) CK(cudaMemsetAsync(ctx->L21.p, 0, (size_t)s.l21_size * sizeof(T), st));
         {
             Prof pr(ctx, ARAP_K_ASSEMBLE);
             launch_assemble<T, T>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->Lval.as<T>(),
@@ -269,7 +277,8 @@ int setup_numeric(arap_ctx *ctx) {
         for (int l = 0; l < nlev; ++l) {
             Prof pr(ctx, ARAP_K_FACTOR);
             launch_factor_level<T>(d, s.level_ptr[l], s.level_ptr[l + 1] - s.level_ptr[l], ctx->Lval.as<T>(),
-                                   ctx->Upd.as<T>(), ctx->Dinv.as<T>(), ctx->errw.as<int>(), st);
+                                   ctx->Upd.as<T>(), ctx->Dinv.as<T>(), ctx->Xinv.as<T>(), ctx->L21.as<T>(),
+                                   ctx->errw.as<int>(), st);
             ctx->launches += 1;
         }
     }
@@ -308,15 +317,15 @@ int run_iterations<double>(arap_ctx *ctx, int iterations) {
         }
         {
             Prof pr(ctx, ARAP_K_SOLVE_FWD);
-            launch_solve_fwd<double>(d, ctx->Lval.as<double>(), ctx->Dinv.as<double>(),
+            launch_solve_fwd<double>(d, ctx->Xinv.as<double>(), ctx->L21.as<double>(),
                                      ctx->sol.as<Vec4<double>>(), ctx->uvec.as<Vec4<double>>(), tk, fl,
-                                     ctx->errw.as<int>(), ctx->smem_rows, st);
+                                     ctx->errw.as<int>(), st);
         }
         {
             Prof pr(ctx, ARAP_K_SOLVE_BWD);
-            launch_solve_bwd<double>(d, ctx->Lval.as<double>(), ctx->Dinv.as<double>(),
+            launch_solve_bwd<double>(d, ctx->Xinv.as<double>(), ctx->L21.as<double>(),
                                      ctx->sol.as<Vec4<double>>(), ctx->pc64.as<Vec4<double>>(), nullptr, 0, tk + 1,
-                                     fl + s.S, ctx->errw.as<int>(), ctx->smem_rows, st);
+                                     fl + s.S, ctx->errw.as<int>(), st);
         }
         ctx->launches += 3;
     }
@@ -353,16 +362,15 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_FWD);
-                launch_solve_fwd<float>(d, ctx->Lval.as<float>(), ctx->Dinv.as<float>(),
+                launch_solve_fwd<float>(d, ctx->Xinv.as<float>(), ctx->L21.as<float>(),
                                         ctx->sol.as<Vec4<float>>(), ctx->uvec.as<Vec4<float>>(), tk, fl,
-                                        ctx->errw.as<int>(), ctx->smem_rows, st);
+                                        ctx->errw.as<int>(), st);
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_BWD);
-                launch_solve_bwd<float>(d, ctx->Lval.as<float>(), ctx->Dinv.as<float>(),
+                launch_solve_bwd<float>(d, ctx->Xinv.as<float>(), ctx->L21.as<float>(),
                                         ctx->sol.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(),
-                                        ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(),
-                                        ctx->smem_rows, st);
+                                        ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(), st);
             }
             ctx->launches += 3;
         }
@@ -468,7 +476,7 @@ void arap_destroy(arap_ctx *ctx) {
                       &ctx->amap, &ctx->dmap, &ctx->sn, &ctx->rows, &ctx->relind, &ctx->child,
                       &ctx->level_sn, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
                       &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
-                      &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->errw, &ctx->ticket,
+                      &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->errw, &ctx->ticket,
                       &ctx->flags};
     for (DevBuf *b : bufs) b->release();
     for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
@@ -754,13 +762,11 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
     const double V = s.V, m = s.m, nnz = (double)s.dcol.size(), F = ctx->topo.F;
     // panel entries below the diagonal blocks and lower-triangular entries of the
     // inverted diagonal blocks, read once per solve sweep
-    double below = 0.0, dlow = 0.0, nbsum = 0.0;
+    // per solve sweep: the lower triangle of X = inv(L11) and L21, once each
+    double xlow = 0.0, l21 = 0.0, nbsum = 0.0;
     for (const SnInfo &d : s.sn) {
-        for (int b0 = 0; b0 < d.ncol; b0 += kDiagBlock) {
-            const double w = std::min(kDiagBlock, d.ncol - b0);
-            below += (d.nrow - b0 - w) * w;
-            dlow += w * (w + 1) / 2;
-        }
+        xlow += (double)d.ncol * (d.ncol + 1) / 2;
+        l21 += (double)(d.nrow - d.ncol) * d.ncol;
         nbsum += d.nrow - d.ncol;
     }
     double B = 0.0, FL = 0.0;
@@ -770,11 +776,12 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
         FL = F * 40;
         break;
     case ARAP_K_ASSEMBLE:
-        B = V * (24 + 24 + 3 * sz * 2 + 9 * sz) + m * (8 + 3 * sz) + nnz * (4 + 8 + 8) + (below + dlow) * 0;
+        B = V * (24 + 24 + 3 * sz * 2 + 9 * sz) + m * (8 + 3 * sz) + nnz * (4 + 8 + 8);
         FL = nnz * 4;
         break;
     case ARAP_K_FACTOR:
-        B = (double)s.panel_size * sz * 2 + (double)s.upd_size * sz * 2 + (double)s.dinv_size * sz;
+        B = (double)s.panel_size * sz * 2 + (double)s.upd_size * sz * 2 + (double)s.dinv_size * sz +
+            (xlow + l21) * sz;
         FL = s.factor_flops;
         break;
     case ARAP_K_LOCAL:  // rest + current positions, rotations out, adjacency + weights
@@ -791,9 +798,9 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
         break;
     case ARAP_K_SOLVE_FWD:
     case ARAP_K_SOLVE_BWD:
-        B = (below + dlow) * sz + m * 3 * sz * 2 + nbsum * 3 * sz * 2;
+        B = (xlow + l21) * sz + m * 3 * sz * 2 + nbsum * 3 * sz * 2;
         if (kernel_class == ARAP_K_SOLVE_BWD && ctx->state_prec != ARAP_PRECISION_FP64) B += m * (24 * 2 + 12);
-        FL = (below + dlow) * 6;
+        FL = (xlow + l21) * 6;
         break;
     case ARAP_K_GATHER:
         B = V * (24 + 24 + 4);

@@ -182,14 +182,31 @@ __global__ void k_assemble(int m, const int32_t *__restrict__ drow, const int32_
 constexpr int kFactorThreads = 256;
 constexpr int kTile = 64;
 
+// Front of supernode d: the nrow x ncol panel P (column-major, ld nrow; rows are
+// the supernode's columns then its struct rows) and the nb x nb update matrix U.
+// Element (row i, column k) of the front, k <= i.
+template <typename TF>
+__device__ __forceinline__ TF &front(TF *P, TF *U, int n, int nc, int nb, int i, int k) {
+    return k < nc ? P[(int64_t)k * n + i] : U[(int64_t)(k - nc) * nb + (i - nc)];
+}
+
+// Per level, one CTA per supernode: extend-add of the children's update
+// matrices, blocked right-looking partial Cholesky of the front (32-column
+// blocks: diagonal block factored and inverted in shared memory, rows below
+// solved against it, trailing update in 64x64 tiles), then the two arrays the
+// solves read: X = inverse of L11 (lower, ldx rows) and L21 (ld21 rows).
 template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
 k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
                const int32_t *__restrict__ relind, TF *__restrict__ Lval, TF *__restrict__ Upd,
-               TF *__restrict__ Dinv, int *err) {
-    __shared__ TF As[NB][kTile];
-    __shared__ TF Bs[NB][kTile];
+               TF *__restrict__ Dinv, TF *__restrict__ Xall, TF *__restrict__ L21all, int *err) {
+    // one buffer, carved differently by the phases (separated by barriers)
+    __shared__ __align__(16) TF sm[2 * NB * kTile];
     __shared__ TF s_inv;
+    TF(*As)[kTile] = reinterpret_cast<TF(*)[kTile]>(sm);
+    TF(*Bs)[kTile] = reinterpret_cast<TF(*)[kTile]>(sm + NB * kTile);
+    TF(*Db)[NB + 1] = reinterpret_cast<TF(*)[NB + 1]>(sm);                   // diagonal block, row-major
+    TF(*Di)[NB + 1] = reinterpret_cast<TF(*)[NB + 1]>(sm + NB * (NB + 1));  // its inverse, row-major
     const int tid = threadIdx.x;
     const SnInfo d = sn[level_sn[blockIdx.x]];
     const int n = d.nrow, nc = d.ncol, nb = n - nc;
@@ -206,60 +223,71 @@ k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ 
         for (int64_t t = tid; t < total; t += kFactorThreads) {
             const int k = (int)(t / nbc), i = (int)(t - (int64_t)k * nbc);
             if (i < k) continue;
-            const int pi = ri[i], pk = ri[k];
-            const TF v = Uc[t];
-            if (pk < nc) P[(int64_t)pk * n + pi] += v;
-            else U[(int64_t)(pk - nc) * nb + (pi - nc)] += v;
+            front(P, U, n, nc, nb, ri[i], ri[k]) += Uc[t];
         }
         __syncthreads();
     }
 
-    // blocked right-looking partial Cholesky of the front [P | U]
     for (int j0 = 0; j0 < nc; j0 += NB) {
         const int w = min(NB, nc - j0);
-        // (a) panel columns j0..j0+w-1, rows j0..n-1
-        for (int jj = 0; jj < w; ++jj) {
-            const int j = j0 + jj;
-            TF *Pj = P + (int64_t)j * n;
+        // (a1) diagonal block: load, factor and invert in shared memory
+        for (int q = tid; q < NB * NB; q += kFactorThreads) {
+            const int r = q % NB, c = q / NB;
+            Db[r][c] = (r < w && c < w && c <= r) ? P[(int64_t)(j0 + c) * n + j0 + r] : (TF)0;
+        }
+        __syncthreads();
+        for (int k = 0; k < w; ++k) {
             if (tid == 0) {
-                TF dj = Pj[j];
-                if (!(dj > (TF)0)) { atomicOr(err, kErrNotSpd); dj = (TF)1; }
-                dj = tsqrt(dj);
-                Pj[j] = dj;
-                s_inv = (TF)1 / dj;
+                TF dk = Db[k][k];
+                if (!(dk > (TF)0)) { atomicOr(err, kErrNotSpd); dk = (TF)1; }
+                dk = tsqrt(dk);
+                Db[k][k] = dk;
+                s_inv = (TF)1 / dk;
             }
             __syncthreads();
-            const TF inv = s_inv;
-            for (int i = j + 1 + tid; i < n; i += kFactorThreads) Pj[i] *= inv;
+            if (tid > k && tid < w) Db[tid][k] *= s_inv;
             __syncthreads();
-            const int ncols = j0 + w - j - 1, nr = n - j - 1;
-            for (int t = tid; t < ncols * nr; t += kFactorThreads) {
-                const int kk = t / nr, i = j + 1 + (t - kk * nr);
-                const int k = j + 1 + kk;
-                if (i >= k) P[(int64_t)k * n + i] -= Pj[i] * Pj[k];
+            const int m = w - k - 1;
+            for (int q = tid; q < m * m; q += kFactorThreads) {
+                const int r = k + 1 + q / m, c = k + 1 + q % m;
+                if (c <= r) Db[r][c] -= Db[r][k] * Db[c][k];
             }
             __syncthreads();
         }
-        // (b) inverse of the w x w diagonal block (column c by thread c)
-        if (tid < NB) {
+        if (tid < NB) {  // inverse of the lower-triangular block, column tid
             const int c = tid;
-            TF x[NB];
-#pragma unroll
             for (int i = 0; i < NB; ++i) {
                 TF v = (TF)0;
                 if (i >= c && i < w) {
-                    TF s = (i == c) ? (TF)1 : (TF)0;
-#pragma unroll
-                    for (int t = 0; t < NB; ++t)
-                        if (t >= c && t < i) s -= P[(int64_t)(j0 + t) * n + j0 + i] * x[t];
-                    v = s / P[(int64_t)(j0 + i) * n + j0 + i];
+                    TF acc = (i == c) ? (TF)1 : (TF)0;
+                    for (int t = c; t < i; ++t) acc -= Db[i][t] * Di[t][c];
+                    v = acc / Db[i][i];
                 }
-                x[i] = v;
+                Di[i][c] = v;
             }
-            TF *D = Dinv + d.dinv_off + (int64_t)(j0 / NB) * NB * NB + (int64_t)c * NB;
-#pragma unroll
-            for (int i = 0; i < NB; ++i) D[i] = x[i];
         }
+        __syncthreads();
+        for (int q = tid; q < NB * NB; q += kFactorThreads) {
+            const int r = q % NB, c = q / NB;
+            if (r < w && c < w && c <= r) P[(int64_t)(j0 + c) * n + j0 + r] = Db[r][c];
+            Dinv[d.dinv_off + (int64_t)(j0 / NB) * NB * NB + (int64_t)c * NB + r] = Di[r][c];
+        }
+        // (a2) rows below the block: L_ib = A_ib * inv(L_bb)^T, one row per thread
+        for (int i = j0 + w + tid; i < n; i += kFactorThreads) {
+            TF a[NB];
+#pragma unroll
+            for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i] : (TF)0;
+#pragma unroll 4
+            for (int r = 0; r < NB; ++r) {
+                if (r >= w) break;
+                TF acc = (TF)0;
+#pragma unroll
+                for (int c = 0; c < NB; ++c)
+                    if (c <= r) acc += a[c] * Di[r][c];
+                P[(int64_t)(j0 + r) * n + i] = acc;
+            }
+        }
+        __syncthreads();
         // (c) trailing update F[i][k] -= sum_t L[i][j0+t] L[k][j0+t], k,i >= j0+w
         const int c0 = j0 + w;
         const int rem = n - c0;
@@ -271,14 +299,14 @@ k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ 
                     const int rb = c0 + ti * kTile, cb = c0 + tk * kTile;
                     for (int q = tid; q < NB * kTile; q += kFactorThreads) {
                         const int t = q / kTile, r = q % kTile;
-                        TF a = (TF)0, b = (TF)0;
+                        TF av = (TF)0, bv = (TF)0;
                         if (t < w) {
                             const TF *col = P + (int64_t)(j0 + t) * n;
-                            if (rb + r < n) a = col[rb + r];
-                            if (cb + r < n) b = col[cb + r];
+                            if (rb + r < n) av = col[rb + r];
+                            if (cb + r < n) bv = col[cb + r];
                         }
-                        As[t][r] = a;
-                        Bs[t][r] = b;
+                        As[t][r] = av;
+                        Bs[t][r] = bv;
                     }
                     __syncthreads();
                     TF acc[4][4];
@@ -303,10 +331,7 @@ k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ 
 #pragma unroll
                         for (int b = 0; b < 4; ++b) {
                             const int colf = cb + tx + 16 * b;
-                            if (row < n && colf < n && row >= colf) {
-                                if (colf < nc) P[(int64_t)colf * n + row] -= acc[a][b];
-                                else U[(int64_t)(colf - nc) * nb + (row - nc)] -= acc[a][b];
-                            }
+                            if (row < n && colf < n && row >= colf) front(P, U, n, nc, nb, row, colf) -= acc[a][b];
                         }
                     }
                     __syncthreads();
@@ -314,6 +339,54 @@ k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ 
             }
         }
         __syncthreads();
+    }
+
+    // X = inverse of L11 by block rows: X_ii = inv(L_ii),
+    // X_ij = -inv(L_ii) * sum_{k=j..i-1} L_ik X_kj
+    TF *X = Xall + d.x_off;
+    const int ldx = d.ldx;
+    const int nblk = (nc + NB - 1) / NB;
+    TF(*Ts)[NB + 1] = reinterpret_cast<TF(*)[NB + 1]>(sm);
+    const int r = tid % NB, cg = tid / NB;  // row in block, group of 4 columns
+    for (int ib = 0; ib < nblk; ++ib) {
+        const int i0 = ib * NB, wi = min(NB, nc - i0);
+        const TF *Dii = Dinv + d.dinv_off + (int64_t)ib * NB * NB;
+        for (int q = tid; q < NB * NB; q += kFactorThreads) {
+            const int rr = q % NB, cc = q / NB;
+            if (rr < wi && cc < wi) X[(int64_t)(i0 + cc) * ldx + i0 + rr] = Dii[(int64_t)cc * NB + rr];
+        }
+        for (int jb = 0; jb < ib; ++jb) {
+            const int j0 = jb * NB;
+            TF acc[4] = {(TF)0, (TF)0, (TF)0, (TF)0};
+            if (r < wi) {
+                for (int k = j0; k < i0; ++k) {
+                    const TF l = P[(int64_t)k * n + i0 + r];
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) acc[cc] += l * X[(int64_t)(j0 + cg * 4 + cc) * ldx + k];
+                }
+            }
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) Ts[cg * 4 + cc][r] = acc[cc];
+            __syncthreads();
+            if (r < wi) {
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) {
+                    const int c = cg * 4 + cc;
+                    TF v = (TF)0;
+                    for (int t = 0; t <= r; ++t) v += Dii[(int64_t)t * NB + r] * Ts[c][t];
+                    X[(int64_t)(j0 + c) * ldx + i0 + r] = -v;
+                }
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+    }
+    // L21 with aligned columns
+    TF *L21 = L21all + d.l21_off;
+    const int ld21 = d.ld21;
+    for (int64_t q = tid; q < (int64_t)nb * nc; q += kFactorThreads) {
+        const int c = (int)(q / nb), i = (int)(q - (int64_t)c * nb);
+        L21[(int64_t)c * ld21 + i] = P[(int64_t)c * n + nc + i];
     }
 }
 
@@ -524,21 +597,141 @@ k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ 
 // supernodal triangular solves
 
 constexpr int kSolveThreads = 256;
+constexpr int kRedRows = 1024;  // reduction scratch (rows x groups) of gemv_cols
 
-// Forward: for supernode s (children first), front f = [b(cols); 0] plus the
-// children's update vectors; y = L11^{-1} f(cols) block by block with the
-// inverted diagonal blocks; u_s = f(struct) - L21 y goes to the parent.
+// Four consecutive elements from a 16-byte aligned address.
+__device__ __forceinline__ void load4(const float *p, float v[4]) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void load4(const double *p, double v[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+// out[r] (-)= sum_{c < C} M[c*ld + r] * v[c] for r < R (M column-major, ld a
+// multiple of 4, columns 16-byte aligned, rows R..ld-1 zero). LOWER: only
+// c <= r contribute (column blocks above the diagonal are skipped). Threads own
+// 4-row quads; when there are fewer quads than threads, G groups of threads
+// split the columns and reduce through `red`. Ends with a barrier.
+template <typename T, bool LOWER, bool SUB>
+__device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R, int C, const Vec4<T> *v,
+                                          Vec4<T> *out, Vec4<T> *red) {
+    const int tid = threadIdx.x;
+    const int NQ = (R + 3) >> 2;
+    int G = NQ > 0 ? kSolveThreads / NQ : 1;
+    G = max(1, min(G, kRedRows / max(4 * NQ, 1)));
+    G = min(G, 8);
+    if (G == 1) {
+        for (int q = tid; q < NQ; q += kSolveThreads) {
+            const int cend = LOWER ? min(C, 4 * q + 4) : C;
+            T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+#pragma unroll 4
+            for (int c = 0; c < cend; ++c) {
+                T m4[4];
+                load4(M + (int64_t)c * ld + 4 * q, m4);
+                const Vec4<T> vc = v[c];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) { ax[k] += m4[k] * vc.x; ay[k] += m4[k] * vc.y; az[k] += m4[k] * vc.z; }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                Vec4<T> &o = out[4 * q + k];
+                if (SUB) { o.x -= ax[k]; o.y -= ay[k]; o.z -= az[k]; }
+                else o = {ax[k], ay[k], az[k], (T)0};
+            }
+        }
+        __syncthreads();
+        return;
+    }
+    const int q = tid % NQ, g = tid / NQ;
+    if (g < G) {
+        const int chunk = (C + G - 1) / G;
+        const int cb = g * chunk;
+        const int ce = min(LOWER ? min(C, 4 * q + 4) : C, cb + chunk);
+        T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+#pragma unroll 4
+        for (int c = cb; c < ce; ++c) {
+            T m4[4];
+            load4(M + (int64_t)c * ld + 4 * q, m4);
+            const Vec4<T> vc = v[c];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { ax[k] += m4[k] * vc.x; ay[k] += m4[k] * vc.y; az[k] += m4[k] * vc.z; }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) red[g * 4 * NQ + 4 * q + k] = {ax[k], ay[k], az[k], (T)0};
+    }
+    __syncthreads();
+    for (int rr = tid; rr < 4 * NQ; rr += kSolveThreads) {
+        T sx = 0, sy = 0, sz = 0;
+        for (int gg = 0; gg < G; ++gg) {
+            const Vec4<T> p = red[gg * 4 * NQ + rr];
+            sx += p.x; sy += p.y; sz += p.z;
+        }
+        Vec4<T> &o = out[rr];
+        if (SUB) { o.x -= sx; o.y -= sy; o.z -= sz; }
+        else o = {sx, sy, sz, (T)0};
+    }
+    __syncthreads();
+}
+
+// out[c] = sum_{r < R} M[c*ld + r] * v[r] for c < C (dot of column c with v);
+// LOWER: rows r >= c only (the quads below the diagonal). v must be zero-padded
+// to a multiple of 4 rows. One warp per column. Ends with a barrier.
+template <typename T, bool LOWER>
+__device__ __forceinline__ void gemv_dots(const T *__restrict__ M, int ld, int R, int C, const Vec4<T> *v,
+                                          Vec4<T> *out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int nwarps = kSolveThreads / 32;
+    const int NQ = (R + 3) >> 2;
+    for (int c = warp; c < C; c += nwarps) {
+        const T *col = M + (int64_t)c * ld;
+        T ax = 0, ay = 0, az = 0;
+        for (int q = (LOWER ? (c >> 2) : 0) + lane; q < NQ; q += 32) {
+            T m4[4];
+            load4(col + 4 * q, m4);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const Vec4<T> x = v[4 * q + k];
+                ax += m4[k] * x.x;
+                ay += m4[k] * x.y;
+                az += m4[k] * x.z;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o);
+            az += __shfl_xor_sync(0xffffffffu, az, o);
+        }
+        if (lane == 0) out[c] = {ax, ay, az, (T)0};
+    }
+    __syncthreads();
+}
+
+// Shared-memory layout of the solve kernels (dynamic): two vectors of max_ldx
+// rows, one of max_ld21 rows and the kRedRows reduction scratch.
+struct SolveSmem {
+    int ldx_max, ld21_max;
+};
+
+// Forward: for supernode s (children first), f = [b(cols); 0] plus the
+// children's update vectors; y = X f(cols); u_s = f(struct) - L21 y goes to
+// the parent.
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads)
-k_solve_fwd(int S, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
-            const int32_t *__restrict__ relind, const T *__restrict__ Lval, const T *__restrict__ Dinv,
+k_solve_fwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
+            const int32_t *__restrict__ relind, const T *__restrict__ Xall, const T *__restrict__ L21all,
             Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec, unsigned long long *ticket, unsigned *flags,
             int *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Vec4<T> *f = reinterpret_cast<Vec4<T> *>(smem_raw);
+    Vec4<T> *fc = reinterpret_cast<Vec4<T> *>(smem_raw);
+    Vec4<T> *yv = fc + lay.ldx_max;
+    Vec4<T> *fb = yv + lay.ldx_max;
+    Vec4<T> *red = fb + lay.ld21_max;
     __shared__ int s_task;
     __shared__ unsigned s_epoch;
-    __shared__ Vec4<T> yblk[NB];
     const int tid = threadIdx.x;
     if (tid == 0) {
         const unsigned long long t = atomicAdd(ticket, 1ull);
@@ -549,14 +742,23 @@ k_solve_fwd(int S, const SnInfo *__restrict__ sn, const int32_t *__restrict__ ch
     const int s = s_task;
     const unsigned epoch = s_epoch;
     const SnInfo d = sn[s];
-    const int n = d.nrow, nc = d.ncol;
+    const int nc = d.ncol, nb = d.nrow - d.ncol;
+    // warm L2/L1 with this supernode's matrices while the children finish
+    {
+        const T *X = Xall + d.x_off;
+        const T *L = L21all + d.l21_off;
+        const int64_t nx = (int64_t)d.ldx * nc, nl = (int64_t)d.ld21 * nc;
+        for (int64_t q = (int64_t)tid * 32; q < nx; q += (int64_t)kSolveThreads * 32)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(X + q));
+        for (int64_t q = (int64_t)tid * 32; q < nl; q += (int64_t)kSolveThreads * 32)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(L + q));
+    }
     if (tid == 0)
         for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
     __syncthreads();
-    for (int i = tid; i < n; i += kSolveThreads) {
-        if (i < nc) f[i] = sol[d.first + i];
-        else f[i] = {(T)0, (T)0, (T)0, (T)0};
-    }
+    for (int i = tid; i < d.ldx; i += kSolveThreads)
+        fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+    for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
     __syncthreads();
     for (int ci = d.child_begin; ci < d.child_end; ++ci) {
         const SnInfo c = sn[child[ci]];
@@ -564,69 +766,38 @@ k_solve_fwd(int S, const SnInfo *__restrict__ sn, const int32_t *__restrict__ ch
         const int32_t *ri = relind + c.relind_off;
         for (int i = tid; i < nbc; i += kSolveThreads) {
             const Vec4<T> u = ldcg4(uvec + c.uvec_off + i);
-            Vec4<T> &t = f[ri[i]];
+            const int pos = ri[i];
+            Vec4<T> &t = pos < nc ? fc[pos] : fb[pos - nc];
             t.x += u.x;
             t.y += u.y;
             t.z += u.z;
         }
         __syncthreads();
     }
-    const T *P = Lval + d.panel_off;
-    for (int b0 = 0; b0 < nc; b0 += NB) {
-        const int w = min(NB, nc - b0);
-        if (tid < w) {
-            const T *D = Dinv + d.dinv_off + (int64_t)(b0 / NB) * NB * NB;
-            T yx = 0, yy = 0, yz = 0;
-            for (int c = 0; c <= tid; ++c) {
-                const T dv = D[c * NB + tid];
-                const Vec4<T> fc = f[b0 + c];
-                yx += dv * fc.x;
-                yy += dv * fc.y;
-                yz += dv * fc.z;
-            }
-            yblk[tid] = {yx, yy, yz, (T)0};
-        }
-        __syncthreads();
-        if (tid < w) f[b0 + tid] = yblk[tid];
-        for (int i = b0 + w + tid; i < n; i += kSolveThreads) {
-            T ax = 0, ay = 0, az = 0;
-            for (int c = 0; c < w; ++c) {
-                const T l = P[(int64_t)(b0 + c) * n + i];
-                const Vec4<T> y = yblk[c];
-                ax += l * y.x;
-                ay += l * y.y;
-                az += l * y.z;
-            }
-            Vec4<T> &t = f[i];
-            t.x -= ax;
-            t.y -= ay;
-            t.z -= az;
-        }
-        __syncthreads();
-    }
-    for (int i = tid; i < n; i += kSolveThreads) {
-        if (i < nc) sol[d.first + i] = f[i];
-        else uvec[d.uvec_off + (i - nc)] = f[i];
-    }
+    gemv_cols<T, true, false>(Xall + d.x_off, d.ldx, nc, nc, fc, yv, red);
+    if (nb > 0) gemv_cols<T, false, true>(L21all + d.l21_off, d.ld21, nb, nc, yv, fb, red);
+    for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
+    for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
     __threadfence();
     __syncthreads();
     if (tid == 0) st_release(flags + s, epoch);
 }
 
-// Backward: for supernode s (root first), g = [y(cols); x(struct)]; block by
-// block from the last, z = g_b - L(rows below, b)^T g(rows below), x_b = Dinv_b^T z.
+// Backward: for supernode s (root first), z = y - L21^T x(struct) and
+// x(cols) = X^T z. mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k, pc32[k] = float(pc64[k]).
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads)
-k_solve_bwd(int S, const SnInfo *__restrict__ sn, const int32_t *__restrict__ rows, const T *__restrict__ Lval,
-            const T *__restrict__ Dinv, Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64,
-            Vec4<float> *__restrict__ pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err) {
+k_solve_bwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *__restrict__ rows,
+            const T *__restrict__ Xall, const T *__restrict__ L21all, Vec4<T> *__restrict__ sol,
+            Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode, unsigned long long *ticket,
+            unsigned *flags, int *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Vec4<T> *g = reinterpret_cast<Vec4<T> *>(smem_raw);
+    Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw);
+    Vec4<T> *xv = zv + lay.ldx_max;
+    Vec4<T> *gb = xv + lay.ldx_max;
     __shared__ int s_task;
     __shared__ unsigned s_epoch;
-    __shared__ Vec4<T> zblk[NB];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int nwarps = kSolveThreads / 32;
+    const int tid = threadIdx.x;
     if (tid == 0) {
         const unsigned long long t = atomicAdd(ticket, 1ull);
         s_task = S - 1 - (int)(t % (unsigned long long)S);
@@ -636,59 +807,40 @@ k_solve_bwd(int S, const SnInfo *__restrict__ sn, const int32_t *__restrict__ ro
     const int s = s_task;
     const unsigned epoch = s_epoch;
     const SnInfo d = sn[s];
-    const int n = d.nrow, nc = d.ncol;
+    const int nc = d.ncol, nb = d.nrow - d.ncol;
+    {
+        const T *X = Xall + d.x_off;
+        const T *L = L21all + d.l21_off;
+        const int64_t nx = (int64_t)d.ldx * nc, nl = (int64_t)d.ld21 * nc;
+        for (int64_t q = (int64_t)tid * 32; q < nx; q += (int64_t)kSolveThreads * 32)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(X + q));
+        for (int64_t q = (int64_t)tid * 32; q < nl; q += (int64_t)kSolveThreads * 32)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(L + q));
+    }
     if (tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
     __syncthreads();
     const int32_t *rs = rows + d.rows_off;
-    for (int i = tid; i < n; i += kSolveThreads) {
-        if (i < nc) g[i] = sol[d.first + i];
-        else g[i] = ldcg4(sol + rs[i - nc]);
+    for (int i = tid; i < d.ld21; i += kSolveThreads)
+        gb[i] = (i < nb) ? ldcg4(sol + rs[i]) : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+    __syncthreads();
+    if (nb > 0) {
+        gemv_dots<T, false>(L21all + d.l21_off, d.ld21, nb, nc, gb, xv);  // xv = L21^T g
+        for (int i = tid; i < d.ldx; i += kSolveThreads) {
+            if (i < nc) {
+                const Vec4<T> y = sol[d.first + i], a = xv[i];
+                zv[i] = {y.x - a.x, y.y - a.y, y.z - a.z, (T)0};
+            } else {
+                zv[i] = {(T)0, (T)0, (T)0, (T)0};
+            }
+        }
+    } else {
+        for (int i = tid; i < d.ldx; i += kSolveThreads)
+            zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
     }
     __syncthreads();
-    const T *P = Lval + d.panel_off;
-    const int nblk = (nc + NB - 1) / NB;
-    for (int bi = nblk - 1; bi >= 0; --bi) {
-        const int b0 = bi * NB;
-        const int w = min(NB, nc - b0);
-        for (int r = warp; r < w; r += nwarps) {
-            const T *col = P + (int64_t)(b0 + r) * n;
-            T ax = 0, ay = 0, az = 0;
-            for (int i = b0 + w + lane; i < n; i += 32) {
-                const T l = col[i];
-                const Vec4<T> x = g[i];
-                ax += l * x.x;
-                ay += l * x.y;
-                az += l * x.z;
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                ax += __shfl_xor_sync(0xffffffffu, ax, o);
-                ay += __shfl_xor_sync(0xffffffffu, ay, o);
-                az += __shfl_xor_sync(0xffffffffu, az, o);
-            }
-            if (lane == 0) {
-                const Vec4<T> gv = g[b0 + r];
-                zblk[r] = {gv.x - ax, gv.y - ay, gv.z - az, (T)0};
-            }
-        }
-        __syncthreads();
-        Vec4<T> xr = {(T)0, (T)0, (T)0, (T)0};
-        if (tid < w) {
-            const T *D = Dinv + d.dinv_off + (int64_t)bi * NB * NB + (int64_t)tid * NB;
-            for (int c = tid; c < w; ++c) {
-                const T dv = D[c];
-                const Vec4<T> z = zblk[c];
-                xr.x += dv * z.x;
-                xr.y += dv * z.y;
-                xr.z += dv * z.z;
-            }
-        }
-        __syncthreads();
-        if (tid < w) g[b0 + tid] = xr;
-        __syncthreads();
-    }
+    gemv_dots<T, true>(Xall + d.x_off, d.ldx, nc, nc, zv, xv);  // xv = X^T z
     for (int i = tid; i < nc; i += kSolveThreads) {
-        const Vec4<T> x = g[i];
+        const Vec4<T> x = xv[i];
         const int k = d.first + i;
         sol[k] = x;
         if (mode == 0) {
@@ -775,11 +927,11 @@ void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc6
 }
 
 template <typename TF>
-void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv,
-                         int *err, cudaStream_t st) {
+void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv, TF *X,
+                         TF *L21, int *err, cudaStream_t st) {
     if (level_count == 0) return;
     k_factor_level<TF><<<level_count, kFactorThreads, 0, st>>>(s.level_sn + level_begin, s.sn, s.child, s.relind,
-                                                               Lval, Upd, Dinv, err);
+                                                               Lval, Upd, Dinv, X, L21, err);
 }
 
 template <typename T>
@@ -802,22 +954,28 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
     k_residual<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, b, x64, r);
 }
 
+size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
+    return (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
+}
+
 template <typename T>
-void launch_solve_fwd(const DevSym &s, const T *Lval, const T *Dinv, Vec4<T> *sol, Vec4<T> *uvec,
-                      unsigned long long *ticket, unsigned *flags, int *err, int smem_rows, cudaStream_t st) {
+void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
+                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st) {
     if (s.S == 0) return;
-    const size_t smem = (size_t)smem_rows * sizeof(Vec4<T>);
-    k_solve_fwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, s.sn, s.child, s.relind, Lval, Dinv, sol, uvec, ticket,
+    const SolveSmem lay{s.max_ldx, s.max_ld21};
+    const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
+    k_solve_fwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.sn, s.child, s.relind, X, L21, sol, uvec, ticket,
                                                      flags, err);
 }
 
 template <typename T>
-void launch_solve_bwd(const DevSym &s, const T *Lval, const T *Dinv, Vec4<T> *sol, Vec4<double> *pc64,
+void launch_solve_bwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
-                      int smem_rows, cudaStream_t st) {
+                      cudaStream_t st) {
     if (s.S == 0) return;
-    const size_t smem = (size_t)smem_rows * sizeof(Vec4<T>);
-    k_solve_bwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, s.sn, s.rows, Lval, Dinv, sol, pc64, pc32, mode, ticket,
+    const SolveSmem lay{s.max_ldx, s.max_ld21};
+    const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
+    k_solve_bwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.sn, s.rows, X, L21, sol, pc64, pc32, mode, ticket,
                                                      flags, err);
 }
 
@@ -832,7 +990,7 @@ void launch_gather_rotations(const DevSym &s, const Vec4<T> *R, double *out9, cu
     k_gather_rotations<T><<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.oldidx, R, out9);
 }
 
-// Raises the dynamic shared-memory limit of the solve kernels.
+// Raises the dynamic shared-memory limit of the solve kernels (bytes per CTA).
 cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64) {
     cudaError_t e = cudaFuncSetAttribute(k_solve_fwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f32);
     if (e != cudaSuccess) return e;
@@ -854,9 +1012,10 @@ template void launch_assemble<float, float>(const DevSym &, const double *, cons
                                             Vec4<float> *, cudaStream_t);
 template void launch_assemble<double, double>(const DevSym &, const double *, const Vec4<double> *, double *,
                                               double *, Vec4<double> *, cudaStream_t);
-template void launch_factor_level<float>(const DevSym &, int, int, float *, float *, float *, int *, cudaStream_t);
-template void launch_factor_level<double>(const DevSym &, int, int, double *, double *, double *, int *,
-                                          cudaStream_t);
+template void launch_factor_level<float>(const DevSym &, int, int, float *, float *, float *, float *, float *,
+                                         int *, cudaStream_t);
+template void launch_factor_level<double>(const DevSym &, int, int, double *, double *, double *, double *,
+                                          double *, int *, cudaStream_t);
 template void launch_local_step<float>(const DevSym &, const float *, const Vec4<float> *, const Vec4<float> *,
                                        Vec4<float> *, cudaStream_t);
 template void launch_local_step<double>(const DevSym &, const double *, const Vec4<double> *, const Vec4<double> *,
@@ -866,15 +1025,14 @@ template void launch_rhs<float>(const DevSym &, const float *, const Vec4<float>
 template void launch_rhs<double>(const DevSym &, const double *, const Vec4<double> *, const Vec4<double> *,
                                  const Vec4<double> *, Vec4<double> *, cudaStream_t);
 template void launch_solve_fwd<float>(const DevSym &, const float *, const float *, Vec4<float> *, Vec4<float> *,
-                                      unsigned long long *, unsigned *, int *, int, cudaStream_t);
+                                      unsigned long long *, unsigned *, int *, cudaStream_t);
 template void launch_solve_fwd<double>(const DevSym &, const double *, const double *, Vec4<double> *,
-                                       Vec4<double> *, unsigned long long *, unsigned *, int *, int, cudaStream_t);
+                                       Vec4<double> *, unsigned long long *, unsigned *, int *, cudaStream_t);
 template void launch_solve_bwd<float>(const DevSym &, const float *, const float *, Vec4<float> *, Vec4<double> *,
-                                      Vec4<float> *, int, unsigned long long *, unsigned *, int *, int,
-                                      cudaStream_t);
+                                      Vec4<float> *, int, unsigned long long *, unsigned *, int *, cudaStream_t);
 template void launch_solve_bwd<double>(const DevSym &, const double *, const double *, Vec4<double> *,
                                        Vec4<double> *, Vec4<float> *, int, unsigned long long *, unsigned *, int *,
-                                       int, cudaStream_t);
+                                       cudaStream_t);
 template void launch_gather_rotations<float>(const DevSym &, const Vec4<float> *, double *, cudaStream_t);
 template void launch_gather_rotations<double>(const DevSym &, const Vec4<double> *, double *, cudaStream_t);
 

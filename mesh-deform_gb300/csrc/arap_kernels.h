@@ -35,6 +35,7 @@ struct DevTopo {
 
 struct DevSym {
     int V, m, S, nnz;
+    int max_ldx, max_ld21;
     const int32_t *drow, *dcol, *dent, *oldidx;
     const int64_t *amap, *dmap;
     const SnInfo *sn;
@@ -59,10 +60,11 @@ void launch_setup_vertices(const DevSym &s, const double *rest_xyz, const double
 template <typename TF, typename T>
 void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc64, TF *Lval, double *diag64,
                      Vec4<T> *bfixed, cudaStream_t st);
-// multifrontal Cholesky of one level of the supernodal tree
+// multifrontal Cholesky of one level of the supernodal tree; also writes
+// X = inverse of L11 and the aligned L21 copy the solves read
 template <typename TF>
-void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv,
-                         int *err, cudaStream_t st);
+void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv, TF *X,
+                         TF *L21, int *err, cudaStream_t st);
 // local step: covariance + rotation fit (estimateRotations arap.h:354-384)
 template <typename T>
 void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *pc, Vec4<T> *R,
@@ -77,13 +79,14 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 // supernodal triangular solves L y = b (forward) and L^T x = y (backward),
 // one launch each, supernodes scheduled by a ticket counter with bounded waits.
 // mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k and pc32[k] = float(pc64[k]).
+size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
 template <typename T>
-void launch_solve_fwd(const DevSym &s, const T *Lval, const T *Dinv, Vec4<T> *sol, Vec4<T> *uvec,
-                      unsigned long long *ticket, unsigned *flags, int *err, int smem_rows, cudaStream_t st);
+void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
+                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st);
 template <typename T>
-void launch_solve_bwd(const DevSym &s, const T *Lval, const T *Dinv, Vec4<T> *sol, Vec4<double> *pc64,
+void launch_solve_bwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
-                      int smem_rows, cudaStream_t st);
+                      cudaStream_t st);
 // deformed positions back to the original vertex order as doubles (arap.h:133-135)
 void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st);
 template <typename T>

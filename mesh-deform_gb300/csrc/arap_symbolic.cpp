@@ -355,7 +355,7 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     }
     // levels, offsets, struct rows, children, relative indices
     int maxlev = 0;
-    int64_t poff = 0, doff = 0, uoff = 0, voff = 0;
+    int64_t poff = 0, doff = 0, uoff = 0, voff = 0, xoff = 0, loff = 0;
     double flops = 0.0;
     for (int s = 0; s < S; ++s) {
         SnInfo &d = sym.sn[s];
@@ -372,6 +372,16 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         uoff += (int64_t)nb * nb;
         d.uvec_off = voff;
         voff += nb;
+        // solve-time copies with 16-byte aligned columns (offsets and leading
+        // dimensions are multiples of 4 elements)
+        d.ldx = (d.ncol + 3) & ~3;
+        d.ld21 = (nb + 3) & ~3;
+        d.x_off = xoff;
+        xoff += (int64_t)d.ldx * d.ncol;
+        d.l21_off = loff;
+        loff += (int64_t)d.ld21 * d.ncol;
+        sym.max_ldx = std::max(sym.max_ldx, (int)d.ldx);
+        sym.max_ld21 = std::max(sym.max_ld21, (int)d.ld21);
         d.rows_off = (int32_t)sym.rows.size();
         sym.rows.insert(sym.rows.end(), strct[s].begin(), strct[s].end());
         d.child_begin = (int32_t)sym.child.size();
@@ -388,6 +398,8 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     sym.dinv_size = doff;
     sym.upd_size = uoff;
     sym.uvec_size = voff;
+    sym.x_size = xoff;
+    sym.l21_size = loff;
     // relind: where each struct row of s sits in its parent's front
     for (int s = 0; s < S; ++s) {
         SnInfo &d = sym.sn[s];

@@ -53,6 +53,10 @@ struct SnInfo {
     int32_t child_begin; // children [child_begin, child_end) in the child list
     int32_t child_end;
     int32_t level;       // height in the supernodal tree (leaves = 0)
+    int32_t ldx;         // leading dimension of X (ncol rounded up to 4)
+    int64_t x_off;       // X = inverse of L11, ncol columns of ldx rows (lower, zero above)
+    int64_t l21_off;     // L21 copy, ncol columns of ld21 rows
+    int32_t ld21;        // leading dimension of L21 (nb rounded up to 4)
     int32_t pad;
 };
 
@@ -76,8 +80,8 @@ struct Symbolic {
     std::vector<int32_t> child;       // concatenated children lists
     std::vector<int32_t> level_ptr;   // levels+1
     std::vector<int32_t> level_sn;    // supernodes grouped by level (leaves first)
-    int max_nrow = 0, max_ncol = 0, max_children = 0;
-    int64_t panel_size = 0, dinv_size = 0, upd_size = 0, uvec_size = 0;
+    int max_nrow = 0, max_ncol = 0, max_children = 0, max_ldx = 0, max_ld21 = 0;
+    int64_t panel_size = 0, dinv_size = 0, upd_size = 0, uvec_size = 0, x_size = 0, l21_size = 0;
     int64_t factor_nnz = 0;           // nonzeros of the scalar factor (from the etree)
     double factor_flops = 0.0;        // dense flops of the supernodal factorisation
     // assembly maps into the factor array
