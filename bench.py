@@ -193,7 +193,7 @@ def main():
     ap.add_argument("--h", type=float, default=0.025)
     ap.add_argument("--iterations", type=int, default=30)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--refine", type=int, default=2)
+    ap.add_argument("--refine", type=int, default=1)
     ap.add_argument("--cpu-requests", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: skip the end-to-end pass")

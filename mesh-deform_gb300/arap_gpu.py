@@ -148,7 +148,7 @@ class ArapContext:
     def __exit__(self, *a):
         self.close()
 
-    def set_precision(self, precision: str = "fp64", refine_steps: int = 2):
+    def set_precision(self, precision: str = "fp64", refine_steps: int = 1):
         self._check(self.lib.arap_set_precision(self.h, PRECISION[precision], int(refine_steps)))
 
     def set_rest_positions(self, xyz: np.ndarray):

@@ -62,7 +62,7 @@ struct arap_ctx {
     std::vector<double> ctgt;     // 3 per constrained vertex (sorted order)
     std::vector<uint8_t> cmask;   // V
     int precision = ARAP_PRECISION_FP64;
-    int refine = 2;
+    int refine = 1;
     bool dirty = true;
     // symbolic cache (keyed by the constrained-vertex mask)
     bool sym_valid = false;
@@ -75,7 +75,7 @@ struct arap_ctx {
     DevBuf faces, ent_ptr, ent_fc, hc, w_orig;
     DevBuf rest, targets, out;
     DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn;
-    DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21;
+    DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T;
     DevBuf errw, ticket, flags;
     DevTopo dt{};
     DevSym ds{};
@@ -244,6 +244,7 @@ int setup_numeric(arap_ctx *ctx) {
     CK(ctx->Upd.ensure((size_t)std::max<int64_t>(s.upd_size, 1) * sizeof(T)));
     CK(ctx->Xinv.ensure((size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T)));
     CK(ctx->L21.ensure((size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T)));
+    CK(ctx->L21T.ensure((size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T)));
     CK(ctx->errw.ensure(sizeof(int)));
     CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
 
@@ -267,6 +268,7 @@ int setup_numeric(arap_ctx *ctx) {
         if (s.upd_size > 0) CK(cudaMemsetAsync(ctx->Upd.p, 0, (size_t)s.upd_size * sizeof(T), st));
         CK(cudaMemsetAsync(ctx->Xinv.p, 0, (size_t)s.x_size * sizeof(T), st));
         if (s.l21_size > 0) CK(cudaMemsetAsync(ctx->L21.p, 0, (size_t)s.l21_size * sizeof(T), st));
+        if (s.l21t_size > 0) CK(cudaMemsetAsync(ctx->L21T.p, 0, (size_t)s.l21t_size * sizeof(T), st));
         {
             Prof pr(ctx, ARAP_K_ASSEMBLE);
             launch_assemble<T, T>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->Lval.as<T>(),
@@ -278,7 +280,7 @@ int setup_numeric(arap_ctx *ctx) {
             Prof pr(ctx, ARAP_K_FACTOR);
             launch_factor_level<T>(d, s.level_ptr[l], s.level_ptr[l + 1] - s.level_ptr[l], ctx->Lval.as<T>(),
                                    ctx->Upd.as<T>(), ctx->Dinv.as<T>(), ctx->Xinv.as<T>(), ctx->L21.as<T>(),
-                                   ctx->errw.as<int>(), st);
+                                   ctx->L21T.as<T>(), ctx->errw.as<int>(), st);
             ctx->launches += 1;
         }
     }
@@ -323,7 +325,7 @@ int run_iterations<double>(arap_ctx *ctx, int iterations) {
         }
         {
             Prof pr(ctx, ARAP_K_SOLVE_BWD);
-            launch_solve_bwd<double>(d, ctx->Xinv.as<double>(), ctx->L21.as<double>(),
+            launch_solve_bwd<double>(d, ctx->Xinv.as<double>(), ctx->L21T.as<double>(),
                                      ctx->sol.as<Vec4<double>>(), ctx->pc64.as<Vec4<double>>(), nullptr, 0, tk + 1,
                                      fl + s.S, ctx->errw.as<int>(), st);
         }
@@ -368,7 +370,7 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_BWD);
-                launch_solve_bwd<float>(d, ctx->Xinv.as<float>(), ctx->L21.as<float>(),
+                launch_solve_bwd<float>(d, ctx->Xinv.as<float>(), ctx->L21T.as<float>(),
                                         ctx->sol.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(),
                                         ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(), st);
             }
@@ -476,7 +478,7 @@ void arap_destroy(arap_ctx *ctx) {
                       &ctx->amap, &ctx->dmap, &ctx->sn, &ctx->rows, &ctx->relind, &ctx->child,
                       &ctx->level_sn, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
                       &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
-                      &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->errw, &ctx->ticket,
+                      &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->L21T, &ctx->errw, &ctx->ticket,
                       &ctx->flags};
     for (DevBuf *b : bufs) b->release();
     for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);

@@ -199,7 +199,8 @@ template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
 k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
                const int32_t *__restrict__ relind, TF *__restrict__ Lval, TF *__restrict__ Upd,
-               TF *__restrict__ Dinv, TF *__restrict__ Xall, TF *__restrict__ L21all, int *err) {
+               TF *__restrict__ Dinv, TF *__restrict__ Xall, TF *__restrict__ L21all, TF *__restrict__ L21Tall,
+               int *err) {
     // one buffer, carved differently by the phases (separated by barriers)
     __shared__ __align__(16) TF sm[2 * NB * kTile];
     __shared__ TF s_inv;
@@ -381,12 +382,21 @@ k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ 
         }
         __syncthreads();
     }
-    // L21 with aligned columns
+    // L21 with aligned columns, and the transposes the backward solve reads
     TF *L21 = L21all + d.l21_off;
+    TF *L21T = L21Tall + d.l21t_off;
     const int ld21 = d.ld21;
     for (int64_t q = tid; q < (int64_t)nb * nc; q += kFactorThreads) {
         const int c = (int)(q / nb), i = (int)(q - (int64_t)c * nb);
-        L21[(int64_t)c * ld21 + i] = P[(int64_t)c * n + nc + i];
+        const TF v = P[(int64_t)c * n + nc + i];
+        L21[(int64_t)c * ld21 + i] = v;
+        L21T[(int64_t)i * ldx + c] = v;
+    }
+    __syncthreads();
+    TF *XT = Xall + d.xt_off;
+    for (int64_t q = tid; q < (int64_t)nc * nc; q += kFactorThreads) {
+        const int c = (int)(q / nc), rr = (int)(q - (int64_t)c * nc);  // X(rr, c)
+        if (rr >= c) XT[(int64_t)rr * ldx + c] = X[(int64_t)c * ldx + rr];
     }
 }
 
@@ -610,12 +620,41 @@ __device__ __forceinline__ void load4(const double *p, double v[4]) {
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
 }
 
+constexpr int kTriNone = 0, kTriLower = 1, kTriUpper = 2;
+
+// acc(4 rows x 3 components) += sum_{c in [c0,c1)} M[c*ld + 4q..4q+3] * v[c],
+// loads issued eight columns at a time so that they are in flight together.
+template <typename T>
+__device__ __forceinline__ void axpy_quad(const T *__restrict__ M, int ld, int q, int c0, int c1, const Vec4<T> *v,
+                                          T ax[4], T ay[4], T az[4]) {
+    int c = c0;
+    for (; c + 8 <= c1; c += 8) {
+        T m[8][4];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) load4(M + (int64_t)(c + u) * ld + 4 * q, m[u]);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const Vec4<T> vc = v[c + u];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { ax[k] += m[u][k] * vc.x; ay[k] += m[u][k] * vc.y; az[k] += m[u][k] * vc.z; }
+        }
+    }
+    for (; c < c1; ++c) {
+        T m4[4];
+        load4(M + (int64_t)c * ld + 4 * q, m4);
+        const Vec4<T> vc = v[c];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { ax[k] += m4[k] * vc.x; ay[k] += m4[k] * vc.y; az[k] += m4[k] * vc.z; }
+    }
+}
+
 // out[r] (-)= sum_{c < C} M[c*ld + r] * v[c] for r < R (M column-major, ld a
-// multiple of 4, columns 16-byte aligned, rows R..ld-1 zero). LOWER: only
-// c <= r contribute (column blocks above the diagonal are skipped). Threads own
-// 4-row quads; when there are fewer quads than threads, G groups of threads
-// split the columns and reduce through `red`. Ends with a barrier.
-template <typename T, bool LOWER, bool SUB>
+// multiple of 4, columns 16-byte aligned, rows R..ld-1 zero). TRI skips the
+// column range that is zero for a row quad: lower (c <= r) or upper (c >= r)
+// triangular M. Threads own 4-row quads; when there are fewer quads than
+// threads, G groups of threads split the columns and reduce through `red`.
+// Ends with a barrier.
+template <typename T, int TRI, bool SUB>
 __device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R, int C, const Vec4<T> *v,
                                           Vec4<T> *out, Vec4<T> *red) {
     const int tid = threadIdx.x;
@@ -625,16 +664,10 @@ __device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R
     G = min(G, 8);
     if (G == 1) {
         for (int q = tid; q < NQ; q += kSolveThreads) {
-            const int cend = LOWER ? min(C, 4 * q + 4) : C;
+            const int c0 = TRI == kTriUpper ? 4 * q : 0;
+            const int c1 = TRI == kTriLower ? min(C, 4 * q + 4) : C;
             T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-#pragma unroll 4
-            for (int c = 0; c < cend; ++c) {
-                T m4[4];
-                load4(M + (int64_t)c * ld + 4 * q, m4);
-                const Vec4<T> vc = v[c];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) { ax[k] += m4[k] * vc.x; ay[k] += m4[k] * vc.y; az[k] += m4[k] * vc.z; }
-            }
+            axpy_quad(M, ld, q, c0, c1, v, ax, ay, az);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 Vec4<T> &o = out[4 * q + k];
@@ -648,17 +681,10 @@ __device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R
     const int q = tid % NQ, g = tid / NQ;
     if (g < G) {
         const int chunk = (C + G - 1) / G;
-        const int cb = g * chunk;
-        const int ce = min(LOWER ? min(C, 4 * q + 4) : C, cb + chunk);
+        const int c0 = max(g * chunk, TRI == kTriUpper ? 4 * q : 0);
+        const int c1 = min(TRI == kTriLower ? min(C, 4 * q + 4) : C, g * chunk + chunk);
         T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-#pragma unroll 4
-        for (int c = cb; c < ce; ++c) {
-            T m4[4];
-            load4(M + (int64_t)c * ld + 4 * q, m4);
-            const Vec4<T> vc = v[c];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) { ax[k] += m4[k] * vc.x; ay[k] += m4[k] * vc.y; az[k] += m4[k] * vc.z; }
-        }
+        axpy_quad(M, ld, q, c0, c1, v, ax, ay, az);
 #pragma unroll
         for (int k = 0; k < 4; ++k) red[g * 4 * NQ + 4 * q + k] = {ax[k], ay[k], az[k], (T)0};
     }
@@ -672,40 +698,6 @@ __device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R
         Vec4<T> &o = out[rr];
         if (SUB) { o.x -= sx; o.y -= sy; o.z -= sz; }
         else o = {sx, sy, sz, (T)0};
-    }
-    __syncthreads();
-}
-
-// out[c] = sum_{r < R} M[c*ld + r] * v[r] for c < C (dot of column c with v);
-// LOWER: rows r >= c only (the quads below the diagonal). v must be zero-padded
-// to a multiple of 4 rows. One warp per column. Ends with a barrier.
-template <typename T, bool LOWER>
-__device__ __forceinline__ void gemv_dots(const T *__restrict__ M, int ld, int R, int C, const Vec4<T> *v,
-                                          Vec4<T> *out) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int nwarps = kSolveThreads / 32;
-    const int NQ = (R + 3) >> 2;
-    for (int c = warp; c < C; c += nwarps) {
-        const T *col = M + (int64_t)c * ld;
-        T ax = 0, ay = 0, az = 0;
-        for (int q = (LOWER ? (c >> 2) : 0) + lane; q < NQ; q += 32) {
-            T m4[4];
-            load4(col + 4 * q, m4);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const Vec4<T> x = v[4 * q + k];
-                ax += m4[k] * x.x;
-                ay += m4[k] * x.y;
-                az += m4[k] * x.z;
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            ax += __shfl_xor_sync(0xffffffffu, ax, o);
-            ay += __shfl_xor_sync(0xffffffffu, ay, o);
-            az += __shfl_xor_sync(0xffffffffu, az, o);
-        }
-        if (lane == 0) out[c] = {ax, ay, az, (T)0};
     }
     __syncthreads();
 }
@@ -774,8 +766,8 @@ k_solve_fwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
         }
         __syncthreads();
     }
-    gemv_cols<T, true, false>(Xall + d.x_off, d.ldx, nc, nc, fc, yv, red);
-    if (nb > 0) gemv_cols<T, false, true>(L21all + d.l21_off, d.ld21, nb, nc, yv, fb, red);
+    gemv_cols<T, kTriLower, false>(Xall + d.x_off, d.ldx, nc, nc, fc, yv, red);
+    if (nb > 0) gemv_cols<T, kTriNone, true>(L21all + d.l21_off, d.ld21, nb, nc, yv, fb, red);
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
     __threadfence();
@@ -784,17 +776,19 @@ k_solve_fwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
 }
 
 // Backward: for supernode s (root first), z = y - L21^T x(struct) and
-// x(cols) = X^T z. mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k, pc32[k] = float(pc64[k]).
+// x(cols) = X^T z, both as column sweeps over the stored transposes.
+// mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k, pc32[k] = float(pc64[k]).
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_bwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *__restrict__ rows,
-            const T *__restrict__ Xall, const T *__restrict__ L21all, Vec4<T> *__restrict__ sol,
+            const T *__restrict__ Xall, const T *__restrict__ L21Tall, Vec4<T> *__restrict__ sol,
             Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode, unsigned long long *ticket,
             unsigned *flags, int *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw);
     Vec4<T> *xv = zv + lay.ldx_max;
     Vec4<T> *gb = xv + lay.ldx_max;
+    Vec4<T> *red = gb + lay.ld21_max;
     __shared__ int s_task;
     __shared__ unsigned s_epoch;
     const int tid = threadIdx.x;
@@ -809,9 +803,9 @@ k_solve_bwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
     {
-        const T *X = Xall + d.x_off;
-        const T *L = L21all + d.l21_off;
-        const int64_t nx = (int64_t)d.ldx * nc, nl = (int64_t)d.ld21 * nc;
+        const T *X = Xall + d.xt_off;
+        const T *L = L21Tall + d.l21t_off;
+        const int64_t nx = (int64_t)d.ldx * nc, nl = (int64_t)d.ldx * nb;
         for (int64_t q = (int64_t)tid * 32; q < nx; q += (int64_t)kSolveThreads * 32)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(X + q));
         for (int64_t q = (int64_t)tid * 32; q < nl; q += (int64_t)kSolveThreads * 32)
@@ -820,25 +814,12 @@ k_solve_bwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
     if (tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
     __syncthreads();
     const int32_t *rs = rows + d.rows_off;
-    for (int i = tid; i < d.ld21; i += kSolveThreads)
-        gb[i] = (i < nb) ? ldcg4(sol + rs[i]) : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+    for (int i = tid; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
+    for (int i = tid; i < d.ldx; i += kSolveThreads)
+        zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
     __syncthreads();
-    if (nb > 0) {
-        gemv_dots<T, false>(L21all + d.l21_off, d.ld21, nb, nc, gb, xv);  // xv = L21^T g
-        for (int i = tid; i < d.ldx; i += kSolveThreads) {
-            if (i < nc) {
-                const Vec4<T> y = sol[d.first + i], a = xv[i];
-                zv[i] = {y.x - a.x, y.y - a.y, y.z - a.z, (T)0};
-            } else {
-                zv[i] = {(T)0, (T)0, (T)0, (T)0};
-            }
-        }
-    } else {
-        for (int i = tid; i < d.ldx; i += kSolveThreads)
-            zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
-    }
-    __syncthreads();
-    gemv_dots<T, true>(Xall + d.x_off, d.ldx, nc, nc, zv, xv);  // xv = X^T z
+    if (nb > 0) gemv_cols<T, kTriNone, true>(L21Tall + d.l21t_off, d.ldx, nc, nb, gb, zv, red);  // z = y - L21^T g
+    gemv_cols<T, kTriUpper, false>(Xall + d.xt_off, d.ldx, nc, nc, zv, xv, red);                 // x = X^T z
     for (int i = tid; i < nc; i += kSolveThreads) {
         const Vec4<T> x = xv[i];
         const int k = d.first + i;
@@ -928,10 +909,10 @@ void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc6
 
 template <typename TF>
 void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv, TF *X,
-                         TF *L21, int *err, cudaStream_t st) {
+                         TF *L21, TF *L21T, int *err, cudaStream_t st) {
     if (level_count == 0) return;
     k_factor_level<TF><<<level_count, kFactorThreads, 0, st>>>(s.level_sn + level_begin, s.sn, s.child, s.relind,
-                                                               Lval, Upd, Dinv, X, L21, err);
+                                                               Lval, Upd, Dinv, X, L21, L21T, err);
 }
 
 template <typename T>
@@ -969,13 +950,13 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
 }
 
 template <typename T>
-void launch_solve_bwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<double> *pc64,
+void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
                       cudaStream_t st) {
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
-    k_solve_bwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.sn, s.rows, X, L21, sol, pc64, pc32, mode, ticket,
+    k_solve_bwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.sn, s.rows, X, L21T, sol, pc64, pc32, mode, ticket,
                                                      flags, err);
 }
 
@@ -1013,9 +994,9 @@ template void launch_assemble<float, float>(const DevSym &, const double *, cons
 template void launch_assemble<double, double>(const DevSym &, const double *, const Vec4<double> *, double *,
                                               double *, Vec4<double> *, cudaStream_t);
 template void launch_factor_level<float>(const DevSym &, int, int, float *, float *, float *, float *, float *,
-                                         int *, cudaStream_t);
+                                         float *, int *, cudaStream_t);
 template void launch_factor_level<double>(const DevSym &, int, int, double *, double *, double *, double *,
-                                          double *, int *, cudaStream_t);
+                                          double *, double *, int *, cudaStream_t);
 template void launch_local_step<float>(const DevSym &, const float *, const Vec4<float> *, const Vec4<float> *,
                                        Vec4<float> *, cudaStream_t);
 template void launch_local_step<double>(const DevSym &, const double *, const Vec4<double> *, const Vec4<double> *,

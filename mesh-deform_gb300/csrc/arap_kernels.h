@@ -64,7 +64,7 @@ void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc6
 // X = inverse of L11 and the aligned L21 copy the solves read
 template <typename TF>
 void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv, TF *X,
-                         TF *L21, int *err, cudaStream_t st);
+                         TF *L21, TF *L21T, int *err, cudaStream_t st);
 // local step: covariance + rotation fit (estimateRotations arap.h:354-384)
 template <typename T>
 void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *pc, Vec4<T> *R,
@@ -84,7 +84,7 @@ template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
                       unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st);
 template <typename T>
-void launch_solve_bwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<double> *pc64,
+void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
                       cudaStream_t st);
 // deformed positions back to the original vertex order as doubles (arap.h:133-135)

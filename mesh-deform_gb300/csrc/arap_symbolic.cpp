@@ -355,7 +355,7 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     }
     // levels, offsets, struct rows, children, relative indices
     int maxlev = 0;
-    int64_t poff = 0, doff = 0, uoff = 0, voff = 0, xoff = 0, loff = 0;
+    int64_t poff = 0, doff = 0, uoff = 0, voff = 0, xoff = 0, loff = 0, ltoff = 0;
     double flops = 0.0;
     for (int s = 0; s < S; ++s) {
         SnInfo &d = sym.sn[s];
@@ -378,6 +378,10 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         d.ld21 = (nb + 3) & ~3;
         d.x_off = xoff;
         xoff += (int64_t)d.ldx * d.ncol;
+        d.xt_off = xoff;  // X and X^T side by side in the same array
+        xoff += (int64_t)d.ldx * d.ncol;
+        d.l21t_off = ltoff;
+        ltoff += (int64_t)d.ldx * nb;
         d.l21_off = loff;
         loff += (int64_t)d.ld21 * d.ncol;
         sym.max_ldx = std::max(sym.max_ldx, (int)d.ldx);
@@ -400,6 +404,7 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     sym.uvec_size = voff;
     sym.x_size = xoff;
     sym.l21_size = loff;
+    sym.l21t_size = ltoff;
     // relind: where each struct row of s sits in its parent's front
     for (int s = 0; s < S; ++s) {
         SnInfo &d = sym.sn[s];

@@ -58,6 +58,8 @@ struct SnInfo {
     int64_t l21_off;     // L21 copy, ncol columns of ld21 rows
     int32_t ld21;        // leading dimension of L21 (nb rounded up to 4)
     int32_t pad;
+    int64_t xt_off;      // X^T, ncol columns of ldx rows (upper, zero below)
+    int64_t l21t_off;    // L21^T, nb columns of ldx rows
 };
 
 struct Symbolic {
@@ -82,6 +84,7 @@ struct Symbolic {
     std::vector<int32_t> level_sn;    // supernodes grouped by level (leaves first)
     int max_nrow = 0, max_ncol = 0, max_children = 0, max_ldx = 0, max_ld21 = 0;
     int64_t panel_size = 0, dinv_size = 0, upd_size = 0, uvec_size = 0, x_size = 0, l21_size = 0;
+    int64_t l21t_size = 0;
     int64_t factor_nnz = 0;           // nonzeros of the scalar factor (from the etree)
     double factor_flops = 0.0;        // dense flops of the supernodal factorisation
     // assembly maps into the factor array
