@@ -607,18 +607,30 @@ k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ 
 // supernodal triangular solves
 
 constexpr int kSolveThreads = 256;
-constexpr int kRedRows = 1024;  // reduction scratch (rows x groups) of gemv_cols
+constexpr int kRedRows = 512;    // reduction scratch (rows x groups) of gemv_cols
+constexpr int kStageBytes = 40 * 1024;  // shared-memory staging of one supernode's matrices
 
-// Four consecutive elements from a 16-byte aligned address.
+// Four consecutive elements from a 16-byte aligned address (shared or global).
 __device__ __forceinline__ void load4(const float *p, float v[4]) {
-    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    const float4 a = *reinterpret_cast<const float4 *>(p);
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
 }
 __device__ __forceinline__ void load4(const double *p, double v[4]) {
-    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
-    const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    const double2 a = reinterpret_cast<const double2 *>(p)[0];
+    const double2 b = reinterpret_cast<const double2 *>(p)[1];
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
 }
+
+// Asynchronous copy of `bytes` (a multiple of 16, both ends 16-byte aligned)
+// from global to shared memory by the whole CTA; completes at cp_async_wait.
+__device__ __forceinline__ void cp_async_bulk16(void *smem, const void *gmem, int64_t bytes) {
+    const unsigned base = (unsigned)__cvta_generic_to_shared(smem);
+    const char *g = static_cast<const char *>(gmem);
+    for (int64_t off = (int64_t)threadIdx.x * 16; off < bytes; off += (int64_t)blockDim.x * 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(base + (unsigned)off), "l"(g + off) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 constexpr int kTriNone = 0, kTriLower = 1, kTriUpper = 2;
 
@@ -661,7 +673,7 @@ __device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R
     const int NQ = (R + 3) >> 2;
     int G = NQ > 0 ? kSolveThreads / NQ : 1;
     G = max(1, min(G, kRedRows / max(4 * NQ, 1)));
-    G = min(G, 8);
+    G = min(G, 4);
     if (G == 1) {
         for (int q = tid; q < NQ; q += kSolveThreads) {
             const int c0 = TRI == kTriUpper ? 4 * q : 0;
@@ -702,23 +714,46 @@ __device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R
     __syncthreads();
 }
 
-// Shared-memory layout of the solve kernels (dynamic): two vectors of max_ldx
-// rows, one of max_ld21 rows and the kRedRows reduction scratch.
+// Shared-memory layout of the solve kernels (dynamic): the staging area for
+// one supernode's matrices, two vectors of max_ldx rows, one of max_ld21 rows
+// and the kRedRows reduction scratch.
 struct SolveSmem {
     int ldx_max, ld21_max;
 };
 
+// Stages the matrices a supernode's solve reads (A: a_elems, then B: b_elems
+// elements) into shared memory when they fit, asynchronously. Returns the
+// pointers the GEMVs should read (shared when staged, global otherwise).
+template <typename T>
+__device__ __forceinline__ void stage_pair(T *stage, const T *A, int64_t a_elems, const T *B, int64_t b_elems,
+                                           const T *&ra, const T *&rb) {
+    const int64_t cap = kStageBytes / (int64_t)sizeof(T);
+    ra = A;
+    rb = B;
+    if (a_elems <= cap) {
+        cp_async_bulk16(stage, A, a_elems * (int64_t)sizeof(T));
+        ra = stage;
+        if (a_elems + b_elems <= cap) {
+            cp_async_bulk16(stage + a_elems, B, b_elems * (int64_t)sizeof(T));
+            rb = stage + a_elems;
+        }
+    }
+    cp_async_commit();
+}
+
 // Forward: for supernode s (children first), f = [b(cols); 0] plus the
 // children's update vectors; y = X f(cols); u_s = f(struct) - L21 y goes to
-// the parent.
+// the parent. Tickets are handed out in level order (leaves first), so a CTA
+// only waits for supernodes of lower levels, which started before it.
 template <typename T>
-__global__ void __launch_bounds__(kSolveThreads)
-k_solve_fwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
-            const int32_t *__restrict__ relind, const T *__restrict__ Xall, const T *__restrict__ L21all,
-            Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec, unsigned long long *ticket, unsigned *flags,
-            int *err) {
+__global__ void __launch_bounds__(kSolveThreads, 3)
+k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+            const int32_t *__restrict__ child, const int32_t *__restrict__ relind, const T *__restrict__ Xall,
+            const T *__restrict__ L21all, Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec,
+            unsigned long long *ticket, unsigned *flags, int *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Vec4<T> *fc = reinterpret_cast<Vec4<T> *>(smem_raw);
+    T *stage = reinterpret_cast<T *>(smem_raw);
+    Vec4<T> *fc = reinterpret_cast<Vec4<T> *>(smem_raw + kStageBytes);
     Vec4<T> *yv = fc + lay.ldx_max;
     Vec4<T> *fb = yv + lay.ldx_max;
     Vec4<T> *red = fb + lay.ld21_max;
@@ -727,7 +762,7 @@ k_solve_fwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
     const int tid = threadIdx.x;
     if (tid == 0) {
         const unsigned long long t = atomicAdd(ticket, 1ull);
-        s_task = (int)(t % (unsigned long long)S);
+        s_task = order[(int)(t % (unsigned long long)S)];
         s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
     }
     __syncthreads();
@@ -735,16 +770,8 @@ k_solve_fwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
     const unsigned epoch = s_epoch;
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
-    // warm L2/L1 with this supernode's matrices while the children finish
-    {
-        const T *X = Xall + d.x_off;
-        const T *L = L21all + d.l21_off;
-        const int64_t nx = (int64_t)d.ldx * nc, nl = (int64_t)d.ld21 * nc;
-        for (int64_t q = (int64_t)tid * 32; q < nx; q += (int64_t)kSolveThreads * 32)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(X + q));
-        for (int64_t q = (int64_t)tid * 32; q < nl; q += (int64_t)kSolveThreads * 32)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(L + q));
-    }
+    const T *Xs, *Ls;
+    stage_pair(stage, Xall + d.x_off, (int64_t)d.ldx * nc, L21all + d.l21_off, (int64_t)d.ld21 * nc, Xs, Ls);
     if (tid == 0)
         for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
     __syncthreads();
@@ -766,8 +793,10 @@ k_solve_fwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
         }
         __syncthreads();
     }
-    gemv_cols<T, kTriLower, false>(Xall + d.x_off, d.ldx, nc, nc, fc, yv, red);
-    if (nb > 0) gemv_cols<T, kTriNone, true>(L21all + d.l21_off, d.ld21, nb, nc, yv, fb, red);
+    cp_async_wait();
+    __syncthreads();
+    gemv_cols<T, kTriLower, false>(Xs, d.ldx, nc, nc, fc, yv, red);
+    if (nb > 0) gemv_cols<T, kTriNone, true>(Ls, d.ld21, nb, nc, yv, fb, red);
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
     __threadfence();
@@ -779,13 +808,14 @@ k_solve_fwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
 // x(cols) = X^T z, both as column sweeps over the stored transposes.
 // mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k, pc32[k] = float(pc64[k]).
 template <typename T>
-__global__ void __launch_bounds__(kSolveThreads)
-k_solve_bwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *__restrict__ rows,
-            const T *__restrict__ Xall, const T *__restrict__ L21Tall, Vec4<T> *__restrict__ sol,
-            Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode, unsigned long long *ticket,
-            unsigned *flags, int *err) {
+__global__ void __launch_bounds__(kSolveThreads, 3)
+k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+            const int32_t *__restrict__ rows, const T *__restrict__ Xall, const T *__restrict__ L21Tall,
+            Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode,
+            unsigned long long *ticket, unsigned *flags, int *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw);
+    T *stage = reinterpret_cast<T *>(smem_raw);
+    Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw + kStageBytes);
     Vec4<T> *xv = zv + lay.ldx_max;
     Vec4<T> *gb = xv + lay.ldx_max;
     Vec4<T> *red = gb + lay.ld21_max;
@@ -794,7 +824,7 @@ k_solve_bwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
     const int tid = threadIdx.x;
     if (tid == 0) {
         const unsigned long long t = atomicAdd(ticket, 1ull);
-        s_task = S - 1 - (int)(t % (unsigned long long)S);
+        s_task = order[S - 1 - (int)(t % (unsigned long long)S)];
         s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
     }
     __syncthreads();
@@ -802,24 +832,18 @@ k_solve_bwd(int S, SolveSmem lay, const SnInfo *__restrict__ sn, const int32_t *
     const unsigned epoch = s_epoch;
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
-    {
-        const T *X = Xall + d.xt_off;
-        const T *L = L21Tall + d.l21t_off;
-        const int64_t nx = (int64_t)d.ldx * nc, nl = (int64_t)d.ldx * nb;
-        for (int64_t q = (int64_t)tid * 32; q < nx; q += (int64_t)kSolveThreads * 32)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(X + q));
-        for (int64_t q = (int64_t)tid * 32; q < nl; q += (int64_t)kSolveThreads * 32)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(L + q));
-    }
+    const T *XTs, *LTs;
+    stage_pair(stage, Xall + d.xt_off, (int64_t)d.ldx * nc, L21Tall + d.l21t_off, (int64_t)d.ldx * nb, XTs, LTs);
     if (tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
     __syncthreads();
     const int32_t *rs = rows + d.rows_off;
     for (int i = tid; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+    cp_async_wait();
     __syncthreads();
-    if (nb > 0) gemv_cols<T, kTriNone, true>(L21Tall + d.l21t_off, d.ldx, nc, nb, gb, zv, red);  // z = y - L21^T g
-    gemv_cols<T, kTriUpper, false>(Xall + d.xt_off, d.ldx, nc, nc, zv, xv, red);                 // x = X^T z
+    if (nb > 0) gemv_cols<T, kTriNone, true>(LTs, d.ldx, nc, nb, gb, zv, red);  // z = y - L21^T g
+    gemv_cols<T, kTriUpper, false>(XTs, d.ldx, nc, nc, zv, xv, red);             // x = X^T z
     for (int i = tid; i < nc; i += kSolveThreads) {
         const Vec4<T> x = xv[i];
         const int k = d.first + i;
@@ -936,7 +960,7 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 }
 
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
-    return (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
+    return (size_t)kStageBytes + (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
 }
 
 template <typename T>
@@ -945,8 +969,8 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
-    k_solve_fwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.sn, s.child, s.relind, X, L21, sol, uvec, ticket,
-                                                     flags, err);
+    k_solve_fwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.level_sn, s.sn, s.child, s.relind, X, L21, sol,
+                                                     uvec, ticket, flags, err);
 }
 
 template <typename T>
@@ -956,8 +980,8 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
-    k_solve_bwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.sn, s.rows, X, L21T, sol, pc64, pc32, mode, ticket,
-                                                     flags, err);
+    k_solve_bwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.level_sn, s.sn, s.rows, X, L21T, sol, pc64, pc32,
+                                                     mode, ticket, flags, err);
 }
 
 void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st) {
