@@ -14,6 +14,7 @@
 
 namespace arapgpu {
 cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64);
+cudaError_t configure_factor_smem(int max_ncol);
 }
 
 using namespace arapgpu;
@@ -74,7 +75,8 @@ struct arap_ctx {
     // device buffers
     DevBuf faces, ent_ptr, ent_fc, hc, w_orig;
     DevBuf rest, targets, out;
-    DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn;
+    DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn, fitems;
+    int factor_smem_ncol = 0;
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T;
     DevBuf errw, ticket, flags;
     DevTopo dt{};
@@ -175,6 +177,11 @@ int prepare_symbolic(arap_ctx *ctx) {
     CK(upload(ctx->relind, s.relind, st));
     CK(upload(ctx->child, s.child, st));
     CK(upload(ctx->level_sn, s.level_sn, st));
+    CK(upload(ctx->fitems, s.fitems, st));
+    if (s.max_ncol > ctx->factor_smem_ncol) {
+        CK(configure_factor_smem(s.max_ncol));
+        ctx->factor_smem_ncol = s.max_ncol;
+    }
     // solve scheduling state: ticket counters and per-supernode flags start at 0
     CK(ctx->ticket.ensure(2 * sizeof(unsigned long long)));
     CK(ctx->flags.ensure(2 * sizeof(unsigned) * (size_t)std::max(s.S, 1)));
@@ -197,6 +204,7 @@ int prepare_symbolic(arap_ctx *ctx) {
     d.nnz = (int)s.dcol.size();
     d.max_ldx = s.max_ldx;
     d.max_ld21 = s.max_ld21;
+    d.max_ncol = s.max_ncol;
     d.drow = ctx->drow.as<int32_t>();
     d.dcol = ctx->dcol.as<int32_t>();
     d.dent = ctx->dent.as<int32_t>();
@@ -275,12 +283,11 @@ int setup_numeric(arap_ctx *ctx) {
                                   ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<T>>(), st);
         }
         ctx->launches += 1;
-        const int nlev = (int)s.level_ptr.size() - 1;
-        for (int l = 0; l < nlev; ++l) {
+        for (const FactorLaunch &fl : s.fplan) {
             Prof pr(ctx, ARAP_K_FACTOR);
-            launch_factor_level<T>(d, s.level_ptr[l], s.level_ptr[l + 1] - s.level_ptr[l], ctx->Lval.as<T>(),
-                                   ctx->Upd.as<T>(), ctx->Dinv.as<T>(), ctx->Xinv.as<T>(), ctx->L21.as<T>(),
-                                   ctx->L21T.as<T>(), ctx->errw.as<int>(), st);
+            launch_factor_step<T>(d, fl, ctx->fitems.as<FItem>(), ctx->Lval.as<T>(), ctx->Upd.as<T>(),
+                                  ctx->Dinv.as<T>(), ctx->Xinv.as<T>(), ctx->L21.as<T>(), ctx->L21T.as<T>(),
+                                  ctx->errw.as<int>(), st);
             ctx->launches += 1;
         }
     }
@@ -476,7 +483,7 @@ void arap_destroy(arap_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->faces, &ctx->ent_ptr, &ctx->ent_fc, &ctx->hc, &ctx->w_orig, &ctx->rest,
                       &ctx->targets, &ctx->out, &ctx->drow, &ctx->dcol, &ctx->dent, &ctx->oldidx,
                       &ctx->amap, &ctx->dmap, &ctx->sn, &ctx->rows, &ctx->relind, &ctx->child,
-                      &ctx->level_sn, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
+                      &ctx->level_sn, &ctx->fitems, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
                       &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
                       &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->L21T, &ctx->errw, &ctx->ticket,
                       &ctx->flags};

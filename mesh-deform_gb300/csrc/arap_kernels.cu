@@ -26,7 +26,7 @@ __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
 __device__ __forceinline__ void wait_flag(const unsigned *p, unsigned target, int *err) {
     for (unsigned it = 0; it < kSpinLimit; ++it) {
         if (ld_acquire(p) >= target) return;
-        __nanosleep(100);
+        __nanosleep(it < 64 ? 20 : 200);
     }
     atomicOr(err, kErrTimeout);
 }
@@ -177,10 +177,11 @@ __global__ void k_assemble(int m, const int32_t *__restrict__ drow, const int32_
 }
 
 // ---------------------------------------------------------------------------
-// multifrontal Cholesky, one CTA per supernode of a level
+// multifrontal Cholesky, level by level, many CTAs per front
 
 constexpr int kFactorThreads = 256;
-constexpr int kTile = 64;
+constexpr int kTile = 64;   // rows of an update tile
+constexpr int kSlice = 32;  // parent columns of one extend-add item
 
 // Front of supernode d: the nrow x ncol panel P (column-major, ld nrow; rows are
 // the supernode's columns then its struct rows) and the nb x nb update matrix U.
@@ -190,213 +191,289 @@ __device__ __forceinline__ TF &front(TF *P, TF *U, int n, int nc, int nb, int i,
     return k < nc ? P[(int64_t)k * n + i] : U[(int64_t)(k - nc) * nb + (i - nc)];
 }
 
-// Per level, one CTA per supernode: extend-add of the children's update
-// matrices, blocked right-looking partial Cholesky of the front (32-column
-// blocks: diagonal block factored and inverted in shared memory, rows below
-// solved against it, trailing update in 64x64 tiles), then the two arrays the
-// solves read: X = inverse of L11 (lower, ldx rows) and L21 (ld21 rows).
+// Extend-add: the parent columns [a, b) of a front receive the matching
+// columns of every child's update matrix, children in order. Parent columns
+// are split between CTAs, so no two CTAs touch the same entry.
 template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
-k_factor_level(const int32_t *__restrict__ level_sn, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
-               const int32_t *__restrict__ relind, TF *__restrict__ Lval, TF *__restrict__ Upd,
-               TF *__restrict__ Dinv, TF *__restrict__ Xall, TF *__restrict__ L21all, TF *__restrict__ L21Tall,
-               int *err) {
-    // one buffer, carved differently by the phases (separated by barriers)
-    __shared__ __align__(16) TF sm[2 * NB * kTile];
-    __shared__ TF s_inv;
-    TF(*As)[kTile] = reinterpret_cast<TF(*)[kTile]>(sm);
-    TF(*Bs)[kTile] = reinterpret_cast<TF(*)[kTile]>(sm + NB * kTile);
-    TF(*Db)[NB + 1] = reinterpret_cast<TF(*)[NB + 1]>(sm);                   // diagonal block, row-major
-    TF(*Di)[NB + 1] = reinterpret_cast<TF(*)[NB + 1]>(sm + NB * (NB + 1));  // its inverse, row-major
-    const int tid = threadIdx.x;
-    const SnInfo d = sn[level_sn[blockIdx.x]];
+k_fea(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const int32_t *__restrict__ child,
+      const int32_t *__restrict__ relind, TF *__restrict__ Lval, TF *__restrict__ Upd) {
+    __shared__ int s_k0, s_k1;
+    const FItem it = items[blockIdx.x];
+    const SnInfo d = sn[it.sn];
     const int n = d.nrow, nc = d.ncol, nb = n - nc;
     TF *P = Lval + d.panel_off;
     TF *U = Upd + d.upd_off;
-
-    // extend-add of the children's update matrices (pull; children in order)
+    const int tid = threadIdx.x;
     for (int ci = d.child_begin; ci < d.child_end; ++ci) {
         const SnInfo c = sn[child[ci]];
         const int nbc = c.nrow - c.ncol;
-        const TF *Uc = Upd + c.upd_off;
         const int32_t *ri = relind + c.relind_off;
-        const int64_t total = (int64_t)nbc * nbc;
-        for (int64_t t = tid; t < total; t += kFactorThreads) {
-            const int k = (int)(t / nbc), i = (int)(t - (int64_t)k * nbc);
-            if (i < k) continue;
-            front(P, U, n, nc, nb, ri[i], ri[k]) += Uc[t];
+        if (tid == 0) {  // child columns whose parent column lies in [a, b) (ri increases)
+            int lo = 0, hi = nbc;
+            while (lo < hi) { const int m = (lo + hi) >> 1; if (ri[m] < it.a) lo = m + 1; else hi = m; }
+            s_k0 = lo;
+            hi = nbc;
+            while (lo < hi) { const int m = (lo + hi) >> 1; if (ri[m] < it.b) lo = m + 1; else hi = m; }
+            s_k1 = lo;
+        }
+        __syncthreads();
+        const TF *Uc = Upd + c.upd_off;
+        for (int k = s_k0; k < s_k1; ++k) {
+            const int pk = ri[k];
+            for (int i = k + tid; i < nbc; i += kFactorThreads) front(P, U, n, nc, nb, ri[i], pk) += Uc[(int64_t)k * nbc + i];
         }
         __syncthreads();
     }
+}
 
-    for (int j0 = 0; j0 < nc; j0 += NB) {
-        const int w = min(NB, nc - j0);
-        // (a1) diagonal block: load, factor and invert in shared memory
+// Left-looking update of block column jb: rows [j0 + 64 rt, +64) of columns
+// [j0, j0+w) lose sum_{k < j0} P(r, k) P(j0+c, k).
+template <typename TF>
+__global__ void __launch_bounds__(kFactorThreads)
+k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF *__restrict__ Lval) {
+    __shared__ TF As[NB][kTile];
+    __shared__ TF Bs[NB][NB + 1];
+    const FItem it = items[blockIdx.x];
+    const SnInfo d = sn[it.sn];
+    const int n = d.nrow, nc = d.ncol;
+    const int j0 = jb * NB, w = min(NB, nc - j0);
+    const int r0 = j0 + it.a * kTile;
+    TF *P = Lval + d.panel_off;
+    const int tid = threadIdx.x, tx = tid % 8, ty = tid / 8;  // 4 columns x 2 rows per thread
+    TF acc[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    for (int k0 = 0; k0 < j0; k0 += NB) {
+        for (int q = tid; q < NB * kTile; q += kFactorThreads) {
+            const int t = q / kTile, r = q % kTile;
+            As[t][r] = (r0 + r < n) ? P[(int64_t)(k0 + t) * n + r0 + r] : (TF)0;
+        }
         for (int q = tid; q < NB * NB; q += kFactorThreads) {
-            const int r = q % NB, c = q / NB;
-            Db[r][c] = (r < w && c < w && c <= r) ? P[(int64_t)(j0 + c) * n + j0 + r] : (TF)0;
+            const int t = q / NB, c = q % NB;
+            Bs[t][c] = (c < w) ? P[(int64_t)(k0 + t) * n + j0 + c] : (TF)0;
         }
         __syncthreads();
-        for (int k = 0; k < w; ++k) {
-            if (tid == 0) {
-                TF dk = Db[k][k];
-                if (!(dk > (TF)0)) { atomicOr(err, kErrNotSpd); dk = (TF)1; }
-                dk = tsqrt(dk);
-                Db[k][k] = dk;
-                s_inv = (TF)1 / dk;
-            }
-            __syncthreads();
-            if (tid > k && tid < w) Db[tid][k] *= s_inv;
-            __syncthreads();
-            const int m = w - k - 1;
-            for (int q = tid; q < m * m; q += kFactorThreads) {
-                const int r = k + 1 + q / m, c = k + 1 + q % m;
-                if (c <= r) Db[r][c] -= Db[r][k] * Db[c][k];
-            }
-            __syncthreads();
-        }
-        if (tid < NB) {  // inverse of the lower-triangular block, column tid
-            const int c = tid;
-            for (int i = 0; i < NB; ++i) {
-                TF v = (TF)0;
-                if (i >= c && i < w) {
-                    TF acc = (i == c) ? (TF)1 : (TF)0;
-                    for (int t = c; t < i; ++t) acc -= Db[i][t] * Di[t][c];
-                    v = acc / Db[i][i];
-                }
-                Di[i][c] = v;
-            }
-        }
-        __syncthreads();
-        for (int q = tid; q < NB * NB; q += kFactorThreads) {
-            const int r = q % NB, c = q / NB;
-            if (r < w && c < w && c <= r) P[(int64_t)(j0 + c) * n + j0 + r] = Db[r][c];
-            Dinv[d.dinv_off + (int64_t)(j0 / NB) * NB * NB + (int64_t)c * NB + r] = Di[r][c];
-        }
-        // (a2) rows below the block: L_ib = A_ib * inv(L_bb)^T, one row per thread
-        for (int i = j0 + w + tid; i < n; i += kFactorThreads) {
-            TF a[NB];
+#pragma unroll 8
+        for (int t = 0; t < NB; ++t) {
+            const TF a0 = As[t][ty], a1 = As[t][ty + 32];
 #pragma unroll
-            for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i] : (TF)0;
+            for (int cc = 0; cc < 4; ++cc) {
+                const TF bv = Bs[t][tx * 4 + cc];
+                acc[0][cc] += a0 * bv;
+                acc[1][cc] += a1 * bv;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+        const int r = r0 + ty + 32 * rr;
+        if (r >= n) continue;
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            const int c = tx * 4 + cc;
+            if (c < w) P[(int64_t)(j0 + c) * n + r] -= acc[rr][cc];
+        }
+    }
+}
+
+// Diagonal block jb of a front: Cholesky and inverse in shared memory, then the
+// rows below are solved against it (L_ib = A_ib inv(L_bb)^T), one row per thread.
+template <typename TF>
+__global__ void __launch_bounds__(kFactorThreads)
+k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF *__restrict__ Lval,
+      TF *__restrict__ Dinv, int *err) {
+    __shared__ TF Db[NB][NB + 1];  // row-major
+    __shared__ TF Di[NB][NB + 1];
+    __shared__ TF s_inv;
+    const SnInfo d = sn[items[blockIdx.x].sn];
+    const int n = d.nrow, nc = d.ncol;
+    const int j0 = jb * NB, w = min(NB, nc - j0);
+    TF *P = Lval + d.panel_off;
+    const int tid = threadIdx.x;
+    for (int q = tid; q < NB * NB; q += kFactorThreads) {
+        const int r = q % NB, c = q / NB;
+        Db[r][c] = (r < w && c < w && c <= r) ? P[(int64_t)(j0 + c) * n + j0 + r] : (TF)0;
+    }
+    __syncthreads();
+    for (int k = 0; k < w; ++k) {
+        if (tid == 0) {
+            TF dk = Db[k][k];
+            if (!(dk > (TF)0)) { atomicOr(err, kErrNotSpd); dk = (TF)1; }
+            dk = tsqrt(dk);
+            Db[k][k] = dk;
+            s_inv = (TF)1 / dk;
+        }
+        __syncthreads();
+        if (tid > k && tid < w) Db[tid][k] *= s_inv;
+        __syncthreads();
+        const int m = w - k - 1;
+        for (int q = tid; q < m * m; q += kFactorThreads) {
+            const int r = k + 1 + q / m, c = k + 1 + q % m;
+            if (c <= r) Db[r][c] -= Db[r][k] * Db[c][k];
+        }
+        __syncthreads();
+    }
+    if (tid < NB) {  // inverse of the lower-triangular block, column tid
+        const int c = tid;
+        for (int i = 0; i < NB; ++i) {
+            TF v = (TF)0;
+            if (i >= c && i < w) {
+                TF acc = (i == c) ? (TF)1 : (TF)0;
+                for (int t = c; t < i; ++t) acc -= Db[i][t] * Di[t][c];
+                v = acc / Db[i][i];
+            }
+            Di[i][c] = v;
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < NB * NB; q += kFactorThreads) {
+        const int r = q % NB, c = q / NB;
+        if (r < w && c < w && c <= r) P[(int64_t)(j0 + c) * n + j0 + r] = Db[r][c];
+        Dinv[d.dinv_off + (int64_t)jb * NB * NB + (int64_t)c * NB + r] = Di[r][c];
+    }
+    for (int i = j0 + w + tid; i < n; i += kFactorThreads) {
+        TF a[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i] : (TF)0;
 #pragma unroll 4
-            for (int r = 0; r < NB; ++r) {
-                if (r >= w) break;
-                TF acc = (TF)0;
+        for (int r = 0; r < NB; ++r) {
+            if (r >= w) break;
+            TF acc = (TF)0;
 #pragma unroll
-                for (int c = 0; c < NB; ++c)
-                    if (c <= r) acc += a[c] * Di[r][c];
-                P[(int64_t)(j0 + r) * n + i] = acc;
-            }
+            for (int c = 0; c < NB; ++c)
+                if (c <= r) acc += a[c] * Di[r][c];
+            P[(int64_t)(j0 + r) * n + i] = acc;
         }
-        __syncthreads();
-        // (c) trailing update F[i][k] -= sum_t L[i][j0+t] L[k][j0+t], k,i >= j0+w
-        const int c0 = j0 + w;
-        const int rem = n - c0;
-        if (rem > 0) {
-            const int ntl = (rem + kTile - 1) / kTile;
-            const int tx = tid % 16, ty = tid / 16;
-            for (int ti = 0; ti < ntl; ++ti) {
-                for (int tk = 0; tk <= ti; ++tk) {
-                    const int rb = c0 + ti * kTile, cb = c0 + tk * kTile;
-                    for (int q = tid; q < NB * kTile; q += kFactorThreads) {
-                        const int t = q / kTile, r = q % kTile;
-                        TF av = (TF)0, bv = (TF)0;
-                        if (t < w) {
-                            const TF *col = P + (int64_t)(j0 + t) * n;
-                            if (rb + r < n) av = col[rb + r];
-                            if (cb + r < n) bv = col[cb + r];
-                        }
-                        As[t][r] = av;
-                        Bs[t][r] = bv;
-                    }
-                    __syncthreads();
-                    TF acc[4][4];
-#pragma unroll
-                    for (int a = 0; a < 4; ++a)
-#pragma unroll
-                        for (int b = 0; b < 4; ++b) acc[a][b] = (TF)0;
-                    for (int t = 0; t < w; ++t) {
-                        TF av[4], bv[4];
-#pragma unroll
-                        for (int a = 0; a < 4; ++a) av[a] = As[t][ty + 16 * a];
-#pragma unroll
-                        for (int b = 0; b < 4; ++b) bv[b] = Bs[t][tx + 16 * b];
-#pragma unroll
-                        for (int a = 0; a < 4; ++a)
-#pragma unroll
-                            for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
-                    }
-#pragma unroll
-                    for (int a = 0; a < 4; ++a) {
-                        const int row = rb + ty + 16 * a;
-#pragma unroll
-                        for (int b = 0; b < 4; ++b) {
-                            const int colf = cb + tx + 16 * b;
-                            if (row < n && colf < n && row >= colf) front(P, U, n, nc, nb, row, colf) -= acc[a][b];
-                        }
-                    }
-                    __syncthreads();
-                }
-            }
-        }
-        __syncthreads();
     }
+}
 
-    // X = inverse of L11 by block rows: X_ii = inv(L_ii),
-    // X_ij = -inv(L_ii) * sum_{k=j..i-1} L_ik X_kj
-    TF *X = Xall + d.x_off;
-    const int ldx = d.ldx;
-    const int nblk = (nc + NB - 1) / NB;
-    TF(*Ts)[NB + 1] = reinterpret_cast<TF(*)[NB + 1]>(sm);
-    const int r = tid % NB, cg = tid / NB;  // row in block, group of 4 columns
-    for (int ib = 0; ib < nblk; ++ib) {
-        const int i0 = ib * NB, wi = min(NB, nc - i0);
-        const TF *Dii = Dinv + d.dinv_off + (int64_t)ib * NB * NB;
-        for (int q = tid; q < NB * NB; q += kFactorThreads) {
-            const int rr = q % NB, cc = q / NB;
-            if (rr < wi && cc < wi) X[(int64_t)(i0 + cc) * ldx + i0 + rr] = Dii[(int64_t)cc * NB + rr];
+// Schur complement of a front: the 64x64 tile (rt, ct), rt >= ct, of U loses
+// sum_{k < nc} L21(r, k) L21(c, k); each entry is read and written once.
+template <typename TF>
+__global__ void __launch_bounds__(kFactorThreads)
+k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *__restrict__ Lval,
+        TF *__restrict__ Upd) {
+    __shared__ TF As[NB][kTile];
+    __shared__ TF Bs[NB][kTile];
+    const FItem it = items[blockIdx.x];
+    const SnInfo d = sn[it.sn];
+    const int n = d.nrow, nc = d.ncol, nb = n - nc;
+    const TF *P = Lval + d.panel_off;
+    TF *U = Upd + d.upd_off;
+    const int rb = it.a * kTile, cb = it.b * kTile;  // within U
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    TF acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = (TF)0;
+    for (int k0 = 0; k0 < nc; k0 += NB) {
+        const int kw = min(NB, nc - k0);
+        for (int q = tid; q < NB * kTile; q += kFactorThreads) {
+            const int t = q / kTile, r = q % kTile;
+            TF av = (TF)0, bv = (TF)0;
+            if (t < kw) {
+                const TF *col = P + (int64_t)(k0 + t) * n + nc;
+                if (rb + r < nb) av = col[rb + r];
+                if (cb + r < nb) bv = col[cb + r];
+            }
+            As[t][r] = av;
+            Bs[t][r] = bv;
         }
-        for (int jb = 0; jb < ib; ++jb) {
-            const int j0 = jb * NB;
-            TF acc[4] = {(TF)0, (TF)0, (TF)0, (TF)0};
-            if (r < wi) {
-                for (int k = j0; k < i0; ++k) {
-                    const TF l = P[(int64_t)k * n + i0 + r];
+        __syncthreads();
+#pragma unroll 8
+        for (int t = 0; t < NB; ++t) {
+            TF av[4], bv[4];
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) acc[cc] += l * X[(int64_t)(j0 + cg * 4 + cc) * ldx + k];
-                }
-            }
+            for (int a = 0; a < 4; ++a) av[a] = As[t][ty + 16 * a];
 #pragma unroll
-            for (int cc = 0; cc < 4; ++cc) Ts[cg * 4 + cc][r] = acc[cc];
-            __syncthreads();
-            if (r < wi) {
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[t][tx + 16 * b];
 #pragma unroll
-                for (int cc = 0; cc < 4; ++cc) {
-                    const int c = cg * 4 + cc;
-                    TF v = (TF)0;
-                    for (int t = 0; t <= r; ++t) v += Dii[(int64_t)t * NB + r] * Ts[c][t];
-                    X[(int64_t)(j0 + c) * ldx + i0 + r] = -v;
-                }
-            }
-            __syncthreads();
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
         }
         __syncthreads();
     }
-    // L21 with aligned columns, and the transposes the backward solve reads
-    TF *L21 = L21all + d.l21_off;
-    TF *L21T = L21Tall + d.l21t_off;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int r = rb + ty + 16 * a;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int c = cb + tx + 16 * b;
+            if (r < nb && c < nb && r >= c) U[(int64_t)c * nb + r] -= acc[a][b];
+        }
+    }
+}
+
+// Column block jb of X = inv(L11): X_jj = inv(L_jj) and, block row by block
+// row, X_ij = -inv(L_ii) sum_{k=j..i-1} L_ik X_kj, with the column block kept in
+// shared memory (dynamic, max_ncol x 33). Writes X, its transpose, and the
+// aligned L21 / L21^T copies of the block's columns.
+template <typename TF>
+__global__ void __launch_bounds__(kFactorThreads)
+k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *__restrict__ Lval,
+     const TF *__restrict__ Dinv, TF *__restrict__ Xall, TF *__restrict__ L21all, TF *__restrict__ L21Tall) {
+    extern __shared__ __align__(16) unsigned char fx_raw[];
+    TF *Xc = reinterpret_cast<TF *>(fx_raw);  // [row][NB + 1]
+    __shared__ TF Ts[NB][NB + 1];
+    const FItem it = items[blockIdx.x];
+    const SnInfo d = sn[it.sn];
+    const int n = d.nrow, nc = d.ncol, nb = n - nc;
+    const int jb = it.a, j0 = jb * NB, wj = min(NB, nc - j0);
+    const TF *P = Lval + d.panel_off;
+    const int tid = threadIdx.x;
+    const int nblk = (nc + NB - 1) / NB;
+    {
+        const TF *Djj = Dinv + d.dinv_off + (int64_t)jb * NB * NB;
+        for (int q = tid; q < NB * NB; q += kFactorThreads) {
+            const int r = q % NB, c = q / NB;
+            Xc[(j0 + r) * (NB + 1) + c] = (r < wj && c < wj) ? Djj[(int64_t)c * NB + r] : (TF)0;
+        }
+    }
+    __syncthreads();
+    const int r = tid % NB, cg = tid / NB;  // row in block, group of 4 columns
+    for (int ib = jb + 1; ib < nblk; ++ib) {
+        const int i0 = ib * NB, wi = min(NB, nc - i0);
+        TF acc[4] = {(TF)0, (TF)0, (TF)0, (TF)0};
+        if (r < wi) {
+#pragma unroll 4
+            for (int k = j0; k < i0; ++k) {
+                const TF l = P[(int64_t)k * n + i0 + r];
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) acc[cc] += l * Xc[k * (NB + 1) + cg * 4 + cc];
+            }
+        }
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) Ts[cg * 4 + cc][r] = acc[cc];
+        __syncthreads();
+        const TF *Dii = Dinv + d.dinv_off + (int64_t)ib * NB * NB;
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            const int c = cg * 4 + cc;
+            TF v = (TF)0;
+            if (r < wi)
+                for (int t = 0; t <= r; ++t) v += Dii[(int64_t)t * NB + r] * Ts[c][t];
+            Xc[(i0 + r) * (NB + 1) + c] = (r < wi && c < wj) ? -v : (TF)0;
+        }
+        __syncthreads();
+    }
+    TF *X = Xall + d.x_off, *XT = Xall + d.xt_off;
+    const int ldx = d.ldx;
+    for (int q = tid; q < (nc - j0) * NB; q += kFactorThreads) {
+        const int i = j0 + q / NB, c = q % NB;
+        if (c >= wj) continue;
+        const TF v = Xc[i * (NB + 1) + c];
+        X[(int64_t)(j0 + c) * ldx + i] = v;                 // X(i, j0+c)
+        if (i >= j0 + c) XT[(int64_t)i * ldx + j0 + c] = v;  // X^T stored column i
+    }
+    TF *L21 = L21all + d.l21_off, *L21T = L21Tall + d.l21t_off;
     const int ld21 = d.ld21;
-    for (int64_t q = tid; q < (int64_t)nb * nc; q += kFactorThreads) {
-        const int c = (int)(q / nb), i = (int)(q - (int64_t)c * nb);
+    for (int q = tid; q < wj * nb; q += kFactorThreads) {
+        const int c = j0 + q / nb, i = q % nb;
         const TF v = P[(int64_t)c * n + nc + i];
         L21[(int64_t)c * ld21 + i] = v;
         L21T[(int64_t)i * ldx + c] = v;
-    }
-    __syncthreads();
-    TF *XT = Xall + d.xt_off;
-    for (int64_t q = tid; q < (int64_t)nc * nc; q += kFactorThreads) {
-        const int c = (int)(q / nc), rr = (int)(q - (int64_t)c * nc);  // X(rr, c)
-        if (rr >= c) XT[(int64_t)rr * ldx + c] = X[(int64_t)c * ldx + rr];
     }
 }
 
@@ -772,12 +849,12 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     const int nc = d.ncol, nb = d.nrow - d.ncol;
     const T *Xs, *Ls;
     stage_pair(stage, Xall + d.x_off, (int64_t)d.ldx * nc, L21all + d.l21_off, (int64_t)d.ld21 * nc, Xs, Ls);
-    if (tid == 0)
-        for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
-    __syncthreads();
+    // everything that does not depend on the children is read before waiting
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
     for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
+    if (tid == 0)
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
     __syncthreads();
     for (int ci = d.child_begin; ci < d.child_end; ++ci) {
         const SnInfo c = sn[child[ci]];
@@ -834,12 +911,18 @@ k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     const int nc = d.ncol, nb = d.nrow - d.ncol;
     const T *XTs, *LTs;
     stage_pair(stage, Xall + d.xt_off, (int64_t)d.ldx * nc, L21Tall + d.l21t_off, (int64_t)d.ldx * nb, XTs, LTs);
-    if (tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
-    __syncthreads();
     const int32_t *rs = rows + d.rows_off;
-    for (int i = tid; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+    int myrow[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) myrow[u] = (tid + u * kSolveThreads < nb) ? rs[tid + u * kSolveThreads] : 0;
+    if (tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+        if (tid + u * kSolveThreads < nb) gb[tid + u * kSolveThreads] = ldcg4(sol + myrow[u]);
+    for (int i = tid + 4 * kSolveThreads; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
     cp_async_wait();
     __syncthreads();
     if (nb > 0) gemv_cols<T, kTriNone, true>(LTs, d.ldx, nc, nb, gb, zv, red);  // z = y - L21^T g
@@ -932,11 +1015,21 @@ void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc6
 }
 
 template <typename TF>
-void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv, TF *X,
-                         TF *L21, TF *L21T, int *err, cudaStream_t st) {
-    if (level_count == 0) return;
-    k_factor_level<TF><<<level_count, kFactorThreads, 0, st>>>(s.level_sn + level_begin, s.sn, s.child, s.relind,
-                                                               Lval, Upd, Dinv, X, L21, L21T, err);
+void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *items, TF *Lval, TF *Upd, TF *Dinv,
+                        TF *X, TF *L21, TF *L21T, int *err, cudaStream_t st) {
+    if (fl.count == 0) return;
+    const FItem *it = items + fl.item_off;
+    switch (fl.kind) {
+    case kFea: k_fea<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, s.child, s.relind, Lval, Upd); break;
+    case kFupd: k_fupd<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval); break;
+    case kFdt: k_fdt<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv, err); break;
+    case kFsyrk: k_fsyrk<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Upd); break;
+    case kFx: {
+        const size_t smem = (size_t)((s.max_ncol + NB - 1) / NB * NB) * (NB + 1) * sizeof(TF);
+        k_fx<TF><<<fl.count, kFactorThreads, smem, st>>>(it, s.sn, Lval, Dinv, X, L21, L21T);
+        break;
+    }
+    }
 }
 
 template <typename T>
@@ -995,6 +1088,16 @@ void launch_gather_rotations(const DevSym &s, const Vec4<T> *R, double *out9, cu
     k_gather_rotations<T><<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.oldidx, R, out9);
 }
 
+// Raises the dynamic shared-memory limit of the column-block inverse kernel.
+cudaError_t configure_factor_smem(int max_ncol) {
+    const int rows = (max_ncol + NB - 1) / NB * NB;
+    cudaError_t e = cudaFuncSetAttribute(k_fx<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(rows * (NB + 1) * sizeof(float)));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_fx<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(rows * (NB + 1) * sizeof(double)));
+}
+
 // Raises the dynamic shared-memory limit of the solve kernels (bytes per CTA).
 cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64) {
     cudaError_t e = cudaFuncSetAttribute(k_solve_fwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f32);
@@ -1017,10 +1120,10 @@ template void launch_assemble<float, float>(const DevSym &, const double *, cons
                                             Vec4<float> *, cudaStream_t);
 template void launch_assemble<double, double>(const DevSym &, const double *, const Vec4<double> *, double *,
                                               double *, Vec4<double> *, cudaStream_t);
-template void launch_factor_level<float>(const DevSym &, int, int, float *, float *, float *, float *, float *,
-                                         float *, int *, cudaStream_t);
-template void launch_factor_level<double>(const DevSym &, int, int, double *, double *, double *, double *,
-                                          double *, double *, int *, cudaStream_t);
+template void launch_factor_step<float>(const DevSym &, const FactorLaunch &, const FItem *, float *, float *,
+                                        float *, float *, float *, float *, int *, cudaStream_t);
+template void launch_factor_step<double>(const DevSym &, const FactorLaunch &, const FItem *, double *, double *,
+                                         double *, double *, double *, double *, int *, cudaStream_t);
 template void launch_local_step<float>(const DevSym &, const float *, const Vec4<float> *, const Vec4<float> *,
                                        Vec4<float> *, cudaStream_t);
 template void launch_local_step<double>(const DevSym &, const double *, const Vec4<double> *, const Vec4<double> *,

@@ -23,7 +23,8 @@ template <typename T> struct __align__(4 * sizeof(T)) Vec4 { T x, y, z, w; };
 constexpr int kErrNotSpd = 1;
 constexpr int kErrTimeout = 2;
 
-// Bound on the polls of one in-kernel wait (each poll sleeps ~100 ns).
+// Bound on the polls of one in-kernel wait (each poll sleeps 20-200 ns, so
+// the bound is a few seconds).
 constexpr unsigned kSpinLimit = 1u << 24;
 
 struct DevTopo {
@@ -35,7 +36,7 @@ struct DevTopo {
 
 struct DevSym {
     int V, m, S, nnz;
-    int max_ldx, max_ld21;
+    int max_ldx, max_ld21, max_ncol;
     const int32_t *drow, *dcol, *dent, *oldidx;
     const int64_t *amap, *dmap;
     const SnInfo *sn;
@@ -60,11 +61,12 @@ void launch_setup_vertices(const DevSym &s, const double *rest_xyz, const double
 template <typename TF, typename T>
 void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc64, TF *Lval, double *diag64,
                      Vec4<T> *bfixed, cudaStream_t st);
-// multifrontal Cholesky of one level of the supernodal tree; also writes
-// X = inverse of L11 and the aligned L21 copy the solves read
+// one launch of the multifrontal Cholesky plan (Symbolic::fplan); the last
+// launches of a level also write X = inverse of L11 and the aligned copies of
+// L21 and L21^T that the solves read
 template <typename TF>
-void launch_factor_level(const DevSym &s, int level_begin, int level_count, TF *Lval, TF *Upd, TF *Dinv, TF *X,
-                         TF *L21, TF *L21T, int *err, cudaStream_t st);
+void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *items, TF *Lval, TF *Upd, TF *Dinv,
+                        TF *X, TF *L21, TF *L21T, int *err, cudaStream_t st);
 // local step: covariance + rotation fit (estimateRotations arap.h:354-384)
 template <typename T>
 void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *pc, Vec4<T> *R,

@@ -438,6 +438,54 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         for (int s = 0; s < S; ++s) sym.level_sn[fill[sym.sn[s].level]++] = s;
     }
     if (S == 0) sym.level_ptr.assign(1, 0);
+    // factorisation launch plan
+    {
+        const int nlev = (int)sym.level_ptr.size() - 1;
+        auto add = [&](int kind, int jb, const std::vector<FItem> &items) {
+            if (items.empty()) return;
+            sym.fplan.push_back({kind, jb, (int32_t)sym.fitems.size(), (int32_t)items.size()});
+            sym.fitems.insert(sym.fitems.end(), items.begin(), items.end());
+        };
+        constexpr int kSlice = 32, kRowTile = 64, kTileU = 64;
+        for (int l = 0; l < nlev; ++l) {
+            std::vector<FItem> it;
+            int nblk_max = 0;
+            for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; ++q) {
+                const int sidx = sym.level_sn[q];
+                const SnInfo &d = sym.sn[sidx];
+                nblk_max = std::max(nblk_max, (d.ncol + kDiagBlock - 1) / kDiagBlock);
+                if (d.child_begin == d.child_end) continue;
+                for (int lo = 0; lo < d.nrow; lo += kSlice) it.push_back({sidx, lo, std::min(d.nrow, lo + kSlice), 0});
+            }
+            add(kFea, 0, it);
+            for (int jb = 0; jb < nblk_max; ++jb) {
+                std::vector<FItem> up, dt;
+                for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; ++q) {
+                    const int sidx = sym.level_sn[q];
+                    const SnInfo &d = sym.sn[sidx];
+                    const int j0 = jb * kDiagBlock;
+                    if (j0 >= d.ncol) continue;
+                    dt.push_back({sidx, 0, 0, 0});
+                    if (jb > 0)
+                        for (int rt = 0; j0 + rt * kRowTile < d.nrow; ++rt) up.push_back({sidx, rt, 0, 0});
+                }
+                add(kFupd, jb, up);
+                add(kFdt, jb, dt);
+            }
+            std::vector<FItem> sy, fx;
+            for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; ++q) {
+                const int sidx = sym.level_sn[q];
+                const SnInfo &d = sym.sn[sidx];
+                const int nb = d.nrow - d.ncol;
+                const int nt = (nb + kTileU - 1) / kTileU;
+                for (int rt = 0; rt < nt; ++rt)
+                    for (int ct = 0; ct <= rt; ++ct) sy.push_back({sidx, rt, ct, 0});
+                for (int jb = 0; jb * kDiagBlock < d.ncol; ++jb) fx.push_back({sidx, jb, 0, 0});
+            }
+            add(kFsyrk, 0, sy);
+            add(kFx, 0, fx);
+        }
+    }
     // assembly maps: L_kk and L_lk = -w_kl (l > k, both free) into the panels
     sym.amap.assign(nnz, -1);
     sym.dmap.assign(m, -1);

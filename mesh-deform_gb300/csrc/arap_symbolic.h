@@ -62,6 +62,23 @@ struct SnInfo {
     int64_t l21t_off;    // L21^T, nb columns of ldx rows
 };
 
+// One CTA's share of a factorisation launch: supernode and sub-range (meaning
+// depends on the launch kind, see FactorLaunch).
+struct FItem {
+    int32_t sn, a, b, c;
+};
+
+// Factorisation launch plan, level by level (leaves first):
+//   kFea   extend-add, item = (sn, first parent column, end parent column)
+//   kFupd  left-looking update of block column jb, item = (sn, row tile)
+//   kFdt   diagonal block jb: factor, invert, solve the rows below, item = (sn)
+//   kFsyrk Schur complement U -= L21 L21^T, item = (sn, row tile, column tile)
+//   kFx    X = inv(L11) column block jb and the solve copies, item = (sn, jb)
+enum FactorKind { kFea = 0, kFupd = 1, kFdt = 2, kFsyrk = 3, kFx = 4 };
+struct FactorLaunch {
+    int32_t kind, jb, item_off, count;
+};
+
 struct Symbolic {
     int V = 0, m = 0;                 // vertices, free vertices
     std::vector<uint8_t> constrained; // V
@@ -87,6 +104,8 @@ struct Symbolic {
     int64_t l21t_size = 0;
     int64_t factor_nnz = 0;           // nonzeros of the scalar factor (from the etree)
     double factor_flops = 0.0;        // dense flops of the supernodal factorisation
+    std::vector<FItem> fitems;
+    std::vector<FactorLaunch> fplan;
     // assembly maps into the factor array
     std::vector<int64_t> amap;        // per device entry: destination of -w (or -1)
     std::vector<int64_t> dmap;        // per free device row: destination of the diagonal
