@@ -187,6 +187,12 @@ int prepare_symbolic(arap_ctx *ctx) {
     CK(ctx->flags.ensure(2 * sizeof(unsigned) * (size_t)std::max(s.S, 1)));
     CK(cudaMemsetAsync(ctx->ticket.p, 0, 2 * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
+    // the solve kernels give each thread one 4-row quad of a front (at most
+    // 1024 rows) and stream whole columns through 16 KB chunks
+    if (s.max_ldx > 1024 || s.max_ld21 > 1024)
+        return fail(ctx, ARAP_ERR_UNSUPPORTED,
+                    "supernode front of " + std::to_string(std::max(s.max_ldx, s.max_ld21)) +
+                        " rows exceeds the solve kernels' limit of 1024");
     const size_t b32 = solve_smem_bytes(s.max_ldx, s.max_ld21, 4), b64 = solve_smem_bytes(s.max_ldx, s.max_ld21, 8);
     if (b64 > 227 * 1024)
         return fail(ctx, ARAP_ERR_UNSUPPORTED,

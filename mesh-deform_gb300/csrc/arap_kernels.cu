@@ -181,7 +181,6 @@ __global__ void k_assemble(int m, const int32_t *__restrict__ drow, const int32_
 
 constexpr int kFactorThreads = 256;
 constexpr int kTile = 64;   // rows of an update tile
-constexpr int kSlice = 32;  // parent columns of one extend-add item
 
 // Front of supernode d: the nrow x ncol panel P (column-major, ld nrow; rows are
 // the supernode's columns then its struct rows) and the nb x nb update matrix U.
@@ -682,101 +681,112 @@ k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ 
 
 // ---------------------------------------------------------------------------
 // supernodal triangular solves
+//
+// One CTA per supernode, one launch per sweep. The CTA's matrices (forward: X
+// then L21; backward: L21^T then X^T, all column-major with 16-byte aligned
+// columns) are streamed through two shared-memory buffers by TMA bulk copies
+// (cp.async.bulk + mbarrier). The first two chunks are requested before the
+// CTA waits for the supernodes it depends on, so the copies overlap the wait.
+// Threads own 4-row quads of the result; G groups of threads split each
+// chunk's columns and are reduced once at the end of a matrix.
 
 constexpr int kSolveThreads = 256;
-constexpr int kRedRows = 512;    // reduction scratch (rows x groups) of gemv_cols
-constexpr int kStageBytes = 40 * 1024;  // shared-memory staging of one supernode's matrices
+constexpr int kChunkBytes = 16 * 1024;
+constexpr int kRedRows = 4 * kSolveThreads;  // G * 4 * NQ <= 4 * threads
 
-// Four consecutive elements from a 16-byte aligned address (shared or global).
-__device__ __forceinline__ void load4(const float *p, float v[4]) {
-    const float4 a = *reinterpret_cast<const float4 *>(p);
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ void load4(const double *p, double v[4]) {
-    const double2 a = reinterpret_cast<const double2 *>(p)[0];
-    const double2 b = reinterpret_cast<const double2 *>(p)[1];
-    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bulk copy global -> shared (both 16-byte aligned, bytes a multiple of 16),
+// completion counted on `bar`.
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
 
-// Asynchronous copy of `bytes` (a multiple of 16, both ends 16-byte aligned)
-// from global to shared memory by the whole CTA; completes at cp_async_wait.
-__device__ __forceinline__ void cp_async_bulk16(void *smem, const void *gmem, int64_t bytes) {
-    const unsigned base = (unsigned)__cvta_generic_to_shared(smem);
-    const char *g = static_cast<const char *>(gmem);
-    for (int64_t off = (int64_t)threadIdx.x * 16; off < bytes; off += (int64_t)blockDim.x * 16)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(base + (unsigned)off), "l"(g + off) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-constexpr int kTriNone = 0, kTriLower = 1, kTriUpper = 2;
-
-// acc(4 rows x 3 components) += sum_{c in [c0,c1)} M[c*ld + 4q..4q+3] * v[c],
-// loads issued eight columns at a time so that they are in flight together.
+// The chunks of one task: matrix A (columns [0, CA), leading dimension ldA)
+// then matrix B (columns [0, CB), ldB), each cut into column ranges of at most
+// kChunkBytes.
 template <typename T>
-__device__ __forceinline__ void axpy_quad(const T *__restrict__ M, int ld, int q, int c0, int c1, const Vec4<T> *v,
-                                          T ax[4], T ay[4], T az[4]) {
-    int c = c0;
-    for (; c + 8 <= c1; c += 8) {
-        T m[8][4];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) load4(M + (int64_t)(c + u) * ld + 4 * q, m[u]);
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const Vec4<T> vc = v[c + u];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) { ax[k] += m[u][k] * vc.x; ay[k] += m[u][k] * vc.y; az[k] += m[u][k] * vc.z; }
-        }
+struct ChunkPlan {
+    const T *A, *B;
+    int ldA, ldB, CA, CB, cwA, cwB, nA, nB;
+    __device__ void init(const T *a, int lda, int ca, const T *b, int ldb, int cb) {
+        A = a; B = b; ldA = lda; ldB = ldb; CA = ca; CB = cb;
+        cwA = max(1, kChunkBytes / (lda * (int)sizeof(T)));
+        cwB = ldb > 0 ? max(1, kChunkBytes / (ldb * (int)sizeof(T))) : 1;
+        nA = (CA + cwA - 1) / cwA;
+        nB = CB > 0 ? (CB + cwB - 1) / cwB : 0;
     }
-    for (; c < c1; ++c) {
-        T m4[4];
-        load4(M + (int64_t)c * ld + 4 * q, m4);
-        const Vec4<T> vc = v[c];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) { ax[k] += m4[k] * vc.x; ay[k] += m4[k] * vc.y; az[k] += m4[k] * vc.z; }
+    __device__ int total() const { return nA + nB; }
+    // first column, number of columns and source of chunk k
+    __device__ void chunk(int k, int &c0, int &cn, const T *&src, int &ld) const {
+        if (k < nA) { c0 = k * cwA; cn = min(cwA, CA - c0); src = A + (int64_t)c0 * ldA; ld = ldA; }
+        else { const int j = k - nA; c0 = j * cwB; cn = min(cwB, CB - c0); src = B + (int64_t)c0 * ldB; ld = ldB; }
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ void issue_chunk(const ChunkPlan<T> &pl, int k, T *buf, uint64_t *bar) {
+    int c0, cn, ld;
+    const T *src;
+    pl.chunk(k, c0, cn, src, ld);
+    const unsigned bytes = (unsigned)(cn * ld * (int)sizeof(T));
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // buffer reads done before the async write
+    mbar_expect_tx(bar, bytes);
+    tma_load_1d(buf, src, bytes, bar);
+}
+
+// Bounded wait for a buffer's bytes. On expiry it records kErrTimeout and
+// waits once more (bounded) so that no copy is still writing into shared
+// memory when the CTA moves on.
+__device__ __forceinline__ void wait_chunk(uint64_t *bar, unsigned parity, int *err) {
+    for (unsigned it = 0; it < kSpinLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return;
+    if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
+    for (unsigned it = 0; it < kSpinLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return;
+}
+
+// acc[k] += sum over this thread's columns of the chunk of M(4q+k, c) v[c0+c]
+template <typename T>
+__device__ __forceinline__ void chunk_axpy(const T *buf, int ld, int cn, int c0, int q, int g, int G,
+                                           const Vec4<T> *v, T ax[4], T ay[4], T az[4]) {
+    for (int c = g; c < cn; c += G) {
+        const Vec4<T> m = *reinterpret_cast<const Vec4<T> *>(buf + (int64_t)c * ld + 4 * q);
+        const Vec4<T> vc = v[c0 + c];
+        ax[0] += m.x * vc.x; ay[0] += m.x * vc.y; az[0] += m.x * vc.z;
+        ax[1] += m.y * vc.x; ay[1] += m.y * vc.y; az[1] += m.y * vc.z;
+        ax[2] += m.z * vc.x; ay[2] += m.z * vc.y; az[2] += m.z * vc.z;
+        ax[3] += m.w * vc.x; ay[3] += m.w * vc.y; az[3] += m.w * vc.z;
     }
 }
 
-// out[r] (-)= sum_{c < C} M[c*ld + r] * v[c] for r < R (M column-major, ld a
-// multiple of 4, columns 16-byte aligned, rows R..ld-1 zero). TRI skips the
-// column range that is zero for a row quad: lower (c <= r) or upper (c >= r)
-// triangular M. Threads own 4-row quads; when there are fewer quads than
-// threads, G groups of threads split the columns and reduce through `red`.
-// Ends with a barrier.
-template <typename T, int TRI, bool SUB>
-__device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R, int C, const Vec4<T> *v,
-                                          Vec4<T> *out, Vec4<T> *red) {
+// Sums the G partial results into out (SUB: out -= sum). Ends with a barrier.
+template <typename T, bool SUB>
+__device__ __forceinline__ void reduce_groups(int NQ, int G, int q, int g, const T ax[4], const T ay[4],
+                                              const T az[4], Vec4<T> *red, Vec4<T> *out) {
     const int tid = threadIdx.x;
-    const int NQ = (R + 3) >> 2;
-    int G = NQ > 0 ? kSolveThreads / NQ : 1;
-    G = max(1, min(G, kRedRows / max(4 * NQ, 1)));
-    G = min(G, 4);
-    if (G == 1) {
-        for (int q = tid; q < NQ; q += kSolveThreads) {
-            const int c0 = TRI == kTriUpper ? 4 * q : 0;
-            const int c1 = TRI == kTriLower ? min(C, 4 * q + 4) : C;
-            T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-            axpy_quad(M, ld, q, c0, c1, v, ax, ay, az);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                Vec4<T> &o = out[4 * q + k];
-                if (SUB) { o.x -= ax[k]; o.y -= ay[k]; o.z -= az[k]; }
-                else o = {ax[k], ay[k], az[k], (T)0};
-            }
-        }
-        __syncthreads();
-        return;
-    }
-    const int q = tid % NQ, g = tid / NQ;
-    if (g < G) {
-        const int chunk = (C + G - 1) / G;
-        const int c0 = max(g * chunk, TRI == kTriUpper ? 4 * q : 0);
-        const int c1 = min(TRI == kTriLower ? min(C, 4 * q + 4) : C, g * chunk + chunk);
-        T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-        axpy_quad(M, ld, q, c0, c1, v, ax, ay, az);
+    if (g < G && q < NQ)
 #pragma unroll
         for (int k = 0; k < 4; ++k) red[g * 4 * NQ + 4 * q + k] = {ax[k], ay[k], az[k], (T)0};
-    }
     __syncthreads();
     for (int rr = tid; rr < 4 * NQ; rr += kSolveThreads) {
         T sx = 0, sy = 0, sz = 0;
@@ -791,49 +801,34 @@ __device__ __forceinline__ void gemv_cols(const T *__restrict__ M, int ld, int R
     __syncthreads();
 }
 
-// Shared-memory layout of the solve kernels (dynamic): the staging area for
-// one supernode's matrices, two vectors of max_ldx rows, one of max_ld21 rows
-// and the kRedRows reduction scratch.
+__device__ __forceinline__ int groups_for(int NQ) {
+    return NQ >= kSolveThreads ? 1 : max(1, kSolveThreads / max(NQ, 1));
+}
+
+// Shared memory of a solve CTA (dynamic): two chunk buffers, three vectors
+// (two of max_ldx rows, one of max_ld21 rows) and the reduction scratch.
 struct SolveSmem {
     int ldx_max, ld21_max;
 };
 
-// Stages the matrices a supernode's solve reads (A: a_elems, then B: b_elems
-// elements) into shared memory when they fit, asynchronously. Returns the
-// pointers the GEMVs should read (shared when staged, global otherwise).
-template <typename T>
-__device__ __forceinline__ void stage_pair(T *stage, const T *A, int64_t a_elems, const T *B, int64_t b_elems,
-                                           const T *&ra, const T *&rb) {
-    const int64_t cap = kStageBytes / (int64_t)sizeof(T);
-    ra = A;
-    rb = B;
-    if (a_elems <= cap) {
-        cp_async_bulk16(stage, A, a_elems * (int64_t)sizeof(T));
-        ra = stage;
-        if (a_elems + b_elems <= cap) {
-            cp_async_bulk16(stage + a_elems, B, b_elems * (int64_t)sizeof(T));
-            rb = stage + a_elems;
-        }
-    }
-    cp_async_commit();
-}
-
 // Forward: for supernode s (children first), f = [b(cols); 0] plus the
 // children's update vectors; y = X f(cols); u_s = f(struct) - L21 y goes to
-// the parent. Tickets are handed out in level order (leaves first), so a CTA
-// only waits for supernodes of lower levels, which started before it.
+// the parent. Tickets follow `order` (level by level, leaves first), so a CTA
+// only waits for CTAs that started before it.
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads, 3)
 k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
             const int32_t *__restrict__ child, const int32_t *__restrict__ relind, const T *__restrict__ Xall,
             const T *__restrict__ L21all, Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec,
             unsigned long long *ticket, unsigned *flags, int *err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *stage = reinterpret_cast<T *>(smem_raw);
-    Vec4<T> *fc = reinterpret_cast<Vec4<T> *>(smem_raw + kStageBytes);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T *buf0 = reinterpret_cast<T *>(smem_raw);
+    T *buf1 = reinterpret_cast<T *>(smem_raw + kChunkBytes);
+    Vec4<T> *fc = reinterpret_cast<Vec4<T> *>(smem_raw + 2 * kChunkBytes);
     Vec4<T> *yv = fc + lay.ldx_max;
     Vec4<T> *fb = yv + lay.ldx_max;
     Vec4<T> *red = fb + lay.ld21_max;
+    __shared__ __align__(8) uint64_t bars[2];
     __shared__ int s_task;
     __shared__ unsigned s_epoch;
     const int tid = threadIdx.x;
@@ -841,15 +836,22 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
         const unsigned long long t = atomicAdd(ticket, 1ull);
         s_task = order[(int)(t % (unsigned long long)S)];
         s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     const int s = s_task;
     const unsigned epoch = s_epoch;
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
-    const T *Xs, *Ls;
-    stage_pair(stage, Xall + d.x_off, (int64_t)d.ldx * nc, L21all + d.l21_off, (int64_t)d.ld21 * nc, Xs, Ls);
-    // everything that does not depend on the children is read before waiting
+    ChunkPlan<T> pl;
+    pl.init(Xall + d.x_off, d.ldx, nc, L21all + d.l21_off, d.ld21, nb > 0 ? nc : 0);
+    const int ntot = pl.total();
+    if (tid == 0) {
+        issue_chunk(pl, 0, buf0, &bars[0]);
+        if (ntot > 1) issue_chunk(pl, 1, buf1, &bars[1]);
+    }
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
     for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
@@ -870,10 +872,32 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
         }
         __syncthreads();
     }
-    cp_async_wait();
-    __syncthreads();
-    gemv_cols<T, kTriLower, false>(Xs, d.ldx, nc, nc, fc, yv, red);
-    if (nb > 0) gemv_cols<T, kTriNone, true>(Ls, d.ld21, nb, nc, yv, fb, red);
+    // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb)
+    const int NQa = (nc + 3) >> 2, Ga = groups_for(NQa);
+    const int NQb = (nb + 3) >> 2, Gb = groups_for(NQb);
+    T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+    for (int k = 0; k < ntot; ++k) {
+        T *buf = (k & 1) ? buf1 : buf0;
+        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        int c0, cn, ld;
+        const T *src;
+        pl.chunk(k, c0, cn, src, ld);
+        if (k < pl.nA) {
+            for (int w = tid; w < NQa * Ga; w += kSolveThreads)
+                chunk_axpy(buf, ld, cn, c0, w % NQa, w / NQa, Ga, fc, ax, ay, az);
+        } else {
+            for (int w = tid; w < NQb * Gb; w += kSolveThreads)
+                chunk_axpy(buf, ld, cn, c0, w % NQb, w / NQb, Gb, yv, ax, ay, az);
+        }
+        __syncthreads();
+        if (tid == 0 && k + 2 < ntot) issue_chunk(pl, k + 2, buf, &bars[k & 1]);
+        if (k == pl.nA - 1) {
+            reduce_groups<T, false>(NQa, Ga, tid % NQa, tid / NQa, ax, ay, az, red, yv);
+#pragma unroll
+            for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+        }
+    }
+    if (pl.nB > 0) reduce_groups<T, true>(NQb, Gb, tid % max(NQb, 1), tid / max(NQb, 1), ax, ay, az, red, fb);
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
     __threadfence();
@@ -882,20 +906,23 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
 }
 
 // Backward: for supernode s (root first), z = y - L21^T x(struct) and
-// x(cols) = X^T z, both as column sweeps over the stored transposes.
-// mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k, pc32[k] = float(pc64[k]).
+// x(cols) = X^T z, streaming the stored transposes (L21^T: nb columns of ldx
+// rows; X^T: nc columns of ldx rows). mode 0: pc64[k] = x_k;
+// mode 1: pc64[k] += x_k, pc32[k] = float(pc64[k]).
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads, 3)
 k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
             const int32_t *__restrict__ rows, const T *__restrict__ Xall, const T *__restrict__ L21Tall,
             Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode,
             unsigned long long *ticket, unsigned *flags, int *err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *stage = reinterpret_cast<T *>(smem_raw);
-    Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw + kStageBytes);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T *buf0 = reinterpret_cast<T *>(smem_raw);
+    T *buf1 = reinterpret_cast<T *>(smem_raw + kChunkBytes);
+    Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw + 2 * kChunkBytes);
     Vec4<T> *xv = zv + lay.ldx_max;
     Vec4<T> *gb = xv + lay.ldx_max;
     Vec4<T> *red = gb + lay.ld21_max;
+    __shared__ __align__(8) uint64_t bars[2];
     __shared__ int s_task;
     __shared__ unsigned s_epoch;
     const int tid = threadIdx.x;
@@ -903,14 +930,24 @@ k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
         const unsigned long long t = atomicAdd(ticket, 1ull);
         s_task = order[S - 1 - (int)(t % (unsigned long long)S)];
         s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     const int s = s_task;
     const unsigned epoch = s_epoch;
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
-    const T *XTs, *LTs;
-    stage_pair(stage, Xall + d.xt_off, (int64_t)d.ldx * nc, L21Tall + d.l21t_off, (int64_t)d.ldx * nb, XTs, LTs);
+    ChunkPlan<T> pl;
+    if (nb > 0) pl.init(L21Tall + d.l21t_off, d.ldx, nb, Xall + d.xt_off, d.ldx, nc);
+    else pl.init(Xall + d.xt_off, d.ldx, nc, nullptr, 0, 0);
+    const int ntot = pl.total();
+    const int nA = nb > 0 ? pl.nA : 0;  // chunks of L21^T
+    if (tid == 0) {
+        issue_chunk(pl, 0, buf0, &bars[0]);
+        if (ntot > 1) issue_chunk(pl, 1, buf1, &bars[1]);
+    }
     const int32_t *rs = rows + d.rows_off;
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
@@ -923,10 +960,27 @@ k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     for (int u = 0; u < 4; ++u)
         if (tid + u * kSolveThreads < nb) gb[tid + u * kSolveThreads] = ldcg4(sol + myrow[u]);
     for (int i = tid + 4 * kSolveThreads; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
-    cp_async_wait();
     __syncthreads();
-    if (nb > 0) gemv_cols<T, kTriNone, true>(LTs, d.ldx, nc, nb, gb, zv, red);  // z = y - L21^T g
-    gemv_cols<T, kTriUpper, false>(XTs, d.ldx, nc, nc, zv, xv, red);             // x = X^T z
+    // phase A (nb > 0): z -= L21^T g; phase B: x = X^T z; both have nc rows
+    const int NQ = (nc + 3) >> 2, G = groups_for(NQ);
+    T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+    for (int k = 0; k < ntot; ++k) {
+        T *buf = (k & 1) ? buf1 : buf0;
+        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        int c0, cn, ld;
+        const T *src;
+        pl.chunk(k, c0, cn, src, ld);
+        const Vec4<T> *v = (k < nA) ? gb : zv;
+        for (int w = tid; w < NQ * G; w += kSolveThreads) chunk_axpy(buf, ld, cn, c0, w % NQ, w / NQ, G, v, ax, ay, az);
+        __syncthreads();
+        if (tid == 0 && k + 2 < ntot) issue_chunk(pl, k + 2, buf, &bars[k & 1]);
+        if (k == nA - 1) {
+            reduce_groups<T, true>(NQ, G, tid % NQ, tid / NQ, ax, ay, az, red, zv);
+#pragma unroll
+            for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+        }
+    }
+    reduce_groups<T, false>(NQ, G, tid % NQ, tid / NQ, ax, ay, az, red, xv);
     for (int i = tid; i < nc; i += kSolveThreads) {
         const Vec4<T> x = xv[i];
         const int k = d.first + i;
@@ -1053,7 +1107,7 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 }
 
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
-    return (size_t)kStageBytes + (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
+    return (size_t)2 * kChunkBytes + (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
 }
 
 template <typename T>
