@@ -743,6 +743,16 @@ struct ChunkPlan {
     }
 };
 
+// Asks the TMA unit to pull chunk k into L2 (no shared memory involved).
+template <typename T>
+__device__ __forceinline__ void prefetch_chunk_l2(const ChunkPlan<T> &pl, int k) {
+    int c0, cn, ld;
+    const T *src;
+    pl.chunk(k, c0, cn, src, ld);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"((unsigned)(cn * ld * (int)sizeof(T)))
+                 : "memory");
+}
+
 template <typename T>
 __device__ __forceinline__ void issue_chunk(const ChunkPlan<T> &pl, int k, T *buf, uint64_t *bar) {
     int c0, cn, ld;
@@ -851,26 +861,70 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     if (tid == 0) {
         issue_chunk(pl, 0, buf0, &bars[0]);
         if (ntot > 1) issue_chunk(pl, 1, buf1, &bars[1]);
+        for (int k = 2; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
     for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
+    // the children's entries of this thread (child-major list, kPull per thread):
+    // positions are read before waiting, update vectors in one round trip after
+    constexpr int kPull = 4;
+    int pci[kPull], ppos[kPull], puo[kPull];
+    {
+        int base = 0, u = 0;
+        for (int ci = d.child_begin; ci < d.child_end && u < kPull; ++ci) {
+            const SnInfo c = sn[child[ci]];
+            const int nbc = c.nrow - c.ncol;
+            for (int i = tid - base; i < nbc && u < kPull; i += kSolveThreads) {
+                if (i < 0) continue;
+                pci[u] = ci;
+                ppos[u] = relind[c.relind_off + i];
+                puo[u] = (int)c.uvec_off + i;
+                ++u;
+            }
+            base += nbc;
+        }
+        for (; u < kPull; ++u) pci[u] = -1;
+    }
+    int total_children_rows = 0;
+    for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+        const SnInfo c = sn[child[ci]];
+        total_children_rows += c.nrow - c.ncol;
+    }
     if (tid == 0)
         for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
     __syncthreads();
-    for (int ci = d.child_begin; ci < d.child_end; ++ci) {
-        const SnInfo c = sn[child[ci]];
-        const int nbc = c.nrow - c.ncol;
-        const int32_t *ri = relind + c.relind_off;
-        for (int i = tid; i < nbc; i += kSolveThreads) {
-            const Vec4<T> u = ldcg4(uvec + c.uvec_off + i);
-            const int pos = ri[i];
-            Vec4<T> &t = pos < nc ? fc[pos] : fb[pos - nc];
-            t.x += u.x;
-            t.y += u.y;
-            t.z += u.z;
+    if (total_children_rows <= kPull * kSolveThreads) {
+        Vec4<T> pu[kPull];
+#pragma unroll
+        for (int u = 0; u < kPull; ++u)
+            if (pci[u] >= 0) pu[u] = ldcg4(uvec + puo[u]);
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) {  // children in order
+#pragma unroll
+            for (int u = 0; u < kPull; ++u) {
+                if (pci[u] != ci) continue;
+                Vec4<T> &t = ppos[u] < nc ? fc[ppos[u]] : fb[ppos[u] - nc];
+                t.x += pu[u].x;
+                t.y += pu[u].y;
+                t.z += pu[u].z;
+            }
+            __syncthreads();
         }
-        __syncthreads();
+    } else {
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+            const SnInfo c = sn[child[ci]];
+            const int nbc = c.nrow - c.ncol;
+            const int32_t *ri = relind + c.relind_off;
+            for (int i = tid; i < nbc; i += kSolveThreads) {
+                const Vec4<T> u = ldcg4(uvec + c.uvec_off + i);
+                const int pos = ri[i];
+                Vec4<T> &t = pos < nc ? fc[pos] : fb[pos - nc];
+                t.x += u.x;
+                t.y += u.y;
+                t.z += u.z;
+            }
+            __syncthreads();
+        }
     }
     // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb)
     const int NQa = (nc + 3) >> 2, Ga = groups_for(NQa);
@@ -947,6 +1001,7 @@ k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     if (tid == 0) {
         issue_chunk(pl, 0, buf0, &bars[0]);
         if (ntot > 1) issue_chunk(pl, 1, buf1, &bars[1]);
+        for (int k = 2; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     const int32_t *rs = rows + d.rows_off;
     for (int i = tid; i < d.ldx; i += kSolveThreads)
