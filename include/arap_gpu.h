@@ -91,6 +91,21 @@ int arap_set_constraints(arap_ctx *ctx, int32_t n, const int32_t *indices, const
    the reference's deform returns false. */
 int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz);
 
+/* Many handle poses of one mesh and one constrained-vertex set in one pass,
+   the pattern of DeformationUtil::updateConstraints
+   (inc/deform/deformation_util.h:48-57), where every pose moves the same
+   handles. For each pose p: a dirty deform from the rest pose with the
+   constrained vertices at targets[p], `iterations` local/global iterations
+   (arap.h:102-129). targets: n_poses x n_constrained x 3 doubles, the
+   constrained vertices (as given to arap_set_constraints) in ascending vertex
+   order; NULL reuses the targets of the previous call, already on the device.
+   All poses share the cotan weights and the Cholesky factor of the current
+   rest pose and constraint set; the constraint targets given to
+   arap_set_constraints are not used. MIXED precision only. out_xyz:
+   n_poses x V x 3 doubles (NULL keeps the result on the device). */
+int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
+                      double *out_xyz);
+
 /* Marks the context dirty without uploading anything: the next arap_deform
    rebuilds the problem from the rest pose and targets already on the device.
    Used to time a dirty deform with its inputs resident in device memory. */

@@ -68,6 +68,7 @@ SIGNATURES = {
     "arap_get_kernel_stats": (C.c_int, [_P, _I32, _dp, _lp]),
     "arap_get_kernel_model": (C.c_int, [_P, _I32, _dp, _dp]),
     "arap_cotan_weights_static": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _I32, _P, _P]),
+    "arap_deform_poses": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
 }
 
 KERNEL_CLASSES = ["weights", "assemble", "factor", "local", "rhs", "residual", "solve_fwd", "solve_bwd", "gather"]
@@ -167,6 +168,23 @@ class ArapContext:
     def deform(self, iterations: int, want_output: bool = True) -> np.ndarray | None:
         out = np.empty((self.V, 3), np.float64) if want_output else None
         self._check(self.deform_rc(iterations, out))
+        return out
+
+    def deform_poses_rc(self, targets, iterations: int, out=None) -> int:
+        """arap_deform_poses: targets P x n_constrained x 3 (constrained vertices
+        in ascending order) or None to reuse the device copy."""
+        if targets is None:
+            return self.lib.arap_deform_poses(self.h, int(self._nposes), None, int(iterations),
+                                             _f64(out) if out is not None else None)
+        t = np.ascontiguousarray(targets, dtype=np.float64)
+        self._nposes = t.shape[0]
+        return self.lib.arap_deform_poses(self.h, int(t.shape[0]), _f64(t), int(iterations),
+                                         _f64(out) if out is not None else None)
+
+    def deform_poses(self, targets, iterations: int) -> np.ndarray:
+        t = np.ascontiguousarray(targets, dtype=np.float64)
+        out = np.empty((t.shape[0], self.V, 3), np.float64)
+        self._check(self.deform_poses_rc(t, iterations, out))
         return out
 
     def invalidate(self):

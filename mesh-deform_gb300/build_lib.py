@@ -1,10 +1,11 @@
 """Builds libarap_gb300.so (the C ABI of include/arap_gpu.h) for sm_103a.
 
-Four translation units compiled in parallel, then linked with the static CUDA
+Five translation units compiled in parallel, then linked with the static CUDA
 runtime:
   csrc/arap_kernels.cu   the sm_103a kernels (nvcc)
   csrc/arap_context.cu   context state and the C ABI (nvcc)
   csrc/arap_noalloc.cu   cotan weights with static scratch (nvcc)
+  csrc/arap_batch.cu     many poses of one mesh in one pass (nvcc)
   csrc/arap_symbolic.cpp host symbolic analysis (g++)
 The library is built in-tree (next to this file) and is git-ignored.
 """
@@ -32,9 +33,10 @@ SOURCES = [
     ("nvcc", CSRC / "arap_kernels.cu"),
     ("nvcc", CSRC / "arap_context.cu"),
     ("nvcc", CSRC / "arap_noalloc.cu"),
+    ("nvcc", CSRC / "arap_batch.cu"),
     ("g++", CSRC / "arap_symbolic.cpp"),
 ]
-HEADERS = [CSRC / "arap_kernels.h", CSRC / "arap_symbolic.h", ROOT / "include" / "arap_gpu.h"]
+HEADERS = [CSRC / "arap_kernels.h", CSRC / "arap_symbolic.h", CSRC / "arap_device.cuh", ROOT / "include" / "arap_gpu.h"]
 
 
 def nvcc() -> str:

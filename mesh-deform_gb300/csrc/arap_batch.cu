@@ -1,0 +1,577 @@
+// arap_batch.cu -- many handle poses of one mesh and constraint set in one
+// pass: the mixed-precision iteration of inc/deform/arap.h:122-129 for P poses
+// that share the cotan weights, the constrained Laplacian and its Cholesky
+// factor (the use pattern of inc/deform/deformation_util.h:48-57, where every
+// pose moves the same handles).
+//
+// Layout: per-vertex-per-pose arrays are vertex-major, element (k, p) at
+// k * P + p, so that a supernode's rows for a tile of poses are contiguous.
+// The triangular solves run one CTA per (supernode, tile of PT poses); every
+// 16 KB chunk of a supernode's matrices streamed into shared memory (TMA bulk
+// copies) serves PT poses.
+#include "arap_kernels.h"
+#include "arap_device.cuh"
+
+namespace arapgpu {
+
+namespace {
+
+constexpr int NB = kDiagBlock;
+constexpr int kThreads = 256;
+constexpr int kChunkBytes = 16 * 1024;
+constexpr int kMaxItems = 4;  // (row quad, pose) items per thread
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void wait_flag(const unsigned *p, unsigned target, int *err) {
+    for (unsigned it = 0; it < kSpinLimit; ++it) {
+        if (ld_acquire(p) >= target) return;
+        __nanosleep(it < 64 ? 20 : 200);
+    }
+    atomicOr(err, kErrTimeout);
+}
+__device__ __forceinline__ Vec4<float> ldcg4(const Vec4<float> *p) {
+    const float4 v = __ldcg(reinterpret_cast<const float4 *>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait; on expiry records kErrTimeout and waits once more (bounded) so
+// that no copy still writes into shared memory afterwards.
+__device__ __forceinline__ void wait_chunk(uint64_t *bar, unsigned parity, int *err) {
+    for (unsigned it = 0; it < kSpinLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return;
+    if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
+    for (unsigned it = 0; it < kSpinLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return;
+}
+
+// Column chunks of matrix A then matrix B (both column-major, 16-byte aligned
+// columns), each chunk at most kChunkBytes.
+struct Chunks {
+    const float *A, *B;
+    int ldA, ldB, CA, CB, cwA, cwB, nA, nB;
+    __device__ void init(const float *a, int lda, int ca, const float *b, int ldb, int cb) {
+        A = a; B = b; ldA = lda; ldB = ldb; CA = ca; CB = cb;
+        cwA = max(1, kChunkBytes / (lda * 4));
+        cwB = ldb > 0 ? max(1, kChunkBytes / (ldb * 4)) : 1;
+        nA = (CA + cwA - 1) / cwA;
+        nB = CB > 0 ? (CB + cwB - 1) / cwB : 0;
+    }
+    __device__ void chunk(int k, int &c0, int &cn, const float *&src, int &ld) const {
+        if (k < nA) { c0 = k * cwA; cn = min(cwA, CA - c0); src = A + (int64_t)c0 * ldA; ld = ldA; }
+        else { const int j = k - nA; c0 = j * cwB; cn = min(cwB, CB - c0); src = B + (int64_t)c0 * ldB; ld = ldB; }
+    }
+    __device__ void issue(int k, float *buf, uint64_t *bar) const {
+        int c0, cn, ld;
+        const float *src;
+        chunk(k, c0, cn, src, ld);
+        const unsigned bytes = (unsigned)(cn * ld * 4);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(buf)),
+                     "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                     : "memory");
+    }
+    __device__ void prefetch(int k) const {
+        int c0, cn, ld;
+        const float *src;
+        chunk(k, c0, cn, src, ld);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"((unsigned)(cn * ld * 4)) : "memory");
+    }
+};
+
+// acc[it][k] += sum_c M(4q+k, c) v[(c0+c)*PT + p] for the thread's items
+// (item w = tid + i*kThreads -> q = w / PT, p = w % PT, w < NQ*PT).
+template <int PT>
+__device__ __forceinline__ void chunk_gemm(const float *buf, int ld, int cn, int c0, int NQ, const Vec4<float> *v,
+                                           float acc[kMaxItems][4][3]) {
+#pragma unroll
+    for (int i = 0; i < kMaxItems; ++i) {
+        const int w = threadIdx.x + i * kThreads;
+        if (w >= NQ * PT) break;
+        const int q = w / PT, p = w % PT;
+        for (int c = 0; c < cn; ++c) {
+            const float4 m = *reinterpret_cast<const float4 *>(buf + c * ld + 4 * q);
+            const Vec4<float> f = v[(c0 + c) * PT + p];
+            acc[i][0][0] += m.x * f.x; acc[i][0][1] += m.x * f.y; acc[i][0][2] += m.x * f.z;
+            acc[i][1][0] += m.y * f.x; acc[i][1][1] += m.y * f.y; acc[i][1][2] += m.y * f.z;
+            acc[i][2][0] += m.z * f.x; acc[i][2][1] += m.z * f.y; acc[i][2][2] += m.z * f.z;
+            acc[i][3][0] += m.w * f.x; acc[i][3][1] += m.w * f.y; acc[i][3][2] += m.w * f.z;
+        }
+    }
+}
+
+// out[(4q+k)*PT + p] = acc (MODE 0), -= acc (MODE 1); zeroes acc.
+template <int PT, int MODE>
+__device__ __forceinline__ void store_items(int NQ, float acc[kMaxItems][4][3], Vec4<float> *out) {
+#pragma unroll
+    for (int i = 0; i < kMaxItems; ++i) {
+        const int w = threadIdx.x + i * kThreads;
+        if (w < NQ * PT) {
+            const int q = w / PT, p = w % PT;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                Vec4<float> &o = out[(4 * q + k) * PT + p];
+                if (MODE == 0) o = {acc[i][k][0], acc[i][k][1], acc[i][k][2], 0.f};
+                else { o.x -= acc[i][k][0]; o.y -= acc[i][k][1]; o.z -= acc[i][k][2]; }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[i][k][0] = acc[i][k][1] = acc[i][k][2] = 0.f;
+    }
+}
+
+struct BLayout {
+    int ldx_max, ld21_max;
+};
+
+// Forward solve for a tile of PT poses of one supernode (children first).
+template <int PT>
+__global__ void __launch_bounds__(kThreads)
+k_bsolve_fwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+             const int32_t *__restrict__ child, const int32_t *__restrict__ relind, const float *__restrict__ Xall,
+             const float *__restrict__ L21all, Vec4<float> *__restrict__ sol, Vec4<float> *__restrict__ uvec,
+             unsigned long long *ticket, unsigned *flags, int *err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float *buf[2] = {reinterpret_cast<float *>(smem_raw), reinterpret_cast<float *>(smem_raw + kChunkBytes)};
+    Vec4<float> *F = reinterpret_cast<Vec4<float> *>(smem_raw + 2 * kChunkBytes);
+    Vec4<float> *Y = F + lay.ldx_max * PT;
+    Vec4<float> *Fb = Y + lay.ldx_max * PT;
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_task, s_tile;
+    __shared__ unsigned s_epoch;
+    const int tid = threadIdx.x;
+    const unsigned long long ntask = (unsigned long long)S * T;
+    if (tid == 0) {
+        const unsigned long long t = atomicAdd(ticket, 1ull);
+        const int r = (int)(t % ntask);
+        s_task = order[r / T];
+        s_tile = r % T;
+        s_epoch = (unsigned)(t / ntask) + 1u;
+        mbar_init(&bars[0]);
+        mbar_init(&bars[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int s = s_task, tile = s_tile, p0 = tile * PT;
+    const unsigned epoch = s_epoch;
+    const SnInfo d = sn[s];
+    const int nc = d.ncol, nb = d.nrow - d.ncol;
+    Chunks pl;
+    pl.init(Xall + d.x_off, d.ldx, nc, L21all + d.l21_off, d.ld21, nb > 0 ? nc : 0);
+    const int ntot = pl.nA + pl.nB;
+    if (tid == 0) {
+        pl.issue(0, buf[0], &bars[0]);
+        if (ntot > 1) pl.issue(1, buf[1], &bars[1]);
+        for (int k = 2; k < ntot; ++k) pl.prefetch(k);
+    }
+    for (int e = tid; e < d.ldx * PT; e += kThreads) {
+        const int i = e / PT, p = e % PT;
+        F[e] = (i < nc && p0 + p < P) ? sol[(int64_t)(d.first + i) * P + p0 + p] : Vec4<float>{0.f, 0.f, 0.f, 0.f};
+    }
+    for (int e = tid; e < d.ld21 * PT; e += kThreads) Fb[e] = {0.f, 0.f, 0.f, 0.f};
+    if (tid == 0)
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + (int64_t)child[ci] * T + tile, epoch, err);
+    __syncthreads();
+    for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+        const SnInfo c = sn[child[ci]];
+        const int nbc = c.nrow - c.ncol;
+        const int32_t *ri = relind + c.relind_off;
+        for (int e = tid; e < nbc * PT; e += kThreads) {
+            const int i = e / PT, p = e % PT;
+            if (p0 + p >= P) continue;
+            const Vec4<float> u = ldcg4(uvec + (c.uvec_off + i) * P + p0 + p);
+            const int pos = ri[i];
+            Vec4<float> &t = pos < nc ? F[pos * PT + p] : Fb[(pos - nc) * PT + p];
+            t.x += u.x;
+            t.y += u.y;
+            t.z += u.z;
+        }
+        __syncthreads();
+    }
+    const int NQa = (nc + 3) >> 2, NQb = (nb + 3) >> 2;
+    float acc[kMaxItems][4][3];
+#pragma unroll
+    for (int i = 0; i < kMaxItems; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[i][k][0] = acc[i][k][1] = acc[i][k][2] = 0.f;
+    for (int k = 0; k < ntot; ++k) {
+        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        int c0, cn, ld;
+        const float *src;
+        pl.chunk(k, c0, cn, src, ld);
+        if (k < pl.nA) chunk_gemm<PT>(buf[k & 1], ld, cn, c0, NQa, F, acc);
+        else chunk_gemm<PT>(buf[k & 1], ld, cn, c0, NQb, Y, acc);
+        __syncthreads();
+        if (tid == 0 && k + 2 < ntot) pl.issue(k + 2, buf[k & 1], &bars[k & 1]);
+        if (k == pl.nA - 1) {
+            store_items<PT, 0>(NQa, acc, Y);
+            __syncthreads();
+        }
+    }
+    if (pl.nB > 0) {
+        store_items<PT, 1>(NQb, acc, Fb);
+        __syncthreads();
+    }
+    for (int e = tid; e < nc * PT; e += kThreads) {
+        const int i = e / PT, p = e % PT;
+        if (p0 + p < P) sol[(int64_t)(d.first + i) * P + p0 + p] = Y[e];
+    }
+    for (int e = tid; e < nb * PT; e += kThreads) {
+        const int i = e / PT, p = e % PT;
+        if (p0 + p < P) uvec[(d.uvec_off + i) * P + p0 + p] = Fb[e];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
+}
+
+// Backward solve for a tile of PT poses of one supernode (root first); adds the
+// correction to the FP64 positions and refreshes their FP32 copy.
+template <int PT>
+__global__ void __launch_bounds__(kThreads)
+k_bsolve_bwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+             const int32_t *__restrict__ rows, const float *__restrict__ Xall, const float *__restrict__ L21Tall,
+             Vec4<float> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32,
+             unsigned long long *ticket, unsigned *flags, int *err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float *buf[2] = {reinterpret_cast<float *>(smem_raw), reinterpret_cast<float *>(smem_raw + kChunkBytes)};
+    Vec4<float> *Z = reinterpret_cast<Vec4<float> *>(smem_raw + 2 * kChunkBytes);
+    Vec4<float> *Xv = Z + lay.ldx_max * PT;
+    Vec4<float> *G = Xv + lay.ldx_max * PT;
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_task, s_tile;
+    __shared__ unsigned s_epoch;
+    const int tid = threadIdx.x;
+    const unsigned long long ntask = (unsigned long long)S * T;
+    if (tid == 0) {
+        const unsigned long long t = atomicAdd(ticket, 1ull);
+        const int r = (int)(ntask - 1 - t % ntask);
+        s_task = order[r / T];
+        s_tile = r % T;
+        s_epoch = (unsigned)(t / ntask) + 1u;
+        mbar_init(&bars[0]);
+        mbar_init(&bars[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int s = s_task, tile = s_tile, p0 = tile * PT;
+    const unsigned epoch = s_epoch;
+    const SnInfo d = sn[s];
+    const int nc = d.ncol, nb = d.nrow - d.ncol;
+    Chunks pl;
+    if (nb > 0) pl.init(L21Tall + d.l21t_off, d.ldx, nb, Xall + d.xt_off, d.ldx, nc);
+    else pl.init(Xall + d.xt_off, d.ldx, nc, nullptr, 0, 0);
+    const int ntot = pl.nA + pl.nB;
+    const int nA = nb > 0 ? pl.nA : 0;
+    if (tid == 0) {
+        pl.issue(0, buf[0], &bars[0]);
+        if (ntot > 1) pl.issue(1, buf[1], &bars[1]);
+        for (int k = 2; k < ntot; ++k) pl.prefetch(k);
+    }
+    for (int e = tid; e < d.ldx * PT; e += kThreads) {
+        const int i = e / PT, p = e % PT;
+        Z[e] = (i < nc && p0 + p < P) ? sol[(int64_t)(d.first + i) * P + p0 + p] : Vec4<float>{0.f, 0.f, 0.f, 0.f};
+    }
+    const int32_t *rs = rows + d.rows_off;
+    if (tid == 0 && d.parent >= 0) wait_flag(flags + (int64_t)d.parent * T + tile, epoch, err);
+    __syncthreads();
+    for (int e = tid; e < nb * PT; e += kThreads) {
+        const int i = e / PT, p = e % PT;
+        G[e] = (p0 + p < P) ? ldcg4(sol + (int64_t)rs[i] * P + p0 + p) : Vec4<float>{0.f, 0.f, 0.f, 0.f};
+    }
+    __syncthreads();
+    const int NQ = (nc + 3) >> 2;
+    float acc[kMaxItems][4][3];
+#pragma unroll
+    for (int i = 0; i < kMaxItems; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[i][k][0] = acc[i][k][1] = acc[i][k][2] = 0.f;
+    for (int k = 0; k < ntot; ++k) {
+        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        int c0, cn, ld;
+        const float *src;
+        pl.chunk(k, c0, cn, src, ld);
+        chunk_gemm<PT>(buf[k & 1], ld, cn, c0, NQ, (k < nA) ? G : Z, acc);
+        __syncthreads();
+        if (tid == 0 && k + 2 < ntot) pl.issue(k + 2, buf[k & 1], &bars[k & 1]);
+        if (k == nA - 1) {
+            store_items<PT, 1>(NQ, acc, Z);  // z = y - L21^T g
+            __syncthreads();
+        }
+    }
+    store_items<PT, 0>(NQ, acc, Xv);  // x = X^T z
+    __syncthreads();
+    for (int e = tid; e < nc * PT; e += kThreads) {
+        const int i = e / PT, p = e % PT;
+        if (p0 + p >= P) continue;
+        const int64_t k = (int64_t)(d.first + i) * P + p0 + p;
+        const Vec4<float> x = Xv[e];
+        sol[k] = x;
+        Vec4<double> v = pc64[k];
+        v.x += (double)x.x;
+        v.y += (double)x.y;
+        v.z += (double)x.z;
+        pc64[k] = v;
+        pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
+}
+
+// ---------------------------------------------------------------------------
+// per (vertex, pose) kernels; thread index = k * P + p
+
+// initializeMeshGeometry + initializeConstraints (arap.h:162-168,277-281) per
+// pose: free vertices at rest, constrained ones at the pose's targets
+// (targets: P x nc x 3, constrained vertices in ascending order); R = I.
+__global__ void k_bsetup(int V, int m, int P, const Vec4<double> *__restrict__ p64,
+                         const double *__restrict__ targets, Vec4<double> *__restrict__ pc64,
+                         Vec4<float> *__restrict__ pc32, Vec4<float> *__restrict__ R) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)V * P) return;
+    const int k = (int)(t / P), p = (int)(t % P);
+    Vec4<double> v = p64[k];
+    if (k >= m) {
+        const double *g = targets + ((int64_t)p * (V - m) + (k - m)) * 3;
+        v = {g[0], g[1], g[2], 0.0};
+    }
+    pc64[t] = v;
+    pc32[t] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
+    R[3 * t + 0] = {1.f, 0.f, 0.f, 0.f};
+    R[3 * t + 1] = {0.f, 1.f, 0.f, 0.f};
+    R[3 * t + 2] = {0.f, 0.f, 1.f, 0.f};
+}
+
+// bFixed per pose (arap.h:325-327), adjacency order as in k_assemble
+__global__ void k_bbfixed(int m, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
+                          const double *__restrict__ w64, const Vec4<double> *__restrict__ pc64,
+                          Vec4<float> *__restrict__ bfixed) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)m * P) return;
+    const int k = (int)(t / P), p = (int)(t % P);
+    double bx = 0.0, by = 0.0, bz = 0.0;
+    for (int e = drow[k]; e < drow[k + 1]; ++e) {
+        const int l = dcol[e];
+        if (l < m) continue;
+        const double w = w64[e];
+        const Vec4<double> c = pc64[(int64_t)l * P + p];
+        bx = __dadd_rn(bx, __dmul_rn(w, c.x));
+        by = __dadd_rn(by, __dmul_rn(w, c.y));
+        bz = __dadd_rn(bz, __dmul_rn(w, c.z));
+    }
+    bfixed[t] = {(float)bx, (float)by, (float)bz, 0.f};
+}
+
+// estimateRotations per pose (arap.h:354-384)
+__global__ void __launch_bounds__(256)
+k_blocal(int V, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const float *__restrict__ w,
+         const Vec4<float> *__restrict__ p32, const Vec4<float> *__restrict__ pc32, Vec4<float> *__restrict__ R) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)V * P) return;
+    const int i = (int)(t / P), p = (int)(t % P);
+    const Vec4<float> pi = p32[i], ci = pc32[t];
+    float S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int e = drow[i]; e < drow[i + 1]; ++e) {
+        const int j = dcol[e];
+        const float wj = w[e];
+        const Vec4<float> pj = p32[j], cj = pc32[(int64_t)j * P + p];
+        const float ex = wj * (pi.x - pj.x), ey = wj * (pi.y - pj.y), ez = wj * (pi.z - pj.z);
+        const float fx = ci.x - cj.x, fy = ci.y - cj.y, fz = ci.z - cj.z;
+        S[0][0] += ex * fx; S[0][1] += ex * fy; S[0][2] += ex * fz;
+        S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
+        S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
+    }
+    float Rm[3][3];
+    dev::rotation_from_cov<float>(S, Rm);
+    R[3 * t + 0] = {Rm[0][0], Rm[0][1], Rm[0][2], 0.f};
+    R[3 * t + 1] = {Rm[1][0], Rm[1][1], Rm[1][2], 0.f};
+    R[3 * t + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], 0.f};
+}
+
+// estimatePositions RHS per pose (arap.h:395-414)
+__global__ void __launch_bounds__(256)
+k_brhs(int m, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const float *__restrict__ w,
+       const Vec4<float> *__restrict__ p32, const Vec4<float> *__restrict__ R, const Vec4<float> *__restrict__ bfixed,
+       Vec4<float> *__restrict__ b) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)m * P) return;
+    const int i = (int)(t / P), p = (int)(t % P);
+    const Vec4<float> pi = p32[i];
+    const Vec4<float> r0 = R[3 * t], r1 = R[3 * t + 1], r2 = R[3 * t + 2];
+    Vec4<float> acc = bfixed[t];
+    for (int e = drow[i]; e < drow[i + 1]; ++e) {
+        const int j = dcol[e];
+        if (j == i) continue;
+        const float h = w[e] * 0.5f;
+        const Vec4<float> pj = p32[j];
+        const int64_t tj = (int64_t)j * P + p;
+        const Vec4<float> q0 = R[3 * tj], q1 = R[3 * tj + 1], q2 = R[3 * tj + 2];
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        acc.x += ((r0.x + q0.x) * dx + (r0.y + q0.y) * dy + (r0.z + q0.z) * dz) * h;
+        acc.y += ((r1.x + q1.x) * dx + (r1.y + q1.y) * dy + (r1.z + q1.z) * dz) * h;
+        acc.z += ((r2.x + q2.x) * dx + (r2.y + q2.y) * dy + (r2.z + q2.z) * dz) * h;
+    }
+    b[t] = acc;
+}
+
+// r = b - A x in FP64 per pose
+__global__ void __launch_bounds__(256)
+k_bresidual(int m, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
+            const double *__restrict__ w64, const double *__restrict__ diag64, const Vec4<float> *__restrict__ b,
+            const Vec4<double> *__restrict__ x, Vec4<float> *__restrict__ r) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)m * P) return;
+    const int i = (int)(t / P), p = (int)(t % P);
+    const Vec4<double> xi = x[t];
+    const double dg = diag64[i];
+    double ax = dg * xi.x, ay = dg * xi.y, az = dg * xi.z;
+    for (int e = drow[i]; e < drow[i + 1]; ++e) {
+        const int j = dcol[e];
+        if (j == i || j >= m) continue;
+        const double wj = w64[e];
+        const Vec4<double> xj = x[(int64_t)j * P + p];
+        ax -= wj * xj.x;
+        ay -= wj * xj.y;
+        az -= wj * xj.z;
+    }
+    const Vec4<float> bi = b[t];
+    r[t] = {(float)((double)bi.x - ax), (float)((double)bi.y - ay), (float)((double)bi.z - az), 0.f};
+}
+
+// positions of every pose back to vertex order: out[p][v][3]
+__global__ void k_bgather(int V, int P, const int32_t *__restrict__ oldidx, const Vec4<double> *__restrict__ pc64,
+                          double *__restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)V * P) return;
+    const int k = (int)(t / P), p = (int)(t % P);
+    const Vec4<double> x = pc64[t];
+    double *o = out + ((int64_t)p * V + oldidx[k]) * 3;
+    o[0] = x.x;
+    o[1] = x.y;
+    o[2] = x.z;
+}
+
+inline int nblocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+int batch_pose_tile(int max_ldx, int max_ld21) {
+    const int rows = max_ldx > max_ld21 ? max_ldx : max_ld21;
+    for (int pt = 16; pt >= 1; pt /= 2) {
+        const size_t smem = batch_solve_smem_bytes(max_ldx, max_ld21, pt);
+        if ((rows / 4) * pt <= kMaxItems * kThreads && smem <= 200 * 1024) return pt;
+    }
+    return 0;
+}
+
+size_t batch_solve_smem_bytes(int max_ldx, int max_ld21, int pt) {
+    return (size_t)2 * kChunkBytes + (size_t)(2 * max_ldx + max_ld21) * pt * sizeof(Vec4<float>);
+}
+
+template <int PT>
+static cudaError_t configure_pt(size_t bytes) {
+    cudaError_t e = cudaFuncSetAttribute(k_bsolve_fwd<PT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_bsolve_bwd<PT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t configure_batch_smem(int max_ldx, int max_ld21, int pt) {
+    const size_t bytes = batch_solve_smem_bytes(max_ldx, max_ld21, pt);
+    switch (pt) {
+    case 16: return configure_pt<16>(bytes);
+    case 8: return configure_pt<8>(bytes);
+    case 4: return configure_pt<4>(bytes);
+    case 2: return configure_pt<2>(bytes);
+    default: return configure_pt<1>(bytes);
+    }
+}
+
+void launch_bsetup(const DevSym &s, int P, const Vec4<double> *p64, const double *targets, Vec4<double> *pc64,
+                   Vec4<float> *pc32, Vec4<float> *R, cudaStream_t st) {
+    const int64_t n = (int64_t)s.V * P;
+    if (n) k_bsetup<<<nblocks(n, 256), 256, 0, st>>>(s.V, s.m, P, p64, targets, pc64, pc32, R);
+}
+
+void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double> *pc64, Vec4<float> *bfixed,
+                    cudaStream_t st) {
+    const int64_t n = (int64_t)s.m * P;
+    if (n) k_bbfixed<<<nblocks(n, 256), 256, 0, st>>>(s.m, P, s.drow, s.dcol, w64, pc64, bfixed);
+}
+
+void launch_blocal(const DevSym &s, int P, const float *w32, const Vec4<float> *p32, const Vec4<float> *pc32,
+                   Vec4<float> *R, cudaStream_t st) {
+    const int64_t n = (int64_t)s.V * P;
+    if (n) k_blocal<<<nblocks(n, 256), 256, 0, st>>>(s.V, P, s.drow, s.dcol, w32, p32, pc32, R);
+}
+
+void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *p32, const Vec4<float> *R,
+                 const Vec4<float> *bfixed, Vec4<float> *b, cudaStream_t st) {
+    const int64_t n = (int64_t)s.m * P;
+    if (n) k_brhs<<<nblocks(n, 256), 256, 0, st>>>(s.m, P, s.drow, s.dcol, w32, p32, R, bfixed, b);
+}
+
+void launch_bresidual(const DevSym &s, int P, const double *w64, const double *diag64, const Vec4<float> *b,
+                      const Vec4<double> *x, Vec4<float> *r, cudaStream_t st) {
+    const int64_t n = (int64_t)s.m * P;
+    if (n) k_bresidual<<<nblocks(n, 256), 256, 0, st>>>(s.m, P, s.drow, s.dcol, w64, diag64, b, x, r);
+}
+
+void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *out, cudaStream_t st) {
+    const int64_t n = (int64_t)s.V * P;
+    if (n) k_bgather<<<nblocks(n, 256), 256, 0, st>>>(s.V, P, s.oldidx, pc64, out);
+}
+
+template <int PT>
+static void bsolve(const DevSym &s, int P, const float *X, const float *L21, const float *L21T, Vec4<float> *sol,
+                   Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32, unsigned long long *ticket,
+                   unsigned *flags, int *err, bool forward, cudaStream_t st) {
+    const int T = (P + PT - 1) / PT;
+    const BLayout lay{s.max_ldx, s.max_ld21};
+    const size_t smem = batch_solve_smem_bytes(s.max_ldx, s.max_ld21, PT);
+    const int grid = s.S * T;
+    if (forward)
+        k_bsolve_fwd<PT><<<grid, kThreads, smem, st>>>(s.S, T, P, lay, s.level_sn, s.sn, s.child, s.relind, X, L21,
+                                                       sol, uvec, ticket, flags, err);
+    else
+        k_bsolve_bwd<PT><<<grid, kThreads, smem, st>>>(s.S, T, P, lay, s.level_sn, s.sn, s.rows, X, L21T, sol, pc64,
+                                                       pc32, ticket, flags, err);
+}
+
+void launch_bsolve(const DevSym &s, int P, int pt, const float *X, const float *L21, const float *L21T,
+                   Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
+                   unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st) {
+    if (s.S == 0) return;
+    switch (pt) {
+    case 16: bsolve<16>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    case 8: bsolve<8>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    case 4: bsolve<4>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    case 2: bsolve<2>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    default: bsolve<1>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    }
+}
+
+}  // namespace arapgpu

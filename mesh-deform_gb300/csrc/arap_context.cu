@@ -79,6 +79,10 @@ struct arap_ctx {
     int factor_smem_ncol = 0;
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T;
     DevBuf errw, ticket, flags;
+    // many-pose state (arap_deform_poses)
+    DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
+    int bP = 0, bT = 0, bS = -1, bpt = 0;
+    size_t bsmem = 0;
     DevTopo dt{};
     DevSym ds{};
     int64_t launches = 0;
@@ -492,7 +496,8 @@ void arap_destroy(arap_ctx *ctx) {
                       &ctx->level_sn, &ctx->fitems, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
                       &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
                       &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->L21T, &ctx->errw, &ctx->ticket,
-                      &ctx->flags};
+                      &ctx->flags, &ctx->btargets, &ctx->bpc64, &ctx->bpc32, &ctx->bR, &ctx->bbfixed,
+                      &ctx->bb, &ctx->bsol, &ctx->buvec, &ctx->bout, &ctx->bticket, &ctx->bflags};
     for (DevBuf *b : bufs) b->release();
     for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -552,6 +557,142 @@ int arap_set_constraints(arap_ctx *ctx, int32_t n, const int32_t *indices, const
                            cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));  // the host vector may change on the next call
     ctx->dirty = true;
+    return ARAP_OK;
+}
+
+int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
+                      double *out_xyz) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (n_poses <= 0 || iterations < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "n_poses must be positive");
+    if (ctx->precision != ARAP_PRECISION_MIXED)
+        return fail(ctx, ARAP_ERR_UNSUPPORTED, "arap_deform_poses runs the mixed-precision form only");
+    if (!ctx->have_rest) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "rest positions not set");
+    if (ctx->cidx.empty()) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no constrained vertex");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    CK(cudaStreamSynchronize(st));
+    collect_profile(ctx);
+    ctx->launches = 0;
+    CK(cudaEventRecord(ctx->ev0, st));
+    if (ctx->dirty || ctx->state_prec != ARAP_PRECISION_MIXED) {
+        {
+            Prof pr(ctx, ARAP_K_WEIGHTS);
+            launch_face_cots(ctx->dt, ctx->rest.as<double>(), ctx->hc.as<double>(), st);
+        }
+        ctx->launches += 1;
+        int rc = prepare_symbolic(ctx);
+        if (rc != ARAP_OK) return rc;
+        rc = setup_numeric<float>(ctx);
+        if (rc != ARAP_OK) return rc;
+        ctx->dirty = false;
+    }
+    const Symbolic &s = ctx->sym;
+    const DevSym &d = ctx->ds;
+    const int V = s.V, m = s.m, P = n_poses, nc = V - m;
+    if (ctx->bS != s.S || ctx->bP != P) {
+        const int pt = batch_pose_tile(s.max_ldx, s.max_ld21);
+        if (pt == 0) return fail(ctx, ARAP_ERR_UNSUPPORTED, "supernode fronts too large for the batched solves");
+        const size_t smem = batch_solve_smem_bytes(s.max_ldx, s.max_ld21, pt);
+        if (pt != ctx->bpt || smem > ctx->bsmem) {
+            CK(configure_batch_smem(s.max_ldx, s.max_ld21, pt));
+            ctx->bsmem = smem;
+        }
+        ctx->bpt = pt;
+        ctx->bT = (P + pt - 1) / pt;
+        const size_t VP = (size_t)V * P, MP = (size_t)std::max(m, 1) * P;
+        CK(ctx->bpc64.ensure(VP * sizeof(Vec4<double>)));
+        CK(ctx->bpc32.ensure(VP * sizeof(Vec4<float>)));
+        CK(ctx->bR.ensure(VP * 3 * sizeof(Vec4<float>)));
+        CK(ctx->bbfixed.ensure(MP * sizeof(Vec4<float>)));
+        CK(ctx->bb.ensure(MP * sizeof(Vec4<float>)));
+        CK(ctx->bsol.ensure(MP * sizeof(Vec4<float>)));
+        CK(ctx->buvec.ensure((size_t)std::max<int64_t>(s.uvec_size, 1) * P * sizeof(Vec4<float>)));
+        CK(ctx->bout.ensure(VP * 3 * sizeof(double)));
+        CK(ctx->btargets.ensure((size_t)P * nc * 3 * sizeof(double)));
+        const size_t nflags = (size_t)2 * std::max(s.S, 1) * ctx->bT;
+        CK(ctx->bticket.ensure(2 * sizeof(unsigned long long)));
+        CK(ctx->bflags.ensure(nflags * sizeof(unsigned)));
+        CK(cudaMemsetAsync(ctx->bticket.p, 0, 2 * sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(ctx->bflags.p, 0, nflags * sizeof(unsigned), st));
+        ctx->bS = s.S;
+        ctx->bP = P;
+    } else if (!targets && !ctx->btargets.p) {
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no targets uploaded yet");
+    }
+    if (targets)
+        CK(cudaMemcpyAsync(ctx->btargets.p, targets, (size_t)P * nc * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                           st));
+    CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
+    {
+        Prof pr(ctx, ARAP_K_ASSEMBLE);
+        launch_bsetup(d, P, ctx->p64.as<Vec4<double>>(), ctx->btargets.as<double>(), ctx->bpc64.as<Vec4<double>>(),
+                      ctx->bpc32.as<Vec4<float>>(), ctx->bR.as<Vec4<float>>(), st);
+        launch_bbfixed(d, P, ctx->w64.as<double>(), ctx->bpc64.as<Vec4<double>>(), ctx->bbfixed.as<Vec4<float>>(),
+                       st);
+    }
+    ctx->launches += 2;
+    CK(cudaEventRecord(ctx->ev1, st));
+    unsigned long long *tk = ctx->bticket.as<unsigned long long>();
+    unsigned *fl = ctx->bflags.as<unsigned>();
+    const size_t fhalf = (size_t)std::max(s.S, 1) * ctx->bT;
+    for (int it = 0; it < iterations; ++it) {
+        {
+            Prof pr(ctx, ARAP_K_LOCAL);
+            launch_blocal(d, P, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->bpc32.as<Vec4<float>>(),
+                          ctx->bR.as<Vec4<float>>(), st);
+        }
+        ctx->launches += 1;
+        if (m == 0) continue;
+        {
+            Prof pr(ctx, ARAP_K_RHS);
+            launch_brhs(d, P, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->bR.as<Vec4<float>>(),
+                        ctx->bbfixed.as<Vec4<float>>(), ctx->bb.as<Vec4<float>>(), st);
+        }
+        ctx->launches += 1;
+        for (int r = 0; r <= ctx->refine; ++r) {
+            {
+                Prof pr(ctx, ARAP_K_RESIDUAL);
+                launch_bresidual(d, P, ctx->w64.as<double>(), ctx->diag64.as<double>(), ctx->bb.as<Vec4<float>>(),
+                                 ctx->bpc64.as<Vec4<double>>(), ctx->bsol.as<Vec4<float>>(), st);
+            }
+            {
+                Prof pr(ctx, ARAP_K_SOLVE_FWD);
+                launch_bsolve(d, P, ctx->bpt, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
+                              ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), nullptr, nullptr, tk, fl,
+                              ctx->errw.as<int>(), true, st);
+            }
+            {
+                Prof pr(ctx, ARAP_K_SOLVE_BWD);
+                launch_bsolve(d, P, ctx->bpt, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
+                              ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
+                              ctx->bpc32.as<Vec4<float>>(), tk + 1, fl + fhalf, ctx->errw.as<int>(), false, st);
+            }
+            ctx->launches += 3;
+        }
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev2, st));
+    if (out_xyz) {
+        {
+            Prof pr(ctx, ARAP_K_GATHER);
+            launch_bgather(d, P, ctx->bpc64.as<Vec4<double>>(), ctx->bout.as<double>(), st);
+        }
+        ctx->launches += 1;
+        CK(cudaMemcpyAsync(out_xyz, ctx->bout.p, (size_t)P * V * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    collect_profile(ctx);
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&b, ctx->ev1, ctx->ev2);
+    ctx->setup_ms = a;
+    ctx->iter_ms = b;
+    if (herr & kErrTimeout) {
+        ctx->bS = -1;  // rebuild the scheduling counters next time
+        return fail(ctx, ARAP_ERR_TIMEOUT, "a triangular-solve wait exceeded its bound");
+    }
     return ARAP_OK;
 }
 

@@ -89,6 +89,28 @@ template <typename T>
 void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
                       cudaStream_t st);
+// ---- many poses of one mesh and constraint set (arap_batch.cu); arrays of
+// (vertex, pose) pairs are vertex-major, element (k, p) at k * P + p
+size_t batch_solve_smem_bytes(int max_ldx, int max_ld21, int pt);
+// largest pose tile (16, 8, 4, 2, 1) the batched solves support for these
+// front sizes, 0 when none fits
+int batch_pose_tile(int max_ldx, int max_ld21);
+cudaError_t configure_batch_smem(int max_ldx, int max_ld21, int pt);
+void launch_bsetup(const DevSym &s, int P, const Vec4<double> *p64, const double *targets, Vec4<double> *pc64,
+                   Vec4<float> *pc32, Vec4<float> *R, cudaStream_t st);
+void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double> *pc64, Vec4<float> *bfixed,
+                    cudaStream_t st);
+void launch_blocal(const DevSym &s, int P, const float *w32, const Vec4<float> *p32, const Vec4<float> *pc32,
+                   Vec4<float> *R, cudaStream_t st);
+void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *p32, const Vec4<float> *R,
+                 const Vec4<float> *bfixed, Vec4<float> *b, cudaStream_t st);
+void launch_bresidual(const DevSym &s, int P, const double *w64, const double *diag64, const Vec4<float> *b,
+                      const Vec4<double> *x, Vec4<float> *r, cudaStream_t st);
+void launch_bsolve(const DevSym &s, int P, int pt, const float *X, const float *L21, const float *L21T,
+                   Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
+                   unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st);
+void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *out, cudaStream_t st);
+
 // deformed positions back to the original vertex order as doubles (arap.h:133-135)
 void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st);
 template <typename T>

@@ -1,0 +1,58 @@
+"""Many poses of one mesh in one pass (arap_deform_poses) against the FP64
+oracle run pose by pose: each pose is a dirty deform from the rest pose with
+the handles at that pose's targets (inc/deform/deformation_util.h:48-57
+followed by deform, inc/deform/arap.h:101-138)."""
+import numpy as np
+import pytest
+
+import arap_workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("level,n_poses,iters", [(3, 5, 6), (4, 19, 10)])
+def test_pose_batch_matches_oracle(gpu, level, n_poses, iters):
+    w = W.cfg_pose_batch(level=level, n_poses=n_poses, iterations=iters)
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.poses[0])
+        out = ctx.deform_poses(w.poses, iters)
+    assert out.shape == (n_poses, w.V, 3)
+    for p in range(n_poses):
+        ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.poses[p], iters)
+        assert ok
+        err = W.bbox_rel_error(out[p], ref, w.positions)
+        assert err <= 1e-6, (p, err)
+        np.testing.assert_array_equal(out[p][w.cidx], w.poses[p])
+
+
+def test_pose_batch_equals_single_requests(gpu):
+    """The same poses one at a time through arap_deform agree with the batch
+    to the mixed tolerance, and a second batch call with the targets left on
+    the device repeats the first."""
+    w = W.cfg_pose_batch(level=3, n_poses=4, iterations=5)
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.poses[0])
+        batch = ctx.deform_poses(w.poses, 5)
+        again = np.empty_like(batch)
+        assert ctx.deform_poses_rc(None, 5, again) == gpu.ARAP_OK
+        np.testing.assert_array_equal(batch, again)
+        for p in range(4):
+            ctx.set_constraints(w.cidx, w.poses[p])
+            single = ctx.deform(5)
+            assert W.bbox_rel_error(single, batch[p], w.positions) <= 1e-6
+
+
+def test_pose_batch_rejects_fp64(gpu):
+    w = W.cfg_pose_batch(level=2, n_poses=2, iterations=2)
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("fp64")
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.poses[0])
+        with pytest.raises(gpu.ArapError) as e:
+            ctx.deform_poses(w.poses, 2)
+        assert e.value.code == gpu.ARAP_ERR_UNSUPPORTED
