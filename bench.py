@@ -64,6 +64,8 @@ def workload(args):
         return w
     if args.workload == "noisy_sphere":
         return W.cfg_noisy_sphere(iterations=args.iterations, precision=args.precision)
+    if args.workload == "pose_batch":
+        return W.cfg_pose_batch(level=5, n_poses=args.poses, iterations=args.iterations, precision="mixed")
     raise SystemExit(f"unknown workload {args.workload}")
 
 
@@ -183,6 +185,153 @@ def run_reference(args):
     return 0
 
 
+def run_batch(args):
+    """Many poses of one mesh per step (arap_deform_poses): one factorisation
+    shared by all poses, P x 3 right-hand sides per triangular solve."""
+    import torch
+    import arap_gpu as G
+    import arap_workloads as W
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = workload(args)
+    P = w.poses.shape[0]
+    ctx = G.ArapContext(w.V, w.faces, device=local)
+    ctx.set_precision("mixed", args.refine)
+    ctx.set_rest_positions(w.positions)
+    ctx.set_constraints(w.cidx, w.poses[0])
+    first = ctx.deform_poses(w.poses, w.iterations)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        ctx.invalidate()  # refactor each step: the step is a full dirty deform of every pose
+        rc = ctx.deform_poses_rc(None, w.iterations, None)
+        if rc != G.ARAP_OK:
+            raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step()
+    clocks = ClockSampler(local)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches = 0
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks.start()
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+        launches += ctx.launch_count()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ctx.set_profiling(True)
+    ctx.reset_kernel_stats()
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step()
+    kstats = ctx.kernel_stats()
+    kmodel = ctx.kernel_model()
+    ctx.set_profiling(False)
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    its_total = P * w.iterations * args.steps * world
+    value = its_total / (total_ms / 1e3)
+    tg_h = torch.from_numpy(np.ascontiguousarray(w.poses)).pin_memory().numpy()
+    out_h = torch.empty((P, w.V, 3), dtype=torch.float64).pin_memory().numpy()
+    e2e_s = []
+    for k in range(0 if args.skip_e2e else args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.invalidate()
+        rc = ctx.deform_poses_rc(tg_h, w.iterations, out_h)
+        t1 = time.perf_counter()
+        if rc != G.ARAP_OK:
+            raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+        if k >= args.warmup:
+            e2e_s.append(t1 - t0)
+    e2e_total = sum(e2e_s) if e2e_s else float("nan")
+    if dist is not None and e2e_s:
+        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    dom = max(kstats, key=lambda k: kstats[k][0])
+    dom_ms, dom_n = kstats[dom]
+    per_launch_ms = dom_ms / max(dom_n, 1)
+    if dom == "factor":
+        per_launch_ms = dom_ms / max(args.steps, 1)
+    # the model covers one right-hand side; the batched solves stream the
+    # factor once per pose tile and the per-pose vectors once per pose
+    dom_bytes = kmodel[dom][0]
+    achieved = dom_bytes / (per_launch_ms * 1e-3) / 1e9
+    cpu = None
+    err = None
+    if rank == 0 and not args.no_cpu_baseline and e2e_s:
+        from oracle import oracle as O
+
+        O.build()
+        n = min(args.cpu_requests * 4, P)
+        t0 = time.perf_counter()
+        errs = []
+        for p in range(n):
+            ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.poses[p], w.iterations)
+            errs.append(W.bbox_rel_error(out_h[p], ref, w.positions))
+        dt = time.perf_counter() - t0
+        err = max(errs)
+        cpu = {"value": n * w.iterations / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{n} poses of {w.name}, one dirty deform({w.iterations}) each on one thread ({dt:.1f} s)"}
+        log(f"max error vs FP64 oracle over {n} poses: {err:.3e}")
+    lat = sorted(step_ms)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": config_of(w, args, {"poses": P, "step": f"dirty deform of {P} poses (one shared factor)",
+                                      "precision": "mixed"}),
+        "e2e": {"value": its_total / e2e_total if e2e_s else None, "unit": UNIT,
+                "h2d_bytes_per_step": int(tg_h.nbytes), "d2h_bytes_per_step": int(out_h.nbytes)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None, "bytes_per_launch": dom_bytes,
+                     "ms_per_launch": per_launch_ms},
+        "cpu_baseline": cpu,
+        "error_vs_fp64_oracle": err,
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": float(np.percentile(lat, 99))},
+        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kstats.items()},
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -197,11 +346,14 @@ def main():
     ap.add_argument("--cpu-requests", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: skip the end-to-end pass")
+    ap.add_argument("--poses", type=int, default=256, help="pose_batch: handle poses per step")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "pose_batch":
+        return run_batch(args)
 
     import torch
 

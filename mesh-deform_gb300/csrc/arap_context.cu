@@ -82,6 +82,7 @@ struct arap_ctx {
     // many-pose state (arap_deform_poses)
     DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
     int bP = 0, bT = 0, bS = -1, bpt = 0;
+    int model_P = 1, model_T = 1;  // poses / pose tiles of the last deform (cost model)
     size_t bsmem = 0;
     DevTopo dt{};
     DevSym ds{};
@@ -632,6 +633,8 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
     }
     ctx->launches += 2;
     CK(cudaEventRecord(ctx->ev1, st));
+    ctx->model_P = P;
+    ctx->model_T = ctx->bT;
     unsigned long long *tk = ctx->bticket.as<unsigned long long>();
     unsigned *fl = ctx->bflags.as<unsigned>();
     const size_t fhalf = (size_t)std::max(s.S, 1) * ctx->bT;
@@ -712,6 +715,7 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     collect_profile(ctx);
     ctx->launches = 0;
     ctx->setup_ms = ctx->iter_ms = 0.0;
+    ctx->model_P = ctx->model_T = 1;
     const bool fp64 = ctx->precision == ARAP_PRECISION_FP64;
     CK(cudaEventRecord(ctx->ev0, st));
     if (ctx->dirty) {
@@ -926,6 +930,7 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
         nbsum += d.nrow - d.ncol;
     }
     double B = 0.0, FL = 0.0;
+    const double P = ctx->model_P, T = ctx->model_T;  // poses, pose tiles of the last deform
     switch (kernel_class) {
     case ARAP_K_WEIGHTS:  // faces + rest positions + weights out (two precisions)
         B = F * 12 + V * 24 + F * 24 + nnz * (4 + 8 + sz);
@@ -941,25 +946,25 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
         FL = s.factor_flops;
         break;
     case ARAP_K_LOCAL:  // rest + current positions, rotations out, adjacency + weights
-        B = V * (3 * sz + 3 * sz + 9 * sz) + 4 * (V + 1) + nnz * (4 + sz);
-        FL = nnz * 24 + V * 600;
+        B = V * 3 * sz + P * V * (3 * sz + 9 * sz) + 4 * (V + 1) + nnz * (4 + sz);
+        FL = P * (nnz * 24 + V * 600);
         break;
     case ARAP_K_RHS:
-        B = m * (9 * sz + 3 * sz + 3 * sz + 3 * sz) + 4 * (m + 1) + nnz * (4 + sz);
-        FL = nnz * 24;
+        B = m * 3 * sz + P * m * (9 * sz + 3 * sz + 3 * sz) + 4 * (m + 1) + nnz * (4 + sz);
+        FL = P * nnz * 24;
         break;
     case ARAP_K_RESIDUAL:
-        B = m * (24 + 8 + 12 + 12) + 4 * (m + 1) + nnz * (4 + 8);
-        FL = nnz * 6;
+        B = P * m * (24 + 12 + 12) + m * 8 + 4 * (m + 1) + nnz * (4 + 8);
+        FL = P * nnz * 6;
         break;
     case ARAP_K_SOLVE_FWD:
-    case ARAP_K_SOLVE_BWD:
-        B = (xlow + l21) * sz + m * 3 * sz * 2 + nbsum * 3 * sz * 2;
-        if (kernel_class == ARAP_K_SOLVE_BWD && ctx->state_prec != ARAP_PRECISION_FP64) B += m * (24 * 2 + 12);
-        FL = (xlow + l21) * 6;
+    case ARAP_K_SOLVE_BWD:  // matrices once per pose tile, vectors once per pose
+        B = T * (xlow + l21) * sz + P * (m * 3 * sz * 2 + nbsum * 3 * sz * 2);
+        if (kernel_class == ARAP_K_SOLVE_BWD && ctx->state_prec != ARAP_PRECISION_FP64) B += P * m * (24 * 2 + 12);
+        FL = P * (xlow + l21) * 6;
         break;
     case ARAP_K_GATHER:
-        B = V * (24 + 24 + 4);
+        B = P * V * (24 + 24) + V * 4;
         FL = 0;
         break;
     }
