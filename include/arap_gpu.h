@@ -106,6 +106,21 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz);
 int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
                       double *out_xyz);
 
+/* arap_deform split in two: arap_deform_async enqueues the whole deform on
+   the context's stream and returns at once (out_xyz must stay valid, and is
+   best pinned, until arap_wait returns); arap_wait waits for it and returns
+   its status. Any other call on the context first waits for a pending
+   deform. Contexts on one device run concurrently, so one host thread can
+   keep several requests in flight. */
+int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz);
+int arap_wait(arap_ctx *ctx);
+
+/* enable != 0 (the default) runs the setup and the iteration sequence as CUDA
+   graphs captured on first use and replayed while the problem's size,
+   precision and iteration count stay the same; 0 launches every kernel
+   directly. Profiling (arap_set_profiling) always launches directly. */
+int arap_set_graphs(arap_ctx *ctx, int32_t enable);
+
 /* Marks the context dirty without uploading anything: the next arap_deform
    rebuilds the problem from the rest pose and targets already on the device.
    Used to time a dirty deform with its inputs resident in device memory. */

@@ -69,6 +69,9 @@ SIGNATURES = {
     "arap_get_kernel_model": (C.c_int, [_P, _I32, _dp, _dp]),
     "arap_cotan_weights_static": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _I32, _P, _P]),
     "arap_deform_poses": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
+    "arap_deform_async": (C.c_int, [_P, _I32, _dp]),
+    "arap_wait": (C.c_int, [_P]),
+    "arap_set_graphs": (C.c_int, [_P, _I32]),
 }
 
 KERNEL_CLASSES = ["weights", "assemble", "factor", "local", "rhs", "residual", "solve_fwd", "solve_bwd", "gather"]
@@ -186,6 +189,15 @@ class ArapContext:
         out = np.empty((t.shape[0], self.V, 3), np.float64)
         self._check(self.deform_poses_rc(t, iterations, out))
         return out
+
+    def deform_async(self, iterations: int, out: np.ndarray | None = None) -> None:
+        self._check(self.lib.arap_deform_async(self.h, int(iterations), _f64(out) if out is not None else None))
+
+    def wait(self) -> None:
+        self._check(self.lib.arap_wait(self.h))
+
+    def set_graphs(self, enable: bool) -> None:
+        self._check(self.lib.arap_set_graphs(self.h, 1 if enable else 0))
 
     def invalidate(self):
         self._check(self.lib.arap_invalidate(self.h))

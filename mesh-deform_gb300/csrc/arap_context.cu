@@ -83,6 +83,16 @@ struct arap_ctx {
     DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
     int bP = 0, bT = 0, bS = -1, bpt = 0;
     int model_P = 1, model_T = 1;  // poses / pose tiles of the last deform (cost model)
+    // CUDA graphs of the setup and of the iteration sequence; replayed while
+    // nothing they reference changes (direct launches when profiling)
+    cudaGraphExec_t g_setup = nullptr, g_iter = nullptr;
+    int64_t g_setup_key[4] = {0, 0, 0, 0}, g_iter_key[4] = {0, 0, 0, 0};
+    int64_t g_setup_launches = 0, g_iter_launches = 0;
+    int64_t gen = 1;  // bumped when the symbolic analysis or any device buffer changes
+    bool use_graphs = true;
+    // asynchronous deform (arap_deform_async / arap_wait)
+    bool in_flight = false;    // a deform was enqueued and not waited for
+    int *herr_host = nullptr;  // pinned copy of the device error word
     size_t bsmem = 0;
     DevTopo dt{};
     DevSym ds{};
@@ -171,6 +181,7 @@ int prepare_symbolic(arap_ctx *ctx) {
         return fail(ctx, singular ? ARAP_ERR_NOT_SPD : ARAP_ERR_CUDA, err);
     Symbolic &s = ctx->sym;
     cudaStream_t st = ctx->stream;
+    ctx->gen++;
     CK(upload(ctx->drow, s.drow, st));
     CK(upload(ctx->dcol, s.dcol, st));
     CK(upload(ctx->dent, s.dent, st));
@@ -235,15 +246,18 @@ template <typename T> struct PrecTag;
 template <> struct PrecTag<float> { static constexpr int value = ARAP_PRECISION_MIXED; };
 template <> struct PrecTag<double> { static constexpr int value = ARAP_PRECISION_FP64; };
 
-// Dirty-deform setup in precision T (FP64: T = double for everything; MIXED:
-// T = float for the local step, RHS, factor and solves).
+// Allocates (or keeps) every buffer the setup and the iterations of precision
+// T use. Any reallocation bumps ctx->gen so captured graphs are rebuilt.
 template <typename T>
-int setup_numeric(arap_ctx *ctx) {
+int setup_alloc(arap_ctx *ctx) {
     const Symbolic &s = ctx->sym;
-    const DevSym &d = ctx->ds;
-    cudaStream_t st = ctx->stream;
     const int V = s.V, m = s.m;
     const size_t nnz = s.dcol.size();
+    DevBuf *bufs[] = {&ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32, &ctx->pc32, &ctx->R, &ctx->diag64,
+                      &ctx->bfixed, &ctx->b, &ctx->sol, &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd,
+                      &ctx->Xinv, &ctx->L21, &ctx->L21T};
+    void *before[sizeof(bufs) / sizeof(bufs[0])];
+    for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i) before[i] = bufs[i]->p;
     CK(ctx->w64.ensure(nnz * sizeof(double)));
     if (sizeof(T) == 4) CK(ctx->w32.ensure(nnz * sizeof(float)));
     CK(ctx->p64.ensure((size_t)V * sizeof(Vec4<double>)));
@@ -264,9 +278,22 @@ int setup_numeric(arap_ctx *ctx) {
     CK(ctx->Xinv.ensure((size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T)));
     CK(ctx->L21.ensure((size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T)));
     CK(ctx->L21T.ensure((size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T)));
-    CK(ctx->errw.ensure(sizeof(int)));
-    CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
+    for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
+        if (before[i] != bufs[i]->p) { ctx->gen++; break; }
+    return ARAP_OK;
+}
 
+// Enqueues the dirty-deform setup in precision T (FP64: T = double for
+// everything; MIXED: T = float for the local step, RHS, factor and solves):
+// cotan weights, geometry and constraint snap, rotations reset, Laplacian and
+// bFixed assembly, the factorisation plan. No host synchronisation; a failed
+// pivot shows up in the device error word.
+template <typename T>
+int setup_enqueue(arap_ctx *ctx) {
+    const Symbolic &s = ctx->sym;
+    const DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    const int m = s.m;
     // cotan weights (arap.h:182-239)
     {
         Prof pr(ctx, ARAP_K_WEIGHTS);
@@ -303,12 +330,40 @@ int setup_numeric(arap_ctx *ctx) {
         }
     }
     CK(cudaGetLastError());
-    int herr = 0;
-    CK(cudaMemcpyAsync(&herr, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (herr & kErrNotSpd) return fail(ctx, ARAP_ERR_NOT_SPD, "Cholesky factorisation met a non-positive pivot");
-    ctx->state_prec = PrecTag<T>::value;
-    ctx->have_rotations = true;
+    return ARAP_OK;
+}
+
+// Runs `enqueue` directly, or through a CUDA graph captured from it and kept
+// while `key` stays the same.
+template <class F>
+int graph_or_direct(arap_ctx *ctx, cudaGraphExec_t &exec, int64_t key_store[4], const int64_t key[4],
+                    int64_t &nlaunch, F enqueue) {
+    cudaStream_t st = ctx->stream;
+    if (!ctx->use_graphs || ctx->profiling) return enqueue();
+    const bool same = exec && key_store[0] == key[0] && key_store[1] == key[1] && key_store[2] == key[2] &&
+                      key_store[3] == key[3];
+    if (!same) {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        const int64_t before = ctx->launches;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue();
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc != ARAP_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CK(e);
+        const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        CK(ei);
+        nlaunch = ctx->launches - before;
+        ctx->launches = before;
+        for (int i = 0; i < 4; ++i) key_store[i] = key[i];
+    }
+    CK(cudaGraphLaunch(exec, st));
+    ctx->launches += nlaunch;
     return ARAP_OK;
 }
 
@@ -476,6 +531,9 @@ int arap_create(int32_t n_vertices, int32_t n_faces, const int32_t *faces, int32
         return bail(e, "alloc");
     if ((e = ctx->out.ensure((size_t)9 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
         return bail(e, "alloc");
+    if ((e = ctx->errw.ensure(sizeof(int))) != cudaSuccess) return bail(e, "alloc");
+    if ((e = cudaMallocHost(&ctx->herr_host, sizeof(int))) != cudaSuccess) return bail(e, "alloc");
+    *ctx->herr_host = 0;
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return bail(e, "sync");
     ctx->dt.V = n_vertices;
     ctx->dt.F = n_faces;
@@ -501,6 +559,9 @@ void arap_destroy(arap_ctx *ctx) {
                       &ctx->bb, &ctx->bsol, &ctx->buvec, &ctx->bout, &ctx->bticket, &ctx->bflags};
     for (DevBuf *b : bufs) b->release();
     for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+    if (ctx->g_setup) cudaGraphExecDestroy(ctx->g_setup);
+    if (ctx->g_iter) cudaGraphExecDestroy(ctx->g_iter);
+    if (ctx->herr_host) cudaFreeHost(ctx->herr_host);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev2) cudaEventDestroy(ctx->ev2);
@@ -510,6 +571,10 @@ void arap_destroy(arap_ctx *ctx) {
 
 int arap_set_precision(arap_ctx *ctx, int32_t precision, int32_t refine_steps) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
     if (precision != ARAP_PRECISION_FP64 && precision != ARAP_PRECISION_MIXED)
         return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "unknown precision");
     if (refine_steps < 0 || refine_steps > 8) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "refine_steps outside 0..8");
@@ -521,6 +586,10 @@ int arap_set_precision(arap_ctx *ctx, int32_t precision, int32_t refine_steps) {
 
 int arap_set_rest_positions(arap_ctx *ctx, const double *xyz) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
     if (!xyz && ctx->topo.V > 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "null positions");
     cudaSetDevice(ctx->device);
     if (ctx->topo.V > 0)
@@ -533,6 +602,10 @@ int arap_set_rest_positions(arap_ctx *ctx, const double *xyz) {
 
 int arap_set_constraints(arap_ctx *ctx, int32_t n, const int32_t *indices, const double *xyz) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
     if (n < 0 || (n > 0 && (!indices || !xyz))) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "invalid constraint arrays");
     const int V = ctx->topo.V;
     for (int i = 0; i < n; ++i)
@@ -564,6 +637,10 @@ int arap_set_constraints(arap_ctx *ctx, int32_t n, const int32_t *indices, const
 int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
                       double *out_xyz) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
     if (n_poses <= 0 || iterations < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "n_poses must be positive");
     if (ctx->precision != ARAP_PRECISION_MIXED)
         return fail(ctx, ARAP_ERR_UNSUPPORTED, "arap_deform_poses runs the mixed-precision form only");
@@ -583,8 +660,17 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
         ctx->launches += 1;
         int rc = prepare_symbolic(ctx);
         if (rc != ARAP_OK) return rc;
-        rc = setup_numeric<float>(ctx);
+        rc = setup_alloc<float>(ctx);
         if (rc != ARAP_OK) return rc;
+        CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
+        rc = setup_enqueue<float>(ctx);
+        if (rc != ARAP_OK) return rc;
+        CK(cudaMemcpyAsync(ctx->herr_host, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (*ctx->herr_host & kErrNotSpd)
+            return fail(ctx, ARAP_ERR_NOT_SPD, "Cholesky factorisation met a non-positive pivot");
+        ctx->state_prec = ARAP_PRECISION_MIXED;
+        ctx->have_rotations = true;
         ctx->dirty = false;
     }
     const Symbolic &s = ctx->sym;
@@ -705,19 +791,26 @@ int arap_invalidate(arap_ctx *ctx) {
     return ARAP_OK;
 }
 
-int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
+int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
     if (iterations < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "negative iteration count");
     if (!ctx->have_rest) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "rest positions not set");
+    if (ctx->in_flight) {
+        const int rc = arap_wait(ctx);
+        if (rc != ARAP_OK) return rc;
+    }
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
-    CK(cudaStreamSynchronize(st));
-    collect_profile(ctx);
+    if (ctx->profiling) {
+        CK(cudaStreamSynchronize(st));
+        collect_profile(ctx);
+    }
     ctx->launches = 0;
     ctx->setup_ms = ctx->iter_ms = 0.0;
     ctx->model_P = ctx->model_T = 1;
     const bool fp64 = ctx->precision == ARAP_PRECISION_FP64;
     CK(cudaEventRecord(ctx->ev0, st));
+    CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
     if (ctx->dirty) {
         {
             Prof pr(ctx, ARAP_K_WEIGHTS);
@@ -735,14 +828,26 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         }
         int rc = prepare_symbolic(ctx);
         if (rc != ARAP_OK) return rc;
-        rc = fp64 ? setup_numeric<double>(ctx) : setup_numeric<float>(ctx);
+        rc = fp64 ? setup_alloc<double>(ctx) : setup_alloc<float>(ctx);
         if (rc != ARAP_OK) return rc;
+        const int64_t key[4] = {ctx->gen, fp64 ? 1 : 2, 0, 0};
+        rc = graph_or_direct(ctx, ctx->g_setup, ctx->g_setup_key, key, ctx->g_setup_launches, [&] {
+            return fp64 ? setup_enqueue<double>(ctx) : setup_enqueue<float>(ctx);
+        });
+        if (rc != ARAP_OK) return rc;
+        ctx->state_prec = fp64 ? ARAP_PRECISION_FP64 : ARAP_PRECISION_MIXED;
+        ctx->have_rotations = true;
         ctx->dirty = false;
     }
     CK(cudaEventRecord(ctx->ev1, st));
-    int rc = ctx->state_prec == ARAP_PRECISION_FP64 ? run_iterations<double>(ctx, iterations)
-                                                     : run_iterations<float>(ctx, iterations);
-    if (rc != ARAP_OK) return rc;
+    if (iterations > 0) {
+        const bool it64 = ctx->state_prec == ARAP_PRECISION_FP64;
+        const int64_t key[4] = {ctx->gen, it64 ? 1 : 2, iterations, ctx->refine};
+        const int rc = graph_or_direct(ctx, ctx->g_iter, ctx->g_iter_key, key, ctx->g_iter_launches, [&] {
+            return it64 ? run_iterations<double>(ctx, iterations) : run_iterations<float>(ctx, iterations);
+        });
+        if (rc != ARAP_OK) return rc;
+    }
     CK(cudaEventRecord(ctx->ev2, st));
     if (out_xyz) {
         {
@@ -753,26 +858,56 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         CK(cudaMemcpyAsync(out_xyz, ctx->out.p, (size_t)3 * ctx->topo.V * sizeof(double), cudaMemcpyDeviceToHost,
                            st));
     }
-    int herr = 0;
-    CK(cudaMemcpyAsync(&herr, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpyAsync(ctx->herr_host, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaGetLastError());
+    ctx->in_flight = true;
+    return ARAP_OK;
+}
+
+int arap_wait(arap_ctx *ctx) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (!ctx->in_flight) return ARAP_OK;
+    ctx->in_flight = false;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
     collect_profile(ctx);
     float a = 0.f, b = 0.f;
     cudaEventElapsedTime(&a, ctx->ev0, ctx->ev1);
     cudaEventElapsedTime(&b, ctx->ev1, ctx->ev2);
     ctx->setup_ms = a;
     ctx->iter_ms = b;
+    const int herr = *ctx->herr_host;
+    if (herr & kErrNotSpd) {
+        ctx->dirty = true;  // as the reference: the next deform sets the problem up again
+        return fail(ctx, ARAP_ERR_NOT_SPD, "Cholesky factorisation met a non-positive pivot");
+    }
     if (herr & kErrTimeout) {
         // scheduling counters may be inconsistent now: rebuild them next time
         ctx->sym_valid = false;
         ctx->dirty = true;
-        return fail(ctx, ARAP_ERR_TIMEOUT, "a triangular-solve wait exceeded its bound");
+        return fail(ctx, ARAP_ERR_TIMEOUT, "a bounded in-kernel wait expired");
     }
+    return ARAP_OK;
+}
+
+int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
+    const int rc = arap_deform_async(ctx, iterations, out_xyz);
+    if (rc != ARAP_OK) return rc;
+    return arap_wait(ctx);
+}
+
+int arap_set_graphs(arap_ctx *ctx, int32_t enable) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    ctx->use_graphs = enable != 0;
     return ARAP_OK;
 }
 
 int arap_get_positions(arap_ctx *ctx, double *out_xyz) {
     if (check_ctx(ctx) || !out_xyz) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
     if (!ctx->sym_valid || ctx->state_prec < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no deformed state yet");
     CK(cudaSetDevice(ctx->device));
     launch_gather_positions(ctx->ds, ctx->pc64.as<Vec4<double>>(), ctx->out.as<double>(), ctx->stream);
@@ -790,6 +925,10 @@ int arap_edge_weights_nnz(arap_ctx *ctx, int32_t *nnz) {
 
 int arap_get_edge_weights(arap_ctx *ctx, int32_t *rowptr, int32_t *col, double *val) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
     const Topology &t = ctx->topo;
     if (rowptr) std::memcpy(rowptr, t.rowptr.data(), t.rowptr.size() * sizeof(int32_t));
     if (col && t.nnz()) std::memcpy(col, t.col.data(), t.col.size() * sizeof(int32_t));
@@ -804,6 +943,10 @@ int arap_get_edge_weights(arap_ctx *ctx, int32_t *rowptr, int32_t *col, double *
 
 int arap_get_rotations(arap_ctx *ctx, double *R9) {
     if (check_ctx(ctx) || !R9) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
     const int V = ctx->topo.V;
     if (!ctx->have_rotations || !ctx->sym_valid) {
         for (int v = 0; v < V; ++v)
