@@ -367,7 +367,7 @@ __global__ void k_bsetup(int V, int m, int P, const Vec4<double> *__restrict__ p
 // bFixed per pose (arap.h:325-327), adjacency order as in k_assemble
 __global__ void k_bbfixed(int m, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
                           const double *__restrict__ w64, const Vec4<double> *__restrict__ pc64,
-                          Vec4<float> *__restrict__ bfixed) {
+                          Vec4<double> *__restrict__ bfixed) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)m * P) return;
     const int k = (int)(t / P), p = (int)(t % P);
@@ -381,24 +381,25 @@ __global__ void k_bbfixed(int m, int P, const int32_t *__restrict__ drow, const 
         by = __dadd_rn(by, __dmul_rn(w, c.y));
         bz = __dadd_rn(bz, __dmul_rn(w, c.z));
     }
-    bfixed[t] = {(float)bx, (float)by, (float)bz, 0.f};
+    bfixed[t] = {bx, by, bz, 0.0};
 }
 
-// estimateRotations per pose (arap.h:354-384)
+// estimateRotations per pose (arap.h:354-384): FP32 covariance from the FP32
+// rest edges and the pose's current edges differenced in FP64
 __global__ void __launch_bounds__(256)
 k_blocal(int V, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const float *__restrict__ w,
-         const Vec4<float> *__restrict__ p32, const Vec4<float> *__restrict__ pc32, Vec4<float> *__restrict__ R) {
+         const Vec4<float> *__restrict__ redge, const Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ R) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)V * P) return;
     const int i = (int)(t / P), p = (int)(t % P);
-    const Vec4<float> pi = p32[i], ci = pc32[t];
+    const Vec4<double> ci = pc64[t];
     float S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     for (int e = drow[i]; e < drow[i + 1]; ++e) {
-        const int j = dcol[e];
         const float wj = w[e];
-        const Vec4<float> pj = p32[j], cj = pc32[(int64_t)j * P + p];
-        const float ex = wj * (pi.x - pj.x), ey = wj * (pi.y - pj.y), ez = wj * (pi.z - pj.z);
-        const float fx = ci.x - cj.x, fy = ci.y - cj.y, fz = ci.z - cj.z;
+        const Vec4<float> re = redge[e];
+        const Vec4<double> cj = pc64[(int64_t)dcol[e] * P + p];
+        const float ex = wj * re.x, ey = wj * re.y, ez = wj * re.z;
+        const float fx = (float)(ci.x - cj.x), fy = (float)(ci.y - cj.y), fz = (float)(ci.z - cj.z);
         S[0][0] += ex * fx; S[0][1] += ex * fy; S[0][2] += ex * fz;
         S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
         S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
@@ -410,37 +411,35 @@ k_blocal(int V, int P, const int32_t *__restrict__ drow, const int32_t *__restri
     R[3 * t + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], 0.f};
 }
 
-// estimatePositions RHS per pose (arap.h:395-414)
+// estimatePositions RHS terms per pose (arap.h:395-414), bFixed added in FP64
+// by the residual
 __global__ void __launch_bounds__(256)
 k_brhs(int m, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const float *__restrict__ w,
-       const Vec4<float> *__restrict__ p32, const Vec4<float> *__restrict__ R, const Vec4<float> *__restrict__ bfixed,
-       Vec4<float> *__restrict__ b) {
+       const Vec4<float> *__restrict__ redge, const Vec4<float> *__restrict__ R, Vec4<float> *__restrict__ b) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)m * P) return;
     const int i = (int)(t / P), p = (int)(t % P);
-    const Vec4<float> pi = p32[i];
     const Vec4<float> r0 = R[3 * t], r1 = R[3 * t + 1], r2 = R[3 * t + 2];
-    Vec4<float> acc = bfixed[t];
+    float ax = 0.f, ay = 0.f, az = 0.f;
     for (int e = drow[i]; e < drow[i + 1]; ++e) {
         const int j = dcol[e];
         if (j == i) continue;
         const float h = w[e] * 0.5f;
-        const Vec4<float> pj = p32[j];
+        const Vec4<float> d = redge[e];
         const int64_t tj = (int64_t)j * P + p;
         const Vec4<float> q0 = R[3 * tj], q1 = R[3 * tj + 1], q2 = R[3 * tj + 2];
-        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-        acc.x += ((r0.x + q0.x) * dx + (r0.y + q0.y) * dy + (r0.z + q0.z) * dz) * h;
-        acc.y += ((r1.x + q1.x) * dx + (r1.y + q1.y) * dy + (r1.z + q1.z) * dz) * h;
-        acc.z += ((r2.x + q2.x) * dx + (r2.y + q2.y) * dy + (r2.z + q2.z) * dz) * h;
+        ax += ((r0.x + q0.x) * d.x + (r0.y + q0.y) * d.y + (r0.z + q0.z) * d.z) * h;
+        ay += ((r1.x + q1.x) * d.x + (r1.y + q1.y) * d.y + (r1.z + q1.z) * d.z) * h;
+        az += ((r2.x + q2.x) * d.x + (r2.y + q2.y) * d.y + (r2.z + q2.z) * d.z) * h;
     }
-    b[t] = acc;
+    b[t] = {ax, ay, az, 0.f};
 }
 
 // r = b - A x in FP64 per pose
 __global__ void __launch_bounds__(256)
 k_bresidual(int m, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
-            const double *__restrict__ w64, const double *__restrict__ diag64, const Vec4<float> *__restrict__ b,
-            const Vec4<double> *__restrict__ x, Vec4<float> *__restrict__ r) {
+            const double *__restrict__ w64, const double *__restrict__ diag64, const Vec4<double> *__restrict__ bfixed,
+            const Vec4<float> *__restrict__ b, const Vec4<double> *__restrict__ x, Vec4<float> *__restrict__ r) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)m * P) return;
     const int i = (int)(t / P), p = (int)(t % P);
@@ -457,7 +456,9 @@ k_bresidual(int m, int P, const int32_t *__restrict__ drow, const int32_t *__res
         az -= wj * xj.z;
     }
     const Vec4<float> bi = b[t];
-    r[t] = {(float)((double)bi.x - ax), (float)((double)bi.y - ay), (float)((double)bi.z - az), 0.f};
+    const Vec4<double> bf = bfixed[t];
+    r[t] = {(float)((bf.x + (double)bi.x) - ax), (float)((bf.y + (double)bi.y) - ay),
+            (float)((bf.z + (double)bi.z) - az), 0.f};
 }
 
 // positions of every pose back to vertex order: out[p][v][3]
@@ -516,28 +517,28 @@ void launch_bsetup(const DevSym &s, int P, const Vec4<double> *p64, const double
     if (n) k_bsetup<<<nblocks(n, 256), 256, 0, st>>>(s.V, s.m, P, p64, targets, pc64, pc32, R);
 }
 
-void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double> *pc64, Vec4<float> *bfixed,
+void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double> *pc64, Vec4<double> *bfixed,
                     cudaStream_t st) {
     const int64_t n = (int64_t)s.m * P;
     if (n) k_bbfixed<<<nblocks(n, 256), 256, 0, st>>>(s.m, P, s.drow, s.dcol, w64, pc64, bfixed);
 }
 
-void launch_blocal(const DevSym &s, int P, const float *w32, const Vec4<float> *p32, const Vec4<float> *pc32,
+void launch_blocal(const DevSym &s, int P, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
                    Vec4<float> *R, cudaStream_t st) {
     const int64_t n = (int64_t)s.V * P;
-    if (n) k_blocal<<<nblocks(n, 256), 256, 0, st>>>(s.V, P, s.drow, s.dcol, w32, p32, pc32, R);
+    if (n) k_blocal<<<nblocks(n, 256), 256, 0, st>>>(s.V, P, s.drow, s.dcol, w32, redge, pc64, R);
 }
 
-void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *p32, const Vec4<float> *R,
-                 const Vec4<float> *bfixed, Vec4<float> *b, cudaStream_t st) {
+void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,
+                 Vec4<float> *b, cudaStream_t st) {
     const int64_t n = (int64_t)s.m * P;
-    if (n) k_brhs<<<nblocks(n, 256), 256, 0, st>>>(s.m, P, s.drow, s.dcol, w32, p32, R, bfixed, b);
+    if (n) k_brhs<<<nblocks(n, 256), 256, 0, st>>>(s.m, P, s.drow, s.dcol, w32, redge, R, b);
 }
 
-void launch_bresidual(const DevSym &s, int P, const double *w64, const double *diag64, const Vec4<float> *b,
-                      const Vec4<double> *x, Vec4<float> *r, cudaStream_t st) {
+void launch_bresidual(const DevSym &s, int P, const double *w64, const double *diag64, const Vec4<double> *bfixed,
+                      const Vec4<float> *b, const Vec4<double> *x, Vec4<float> *r, cudaStream_t st) {
     const int64_t n = (int64_t)s.m * P;
-    if (n) k_bresidual<<<nblocks(n, 256), 256, 0, st>>>(s.m, P, s.drow, s.dcol, w64, diag64, b, x, r);
+    if (n) k_bresidual<<<nblocks(n, 256), 256, 0, st>>>(s.m, P, s.drow, s.dcol, w64, diag64, bfixed, b, x, r);
 }
 
 void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *out, cudaStream_t st) {

@@ -77,7 +77,7 @@ struct arap_ctx {
     DevBuf rest, targets, out;
     DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn, fitems;
     int factor_smem_ncol = 0;
-    DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T;
+    DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T, redge;
     DevBuf errw, ticket, flags;
     // many-pose state (arap_deform_poses)
     DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
@@ -255,7 +255,7 @@ int setup_alloc(arap_ctx *ctx) {
     const size_t nnz = s.dcol.size();
     DevBuf *bufs[] = {&ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32, &ctx->pc32, &ctx->R, &ctx->diag64,
                       &ctx->bfixed, &ctx->b, &ctx->sol, &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd,
-                      &ctx->Xinv, &ctx->L21, &ctx->L21T};
+                      &ctx->Xinv, &ctx->L21, &ctx->L21T, &ctx->redge};
     void *before[sizeof(bufs) / sizeof(bufs[0])];
     for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i) before[i] = bufs[i]->p;
     CK(ctx->w64.ensure(nnz * sizeof(double)));
@@ -268,7 +268,8 @@ int setup_alloc(arap_ctx *ctx) {
     }
     CK(ctx->R.ensure((size_t)V * 3 * sizeof(Vec4<T>)));
     CK(ctx->diag64.ensure((size_t)std::max(m, 1) * sizeof(double)));
-    CK(ctx->bfixed.ensure((size_t)std::max(m, 1) * sizeof(Vec4<T>)));
+    CK(ctx->bfixed.ensure((size_t)std::max(m, 1) * sizeof(Vec4<double>)));
+    if (sizeof(T) == 4) CK(ctx->redge.ensure(std::max<size_t>(nnz, 1) * sizeof(Vec4<float>)));
     CK(ctx->b.ensure((size_t)std::max(m, 1) * sizeof(Vec4<T>)));
     CK(ctx->sol.ensure((size_t)std::max(m, 1) * sizeof(Vec4<T>)));
     CK(ctx->uvec.ensure((size_t)std::max<int64_t>(s.uvec_size, 1) * sizeof(Vec4<T>)));
@@ -307,8 +308,9 @@ int setup_enqueue(arap_ctx *ctx) {
         Prof pr(ctx, ARAP_K_ASSEMBLE);
         launch_setup_vertices<T>(d, ctx->rest.as<double>(), ctx->targets.as<double>(), ctx->p64.as<Vec4<double>>(),
                                  ctx->pc64.as<Vec4<double>>(), p_t, pc_t, ctx->R.as<Vec4<T>>(), st);
+        if (sizeof(T) == 4) launch_rest_edges(d, ctx->p64.as<Vec4<double>>(), ctx->redge.as<Vec4<float>>(), st);
     }
-    ctx->launches += 2;
+    ctx->launches += sizeof(T) == 4 ? 3 : 2;
     if (m > 0) {
         CK(cudaMemsetAsync(ctx->Lval.p, 0, (size_t)s.panel_size * sizeof(T), st));
         if (s.upd_size > 0) CK(cudaMemsetAsync(ctx->Upd.p, 0, (size_t)s.upd_size * sizeof(T), st));
@@ -317,8 +319,8 @@ int setup_enqueue(arap_ctx *ctx) {
         if (s.l21t_size > 0) CK(cudaMemsetAsync(ctx->L21T.p, 0, (size_t)s.l21t_size * sizeof(T), st));
         {
             Prof pr(ctx, ARAP_K_ASSEMBLE);
-            launch_assemble<T, T>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->Lval.as<T>(),
-                                  ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<T>>(), st);
+            launch_assemble<T>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->Lval.as<T>(),
+                               ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<double>>(), st);
         }
         ctx->launches += 1;
         for (const FactorLaunch &fl : s.fplan) {
@@ -418,22 +420,22 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
     for (int it = 0; it < iterations; ++it) {
         {
             Prof pr(ctx, ARAP_K_LOCAL);
-            launch_local_step<float>(d, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(),
-                                     ctx->pc32.as<Vec4<float>>(), ctx->R.as<Vec4<float>>(), st);
+            launch_local_step_mixed(d, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(),
+                                    ctx->pc64.as<Vec4<double>>(), ctx->R.as<Vec4<float>>(), st);
         }
         ctx->launches += 1;
         if (s.m == 0) continue;
         {
             Prof pr(ctx, ARAP_K_RHS);
-            launch_rhs<float>(d, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->R.as<Vec4<float>>(),
-                              ctx->bfixed.as<Vec4<float>>(), ctx->b.as<Vec4<float>>(), st);
+            launch_rhs_mixed(d, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(), ctx->R.as<Vec4<float>>(),
+                             ctx->b.as<Vec4<float>>(), st);
         }
         ctx->launches += 1;
         for (int r = 0; r <= ctx->refine; ++r) {
             {
                 Prof pr(ctx, ARAP_K_RESIDUAL);
-                launch_residual(d, ctx->w64.as<double>(), ctx->diag64.as<double>(), ctx->b.as<Vec4<float>>(),
-                                ctx->pc64.as<Vec4<double>>(), ctx->sol.as<Vec4<float>>(), st);
+                launch_residual(d, ctx->w64.as<double>(), ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<double>>(),
+                                ctx->b.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(), ctx->sol.as<Vec4<float>>(), st);
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_FWD);
@@ -690,7 +692,7 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
         CK(ctx->bpc64.ensure(VP * sizeof(Vec4<double>)));
         CK(ctx->bpc32.ensure(VP * sizeof(Vec4<float>)));
         CK(ctx->bR.ensure(VP * 3 * sizeof(Vec4<float>)));
-        CK(ctx->bbfixed.ensure(MP * sizeof(Vec4<float>)));
+        CK(ctx->bbfixed.ensure(MP * sizeof(Vec4<double>)));
         CK(ctx->bb.ensure(MP * sizeof(Vec4<float>)));
         CK(ctx->bsol.ensure(MP * sizeof(Vec4<float>)));
         CK(ctx->buvec.ensure((size_t)std::max<int64_t>(s.uvec_size, 1) * P * sizeof(Vec4<float>)));
@@ -714,7 +716,7 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
         Prof pr(ctx, ARAP_K_ASSEMBLE);
         launch_bsetup(d, P, ctx->p64.as<Vec4<double>>(), ctx->btargets.as<double>(), ctx->bpc64.as<Vec4<double>>(),
                       ctx->bpc32.as<Vec4<float>>(), ctx->bR.as<Vec4<float>>(), st);
-        launch_bbfixed(d, P, ctx->w64.as<double>(), ctx->bpc64.as<Vec4<double>>(), ctx->bbfixed.as<Vec4<float>>(),
+        launch_bbfixed(d, P, ctx->w64.as<double>(), ctx->bpc64.as<Vec4<double>>(), ctx->bbfixed.as<Vec4<double>>(),
                        st);
     }
     ctx->launches += 2;
@@ -727,21 +729,22 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
     for (int it = 0; it < iterations; ++it) {
         {
             Prof pr(ctx, ARAP_K_LOCAL);
-            launch_blocal(d, P, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->bpc32.as<Vec4<float>>(),
+            launch_blocal(d, P, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
                           ctx->bR.as<Vec4<float>>(), st);
         }
         ctx->launches += 1;
         if (m == 0) continue;
         {
             Prof pr(ctx, ARAP_K_RHS);
-            launch_brhs(d, P, ctx->w32.as<float>(), ctx->p32.as<Vec4<float>>(), ctx->bR.as<Vec4<float>>(),
-                        ctx->bbfixed.as<Vec4<float>>(), ctx->bb.as<Vec4<float>>(), st);
+            launch_brhs(d, P, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(), ctx->bR.as<Vec4<float>>(),
+                        ctx->bb.as<Vec4<float>>(), st);
         }
         ctx->launches += 1;
         for (int r = 0; r <= ctx->refine; ++r) {
             {
                 Prof pr(ctx, ARAP_K_RESIDUAL);
-                launch_bresidual(d, P, ctx->w64.as<double>(), ctx->diag64.as<double>(), ctx->bb.as<Vec4<float>>(),
+                launch_bresidual(d, P, ctx->w64.as<double>(), ctx->diag64.as<double>(),
+                                 ctx->bbfixed.as<Vec4<double>>(), ctx->bb.as<Vec4<float>>(),
                                  ctx->bpc64.as<Vec4<double>>(), ctx->bsol.as<Vec4<float>>(), st);
             }
             {

@@ -146,11 +146,11 @@ __global__ void k_setup_vertices(int V, int m, const int32_t *__restrict__ oldid
 // setupLinearSystem, arap.h:310-336: L_kk = sum_j w_kj, L_lk = -w_kl for free
 // l > k (written into the supernodal panel of column k), bFixed_k = sum over
 // constrained neighbours of w_kj * c_j, all summed in adjacency order.
-template <typename TF, typename T>
+template <typename TF>
 __global__ void k_assemble(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
                            const double *__restrict__ w64, const int64_t *__restrict__ amap,
                            const int64_t *__restrict__ dmap, const Vec4<double> *__restrict__ pc64,
-                           TF *__restrict__ Lval, double *__restrict__ diag64, Vec4<T> *__restrict__ bfixed) {
+                           TF *__restrict__ Lval, double *__restrict__ diag64, Vec4<double> *__restrict__ bfixed) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     double diag = 0.0, bx = 0.0, by = 0.0, bz = 0.0;
@@ -170,7 +170,22 @@ __global__ void k_assemble(int m, const int32_t *__restrict__ drow, const int32_
     }
     Lval[dmap[k]] = (TF)diag;
     diag64[k] = diag;
-    bfixed[k] = {(T)bx, (T)by, (T)bz, (T)0};
+    bfixed[k] = {bx, by, bz, 0.0};
+}
+
+// Rest edge vectors p_k - p_l per adjacency entry, differenced in FP64 and
+// stored in FP32: exact to FP32 rounding of the (short) edge itself, where
+// differencing FP32 positions would lose the digits the positions' magnitude
+// takes.
+__global__ void k_rest_edges(int V, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
+                             const Vec4<double> *__restrict__ p64, Vec4<float> *__restrict__ redge) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= V) return;
+    const Vec4<double> pk = p64[k];
+    for (int e = drow[k]; e < drow[k + 1]; ++e) {
+        const Vec4<double> pl = p64[dcol[e]];
+        redge[e] = {(float)(pk.x - pl.x), (float)(pk.y - pl.y), (float)(pk.z - pl.z), 0.f};
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -506,6 +521,58 @@ k_local_step(int V, const int32_t *__restrict__ drow, const int32_t *__restrict_
     R[3 * (int64_t)i + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], (T)0};
 }
 
+// Local step of the mixed form: the covariance in FP32 from the FP32 rest
+// edges and the current edges differenced in FP64 (the positions are kept in
+// FP64), then the FP32 rotation fit.
+__global__ void __launch_bounds__(256)
+k_local_step_mixed(int V, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
+                   const float *__restrict__ w, const Vec4<float> *__restrict__ redge,
+                   const Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ R) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const Vec4<double> ci = pc64[i];
+    float S[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    const int e1 = drow[i + 1];
+    for (int e = drow[i]; e < e1; ++e) {
+        const float wj = w[e];
+        const Vec4<float> re = redge[e];
+        const Vec4<double> cj = pc64[dcol[e]];
+        const float ex = wj * re.x, ey = wj * re.y, ez = wj * re.z;
+        const float fx = (float)(ci.x - cj.x), fy = (float)(ci.y - cj.y), fz = (float)(ci.z - cj.z);
+        S[0][0] += ex * fx; S[0][1] += ex * fy; S[0][2] += ex * fz;
+        S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
+        S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
+    }
+    float Rm[3][3];
+    rotation_from_cov(S, Rm);
+    R[3 * (int64_t)i + 0] = {Rm[0][0], Rm[0][1], Rm[0][2], 0.f};
+    R[3 * (int64_t)i + 1] = {Rm[1][0], Rm[1][1], Rm[1][2], 0.f};
+    R[3 * (int64_t)i + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], 0.f};
+}
+
+// RHS of the mixed form without bFixed (added in FP64 by the residual):
+// sum_j 1/2 w (R_i + R_j)(p_i - p_j) over the FP32 rest edges.
+__global__ void __launch_bounds__(256)
+k_rhs_mixed(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const float *__restrict__ w,
+            const Vec4<float> *__restrict__ redge, const Vec4<float> *__restrict__ R, Vec4<float> *__restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const Vec4<float> r0 = R[3 * (int64_t)i], r1 = R[3 * (int64_t)i + 1], r2 = R[3 * (int64_t)i + 2];
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    const int e1 = drow[i + 1];
+    for (int e = drow[i]; e < e1; ++e) {
+        const int j = dcol[e];
+        if (j == i) continue;
+        const float h = w[e] * 0.5f;
+        const Vec4<float> d = redge[e];
+        const Vec4<float> q0 = R[3 * (int64_t)j], q1 = R[3 * (int64_t)j + 1], q2 = R[3 * (int64_t)j + 2];
+        ax += ((r0.x + q0.x) * d.x + (r0.y + q0.y) * d.y + (r0.z + q0.z) * d.z) * h;
+        ay += ((r1.x + q1.x) * d.x + (r1.y + q1.y) * d.y + (r1.z + q1.z) * d.z) * h;
+        az += ((r2.x + q2.x) * d.x + (r2.y + q2.y) * d.y + (r2.z + q2.z) * d.z) * h;
+    }
+    b[i] = {ax, ay, az, 0.f};
+}
+
 // estimatePositions RHS, arap.h:395-414
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -535,8 +602,8 @@ k_rhs(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
 // r = b - A x in FP64 over the free vertices (A = constrained Laplacian)
 __global__ void __launch_bounds__(256)
 k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const double *__restrict__ w64,
-           const double *__restrict__ diag64, const Vec4<float> *__restrict__ b, const Vec4<double> *__restrict__ x,
-           Vec4<float> *__restrict__ r) {
+           const double *__restrict__ diag64, const Vec4<double> *__restrict__ bfixed,
+           const Vec4<float> *__restrict__ b, const Vec4<double> *__restrict__ x, Vec4<float> *__restrict__ r) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const Vec4<double> xi = x[i];
@@ -553,7 +620,9 @@ k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ 
         az -= wj * xj.z;
     }
     const Vec4<float> bi = b[i];
-    r[i] = {(float)((double)bi.x - ax), (float)((double)bi.y - ay), (float)((double)bi.z - az), 0.f};
+    const Vec4<double> bf = bfixed[i];
+    r[i] = {(float)((bf.x + (double)bi.x) - ax), (float)((bf.y + (double)bi.y) - ay),
+            (float)((bf.z + (double)bi.z) - az), 0.f};
 }
 
 // ---------------------------------------------------------------------------
@@ -992,12 +1061,29 @@ void launch_setup_vertices(const DevSym &s, const double *rest_xyz, const double
                                                               p_t, pc_t, R);
 }
 
-template <typename TF, typename T>
+template <typename TF>
 void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc64, TF *Lval, double *diag64,
-                     Vec4<T> *bfixed, cudaStream_t st) {
+                     Vec4<double> *bfixed, cudaStream_t st) {
     if (s.m == 0) return;
-    k_assemble<TF, T><<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, s.amap, s.dmap, pc64, Lval,
-                                                            diag64, bfixed);
+    k_assemble<TF><<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, s.amap, s.dmap, pc64, Lval,
+                                                         diag64, bfixed);
+}
+
+void launch_rest_edges(const DevSym &s, const Vec4<double> *p64, Vec4<float> *redge, cudaStream_t st) {
+    if (s.V == 0) return;
+    k_rest_edges<<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.drow, s.dcol, p64, redge);
+}
+
+void launch_local_step_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
+                             Vec4<float> *R, cudaStream_t st) {
+    if (s.V == 0) return;
+    k_local_step_mixed<<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.drow, s.dcol, w32, redge, pc64, R);
+}
+
+void launch_rhs_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,
+                      Vec4<float> *b, cudaStream_t st) {
+    if (s.m == 0) return;
+    k_rhs_mixed<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w32, redge, R, b);
 }
 
 template <typename TF>
@@ -1032,10 +1118,10 @@ void launch_rhs(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *R,
     k_rhs<T><<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w, p, R, bfixed, b);
 }
 
-void launch_residual(const DevSym &s, const double *w64, const double *diag64, const Vec4<float> *b,
-                     const Vec4<double> *x64, Vec4<float> *r, cudaStream_t st) {
+void launch_residual(const DevSym &s, const double *w64, const double *diag64, const Vec4<double> *bfixed,
+                     const Vec4<float> *b, const Vec4<double> *x64, Vec4<float> *r, cudaStream_t st) {
     if (s.m == 0) return;
-    k_residual<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, b, x64, r);
+    k_residual<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, bfixed, b, x64, r);
 }
 
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
@@ -1102,10 +1188,10 @@ template void launch_setup_vertices<float>(const DevSym &, const double *, const
 template void launch_setup_vertices<double>(const DevSym &, const double *, const double *, Vec4<double> *,
                                             Vec4<double> *, Vec4<double> *, Vec4<double> *, Vec4<double> *,
                                             cudaStream_t);
-template void launch_assemble<float, float>(const DevSym &, const double *, const Vec4<double> *, float *, double *,
-                                            Vec4<float> *, cudaStream_t);
-template void launch_assemble<double, double>(const DevSym &, const double *, const Vec4<double> *, double *,
-                                              double *, Vec4<double> *, cudaStream_t);
+template void launch_assemble<float>(const DevSym &, const double *, const Vec4<double> *, float *, double *,
+                                     Vec4<double> *, cudaStream_t);
+template void launch_assemble<double>(const DevSym &, const double *, const Vec4<double> *, double *, double *,
+                                      Vec4<double> *, cudaStream_t);
 template void launch_factor_step<float>(const DevSym &, const FactorLaunch &, const FItem *, float *, float *,
                                         float *, float *, float *, float *, int *, cudaStream_t);
 template void launch_factor_step<double>(const DevSym &, const FactorLaunch &, const FItem *, double *, double *,

@@ -58,9 +58,17 @@ void launch_setup_vertices(const DevSym &s, const double *rest_xyz, const double
                            Vec4<double> *p64, Vec4<double> *pc64, Vec4<T> *p_t, Vec4<T> *pc_t, Vec4<T> *R,
                            cudaStream_t st);
 // constrained Laplacian into the supernodal panels + bFixed (arap.h:292-336)
-template <typename TF, typename T>
+template <typename TF>
 void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc64, TF *Lval, double *diag64,
-                     Vec4<T> *bfixed, cudaStream_t st);
+                     Vec4<double> *bfixed, cudaStream_t st);
+// FP32 rest edge vectors per adjacency entry, differenced in FP64
+void launch_rest_edges(const DevSym &s, const Vec4<double> *p64, Vec4<float> *redge, cudaStream_t st);
+// mixed form: FP32 covariance from FP32 rest edges and FP64-differenced current edges
+void launch_local_step_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
+                             Vec4<float> *R, cudaStream_t st);
+// mixed form: the RHS terms sum 1/2 w (Ri+Rj)(pi-pj) without bFixed
+void launch_rhs_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,
+                      Vec4<float> *b, cudaStream_t st);
 // one launch of the multifrontal Cholesky plan (Symbolic::fplan); the last
 // launches of a level also write X = inverse of L11 and the aligned copies of
 // L21 and L21^T that the solves read
@@ -75,9 +83,9 @@ void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4
 template <typename T>
 void launch_rhs(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *R, const Vec4<T> *bfixed,
                 Vec4<T> *b, cudaStream_t st);
-// FP64 residual of the global system: r = b - A x over the free vertices
-void launch_residual(const DevSym &s, const double *w64, const double *diag64, const Vec4<float> *b,
-                     const Vec4<double> *x64, Vec4<float> *r, cudaStream_t st);
+// FP64 residual of the global system: r = (bFixed + b) - A x over the free vertices
+void launch_residual(const DevSym &s, const double *w64, const double *diag64, const Vec4<double> *bfixed,
+                     const Vec4<float> *b, const Vec4<double> *x64, Vec4<float> *r, cudaStream_t st);
 // supernodal triangular solves L y = b (forward) and L^T x = y (backward),
 // one launch each, supernodes scheduled by a ticket counter with bounded waits.
 // mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k and pc32[k] = float(pc64[k]).
@@ -98,14 +106,14 @@ int batch_pose_tile(int max_ldx, int max_ld21);
 cudaError_t configure_batch_smem(int max_ldx, int max_ld21, int pt);
 void launch_bsetup(const DevSym &s, int P, const Vec4<double> *p64, const double *targets, Vec4<double> *pc64,
                    Vec4<float> *pc32, Vec4<float> *R, cudaStream_t st);
-void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double> *pc64, Vec4<float> *bfixed,
+void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double> *pc64, Vec4<double> *bfixed,
                     cudaStream_t st);
-void launch_blocal(const DevSym &s, int P, const float *w32, const Vec4<float> *p32, const Vec4<float> *pc32,
+void launch_blocal(const DevSym &s, int P, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
                    Vec4<float> *R, cudaStream_t st);
-void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *p32, const Vec4<float> *R,
-                 const Vec4<float> *bfixed, Vec4<float> *b, cudaStream_t st);
-void launch_bresidual(const DevSym &s, int P, const double *w64, const double *diag64, const Vec4<float> *b,
-                      const Vec4<double> *x, Vec4<float> *r, cudaStream_t st);
+void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,
+                 Vec4<float> *b, cudaStream_t st);
+void launch_bresidual(const DevSym &s, int P, const double *w64, const double *diag64, const Vec4<double> *bfixed,
+                      const Vec4<float> *b, const Vec4<double> *x, Vec4<float> *r, cudaStream_t st);
 void launch_bsolve(const DevSym &s, int P, int pt, const float *X, const float *L21, const float *L21T,
                    Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
                    unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st);
