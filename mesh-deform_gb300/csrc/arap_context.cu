@@ -75,7 +75,7 @@ struct arap_ctx {
     // device buffers
     DevBuf faces, ent_ptr, ent_fc, hc, w_orig;
     DevBuf rest, targets, out;
-    DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn, fitems, leaves;
+    DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn, fitems;
     int factor_smem_ncol = 0;
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T, redge;
     DevBuf errw, ticket, flags;
@@ -194,7 +194,6 @@ int prepare_symbolic(arap_ctx *ctx) {
     CK(upload(ctx->child, s.child, st));
     CK(upload(ctx->level_sn, s.level_sn, st));
     CK(upload(ctx->fitems, s.fitems, st));
-    CK(upload(ctx->leaves, s.leaves, st));
     if (s.max_ncol > ctx->factor_smem_ncol) {
         CK(configure_factor_smem(s.max_ncol));
         ctx->factor_smem_ncol = s.max_ncol;
@@ -239,8 +238,6 @@ int prepare_symbolic(arap_ctx *ctx) {
     d.relind = ctx->relind.as<int32_t>();
     d.child = ctx->child.as<int32_t>();
     d.level_sn = ctx->level_sn.as<int32_t>();
-    d.leaves = ctx->leaves.as<int32_t>();
-    d.nleaves = (int)s.leaves.size();
     ctx->sym_valid = true;
     return ARAP_OK;
 }
@@ -557,7 +554,7 @@ void arap_destroy(arap_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->faces, &ctx->ent_ptr, &ctx->ent_fc, &ctx->hc, &ctx->w_orig, &ctx->rest,
                       &ctx->targets, &ctx->out, &ctx->drow, &ctx->dcol, &ctx->dent, &ctx->oldidx,
                       &ctx->amap, &ctx->dmap, &ctx->sn, &ctx->rows, &ctx->relind, &ctx->child,
-                      &ctx->level_sn, &ctx->fitems, &ctx->leaves, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
+                      &ctx->level_sn, &ctx->fitems, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
                       &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
                       &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->L21T, &ctx->errw, &ctx->ticket,
                       &ctx->flags, &ctx->btargets, &ctx->bpc64, &ctx->bpc32, &ctx->bR, &ctx->bbfixed,

@@ -769,17 +769,14 @@ struct SolveSmem {
 
 // Forward: for supernode s (children first), f = [b(cols); 0] plus the
 // children's update vectors; y = X f(cols); u_s = f(struct) - L21 y goes to
-// the parent. One CTA per leaf; after a supernode the CTA counts itself in at
-// its parent and, if it is the parent's last child to finish, goes on with the
-// parent (the other children's results are visible: each of them fenced its
-// stores before counting). No CTA ever waits; the counters only grow, each
-// sweep adding the parent's number of children.
+// the parent. Tickets follow `order` (level by level, leaves first), so a CTA
+// only waits for CTAs that started before it.
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads, 3)
-k_solve_fwd(SolveSmem lay, const int32_t *__restrict__ leaves, const SnInfo *__restrict__ sn,
+k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
             const int32_t *__restrict__ child, const int32_t *__restrict__ relind, const T *__restrict__ Xall,
             const T *__restrict__ L21all, Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec,
-            unsigned *counters, int *err) {
+            unsigned long long *ticket, unsigned *flags, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T *buf0 = reinterpret_cast<T *>(smem_raw);
     T *buf1 = reinterpret_cast<T *>(smem_raw + kChunkBytes);
@@ -788,32 +785,79 @@ k_solve_fwd(SolveSmem lay, const int32_t *__restrict__ leaves, const SnInfo *__r
     Vec4<T> *fb = yv + lay.ldx_max;
     Vec4<T> *red = fb + lay.ld21_max;
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_last;
+    __shared__ int s_task;
+    __shared__ unsigned s_epoch;
     const int tid = threadIdx.x;
     if (tid == 0) {
+        const unsigned long long t = atomicAdd(ticket, 1ull);
+        s_task = order[(int)(t % (unsigned long long)S)];
+        s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    unsigned uses0 = 0, uses1 = 0;  // completed phases of each buffer's barrier
-    int s = leaves[blockIdx.x];
-    for (;;) {
-        const SnInfo d = sn[s];
-        const int nc = d.ncol, nb = d.nrow - d.ncol;
-        ChunkPlan<T> pl;
-        pl.init(Xall + d.x_off, d.ldx, nc, L21all + d.l21_off, d.ld21, nb > 0 ? nc : 0);
-        const int ntot = pl.total();
-        if (tid == 0) {
-            issue_chunk(pl, 0, buf0, &bars[0]);
-            if (ntot > 1) issue_chunk(pl, 1, buf1, &bars[1]);
-            for (int k = 2; k < ntot; ++k) prefetch_chunk_l2(pl, k);
+    const int s = s_task;
+    const unsigned epoch = s_epoch;
+    const SnInfo d = sn[s];
+    const int nc = d.ncol, nb = d.nrow - d.ncol;
+    ChunkPlan<T> pl;
+    pl.init(Xall + d.x_off, d.ldx, nc, L21all + d.l21_off, d.ld21, nb > 0 ? nc : 0);
+    const int ntot = pl.total();
+    if (tid == 0) {
+        issue_chunk(pl, 0, buf0, &bars[0]);
+        if (ntot > 1) issue_chunk(pl, 1, buf1, &bars[1]);
+        for (int k = 2; k < ntot; ++k) prefetch_chunk_l2(pl, k);
+    }
+    for (int i = tid; i < d.ldx; i += kSolveThreads)
+        fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+    for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
+    // the children's entries of this thread (child-major list, kPull per thread):
+    // positions are read before waiting, update vectors in one round trip after
+    constexpr int kPull = 4;
+    int pci[kPull], ppos[kPull], puo[kPull];
+    {
+        int base = 0, u = 0;
+        for (int ci = d.child_begin; ci < d.child_end && u < kPull; ++ci) {
+            const SnInfo c = sn[child[ci]];
+            const int nbc = c.nrow - c.ncol;
+            for (int i = tid - base; i < nbc && u < kPull; i += kSolveThreads) {
+                if (i < 0) continue;
+                pci[u] = ci;
+                ppos[u] = relind[c.relind_off + i];
+                puo[u] = (int)c.uvec_off + i;
+                ++u;
+            }
+            base += nbc;
         }
-        for (int i = tid; i < d.ldx; i += kSolveThreads)
-            fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
-        for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
-        __syncthreads();
+        for (; u < kPull; ++u) pci[u] = -1;
+    }
+    int total_children_rows = 0;
+    for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+        const SnInfo c = sn[child[ci]];
+        total_children_rows += c.nrow - c.ncol;
+    }
+    if (tid == 0)
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
+    __syncthreads();
+    if (total_children_rows <= kPull * kSolveThreads) {
+        Vec4<T> pu[kPull];
+#pragma unroll
+        for (int u = 0; u < kPull; ++u)
+            if (pci[u] >= 0) pu[u] = ldcg4(uvec + puo[u]);
         for (int ci = d.child_begin; ci < d.child_end; ++ci) {  // children in order
+#pragma unroll
+            for (int u = 0; u < kPull; ++u) {
+                if (pci[u] != ci) continue;
+                Vec4<T> &t = ppos[u] < nc ? fc[ppos[u]] : fb[ppos[u] - nc];
+                t.x += pu[u].x;
+                t.y += pu[u].y;
+                t.z += pu[u].z;
+            }
+            __syncthreads();
+        }
+    } else {
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) {
             const SnInfo c = sn[child[ci]];
             const int nbc = c.nrow - c.ncol;
             const int32_t *ri = relind + c.relind_off;
@@ -827,51 +871,38 @@ k_solve_fwd(SolveSmem lay, const int32_t *__restrict__ leaves, const SnInfo *__r
             }
             __syncthreads();
         }
-        // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb)
-        const int NQa = (nc + 3) >> 2, Ga = groups_for(NQa);
-        const int NQb = (nb + 3) >> 2, Gb = groups_for(NQb);
-        T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-        for (int k = 0; k < ntot; ++k) {
-            T *buf = (k & 1) ? buf1 : buf0;
-            unsigned &uses = (k & 1) ? uses1 : uses0;
-            wait_chunk(&bars[k & 1], uses & 1u, err);
-            ++uses;
-            int c0, cn, ld;
-            const T *src;
-            pl.chunk(k, c0, cn, src, ld);
-            if (k < pl.nA) {
-                for (int w = tid; w < NQa * Ga; w += kSolveThreads)
-                    chunk_axpy(buf, ld, cn, c0, w % NQa, w / NQa, Ga, fc, ax, ay, az);
-            } else {
-                for (int w = tid; w < NQb * Gb; w += kSolveThreads)
-                    chunk_axpy(buf, ld, cn, c0, w % NQb, w / NQb, Gb, yv, ax, ay, az);
-            }
-            __syncthreads();
-            if (tid == 0 && k + 2 < ntot) issue_chunk(pl, k + 2, buf, &bars[k & 1]);
-            if (k == pl.nA - 1) {
-                reduce_groups<T, false>(NQa, Ga, tid % NQa, tid / NQa, ax, ay, az, red, yv);
-#pragma unroll
-                for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
-            }
-        }
-        if (pl.nB > 0) reduce_groups<T, true>(NQb, Gb, tid % max(NQb, 1), tid / max(NQb, 1), ax, ay, az, red, fb);
-        for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
-        for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
-        __threadfence();
-        __syncthreads();
-        const int p = d.parent;
-        if (p < 0) break;
-        if (tid == 0) {
-            const SnInfo pd = sn[p];
-            const unsigned nch = (unsigned)(pd.child_end - pd.child_begin);
-            const unsigned old = atomicAdd(counters + p, 1u);
-            s_last = ((old + 1u) % nch) == 0u;
-            __threadfence();
-        }
-        __syncthreads();
-        if (!s_last) break;
-        s = p;
     }
+    // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb)
+    const int NQa = (nc + 3) >> 2, Ga = groups_for(NQa);
+    const int NQb = (nb + 3) >> 2, Gb = groups_for(NQb);
+    T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+    for (int k = 0; k < ntot; ++k) {
+        T *buf = (k & 1) ? buf1 : buf0;
+        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        int c0, cn, ld;
+        const T *src;
+        pl.chunk(k, c0, cn, src, ld);
+        if (k < pl.nA) {
+            for (int w = tid; w < NQa * Ga; w += kSolveThreads)
+                chunk_axpy(buf, ld, cn, c0, w % NQa, w / NQa, Ga, fc, ax, ay, az);
+        } else {
+            for (int w = tid; w < NQb * Gb; w += kSolveThreads)
+                chunk_axpy(buf, ld, cn, c0, w % NQb, w / NQb, Gb, yv, ax, ay, az);
+        }
+        __syncthreads();
+        if (tid == 0 && k + 2 < ntot) issue_chunk(pl, k + 2, buf, &bars[k & 1]);
+        if (k == pl.nA - 1) {
+            reduce_groups<T, false>(NQa, Ga, tid % NQa, tid / NQa, ax, ay, az, red, yv);
+#pragma unroll
+            for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+        }
+    }
+    if (pl.nB > 0) reduce_groups<T, true>(NQb, Gb, tid % max(NQb, 1), tid / max(NQb, 1), ax, ay, az, red, fb);
+    for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
+    for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(flags + s, epoch);
 }
 
 // Backward: for supernode s (root first), z = y - L21^T x(struct) and
@@ -1100,12 +1131,11 @@ size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
                       unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st) {
-    (void)ticket;
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
-    k_solve_fwd<T><<<s.nleaves, kSolveThreads, smem, st>>>(lay, s.leaves, s.sn, s.child, s.relind, X, L21, sol, uvec,
-                                                           flags, err);
+    k_solve_fwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.level_sn, s.sn, s.child, s.relind, X, L21, sol,
+                                                     uvec, ticket, flags, err);
 }
 
 template <typename T>

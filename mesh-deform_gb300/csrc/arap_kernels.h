@@ -41,8 +41,6 @@ struct DevSym {
     const int64_t *amap, *dmap;
     const SnInfo *sn;
     const int32_t *rows, *relind, *child, *level_sn;
-    const int32_t *leaves;  // supernodes without children
-    int nleaves;
 };
 
 // cotangent halves per face (computeCotanWeights arap.h:189-222), FP64

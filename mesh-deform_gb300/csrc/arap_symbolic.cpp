@@ -438,8 +438,6 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         for (int s = 0; s < S; ++s) sym.level_sn[fill[sym.sn[s].level]++] = s;
     }
     if (S == 0) sym.level_ptr.assign(1, 0);
-    for (int q = 0; q < S; ++q)
-        if (sym.sn[q].child_begin == sym.sn[q].child_end) sym.leaves.push_back(q);
     // factorisation launch plan
     {
         const int nlev = (int)sym.level_ptr.size() - 1;

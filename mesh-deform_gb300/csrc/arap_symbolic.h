@@ -99,7 +99,6 @@ struct Symbolic {
     std::vector<int32_t> child;       // concatenated children lists
     std::vector<int32_t> level_ptr;   // levels+1
     std::vector<int32_t> level_sn;    // supernodes grouped by level (leaves first)
-    std::vector<int32_t> leaves;      // supernodes without children, ascending
     int max_nrow = 0, max_ncol = 0, max_children = 0, max_ldx = 0, max_ld21 = 0;
     int64_t panel_size = 0, dinv_size = 0, upd_size = 0, uvec_size = 0, x_size = 0, l21_size = 0;
     int64_t l21t_size = 0;
