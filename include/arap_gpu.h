@@ -121,6 +121,19 @@ int arap_wait(arap_ctx *ctx);
    directly. Profiling (arap_set_profiling) always launches directly. */
 int arap_set_graphs(arap_ctx *ctx, int32_t enable);
 
+/* New targets for the SAME constrained vertices (3*n doubles, n = the number
+   of vertices of the last arap_set_constraints, in ascending vertex order).
+   Unlike arap_set_constraints it keeps the rest pose, the cotan weights and
+   the Cholesky factor: the next arap_deform starts from the rest pose with
+   the constrained vertices at the new targets and rotations reset, as a dirty
+   deform of the reference would on an unchanged rest pose, without the
+   factorisation (an extension: the reference always refactors after
+   setConstraint). */
+int arap_set_targets(arap_ctx *ctx, int32_t n, const double *xyz);
+
+/* Device memory held by the context, in bytes. */
+int64_t arap_device_bytes(const arap_ctx *ctx);
+
 /* Marks the context dirty without uploading anything: the next arap_deform
    rebuilds the problem from the rest pose and targets already on the device.
    Used to time a dirty deform with its inputs resident in device memory. */

@@ -72,6 +72,8 @@ SIGNATURES = {
     "arap_deform_async": (C.c_int, [_P, _I32, _dp]),
     "arap_wait": (C.c_int, [_P]),
     "arap_set_graphs": (C.c_int, [_P, _I32]),
+    "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
+    "arap_device_bytes": (C.c_int64, [_P]),
 }
 
 KERNEL_CLASSES = ["weights", "assemble", "factor", "local", "rhs", "residual", "solve_fwd", "solve_bwd", "gather"]
@@ -198,6 +200,13 @@ class ArapContext:
 
     def set_graphs(self, enable: bool) -> None:
         self._check(self.lib.arap_set_graphs(self.h, 1 if enable else 0))
+
+    def set_targets(self, xyz):
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        self._check(self.lib.arap_set_targets(self.h, len(x), _f64(x)))
+
+    def device_bytes(self) -> int:
+        return int(self.lib.arap_device_bytes(self.h))
 
     def invalidate(self):
         self._check(self.lib.arap_invalidate(self.h))

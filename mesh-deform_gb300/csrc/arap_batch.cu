@@ -16,7 +16,6 @@ namespace arapgpu {
 
 namespace {
 
-constexpr int NB = kDiagBlock;
 constexpr int kThreads = 256;
 constexpr int kChunkBytes = 16 * 1024;
 constexpr int kMaxItems = 4;  // (row quad, pose) items per thread

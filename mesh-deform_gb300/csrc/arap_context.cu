@@ -65,6 +65,7 @@ struct arap_ctx {
     int precision = ARAP_PRECISION_FP64;
     int refine = 1;
     bool dirty = true;
+    bool retarget = false;  // same constrained set, new targets: reuse weights and factor
     // symbolic cache (keyed by the constrained-vertex mask)
     bool sym_valid = false;
     Symbolic sym;
@@ -242,9 +243,6 @@ int prepare_symbolic(arap_ctx *ctx) {
     return ARAP_OK;
 }
 
-template <typename T> struct PrecTag;
-template <> struct PrecTag<float> { static constexpr int value = ARAP_PRECISION_MIXED; };
-template <> struct PrecTag<double> { static constexpr int value = ARAP_PRECISION_FP64; };
 
 // Allocates (or keeps) every buffer the setup and the iterations of precision
 // T use. Any reallocation bumps ctx->gen so captured graphs are rebuilt.
@@ -331,6 +329,26 @@ int setup_enqueue(arap_ctx *ctx) {
             ctx->launches += 1;
         }
     }
+    CK(cudaGetLastError());
+    return ARAP_OK;
+}
+
+// Enqueues a re-pose of the set-up problem (arap_set_targets): positions back
+// to the rest pose with the constrained vertices at their new targets,
+// rotations reset, bFixed recomputed; weights and factor stay.
+template <typename T>
+int retarget_enqueue(arap_ctx *ctx) {
+    const DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    Vec4<T> *p_t = sizeof(T) == 4 ? ctx->p32.as<Vec4<T>>() : ctx->p64.as<Vec4<T>>();
+    Vec4<T> *pc_t = sizeof(T) == 4 ? ctx->pc32.as<Vec4<T>>() : ctx->pc64.as<Vec4<T>>();
+    {
+        Prof pr(ctx, ARAP_K_ASSEMBLE);
+        launch_setup_vertices<T>(d, ctx->rest.as<double>(), ctx->targets.as<double>(), ctx->p64.as<Vec4<double>>(),
+                                 ctx->pc64.as<Vec4<double>>(), p_t, pc_t, ctx->R.as<Vec4<T>>(), st);
+        launch_bfixed(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->bfixed.as<Vec4<double>>(), st);
+    }
+    ctx->launches += 2;
     CK(cudaGetLastError());
     return ARAP_OK;
 }
@@ -788,6 +806,26 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
     return ARAP_OK;
 }
 
+int arap_set_targets(arap_ctx *ctx, int32_t n, const double *xyz) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (n != (int32_t)ctx->cidx.size() || (n > 0 && !xyz))
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "arap_set_targets needs one target per constrained vertex");
+    std::memcpy(ctx->ctgt.data(), xyz, sizeof(double) * 3 * (size_t)n);
+    CK(cudaSetDevice(ctx->device));
+    if (n > 0)
+        CK(cudaMemcpyAsync(ctx->targets.p, ctx->ctgt.data(), ctx->ctgt.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (!ctx->dirty) ctx->retarget = true;
+    return ARAP_OK;
+}
+
+int64_t arap_device_bytes(const arap_ctx *ctx);
+
 int arap_invalidate(arap_ctx *ctx) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
     ctx->dirty = true;
@@ -841,6 +879,12 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         ctx->state_prec = fp64 ? ARAP_PRECISION_FP64 : ARAP_PRECISION_MIXED;
         ctx->have_rotations = true;
         ctx->dirty = false;
+        ctx->retarget = false;
+    } else if (ctx->retarget) {
+        const int rc = ctx->state_prec == ARAP_PRECISION_FP64 ? retarget_enqueue<double>(ctx)
+                                                               : retarget_enqueue<float>(ctx);
+        if (rc != ARAP_OK) return rc;
+        ctx->retarget = false;
     }
     CK(cudaEventRecord(ctx->ev1, st));
     if (iterations > 0) {
@@ -1034,6 +1078,22 @@ int arap_get_launch_count(arap_ctx *ctx, int64_t *launches) {
     if (check_ctx(ctx) || !launches) return ARAP_ERR_INVALID_ARGUMENT;
     *launches = ctx->launches;
     return ARAP_OK;
+}
+
+int64_t arap_device_bytes(const arap_ctx *ctx) {
+    if (!ctx) return 0;
+    const DevBuf *bufs[] = {&ctx->faces, &ctx->ent_ptr, &ctx->ent_fc, &ctx->hc, &ctx->w_orig, &ctx->rest,
+                            &ctx->targets, &ctx->out, &ctx->drow, &ctx->dcol, &ctx->dent, &ctx->oldidx,
+                            &ctx->amap, &ctx->dmap, &ctx->sn, &ctx->rows, &ctx->relind, &ctx->child,
+                            &ctx->level_sn, &ctx->fitems, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64,
+                            &ctx->p32, &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
+                            &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->L21T,
+                            &ctx->redge, &ctx->errw, &ctx->ticket, &ctx->flags, &ctx->btargets, &ctx->bpc64,
+                            &ctx->bpc32, &ctx->bR, &ctx->bbfixed, &ctx->bb, &ctx->bsol, &ctx->buvec, &ctx->bout,
+                            &ctx->bticket, &ctx->bflags};
+    int64_t total = 0;
+    for (const DevBuf *b : bufs) total += (int64_t)b->cap;
+    return total;
 }
 
 int arap_get_stream(arap_ctx *ctx, void **stream) {

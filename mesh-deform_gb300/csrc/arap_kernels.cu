@@ -173,6 +173,25 @@ __global__ void k_assemble(int m, const int32_t *__restrict__ drow, const int32_
     bfixed[k] = {bx, by, bz, 0.0};
 }
 
+// bFixed alone (arap.h:325-327), for a re-pose that keeps the factor
+__global__ void k_bfixed(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
+                         const double *__restrict__ w64, const Vec4<double> *__restrict__ pc64,
+                         Vec4<double> *__restrict__ bfixed) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    double bx = 0.0, by = 0.0, bz = 0.0;
+    for (int e = drow[k]; e < drow[k + 1]; ++e) {
+        const int l = dcol[e];
+        if (l < m) continue;
+        const double w = w64[e];
+        const Vec4<double> c = pc64[l];
+        bx = __dadd_rn(bx, __dmul_rn(w, c.x));
+        by = __dadd_rn(by, __dmul_rn(w, c.y));
+        bz = __dadd_rn(bz, __dmul_rn(w, c.z));
+    }
+    bfixed[k] = {bx, by, bz, 0.0};
+}
+
 // Rest edge vectors p_k - p_l per adjacency entry, differenced in FP64 and
 // stored in FP32: exact to FP32 rounding of the (short) edge itself, where
 // differencing FP32 positions would lose the digits the positions' magnitude
@@ -1067,6 +1086,12 @@ void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc6
     if (s.m == 0) return;
     k_assemble<TF><<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, s.amap, s.dmap, pc64, Lval,
                                                          diag64, bfixed);
+}
+
+void launch_bfixed(const DevSym &s, const double *w64, const Vec4<double> *pc64, Vec4<double> *bfixed,
+                   cudaStream_t st) {
+    if (s.m == 0) return;
+    k_bfixed<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, pc64, bfixed);
 }
 
 void launch_rest_edges(const DevSym &s, const Vec4<double> *p64, Vec4<float> *redge, cudaStream_t st) {

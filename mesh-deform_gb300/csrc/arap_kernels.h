@@ -61,6 +61,9 @@ void launch_setup_vertices(const DevSym &s, const double *rest_xyz, const double
 template <typename TF>
 void launch_assemble(const DevSym &s, const double *w64, const Vec4<double> *pc64, TF *Lval, double *diag64,
                      Vec4<double> *bfixed, cudaStream_t st);
+// bFixed alone for a re-pose with the same constrained set
+void launch_bfixed(const DevSym &s, const double *w64, const Vec4<double> *pc64, Vec4<double> *bfixed,
+                   cudaStream_t st);
 // FP32 rest edge vectors per adjacency entry, differenced in FP64
 void launch_rest_edges(const DevSym &s, const Vec4<double> *p64, Vec4<float> *redge, cudaStream_t st);
 // mixed form: FP32 covariance from FP32 rest edges and FP64-differenced current edges

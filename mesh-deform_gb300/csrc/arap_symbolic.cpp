@@ -38,36 +38,50 @@ bool build_topology(int V, int F, const int32_t *faces, Topology &topo, std::str
     }
     // Directed contributions in the order computeCotanWeights pushes them
     // (arap.h:225-232): per face e0,e1,e2 as (min,max), then as (max,min).
-    struct Contrib { int32_t r, c, fc; };
-    std::vector<Contrib> t;
-    t.reserve((size_t)6 * F);
+    // A counting sort by row, then a stable insertion sort by column inside
+    // each row (a handful of entries), orders them as a stable sort by
+    // (row, column) would.
+    struct Contrib { int32_t c, fc; };
+    std::vector<int32_t> rstart((size_t)V + 1, 0);
+    for (int64_t i = 0; i < (int64_t)3 * F; ++i) rstart[faces[i] + 1] += 2;
+    for (int v = 0; v < V; ++v) rstart[v + 1] += rstart[v];
+    std::vector<int32_t> fillp(rstart.begin(), rstart.end() - 1);
+    std::vector<Contrib> t((size_t)6 * F);
     for (int f = 0; f < F; ++f) {
         const int32_t v[3] = {faces[3 * f], faces[3 * f + 1], faces[3 * f + 2]};
         int32_t a[3], b[3];
         for (int k = 0; k < 3; ++k) {
-            int32_t x = v[k], y = v[(k + 1) % 3];
-            a[k] = std::min(x, y);
-            b[k] = std::max(x, y);
+            a[k] = std::min(v[k], v[(k + 1) % 3]);
+            b[k] = std::max(v[k], v[(k + 1) % 3]);
         }
-        for (int k = 0; k < 3; ++k) t.push_back({a[k], b[k], 3 * f + k});
-        for (int k = 0; k < 3; ++k) t.push_back({b[k], a[k], 3 * f + k});
+        for (int k = 0; k < 3; ++k) t[fillp[a[k]]++] = {b[k], 3 * f + k};
+        for (int k = 0; k < 3; ++k) t[fillp[b[k]]++] = {a[k], 3 * f + k};
     }
-    std::stable_sort(t.begin(), t.end(), [](const Contrib &x, const Contrib &y) {
-        return x.r != y.r ? x.r < y.r : x.c < y.c;
-    });
+    for (int v = 0; v < V; ++v)
+        for (int32_t i = rstart[v] + 1; i < rstart[v + 1]; ++i) {
+            const Contrib x = t[i];
+            int32_t j = i - 1;
+            while (j >= rstart[v] && t[j].c > x.c) { t[j + 1] = t[j]; --j; }
+            t[j + 1] = x;
+        }
     topo.rowptr.assign((size_t)V + 1, 0);
     topo.ent_ptr.clear();
+    topo.ent_ptr.reserve((size_t)3 * F + 1);
     topo.ent_ptr.push_back(0);
-    for (size_t i = 0; i < t.size();) {
-        size_t j = i;
-        while (j < t.size() && t[j].r == t[i].r && t[j].c == t[i].c) {
-            topo.ent_fc.push_back(t[j].fc);
-            ++j;
+    topo.ent_fc.reserve((size_t)6 * F);
+    topo.col.reserve((size_t)3 * F);
+    for (int v = 0; v < V; ++v) {
+        for (int32_t i = rstart[v]; i < rstart[v + 1];) {
+            int32_t j = i;
+            while (j < rstart[v + 1] && t[j].c == t[i].c) {
+                topo.ent_fc.push_back(t[j].fc);
+                ++j;
+            }
+            topo.col.push_back(t[i].c);
+            topo.rowptr[v + 1]++;
+            topo.ent_ptr.push_back((int32_t)topo.ent_fc.size());
+            i = j;
         }
-        topo.col.push_back(t[i].c);
-        topo.rowptr[t[i].r + 1]++;
-        topo.ent_ptr.push_back((int32_t)topo.ent_fc.size());
-        i = j;
     }
     for (int v = 0; v < V; ++v) topo.rowptr[v + 1] += topo.rowptr[v];
     return true;
@@ -81,7 +95,10 @@ namespace {
 struct NestedDissection {
     const int32_t *rowptr, *col;
     int n;
-    std::vector<int32_t> inset, seen, lev, queue;
+    // two BFS buffers (queue + level per vertex): a trial BFS from a new root
+    // fills the spare one, which becomes current when the trial is kept
+    std::vector<int32_t> inset, seen, lev_buf[2], queue_buf[2];
+    int cur = 0;
     int32_t stamp = 0;
     std::vector<int32_t> *perm, *block_ptr;
 
@@ -90,9 +107,10 @@ struct NestedDissection {
         block_ptr->push_back((int32_t)perm->size());
     }
 
-    // BFS inside the stamped set; neighbours visited in CSR order. Returns the
-    // number of levels, level offsets into queue in levptr.
-    int bfs(int32_t setstamp, int32_t root, std::vector<int32_t> &levptr) {
+    // BFS inside the stamped set into buffer `buf`; neighbours visited in CSR
+    // order. Returns the number of levels, level offsets into the queue in levptr.
+    int bfs(int32_t setstamp, int32_t root, std::vector<int32_t> &levptr, int buf) {
+        int32_t *queue = queue_buf[buf].data(), *lev = lev_buf[buf].data();
         const int32_t bs = ++stamp;
         int head = 0, tail = 0;
         queue[tail++] = root;
@@ -115,29 +133,41 @@ struct NestedDissection {
         return (int)levptr.size() - 1;
     }
 
+    // S arrives in any order; only the blocks emitted are sorted, and the
+    // smallest vertex of S is the first BFS root, so the result is that of
+    // recursing on sorted sets.
     void recurse(std::vector<int32_t> S) {
         const int ns = (int)S.size();
-        if (ns <= kNdLeaf) { emit(S); return; }
+        if (ns <= kNdLeaf) {
+            std::sort(S.begin(), S.end());
+            emit(S);
+            return;
+        }
         const int32_t setstamp = ++stamp;
-        for (int32_t v : S) inset[v] = setstamp;
+        int32_t smin = S[0];
+        for (int32_t v : S) {
+            inset[v] = setstamp;
+            smin = std::min(smin, v);
+        }
         std::vector<int32_t> levptr;
-        int h = bfs(setstamp, S[0], levptr);
+        int h = bfs(setstamp, smin, levptr, cur);
         if (levptr[h] < ns) {
             // several components, each in order of its smallest vertex
+            std::sort(S.begin(), S.end());
             for (int32_t v : S) {
                 if (inset[v] != setstamp) continue;
-                const int hl = bfs(setstamp, v, levptr);
-                std::vector<int32_t> comp(queue.begin(), queue.begin() + levptr[hl]);
+                const int hl = bfs(setstamp, v, levptr, cur);
+                std::vector<int32_t> comp(queue_buf[cur].begin(), queue_buf[cur].begin() + levptr[hl]);
                 const int32_t cs = ++stamp;
                 for (int32_t u : comp) inset[u] = cs;
-                std::sort(comp.begin(), comp.end());
                 recurse(std::move(comp));
             }
             return;
         }
         // pseudo-peripheral vertex
-        int32_t root = S[0];
+        std::vector<int32_t> lp2;
         for (int it = 0; it < kNdPseudoPeripheralRounds; ++it) {
+            const int32_t *queue = queue_buf[cur].data();
             int32_t best = -1, bestdeg = 0;
             for (int q = levptr[h - 1]; q < levptr[h]; ++q) {
                 const int32_t v = queue[q];
@@ -145,13 +175,16 @@ struct NestedDissection {
                 for (int32_t e = rowptr[v]; e < rowptr[v + 1]; ++e) deg += (inset[col[e]] == setstamp);
                 if (best < 0 || deg < bestdeg || (deg == bestdeg && v < best)) { best = v; bestdeg = deg; }
             }
-            std::vector<int32_t> lp2;
-            const int h2 = bfs(setstamp, best, lp2);
-            if (h2 > h) { root = best; h = h2; levptr = lp2; }
+            const int h2 = bfs(setstamp, best, lp2, cur ^ 1);
+            if (h2 > h) { h = h2; levptr.swap(lp2); cur ^= 1; }
             else break;
         }
-        h = bfs(setstamp, root, levptr);
-        if (h < 3) { emit(S); return; }
+        const int32_t *queue = queue_buf[cur].data(), *lev = lev_buf[cur].data();
+        if (h < 3) {
+            std::sort(S.begin(), S.end());
+            emit(S);
+            return;
+        }
         int bestk = -1;
         int64_t bsz = 0, bdiff = 0;
         for (int k = 1; k <= h - 2; ++k) {
@@ -168,7 +201,7 @@ struct NestedDissection {
         }
         const int k = bestk;
         std::vector<int32_t> A, B, Sep;
-        A.assign(queue.begin(), queue.begin() + levptr[k]);
+        A.assign(queue, queue + levptr[k]);
         for (int q = levptr[k]; q < levptr[k + 1]; ++q) {
             const int32_t v = queue[q];
             bool touches = false;
@@ -178,9 +211,7 @@ struct NestedDissection {
             }
             (touches ? Sep : A).push_back(v);
         }
-        B.assign(queue.begin() + levptr[k + 1], queue.begin() + levptr[h]);
-        std::sort(A.begin(), A.end());
-        std::sort(B.begin(), B.end());
+        B.assign(queue + levptr[k + 1], queue + levptr[h]);
         std::sort(Sep.begin(), Sep.end());
         recurse(std::move(A));
         recurse(std::move(B));
@@ -201,8 +232,10 @@ void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int3
     nd.n = n;
     nd.inset.assign(n, 0);
     nd.seen.assign(n, 0);
-    nd.lev.assign(n, 0);
-    nd.queue.assign(n, 0);
+    for (int b = 0; b < 2; ++b) {
+        nd.lev_buf[b].assign(n, 0);
+        nd.queue_buf[b].assign(n, 0);
+    }
     nd.perm = &perm;
     nd.block_ptr = &block_ptr;
     std::vector<int32_t> S(n);
