@@ -331,6 +331,155 @@ def run_batch(args):
         dist.destroy_process_group()
     return 0
 
+def _pct(xs, q):
+    return float(np.percentile(xs, q)) if xs else None
+
+
+def _serve_stream(G, W, pool, reqs, args, local, clocks=None):
+    """Submits reqs at their arrival times to a fresh server, collects every
+    result; returns per-request (latency_ms, queue_ms, reused, batch, mesh V,
+    iterations) and the stream's wall time and server stats."""
+    srv = G.ArapServer(device=local, precision="mixed", refine_steps=args.refine,
+                       max_in_flight=args.serve_in_flight, prep_threads=args.serve_prep_threads,
+                       max_batch=args.serve_max_batch)
+    ids = [srv.add_mesh(m.positions, m.faces) for m in pool]
+    tickets = [None] * len(reqs)
+    t0 = time.perf_counter()
+
+    def submitter():
+        for k, r in enumerate(reqs):
+            dt = r.arrival - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets[k] = srv.submit(ids[r.mesh], r.cidx, r.ctargets, r.iterations)
+
+    th = threading.Thread(target=submitter)
+    if clocks:
+        clocks.start()
+    th.start()
+    rows, outs = [], {}
+    for k, r in enumerate(reqs):
+        while tickets[k] is None:
+            time.sleep(50e-6)
+        out, info = srv.wait(tickets[k])
+        rows.append((info["latency_ms"], info["queue_ms"], info["factor_reused"], info["batch_size"],
+                     pool[r.mesh].V, r.iterations))
+        if k < args.serve_check:
+            outs[k] = out
+    wall = time.perf_counter() - t0
+    th.join()
+    clk = clocks.stop() if clocks else None
+    st = srv.stats()
+    srv.close()
+    return rows, wall, st, outs, clk
+
+
+def run_serving(args):
+    """Serving stream: Poisson arrivals of deform requests over a pool of 64
+    meshes (noisy icospheres L3-L6, bars of 1k-200k vertices), each with 1-8
+    handle caps plus an anchor cap, half reusing a constraint set seen before,
+    5-50 iterations; through arap_srv_* (resident factors keyed by mesh and
+    constraint set, admission by device footprint, multi-pose batching,
+    concurrent launches). Reported per arrival rate: iterations/s and p50/p99
+    latency (submit -> result in host memory), beside the plain per-request
+    FP64 GPU form (a dirty arap_deform per request, one at a time)."""
+    import torch
+    import arap_gpu as G
+    import arap_workloads as W
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    pool = W.serving_pool(n_meshes=64, seed=20261203)
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    runs = []
+    peak_clk = None
+    # warm-up: a short stream (graph capture, kernel attribute set-up, pool memory)
+    warm = W.serving_requests(pool, max(8, args.warmup * 4), seed=1, rate_hz=None)
+    _serve_stream(G, W, pool, warm, args, local)
+    for i, rate in enumerate(rates):
+        reqs = W.serving_requests(pool, args.serve_requests, seed=20261204 + i, rate_hz=None if rate <= 0 else rate)
+        clocks = ClockSampler(local)
+        rows, wall, st, outs, clk = _serve_stream(G, W, pool, reqs, args, local, clocks)
+        lat = [r[0] for r in rows]
+        hit = [r[0] for r in rows if r[2]]
+        miss = [r[0] for r in rows if not r[2]]
+        its = sum(r[5] for r in rows)
+        small = [r[0] for r in rows if 8000 <= r[4] <= 12000]
+        run = {"rate_hz": rate if rate > 0 else "all at t=0", "requests": len(rows), "wall_s": wall,
+               "iterations_per_s": its / wall, "requests_per_s": len(rows) / wall,
+               "latency_ms": {"p50": _pct(lat, 50), "p99": _pct(lat, 99)},
+               "latency_ms_factor_reused": {"n": len(hit), "p50": _pct(hit, 50), "p99": _pct(hit, 99)},
+               "latency_ms_new_factor": {"n": len(miss), "p50": _pct(miss, 50), "p99": _pct(miss, 99)},
+               "latency_ms_10k_meshes": {"n": len(small), "p50": _pct(small, 50), "p99": _pct(small, 99)},
+               "queue_ms": {"p50": _pct([r[1] for r in rows], 50), "p99": _pct([r[1] for r in rows], 99)},
+               "stats": {k: st[k] for k in ("factor_hits", "factor_misses", "evictions", "launches",
+                                             "batched_launches", "batched_requests", "peak_resident_bytes",
+                                             "budget_bytes")},
+               "clocks": clk}
+        # error against the FP64 oracle on a sample of small requests
+        if rank == 0 and not args.no_cpu_baseline:
+            from oracle import oracle as O
+
+            O.build()
+            errs = []
+            for k, out in outs.items():
+                r = reqs[k]
+                m = pool[r.mesh]
+                if m.V > 20000:
+                    continue
+                ok, ref = O.run_deform(m.positions, m.faces, r.cidx, r.ctargets, r.iterations)
+                errs.append(W.bbox_rel_error(out, ref, m.positions))
+            run["error_vs_fp64_oracle"] = {"max": max(errs) if errs else None, "checked": len(errs)}
+        runs.append(run)
+        log(json.dumps(run))
+        if clk:
+            peak_clk = clk
+    # the plain per-request FP64 GPU form on the first requests of the same stream
+    reqs = W.serving_requests(pool, args.serve_fp64_requests, seed=20261204)
+    ctxs = {}
+    lat64 = []
+    its64 = 0
+    t0 = time.perf_counter()
+    for r in reqs:
+        m = pool[r.mesh]
+        if r.mesh not in ctxs:
+            c = G.ArapContext(m.V, m.faces, device=local)
+            c.set_precision("fp64", 0)
+            c.set_rest_positions(m.positions)
+            ctxs[r.mesh] = c
+        c = ctxs[r.mesh]
+        a = time.perf_counter()
+        c.set_constraints(r.cidx, r.ctargets)
+        c.deform(r.iterations)
+        lat64.append(1e3 * (time.perf_counter() - a))
+        its64 += r.iterations
+    wall64 = time.perf_counter() - t0
+    for c in ctxs.values():
+        c.close()
+    fp64 = {"requests": len(reqs), "iterations_per_s": its64 / wall64,
+            "latency_ms": {"p50": _pct(lat64, 50), "p99": _pct(lat64, 99)},
+            "form": "one dirty arap_deform per request, FP64, one request at a time"}
+    best = max(runs, key=lambda x: x["iterations_per_s"])
+    line = {
+        "metric": METRIC, "value": best["iterations_per_s"], "unit": UNIT, "n_gpus": 1,
+        "steps": len(runs), "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "serving_stream", "meshes": len(pool),
+                   "pool_vertices": int(sum(m.V for m in pool)),
+                   "requests_per_rate": args.serve_requests, "rates_hz": rates,
+                   "max_in_flight": args.serve_in_flight, "prep_threads": args.serve_prep_threads,
+                   "max_batch": args.serve_max_batch, "precision": "mixed", "refine_steps": args.refine},
+        "latency_ms": best["latency_ms"],
+        "runs": runs,
+        "fp64_per_request": fp64,
+        "served_vs_fp64_iterations_ratio": best["iterations_per_s"] / fp64["iterations_per_s"],
+        "clocks": peak_clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
 
 def main():
     ap = argparse.ArgumentParser()
@@ -349,6 +498,14 @@ def main():
     ap.add_argument("--poses", type=int, default=256, help="pose_batch: handle poses per step")
     ap.add_argument("--concurrent", type=int, default=os.cpu_count() or 1,
                     help="independent requests in flight per step (default: host threads, as the reference arm)")
+    ap.add_argument("--serve-rates", default="50,100,200,0",
+                    help="serving: Poisson arrival rates in requests/s (0: all requests at once)")
+    ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--serve-in-flight", type=int, default=16)
+    ap.add_argument("--serve-prep-threads", type=int, default=min(12, os.cpu_count() or 4))
+    ap.add_argument("--serve-max-batch", type=int, default=64)
+    ap.add_argument("--serve-check", type=int, default=40, help="serving: results checked against the oracle")
+    ap.add_argument("--serve-fp64-requests", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -356,6 +513,8 @@ def main():
         return run_reference(args)
     if args.workload == "pose_batch":
         return run_batch(args)
+    if args.workload == "serving":
+        return run_serving(args)
 
     import torch
 

@@ -32,7 +32,8 @@ typedef enum arap_status {
     ARAP_ERR_TIMEOUT = 6,          /* a bounded in-kernel wait expired */
     ARAP_ERR_ADMISSION_REFUSED = 7,/* request does not fit the device memory budget */
     ARAP_ERR_NO_DEVICE = 8,        /* no CUDA device visible */
-    ARAP_ERR_UNSUPPORTED = 9       /* input outside the implemented limits */
+    ARAP_ERR_UNSUPPORTED = 9,      /* input outside the implemented limits */
+    ARAP_PENDING = 10              /* (arap_srv_poll / arap_srv_wait) not finished yet */
 } arap_status;
 
 typedef enum arap_precision {
@@ -61,6 +62,10 @@ const char *arap_last_error(const arap_ctx *ctx);
 int arap_create(int32_t n_vertices, int32_t n_faces, const int32_t *faces, int32_t device,
                 arap_ctx **out);
 void arap_destroy(arap_ctx *ctx);
+/* A new context for the same mesh as src (same device, topology, precision
+   and rest positions, copied on the device; no constraints): skips the
+   adjacency build of arap_create. src is only read. */
+int arap_create_like(const arap_ctx *src, arap_ctx **out);
 
 /* Precision form and number of FP64-residual refinement solves per iteration
    (MIXED only; 0..8). The default is ARAP_PRECISION_FP64. Marks the context
@@ -114,6 +119,14 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
    keep several requests in flight. */
 int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz);
 int arap_wait(arap_ctx *ctx);
+/* arap_deform_poses split the same way (completed by arap_wait or
+   arap_query). */
+int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
+                            double *out_xyz);
+/* Non-blocking completion check of a pending asynchronous deform: *done = 0
+   while it runs (returns ARAP_OK); otherwise *done = 1 and the return value
+   is what arap_wait returns. */
+int arap_query(arap_ctx *ctx, int32_t *done);
 
 /* enable != 0 (the default) runs the setup and the iteration sequence as CUDA
    graphs captured on first use and replayed while the problem's size,
@@ -133,6 +146,12 @@ int arap_set_targets(arap_ctx *ctx, int32_t n, const double *xyz);
 
 /* Device memory held by the context, in bytes. */
 int64_t arap_device_bytes(const arap_ctx *ctx);
+/* Device memory the context will hold after its next arap_deform
+   (n_poses = 0) or arap_deform_poses with n_poses poses, in bytes. Runs the
+   host-side symbolic analysis of the current constraint set if it has not
+   run yet (kept for the deform); launches nothing and allocates nothing on
+   the device. */
+int arap_plan_bytes(arap_ctx *ctx, int32_t n_poses, int64_t *bytes);
 
 /* Marks the context dirty without uploading anything: the next arap_deform
    rebuilds the problem from the rest pose and targets already on the device.
@@ -228,6 +247,82 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
    every edge lies on at most two faces. */
 int arap_cotan_weights_static(int32_t n_vertices, int32_t n_faces, const int32_t *faces, const double *xyz,
                               const int32_t *rowptr, const int32_t *col, int32_t nnz, double *val, void *stream);
+
+/* ------------------------------------------------------------------------
+   Deform server: a request loop over resident contexts (no counterpart in the
+   reference, whose deform() is a synchronous call on one object).
+
+   Requests (mesh, constraint set with targets, iteration count) are queued as
+   they arrive. One context per (mesh, constraint set) stays resident on the
+   device with its cotan weights and Cholesky factor; a request whose
+   constraint set is resident re-poses it (arap_set_targets) instead of
+   refactoring. New constraint sets are analysed on host worker threads and
+   admitted when their planned device footprint fits the budget, evicting
+   the least recently used idle contexts. Requests of one resident constraint
+   set with the same iteration count that wait together run as one
+   multi-pose launch (arap_deform_poses, MIXED precision). Up to
+   max_in_flight launches run concurrently on their own streams. Each result
+   equals that of a lone arap_deform of the same request on a fresh context,
+   within the precision form's tolerance. Thread-safe. */
+typedef struct arap_server arap_server;
+
+typedef struct arap_server_config {
+    int32_t device;
+    int32_t precision;           /* arap_precision of every request (ARAP_PRECISION_MIXED) */
+    int32_t refine_steps;        /* MIXED refinement solves per iteration (1) */
+    int32_t max_in_flight;       /* launches on the device at once (0: 16) */
+    int64_t device_budget_bytes; /* resident device memory limit (0: 80% of the free memory) */
+    int32_t prep_threads;        /* host threads for analysis and first launches (0: 4) */
+    int32_t max_batch;           /* most requests per multi-pose launch (0: 64; 1: no batching) */
+    int32_t max_queue;           /* waiting requests before submit refuses (0: 65536) */
+    int32_t poll_us;             /* completion polling interval of the scheduler (0: 20) */
+} arap_server_config;
+
+typedef struct arap_request {
+    int32_t mesh;             /* id from arap_srv_add_mesh */
+    int32_t n_constraints;
+    const int32_t *indices;   /* copied by submit; a vertex listed twice keeps its last target */
+    const double *targets;    /* 3 per constraint, copied by submit */
+    int32_t iterations;
+    int32_t pad;
+    double *out_xyz;          /* V x 3, written before the request completes; must stay valid until then */
+} arap_request;
+
+typedef struct arap_request_info {
+    int32_t status;           /* ARAP_OK or the error of this request */
+    int32_t factor_reused;    /* 1: served by a resident factor of the same constraint set */
+    int32_t batch_size;       /* requests in the launch that served it */
+    int32_t pad;
+    double queue_ms;          /* submit -> launch */
+    double latency_ms;        /* submit -> result in out_xyz */
+} arap_request_info;
+
+typedef struct arap_server_stats {
+    int64_t submitted, completed, failed, refused;
+    int64_t factor_hits, factor_misses, evictions, launches, batched_launches, batched_requests;
+    int64_t iterations_done;  /* iterations of completed requests */
+    int64_t resident_bytes, peak_resident_bytes, budget_bytes;
+    int32_t resident_factors, queue_depth, in_flight, pad;
+} arap_server_stats;
+
+int arap_srv_create(const arap_server_config *cfg, arap_server **out);
+/* Finishes every submitted request, then frees everything. */
+void arap_srv_destroy(arap_server *srv);
+/* Registers a mesh (faces and rest positions are copied; one context holds
+   its topology on the device). */
+int arap_srv_add_mesh(arap_server *srv, int32_t n_vertices, int32_t n_faces, const int32_t *faces,
+                      const double *rest_xyz, int32_t *mesh_id);
+/* Queues a request; ARAP_ERR_BAD_INDEX / INVALID_ARGUMENT for malformed ones,
+   ARAP_ERR_ADMISSION_REFUSED when max_queue requests already wait. */
+int arap_srv_submit(arap_server *srv, const arap_request *req, int64_t *ticket);
+/* ARAP_PENDING while the request runs; otherwise its final status, with info
+   filled in (when non-NULL) and the ticket released. */
+int arap_srv_poll(arap_server *srv, int64_t ticket, arap_request_info *info);
+/* As arap_srv_poll, waiting up to timeout_ms (negative: no limit). */
+int arap_srv_wait(arap_server *srv, int64_t ticket, int32_t timeout_ms, arap_request_info *info);
+int arap_srv_stats(arap_server *srv, arap_server_stats *stats);
+/* Message of the last failed arap_srv_* call on this server. */
+const char *arap_srv_last_error(const arap_server *srv);
 
 #ifdef __cplusplus
 }

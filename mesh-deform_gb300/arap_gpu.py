@@ -33,6 +33,7 @@ ARAP_ERR_TIMEOUT = 6
 ARAP_ERR_ADMISSION_REFUSED = 7
 ARAP_ERR_NO_DEVICE = 8
 ARAP_ERR_UNSUPPORTED = 9
+ARAP_PENDING = 10
 
 PRECISION = {"fp64": 0, "mixed": 1}
 
@@ -43,6 +44,32 @@ _I64 = C.c_int64
 _ip = C.POINTER(C.c_int32)
 _lp = C.POINTER(C.c_int64)
 _dp = C.POINTER(C.c_double)
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("refine_steps", C.c_int32),
+                ("max_in_flight", C.c_int32), ("device_budget_bytes", C.c_int64), ("prep_threads", C.c_int32),
+                ("max_batch", C.c_int32), ("max_queue", C.c_int32), ("poll_us", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("mesh", C.c_int32), ("n_constraints", C.c_int32), ("indices", _ip), ("targets", _dp),
+                ("iterations", C.c_int32), ("pad", C.c_int32), ("out_xyz", _dp)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("factor_reused", C.c_int32), ("batch_size", C.c_int32),
+                ("pad", C.c_int32), ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "refused", "factor_hits",
+                                         "factor_misses", "evictions", "launches", "batched_launches",
+                                         "batched_requests", "iterations_done", "resident_bytes",
+                                         "peak_resident_bytes", "budget_bytes")] + \
+        [(n, C.c_int32) for n in ("resident_factors", "queue_depth", "in_flight", "pad")]
+
+
 SIGNATURES = {
     "arap_status_string": (C.c_char_p, [C.c_int]),
     "arap_last_error": (C.c_char_p, [_P]),
@@ -73,7 +100,19 @@ SIGNATURES = {
     "arap_wait": (C.c_int, [_P]),
     "arap_set_graphs": (C.c_int, [_P, _I32]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
+    "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
+    "arap_query": (C.c_int, [_P, C.POINTER(C.c_int32)]),
+    "arap_create_like": (C.c_int, [_P, C.POINTER(_P)]),
+    "arap_plan_bytes": (C.c_int, [_P, _I32, C.POINTER(C.c_int64)]),
     "arap_device_bytes": (C.c_int64, [_P]),
+    "arap_srv_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "arap_srv_destroy": (None, [_P]),
+    "arap_srv_add_mesh": (C.c_int, [_P, _I32, _I32, _ip, _dp, _ip]),
+    "arap_srv_submit": (C.c_int, [_P, C.POINTER(Request), _lp]),
+    "arap_srv_poll": (C.c_int, [_P, _I64, C.POINTER(RequestInfo)]),
+    "arap_srv_wait": (C.c_int, [_P, _I64, _I32, C.POINTER(RequestInfo)]),
+    "arap_srv_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "arap_srv_last_error": (C.c_char_p, [_P]),
 }
 
 KERNEL_CLASSES = ["weights", "assemble", "factor", "local", "rhs", "residual", "solve_fwd", "solve_bwd", "gather"]
@@ -294,6 +333,85 @@ def analyze_pattern(n_vertices: int, faces: np.ndarray, constrained) -> dict:
         raise ArapError(rc, lib.arap_last_error(None).decode())
     return {"m": m.value, "perm": perm[: m.value], "etree": et[: m.value], "block_ptr": bp[: s.value + 1],
             "factor_nnz": nz.value}
+
+
+class ArapServer:
+    """The request loop of ``arap_srv_*``: submit deform requests (mesh,
+    constraint set, targets, iterations) from any thread; results arrive in
+    per-request numpy arrays kept alive here until the ticket is collected."""
+
+    def __init__(self, device: int = 0, precision: str = "mixed", refine_steps: int = 1, max_in_flight: int = 0,
+                 budget_bytes: int = 0, prep_threads: int = 0, max_batch: int = 0, max_queue: int = 0,
+                 poll_us: int = 0):
+        self.lib = load()
+        cfg = ServerConfig(int(device), PRECISION[precision], int(refine_steps), int(max_in_flight),
+                           int(budget_bytes), int(prep_threads), int(max_batch), int(max_queue), int(poll_us))
+        h = _P()
+        rc = self.lib.arap_srv_create(C.byref(cfg), C.byref(h))
+        if rc != ARAP_OK:
+            raise ArapError(rc, self.lib.arap_srv_last_error(None).decode())
+        self.h = h
+        self.V = {}
+        self._live = {}
+
+    def _check(self, rc: int):
+        if rc != ARAP_OK:
+            raise ArapError(rc, self.lib.arap_srv_last_error(self.h).decode())
+
+    def add_mesh(self, positions, faces) -> int:
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+        mid = C.c_int32()
+        self._check(self.lib.arap_srv_add_mesh(self.h, len(pos), len(f), _i32(f), _f64(pos), C.byref(mid)))
+        self.V[mid.value] = len(pos)
+        return mid.value
+
+    def submit(self, mesh: int, cidx, ctargets, iterations: int) -> int:
+        idx = np.ascontiguousarray(cidx, dtype=np.int32).reshape(-1)
+        tgt = np.ascontiguousarray(ctargets, dtype=np.float64).reshape(-1, 3)
+        out = np.empty((self.V[mesh], 3), np.float64)
+        req = Request(int(mesh), len(idx), _i32(idx), _f64(tgt), int(iterations), 0, _f64(out))
+        t = C.c_int64()
+        self._check(self.lib.arap_srv_submit(self.h, C.byref(req), C.byref(t)))
+        self._live[t.value] = out
+        return t.value
+
+    @staticmethod
+    def _info(i: RequestInfo) -> dict:
+        return {"status": i.status, "factor_reused": bool(i.factor_reused), "batch_size": i.batch_size,
+                "queue_ms": i.queue_ms, "latency_ms": i.latency_ms}
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """(positions, info) once the request finished; None on timeout.
+        Raises ArapError when the request failed."""
+        info = RequestInfo()
+        rc = self.lib.arap_srv_wait(self.h, int(ticket), int(timeout_ms), C.byref(info))
+        if rc == ARAP_PENDING:
+            return None
+        out = self._live.pop(ticket, None)
+        if rc != ARAP_OK:
+            raise ArapError(rc, self.lib.arap_srv_last_error(self.h).decode())
+        return out, self._info(info)
+
+    def poll(self, ticket: int):
+        return self.wait(ticket, 0)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self._check(self.lib.arap_srv_stats(self.h, C.byref(st)))
+        return {n: getattr(st, n) for n, _ in ServerStats._fields_ if n != "pad"}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.arap_srv_destroy(self.h)
+            self.h = None
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class ArrayMesh:

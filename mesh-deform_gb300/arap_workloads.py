@@ -14,6 +14,11 @@ the benchmark sizes:
                            shifted (0,0.5,0)
 * ``cfg_noisy_sphere``     icosphere level 7 with radial noise, 16 handle caps, 1 anchor cap
 * ``cfg_pose_batch``       icosphere level 5, bottom cap anchored, top cap handle, many poses
+* ``serving_pool`` / ``serving_requests``
+                           a pool of noisy icospheres (levels 3-6) and bars (1k-200k
+                           vertices, log-uniform) and a stream of requests with 1-8
+                           handle caps plus one anchor cap, half of them reusing a
+                           constraint set seen before, 5-50 iterations
 
 Every function is deterministic for a given seed. Faces are counter-clockwise
 seen from outside, as the adapter concept asks (inc/deform/openmesh_adapter.h:88).
@@ -247,6 +252,106 @@ def cfg_pose_batch(level: int = 5, n_poses: int = 256, seed: int = 20261203,
     return Workload(f"pose_batch_l{level}x{n_poses}", v, f, cidx, poses[0].copy(), iterations,
                     precision, poses=poses,
                     info={"seed": seed, "anchors": int(len(anchors)), "handles": int(len(handles))})
+
+
+@dataclass
+class PoolMesh:
+    name: str
+    positions: np.ndarray
+    faces: np.ndarray
+    kind: str                      # "sphere" | "bar"
+
+    @property
+    def V(self) -> int:
+        return int(self.positions.shape[0])
+
+
+@dataclass
+class ServeRequest:
+    mesh: int
+    cidx: np.ndarray
+    ctargets: np.ndarray
+    iterations: int
+    reused: bool                   # constraint set drawn from the ones used before
+    arrival: float = 0.0           # seconds from the stream's start
+
+
+def serving_pool(n_meshes: int = 64, seed: int = 20261203, levels=(3, 4, 5, 6), v_min: int = 1000,
+                 v_max: int = 200_000) -> list:
+    """Half noisy icospheres (radius 1+N(0,0.01), level uniform in `levels`),
+    half bars 10x1x1 whose vertex count is log-uniform in [v_min, v_max]
+    (the grid spacing that gives it: V ~ 42/h^2)."""
+    rng = np.random.default_rng(seed)
+    pool, spheres = [], {}
+    for i in range(n_meshes):
+        if rng.uniform() < 0.5:
+            lv = int(rng.choice(levels))
+            if lv not in spheres:
+                spheres[lv] = icosphere(lv)
+            v, f = spheres[lv]
+            v = v * (1.0 + rng.normal(0.0, 0.01, size=(len(v), 1)))
+            pool.append(PoolMesh(f"sphere{i}_l{lv}", v, f, "sphere"))
+        else:
+            target = float(np.exp(rng.uniform(np.log(v_min), np.log(v_max))))
+            h = 10.0 / max(2, round(10.0 / np.sqrt(42.0 / target)))
+            v, f, _ = bar_grid(10.0, 1.0, 1.0, h)
+            pool.append(PoolMesh(f"bar{i}_h{h:.4f}", v, f, "bar"))
+    return pool
+
+
+def _cap_sets(mesh: PoolMesh, rng, n_handles: int, radius: float = 0.15):
+    """Index sets of n_handles handle caps and one anchor cap: geodesic disks
+    on a sphere (the anchor at the south pole), Euclidean balls around random
+    surface vertices on a bar (the anchor at the x=0 end)."""
+    v = mesh.positions
+    if mesh.kind == "sphere":
+        c = rng.normal(size=(n_handles, 3))
+        c /= np.linalg.norm(c, axis=1, keepdims=True)
+        handles = _caps(v, c, radius)
+        (anchor,) = _caps(v, [np.array([0.0, 0.0, -1.0])], radius)
+    else:
+        centres = v[rng.integers(0, len(v), size=n_handles)]
+        handles = [np.nonzero(np.linalg.norm(v - c, axis=1) <= radius)[0] for c in centres]
+        anchor = np.nonzero(v[:, 0] < 0.2)[0]
+    return handles, anchor
+
+
+def serving_requests(pool: list, n_requests: int, seed: int = 20261204, reuse: float = 0.5,
+                     rate_hz: float | None = None, it_range=(5, 50), max_handles: int = 8) -> list:
+    """Requests over `pool`: mesh uniform; with probability `reuse` the
+    constraint set of an earlier request on the same mesh (new handle
+    translations), otherwise 1..max_handles new handle caps plus the anchor cap
+    (anchor wins overlaps, a vertex in several handle caps follows the first);
+    handle translations U[-0.3,0.3]^3; iterations uniform in it_range; Poisson
+    arrivals at rate_hz (all at t=0 when None)."""
+    rng = np.random.default_rng(seed)
+    seen = {i: [] for i in range(len(pool))}
+    out, t = [], 0.0
+    for _ in range(n_requests):
+        mi = int(rng.integers(0, len(pool)))
+        mesh = pool[mi]
+        reused = bool(seen[mi]) and rng.uniform() < reuse
+        if reused:
+            cidx, owner, nh = seen[mi][int(rng.integers(0, len(seen[mi])))]
+        else:
+            nh = int(rng.integers(1, max_handles + 1))
+            handles, anchor = _cap_sets(mesh, rng, nh)
+            own = -np.ones(mesh.V, np.int64)
+            for k, idx in enumerate(handles):
+                sel = idx[own[idx] == -1]
+                own[sel] = k
+            own[anchor] = nh
+            cidx = np.nonzero(own >= 0)[0].astype(np.int32)
+            owner = own[cidx]
+            seen[mi].append((cidx, owner, nh))
+        trans = rng.uniform(-0.3, 0.3, size=(nh + 1, 3))
+        trans[nh] = 0.0
+        tgt = mesh.positions[cidx] + trans[owner]
+        iters = int(rng.integers(it_range[0], it_range[1] + 1))
+        if rate_hz:
+            t += float(rng.exponential(1.0 / rate_hz))
+        out.append(ServeRequest(mi, cidx, tgt, iters, reused, t))
+    return out
 
 
 def bbox_rel_error(x: np.ndarray, ref: np.ndarray, rest: np.ndarray) -> float:

@@ -1,12 +1,13 @@
 """Builds libarap_gb300.so (the C ABI of include/arap_gpu.h) for sm_103a.
 
-Five translation units compiled in parallel, then linked with the static CUDA
+Six translation units compiled in parallel, then linked with the static CUDA
 runtime:
   csrc/arap_kernels.cu   the sm_103a kernels (nvcc)
   csrc/arap_context.cu   context state and the C ABI (nvcc)
   csrc/arap_noalloc.cu   cotan weights with static scratch (nvcc)
   csrc/arap_batch.cu     many poses of one mesh in one pass (nvcc)
   csrc/arap_symbolic.cpp host symbolic analysis (g++)
+  csrc/arap_server.cpp   the request scheduler of arap_srv_* (g++)
 The library is built in-tree (next to this file) and is git-ignored.
 """
 from __future__ import annotations
@@ -27,7 +28,11 @@ LIB = PKG / "libarap_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
                      f"-I{ROOT / 'include'}", "--expt-relaxed-constexpr"]
-GXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", f"-I{ROOT / 'include'}"]
+def cuda_include() -> str:
+    return str(Path(nvcc()).resolve().parent.parent / "include")
+
+
+GXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-pthread", f"-I{ROOT / 'include'}"]
 
 SOURCES = [
     ("nvcc", CSRC / "arap_kernels.cu"),
@@ -35,8 +40,10 @@ SOURCES = [
     ("nvcc", CSRC / "arap_noalloc.cu"),
     ("nvcc", CSRC / "arap_batch.cu"),
     ("g++", CSRC / "arap_symbolic.cpp"),
+    ("g++", CSRC / "arap_server.cpp"),
 ]
-HEADERS = [CSRC / "arap_kernels.h", CSRC / "arap_symbolic.h", CSRC / "arap_device.cuh", ROOT / "include" / "arap_gpu.h"]
+HEADERS = [CSRC / "arap_kernels.h", CSRC / "arap_symbolic.h", CSRC / "arap_device.cuh", CSRC / "arap_server.h",
+           ROOT / "include" / "arap_gpu.h"]
 
 
 def nvcc() -> str:
@@ -58,7 +65,7 @@ def _compile(kind: str, src: Path, extra: list[str]) -> Path:
     if kind == "nvcc":
         cmd = [nvcc()] + NVCC_FLAGS + extra + ["-c", str(src), "-o", str(obj)]
     else:
-        cmd = ["g++"] + GXX_FLAGS + ["-c", str(src), "-o", str(obj)]
+        cmd = ["g++"] + GXX_FLAGS + [f"-I{cuda_include()}", "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
@@ -78,7 +85,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     if LIB.exists() and not force and all(LIB.stat().st_mtime >= o.stat().st_mtime for o in objs):
         return LIB
     tmp = LIB.with_suffix(f".so.tmp{os.getpid()}")
-    cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", str(tmp)] + [str(o) for o in objs]
+    cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-Xcompiler", "-pthread", "-o", str(tmp)] + \
+        [str(o) for o in objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

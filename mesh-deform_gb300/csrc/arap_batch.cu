@@ -494,9 +494,9 @@ size_t batch_solve_smem_bytes(int max_ldx, int max_ld21, int pt) {
 
 template <int PT>
 static cudaError_t configure_pt(size_t bytes) {
-    cudaError_t e = cudaFuncSetAttribute(k_bsolve_fwd<PT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t e = raise_smem_limit((const void *)k_bsolve_fwd<PT>, (int)bytes);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_bsolve_bwd<PT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return raise_smem_limit((const void *)k_bsolve_bwd<PT>, (int)bytes);
 }
 
 cudaError_t configure_batch_smem(int max_ldx, int max_ld21, int pt) {

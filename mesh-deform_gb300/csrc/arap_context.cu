@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -21,26 +22,77 @@ using namespace arapgpu;
 
 namespace {
 
+// Device buffer from the device's stream-ordered memory pool, allocated and
+// freed on the owning context's stream: growing or dropping a buffer never
+// waits for work on other streams (a plain cudaFree would wait for the whole
+// device).
 struct DevBuf {
     void *p = nullptr;
     size_t cap = 0;
+    cudaStream_t st = nullptr;
     cudaError_t ensure(size_t bytes) {
         if (bytes <= cap && p) return cudaSuccess;
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, st);
         p = nullptr;
         cap = 0;
         const size_t want = std::max<size_t>(bytes, 256);
-        cudaError_t e = cudaMalloc(&p, want);
+        cudaError_t e = cudaMallocAsync(&p, want, st);
         if (e == cudaSuccess) cap = want;
+        else p = nullptr;
         return e;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, st);
         p = nullptr;
         cap = 0;
     }
     template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
 };
+
+// Freed pool memory stays with the process (release threshold at its
+// maximum), so contexts created after others were destroyed reuse it without
+// a trip to the driver. Set once per device.
+cudaError_t keep_pool_memory(int device) {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), device) != done.end()) return cudaSuccess;
+    cudaMemPool_t pool;
+    cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, device);
+    if (e != cudaSuccess) return e;
+    uint64_t thr = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (e == cudaSuccess) done.push_back(device);
+    return e;
+}
+
+// 64-byte words of pinned host memory for the per-context error word, handed
+// out from pages that live as long as the process (freeing pinned memory can
+// wait for the device).
+struct PinnedWords {
+    std::mutex mu;
+    std::vector<int *> free_words;
+    int *get() {
+        std::lock_guard<std::mutex> lk(mu);
+        if (free_words.empty()) {
+            char *page = nullptr;
+            if (cudaMallocHost(&page, 4096) != cudaSuccess) return nullptr;
+            for (int i = 0; i < 4096 / 64; ++i) free_words.push_back(reinterpret_cast<int *>(page + 64 * i));
+        }
+        int *w = free_words.back();
+        free_words.pop_back();
+        return w;
+    }
+    void put(int *w) {
+        std::lock_guard<std::mutex> lk(mu);
+        free_words.push_back(w);
+    }
+};
+
+PinnedWords &pinned_words() {
+    static PinnedWords *pw = new PinnedWords();  // never destroyed: pages outlive every context
+    return *pw;
+}
 
 thread_local std::string g_create_error;
 
@@ -67,7 +119,8 @@ struct arap_ctx {
     bool dirty = true;
     bool retarget = false;  // same constrained set, new targets: reuse weights and factor
     // symbolic cache (keyed by the constrained-vertex mask)
-    bool sym_valid = false;
+    bool sym_valid = false;  // analysed and uploaded
+    bool sym_host = false;   // analysed (host only)
     Symbolic sym;
     size_t smem_f32 = 0, smem_f64 = 0;  // dynamic shared memory the solve kernels are configured for
     // which precision the iteration state was set up for
@@ -94,6 +147,8 @@ struct arap_ctx {
     // asynchronous deform (arap_deform_async / arap_wait)
     bool in_flight = false;    // a deform was enqueued and not waited for
     int *herr_host = nullptr;  // pinned copy of the device error word
+    bool poses_in_flight = false;  // the pending deform is an arap_deform_poses_async
+    cudaEvent_t ev_done = nullptr;  // recorded after the last copy of an async deform
     size_t bsmem = 0;
     DevTopo dt{};
     DevSym ds{};
@@ -107,6 +162,14 @@ struct arap_ctx {
     std::vector<Pending> pending;
     double kms[ARAP_K_NUM_CLASSES] = {0};
     int64_t kcnt[ARAP_K_NUM_CLASSES] = {0};
+
+    std::vector<DevBuf *> buffers() {
+        return {&faces, &ent_ptr, &ent_fc, &hc, &w_orig, &rest, &targets, &out, &drow, &dcol, &dent, &oldidx,
+                &amap, &dmap, &sn, &rows, &relind, &child, &level_sn, &fitems, &w64, &w32, &p64, &pc64, &p32,
+                &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
+                &errw, &ticket, &flags, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
+                &bticket, &bflags};
+    }
 };
 
 #define CK(call)                                                                       \
@@ -173,13 +236,88 @@ int fail(arap_ctx *ctx, int code, const std::string &msg) {
 
 // Builds (or reuses) the symbolic analysis for the current constraint mask and
 // uploads it.
-int prepare_symbolic(arap_ctx *ctx) {
-    if (ctx->sym_valid && ctx->sym.constrained == ctx->cmask) return ARAP_OK;
+// Host part of prepare_symbolic: the analysis of the current mask, kept until
+// the mask changes.
+int analyze_symbolic(arap_ctx *ctx) {
+    if (ctx->sym_host && ctx->sym.constrained == ctx->cmask) return ARAP_OK;
     ctx->sym_valid = false;
+    ctx->sym_host = false;
     std::string err;
     bool singular = false;
     if (!build_symbolic(ctx->topo, ctx->cmask, ctx->sym, err, singular))
         return fail(ctx, singular ? ARAP_ERR_NOT_SPD : ARAP_ERR_CUDA, err);
+    ctx->sym_host = true;
+    return ARAP_OK;
+}
+
+// Bytes of every device buffer the setup of precision T (and, for n_poses > 0,
+// arap_deform_poses with that many poses) holds, buffer by buffer.
+template <typename T>
+void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, size_t>> &out) {
+    const Symbolic &s = ctx->sym;
+    const size_t V = (size_t)s.V, m1 = (size_t)std::max(s.m, 1), nnz = s.dcol.size(), S1 = (size_t)std::max(s.S, 1);
+    out.clear();
+    auto add = [&](DevBuf &b, size_t bytes) { out.push_back({&b, bytes}); };
+    // symbolic uploads and solve scheduling state
+    add(ctx->drow, s.drow.size() * 4);
+    add(ctx->dcol, s.dcol.size() * 4);
+    add(ctx->dent, s.dent.size() * 4);
+    add(ctx->oldidx, s.oldidx.size() * 4);
+    add(ctx->amap, s.amap.size() * 8);
+    add(ctx->dmap, s.dmap.size() * 8);
+    add(ctx->sn, s.sn.size() * sizeof(SnInfo));
+    add(ctx->rows, s.rows.size() * 4);
+    add(ctx->relind, s.relind.size() * 4);
+    add(ctx->child, s.child.size() * 4);
+    add(ctx->level_sn, s.level_sn.size() * 4);
+    add(ctx->fitems, s.fitems.size() * sizeof(FItem));
+    add(ctx->ticket, 2 * sizeof(unsigned long long));
+    add(ctx->flags, 2 * sizeof(unsigned) * S1);
+    // iteration state and factor (setup_alloc)
+    const bool f32 = sizeof(T) == 4;
+    add(ctx->w64, nnz * sizeof(double));
+    if (f32) add(ctx->w32, nnz * sizeof(float));
+    add(ctx->p64, V * sizeof(Vec4<double>));
+    add(ctx->pc64, V * sizeof(Vec4<double>));
+    if (f32) {
+        add(ctx->p32, V * sizeof(Vec4<float>));
+        add(ctx->pc32, V * sizeof(Vec4<float>));
+    }
+    add(ctx->R, V * 3 * sizeof(Vec4<T>));
+    add(ctx->diag64, m1 * sizeof(double));
+    add(ctx->bfixed, m1 * sizeof(Vec4<double>));
+    if (f32) add(ctx->redge, std::max<size_t>(nnz, 1) * sizeof(Vec4<float>));
+    add(ctx->b, m1 * sizeof(Vec4<T>));
+    add(ctx->sol, m1 * sizeof(Vec4<T>));
+    add(ctx->uvec, (size_t)std::max<int64_t>(s.uvec_size, 1) * sizeof(Vec4<T>));
+    add(ctx->Lval, (size_t)std::max<int64_t>(s.panel_size, 1) * sizeof(T));
+    add(ctx->Dinv, (size_t)std::max<int64_t>(s.dinv_size, 1) * sizeof(T));
+    add(ctx->Upd, (size_t)std::max<int64_t>(s.upd_size, 1) * sizeof(T));
+    add(ctx->Xinv, (size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T));
+    add(ctx->L21, (size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T));
+    add(ctx->L21T, (size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T));
+    if (n_poses > 0) {
+        const size_t P = (size_t)n_poses, VP = V * P, MP = m1 * P, nc = V - (size_t)s.m;
+        const int pt = std::max(batch_pose_tile(s.max_ldx, s.max_ld21), 1);
+        const size_t T_ = (P + pt - 1) / pt;
+        add(ctx->bpc64, VP * sizeof(Vec4<double>));
+        add(ctx->bpc32, VP * sizeof(Vec4<float>));
+        add(ctx->bR, VP * 3 * sizeof(Vec4<float>));
+        add(ctx->bbfixed, MP * sizeof(Vec4<double>));
+        add(ctx->bb, MP * sizeof(Vec4<float>));
+        add(ctx->bsol, MP * sizeof(Vec4<float>));
+        add(ctx->buvec, (size_t)std::max<int64_t>(s.uvec_size, 1) * P * sizeof(Vec4<float>));
+        add(ctx->bout, VP * 3 * sizeof(double));
+        add(ctx->btargets, P * nc * 3 * sizeof(double));
+        add(ctx->bticket, 2 * sizeof(unsigned long long));
+        add(ctx->bflags, 2 * S1 * T_ * sizeof(unsigned));
+    }
+}
+
+int prepare_symbolic(arap_ctx *ctx) {
+    if (ctx->sym_valid && ctx->sym.constrained == ctx->cmask) return ARAP_OK;
+    const int rc = analyze_symbolic(ctx);
+    if (rc != ARAP_OK) return rc;
     Symbolic &s = ctx->sym;
     cudaStream_t st = ctx->stream;
     ctx->gen++;
@@ -248,37 +386,15 @@ int prepare_symbolic(arap_ctx *ctx) {
 // T use. Any reallocation bumps ctx->gen so captured graphs are rebuilt.
 template <typename T>
 int setup_alloc(arap_ctx *ctx) {
-    const Symbolic &s = ctx->sym;
-    const int V = s.V, m = s.m;
-    const size_t nnz = s.dcol.size();
-    DevBuf *bufs[] = {&ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32, &ctx->pc32, &ctx->R, &ctx->diag64,
-                      &ctx->bfixed, &ctx->b, &ctx->sol, &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd,
-                      &ctx->Xinv, &ctx->L21, &ctx->L21T, &ctx->redge};
-    void *before[sizeof(bufs) / sizeof(bufs[0])];
-    for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i) before[i] = bufs[i]->p;
-    CK(ctx->w64.ensure(nnz * sizeof(double)));
-    if (sizeof(T) == 4) CK(ctx->w32.ensure(nnz * sizeof(float)));
-    CK(ctx->p64.ensure((size_t)V * sizeof(Vec4<double>)));
-    CK(ctx->pc64.ensure((size_t)V * sizeof(Vec4<double>)));
-    if (sizeof(T) == 4) {
-        CK(ctx->p32.ensure((size_t)V * sizeof(Vec4<float>)));
-        CK(ctx->pc32.ensure((size_t)V * sizeof(Vec4<float>)));
+    std::vector<std::pair<DevBuf *, size_t>> plan;
+    planned_sizes<T>(ctx, 0, plan);
+    bool moved = false;
+    for (auto &pb : plan) {
+        void *before = pb.first->p;
+        CK(pb.first->ensure(pb.second));
+        moved |= before != pb.first->p;
     }
-    CK(ctx->R.ensure((size_t)V * 3 * sizeof(Vec4<T>)));
-    CK(ctx->diag64.ensure((size_t)std::max(m, 1) * sizeof(double)));
-    CK(ctx->bfixed.ensure((size_t)std::max(m, 1) * sizeof(Vec4<double>)));
-    if (sizeof(T) == 4) CK(ctx->redge.ensure(std::max<size_t>(nnz, 1) * sizeof(Vec4<float>)));
-    CK(ctx->b.ensure((size_t)std::max(m, 1) * sizeof(Vec4<T>)));
-    CK(ctx->sol.ensure((size_t)std::max(m, 1) * sizeof(Vec4<T>)));
-    CK(ctx->uvec.ensure((size_t)std::max<int64_t>(s.uvec_size, 1) * sizeof(Vec4<T>)));
-    CK(ctx->Lval.ensure((size_t)std::max<int64_t>(s.panel_size, 1) * sizeof(T)));
-    CK(ctx->Dinv.ensure((size_t)std::max<int64_t>(s.dinv_size, 1) * sizeof(T)));
-    CK(ctx->Upd.ensure((size_t)std::max<int64_t>(s.upd_size, 1) * sizeof(T)));
-    CK(ctx->Xinv.ensure((size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T)));
-    CK(ctx->L21.ensure((size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T)));
-    CK(ctx->L21T.ensure((size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T)));
-    for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
-        if (before[i] != bufs[i]->p) { ctx->gen++; break; }
+    if (moved) ctx->gen++;
     return ARAP_OK;
 }
 
@@ -492,6 +608,7 @@ const char *arap_status_string(int status) {
     case ARAP_ERR_ADMISSION_REFUSED: return "ARAP_ERR_ADMISSION_REFUSED";
     case ARAP_ERR_NO_DEVICE: return "ARAP_ERR_NO_DEVICE";
     case ARAP_ERR_UNSUPPORTED: return "ARAP_ERR_UNSUPPORTED";
+    case ARAP_PENDING: return "ARAP_PENDING";
     default: return "ARAP_ERR_UNKNOWN";
     }
 }
@@ -499,6 +616,76 @@ const char *arap_status_string(int status) {
 const char *arap_last_error(const arap_ctx *ctx) {
     return ctx ? ctx->err.c_str() : g_create_error.c_str();
 }
+
+namespace {
+// Everything arap_create does after the topology is built: stream, events,
+// device copies of the topology (uploaded, or copied from src's), the
+// per-mesh buffers. On failure the context is destroyed.
+int finish_create(arap_ctx *ctx, int device, const arap_ctx *src, arap_ctx **out) {
+    const int n_vertices = ctx->topo.V, n_faces = ctx->topo.F;
+    ctx->cmask.assign(n_vertices, 0);
+    auto bail = [&](cudaError_t e, const char *what) {
+        g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
+        arap_destroy(ctx);
+        return e == cudaErrorMemoryAllocation ? ARAP_ERR_OUT_OF_MEMORY : ARAP_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e, "cudaSetDevice");
+    if ((e = keep_pool_memory(device)) != cudaSuccess) return bail(e, "memory pool");
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(e, "cudaStreamCreate");
+    for (DevBuf *b : ctx->buffers()) b->st = ctx->stream;
+    if ((e = cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming)) != cudaSuccess)
+        return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&ctx->ev2)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    const Topology &t = ctx->topo;
+    if (!src) {
+        if ((e = upload(ctx->faces, t.faces, ctx->stream)) != cudaSuccess) return bail(e, "upload faces");
+        if ((e = upload(ctx->ent_ptr, t.ent_ptr, ctx->stream)) != cudaSuccess) return bail(e, "upload adjacency");
+        if ((e = upload(ctx->ent_fc, t.ent_fc, ctx->stream)) != cudaSuccess) return bail(e, "upload adjacency");
+    } else {
+        const std::pair<DevBuf *, const DevBuf *> copies[] = {
+            {&ctx->faces, &src->faces}, {&ctx->ent_ptr, &src->ent_ptr}, {&ctx->ent_fc, &src->ent_fc}};
+        for (const auto &c : copies) {
+            if ((e = c.first->ensure(c.second->cap)) != cudaSuccess) return bail(e, "alloc");
+            if ((e = cudaMemcpyAsync(c.first->p, c.second->p, c.second->cap, cudaMemcpyDeviceToDevice,
+                                     ctx->stream)) != cudaSuccess)
+                return bail(e, "copy topology");
+        }
+    }
+    if ((e = ctx->hc.ensure((size_t)3 * std::max(n_faces, 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->w_orig.ensure((size_t)std::max(t.nnz(), 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->rest.ensure((size_t)3 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->targets.ensure((size_t)3 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->out.ensure((size_t)9 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
+        return bail(e, "alloc");
+    if ((e = ctx->errw.ensure(sizeof(int))) != cudaSuccess) return bail(e, "alloc");
+    if (!(ctx->herr_host = pinned_words().get())) return bail(cudaErrorMemoryAllocation, "pinned error word");
+    *ctx->herr_host = 0;
+    if (src && src->have_rest) {
+        if ((e = cudaMemcpyAsync(ctx->rest.p, src->rest.p, (size_t)3 * n_vertices * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, ctx->stream)) != cudaSuccess)
+            return bail(e, "copy rest positions");
+        ctx->have_rest = true;
+    }
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return bail(e, "sync");
+    ctx->dt.V = n_vertices;
+    ctx->dt.F = n_faces;
+    ctx->dt.nnz = t.nnz();
+    ctx->dt.faces = ctx->faces.as<int32_t>();
+    ctx->dt.ent_ptr = ctx->ent_ptr.as<int32_t>();
+    ctx->dt.ent_fc = ctx->ent_fc.as<int32_t>();
+    *out = ctx;
+    return ARAP_OK;
+}
+
+}  // namespace
 
 int arap_create(int32_t n_vertices, int32_t n_faces, const int32_t *faces, int32_t device, arap_ctx **out) {
     g_create_error.clear();
@@ -524,64 +711,35 @@ int arap_create(int32_t n_vertices, int32_t n_faces, const int32_t *faces, int32
         delete ctx;
         return ARAP_ERR_BAD_INDEX;
     }
-    ctx->cmask.assign(n_vertices, 0);
-    auto bail = [&](cudaError_t e, const char *what) {
-        g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
-        arap_destroy(ctx);
-        return e == cudaErrorMemoryAllocation ? ARAP_ERR_OUT_OF_MEMORY : ARAP_ERR_CUDA;
-    };
-    cudaError_t e;
-    if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e, "cudaSetDevice");
-    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
-        return bail(e, "cudaStreamCreate");
-    if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
-    if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
-    if ((e = cudaEventCreate(&ctx->ev2)) != cudaSuccess) return bail(e, "cudaEventCreate");
-    const Topology &t = ctx->topo;
-    if ((e = upload(ctx->faces, t.faces, ctx->stream)) != cudaSuccess) return bail(e, "upload faces");
-    if ((e = upload(ctx->ent_ptr, t.ent_ptr, ctx->stream)) != cudaSuccess) return bail(e, "upload adjacency");
-    if ((e = upload(ctx->ent_fc, t.ent_fc, ctx->stream)) != cudaSuccess) return bail(e, "upload adjacency");
-    if ((e = ctx->hc.ensure((size_t)3 * std::max(n_faces, 1) * sizeof(double))) != cudaSuccess)
-        return bail(e, "alloc");
-    if ((e = ctx->w_orig.ensure((size_t)std::max(t.nnz(), 1) * sizeof(double))) != cudaSuccess)
-        return bail(e, "alloc");
-    if ((e = ctx->rest.ensure((size_t)3 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
-        return bail(e, "alloc");
-    if ((e = ctx->targets.ensure((size_t)3 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
-        return bail(e, "alloc");
-    if ((e = ctx->out.ensure((size_t)9 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
-        return bail(e, "alloc");
-    if ((e = ctx->errw.ensure(sizeof(int))) != cudaSuccess) return bail(e, "alloc");
-    if ((e = cudaMallocHost(&ctx->herr_host, sizeof(int))) != cudaSuccess) return bail(e, "alloc");
-    *ctx->herr_host = 0;
-    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return bail(e, "sync");
-    ctx->dt.V = n_vertices;
-    ctx->dt.F = n_faces;
-    ctx->dt.nnz = t.nnz();
-    ctx->dt.faces = ctx->faces.as<int32_t>();
-    ctx->dt.ent_ptr = ctx->ent_ptr.as<int32_t>();
-    ctx->dt.ent_fc = ctx->ent_fc.as<int32_t>();
-    *out = ctx;
-    return ARAP_OK;
+    return finish_create(ctx, device, nullptr, out);
+}
+
+int arap_create_like(const arap_ctx *src, arap_ctx **out) {
+    g_create_error.clear();
+    if (!out || !src) {
+        g_create_error = "arap_create_like: invalid argument";
+        return ARAP_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    arap_ctx *ctx = new arap_ctx();
+    ctx->device = src->device;
+    ctx->topo = src->topo;
+    ctx->precision = src->precision;
+    ctx->refine = src->refine;
+    ctx->use_graphs = src->use_graphs;
+    return finish_create(ctx, src->device, src, out);
 }
 
 void arap_destroy(arap_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    DevBuf *bufs[] = {&ctx->faces, &ctx->ent_ptr, &ctx->ent_fc, &ctx->hc, &ctx->w_orig, &ctx->rest,
-                      &ctx->targets, &ctx->out, &ctx->drow, &ctx->dcol, &ctx->dent, &ctx->oldidx,
-                      &ctx->amap, &ctx->dmap, &ctx->sn, &ctx->rows, &ctx->relind, &ctx->child,
-                      &ctx->level_sn, &ctx->fitems, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64, &ctx->p32,
-                      &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
-                      &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->L21T, &ctx->errw, &ctx->ticket,
-                      &ctx->flags, &ctx->btargets, &ctx->bpc64, &ctx->bpc32, &ctx->bR, &ctx->bbfixed,
-                      &ctx->bb, &ctx->bsol, &ctx->buvec, &ctx->bout, &ctx->bticket, &ctx->bflags};
-    for (DevBuf *b : bufs) b->release();
+    for (DevBuf *b : ctx->buffers()) b->release();
     for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
     if (ctx->g_setup) cudaGraphExecDestroy(ctx->g_setup);
     if (ctx->g_iter) cudaGraphExecDestroy(ctx->g_iter);
-    if (ctx->herr_host) cudaFreeHost(ctx->herr_host);
+    if (ctx->herr_host) pinned_words().put(ctx->herr_host);
+    if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev2) cudaEventDestroy(ctx->ev2);
@@ -654,8 +812,8 @@ int arap_set_constraints(arap_ctx *ctx, int32_t n, const int32_t *indices, const
     return ARAP_OK;
 }
 
-int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
-                      double *out_xyz) {
+int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
+                            double *out_xyz) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
     if (ctx->in_flight) {
         const int rc_ = arap_wait(ctx);
@@ -668,10 +826,14 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
     if (ctx->cidx.empty()) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no constrained vertex");
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
-    CK(cudaStreamSynchronize(st));
-    collect_profile(ctx);
+    if (ctx->profiling) {
+        CK(cudaStreamSynchronize(st));
+        collect_profile(ctx);
+    }
     ctx->launches = 0;
+    ctx->setup_ms = ctx->iter_ms = 0.0;
     CK(cudaEventRecord(ctx->ev0, st));
+    CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
     if (ctx->dirty || ctx->state_prec != ARAP_PRECISION_MIXED) {
         {
             Prof pr(ctx, ARAP_K_WEIGHTS);
@@ -682,13 +844,10 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
         if (rc != ARAP_OK) return rc;
         rc = setup_alloc<float>(ctx);
         if (rc != ARAP_OK) return rc;
-        CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
         rc = setup_enqueue<float>(ctx);
         if (rc != ARAP_OK) return rc;
-        CK(cudaMemcpyAsync(ctx->herr_host, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (*ctx->herr_host & kErrNotSpd)
-            return fail(ctx, ARAP_ERR_NOT_SPD, "Cholesky factorisation met a non-positive pivot");
+        // a failed pivot is reported by arap_wait (the device error word)
+        ctx->retarget = false;
         ctx->state_prec = ARAP_PRECISION_MIXED;
         ctx->have_rotations = true;
         ctx->dirty = false;
@@ -729,7 +888,6 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
     if (targets)
         CK(cudaMemcpyAsync(ctx->btargets.p, targets, (size_t)P * nc * 3 * sizeof(double), cudaMemcpyHostToDevice,
                            st));
-    CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
     {
         Prof pr(ctx, ARAP_K_ASSEMBLE);
         launch_bsetup(d, P, ctx->p64.as<Vec4<double>>(), ctx->btargets.as<double>(), ctx->bpc64.as<Vec4<double>>(),
@@ -790,20 +948,19 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
         ctx->launches += 1;
         CK(cudaMemcpyAsync(out_xyz, ctx->bout.p, (size_t)P * V * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     }
-    int herr = 0;
-    CK(cudaMemcpyAsync(&herr, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    collect_profile(ctx);
-    float a = 0.f, b = 0.f;
-    cudaEventElapsedTime(&a, ctx->ev0, ctx->ev1);
-    cudaEventElapsedTime(&b, ctx->ev1, ctx->ev2);
-    ctx->setup_ms = a;
-    ctx->iter_ms = b;
-    if (herr & kErrTimeout) {
-        ctx->bS = -1;  // rebuild the scheduling counters next time
-        return fail(ctx, ARAP_ERR_TIMEOUT, "a triangular-solve wait exceeded its bound");
-    }
+    CK(cudaMemcpyAsync(ctx->herr_host, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(ctx->ev_done, st));
+    CK(cudaGetLastError());
+    ctx->in_flight = true;
+    ctx->poses_in_flight = true;
     return ARAP_OK;
+}
+
+int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
+                      double *out_xyz) {
+    const int rc = arap_deform_poses_async(ctx, n_poses, targets, iterations, out_xyz);
+    if (rc != ARAP_OK) return rc;
+    return arap_wait(ctx);
 }
 
 int arap_set_targets(arap_ctx *ctx, int32_t n, const double *xyz) {
@@ -816,10 +973,11 @@ int arap_set_targets(arap_ctx *ctx, int32_t n, const double *xyz) {
         return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "arap_set_targets needs one target per constrained vertex");
     std::memcpy(ctx->ctgt.data(), xyz, sizeof(double) * 3 * (size_t)n);
     CK(cudaSetDevice(ctx->device));
+    // a copy from pageable memory returns once the source is staged, so the
+    // host vector may change right after
     if (n > 0)
         CK(cudaMemcpyAsync(ctx->targets.p, ctx->ctgt.data(), ctx->ctgt.size() * sizeof(double),
                            cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
     if (!ctx->dirty) ctx->retarget = true;
     return ARAP_OK;
 }
@@ -906,8 +1064,10 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
                            st));
     }
     CK(cudaMemcpyAsync(ctx->herr_host, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(ctx->ev_done, st));
     CK(cudaGetLastError());
     ctx->in_flight = true;
+    ctx->poses_in_flight = false;
     return ARAP_OK;
 }
 
@@ -932,9 +1092,24 @@ int arap_wait(arap_ctx *ctx) {
         // scheduling counters may be inconsistent now: rebuild them next time
         ctx->sym_valid = false;
         ctx->dirty = true;
+        ctx->bS = -1;
         return fail(ctx, ARAP_ERR_TIMEOUT, "a bounded in-kernel wait expired");
     }
     return ARAP_OK;
+}
+
+int arap_query(arap_ctx *ctx, int32_t *done) {
+    if (check_ctx(ctx) || !done) return ARAP_ERR_INVALID_ARGUMENT;
+    *done = 1;
+    if (!ctx->in_flight) return ARAP_OK;
+    CK(cudaSetDevice(ctx->device));
+    const cudaError_t q = cudaEventQuery(ctx->ev_done);
+    if (q == cudaErrorNotReady) {
+        *done = 0;
+        return ARAP_OK;
+    }
+    if (q != cudaSuccess) CK(q);
+    return arap_wait(ctx);
 }
 
 int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
@@ -1080,19 +1255,35 @@ int arap_get_launch_count(arap_ctx *ctx, int64_t *launches) {
     return ARAP_OK;
 }
 
+int arap_plan_bytes(arap_ctx *ctx, int32_t n_poses, int64_t *bytes) {
+    if (check_ctx(ctx) || !bytes || n_poses < 0) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    *bytes = 0;
+    int64_t total = 0;
+    std::vector<std::pair<DevBuf *, size_t>> plan;
+    if (!ctx->cidx.empty()) {
+        const int rc = analyze_symbolic(ctx);
+        if (rc != ARAP_OK) return rc;
+        if (ctx->precision == ARAP_PRECISION_FP64 && n_poses == 0) planned_sizes<double>(ctx, 0, plan);
+        else planned_sizes<float>(ctx, n_poses, plan);
+    }
+    for (DevBuf *b : ctx->buffers()) {
+        size_t want = b->cap;
+        for (auto &pb : plan)
+            if (pb.first == b) want = std::max(want, std::max<size_t>(pb.second, 256));
+        total += (int64_t)want;
+    }
+    *bytes = total;
+    return ARAP_OK;
+}
+
 int64_t arap_device_bytes(const arap_ctx *ctx) {
     if (!ctx) return 0;
-    const DevBuf *bufs[] = {&ctx->faces, &ctx->ent_ptr, &ctx->ent_fc, &ctx->hc, &ctx->w_orig, &ctx->rest,
-                            &ctx->targets, &ctx->out, &ctx->drow, &ctx->dcol, &ctx->dent, &ctx->oldidx,
-                            &ctx->amap, &ctx->dmap, &ctx->sn, &ctx->rows, &ctx->relind, &ctx->child,
-                            &ctx->level_sn, &ctx->fitems, &ctx->w64, &ctx->w32, &ctx->p64, &ctx->pc64,
-                            &ctx->p32, &ctx->pc32, &ctx->R, &ctx->diag64, &ctx->bfixed, &ctx->b, &ctx->sol,
-                            &ctx->uvec, &ctx->Lval, &ctx->Dinv, &ctx->Upd, &ctx->Xinv, &ctx->L21, &ctx->L21T,
-                            &ctx->redge, &ctx->errw, &ctx->ticket, &ctx->flags, &ctx->btargets, &ctx->bpc64,
-                            &ctx->bpc32, &ctx->bR, &ctx->bbfixed, &ctx->bb, &ctx->bsol, &ctx->buvec, &ctx->bout,
-                            &ctx->bticket, &ctx->bflags};
     int64_t total = 0;
-    for (const DevBuf *b : bufs) total += (int64_t)b->cap;
+    for (const DevBuf *b : const_cast<arap_ctx *>(ctx)->buffers()) total += (int64_t)b->cap;
     return total;
 }
 

@@ -6,6 +6,8 @@
 #include "arap_device.cuh"
 
 #include <cstdio>
+#include <map>
+#include <mutex>
 
 namespace arapgpu {
 
@@ -1186,24 +1188,39 @@ void launch_gather_rotations(const DevSym &s, const Vec4<T> *R, double *out9, cu
 }
 
 // Raises the dynamic shared-memory limit of the column-block inverse kernel.
+// Raises, never lowers, a kernel's dynamic shared-memory limit on the current
+// device. The limit belongs to the kernel, not to a context: contexts of
+// different sizes in one process must not lower each other's.
+cudaError_t raise_smem_limit(const void *func, int bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, int> current;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    int &cur = current[{dev, func}];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
 cudaError_t configure_factor_smem(int max_ncol) {
     const int rows = (max_ncol + NB - 1) / NB * NB;
-    cudaError_t e = cudaFuncSetAttribute(k_fx<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(rows * (NB + 1) * sizeof(float)));
+    cudaError_t e = raise_smem_limit((const void *)k_fx<float>, (int)(rows * (NB + 1) * sizeof(float)));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_fx<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(rows * (NB + 1) * sizeof(double)));
+    return raise_smem_limit((const void *)k_fx<double>, (int)(rows * (NB + 1) * sizeof(double)));
 }
 
 // Raises the dynamic shared-memory limit of the solve kernels (bytes per CTA).
 cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64) {
-    cudaError_t e = cudaFuncSetAttribute(k_solve_fwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f32);
+    cudaError_t e = raise_smem_limit((const void *)k_solve_fwd<float>, bytes_f32);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_solve_bwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f32);
+    e = raise_smem_limit((const void *)k_solve_bwd<float>, bytes_f32);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_solve_fwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f64);
+    e = raise_smem_limit((const void *)k_solve_fwd<double>, bytes_f64);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_solve_bwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes_f64);
+    return raise_smem_limit((const void *)k_solve_bwd<double>, bytes_f64);
 }
 
 // explicit instantiations

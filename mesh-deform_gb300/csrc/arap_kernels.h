@@ -43,6 +43,8 @@ struct DevSym {
     const int32_t *rows, *relind, *child, *level_sn;
 };
 
+// raises (never lowers) a kernel's dynamic shared-memory limit on the current device
+cudaError_t raise_smem_limit(const void *func, int bytes);
 // cotangent halves per face (computeCotanWeights arap.h:189-222), FP64
 void launch_face_cots(const DevTopo &t, const double *rest_xyz, double *hc, cudaStream_t st);
 // edge weights per device entry (w64/w32) and per original entry (w_orig); any

@@ -48,6 +48,16 @@ def test_create_without_device_fails_loudly(gpu):
     assert e.value.code == gpu.ARAP_ERR_NO_DEVICE
 
 
+def test_server_without_device_fails_loudly(gpu):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(gpu.ArapError) as e:
+        gpu.ArapServer()
+    assert e.value.code == gpu.ARAP_ERR_NO_DEVICE
+
+
 CASES = [
     lambda: W.cfg_icosphere_l4(level=4),
     lambda: W.cfg_twisted_bar(h=0.05),
