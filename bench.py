@@ -341,7 +341,7 @@ def _serve_stream(G, W, pool, reqs, args, local, clocks=None):
     iterations) and the stream's wall time and server stats."""
     srv = G.ArapServer(device=local, precision="mixed", refine_steps=args.refine,
                        max_in_flight=args.serve_in_flight, prep_threads=args.serve_prep_threads,
-                       max_batch=args.serve_max_batch)
+                       max_batch=args.serve_max_batch, solve_ctas=args.serve_solve_ctas)
     ids = [srv.add_mesh(m.positions, m.faces) for m in pool]
     tickets = [None] * len(reqs)
     t0 = time.perf_counter()
@@ -496,6 +496,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: skip the end-to-end pass")
     ap.add_argument("--poses", type=int, default=256, help="pose_batch: handle poses per step")
+    ap.add_argument("--solve-ctas", type=int, default=0, help="CTAs per triangular-solve launch (0: auto)")
     ap.add_argument("--concurrent", type=int, default=os.cpu_count() or 1,
                     help="independent requests in flight per step (default: host threads, as the reference arm)")
     ap.add_argument("--serve-rates", default="50,100,200,0",
@@ -506,6 +507,7 @@ def main():
     ap.add_argument("--serve-max-batch", type=int, default=64)
     ap.add_argument("--serve-check", type=int, default=40, help="serving: results checked against the oracle")
     ap.add_argument("--serve-fp64-requests", type=int, default=100)
+    ap.add_argument("--serve-solve-ctas", type=int, default=0, help="serving: CTAs per solve launch (0: auto)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -543,6 +545,7 @@ def main():
     for _ in range(N):
         c = G.ArapContext(w.V, w.faces, device=local)
         c.set_precision(args.precision, args.refine)
+        c.set_solve_ctas(args.solve_ctas)
         c.set_rest_positions(w.positions)
         c.set_constraints(w.cidx, w.ctargets)
         ctxs.append(c)

@@ -128,6 +128,13 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
    is what arap_wait returns. */
 int arap_query(arap_ctx *ctx, int32_t *done);
 
+/* Most CTAs one triangular-solve launch uses (0, the default: as many as fit
+   on the device). Each CTA works through the supernodes in schedule order, so
+   any count gives the same result; a smaller count leaves room for the
+   launches of other contexts running at the same time. Takes effect at the
+   next deform (which sets the problem up again). */
+int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas);
+
 /* enable != 0 (the default) runs the setup and the iteration sequence as CUDA
    graphs captured on first use and replayed while the problem's size,
    precision and iteration count stay the same; 0 launches every kernel
@@ -276,6 +283,7 @@ typedef struct arap_server_config {
     int32_t max_batch;           /* most requests per multi-pose launch (0: 64; 1: no batching) */
     int32_t max_queue;           /* waiting requests before submit refuses (0: 65536) */
     int32_t poll_us;             /* completion polling interval of the scheduler (0: 20) */
+    int32_t solve_ctas;          /* arap_set_solve_ctas of every context (0: as many as fit) */
 } arap_server_config;
 
 typedef struct arap_request {

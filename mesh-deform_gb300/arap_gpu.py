@@ -49,7 +49,8 @@ _dp = C.POINTER(C.c_double)
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("refine_steps", C.c_int32),
                 ("max_in_flight", C.c_int32), ("device_budget_bytes", C.c_int64), ("prep_threads", C.c_int32),
-                ("max_batch", C.c_int32), ("max_queue", C.c_int32), ("poll_us", C.c_int32)]
+                ("max_batch", C.c_int32), ("max_queue", C.c_int32), ("poll_us", C.c_int32),
+                ("solve_ctas", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -99,6 +100,7 @@ SIGNATURES = {
     "arap_deform_async": (C.c_int, [_P, _I32, _dp]),
     "arap_wait": (C.c_int, [_P]),
     "arap_set_graphs": (C.c_int, [_P, _I32]),
+    "arap_set_solve_ctas": (C.c_int, [_P, _I32]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
     "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
     "arap_query": (C.c_int, [_P, C.POINTER(C.c_int32)]),
@@ -240,6 +242,9 @@ class ArapContext:
     def set_graphs(self, enable: bool) -> None:
         self._check(self.lib.arap_set_graphs(self.h, 1 if enable else 0))
 
+    def set_solve_ctas(self, n: int):
+        self._check(self.lib.arap_set_solve_ctas(self.h, int(n)))
+
     def set_targets(self, xyz):
         x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
         self._check(self.lib.arap_set_targets(self.h, len(x), _f64(x)))
@@ -342,10 +347,11 @@ class ArapServer:
 
     def __init__(self, device: int = 0, precision: str = "mixed", refine_steps: int = 1, max_in_flight: int = 0,
                  budget_bytes: int = 0, prep_threads: int = 0, max_batch: int = 0, max_queue: int = 0,
-                 poll_us: int = 0):
+                 poll_us: int = 0, solve_ctas: int = 0):
         self.lib = load()
         cfg = ServerConfig(int(device), PRECISION[precision], int(refine_steps), int(max_in_flight),
-                           int(budget_bytes), int(prep_threads), int(max_batch), int(max_queue), int(poll_us))
+                           int(budget_bytes), int(prep_threads), int(max_batch), int(max_queue), int(poll_us),
+                           int(solve_ctas))
         h = _P()
         rc = self.lib.arap_srv_create(C.byref(cfg), C.byref(h))
         if rc != ARAP_OK:

@@ -144,6 +144,7 @@ struct arap_ctx {
     int64_t g_setup_launches = 0, g_iter_launches = 0;
     int64_t gen = 1;  // bumped when the symbolic analysis or any device buffer changes
     bool use_graphs = true;
+    int solve_cap = 0;  // most CTAs per triangular-solve launch (0: as many as fit the device)
     // asynchronous deform (arap_deform_async / arap_wait)
     bool in_flight = false;    // a deform was enqueued and not waited for
     int *herr_host = nullptr;  // pinned copy of the device error word
@@ -359,6 +360,12 @@ int prepare_symbolic(arap_ctx *ctx) {
         ctx->smem_f64 = b64;
     }
     DevSym &d = ctx->ds;
+    {
+        const int res32 = solve_resident_ctas((int)b32, 4), res64 = solve_resident_ctas((int)b64, 8);
+        const int cap = ctx->solve_cap;
+        d.solve_grid32 = std::max(1, std::min(s.S, cap > 0 ? std::min(cap, res32) : res32));
+        d.solve_grid64 = std::max(1, std::min(s.S, cap > 0 ? std::min(cap, res64) : res64));
+    }
     d.V = s.V;
     d.m = s.m;
     d.S = s.S;
@@ -727,6 +734,7 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->precision = src->precision;
     ctx->refine = src->refine;
     ctx->use_graphs = src->use_graphs;
+    ctx->solve_cap = src->solve_cap;
     return finish_create(ctx, src->device, src, out);
 }
 
@@ -1116,6 +1124,20 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     const int rc = arap_deform_async(ctx, iterations, out_xyz);
     if (rc != ARAP_OK) return rc;
     return arap_wait(ctx);
+}
+
+int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas) {
+    if (check_ctx(ctx) || max_ctas < 0) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (max_ctas != ctx->solve_cap) {
+        ctx->solve_cap = max_ctas;
+        ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
+        ctx->dirty = true;
+    }
+    return ARAP_OK;
 }
 
 int arap_set_graphs(arap_ctx *ctx, int32_t enable) {

@@ -5,6 +5,7 @@
 #include "arap_kernels.h"
 #include "arap_device.cuh"
 
+#include <algorithm>
 #include <cstdio>
 #include <map>
 #include <mutex>
@@ -782,6 +783,21 @@ __device__ __forceinline__ int groups_for(int NQ) {
     return NQ >= kSolveThreads ? 1 : max(1, kSolveThreads / max(NQ, 1));
 }
 
+// Ticket of the calling CTA's next task (thread 0 only). A launch of G CTAs
+// over S tasks consumes exactly Z = S + G tickets: S tasks, then one ticket
+// per CTA that finds no task left and leaves the loop. Launch e (counted from
+// the last reset of the counter) owns tickets [e*Z, (e+1)*Z) and publishes
+// its flags with epoch e + 1. Once any wait of the context expired, every CTA
+// leaves at its next ticket. `reverse`: tasks in reverse `order`.
+__device__ __forceinline__ void next_task(unsigned long long *ticket, int S, int Z, const int32_t *order,
+                                          bool reverse, const int *err, int &task, unsigned &epoch) {
+    const unsigned long long t = atomicAdd(ticket, 1ull);
+    const int r = (int)(t % (unsigned long long)Z);
+    const bool stop = (*(volatile const int *)err & kErrTimeout) != 0;
+    task = (r < S && !stop) ? order[reverse ? S - 1 - r : r] : -1;
+    epoch = (unsigned)(t / (unsigned long long)Z) + 1u;
+}
+
 // Shared memory of a solve CTA (dynamic): two chunk buffers, three vectors
 // (two of max_ldx rows, one of max_ld21 rows) and the reduction scratch.
 struct SolveSmem {
@@ -794,7 +810,7 @@ struct SolveSmem {
 // only waits for CTAs that started before it.
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads, 3)
-k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
             const int32_t *__restrict__ child, const int32_t *__restrict__ relind, const T *__restrict__ Xall,
             const T *__restrict__ L21all, Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec,
             unsigned long long *ticket, unsigned *flags, int *err) {
@@ -810,15 +826,16 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     __shared__ unsigned s_epoch;
     const int tid = threadIdx.x;
     if (tid == 0) {
-        const unsigned long long t = atomicAdd(ticket, 1ull);
-        s_task = order[(int)(t % (unsigned long long)S)];
-        s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
+    for (;;) {
+    if (tid == 0) next_task(ticket, S, Z, order, false, err, s_task, s_epoch);
     __syncthreads();
     const int s = s_task;
+    if (s < 0) break;
     const unsigned epoch = s_epoch;
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
@@ -899,7 +916,7 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
     for (int k = 0; k < ntot; ++k) {
         T *buf = (k & 1) ? buf1 : buf0;
-        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        wait_chunk(&bars[k & 1], (ph[k & 1] + (unsigned)(k >> 1)) & 1u, err);
         int c0, cn, ld;
         const T *src;
         pl.chunk(k, c0, cn, src, ld);
@@ -924,6 +941,9 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     __threadfence();
     __syncthreads();
     if (tid == 0) st_release(flags + s, epoch);
+    ph[0] += (unsigned)(ntot + 1) / 2u;
+    ph[1] += (unsigned)ntot / 2u;
+    }
 }
 
 // Backward: for supernode s (root first), z = y - L21^T x(struct) and
@@ -932,7 +952,7 @@ k_solve_fwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
 // mode 1: pc64[k] += x_k, pc32[k] = float(pc64[k]).
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads, 3)
-k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+k_solve_bwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
             const int32_t *__restrict__ rows, const T *__restrict__ Xall, const T *__restrict__ L21Tall,
             Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode,
             unsigned long long *ticket, unsigned *flags, int *err) {
@@ -948,15 +968,16 @@ k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     __shared__ unsigned s_epoch;
     const int tid = threadIdx.x;
     if (tid == 0) {
-        const unsigned long long t = atomicAdd(ticket, 1ull);
-        s_task = order[S - 1 - (int)(t % (unsigned long long)S)];
-        s_epoch = (unsigned)(t / (unsigned long long)S) + 1u;
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
+    for (;;) {
+    if (tid == 0) next_task(ticket, S, Z, order, true, err, s_task, s_epoch);
     __syncthreads();
     const int s = s_task;
+    if (s < 0) break;
     const unsigned epoch = s_epoch;
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
@@ -988,7 +1009,7 @@ k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
     for (int k = 0; k < ntot; ++k) {
         T *buf = (k & 1) ? buf1 : buf0;
-        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        wait_chunk(&bars[k & 1], (ph[k & 1] + (unsigned)(k >> 1)) & 1u, err);
         int c0, cn, ld;
         const T *src;
         pl.chunk(k, c0, cn, src, ld);
@@ -1021,6 +1042,9 @@ k_solve_bwd(int S, SolveSmem lay, const int32_t *__restrict__ order, const SnInf
     __threadfence();
     __syncthreads();
     if (tid == 0) st_release(flags + s, epoch);
+    ph[0] += (unsigned)(ntot + 1) / 2u;
+    ph[1] += (unsigned)ntot / 2u;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1161,8 +1185,9 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
-    k_solve_fwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.level_sn, s.sn, s.child, s.relind, X, L21, sol,
-                                                     uvec, ticket, flags, err);
+    const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
+    k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(s.S, s.S + G, lay, s.level_sn, s.sn, s.child, s.relind, X, L21,
+                                                   sol, uvec, ticket, flags, err);
 }
 
 template <typename T>
@@ -1172,8 +1197,9 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
-    k_solve_bwd<T><<<s.S, kSolveThreads, smem, st>>>(s.S, lay, s.level_sn, s.sn, s.rows, X, L21T, sol, pc64, pc32,
-                                                     mode, ticket, flags, err);
+    const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
+    k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(s.S, s.S + G, lay, s.level_sn, s.sn, s.rows, X, L21T, sol, pc64,
+                                                   pc32, mode, ticket, flags, err);
 }
 
 void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st) {
@@ -1210,6 +1236,23 @@ cudaError_t configure_factor_smem(int max_ncol) {
     cudaError_t e = raise_smem_limit((const void *)k_fx<float>, (int)(rows * (NB + 1) * sizeof(float)));
     if (e != cudaSuccess) return e;
     return raise_smem_limit((const void *)k_fx<double>, (int)(rows * (NB + 1) * sizeof(double)));
+}
+
+// CTAs of the solve kernels that fit on the device at once for this dynamic
+// shared memory (precision T), at least 1.
+int solve_resident_ctas(int smem_bytes, int scalar_bytes) {
+    int dev = 0, sms = 0, a = 0, b = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        return 1;
+    if (scalar_bytes == 4) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_solve_fwd<float>, kSolveThreads, smem_bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_solve_bwd<float>, kSolveThreads, smem_bytes);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_solve_fwd<double>, kSolveThreads, smem_bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_solve_bwd<double>, kSolveThreads, smem_bytes);
+    }
+    return std::max(1, std::min(a, b) * sms);
 }
 
 // Raises the dynamic shared-memory limit of the solve kernels (bytes per CTA).

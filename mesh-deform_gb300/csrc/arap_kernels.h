@@ -37,6 +37,7 @@ struct DevTopo {
 struct DevSym {
     int V, m, S, nnz;
     int max_ldx, max_ld21, max_ncol;
+    int solve_grid32, solve_grid64;  // CTAs per solve launch (each loops over tickets)
     const int32_t *drow, *dcol, *dent, *oldidx;
     const int64_t *amap, *dmap;
     const SnInfo *sn;
@@ -95,6 +96,8 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 // one launch each, supernodes scheduled by a ticket counter with bounded waits.
 // mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k and pc32[k] = float(pc64[k]).
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
+// solve CTAs resident on the device at once (occupancy x SMs) for that shared memory
+int solve_resident_ctas(int smem_bytes, int scalar_bytes);
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
                       unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st);

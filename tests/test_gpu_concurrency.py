@@ -49,3 +49,21 @@ def test_graph_replay_matches_direct_launches(gpu, precision):
         replay = ctx.deform(5)         # replays them
     np.testing.assert_array_equal(direct, first)
     np.testing.assert_array_equal(direct, replay)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_cta_count_does_not_change_results(gpu, precision):
+    """The triangular solves give every supernode to whichever CTA takes its
+    ticket; one CTA, a few, or as many as fit compute the same numbers."""
+    w = W.cfg_twisted_bar(h=0.1, iterations=4)
+    outs = []
+    for n in (0, 1, 3, 64):
+        with make(gpu, w, precision) as ctx:
+            ctx.set_solve_ctas(n)
+            a = ctx.deform(4)
+            ctx.set_targets(w.ctargets + 0.05)   # re-pose: same launch shape, counters carry on
+            b = ctx.deform(4)
+            outs.append((a, b))
+    for a, b in outs[1:]:
+        np.testing.assert_array_equal(a, outs[0][0])
+        np.testing.assert_array_equal(b, outs[0][1])
