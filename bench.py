@@ -496,7 +496,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: skip the end-to-end pass")
     ap.add_argument("--poses", type=int, default=256, help="pose_batch: handle poses per step")
-    ap.add_argument("--solve-ctas", type=int, default=0, help="CTAs per triangular-solve launch (0: auto)")
+    ap.add_argument("--solve-ctas", type=int, default=-1,
+                    help="CTAs per triangular-solve launch (0: as many as fit; -1: autotuned for the concurrency)")
     ap.add_argument("--concurrent", type=int, default=os.cpu_count() or 1,
                     help="independent requests in flight per step (default: host threads, as the reference arm)")
     ap.add_argument("--serve-rates", default="50,100,200,0",
@@ -541,6 +542,18 @@ def main():
 
     w = workload(args)
     N = max(1, args.concurrent)
+    tuned = None
+    if args.solve_ctas < 0:
+        import arap_tune
+
+        if N > 1:
+            best, rates = arap_tune.tune_solve_ctas(w.positions, w.faces, w.cidx, w.ctargets, w.iterations,
+                                                    args.precision, args.refine, N, device=local)
+            tuned = {"solve_ctas": best, "iterations_per_s": {str(k): round(v, 1) for k, v in rates.items()}}
+            log(f"autotuned solve CTAs for {N} requests in flight: {best} {tuned['iterations_per_s']}")
+            args.solve_ctas = best
+        else:
+            args.solve_ctas = 0
     ctxs = []
     for _ in range(N):
         c = G.ArapContext(w.V, w.faces, device=local)
@@ -590,7 +603,11 @@ def main():
     barrier()
     clk = clocks.stop()
     step_ms = [max(t_start[k].elapsed_time(e) for e in t_end[k]) for k in range(args.steps)]
-    # per-request latency of a single request alone (p50/p99 over the steps)
+    # per-request latency of a single request alone (p50/p99 over the steps),
+    # with the launch shape a lone request prefers
+    if args.solve_ctas != 0:
+        ctxs[0].set_solve_ctas(0)
+        ctxs[0].deform(w.iterations, want_output=False)
     lat_single = []
     for k in range(args.steps):
         flush.zero_()
@@ -616,6 +633,8 @@ def main():
     kstats = c0.kernel_stats()
     kmodel = c0.kernel_model()
     c0.set_profiling(False)
+    if args.solve_ctas != 0:
+        c0.set_solve_ctas(args.solve_ctas)
     total_ms = sum(step_ms)
     if dist is not None:
         t = torch.tensor([total_ms], device="cuda")
@@ -693,7 +712,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": config_of(w, args, {"requests_per_step": N,
+        "config": config_of(w, args, {"requests_per_step": N, "solve_ctas": args.solve_ctas,
+                                      "solve_ctas_autotune": tuned,
                                       "step": f"{N} concurrent dirty deform requests (weights + factor + "
                                               f"{w.iterations} iterations each)"}),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

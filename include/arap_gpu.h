@@ -151,6 +151,14 @@ int arap_set_graphs(arap_ctx *ctx, int32_t enable);
    setConstraint). */
 int arap_set_targets(arap_ctx *ctx, int32_t n, const double *xyz);
 
+/* ARAP energy of the current positions, in FP64 on the device:
+   sum_i sum_j w_ij |(p'_i - p'_j) - R_i (p_i - p_j)|^2 over every adjacency
+   entry (cotan weights of arap.h:182-239, rest pose p, current positions p'),
+   with R_i the rotation the local step (arap.h:354-384) fits to vertex i's
+   one-ring for the current positions (not stored). The quantity the
+   local/global iteration decreases; the reference does not compute it. */
+int arap_energy(arap_ctx *ctx, double *energy);
+
 /* Device memory held by the context, in bytes. */
 int64_t arap_device_bytes(const arap_ctx *ctx);
 /* Device memory the context will hold after its next arap_deform

@@ -101,6 +101,7 @@ SIGNATURES = {
     "arap_wait": (C.c_int, [_P]),
     "arap_set_graphs": (C.c_int, [_P, _I32]),
     "arap_set_solve_ctas": (C.c_int, [_P, _I32]),
+    "arap_energy": (C.c_int, [_P, _dp]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
     "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
     "arap_query": (C.c_int, [_P, C.POINTER(C.c_int32)]),
@@ -241,6 +242,11 @@ class ArapContext:
 
     def set_graphs(self, enable: bool) -> None:
         self._check(self.lib.arap_set_graphs(self.h, 1 if enable else 0))
+
+    def energy(self) -> float:
+        e = C.c_double()
+        self._check(self.lib.arap_energy(self.h, C.byref(e)))
+        return e.value
 
     def set_solve_ctas(self, n: int):
         self._check(self.lib.arap_set_solve_ctas(self.h, int(n)))

@@ -1,0 +1,81 @@
+"""Launch-shape autotuner: picks the number of CTAs per triangular-solve
+launch (arap_set_solve_ctas) for a workload and a number of requests in
+flight, by timing short trial runs through the C ABI.
+
+One request alone is fastest with as many CTAs as fit on the device (the
+default, 0); several requests in flight share the SMs, and a smaller count
+per launch lets their solves run side by side instead of queueing behind
+each other's CTAs. The best count depends on the mesh, the precision and the
+concurrency, so it is measured rather than modelled. Results are cached per
+(device, mesh size, constrained count, precision, concurrency, iterations) in
+memory and, when a path is given, in a JSON file.
+"""
+from __future__ import annotations
+
+import json
+import time
+from pathlib import Path
+
+import numpy as np
+
+import arap_gpu as G
+
+CANDIDATES = (0, 64, 96, 128, 192, 256)
+_cache: dict = {}
+
+
+def _key(device: int, V: int, n_constrained: int, precision: str, concurrency: int, iterations: int) -> str:
+    return f"dev{device}:V{V}:c{n_constrained}:{precision}:x{concurrency}:it{iterations}"
+
+
+def tune_solve_ctas(positions, faces, cidx, ctargets, iterations: int, precision: str = "mixed",
+                    refine: int = 1, concurrency: int = 1, device: int = 0, candidates=CANDIDATES,
+                    trials: int = 2, cache_file: str | Path | None = None):
+    """Returns (best_count, {count: iterations/s}) for `concurrency` concurrent
+    dirty deforms of the given problem."""
+    key = _key(device, len(positions), len(cidx), precision, concurrency, iterations)
+    if cache_file and Path(cache_file).exists():
+        try:
+            _cache.update(json.loads(Path(cache_file).read_text()))
+        except Exception:
+            pass
+    if key in _cache:
+        hit = _cache[key]
+        return int(hit["best"]), {int(k): v for k, v in hit["rates"].items()}
+    faces = np.ascontiguousarray(faces, dtype=np.int32)
+    ctxs = []
+    for _ in range(max(1, concurrency)):
+        c = G.ArapContext(len(positions), faces, device=device)
+        c.set_precision(precision, refine)
+        c.set_rest_positions(positions)
+        c.set_constraints(cidx, ctargets)
+        ctxs.append(c)
+    rates = {}
+    try:
+        for n in candidates:
+            for c in ctxs:
+                c.set_solve_ctas(int(n))
+                c.deform(iterations, want_output=False)  # set-up and graph capture, untimed
+            best_dt = float("inf")
+            for _ in range(max(1, trials)):
+                t0 = time.perf_counter()
+                for c in ctxs:
+                    c.invalidate()
+                    rc = c.lib.arap_deform_async(c.h, iterations, None)
+                    if rc != G.ARAP_OK:
+                        raise G.ArapError(rc, c.lib.arap_last_error(c.h).decode())
+                for c in ctxs:
+                    c.wait()
+                best_dt = min(best_dt, time.perf_counter() - t0)
+            rates[int(n)] = len(ctxs) * iterations / best_dt
+    finally:
+        for c in ctxs:
+            c.close()
+    best = max(rates, key=rates.get)
+    _cache[key] = {"best": best, "rates": rates}
+    if cache_file:
+        try:
+            Path(cache_file).write_text(json.dumps(_cache, indent=1))
+        except Exception:
+            pass
+    return best, rates

@@ -132,7 +132,7 @@ struct arap_ctx {
     DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn, fitems;
     int factor_smem_ncol = 0;
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T, redge;
-    DevBuf errw, ticket, flags;
+    DevBuf errw, ticket, flags, energy;
     // many-pose state (arap_deform_poses)
     DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
     int bP = 0, bT = 0, bS = -1, bpt = 0;
@@ -168,7 +168,7 @@ struct arap_ctx {
         return {&faces, &ent_ptr, &ent_fc, &hc, &w_orig, &rest, &targets, &out, &drow, &dcol, &dent, &oldidx,
                 &amap, &dmap, &sn, &rows, &relind, &child, &level_sn, &fitems, &w64, &w32, &p64, &pc64, &p32,
                 &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
-                &errw, &ticket, &flags, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
+                &errw, &ticket, &flags, &energy, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
                 &bticket, &bflags};
     }
 };
@@ -1157,6 +1157,26 @@ int arap_get_positions(arap_ctx *ctx, double *out_xyz) {
     launch_gather_positions(ctx->ds, ctx->pc64.as<Vec4<double>>(), ctx->out.as<double>(), ctx->stream);
     CK(cudaMemcpyAsync(out_xyz, ctx->out.p, (size_t)3 * ctx->topo.V * sizeof(double), cudaMemcpyDeviceToHost,
                        ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ARAP_OK;
+}
+
+int arap_energy(arap_ctx *ctx, double *energy) {
+    if (check_ctx(ctx) || !energy) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (!ctx->sym_valid || ctx->state_prec < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no deformed state yet");
+    CK(cudaSetDevice(ctx->device));
+    // scratch: the partial sums, then the total
+    CK(ctx->energy.ensure(((size_t)energy_partials(ctx->ds.V) + 1) * sizeof(double)));
+    double *scratch = ctx->energy.as<double>();
+    const int np = energy_partials(ctx->ds.V);
+    launch_energy(ctx->ds, ctx->w64.as<double>(), ctx->p64.as<Vec4<double>>(), ctx->pc64.as<Vec4<double>>(), scratch,
+                  scratch + np, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(energy, scratch + np, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return ARAP_OK;
 }

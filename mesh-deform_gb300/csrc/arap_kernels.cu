@@ -1048,6 +1048,71 @@ k_solve_bwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
 }
 
 // ---------------------------------------------------------------------------
+// ARAP energy (FP64): per vertex the rotation the local step would fit to its
+// one-ring now, then sum over its entries of w |(p'_k - p'_l) - R_k (p_k - p_l)|^2.
+// One partial sum per block (warp shuffles, then the warps in order), summed
+// by k_sum_partials in a fixed order: the result does not depend on timing.
+
+constexpr int kEnergyThreads = 256;
+
+__global__ void __launch_bounds__(kEnergyThreads)
+k_energy(int V, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const double *__restrict__ w,
+         const Vec4<double> *__restrict__ p, const Vec4<double> *__restrict__ pc, double *__restrict__ partial) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double ev = 0.0;
+    if (i < V) {
+        const Vec4<double> pi = p[i], ci = pc[i];
+        double S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        const int e0 = drow[i], e1 = drow[i + 1];
+        for (int e = e0; e < e1; ++e) {
+            const int j = dcol[e];
+            const double wj = w[e];
+            const Vec4<double> pj = p[j], cj = pc[j];
+            const double ex = wj * (pi.x - pj.x), ey = wj * (pi.y - pj.y), ez = wj * (pi.z - pj.z);
+            const double fx = ci.x - cj.x, fy = ci.y - cj.y, fz = ci.z - cj.z;
+            S[0][0] += ex * fx; S[0][1] += ex * fy; S[0][2] += ex * fz;
+            S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
+            S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
+        }
+        double R[3][3];
+        rotation_from_cov(S, R);
+        for (int e = e0; e < e1; ++e) {
+            const int j = dcol[e];
+            const Vec4<double> pj = p[j], cj = pc[j];
+            const double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            const double rx = (ci.x - cj.x) - (R[0][0] * dx + R[0][1] * dy + R[0][2] * dz);
+            const double ry = (ci.y - cj.y) - (R[1][0] * dx + R[1][1] * dy + R[1][2] * dz);
+            const double rz = (ci.z - cj.z) - (R[2][0] * dx + R[2][1] * dy + R[2][2] * dz);
+            ev += w[e] * (rx * rx + ry * ry + rz * rz);
+        }
+    }
+    __shared__ double warp_sum[kEnergyThreads / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ev += __shfl_down_sync(0xffffffffu, ev, off);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = ev;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kEnergyThreads / 32; ++k) t += warp_sum[k];
+        partial[blockIdx.x] = t;
+    }
+}
+
+// out[0] = sum of n partial sums (one block; strided per-thread sums, then a
+// fixed tree)
+__global__ void __launch_bounds__(kEnergyThreads) k_sum_partials(int n, const double *__restrict__ partial,
+                                                                 double *__restrict__ out) {
+    __shared__ double buf[kEnergyThreads];
+    double t = 0.0;
+    for (int k = threadIdx.x; k < n; k += kEnergyThreads) t += partial[k];
+    buf[threadIdx.x] = t;
+    __syncthreads();
+    for (int h = kEnergyThreads / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) buf[threadIdx.x] += buf[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = buf[0];
+}
 
 __global__ void k_gather_positions(int V, const int32_t *__restrict__ oldidx, const Vec4<double> *__restrict__ pc64,
                                    double *__restrict__ out) {
@@ -1200,6 +1265,15 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
     k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(s.S, s.S + G, lay, s.level_sn, s.sn, s.rows, X, L21T, sol, pc64,
                                                    pc32, mode, ticket, flags, err);
+}
+
+int energy_partials(int V) { return std::max(1, blocks_for(V, kEnergyThreads)); }
+
+void launch_energy(const DevSym &s, const double *w64, const Vec4<double> *p64, const Vec4<double> *pc64,
+                   double *partial, double *out, cudaStream_t st) {
+    const int nb = energy_partials(s.V);
+    k_energy<<<nb, kEnergyThreads, 0, st>>>(s.V, s.drow, s.dcol, w64, p64, pc64, partial);
+    k_sum_partials<<<1, kEnergyThreads, 0, st>>>(nb, partial, out);
 }
 
 void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st) {

@@ -127,6 +127,12 @@ void launch_bsolve(const DevSym &s, int P, int pt, const float *X, const float *
                    unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st);
 void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *out, cudaStream_t st);
 
+// ARAP energy of the current positions in FP64 (best rotation per vertex for
+// its one-ring): energy_partials(V) doubles of scratch, the sum in out[0]
+int energy_partials(int V);
+void launch_energy(const DevSym &s, const double *w64, const Vec4<double> *p64, const Vec4<double> *pc64,
+                   double *partial, double *out, cudaStream_t st);
+
 // deformed positions back to the original vertex order as doubles (arap.h:133-135)
 void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st);
 template <typename T>

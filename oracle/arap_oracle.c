@@ -725,6 +725,44 @@ static void estimate_rotations(oracle_arap *oa) {
     }
 }
 
+/* ARAP energy of the current positions (not computed by the reference; the
+   quantity its local/global iteration decreases, Sorkine & Alexa 2007 eq. 3
+   with the cotan weights of arap.h:182-239): for every vertex the rotation
+   estimate_rotations would fit to its one-ring now, then
+   sum_i sum_j w_ij |(p'_i - p'_j) - R_i (p_i - p_j)|^2 over all adjacency
+   entries. Vertices in ascending order, entries in CSR order. */
+double oa_energy(const oracle_arap *oa) {
+    double total = 0.0;
+    for (int vi = 0; vi < oa->V; ++vi) {
+        const double *pi = oa->p + 3 * vi, *ppi = oa->pp + 3 * vi;
+        double cov[9] = {0}, R[9];
+        for (int q = oa->wrow[vi]; q < oa->wrow[vi + 1]; ++q) {
+            const int vj = oa->wcol[q];
+            const double wij = oa->wval[q];
+            const double *pj = oa->p + 3 * vj, *ppj = oa->pp + 3 * vj;
+            double e[3], f[3];
+            for (int c = 0; c < 3; ++c) { e[c] = pi[c] - pj[c]; f[c] = ppi[c] - ppj[c]; }
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) cov[3 * r + c] = cov[3 * r + c] + wij * e[r] * f[c];
+        }
+        oa_rotation_from_covariance(cov, R);
+        double ev = 0.0;
+        for (int q = oa->wrow[vi]; q < oa->wrow[vi + 1]; ++q) {
+            const int vj = oa->wcol[q];
+            const double *pj = oa->p + 3 * vj, *ppj = oa->pp + 3 * vj;
+            double d[3], r2 = 0.0;
+            for (int c = 0; c < 3; ++c) d[c] = pi[c] - pj[c];
+            for (int c = 0; c < 3; ++c) {
+                const double rc = (ppi[c] - ppj[c]) - (R[3 * c + 0] * d[0] + R[3 * c + 1] * d[1] + R[3 * c + 2] * d[2]);
+                r2 = r2 + rc * rc;
+            }
+            ev = ev + oa->wval[q] * r2;
+        }
+        total = total + ev;
+    }
+    return total;
+}
+
 /* estimatePositions, arap.h:393-430 */
 static void estimate_positions(oracle_arap *oa, double *work, double *rhs, double *u) {
     const int m = oa->nfree;

@@ -61,6 +61,8 @@ void oa_get_etree(const oracle_arap *oa, int *parent);
 int oa_num_blocks(const oracle_arap *oa);
 void oa_get_blocks(const oracle_arap *oa, int *block_ptr);
 long long oa_factor_nnz(const oracle_arap *oa);
+/* ARAP energy of the current positions with the best rotation per vertex. */
+double oa_energy(const oracle_arap *oa);
 
 /* Pure helpers. */
 void oa_rotation_from_covariance(const double *cov9, double *R9);

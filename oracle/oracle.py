@@ -66,6 +66,7 @@ def load():
         "oa_get_bfixed": (None, [P, dp]),
         "oa_get_ordering": (None, [P, ip]),
         "oa_get_etree": (None, [P, ip]),
+        "oa_energy": (C.c_double, [P]),
         "oa_num_blocks": (C.c_int, [P]),
         "oa_get_blocks": (None, [P, ip]),
         "oa_factor_nnz": (C.c_longlong, [P]),
@@ -166,6 +167,9 @@ class OracleARAP:
         out = np.zeros(max(m, 1), np.int32)
         self.lib.oa_get_ordering(self.h, _ip(out))
         return out[:m]
+
+    def energy(self) -> float:
+        return float(self.lib.oa_energy(self.h))
 
     def etree(self) -> np.ndarray:
         m = self.num_free()

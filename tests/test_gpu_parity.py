@@ -220,3 +220,29 @@ def test_golden_fixture_deforms(gpu, name, precision):
         ctx.set_constraints(d[f"{name}_cidx"], d[f"{name}_targets"])
         out = ctx.deform(int(d[f"{name}_iterations"]))
     assert W.bbox_rel_error(out, d[f"{name}_out"], v) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-5)])
+def test_energy_matches_oracle_and_decreases(gpu, precision, tol):
+    """K9: the FP64 ARAP energy of the GPU state equals the oracle's energy of
+    its own state (relative tolerance of the precision form) after every
+    iteration, and the iteration does not increase it."""
+    from oracle import oracle as O
+
+    w = W.cfg_icosphere_l4(level=3, iterations=1)
+    o = O.OracleARAP(w.positions, w.faces)
+    o.set_constraints(w.cidx, w.ctargets)
+    ctx = gpu.ArapContext(w.V, w.faces)
+    ctx.set_precision(precision, 1)
+    ctx.set_rest_positions(w.positions)
+    ctx.set_constraints(w.cidx, w.ctargets)
+    prev = None
+    for k in range(6):
+        ctx.deform(1)
+        o.deform(1)
+        eg, eo = ctx.energy(), o.energy()
+        assert abs(eg - eo) <= tol * eo, (k, eg, eo)
+        if prev is not None and precision == "fp64":
+            assert eg <= prev * (1 + 1e-12)
+        prev = eg
+    ctx.close()
