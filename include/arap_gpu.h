@@ -111,6 +111,19 @@ int arap_deform(arap_ctx *ctx, int32_t iterations, double *out_xyz);
 int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
                       double *out_xyz);
 
+/* DeformationUtil::updateConstraints (inc/deform/deformation_util.h:48-57) for
+   n_poses rigid poses at once, computed on the device into the targets
+   arap_deform_poses(ctx, n_poses, NULL, ...) then uses. For pose p and
+   constrained vertex v (ascending order): a handle (listed in handles, which
+   must all be constrained) goes to tabs_p * rest(v) with
+   tabs_p = origin * transforms[p] * origin^-1 (the inverse taken as an
+   isometry's, as Transform::inverse(Eigen::Isometry)); any other constrained
+   vertex keeps its arap_set_constraints target. origin and each transform are
+   row-major 3x4 affine matrices (12 doubles; origin NULL: identity). Uploads
+   12 doubles per pose instead of 3 per constrained vertex and pose. */
+int arap_pose_targets(arap_ctx *ctx, int32_t n_handles, const int32_t *handles, const double *origin,
+                      int32_t n_poses, const double *transforms);
+
 /* arap_deform split in two: arap_deform_async enqueues the whole deform on
    the context's stream and returns at once (out_xyz must stay valid, and is
    best pinned, until arap_wait returns); arap_wait waits for it and returns

@@ -102,6 +102,7 @@ SIGNATURES = {
     "arap_set_graphs": (C.c_int, [_P, _I32]),
     "arap_set_solve_ctas": (C.c_int, [_P, _I32]),
     "arap_energy": (C.c_int, [_P, _dp]),
+    "arap_pose_targets": (C.c_int, [_P, _I32, _ip, _dp, _I32, _dp]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
     "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
     "arap_query": (C.c_int, [_P, C.POINTER(C.c_int32)]),
@@ -229,8 +230,10 @@ class ArapContext:
                                          _f64(out) if out is not None else None)
 
     def deform_poses(self, targets, iterations: int) -> np.ndarray:
-        t = np.ascontiguousarray(targets, dtype=np.float64)
-        out = np.empty((t.shape[0], self.V, 3), np.float64)
+        """targets None: the ones already on the device (the previous call's,
+        or arap_pose_targets')."""
+        t = None if targets is None else np.ascontiguousarray(targets, dtype=np.float64)
+        out = np.empty((self._nposes if t is None else t.shape[0], self.V, 3), np.float64)
         self._check(self.deform_poses_rc(t, iterations, out))
         return out
 
@@ -242,6 +245,16 @@ class ArapContext:
 
     def set_graphs(self, enable: bool) -> None:
         self._check(self.lib.arap_set_graphs(self.h, 1 if enable else 0))
+
+    def pose_targets(self, handles, transforms, origin=None):
+        """Targets of len(transforms) rigid poses computed on the device
+        (arap_pose_targets); the next deform_poses(None, ...) uses them."""
+        h = np.ascontiguousarray(handles, dtype=np.int32).reshape(-1)
+        t = np.ascontiguousarray(transforms, dtype=np.float64).reshape(-1, 12)
+        o = None if origin is None else np.ascontiguousarray(origin, dtype=np.float64).reshape(12)
+        self._check(self.lib.arap_pose_targets(self.h, len(h), _i32(h), _f64(o) if o is not None else None,
+                                               len(t), _f64(t)))
+        self._nposes = len(t)
 
     def energy(self) -> float:
         e = C.c_double()

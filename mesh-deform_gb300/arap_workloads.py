@@ -241,6 +241,7 @@ def cfg_pose_batch(level: int = 5, n_poses: int = 256, seed: int = 20261203,
     hm = np.isin(cidx, handles)
     origin = v[handles].mean(0)
     poses = np.empty((n_poses, len(cidx), 3))
+    transforms = np.zeros((n_poses, 3, 4))
     for p in range(n_poses):
         axis = rng.normal(size=3)
         ang = rng.uniform(0.0, np.pi / 3)
@@ -249,9 +250,16 @@ def cfg_pose_batch(level: int = 5, n_poses: int = 256, seed: int = 20261203,
         tg = v[cidx].copy()
         tg[hm] = (tg[hm] - origin) @ R.T + origin + t
         poses[p] = tg
+        transforms[p, :, :3] = R
+        transforms[p, :, 3] = t
+    # the same poses as DeformationUtil inputs: tabs = O * [R|t] * O^-1 with O = [I|origin]
+    O = np.zeros((3, 4))
+    O[:, :3] = np.eye(3)
+    O[:, 3] = origin
     return Workload(f"pose_batch_l{level}x{n_poses}", v, f, cidx, poses[0].copy(), iterations,
                     precision, poses=poses,
-                    info={"seed": seed, "anchors": int(len(anchors)), "handles": int(len(handles))})
+                    info={"seed": seed, "anchors": int(len(anchors)), "handles": int(len(handles)),
+                          "handle_ids": handles.astype(np.int32), "transforms": transforms, "origin": O})
 
 
 @dataclass

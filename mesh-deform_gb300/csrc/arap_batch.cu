@@ -510,6 +510,38 @@ cudaError_t configure_batch_smem(int max_ldx, int max_ld21, int pt) {
     }
 }
 
+// DeformationUtil::updateConstraints (inc/deform/deformation_util.h:48-57) for
+// P poses at once: constrained vertex i of pose p (ascending vertex order) is
+// tabs_p * rest(v) for a handle, its arap_set_constraints target otherwise.
+// tabs_p = origin * t_p * origin^-1 as a row-major 3x4 affine matrix.
+__global__ void k_pose_targets(int P, int nc, const int32_t *__restrict__ cidx, const uint8_t *__restrict__ handle,
+                               const double *__restrict__ rest, const double *__restrict__ ctgt,
+                               const double *__restrict__ tabs, double *__restrict__ out) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (int64_t)P * nc) return;
+    const int p = (int)(q / nc), i = (int)(q % nc);
+    double *o = out + 3 * q;
+    if (!handle[i]) {
+        o[0] = ctgt[3 * i];
+        o[1] = ctgt[3 * i + 1];
+        o[2] = ctgt[3 * i + 2];
+        return;
+    }
+    const double *x = rest + 3 * (int64_t)cidx[i];
+    const double *M = tabs + 12 * (int64_t)p;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        o[r] = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(M[4 * r], x[0]), __dmul_rn(M[4 * r + 1], x[1])),
+                                   __dmul_rn(M[4 * r + 2], x[2])),
+                         M[4 * r + 3]);
+}
+
+void launch_pose_targets(int P, int nc, const int32_t *cidx, const uint8_t *handle, const double *rest,
+                         const double *ctgt, const double *tabs, double *out, cudaStream_t st) {
+    const int64_t n = (int64_t)P * nc;
+    if (n) k_pose_targets<<<nblocks(n, 256), 256, 0, st>>>(P, nc, cidx, handle, rest, ctgt, tabs, out);
+}
+
 void launch_bsetup(const DevSym &s, int P, const Vec4<double> *p64, const double *targets, Vec4<double> *pc64,
                    Vec4<float> *pc32, Vec4<float> *R, cudaStream_t st) {
     const int64_t n = (int64_t)s.V * P;

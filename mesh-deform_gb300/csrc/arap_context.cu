@@ -133,9 +133,11 @@ struct arap_ctx {
     int factor_smem_ncol = 0;
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T, redge;
     DevBuf errw, ticket, flags, energy;
+    DevBuf cidx_dev, handle_dev, tabs_dev;  // arap_pose_targets inputs
     // many-pose state (arap_deform_poses)
     DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
     int bP = 0, bT = 0, bS = -1, bpt = 0;
+    int tP = -1;  // poses whose targets arap_pose_targets left in btargets (-1: none)
     int model_P = 1, model_T = 1;  // poses / pose tiles of the last deform (cost model)
     // CUDA graphs of the setup and of the iteration sequence; replayed while
     // nothing they reference changes (direct launches when profiling)
@@ -168,7 +170,7 @@ struct arap_ctx {
         return {&faces, &ent_ptr, &ent_fc, &hc, &w_orig, &rest, &targets, &out, &drow, &dcol, &dent, &oldidx,
                 &amap, &dmap, &sn, &rows, &relind, &child, &level_sn, &fitems, &w64, &w32, &p64, &pc64, &p32,
                 &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
-                &errw, &ticket, &flags, &energy, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
+                &errw, &ticket, &flags, &energy, &cidx_dev, &handle_dev, &tabs_dev, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
                 &bticket, &bflags};
     }
 };
@@ -783,6 +785,7 @@ int arap_set_rest_positions(arap_ctx *ctx, const double *xyz) {
                            ctx->stream));
     ctx->have_rest = true;
     ctx->dirty = true;
+    ctx->tP = -1;
     return ARAP_OK;
 }
 
@@ -817,6 +820,7 @@ int arap_set_constraints(arap_ctx *ctx, int32_t n, const int32_t *indices, const
                            cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));  // the host vector may change on the next call
     ctx->dirty = true;
+    ctx->tP = -1;
     return ARAP_OK;
 }
 
@@ -893,9 +897,13 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
     } else if (!targets && !ctx->btargets.p) {
         return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no targets uploaded yet");
     }
-    if (targets)
+    if (!targets && ctx->tP >= 0 && ctx->tP != P)
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "arap_pose_targets computed targets for another pose count");
+    if (targets) {
         CK(cudaMemcpyAsync(ctx->btargets.p, targets, (size_t)P * nc * 3 * sizeof(double), cudaMemcpyHostToDevice,
                            st));
+        ctx->tP = -1;
+    }
     {
         Prof pr(ctx, ARAP_K_ASSEMBLE);
         launch_bsetup(d, P, ctx->p64.as<Vec4<double>>(), ctx->btargets.as<double>(), ctx->bpc64.as<Vec4<double>>(),
@@ -969,6 +977,67 @@ int arap_deform_poses(arap_ctx *ctx, int32_t n_poses, const double *targets, int
     const int rc = arap_deform_poses_async(ctx, n_poses, targets, iterations, out_xyz);
     if (rc != ARAP_OK) return rc;
     return arap_wait(ctx);
+}
+
+namespace {
+// a = b * c for row-major 3x4 affine matrices (implicit last row 0 0 0 1)
+void affine_mul(const double *b, const double *c, double *a) {
+    for (int r = 0; r < 3; ++r) {
+        for (int k = 0; k < 4; ++k) {
+            double v = b[4 * r] * c[k] + b[4 * r + 1] * c[4 + k] + b[4 * r + 2] * c[8 + k];
+            if (k == 3) v += b[4 * r + 3];
+            a[4 * r + k] = v;
+        }
+    }
+}
+}  // namespace
+
+int arap_pose_targets(arap_ctx *ctx, int32_t n_handles, const int32_t *handles, const double *origin,
+                      int32_t n_poses, const double *transforms) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (n_poses <= 0 || n_handles < 0 || !transforms || (n_handles > 0 && !handles))
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "invalid pose arrays");
+    if (!ctx->have_rest) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "rest positions not set");
+    const int nc = (int)ctx->cidx.size();
+    if (nc == 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no constrained vertex");
+    std::vector<uint8_t> is_handle(nc, 0);
+    for (int h = 0; h < n_handles; ++h) {
+        const auto it = std::lower_bound(ctx->cidx.begin(), ctx->cidx.end(), handles[h]);
+        if (it == ctx->cidx.end() || *it != handles[h])
+            return fail(ctx, ARAP_ERR_BAD_INDEX,
+                        "handle " + std::to_string(handles[h]) + " is not a constrained vertex");
+        is_handle[it - ctx->cidx.begin()] = 1;
+    }
+    // tabs = origin * t * origin^-1, the inverse taken as an isometry's
+    // ([R^T | -R^T x]), as Transform::inverse(Eigen::Isometry) does
+    static const double identity[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    const double *O = origin ? origin : identity;
+    double Oinv[12];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) Oinv[4 * r + c] = O[4 * c + r];
+        Oinv[4 * r + 3] = -(O[r] * O[3] + O[4 + r] * O[7] + O[8 + r] * O[11]);
+    }
+    std::vector<double> tabs((size_t)12 * n_poses);
+    for (int p = 0; p < n_poses; ++p) {
+        double tmp[12];
+        affine_mul(O, transforms + 12 * (size_t)p, tmp);
+        affine_mul(tmp, Oinv, tabs.data() + 12 * (size_t)p);
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    CK(upload(ctx->cidx_dev, ctx->cidx, st));
+    CK(upload(ctx->handle_dev, is_handle, st));
+    CK(upload(ctx->tabs_dev, tabs, st));
+    CK(ctx->btargets.ensure((size_t)n_poses * nc * 3 * sizeof(double)));
+    launch_pose_targets(n_poses, nc, ctx->cidx_dev.as<int32_t>(), ctx->handle_dev.as<uint8_t>(), ctx->rest.as<double>(),
+                        ctx->targets.as<double>(), ctx->tabs_dev.as<double>(), ctx->btargets.as<double>(), st);
+    CK(cudaGetLastError());
+    ctx->tP = n_poses;
+    return ARAP_OK;
 }
 
 int arap_set_targets(arap_ctx *ctx, int32_t n, const double *xyz) {

@@ -126,6 +126,9 @@ void launch_bsolve(const DevSym &s, int P, int pt, const float *X, const float *
                    Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
                    unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st);
 void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *out, cudaStream_t st);
+// handle targets of P rigid poses (P x nc x 3, ascending constrained order)
+void launch_pose_targets(int P, int nc, const int32_t *cidx, const uint8_t *handle, const double *rest,
+                         const double *ctgt, const double *tabs, double *out, cudaStream_t st);
 
 // ARAP energy of the current positions in FP64 (best rotation per vertex for
 // its one-ring): energy_partials(V) doubles of scratch, the sum in out[0]

@@ -56,3 +56,32 @@ def test_pose_batch_rejects_fp64(gpu):
         with pytest.raises(gpu.ArapError) as e:
             ctx.deform_poses(w.poses, 2)
         assert e.value.code == gpu.ARAP_ERR_UNSUPPORTED
+
+
+def test_pose_targets_on_device_match_host_targets(gpu):
+    """arap_pose_targets (DeformationUtil::updateConstraints for many rigid
+    poses, inc/deform/deformation_util.h:48-57) gives the targets the host
+    computes, and the poses deformed from them."""
+    w = W.cfg_pose_batch(level=3, n_poses=12, iterations=5)
+    ctx = gpu.ArapContext(w.V, w.faces)
+    ctx.set_precision("mixed", 1)
+    ctx.set_rest_positions(w.positions)
+    ctx.set_constraints(w.cidx, w.poses[0] * 0 + w.positions[w.cidx])
+    host = ctx.deform_poses(w.poses, w.iterations)
+    ctx.pose_targets(w.info["handle_ids"], w.info["transforms"], w.info["origin"])
+    dev = ctx.deform_poses(None, w.iterations)
+    ctx.close()
+    for p in range(len(w.poses)):
+        assert W.bbox_rel_error(dev[p], host[p], w.positions) <= 1e-12
+
+
+def test_pose_targets_rejects_unconstrained_handle(gpu):
+    w = W.cfg_pose_batch(level=2, n_poses=2, iterations=2)
+    free = np.setdiff1d(np.arange(w.V), w.cidx)[0]
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.poses[0])
+        with pytest.raises(gpu.ArapError) as e:
+            ctx.pose_targets([int(free)], w.info["transforms"], w.info["origin"])
+        assert e.value.code == gpu.ARAP_ERR_BAD_INDEX
