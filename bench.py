@@ -255,19 +255,29 @@ def run_batch(args):
     its_total = P * w.iterations * args.steps * world
     value = its_total / (total_ms / 1e3)
     tg_h = torch.from_numpy(np.ascontiguousarray(w.poses)).pin_memory().numpy()
+    tf_h = torch.from_numpy(np.ascontiguousarray(w.info["transforms"].reshape(P, 12))).pin_memory().numpy()
+    handles = w.info["handle_ids"]
     out_h = torch.empty((P, w.V, 3), dtype=torch.float64).pin_memory().numpy()
-    e2e_s = []
+    # e2e: each step maps the P rigid poses to handle targets on the device
+    # (arap_pose_targets, DeformationUtil::updateConstraints) and deforms them;
+    # e2e_explicit_targets uploads the P x n_constrained x 3 targets instead
+    e2e_s, e2e_x = [], []
     for k in range(0 if args.skip_e2e else args.warmup + args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.invalidate()
-        rc = ctx.deform_poses_rc(tg_h, w.iterations, out_h)
-        t1 = time.perf_counter()
-        if rc != G.ARAP_OK:
-            raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
-        if k >= args.warmup:
-            e2e_s.append(t1 - t0)
+        for mode in ("rigid", "explicit"):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.invalidate()
+            if mode == "rigid":
+                ctx.pose_targets(handles, tf_h, w.info["origin"])
+                rc = ctx.deform_poses_rc(None, w.iterations, out_h)
+            else:
+                rc = ctx.deform_poses_rc(tg_h, w.iterations, out_h)
+            t1 = time.perf_counter()
+            if rc != G.ARAP_OK:
+                raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+            if k >= args.warmup:
+                (e2e_s if mode == "rigid" else e2e_x).append(t1 - t0)
     e2e_total = sum(e2e_s) if e2e_s else float("nan")
     if dist is not None and e2e_s:
         t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
@@ -313,7 +323,10 @@ def run_batch(args):
         "config": config_of(w, args, {"poses": P, "step": f"dirty deform of {P} poses (one shared factor)",
                                       "precision": "mixed"}),
         "e2e": {"value": its_total / e2e_total if e2e_s else None, "unit": UNIT,
-                "h2d_bytes_per_step": int(tg_h.nbytes), "d2h_bytes_per_step": int(out_h.nbytes)},
+                "h2d_bytes_per_step": int(tf_h.nbytes + handles.nbytes + 96), "d2h_bytes_per_step": int(out_h.nbytes),
+                "inputs": "P rigid transforms, targets mapped on the device"},
+        "e2e_explicit_targets": {"value": its_total / sum(e2e_x) if e2e_x else None, "unit": UNIT,
+                                 "h2d_bytes_per_step": int(tg_h.nbytes), "d2h_bytes_per_step": int(out_h.nbytes)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": None, "bytes_per_launch": dom_bytes,
