@@ -709,13 +709,20 @@ def main():
     # ---- CPU baseline (oracle, one core) + error of the GPU result ----
     cpu = None
     err = None
-    if rank == 0 and not args.no_cpu_baseline and e2e_s:
+    if rank == 0 and not args.no_cpu_baseline:
         dt, ref = cpu_oracle_requests(w, args.cpu_requests, 1)
+        from oracle import oracle as O
+
+        t0 = time.perf_counter()
+        O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, 0)  # set-up alone: weights + factor
+        setup_s = time.perf_counter() - t0
+        per_req = dt / args.cpu_requests
         cpu = {"value": args.cpu_requests * w.iterations / dt, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"{args.cpu_requests} dirty deform({w.iterations}) requests of {w.name} on one thread "
-                         f"({dt:.1f} s)"}
-        err = max(W.bbox_rel_error(o, ref, w.positions) for o in outs_h)
+                         f"({dt:.1f} s)",
+               "setup_ms": 1e3 * setup_s, "ms_per_iteration": 1e3 * max(per_req - setup_s, 0.0) / w.iterations}
         err_first = W.bbox_rel_error(first, ref, w.positions)
+        err = max([W.bbox_rel_error(o, ref, w.positions) for o in outs_h] if e2e_s else [err_first])
         log(f"error vs FP64 oracle: {err:.3e} (first deform {err_first:.3e})")
 
     setup_ms, iter_ms = c0.timing()

@@ -1453,12 +1453,18 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
             (xlow + l21) * sz;
         FL = s.factor_flops;
         break;
-    case ARAP_K_LOCAL:  // rest + current positions, rotations out, adjacency + weights
-        B = V * 3 * sz + P * V * (3 * sz + 9 * sz) + 4 * (V + 1) + nnz * (4 + sz);
+    case ARAP_K_LOCAL:
+        if (sz == 8.0)  // rest + current positions, rotations out, adjacency + weights
+            B = V * 3 * sz + P * V * (3 * sz + 9 * sz) + 4 * (V + 1) + nnz * (4 + sz);
+        else  // FP32 rest edges + weights per entry; FP64 current positions, FP32 rotations per vertex and pose
+            B = nnz * (4 + 4 + 12) + 4 * (V + 1) + P * V * (24 + 36);
         FL = P * (nnz * 24 + V * 600);
         break;
     case ARAP_K_RHS:
-        B = m * 3 * sz + P * m * (9 * sz + 3 * sz + 3 * sz) + 4 * (m + 1) + nnz * (4 + sz);
+        if (sz == 8.0)
+            B = m * 3 * sz + P * m * (9 * sz + 3 * sz + 3 * sz) + 4 * (m + 1) + nnz * (4 + sz);
+        else  // rest edges + weights per entry; rotations of every vertex, b of the free ones, per pose
+            B = nnz * (4 + 4 + 12) + 4 * (m + 1) + P * (V * 36 + m * 12);
         FL = P * nnz * 24;
         break;
     case ARAP_K_RESIDUAL:

@@ -658,8 +658,11 @@ k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ 
 // Threads own 4-row quads of the result; G groups of threads split each
 // chunk's columns and are reduced once at the end of a matrix.
 
+#ifndef ARAP_SOLVE_CHUNK_KB
+#define ARAP_SOLVE_CHUNK_KB 16
+#endif
 constexpr int kSolveThreads = 256;
-constexpr int kChunkBytes = 16 * 1024;
+constexpr int kChunkBytes = ARAP_SOLVE_CHUNK_KB * 1024;  // bytes per TMA chunk buffer (two buffers)
 constexpr int kRedRows = 4 * kSolveThreads;  // G * 4 * NQ <= 4 * threads
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
