@@ -148,6 +148,16 @@ int arap_query(arap_ctx *ctx, int32_t *done);
    next deform (which sets the problem up again). */
 int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas);
 
+/* The triangular solves take the top levels of the elimination tree (large
+   fronts, one or a few supernodes per level) with clusters of 8 CTAs that
+   split each supernode's matrices, and the levels below with one CTA per
+   supernode. A level goes to the clusters when one of its supernodes holds at
+   least `bytes` of X = inv(L11) and L21 (as FP32) and every level above it does
+   too. 0 (the default): 64 KiB; negative: no cluster levels. The split changes
+   only the order of some sums. Takes effect at the next deform (which sets the
+   problem up again). */
+int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes);
+
 /* enable != 0 (the default) runs the setup and the iteration sequence as CUDA
    graphs captured on first use and replayed while the problem's size,
    precision and iteration count stay the same; 0 launches every kernel

@@ -102,6 +102,7 @@ SIGNATURES = {
     "arap_set_graphs": (C.c_int, [_P, _I32]),
     "arap_set_solve_ctas": (C.c_int, [_P, _I32]),
     "arap_energy": (C.c_int, [_P, _dp]),
+    "arap_set_cluster_threshold": (C.c_int, [_P, _I32]),
     "arap_pose_targets": (C.c_int, [_P, _I32, _ip, _dp, _I32, _dp]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
     "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
@@ -260,6 +261,9 @@ class ArapContext:
         e = C.c_double()
         self._check(self.lib.arap_energy(self.h, C.byref(e)))
         return e.value
+
+    def set_cluster_threshold(self, nbytes: int):
+        self._check(self.lib.arap_set_cluster_threshold(self.h, int(nbytes)))
 
     def set_solve_ctas(self, n: int):
         self._check(self.lib.arap_set_solve_ctas(self.h, int(n)))

@@ -123,6 +123,7 @@ struct arap_ctx {
     bool sym_host = false;   // analysed (host only)
     Symbolic sym;
     size_t smem_f32 = 0, smem_f64 = 0;  // dynamic shared memory the solve kernels are configured for
+    size_t top_smem_f32 = 0, top_smem_f64 = 0;
     // which precision the iteration state was set up for
     int state_prec = -1;
     bool have_rotations = false;
@@ -147,6 +148,7 @@ struct arap_ctx {
     int64_t gen = 1;  // bumped when the symbolic analysis or any device buffer changes
     bool use_graphs = true;
     int solve_cap = 0;  // most CTAs per triangular-solve launch (0: as many as fit the device)
+    int top_bytes = 0;  // supernode size from which tree levels go to the cluster solves (0: default, <0: never)
     // asynchronous deform (arap_deform_async / arap_wait)
     bool in_flight = false;    // a deform was enqueued and not waited for
     int *herr_host = nullptr;  // pinned copy of the device error word
@@ -274,7 +276,7 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     add(ctx->child, s.child.size() * 4);
     add(ctx->level_sn, s.level_sn.size() * 4);
     add(ctx->fitems, s.fitems.size() * sizeof(FItem));
-    add(ctx->ticket, 2 * sizeof(unsigned long long));
+    add(ctx->ticket, 4 * sizeof(unsigned long long));
     add(ctx->flags, 2 * sizeof(unsigned) * S1);
     // iteration state and factor (setup_alloc)
     const bool f32 = sizeof(T) == 4;
@@ -341,9 +343,10 @@ int prepare_symbolic(arap_ctx *ctx) {
         ctx->factor_smem_ncol = s.max_ncol;
     }
     // solve scheduling state: ticket counters and per-supernode flags start at 0
-    CK(ctx->ticket.ensure(2 * sizeof(unsigned long long)));
+    // counters: forward / backward of the lower levels, then of the top levels
+    CK(ctx->ticket.ensure(4 * sizeof(unsigned long long)));
     CK(ctx->flags.ensure(2 * sizeof(unsigned) * (size_t)std::max(s.S, 1)));
-    CK(cudaMemsetAsync(ctx->ticket.p, 0, 2 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(ctx->ticket.p, 0, 4 * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
     // the solve kernels give each thread one 4-row quad of a front (at most
     // 1024 rows) and stream whole columns through 16 KB chunks
@@ -363,10 +366,37 @@ int prepare_symbolic(arap_ctx *ctx) {
     }
     DevSym &d = ctx->ds;
     {
+        // split of the tree between the single-CTA and the cluster solves
+        const int nlev = (int)s.level_ptr.size() - 1;
+        std::vector<char> big(std::max(nlev, 1), 0);
+        for (const SnInfo &q : s.sn) {
+            const int64_t bytes = ((int64_t)q.ldx * q.ncol + (int64_t)q.ld21 * q.ncol) * 4;
+            const int64_t thr = ctx->top_bytes == 0 ? kTopTaskBytes : ctx->top_bytes;
+            if (ctx->top_bytes >= 0 && bytes >= thr) big[q.level] = 1;
+        }
+        int ltop = nlev;
+        while (ltop > 0 && big[ltop - 1]) --ltop;
+        d.ltop = ltop;
+        d.s_low = nlev > 0 ? s.level_ptr[ltop] : 0;
+        d.s_top = s.S - d.s_low;
+        int width = 0;
+        for (int l = ltop; l < nlev; ++l) width = std::max(width, s.level_ptr[l + 1] - s.level_ptr[l]);
+        d.top_clusters = std::max(1, std::min(width, kTopMaxClusters));
         const int res32 = solve_resident_ctas((int)b32, 4), res64 = solve_resident_ctas((int)b64, 8);
         const int cap = ctx->solve_cap;
-        d.solve_grid32 = std::max(1, std::min(s.S, cap > 0 ? std::min(cap, res32) : res32));
-        d.solve_grid64 = std::max(1, std::min(s.S, cap > 0 ? std::min(cap, res64) : res64));
+        const int nl = std::max(d.s_low, 1);
+        d.solve_grid32 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res32) : res32));
+        d.solve_grid64 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res64) : res64));
+        if (d.s_top > 0) {
+            const size_t t32 = top_smem_bytes(s.max_ldx, s.max_ld21, 4), t64 = top_smem_bytes(s.max_ldx, s.max_ld21, 8);
+            if (t64 > 227 * 1024)
+                return fail(ctx, ARAP_ERR_UNSUPPORTED, "top supernode fronts exceed the cluster solve's shared memory");
+            if (t32 > ctx->top_smem_f32 || t64 > ctx->top_smem_f64) {
+                CK(configure_top_smem((int)t32, (int)t64));
+                ctx->top_smem_f32 = t32;
+                ctx->top_smem_f64 = t64;
+            }
+        }
     }
     d.V = s.V;
     d.m = s.m;
@@ -515,6 +545,9 @@ int graph_or_direct(arap_ctx *ctx, cudaGraphExec_t &exec, int64_t key_store[4], 
 template <typename T>
 int run_iterations(arap_ctx *ctx, int iterations);
 
+// kernels of one forward + backward sweep (lower levels and cluster levels)
+int solve_launches(const DevSym &d) { return 2 * ((d.s_low > 0) + (d.s_top > 0)); }
+
 template <>
 int run_iterations<double>(arap_ctx *ctx, int iterations) {
     const Symbolic &s = ctx->sym;
@@ -547,7 +580,7 @@ int run_iterations<double>(arap_ctx *ctx, int iterations) {
                                      ctx->sol.as<Vec4<double>>(), ctx->pc64.as<Vec4<double>>(), nullptr, 0, tk + 1,
                                      fl + s.S, ctx->errw.as<int>(), st);
         }
-        ctx->launches += 3;
+        ctx->launches += solve_launches(d) + 1;
     }
     CK(cudaGetLastError());
     return ARAP_OK;
@@ -592,7 +625,7 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
                                         ctx->sol.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(),
                                         ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(), st);
             }
-            ctx->launches += 3;
+            ctx->launches += solve_launches(d) + 1;
         }
     }
     CK(cudaGetLastError());
@@ -737,6 +770,7 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->refine = src->refine;
     ctx->use_graphs = src->use_graphs;
     ctx->solve_cap = src->solve_cap;
+    ctx->top_bytes = src->top_bytes;
     return finish_create(ctx, src->device, src, out);
 }
 
@@ -1203,6 +1237,20 @@ int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas) {
     }
     if (max_ctas != ctx->solve_cap) {
         ctx->solve_cap = max_ctas;
+        ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
+        ctx->dirty = true;
+    }
+    return ARAP_OK;
+}
+
+int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (bytes != ctx->top_bytes) {
+        ctx->top_bytes = bytes;
         ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
         ctx->dirty = true;
     }

@@ -5,6 +5,8 @@
 #include "arap_kernels.h"
 #include "arap_device.cuh"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <map>
@@ -955,7 +957,7 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
 // mode 1: pc64[k] += x_k, pc32[k] = float(pc64[k]).
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads, 3)
-k_solve_bwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
             const int32_t *__restrict__ rows, const T *__restrict__ Xall, const T *__restrict__ L21Tall,
             Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode,
             unsigned long long *ticket, unsigned *flags, int *err) {
@@ -1000,7 +1002,8 @@ k_solve_bwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     int myrow[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) myrow[u] = (tid + u * kSolveThreads < nb) ? rs[tid + u * kSolveThreads] : 0;
-    if (tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
+    // a parent in the top levels was finished by the launch before this one
+    if (tid == 0 && d.parent >= 0 && sn[d.parent].level < ltop) wait_flag(flags + d.parent, epoch, err);
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < 4; ++u)
@@ -1047,6 +1050,301 @@ k_solve_bwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     if (tid == 0) st_release(flags + s, epoch);
     ph[0] += (unsigned)(ntot + 1) / 2u;
     ph[1] += (unsigned)ntot / 2u;
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Top levels of the elimination tree: few supernodes with large fronts, where
+// one CTA streaming its matrices is the critical path. A cluster of CL CTAs
+// takes each such supernode: CTA r streams the chunks k = r, r+CL, ... of the
+// task's matrices into its own shared memory and forms a partial product;
+// the partials are summed through distributed shared memory in rank order
+// (same order every run). Rank 0 takes the tickets (same S + G scheme, G =
+// clusters) and publishes the flags. These launches run after (forward) or
+// before (backward) the launch of the lower levels, so dependencies that cross
+// the boundary are already met by stream order.
+
+constexpr int kTopCluster = 8;
+
+template <typename T, int CL>
+struct TopSmem {
+    // byte offsets of the vectors after the two chunk buffers
+    __device__ static Vec4<T> *vec(unsigned char *raw, int k, int ldx_max, int ld21_max) {
+        Vec4<T> *base = reinterpret_cast<Vec4<T> *>(raw + 2 * kChunkBytes);
+        // 0: fc/zv (ldx)  1: yv/xfull (ldx)  2: fb/gb (ld21)  3: red (kRedRows)  4: part A (ldx)  5: part B (ld21 or ldx)
+        const int off[6] = {0, ldx_max, 2 * ldx_max, 2 * ldx_max + ld21_max, 2 * ldx_max + ld21_max + kRedRows,
+                            3 * ldx_max + ld21_max + kRedRows};
+        return base + off[k];
+    }
+};
+
+size_t top_smem_bytes_impl(int ldx_max, int ld21_max, int scalar_bytes) {
+    return (size_t)2 * kChunkBytes +
+           (size_t)(3 * ldx_max + ld21_max + kRedRows + std::max(ldx_max, ld21_max)) * 4 * scalar_bytes;
+}
+
+// my chunks are k = rank + j*CL, j = 0, 1, ...
+template <typename T, int CL>
+__device__ __forceinline__ void top_issue(const ChunkPlan<T> &pl, int rank, int j, T *buf0, T *buf1, uint64_t *bars) {
+    const int k = rank + j * CL;
+    if (k < pl.total()) issue_chunk(pl, k, (j & 1) ? buf1 : buf0, &bars[j & 1]);
+}
+
+template <typename T, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kSolveThreads, 1)
+k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ order,
+                const SnInfo *__restrict__ sn, const int32_t *__restrict__ child, const int32_t *__restrict__ relind,
+                const T *__restrict__ Xall, const T *__restrict__ L21all, Vec4<T> *__restrict__ sol,
+                Vec4<T> *__restrict__ uvec, unsigned long long *ticket, unsigned *flags, int *err) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T *buf0 = reinterpret_cast<T *>(smem_raw);
+    T *buf1 = reinterpret_cast<T *>(smem_raw + kChunkBytes);
+    Vec4<T> *fc = TopSmem<T, CL>::vec(smem_raw, 0, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *yv = TopSmem<T, CL>::vec(smem_raw, 1, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *fb = TopSmem<T, CL>::vec(smem_raw, 2, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *red = TopSmem<T, CL>::vec(smem_raw, 3, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *ypart = TopSmem<T, CL>::vec(smem_raw, 4, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *upart = TopSmem<T, CL>::vec(smem_raw, 5, lay.ldx_max, lay.ld21_max);
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_task;
+    __shared__ unsigned s_epoch;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    unsigned ph[2] = {0u, 0u};
+    for (;;) {
+        if (rank == 0 && tid == 0) next_task(ticket, S, Z, order, false, err, s_task, s_epoch);
+        cluster.sync();
+        const int s = *cluster.map_shared_rank(&s_task, 0);
+        const unsigned epoch = *cluster.map_shared_rank(&s_epoch, 0);
+        cluster.sync();  // rank 0 leaves only after every rank read its task
+        if (s < 0) break;
+        const SnInfo d = sn[s];
+        const int nc = d.ncol, nb = d.nrow - d.ncol;
+        ChunkPlan<T> pl;
+        pl.init(Xall + d.x_off, d.ldx, nc, L21all + d.l21_off, d.ld21, nb > 0 ? nc : 0);
+        const int ntot = pl.total();
+        const int mine = rank < ntot ? (ntot - rank + CL - 1) / CL : 0;
+        if (tid == 0) {
+            top_issue<T, CL>(pl, rank, 0, buf0, buf1, bars);
+            top_issue<T, CL>(pl, rank, 1, buf0, buf1, bars);
+            for (int j = 2; j < mine; ++j) prefetch_chunk_l2(pl, rank + j * CL);
+        }
+        for (int i = tid; i < d.ldx; i += kSolveThreads)
+            fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+        for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
+        if (rank == 0 && tid == 0)
+            for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+                const int c = child[ci];
+                if (sn[c].level >= ltop) wait_flag(flags + c, epoch, err);
+            }
+        cluster.sync();  // the children's update vectors are complete for every rank
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+            const SnInfo c = sn[child[ci]];
+            const int nbc = c.nrow - c.ncol;
+            const int32_t *ri = relind + c.relind_off;
+            for (int i = tid; i < nbc; i += kSolveThreads) {
+                const Vec4<T> u = ldcg4(uvec + c.uvec_off + i);
+                const int pos = ri[i];
+                Vec4<T> &t = pos < nc ? fc[pos] : fb[pos - nc];
+                t.x += u.x;
+                t.y += u.y;
+                t.z += u.z;
+            }
+            __syncthreads();
+        }
+        const int NQa = (nc + 3) >> 2, Ga = groups_for(NQa);
+        const int NQb = (nb + 3) >> 2, Gb = groups_for(NQb);
+        T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+        bool a_done = false;
+        for (int j = 0; j <= mine; ++j) {
+            const int k = rank + j * CL;
+            if (!a_done && (j == mine || k >= pl.nA)) {
+                // my part of y = X fc, then the sum over the ranks
+                reduce_groups<T, false>(NQa, Ga, tid % NQa, tid / NQa, ax, ay, az, red, ypart);
+#pragma unroll
+                for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+                cluster.sync();
+                for (int i = tid; i < nc; i += kSolveThreads) {
+                    Vec4<T> a = {(T)0, (T)0, (T)0, (T)0};
+                    for (int r = 0; r < CL; ++r) {
+                        const Vec4<T> p = cluster.map_shared_rank(ypart, r)[i];
+                        a.x += p.x;
+                        a.y += p.y;
+                        a.z += p.z;
+                    }
+                    yv[i] = a;
+                }
+                __syncthreads();
+                a_done = true;
+            }
+            if (j == mine) break;
+            T *buf = (j & 1) ? buf1 : buf0;
+            wait_chunk(&bars[j & 1], (ph[j & 1] + (unsigned)(j >> 1)) & 1u, err);
+            int c0, cn, ld;
+            const T *src;
+            pl.chunk(k, c0, cn, src, ld);
+            if (k < pl.nA) {
+                for (int w = tid; w < NQa * Ga; w += kSolveThreads)
+                    chunk_axpy(buf, ld, cn, c0, w % NQa, w / NQa, Ga, fc, ax, ay, az);
+            } else {
+                for (int w = tid; w < NQb * Gb; w += kSolveThreads)
+                    chunk_axpy(buf, ld, cn, c0, w % NQb, w / NQb, Gb, yv, ax, ay, az);
+            }
+            __syncthreads();
+            if (tid == 0) top_issue<T, CL>(pl, rank, j + 2, buf0, buf1, bars);
+        }
+        if (nb > 0) reduce_groups<T, false>(NQb, Gb, tid % max(NQb, 1), tid / max(NQb, 1), ax, ay, az, red, upart);
+        cluster.sync();  // every rank's part of L21 y is in its shared memory
+        for (int i = rank * kSolveThreads + tid; i < nb; i += CL * kSolveThreads) {
+            Vec4<T> u = fb[i];
+            for (int r = 0; r < CL; ++r) {
+                const Vec4<T> p = cluster.map_shared_rank(upart, r)[i];
+                u.x -= p.x;
+                u.y -= p.y;
+                u.z -= p.z;
+            }
+            uvec[d.uvec_off + i] = u;
+        }
+        for (int i = rank * kSolveThreads + tid; i < nc; i += CL * kSolveThreads) sol[d.first + i] = yv[i];
+        __threadfence();
+        cluster.sync();  // every rank's results are written (and fenced) before the flag
+        if (rank == 0 && tid == 0) st_release(flags + s, epoch);
+        ph[0] += (unsigned)(mine + 1) / 2u;
+        ph[1] += (unsigned)mine / 2u;
+    }
+}
+
+// Backward counterpart: z = y - L21^T g (g: the solution at the struct rows),
+// x = X^T z, both split over the ranks by chunks and summed in rank order.
+template <typename T, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kSolveThreads, 1)
+k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+                const int32_t *__restrict__ rows, const T *__restrict__ Xall, const T *__restrict__ L21Tall,
+                Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32,
+                int mode, unsigned long long *ticket, unsigned *flags, int *err) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T *buf0 = reinterpret_cast<T *>(smem_raw);
+    T *buf1 = reinterpret_cast<T *>(smem_raw + kChunkBytes);
+    Vec4<T> *zv = TopSmem<T, CL>::vec(smem_raw, 0, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *zf = TopSmem<T, CL>::vec(smem_raw, 1, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *gb = TopSmem<T, CL>::vec(smem_raw, 2, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *red = TopSmem<T, CL>::vec(smem_raw, 3, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *zpart = TopSmem<T, CL>::vec(smem_raw, 4, lay.ldx_max, lay.ld21_max);
+    Vec4<T> *xpart = TopSmem<T, CL>::vec(smem_raw, 5, lay.ldx_max, lay.ld21_max);
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_task;
+    __shared__ unsigned s_epoch;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    unsigned ph[2] = {0u, 0u};
+    for (;;) {
+        if (rank == 0 && tid == 0) next_task(ticket, S, Z, order, true, err, s_task, s_epoch);
+        cluster.sync();
+        const int s = *cluster.map_shared_rank(&s_task, 0);
+        const unsigned epoch = *cluster.map_shared_rank(&s_epoch, 0);
+        cluster.sync();
+        if (s < 0) break;
+        const SnInfo d = sn[s];
+        const int nc = d.ncol, nb = d.nrow - d.ncol;
+        ChunkPlan<T> pl;
+        if (nb > 0) pl.init(L21Tall + d.l21t_off, d.ldx, nb, Xall + d.xt_off, d.ldx, nc);
+        else pl.init(Xall + d.xt_off, d.ldx, nc, nullptr, 0, 0);
+        const int ntot = pl.total();
+        const int nA = nb > 0 ? pl.nA : 0;  // chunks of L21^T
+        const int mine = rank < ntot ? (ntot - rank + CL - 1) / CL : 0;
+        if (tid == 0) {
+            top_issue<T, CL>(pl, rank, 0, buf0, buf1, bars);
+            top_issue<T, CL>(pl, rank, 1, buf0, buf1, bars);
+            for (int j = 2; j < mine; ++j) prefetch_chunk_l2(pl, rank + j * CL);
+        }
+        for (int i = tid; i < d.ldx; i += kSolveThreads)
+            zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+        if (rank == 0 && tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
+        cluster.sync();  // the parent's solution is complete for every rank
+        const int32_t *rs = rows + d.rows_off;
+        for (int i = tid; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
+        __syncthreads();
+        const int NQ = (nc + 3) >> 2, G = groups_for(NQ);
+        T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+        bool a_done = false;
+        for (int j = 0; j <= mine; ++j) {
+            const int k = rank + j * CL;
+            if (!a_done && (j == mine || k >= nA)) {
+                // z = y - sum over the ranks of their part of L21^T g
+                if (nb > 0) {
+                    reduce_groups<T, false>(NQ, G, tid % NQ, tid / NQ, ax, ay, az, red, zpart);
+#pragma unroll
+                    for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+                    cluster.sync();
+                }
+                for (int i = tid; i < nc; i += kSolveThreads) {
+                    Vec4<T> a = zv[i];
+                    if (nb > 0)
+                        for (int r = 0; r < CL; ++r) {
+                            const Vec4<T> p = cluster.map_shared_rank(zpart, r)[i];
+                            a.x -= p.x;
+                            a.y -= p.y;
+                            a.z -= p.z;
+                        }
+                    zf[i] = a;
+                }
+                __syncthreads();
+                a_done = true;
+            }
+            if (j == mine) break;
+            T *buf = (j & 1) ? buf1 : buf0;
+            wait_chunk(&bars[j & 1], (ph[j & 1] + (unsigned)(j >> 1)) & 1u, err);
+            int c0, cn, ld;
+            const T *src;
+            pl.chunk(k, c0, cn, src, ld);
+            const Vec4<T> *v = (k < nA) ? gb : zf;
+            for (int w = tid; w < NQ * G; w += kSolveThreads) chunk_axpy(buf, ld, cn, c0, w % NQ, w / NQ, G, v, ax, ay, az);
+            __syncthreads();
+            if (tid == 0) top_issue<T, CL>(pl, rank, j + 2, buf0, buf1, bars);
+        }
+        reduce_groups<T, false>(NQ, G, tid % NQ, tid / NQ, ax, ay, az, red, xpart);
+        cluster.sync();  // every rank's part of X^T z is in its shared memory
+        for (int i = rank * kSolveThreads + tid; i < nc; i += CL * kSolveThreads) {
+            Vec4<T> x = {(T)0, (T)0, (T)0, (T)0};
+            for (int r = 0; r < CL; ++r) {
+                const Vec4<T> p = cluster.map_shared_rank(xpart, r)[i];
+                x.x += p.x;
+                x.y += p.y;
+                x.z += p.z;
+            }
+            const int kk = d.first + i;
+            sol[kk] = x;
+            if (mode == 0) {
+                pc64[kk] = {(double)x.x, (double)x.y, (double)x.z, 0.0};
+            } else {
+                Vec4<double> v = pc64[kk];
+                v.x += (double)x.x;
+                v.y += (double)x.y;
+                v.z += (double)x.z;
+                pc64[kk] = v;
+                pc32[kk] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
+            }
+        }
+        __threadfence();
+        cluster.sync();
+        if (rank == 0 && tid == 0) st_release(flags + s, epoch);
+        ph[0] += (unsigned)(mine + 1) / 2u;
+        ph[1] += (unsigned)mine / 2u;
     }
 }
 
@@ -1254,8 +1552,15 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
-    k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(s.S, s.S + G, lay, s.level_sn, s.sn, s.child, s.relind, X, L21,
-                                                   sol, uvec, ticket, flags, err);
+    if (s.s_low > 0)
+        k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(s.s_low, s.s_low + G, lay, s.level_sn, s.sn, s.child, s.relind,
+                                                       X, L21, sol, uvec, ticket, flags, err);
+    if (s.s_top > 0) {
+        const size_t tsmem = top_smem_bytes_impl(s.max_ldx, s.max_ld21, sizeof(T));
+        k_solve_fwd_top<T, kTopCluster><<<s.top_clusters * kTopCluster, kSolveThreads, tsmem, st>>>(
+            s.s_top, s.s_top + s.top_clusters, s.ltop, lay, s.level_sn + s.s_low, s.sn, s.child, s.relind, X, L21, sol,
+            uvec, ticket + 2, flags, err);
+    }
 }
 
 template <typename T>
@@ -1266,8 +1571,15 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
-    k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(s.S, s.S + G, lay, s.level_sn, s.sn, s.rows, X, L21T, sol, pc64,
-                                                   pc32, mode, ticket, flags, err);
+    if (s.s_top > 0) {
+        const size_t tsmem = top_smem_bytes_impl(s.max_ldx, s.max_ld21, sizeof(T));
+        k_solve_bwd_top<T, kTopCluster><<<s.top_clusters * kTopCluster, kSolveThreads, tsmem, st>>>(
+            s.s_top, s.s_top + s.top_clusters, lay, s.level_sn + s.s_low, s.sn, s.rows, X, L21T, sol, pc64, pc32, mode,
+            ticket + 2, flags, err);
+    }
+    if (s.s_low > 0)
+        k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(s.s_low, s.s_low + G, s.ltop, lay, s.level_sn, s.sn, s.rows, X,
+                                                       L21T, sol, pc64, pc32, mode, ticket, flags, err);
 }
 
 int energy_partials(int V) { return std::max(1, blocks_for(V, kEnergyThreads)); }
@@ -1341,6 +1653,20 @@ cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64) {
     e = raise_smem_limit((const void *)k_solve_fwd<double>, bytes_f64);
     if (e != cudaSuccess) return e;
     return raise_smem_limit((const void *)k_solve_bwd<double>, bytes_f64);
+}
+
+size_t top_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
+    return top_smem_bytes_impl(ldx_max, ld21_max, scalar_bytes);
+}
+
+cudaError_t configure_top_smem(int bytes_f32, int bytes_f64) {
+    cudaError_t e = raise_smem_limit((const void *)k_solve_fwd_top<float, kTopCluster>, bytes_f32);
+    if (e != cudaSuccess) return e;
+    e = raise_smem_limit((const void *)k_solve_bwd_top<float, kTopCluster>, bytes_f32);
+    if (e != cudaSuccess) return e;
+    e = raise_smem_limit((const void *)k_solve_fwd_top<double, kTopCluster>, bytes_f64);
+    if (e != cudaSuccess) return e;
+    return raise_smem_limit((const void *)k_solve_bwd_top<double, kTopCluster>, bytes_f64);
 }
 
 // explicit instantiations

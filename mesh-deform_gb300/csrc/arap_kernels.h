@@ -37,7 +37,10 @@ struct DevTopo {
 struct DevSym {
     int V, m, S, nnz;
     int max_ldx, max_ld21, max_ncol;
-    int solve_grid32, solve_grid64;  // CTAs per solve launch (each loops over tickets)
+    int solve_grid32, solve_grid64;  // CTAs per lower-level solve launch (each loops over tickets)
+    // the solves split the tree: levels [0, ltop) by single CTAs (s_low tasks),
+    // levels [ltop, top) by clusters (s_top tasks, top_clusters clusters)
+    int ltop, s_low, s_top, top_clusters;
     const int32_t *drow, *dcol, *dent, *oldidx;
     const int64_t *amap, *dmap;
     const SnInfo *sn;
@@ -98,6 +101,16 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
 // solve CTAs resident on the device at once (occupancy x SMs) for that shared memory
 int solve_resident_ctas(int smem_bytes, int scalar_bytes);
+// shared memory of the cluster solves of the top levels, and its limit
+size_t top_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
+cudaError_t configure_top_smem(int bytes_f32, int bytes_f64);
+// a tree level goes to the cluster solves when one of its supernodes holds at
+// least this many bytes of X and L21 (FP32), and every level above does too
+#ifndef ARAP_TOP_TASK_KB
+#define ARAP_TOP_TASK_KB 64
+#endif
+constexpr int kTopTaskBytes = ARAP_TOP_TASK_KB * 1024;
+constexpr int kTopMaxClusters = 16;
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
                       unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st);

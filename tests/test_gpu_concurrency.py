@@ -67,3 +67,28 @@ def test_solve_cta_count_does_not_change_results(gpu, precision):
     for a, b in outs[1:]:
         np.testing.assert_array_equal(a, outs[0][0])
         np.testing.assert_array_equal(b, outs[0][1])
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-6)])
+@pytest.mark.parametrize("threshold", [1, 4096, 16384])
+def test_cluster_levels_match_single_cta_levels(gpu, precision, tol, threshold):
+    """Solving the top levels of the tree with CTA clusters (a low threshold
+    puts most levels there) gives the positions of the single-CTA solves up to
+    the order of the sums, and stays within the oracle tolerance."""
+    from oracle import oracle as O
+
+    w = W.cfg_twisted_bar(h=0.1, iterations=6)
+    with make(gpu, w, precision) as ctx:
+        ctx.set_cluster_threshold(-1)
+        ref = ctx.deform(6)
+    with make(gpu, w, precision) as ctx:
+        ctx.set_cluster_threshold(threshold)
+        got = ctx.deform(6)
+        ctx.set_targets(w.ctargets + 0.02)   # a second deform on the same launch shape
+        got2 = ctx.deform(6)
+        ctx.set_cluster_threshold(-1)
+        ref2 = ctx.deform(6)
+    assert W.bbox_rel_error(got, ref, w.positions) <= tol
+    assert W.bbox_rel_error(got2, ref2, w.positions) <= tol
+    ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, 6)
+    assert ok and W.bbox_rel_error(got, o, w.positions) <= (1e-10 if precision == "fp64" else 1e-6)
