@@ -240,7 +240,8 @@ k_bsolve_fwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
         const int i = e / PT, p = e % PT;
         if (p0 + p < P) uvec[(d.uvec_off + i) * P + p0 + p] = Fb[e];
     }
-    __threadfence();
+    // the barrier orders every thread's writes before thread 0's release,
+    // which is cumulative: a CTA that acquires the flag sees them all
     __syncthreads();
     if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
 }
@@ -334,7 +335,8 @@ k_bsolve_bwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
         pc64[k] = v;
         pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
     }
-    __threadfence();
+    // the barrier orders every thread's writes before thread 0's release,
+    // which is cumulative: a CTA that acquires the flag sees them all
     __syncthreads();
     if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
 }

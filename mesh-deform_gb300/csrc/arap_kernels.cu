@@ -827,21 +827,21 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     Vec4<T> *fb = yv + lay.ldx_max;
     Vec4<T> *red = fb + lay.ld21_max;
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_task;
-    __shared__ unsigned s_epoch;
+    __shared__ int s_task[2];  // this task's and the next one's ticket (taken early)
+    __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
     if (tid == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        next_task(ticket, S, Z, order, false, err, s_task[0], s_epoch[0]);
     }
-    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
-    for (;;) {
-    if (tid == 0) next_task(ticket, S, Z, order, false, err, s_task, s_epoch);
     __syncthreads();
-    const int s = s_task;
+    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
+    for (int slot = 0;; slot ^= 1) {
+    const int s = s_task[slot];
     if (s < 0) break;
-    const unsigned epoch = s_epoch;
+    const unsigned epoch = s_epoch[slot];
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
     ChunkPlan<T> pl;
@@ -943,7 +943,10 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     if (pl.nB > 0) reduce_groups<T, true>(NQb, Gb, tid % max(NQb, 1), tid / max(NQb, 1), ax, ay, az, red, fb);
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
-    __threadfence();
+    // the next ticket is taken while the stores drain; the barrier orders
+    // every thread's writes before thread 0's release, which is cumulative: a
+    // CTA that acquires the flag sees them all
+    if (tid == 32) next_task(ticket, S, Z, order, false, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
     __syncthreads();
     if (tid == 0) st_release(flags + s, epoch);
     ph[0] += (unsigned)(ntot + 1) / 2u;
@@ -969,21 +972,21 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     Vec4<T> *gb = xv + lay.ldx_max;
     Vec4<T> *red = gb + lay.ld21_max;
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_task;
-    __shared__ unsigned s_epoch;
+    __shared__ int s_task[2];  // this task's and the next one's ticket (taken early)
+    __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
     if (tid == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        next_task(ticket, S, Z, order, true, err, s_task[0], s_epoch[0]);
     }
-    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
-    for (;;) {
-    if (tid == 0) next_task(ticket, S, Z, order, true, err, s_task, s_epoch);
     __syncthreads();
-    const int s = s_task;
+    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
+    for (int slot = 0;; slot ^= 1) {
+    const int s = s_task[slot];
     if (s < 0) break;
-    const unsigned epoch = s_epoch;
+    const unsigned epoch = s_epoch[slot];
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
     ChunkPlan<T> pl;
@@ -1045,7 +1048,10 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
             pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
         }
     }
-    __threadfence();
+    // the next ticket is taken while the stores drain; the barrier orders
+    // every thread's writes before thread 0's release, which is cumulative: a
+    // CTA that acquires the flag sees them all
+    if (tid == 32) next_task(ticket, S, Z, order, true, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
     __syncthreads();
     if (tid == 0) st_release(flags + s, epoch);
     ph[0] += (unsigned)(ntot + 1) / 2u;
@@ -1110,22 +1116,24 @@ k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict
     Vec4<T> *ypart = TopSmem<T, CL>::vec(smem_raw, 4, lay.ldx_max, lay.ld21_max);
     Vec4<T> *upart = TopSmem<T, CL>::vec(smem_raw, 5, lay.ldx_max, lay.ld21_max);
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_task;
-    __shared__ unsigned s_epoch;
+    __shared__ int s_task[2];  // rank 0 holds this task's and the next one's ticket
+    __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
     if (tid == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (rank == 0) next_task(ticket, S, Z, order, false, err, s_task[0], s_epoch[0]);
     }
+    cluster.sync();
     unsigned ph[2] = {0u, 0u};
-    for (;;) {
-        if (rank == 0 && tid == 0) next_task(ticket, S, Z, order, false, err, s_task, s_epoch);
-        cluster.sync();
-        const int s = *cluster.map_shared_rank(&s_task, 0);
-        const unsigned epoch = *cluster.map_shared_rank(&s_epoch, 0);
-        cluster.sync();  // rank 0 leaves only after every rank read its task
-        if (s < 0) break;
+    for (int slot = 0;; slot ^= 1) {
+        const int s = cluster.map_shared_rank(s_task, 0)[slot];
+        const unsigned epoch = cluster.map_shared_rank(s_epoch, 0)[slot];
+        if (s < 0) {
+            cluster.sync();  // rank 0 leaves only after every rank read its shared memory
+            break;
+        }
         const SnInfo d = sn[s];
         const int nc = d.ncol, nb = d.nrow - d.ncol;
         ChunkPlan<T> pl;
@@ -1214,8 +1222,10 @@ k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict
             uvec[d.uvec_off + i] = u;
         }
         for (int i = rank * kSolveThreads + tid; i < nc; i += CL * kSolveThreads) sol[d.first + i] = yv[i];
-        __threadfence();
-        cluster.sync();  // every rank's results are written (and fenced) before the flag
+        // rank 0 takes the next ticket meanwhile; the cluster barrier orders every
+        // rank's writes before rank 0's (cumulative) release
+        if (rank == 0 && tid == 32) next_task(ticket, S, Z, order, false, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
+        cluster.sync();
         if (rank == 0 && tid == 0) st_release(flags + s, epoch);
         ph[0] += (unsigned)(mine + 1) / 2u;
         ph[1] += (unsigned)mine / 2u;
@@ -1243,22 +1253,24 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
     Vec4<T> *zpart = TopSmem<T, CL>::vec(smem_raw, 4, lay.ldx_max, lay.ld21_max);
     Vec4<T> *xpart = TopSmem<T, CL>::vec(smem_raw, 5, lay.ldx_max, lay.ld21_max);
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_task;
-    __shared__ unsigned s_epoch;
+    __shared__ int s_task[2];  // rank 0 holds this task's and the next one's ticket
+    __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
     if (tid == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (rank == 0) next_task(ticket, S, Z, order, true, err, s_task[0], s_epoch[0]);
     }
+    cluster.sync();
     unsigned ph[2] = {0u, 0u};
-    for (;;) {
-        if (rank == 0 && tid == 0) next_task(ticket, S, Z, order, true, err, s_task, s_epoch);
-        cluster.sync();
-        const int s = *cluster.map_shared_rank(&s_task, 0);
-        const unsigned epoch = *cluster.map_shared_rank(&s_epoch, 0);
-        cluster.sync();
-        if (s < 0) break;
+    for (int slot = 0;; slot ^= 1) {
+        const int s = cluster.map_shared_rank(s_task, 0)[slot];
+        const unsigned epoch = cluster.map_shared_rank(s_epoch, 0)[slot];
+        if (s < 0) {
+            cluster.sync();
+            break;
+        }
         const SnInfo d = sn[s];
         const int nc = d.ncol, nb = d.nrow - d.ncol;
         ChunkPlan<T> pl;
@@ -1340,7 +1352,9 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
                 pc32[kk] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
             }
         }
-        __threadfence();
+        // rank 0 takes the next ticket meanwhile; the cluster barrier orders every
+        // rank's writes before rank 0's (cumulative) release
+        if (rank == 0 && tid == 32) next_task(ticket, S, Z, order, true, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
         cluster.sync();
         if (rank == 0 && tid == 0) st_release(flags + s, epoch);
         ph[0] += (unsigned)(mine + 1) / 2u;
