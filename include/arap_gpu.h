@@ -342,6 +342,9 @@ typedef struct arap_server_stats {
     int64_t iterations_done;  /* iterations of completed requests */
     int64_t resident_bytes, peak_resident_bytes, budget_bytes;
     int32_t resident_factors, queue_depth, in_flight, pad;
+    double scheduler_busy_ms;  /* scheduler thread time outside its waits */
+    double worker_busy_ms;     /* prep-thread time in analyses and first launches */
+    double device_ms;          /* sum over launches of their device time (set-up + iterations) */
 } arap_server_stats;
 
 int arap_srv_create(const arap_server_config *cfg, arap_server **out);

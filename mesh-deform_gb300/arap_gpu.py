@@ -68,7 +68,8 @@ class ServerStats(C.Structure):
                                          "factor_misses", "evictions", "launches", "batched_launches",
                                          "batched_requests", "iterations_done", "resident_bytes",
                                          "peak_resident_bytes", "budget_bytes")] + \
-        [(n, C.c_int32) for n in ("resident_factors", "queue_depth", "in_flight", "pad")]
+        [(n, C.c_int32) for n in ("resident_factors", "queue_depth", "in_flight", "pad")] + \
+        [(n, C.c_double) for n in ("scheduler_busy_ms", "worker_busy_ms", "device_ms")]
 
 
 SIGNATURES = {

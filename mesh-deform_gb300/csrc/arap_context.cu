@@ -140,11 +140,14 @@ struct arap_ctx {
     int bP = 0, bT = 0, bS = -1, bpt = 0;
     int tP = -1;  // poses whose targets arap_pose_targets left in btargets (-1: none)
     int model_P = 1, model_T = 1;  // poses / pose tiles of the last deform (cost model)
-    // CUDA graphs of the setup and of the iteration sequence; replayed while
-    // nothing they reference changes (direct launches when profiling)
-    cudaGraphExec_t g_setup = nullptr, g_iter = nullptr;
-    int64_t g_setup_key[4] = {0, 0, 0, 0}, g_iter_key[4] = {0, 0, 0, 0};
-    int64_t g_setup_launches = 0, g_iter_launches = 0;
+    // CUDA graphs of the setup and of 2^k iterations (k < kIterGraphs); a deform
+    // of n iterations replays the graphs of n's binary digits, so any count
+    // reuses them. Replayed while nothing they reference changes (direct
+    // launches when profiling).
+    static constexpr int kIterGraphs = 8;
+    cudaGraphExec_t g_setup = nullptr, g_iter[kIterGraphs] = {};
+    int64_t g_setup_key[4] = {0, 0, 0, 0}, g_iter_key[kIterGraphs][4] = {};
+    int64_t g_setup_launches = 0, g_iter_launches[kIterGraphs] = {};
     int64_t gen = 1;  // bumped when the symbolic analysis or any device buffer changes
     bool use_graphs = true;
     int solve_cap = 0;  // most CTAs per triangular-solve launch (0: as many as fit the device)
@@ -781,7 +784,8 @@ void arap_destroy(arap_ctx *ctx) {
     for (DevBuf *b : ctx->buffers()) b->release();
     for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
     if (ctx->g_setup) cudaGraphExecDestroy(ctx->g_setup);
-    if (ctx->g_iter) cudaGraphExecDestroy(ctx->g_iter);
+    for (cudaGraphExec_t g : ctx->g_iter)
+        if (g) cudaGraphExecDestroy(g);
     if (ctx->herr_host) pinned_words().put(ctx->herr_host);
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -1156,13 +1160,17 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         ctx->retarget = false;
     }
     CK(cudaEventRecord(ctx->ev1, st));
-    if (iterations > 0) {
+    for (int left = iterations; left > 0;) {
         const bool it64 = ctx->state_prec == ARAP_PRECISION_FP64;
-        const int64_t key[4] = {ctx->gen, it64 ? 1 : 2, iterations, ctx->refine};
-        const int rc = graph_or_direct(ctx, ctx->g_iter, ctx->g_iter_key, key, ctx->g_iter_launches, [&] {
-            return it64 ? run_iterations<double>(ctx, iterations) : run_iterations<float>(ctx, iterations);
+        int k = 0;
+        while (k + 1 < arap_ctx::kIterGraphs && (2 << k) <= left) ++k;
+        const int n = 1 << k;
+        const int64_t key[4] = {ctx->gen, it64 ? 1 : 2, n, ctx->refine};
+        const int rc = graph_or_direct(ctx, ctx->g_iter[k], ctx->g_iter_key[k], key, ctx->g_iter_launches[k], [&] {
+            return it64 ? run_iterations<double>(ctx, n) : run_iterations<float>(ctx, n);
         });
         if (rc != ARAP_OK) return rc;
+        left -= n;
     }
     CK(cudaEventRecord(ctx->ev2, st));
     if (out_xyz) {

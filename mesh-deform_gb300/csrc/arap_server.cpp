@@ -32,6 +32,10 @@ struct CtxBackend {
         return arap_deform_poses_async(h, P, tgt, iters, out);
     }
     int query(Handle h, int32_t *done) { return arap_query(h, done); }
+    double device_ms(Handle h) {
+        double a = 0.0, b = 0.0;
+        return arap_get_timing(h, &a, &b) == ARAP_OK ? a + b : 0.0;
+    }
     std::string last_error(Handle h) { return arap_last_error(h); }
     void *alloc_host(size_t bytes) {
         void *p = nullptr;

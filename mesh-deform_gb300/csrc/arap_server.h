@@ -14,6 +14,7 @@
 //   int  deform_async(Handle, int iters, double* out)
 //   int  deform_poses_async(Handle, int P, const double* targets, int iters, double* out)
 //   int  query(Handle, int32_t* done)               non-blocking completion
+//   double device_ms(Handle)                        device time of the last launch
 //   std::string last_error(Handle)
 //   void* alloc_host(size_t); void free_host(void*)  staging for results
 //   int64_t default_budget()
@@ -81,6 +82,7 @@ class Server {
         std::string error;
         int factor_reused = 0, batch = 0;
         uint64_t key = 0;
+        Slot *slot = nullptr;      // set once the request waits on a slot
     };
 
     struct Slot {
@@ -97,6 +99,7 @@ class Server {
         Clock::time_point last_used;
         uint64_t order = 0;       // creation order (admission is first come, first served)
         std::vector<Req *> running;
+        std::deque<Req *> waiting;  // requests of this constraint set not launched yet, oldest first
         std::vector<double> batch_targets;
         double *staging = nullptr;
         size_t staging_doubles = 0;
@@ -366,30 +369,23 @@ class Server {
     }
 
     void fail_key(Slot *s, int rc, const std::string &err) {
-        for (auto it = pending_.begin(); it != pending_.end();) {
-            Req *q = *it;
-            if (q->mesh == s->mesh && q->key == s->key && q->idx == s->idx) {
-                q->t_launch = Clock::now();
-                finish(q, rc, err);
-                it = pending_.erase(it);
-            } else {
-                ++it;
-            }
+        for (Req *q : s->waiting) {
+            q->t_launch = Clock::now();
+            finish(q, rc, err);
         }
+        s->waiting.clear();
     }
 
     // ---- launches ----------------------------------------------------------
     // Takes the oldest waiting request of slot s and the others that can share
-    // its launch (same constraint set and iteration count), at most max_p.
+    // its launch (same iteration count), at most max_p, oldest first.
     std::vector<Req *> take_batch(Slot *s, int max_p) {
         std::vector<Req *> batch;
-        int iters = -1;
-        for (auto it = pending_.begin(); it != pending_.end() && (int)batch.size() < max_p;) {
-            Req *q = *it;
-            if (q->mesh == s->mesh && q->key == s->key && q->idx == s->idx && (iters < 0 || q->iterations == iters)) {
-                iters = q->iterations;
-                batch.push_back(q);
-                it = pending_.erase(it);
+        const int iters = s->waiting.front()->iterations;
+        for (auto it = s->waiting.begin(); it != s->waiting.end() && (int)batch.size() < max_p;) {
+            if ((*it)->iterations == iters) {
+                batch.push_back(*it);
+                it = s->waiting.erase(it);
             } else {
                 ++it;
             }
@@ -397,14 +393,12 @@ class Server {
         return batch;
     }
 
-    int waiting_for(const Slot *s, int *iters) const {
-        int n = 0, it0 = -1;
-        for (const Req *q : pending_)
-            if (q->mesh == s->mesh && q->key == s->key && q->idx == s->idx) {
-                if (it0 < 0) it0 = q->iterations;
-                if (q->iterations == it0) ++n;
-            }
-        if (iters) *iters = it0;
+    // requests of slot s that could share a launch with its oldest one
+    static int batchable(const Slot *s) {
+        if (s->waiting.empty()) return 0;
+        const int iters = s->waiting.front()->iterations;
+        int n = 0;
+        for (const Req *q : s->waiting) n += q->iterations == iters;
         return n;
     }
 
@@ -500,6 +494,7 @@ class Server {
             Slot *s = j.slot;
             int rc = ARAP_OK;
             std::string err;
+            const auto tw0 = Clock::now();
             if (j.kind == Job::Analyze) {
                 const MeshRec &m = *mesh_at(s->mesh);
                 Handle h{};
@@ -526,6 +521,7 @@ class Server {
             s->job_err = err;
             {
                 std::lock_guard<std::mutex> lk(mu_);
+                st_.worker_busy_ms += ms_between(tw0, Clock::now());
                 done_jobs_.push_back(j);
             }
             cv_.notify_all();
@@ -565,6 +561,11 @@ class Server {
             if (!done && rc == ARAP_OK) continue;
             const std::string err = rc == ARAP_OK ? std::string() : b_.last_error(s->ctx);
             const int V = mesh_at(s->mesh)->V;
+            if (rc == ARAP_OK) {
+                const double dms = b_.device_ms(s->ctx);
+                std::lock_guard<std::mutex> lk(mu_);
+                st_.device_ms += dms;
+            }
             for (size_t p = 0; p < s->running.size(); ++p) {
                 Req *q = s->running[p];
                 if (rc == ARAP_OK)
@@ -599,7 +600,7 @@ class Server {
             Slot *victim = nullptr;
             for (auto &p : slots_) {
                 Slot *s = p.get();
-                if (s == keep || s->state != SlotState::Idle || waiting_for(s, nullptr) > 0) continue;
+                if (s == keep || s->state != SlotState::Idle || !s->waiting.empty()) continue;
                 if (!victim || s->last_used < victim->last_used) victim = s;
             }
             if (!victim) return false;
@@ -612,8 +613,16 @@ class Server {
         return true;
     }
 
+    // Device bytes a launch of P requests on s adds to what s holds now.
+    int64_t launch_extra(Slot *s, int P) {
+        int64_t need = s->need;
+        if (P > 1 && b_.plan_bytes(s->ctx, P, &need) != ARAP_OK) return -1;
+        return std::max<int64_t>(0, std::max(need, s->need) - s->bytes);
+    }
+
     void schedule() {
-        // requests of resident constraint sets, and new constraint sets to analyse
+        // attach new requests to their constraint set's slot, creating (and
+        // analysing) a slot for a set not seen yet
         for (auto it = pending_.begin(); it != pending_.end();) {
             Req *q = *it;
             const MeshRec &m = *mesh_at(q->mesh);
@@ -656,28 +665,34 @@ class Server {
                 set_resident();
                 ++busy_jobs_;
                 post_job({Job::Analyze, s, 0, 0});
-                ++it;
-                continue;
             }
-            if (s->state == SlotState::Idle && inflight_ < cfg_.max_in_flight) {
-                int P = std::min(waiting_for(s, nullptr), cfg_.max_batch);
-                int64_t extra = 0;
-                while (P > 1) {
-                    int64_t need = 0;
-                    if (b_.plan_bytes(s->ctx, P, &need) == ARAP_OK) {
-                        extra = std::max<int64_t>(0, need - s->bytes);
-                        if (resident_ + extra <= budget_ || make_room(extra, s)) break;
-                    }
-                    P /= 2;
-                    extra = 0;
-                }
-                s->reserved = extra;
-                resident_ += extra;
-                start(s, take_batch(s, std::max(P, 1)), false);
-                it = pending_.begin();  // take_batch edited the list
-                continue;
+            q->slot = s;
+            s->waiting.push_back(q);
+            it = pending_.erase(it);
+        }
+        // resident constraint sets with waiting requests, oldest request first
+        std::vector<Slot *> idle;
+        for (auto &p : slots_)
+            if (p->state == SlotState::Idle && !p->waiting.empty()) idle.push_back(p.get());
+        std::sort(idle.begin(), idle.end(),
+                  [](const Slot *a, const Slot *b) { return a->waiting.front()->ticket < b->waiting.front()->ticket; });
+        for (Slot *s : idle) {
+            if (inflight_ >= cfg_.max_in_flight) break;
+            int P = std::min(batchable(s), cfg_.max_batch);
+            int64_t extra = 0;
+            while (P > 1) {
+                extra = launch_extra(s, P);
+                if (extra >= 0 && (resident_ + extra <= budget_ || make_room(extra, s))) break;
+                P /= 2;
+                extra = 0;
             }
-            ++it;
+            if (P <= 1) {
+                P = 1;
+                extra = 0;
+            }
+            s->reserved = extra;
+            resident_ += extra;
+            start(s, take_batch(s, P), false);
         }
         // first launches of analysed constraint sets, first come first served;
         // the oldest one that does not fit holds back the later ones
@@ -687,23 +702,20 @@ class Server {
         std::sort(ready.begin(), ready.end(), [](const Slot *a, const Slot *b) { return a->order < b->order; });
         for (Slot *s : ready) {
             if (inflight_ >= cfg_.max_in_flight) break;
-            int it0 = 0;
-            const int waiting = waiting_for(s, &it0);
-            if (waiting == 0) {
+            if (s->waiting.empty()) {
                 remove_slot(s);
                 continue;
             }
-            int P = std::min(waiting, cfg_.max_batch);
-            int64_t need = s->need;
-            if (P > 1 && b_.plan_bytes(s->ctx, P, &need) != ARAP_OK) {
+            int P = std::min(batchable(s), cfg_.max_batch);
+            int64_t extra = launch_extra(s, P);
+            if (extra < 0) {
                 P = 1;
-                need = s->need;
+                extra = launch_extra(s, 1);
             }
-            int64_t extra = std::max<int64_t>(0, need - s->bytes);
             if (resident_ + extra > budget_ && !make_room(extra, s)) {
                 if (P > 1) {
                     P = 1;
-                    extra = std::max<int64_t>(0, s->need - s->bytes);
+                    extra = launch_extra(s, 1);
                     if (resident_ + extra <= budget_ || make_room(extra, s)) goto admit;
                 }
                 if (mesh_bytes_ + s->bytes + extra > budget_ || quiescent()) {
@@ -734,11 +746,16 @@ class Server {
     bool quiescent() const {
         if (inflight_ > 0 || busy_jobs_ > 0) return false;
         for (auto &p : slots_)
-            if (p->state == SlotState::Idle && waiting_for(p.get(), nullptr) > 0) return false;
+            if (p->state == SlotState::Idle && !p->waiting.empty()) return false;
         return true;
     }
 
-    bool has_work() const { return !pending_.empty() || inflight_ > 0 || busy_jobs_ > 0; }
+    bool has_work() const {
+        if (!pending_.empty() || inflight_ > 0 || busy_jobs_ > 0) return true;
+        for (auto &p : slots_)
+            if (!p->waiting.empty()) return true;
+        return false;
+    }
 
     void scheduler_loop() {
         for (;;) {
@@ -754,13 +771,17 @@ class Server {
                 finished.swap(done_jobs_);
                 stopping = stop_;
             }
+            const auto t0 = Clock::now();
             for (Req *q : fresh) pending_.push_back(q);
             for (const Job &j : finished) job_done(j);
             poll_busy();
             schedule();
             {
+                int waiting = (int)pending_.size();
+                for (auto &p : slots_) waiting += (int)p->waiting.size();
                 std::lock_guard<std::mutex> lk(mu_);
-                st_.queue_depth = (int32_t)pending_.size();
+                st_.queue_depth = waiting;
+                st_.scheduler_busy_ms += ms_between(t0, Clock::now());
             }
             if (stopping && !has_work()) {
                 std::lock_guard<std::mutex> lk(mu_);

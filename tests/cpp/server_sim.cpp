@@ -153,6 +153,7 @@ struct FakeBackend {
         return ARAP_OK;
     }
     std::string last_error(Handle h) { return h ? h->err : std::string("create failed"); }
+    double device_ms(Handle) { return 0.05; }
     void *alloc_host(size_t b) { return ::operator new(b); }
     void free_host(void *p) { ::operator delete(p); }
     int64_t default_budget() { return 1LL << 40; }
