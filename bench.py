@@ -428,7 +428,8 @@ def run_serving(args):
                "queue_ms": {"p50": _pct([r[1] for r in rows], 50), "p99": _pct([r[1] for r in rows], 99)},
                "stats": {k: st[k] for k in ("factor_hits", "factor_misses", "evictions", "launches",
                                              "batched_launches", "batched_requests", "peak_resident_bytes",
-                                             "budget_bytes", "scheduler_busy_ms", "worker_busy_ms", "device_ms")},
+                                             "budget_bytes", "scheduler_busy_ms", "worker_busy_ms", "analyze_ms",
+                                             "device_ms")},
                "device_spans_in_flight_avg": st["device_ms"] / (1e3 * wall),
                "scheduler_busy_frac": st["scheduler_busy_ms"] / (1e3 * wall),
                "clocks": clk}

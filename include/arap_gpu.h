@@ -344,6 +344,7 @@ typedef struct arap_server_stats {
     int32_t resident_factors, queue_depth, in_flight, pad;
     double scheduler_busy_ms;  /* scheduler thread time outside its waits */
     double worker_busy_ms;     /* prep-thread time in analyses and first launches */
+    double analyze_ms;         /* of which: contexts created, constraint sets analysed */
     double device_ms;          /* sum over launches of their device time (set-up + iterations) */
 } arap_server_stats;
 

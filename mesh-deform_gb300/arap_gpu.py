@@ -69,7 +69,7 @@ class ServerStats(C.Structure):
                                          "batched_requests", "iterations_done", "resident_bytes",
                                          "peak_resident_bytes", "budget_bytes")] + \
         [(n, C.c_int32) for n in ("resident_factors", "queue_depth", "in_flight", "pad")] + \
-        [(n, C.c_double) for n in ("scheduler_busy_ms", "worker_busy_ms", "device_ms")]
+        [(n, C.c_double) for n in ("scheduler_busy_ms", "worker_busy_ms", "analyze_ms", "device_ms")]
 
 
 SIGNATURES = {

@@ -518,11 +518,18 @@ int graph_or_direct(arap_ctx *ctx, cudaGraphExec_t &exec, int64_t key_store[4], 
                     int64_t &nlaunch, F enqueue) {
     cudaStream_t st = ctx->stream;
     if (!ctx->use_graphs || ctx->profiling) return enqueue();
-    const bool same = exec && key_store[0] == key[0] && key_store[1] == key[1] && key_store[2] == key[2] &&
-                      key_store[3] == key[3];
-    if (!same) {
+    const bool same_key = key_store[0] == key[0] && key_store[1] == key[1] && key_store[2] == key[2] &&
+                          key_store[3] == key[3];
+    if (!same_key) {
+        // first use of this key: launch directly and only remember the key; a
+        // graph is captured when the same sequence comes again (one-shot
+        // contexts never pay for capture and instantiation)
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
+        for (int i = 0; i < 4; ++i) key_store[i] = key[i];
+        return enqueue();
+    }
+    if (!exec) {
         const int64_t before = ctx->launches;
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         const int rc = enqueue();
@@ -538,7 +545,6 @@ int graph_or_direct(arap_ctx *ctx, cudaGraphExec_t &exec, int64_t key_store[4], 
         CK(ei);
         nlaunch = ctx->launches - before;
         ctx->launches = before;
-        for (int i = 0; i < 4; ++i) key_store[i] = key[i];
     }
     CK(cudaGraphLaunch(exec, st));
     ctx->launches += nlaunch;

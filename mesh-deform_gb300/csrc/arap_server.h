@@ -522,6 +522,7 @@ class Server {
             {
                 std::lock_guard<std::mutex> lk(mu_);
                 st_.worker_busy_ms += ms_between(tw0, Clock::now());
+                if (j.kind == Job::Analyze) st_.analyze_ms += ms_between(tw0, Clock::now());
                 done_jobs_.push_back(j);
             }
             cv_.notify_all();
