@@ -47,6 +47,16 @@ typedef enum arap_precision {
     ARAP_PRECISION_MIXED = 1
 } arap_precision;
 
+/* Fill-reducing ordering of the free vertices (arap_set_ordering). */
+typedef enum arap_ordering {
+    /* nested dissection of each constraint set's free vertices (default) */
+    ARAP_ORDER_PER_CONSTRAINT_SET = 0,
+    /* the mesh's own nested dissection (computed once per mesh and shared by
+       contexts made with arap_create_like) restricted to the free vertices:
+       cheaper for a new constraint set, the factor may hold more fill */
+    ARAP_ORDER_MESH = 1
+} arap_ordering;
+
 typedef struct arap_ctx arap_ctx;
 
 /* Human-readable name of a status code. */
@@ -157,6 +167,9 @@ int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas);
    only the order of some sums. Takes effect at the next deform (which sets the
    problem up again). */
 int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes);
+
+/* arap_ordering of the next symbolic analysis (marks the context dirty). */
+int arap_set_ordering(arap_ctx *ctx, int32_t mode);
 
 /* enable != 0 (the default) runs the setup and the iteration sequence as CUDA
    graphs captured on first use and replayed while the problem's size,
@@ -315,6 +328,7 @@ typedef struct arap_server_config {
     int32_t max_queue;           /* waiting requests before submit refuses (0: 65536) */
     int32_t poll_us;             /* completion polling interval of the scheduler (0: 20) */
     int32_t solve_ctas;          /* arap_set_solve_ctas of every context (0: as many as fit) */
+    int32_t per_set_ordering;    /* 1: ARAP_ORDER_PER_CONSTRAINT_SET; 0 (default): ARAP_ORDER_MESH */
 } arap_server_config;
 
 typedef struct arap_request {

@@ -50,7 +50,7 @@ class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("refine_steps", C.c_int32),
                 ("max_in_flight", C.c_int32), ("device_budget_bytes", C.c_int64), ("prep_threads", C.c_int32),
                 ("max_batch", C.c_int32), ("max_queue", C.c_int32), ("poll_us", C.c_int32),
-                ("solve_ctas", C.c_int32)]
+                ("solve_ctas", C.c_int32), ("per_set_ordering", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -104,6 +104,7 @@ SIGNATURES = {
     "arap_set_solve_ctas": (C.c_int, [_P, _I32]),
     "arap_energy": (C.c_int, [_P, _dp]),
     "arap_set_cluster_threshold": (C.c_int, [_P, _I32]),
+    "arap_set_ordering": (C.c_int, [_P, _I32]),
     "arap_pose_targets": (C.c_int, [_P, _I32, _ip, _dp, _I32, _dp]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
     "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
@@ -263,6 +264,10 @@ class ArapContext:
         self._check(self.lib.arap_energy(self.h, C.byref(e)))
         return e.value
 
+    def set_ordering(self, mode: str):
+        """"per_set" (default) or "mesh" (arap_set_ordering)."""
+        self._check(self.lib.arap_set_ordering(self.h, {"per_set": 0, "mesh": 1}[mode]))
+
     def set_cluster_threshold(self, nbytes: int):
         self._check(self.lib.arap_set_cluster_threshold(self.h, int(nbytes)))
 
@@ -371,11 +376,11 @@ class ArapServer:
 
     def __init__(self, device: int = 0, precision: str = "mixed", refine_steps: int = 1, max_in_flight: int = 0,
                  budget_bytes: int = 0, prep_threads: int = 0, max_batch: int = 0, max_queue: int = 0,
-                 poll_us: int = 0, solve_ctas: int = 0):
+                 poll_us: int = 0, solve_ctas: int = 0, per_set_ordering: bool = False):
         self.lib = load()
         cfg = ServerConfig(int(device), PRECISION[precision], int(refine_steps), int(max_in_flight),
                            int(budget_bytes), int(prep_threads), int(max_batch), int(max_queue), int(poll_us),
-                           int(solve_ctas))
+                           int(solve_ctas), int(bool(per_set_ordering)))
         h = _P()
         rc = self.lib.arap_srv_create(C.byref(cfg), C.byref(h))
         if rc != ARAP_OK:

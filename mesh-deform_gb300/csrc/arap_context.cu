@@ -152,6 +152,7 @@ struct arap_ctx {
     bool use_graphs = true;
     int solve_cap = 0;  // most CTAs per triangular-solve launch (0: as many as fit the device)
     int top_bytes = 0;  // supernode size from which tree levels go to the cluster solves (0: default, <0: never)
+    int ordering = ARAP_ORDER_PER_CONSTRAINT_SET;
     // asynchronous deform (arap_deform_async / arap_wait)
     bool in_flight = false;    // a deform was enqueued and not waited for
     int *herr_host = nullptr;  // pinned copy of the device error word
@@ -252,7 +253,7 @@ int analyze_symbolic(arap_ctx *ctx) {
     ctx->sym_host = false;
     std::string err;
     bool singular = false;
-    if (!build_symbolic(ctx->topo, ctx->cmask, ctx->sym, err, singular))
+    if (!build_symbolic(ctx->topo, ctx->cmask, ctx->sym, err, singular, ctx->ordering == ARAP_ORDER_MESH))
         return fail(ctx, singular ? ARAP_ERR_NOT_SPD : ARAP_ERR_CUDA, err);
     ctx->sym_host = true;
     return ARAP_OK;
@@ -780,6 +781,7 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->use_graphs = src->use_graphs;
     ctx->solve_cap = src->solve_cap;
     ctx->top_bytes = src->top_bytes;
+    ctx->ordering = src->ordering;
     return finish_create(ctx, src->device, src, out);
 }
 
@@ -1252,6 +1254,23 @@ int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas) {
     if (max_ctas != ctx->solve_cap) {
         ctx->solve_cap = max_ctas;
         ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
+        ctx->dirty = true;
+    }
+    return ARAP_OK;
+}
+
+int arap_set_ordering(arap_ctx *ctx, int32_t mode) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (mode != ARAP_ORDER_PER_CONSTRAINT_SET && mode != ARAP_ORDER_MESH)
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "unknown ordering mode");
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (mode != ctx->ordering) {
+        ctx->ordering = mode;
+        ctx->sym_host = false;
+        ctx->sym_valid = false;
         ctx->dirty = true;
     }
     return ARAP_OK;

@@ -21,6 +21,7 @@ struct CtxBackend {
     int set_precision(Handle h, int prec, int refine) { return arap_set_precision(h, prec, refine); }
     int set_rest(Handle h, const double *xyz) { return arap_set_rest_positions(h, xyz); }
     int set_solve_ctas(Handle h, int n) { return arap_set_solve_ctas(h, n); }
+    int set_ordering(Handle h, int mode) { return arap_set_ordering(h, mode); }
     int set_constraints(Handle h, int n, const int32_t *idx, const double *xyz) {
         return arap_set_constraints(h, n, idx, xyz);
     }

@@ -7,7 +7,7 @@
 //   int  create(int V, int F, const int32_t*, Handle*); create_like(Handle, Handle*)
 //   void destroy(Handle)
 //   int  set_precision(Handle, int, int); set_rest(Handle, const double*)
-//   int  set_solve_ctas(Handle, int)
+//   int  set_solve_ctas(Handle, int); set_ordering(Handle, int)
 //   int  set_constraints(Handle, int, const int32_t*, const double*)
 //   int  set_targets(Handle, int, const double*)
 //   int  plan_bytes(Handle, int n_poses, int64_t*); int64_t device_bytes(Handle)
@@ -160,6 +160,8 @@ class Server {
         if (rc != ARAP_OK) return fail_rc(rc, "mesh context: " + b_.last_error(Handle{}));
         rc = b_.set_precision(m->proto, cfg_.precision, cfg_.refine_steps);
         if (rc == ARAP_OK) rc = b_.set_solve_ctas(m->proto, cfg_.solve_ctas);
+        if (rc == ARAP_OK)
+            rc = b_.set_ordering(m->proto, cfg_.per_set_ordering ? ARAP_ORDER_PER_CONSTRAINT_SET : ARAP_ORDER_MESH);
         if (rc == ARAP_OK) rc = b_.set_rest(m->proto, rest);
         if (rc != ARAP_OK) {
             const std::string e = b_.last_error(m->proto);

@@ -246,7 +246,7 @@ void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int3
 // ---------------------------------------------------------------------------
 
 bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
-                    std::string &err, bool &singular) {
+                    std::string &err, bool &singular, bool mesh_order) {
     singular = false;
     sym = Symbolic();
     const int V = topo.V;
@@ -294,7 +294,34 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
             }
         }
     }
-    nd_order(m, grow.data(), gcol.data(), sym.perm, sym.block_ptr);
+    if (!mesh_order) {
+        nd_order(m, grow.data(), gcol.data(), sym.perm, sym.block_ptr);
+    } else {
+        MeshOrder &mo = *topo.mesh_order;
+        {
+            std::lock_guard<std::mutex> lk(mo.mu);
+            if (!mo.ready) {
+                // the mesh graph without self entries
+                std::vector<int32_t> mrow(V + 1, 0), mcol;
+                mcol.reserve(topo.col.size());
+                for (int v = 0; v < V; ++v) {
+                    for (int32_t q = topo.rowptr[v]; q < topo.rowptr[v + 1]; ++q)
+                        if (topo.col[q] != v) mcol.push_back(topo.col[q]);
+                    mrow[v + 1] = (int32_t)mcol.size();
+                }
+                nd_order(V, mrow.data(), mcol.data(), mo.perm, mo.block_ptr);
+                mo.ready = true;
+            }
+        }
+        sym.perm.clear();
+        sym.perm.reserve(m);
+        sym.block_ptr.assign(1, 0);
+        for (size_t b = 0; b + 1 < mo.block_ptr.size(); ++b) {
+            for (int32_t k = mo.block_ptr[b]; k < mo.block_ptr[b + 1]; ++k)
+                if (!constrained[mo.perm[k]]) sym.perm.push_back(fidx[mo.perm[k]]);
+            if ((int32_t)sym.perm.size() > sym.block_ptr.back()) sym.block_ptr.push_back((int32_t)sym.perm.size());
+        }
+    }
     std::vector<int32_t> iperm(m);
     for (int k = 0; k < m; ++k) iperm[sym.perm[k]] = k;
     // device order: free vertices in elimination order, then constrained ascending

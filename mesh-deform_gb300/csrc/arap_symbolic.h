@@ -7,6 +7,8 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -26,8 +28,19 @@ constexpr int kDiagBlock = 32;
 // direction (a face whose corners repeat contributes a self entry, as in the
 // reference). For every CSR entry, the faces that contribute to its weight, in
 // face order (setFromTriplets sums duplicates in insertion order).
+// Nested dissection of the whole mesh (constrained vertices included), made
+// once on first use and shared by every context of the mesh (copies of a
+// Topology share it).
+struct MeshOrder {
+    std::mutex mu;
+    bool ready = false;
+    std::vector<int32_t> perm;       // V: vertex eliminated k-th
+    std::vector<int32_t> block_ptr;  // blocks of the dissection
+};
+
 struct Topology {
     int V = 0, F = 0;
+    std::shared_ptr<MeshOrder> mesh_order = std::make_shared<MeshOrder>();
     std::vector<int32_t> faces;      // 3F
     std::vector<int32_t> rowptr;     // V+1
     std::vector<int32_t> col;        // nnz
@@ -114,8 +127,11 @@ struct Symbolic {
 // Builds the symbolic analysis for a constrained-vertex set. Returns false and
 // sets err when the free graph has a component that touches no constrained
 // vertex (the constrained Laplacian is then singular).
+// mesh_order: order the free vertices by the mesh's own dissection restricted
+// to them (one dissection per mesh instead of one per constraint set; blocks
+// left empty are dropped) instead of dissecting the free graph.
 bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
-                    std::string &err, bool &singular);
+                    std::string &err, bool &singular, bool mesh_order = false);
 
 // Nested-dissection order of a symmetric graph (no self loops); exposed for tests.
 void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int32_t> &perm,

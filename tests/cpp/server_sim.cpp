@@ -79,6 +79,7 @@ struct FakeBackend {
     }
     int set_precision(Handle, int, int) { return ARAP_OK; }
     int set_solve_ctas(Handle, int) { return ARAP_OK; }
+    int set_ordering(Handle, int) { return ARAP_OK; }
     int set_rest(Handle h, const double *xyz) {
         h->rest.assign(xyz, xyz + 3 * (size_t)h->V);
         return ARAP_OK;

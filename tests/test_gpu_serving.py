@@ -21,10 +21,13 @@ def small_pool():
     return pool
 
 
-def lone(gpu, mesh, req, precision):
-    """The request on a fresh context, as a plain arap_deform."""
+def lone(gpu, mesh, req, precision, ordering="mesh"):
+    """The request on a fresh context, as a plain arap_deform (with the
+    server's default ordering: the mesh's dissection restricted to the free
+    vertices)."""
     with gpu.ArapContext(mesh.V, mesh.faces) as ctx:
         ctx.set_precision(precision, 1)
+        ctx.set_ordering(ordering)
         ctx.set_rest_positions(mesh.positions)
         ctx.set_constraints(req.cidx, req.ctargets)
         return ctx.deform(req.iterations)
@@ -161,6 +164,24 @@ def test_budget_evicts_cold_factors(gpu):
     srv.close()
     assert st["evictions"] >= 3
     assert st["peak_resident_bytes"] <= budget
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_mesh_ordering_matches_oracle(gpu, precision, tol):
+    """ARAP_ORDER_MESH (one dissection per mesh, restricted to each constraint
+    set's free vertices) changes only the factor's ordering: the positions
+    stay within the form's tolerance of the oracle, for several constraint
+    sets on one mesh."""
+    pool = small_pool()
+    m = max(pool, key=lambda x: x.V)
+    reqs = W.serving_requests([m], 3, seed=9, reuse=0.0, it_range=(5, 5), max_handles=3)
+    for r in reqs:
+        got = lone(gpu, m, r, precision, "mesh")
+        per_set = lone(gpu, m, r, precision, "per_set")
+        ok, o = O.run_deform(m.positions, m.faces, r.cidx, r.ctargets, r.iterations)
+        assert ok
+        assert err(got, o, m.positions) <= tol
+        assert err(per_set, o, m.positions) <= tol
 
 
 def test_errors_reach_their_request(gpu):
