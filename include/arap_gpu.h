@@ -146,6 +146,14 @@ int arap_wait(arap_ctx *ctx);
    arap_query). */
 int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *targets, int32_t iterations,
                             double *out_xyz);
+/* Completion notification: fn(user) is called on a CUDA runtime thread once
+   each later asynchronous deform has finished on the device (its results
+   copied). fn must return quickly and call neither CUDA nor arap_*; the
+   caller then collects the status with arap_wait or arap_query. NULL removes
+   it. */
+typedef void (*arap_done_fn)(void *user);
+int arap_set_done_callback(arap_ctx *ctx, arap_done_fn fn, void *user);
+
 /* Non-blocking completion check of a pending asynchronous deform: *done = 0
    while it runs (returns ARAP_OK); otherwise *done = 1 and the return value
    is what arap_wait returns. */

@@ -105,6 +105,7 @@ SIGNATURES = {
     "arap_energy": (C.c_int, [_P, _dp]),
     "arap_set_cluster_threshold": (C.c_int, [_P, _I32]),
     "arap_set_ordering": (C.c_int, [_P, _I32]),
+    "arap_set_done_callback": (C.c_int, [_P, _P, _P]),
     "arap_pose_targets": (C.c_int, [_P, _I32, _ip, _dp, _I32, _dp]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
     "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),

@@ -153,6 +153,8 @@ struct arap_ctx {
     int solve_cap = 0;  // most CTAs per triangular-solve launch (0: as many as fit the device)
     int top_bytes = 0;  // supernode size from which tree levels go to the cluster solves (0: default, <0: never)
     int ordering = ARAP_ORDER_PER_CONSTRAINT_SET;
+    arap_done_fn done_fn = nullptr;  // called from a CUDA thread when an async deform finished
+    void *done_user = nullptr;
     // asynchronous deform (arap_deform_async / arap_wait)
     bool in_flight = false;    // a deform was enqueued and not waited for
     int *herr_host = nullptr;  // pinned copy of the device error word
@@ -1012,6 +1014,7 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
     }
     CK(cudaMemcpyAsync(ctx->herr_host, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->ev_done, st));
+    if (ctx->done_fn) CK(cudaLaunchHostFunc(st, ctx->done_fn, ctx->done_user));
     CK(cudaGetLastError());
     ctx->in_flight = true;
     ctx->poses_in_flight = true;
@@ -1192,6 +1195,7 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     }
     CK(cudaMemcpyAsync(ctx->herr_host, ctx->errw.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->ev_done, st));
+    if (ctx->done_fn) CK(cudaLaunchHostFunc(st, ctx->done_fn, ctx->done_user));
     CK(cudaGetLastError());
     ctx->in_flight = true;
     ctx->poses_in_flight = false;
@@ -1222,6 +1226,17 @@ int arap_wait(arap_ctx *ctx) {
         ctx->bS = -1;
         return fail(ctx, ARAP_ERR_TIMEOUT, "a bounded in-kernel wait expired");
     }
+    return ARAP_OK;
+}
+
+int arap_set_done_callback(arap_ctx *ctx, arap_done_fn fn, void *user) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    ctx->done_fn = fn;
+    ctx->done_user = user;
     return ARAP_OK;
 }
 

@@ -13,6 +13,7 @@ namespace {
 // Backend of the scheduler: the library's contexts, pinned host staging.
 struct CtxBackend {
     using Handle = arap_ctx *;
+    static constexpr bool kCallbacks = true;
     int device = 0;
 
     int create(int V, int F, const int32_t *faces, Handle *h) { return arap_create(V, F, faces, device, h); }
@@ -33,6 +34,7 @@ struct CtxBackend {
         return arap_deform_poses_async(h, P, tgt, iters, out);
     }
     int query(Handle h, int32_t *done) { return arap_query(h, done); }
+    int set_done_callback(Handle h, void (*fn)(void *), void *user) { return arap_set_done_callback(h, fn, user); }
     double device_ms(Handle h) {
         double a = 0.0, b = 0.0;
         return arap_get_timing(h, &a, &b) == ARAP_OK ? a + b : 0.0;

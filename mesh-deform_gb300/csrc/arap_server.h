@@ -15,6 +15,8 @@
 //   int  deform_poses_async(Handle, int P, const double* targets, int iters, double* out)
 //   int  query(Handle, int32_t* done)               non-blocking completion
 //   double device_ms(Handle)                        device time of the last launch
+//   static constexpr bool kCallbacks; set_done_callback(Handle, void (*)(void*), void*)
+//                                                   completion callbacks (else polling)
 //   std::string last_error(Handle)
 //   void* alloc_host(size_t); void free_host(void*)  staging for results
 //   int64_t default_budget()
@@ -103,6 +105,10 @@ class Server {
         std::vector<double> batch_targets;
         double *staging = nullptr;
         size_t staging_doubles = 0;
+        struct Tag {
+            Server *srv;
+            Slot *slot;
+        } tag{nullptr, nullptr};  // completion-callback argument
         int job_rc = ARAP_OK;     // written by a worker, read by the scheduler after the job
         std::string job_err;
         int64_t job_need = 0, job_bytes = 0;
@@ -506,6 +512,10 @@ class Server {
                 } else {
                     s->ctx = h;
                     s->have_ctx = true;
+                    if (B::kCallbacks) {
+                        s->tag = {this, s};
+                        b_.set_done_callback(h, &Server::on_done, &s->tag);
+                    }
                     std::vector<double> tgt(3 * s->idx.size());
                     for (size_t i = 0; i < s->idx.size(); ++i)
                         std::memcpy(&tgt[3 * i], &m.rest[3 * (size_t)s->idx[i]], 3 * sizeof(double));
@@ -555,9 +565,35 @@ class Server {
     }
 
     // ---- completion ----------------------------------------------------------
-    void poll_busy() {
-        for (size_t i = 0; i < slots_.size(); ++i) {
-            Slot *s = slots_[i].get();
+    // Completion callback (a CUDA runtime thread): queue the slot for the scheduler.
+    static void on_done(void *user) {
+        auto *t = static_cast<typename Slot::Tag *>(user);
+        {
+            std::lock_guard<std::mutex> lk(t->srv->mu_);
+            t->srv->done_slots_.push_back(t->slot);
+        }
+        t->srv->cv_.notify_all();
+    }
+
+    // Collects finished launches: the slots the completion callbacks named
+    // (a notification that arrives before its launch job is marked done waits
+    // for the next round), and every busy slot when there are no callbacks or
+    // a full check is due.
+    void poll_busy(bool full) {
+        std::vector<Slot *> check;
+        if (full) {
+            for (auto &p : slots_)
+                if (p->state == SlotState::Busy) check.push_back(p.get());
+            notified_.clear();
+        } else {
+            std::vector<Slot *> keep;
+            for (Slot *s : notified_) {
+                if (s->state == SlotState::Busy) check.push_back(s);
+                else if (s->state == SlotState::Launching) keep.push_back(s);
+            }
+            notified_.swap(keep);
+        }
+        for (Slot *s : check) {
             if (s->state != SlotState::Busy) continue;
             int32_t done = 0;
             const int rc = b_.query(s->ctx, &done);
@@ -587,8 +623,8 @@ class Server {
             } else {
                 // a failed factorisation (or an expired wait) leaves nothing worth keeping
                 fail_key(s, rc, err);
+                notified_.erase(std::remove(notified_.begin(), notified_.end(), s), notified_.end());
                 remove_slot(s);
-                --i;
             }
         }
         std::lock_guard<std::mutex> lk(mu_);
@@ -767,17 +803,27 @@ class Server {
             bool stopping;
             {
                 std::unique_lock<std::mutex> lk(mu_);
-                auto ready = [&] { return stop_ || !incoming_.empty() || !done_jobs_.empty(); };
-                if (inflight_ > 0) cv_.wait_for(lk, std::chrono::microseconds(cfg_.poll_us), ready);
+                auto ready = [&] {
+                    return stop_ || !incoming_.empty() || !done_jobs_.empty() || !done_slots_.empty();
+                };
+                // with completion callbacks the scheduler sleeps until one
+                // arrives (checking every busy slot now and then regardless)
+                const auto wait = B::kCallbacks ? std::chrono::microseconds(2000)
+                                                : std::chrono::microseconds(cfg_.poll_us);
+                if (inflight_ > 0) cv_.wait_for(lk, wait, ready);
                 else if (!ready()) cv_.wait(lk, ready);
                 fresh.swap(incoming_);
                 finished.swap(done_jobs_);
+                notified_.insert(notified_.end(), done_slots_.begin(), done_slots_.end());
+                done_slots_.clear();
                 stopping = stop_;
             }
             const auto t0 = Clock::now();
             for (Req *q : fresh) pending_.push_back(q);
             for (const Job &j : finished) job_done(j);
-            poll_busy();
+            const bool full = !B::kCallbacks || t0 - last_full_poll_ > std::chrono::milliseconds(2);
+            if (full) last_full_poll_ = t0;
+            poll_busy(full);
             schedule();
             {
                 int waiting = (int)pending_.size();
@@ -803,6 +849,7 @@ class Server {
     std::vector<std::unique_ptr<MeshRec>> meshes_;
     std::deque<Req *> incoming_;
     std::deque<Job> jobs_, done_jobs_;
+    std::vector<Slot *> done_slots_;  // named by completion callbacks
     std::unordered_map<int64_t, Req *> tickets_;
     int64_t next_ticket_ = 1;
     int queued_ = 0;
@@ -811,6 +858,8 @@ class Server {
     std::list<Req *> pending_;
     std::vector<std::unique_ptr<Slot>> slots_;
     std::unordered_map<uint64_t, std::vector<Slot *>> cache_;
+    std::vector<Slot *> notified_;  // finished according to a callback, not collected yet
+    Clock::time_point last_full_poll_{};
     std::map<size_t, std::vector<double *>> staging_pool_;
     int64_t resident_ = 0;
     std::atomic<int64_t> mesh_bytes_{0};

@@ -14,6 +14,10 @@
 
 #include "arap_server.h"
 
+#ifndef CALLBACKS
+#define CALLBACKS 0
+#endif
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -32,6 +36,9 @@ struct FakeCtx {
     std::vector<double> ptgt;
     int pending_rc = ARAP_OK;
     std::string err;
+    std::thread notifier;  // completion-callback thread of the last deform
+    void (*fn)(void *) = nullptr;
+    void *user = nullptr;
 };
 
 struct Model {
@@ -43,9 +50,12 @@ struct Model {
 // Device model: topology 64 B per vertex, a factor of 512 B per vertex, 256 B
 // per vertex and pose for multi-pose launches; 50 us per iteration. A
 // constraint set whose first vertex is V-1 is singular; 13 iterations make
-// the deform fail with an expired wait.
-struct FakeBackend {
+// the deform fail with an expired wait. CB: completion callbacks from a
+// thread of the model (as the CUDA runtime calls them), else polling only.
+template <bool CB>
+struct FakeBackendT {
     using Handle = FakeCtx *;
+    static constexpr bool kCallbacks = CB;
     Model *m;
 
     void add_bytes(FakeCtx *c, int64_t b) {
@@ -72,6 +82,7 @@ struct FakeBackend {
     }
     void destroy(Handle h) {
         if (!h) return;
+        if (h->notifier.joinable()) h->notifier.join();
         add_bytes(h, 0);
         std::lock_guard<std::mutex> lk(m->mu);
         --m->live;
@@ -80,6 +91,11 @@ struct FakeBackend {
     int set_precision(Handle, int, int) { return ARAP_OK; }
     int set_solve_ctas(Handle, int) { return ARAP_OK; }
     int set_ordering(Handle, int) { return ARAP_OK; }
+    int set_done_callback(Handle h, void (*fn)(void *), void *user) {
+        h->fn = fn;
+        h->user = user;
+        return ARAP_OK;
+    }
     int set_rest(Handle h, const double *xyz) {
         h->rest.assign(xyz, xyz + 3 * (size_t)h->V);
         return ARAP_OK;
@@ -114,9 +130,21 @@ struct FakeBackend {
         h->out = out;
         h->P = P;
         h->pending_rc = iters == 13 ? ARAP_ERR_TIMEOUT : ARAP_OK;
-        std::lock_guard<std::mutex> lk(m->mu);
-        ++m->in_flight;
-        m->max_in_flight = std::max(m->max_in_flight, m->in_flight);
+        {
+            std::lock_guard<std::mutex> lk(m->mu);
+            ++m->in_flight;
+            m->max_in_flight = std::max(m->max_in_flight, m->in_flight);
+        }
+        if (CB && h->fn) {
+            if (h->notifier.joinable()) h->notifier.join();
+            const auto when = h->t_done;
+            auto fn = h->fn;
+            void *user = h->user;
+            h->notifier = std::thread([when, fn, user] {
+                std::this_thread::sleep_until(when);
+                fn(user);
+            });
+        }
         return ARAP_OK;
     }
     int deform_async(Handle h, int iters, double *out) {
@@ -161,6 +189,7 @@ struct FakeBackend {
 };
 
 int failures = 0;
+using FakeBackend = FakeBackendT<CALLBACKS>;
 #define CHECK(cond, what)                                                        \
     do {                                                                         \
         if (!(cond)) {                                                           \
@@ -413,6 +442,7 @@ int main() {
     test_admission_and_eviction();
     test_errors();
     test_concurrent_clients();
+    std::printf("completion callbacks: %d\n", CALLBACKS);
     std::printf(failures ? "FAILED %d\n" : "ALL PASSED\n", failures);
     return failures ? 1 : 0;
 }

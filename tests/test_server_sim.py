@@ -11,12 +11,16 @@ import pytest
 ROOT = Path(__file__).resolve().parent.parent
 
 
-def test_scheduler_on_host_model(tmp_path):
+@pytest.mark.parametrize("callbacks", [0, 1])
+def test_scheduler_on_host_model(tmp_path, callbacks):
+    """callbacks=1: completions announced by callbacks from another thread, as
+    the CUDA runtime does; 0: found by polling."""
     gxx = shutil.which("g++")
     if not gxx:
         pytest.skip("g++ not available")
     exe = tmp_path / "server_sim"
-    subprocess.run([gxx, "-O2", "-std=c++17", "-pthread", f"-I{ROOT / 'mesh-deform_gb300' / 'csrc'}",
+    subprocess.run([gxx, "-O2", "-std=c++17", "-pthread", f"-DCALLBACKS={callbacks}",
+                    f"-I{ROOT / 'mesh-deform_gb300' / 'csrc'}",
                     str(ROOT / "tests" / "cpp" / "server_sim.cpp"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
