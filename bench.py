@@ -429,7 +429,7 @@ def run_serving(args):
                "stats": {k: st[k] for k in ("factor_hits", "factor_misses", "evictions", "launches",
                                              "batched_launches", "batched_requests", "peak_resident_bytes",
                                              "budget_bytes", "scheduler_busy_ms", "worker_busy_ms", "analyze_ms",
-                                             "device_ms")},
+                                             "staging_ms", "device_ms")},
                "device_spans_in_flight_avg": st["device_ms"] / (1e3 * wall),
                "scheduler_busy_frac": st["scheduler_busy_ms"] / (1e3 * wall),
                "clocks": clk}
@@ -519,7 +519,7 @@ def main():
     ap.add_argument("--serve-rates", default="50,100,200,0",
                     help="serving: Poisson arrival rates in requests/s (0: all requests at once)")
     ap.add_argument("--serve-requests", type=int, default=400)
-    ap.add_argument("--serve-in-flight", type=int, default=16)
+    ap.add_argument("--serve-in-flight", type=int, default=4)
     ap.add_argument("--serve-prep-threads", type=int, default=min(12, os.cpu_count() or 4))
     ap.add_argument("--serve-max-batch", type=int, default=64)
     ap.add_argument("--serve-check", type=int, default=40, help="serving: results checked against the oracle")

@@ -203,6 +203,12 @@ int arap_set_targets(arap_ctx *ctx, int32_t n, const double *xyz);
    local/global iteration decreases; the reference does not compute it. */
 int arap_energy(arap_ctx *ctx, double *energy);
 
+/* Host time of the last arap_deform_async, in ms, by phase: symbolic
+   analysis and its upload, device allocation, set-up enqueue, iteration
+   enqueue, the rest (gather, copies). The phases of a non-dirty deform are 0
+   but for the last two. */
+int arap_get_host_timing(arap_ctx *ctx, double *ms5);
+
 /* Device memory held by the context, in bytes. */
 int64_t arap_device_bytes(const arap_ctx *ctx);
 /* Device memory the context will hold after its next arap_deform
@@ -329,7 +335,8 @@ typedef struct arap_server_config {
     int32_t device;
     int32_t precision;           /* arap_precision of every request (ARAP_PRECISION_MIXED) */
     int32_t refine_steps;        /* MIXED refinement solves per iteration (1) */
-    int32_t max_in_flight;       /* launches on the device at once (0: 16) */
+    int32_t max_in_flight;       /* launches on the device at once (0: 4; more in flight made the
+                                    measured serving stream slower, not faster) */
     int64_t device_budget_bytes; /* resident device memory limit (0: 80% of the free memory) */
     int32_t prep_threads;        /* host threads for analysis and first launches (0: 4) */
     int32_t max_batch;           /* most requests per multi-pose launch (0: 64; 1: no batching) */
@@ -367,6 +374,7 @@ typedef struct arap_server_stats {
     double scheduler_busy_ms;  /* scheduler thread time outside its waits */
     double worker_busy_ms;     /* prep-thread time in analyses and first launches */
     double analyze_ms;         /* of which: contexts created, constraint sets analysed */
+    double staging_ms;         /* scheduler time allocating pinned result buffers */
     double device_ms;          /* sum over launches of their device time (set-up + iterations) */
 } arap_server_stats;
 

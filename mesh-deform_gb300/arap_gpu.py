@@ -69,7 +69,8 @@ class ServerStats(C.Structure):
                                          "batched_requests", "iterations_done", "resident_bytes",
                                          "peak_resident_bytes", "budget_bytes")] + \
         [(n, C.c_int32) for n in ("resident_factors", "queue_depth", "in_flight", "pad")] + \
-        [(n, C.c_double) for n in ("scheduler_busy_ms", "worker_busy_ms", "analyze_ms", "device_ms")]
+        [(n, C.c_double) for n in ("scheduler_busy_ms", "worker_busy_ms", "analyze_ms", "staging_ms",
+                                             "device_ms")]
 
 
 SIGNATURES = {
@@ -106,6 +107,7 @@ SIGNATURES = {
     "arap_set_cluster_threshold": (C.c_int, [_P, _I32]),
     "arap_set_ordering": (C.c_int, [_P, _I32]),
     "arap_set_done_callback": (C.c_int, [_P, _P, _P]),
+    "arap_get_host_timing": (C.c_int, [_P, _dp]),
     "arap_pose_targets": (C.c_int, [_P, _I32, _ip, _dp, _I32, _dp]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
     "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
@@ -259,6 +261,11 @@ class ArapContext:
         self._check(self.lib.arap_pose_targets(self.h, len(h), _i32(h), _f64(o) if o is not None else None,
                                                len(t), _f64(t)))
         self._nposes = len(t)
+
+    def host_timing(self) -> dict:
+        v = np.zeros(5)
+        self._check(self.lib.arap_get_host_timing(self.h, _f64(v)))
+        return dict(zip(("analysis_upload", "alloc", "setup_enqueue", "iter_enqueue", "rest"), v.tolist()))
 
     def energy(self) -> float:
         e = C.c_double()

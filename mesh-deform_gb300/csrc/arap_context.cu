@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -155,6 +156,9 @@ struct arap_ctx {
     int ordering = ARAP_ORDER_PER_CONSTRAINT_SET;
     arap_done_fn done_fn = nullptr;  // called from a CUDA thread when an async deform finished
     void *done_user = nullptr;
+    // host time of the last arap_deform_async, ms: analysis + uploads,
+    // allocation, set-up enqueue, iteration enqueue, rest
+    double host_ms[5] = {0, 0, 0, 0, 0};
     // asynchronous deform (arap_deform_async / arap_wait)
     bool in_flight = false;    // a deform was enqueued and not waited for
     int *herr_host = nullptr;  // pinned copy of the device error word
@@ -1134,6 +1138,12 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     ctx->setup_ms = ctx->iter_ms = 0.0;
     ctx->model_P = ctx->model_T = 1;
     const bool fp64 = ctx->precision == ARAP_PRECISION_FP64;
+    using HClock = std::chrono::steady_clock;
+    auto hms = [](HClock::time_point a, HClock::time_point b) {
+        return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    const auto h0 = HClock::now();
+    auto h1 = h0, h2 = h0, h3 = h0, h4 = h0;
     CK(cudaEventRecord(ctx->ev0, st));
     CK(cudaMemsetAsync(ctx->errw.p, 0, sizeof(int), st));
     if (ctx->dirty) {
@@ -1153,8 +1163,10 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         }
         int rc = prepare_symbolic(ctx);
         if (rc != ARAP_OK) return rc;
+        h1 = HClock::now();
         rc = fp64 ? setup_alloc<double>(ctx) : setup_alloc<float>(ctx);
         if (rc != ARAP_OK) return rc;
+        h2 = HClock::now();
         const int64_t key[4] = {ctx->gen, fp64 ? 1 : 2, 0, 0};
         rc = graph_or_direct(ctx, ctx->g_setup, ctx->g_setup_key, key, ctx->g_setup_launches, [&] {
             return fp64 ? setup_enqueue<double>(ctx) : setup_enqueue<float>(ctx);
@@ -1170,6 +1182,9 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         if (rc != ARAP_OK) return rc;
         ctx->retarget = false;
     }
+    h1 = std::max(h1, h0);
+    h2 = std::max(h2, h1);
+    h3 = HClock::now();
     CK(cudaEventRecord(ctx->ev1, st));
     for (int left = iterations; left > 0;) {
         const bool it64 = ctx->state_prec == ARAP_PRECISION_FP64;
@@ -1183,6 +1198,7 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         if (rc != ARAP_OK) return rc;
         left -= n;
     }
+    h4 = HClock::now();
     CK(cudaEventRecord(ctx->ev2, st));
     if (out_xyz) {
         {
@@ -1199,6 +1215,18 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     CK(cudaGetLastError());
     ctx->in_flight = true;
     ctx->poses_in_flight = false;
+    const auto h5 = HClock::now();
+    ctx->host_ms[0] = hms(h0, h1);
+    ctx->host_ms[1] = hms(h1, h2);
+    ctx->host_ms[2] = hms(h2, h3);
+    ctx->host_ms[3] = hms(h3, h4);
+    ctx->host_ms[4] = hms(h4, h5);
+    return ARAP_OK;
+}
+
+int arap_get_host_timing(arap_ctx *ctx, double *ms5) {
+    if (check_ctx(ctx) || !ms5) return ARAP_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 5; ++i) ms5[i] = ctx->host_ms[i];
     return ARAP_OK;
 }
 

@@ -122,7 +122,7 @@ class Server {
 
   public:
     Server(B backend, const arap_server_config &cfg) : b_(std::move(backend)), cfg_(cfg) {
-        if (cfg_.max_in_flight <= 0) cfg_.max_in_flight = 16;
+        if (cfg_.max_in_flight <= 0) cfg_.max_in_flight = 4;
         if (cfg_.prep_threads <= 0) cfg_.prep_threads = 4;
         if (cfg_.max_batch <= 0) cfg_.max_batch = 64;
         if (cfg_.max_queue <= 0) cfg_.max_queue = 65536;
@@ -305,7 +305,11 @@ class Server {
             v.pop_back();
             return p;
         }
-        return static_cast<double *>(b_.alloc_host(cls * sizeof(double)));
+        const auto t0 = Clock::now();
+        double *p = static_cast<double *>(b_.alloc_host(cls * sizeof(double)));
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.staging_ms += ms_between(t0, Clock::now());
+        return p;
     }
     void staging_put(double *p, size_t doubles) {
         if (!p) return;
