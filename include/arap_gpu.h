@@ -209,6 +209,21 @@ int arap_energy(arap_ctx *ctx, double *energy);
    but for the last two. */
 int arap_get_host_timing(arap_ctx *ctx, double *ms5);
 
+/* Vertex normals of the current deformed positions, computed on the device
+   as OpenMesh's update_normals does before display
+   (examples/osg_viewer.cpp:53,60-62): face normal = normalised
+   (p1 - p0) x (p2 - p0), vertex normal = normalised sum of the normals of its
+   faces. normals_xyz: V x 3 doubles (host). */
+int arap_vertex_normals(arap_ctx *ctx, double *normals_xyz);
+
+/* The current deformed positions (and, with_normals != 0, their vertex
+   normals) in vertex order, V x 3 doubles each, left in device memory owned
+   by the context: the pointers stay valid until the next call on the context.
+   For consumers on the same device (rendering, further kernels) that need no
+   host copy. Ready when the call returns. */
+int arap_device_positions(arap_ctx *ctx, int32_t with_normals, const double **positions_device,
+                          const double **normals_device);
+
 /* Device memory held by the context, in bytes. */
 int64_t arap_device_bytes(const arap_ctx *ctx);
 /* Device memory the context will hold after its next arap_deform

@@ -108,6 +108,8 @@ SIGNATURES = {
     "arap_set_ordering": (C.c_int, [_P, _I32]),
     "arap_set_done_callback": (C.c_int, [_P, _P, _P]),
     "arap_get_host_timing": (C.c_int, [_P, _dp]),
+    "arap_vertex_normals": (C.c_int, [_P, _dp]),
+    "arap_device_positions": (C.c_int, [_P, _I32, C.POINTER(_P), C.POINTER(_P)]),
     "arap_pose_targets": (C.c_int, [_P, _I32, _ip, _dp, _I32, _dp]),
     "arap_set_targets": (C.c_int, [_P, _I32, _dp]),
     "arap_deform_poses_async": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
@@ -164,6 +166,17 @@ def _i32(a):
 
 def _f64(a):
     return a.ctypes.data_as(_dp)
+
+
+class DeviceArray:
+    """A V x 3 float64 array in device memory owned by a context, exposed
+    through __cuda_array_interface__ (read-only view, no copy)."""
+
+    def __init__(self, ptr: int, shape):
+        self.ptr = int(ptr)
+        self.shape = tuple(shape)
+        self.__cuda_array_interface__ = {"shape": self.shape, "typestr": "<f8", "data": (self.ptr, True),
+                                         "version": 3, "strides": None}
 
 
 class ArapContext:
@@ -261,6 +274,20 @@ class ArapContext:
         self._check(self.lib.arap_pose_targets(self.h, len(h), _i32(h), _f64(o) if o is not None else None,
                                                len(t), _f64(t)))
         self._nposes = len(t)
+
+    def vertex_normals(self) -> np.ndarray:
+        out = np.empty((self.V, 3), np.float64)
+        self._check(self.lib.arap_vertex_normals(self.h, _f64(out)))
+        return out
+
+    def device_positions(self, with_normals: bool = False):
+        """(positions, normals) as DeviceArray views of the context's device
+        buffers (no host copy; normals None unless asked); valid until the next
+        call on the context. torch.as_tensor(view, device="cuda") wraps them."""
+        p, n = _P(), _P()
+        self._check(self.lib.arap_device_positions(self.h, int(bool(with_normals)), C.byref(p), C.byref(n)))
+        pos = DeviceArray(p.value, (self.V, 3))
+        return pos, (DeviceArray(n.value, (self.V, 3)) if with_normals else None)
 
     def host_timing(self) -> dict:
         v = np.zeros(5)

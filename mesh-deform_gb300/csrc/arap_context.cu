@@ -136,6 +136,7 @@ struct arap_ctx {
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T, redge;
     DevBuf errw, ticket, flags, energy;
     DevBuf cidx_dev, handle_dev, tabs_dev;  // arap_pose_targets inputs
+    DevBuf vf_ptr, vf_face, fnorm, vnorm;    // vertex normals
     // many-pose state (arap_deform_poses)
     DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
     int bP = 0, bT = 0, bS = -1, bpt = 0;
@@ -182,7 +183,8 @@ struct arap_ctx {
         return {&faces, &ent_ptr, &ent_fc, &hc, &w_orig, &rest, &targets, &out, &drow, &dcol, &dent, &oldidx,
                 &amap, &dmap, &sn, &rows, &relind, &child, &level_sn, &fitems, &w64, &w32, &p64, &pc64, &p32,
                 &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
-                &errw, &ticket, &flags, &energy, &cidx_dev, &handle_dev, &tabs_dev, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
+                &errw, &ticket, &flags, &energy, &cidx_dev, &handle_dev, &tabs_dev, &vf_ptr, &vf_face, &fnorm,
+                &vnorm, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
                 &bticket, &bflags};
     }
 };
@@ -1371,6 +1373,62 @@ int arap_energy(arap_ctx *ctx, double *energy) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(energy, scratch + np, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return ARAP_OK;
+}
+
+namespace {
+// Deformed positions (vertex order) into ctx->out and their vertex normals into
+// ctx->vnorm, on the context's stream.
+int enqueue_positions_normals(arap_ctx *ctx, bool normals) {
+    cudaStream_t st = ctx->stream;
+    launch_gather_positions(ctx->ds, ctx->pc64.as<Vec4<double>>(), ctx->out.as<double>(), st);
+    if (normals) {
+        const Topology &t = ctx->topo;
+        if (!ctx->vf_ptr.p || ctx->vf_ptr.cap < t.vf_ptr.size() * sizeof(int32_t)) {
+            CK(upload(ctx->vf_ptr, t.vf_ptr, st));
+            CK(upload(ctx->vf_face, t.vf_face, st));
+        }
+        CK(ctx->fnorm.ensure((size_t)3 * std::max(t.F, 1) * sizeof(double)));
+        CK(ctx->vnorm.ensure((size_t)3 * std::max(t.V, 1) * sizeof(double)));
+        launch_vertex_normals(t.V, t.F, ctx->faces.as<int32_t>(), ctx->vf_ptr.as<int32_t>(),
+                              ctx->vf_face.as<int32_t>(), ctx->out.as<double>(), ctx->fnorm.as<double>(),
+                              ctx->vnorm.as<double>(), st);
+    }
+    CK(cudaGetLastError());
+    return ARAP_OK;
+}
+}  // namespace
+
+int arap_vertex_normals(arap_ctx *ctx, double *normals_xyz) {
+    if (check_ctx(ctx) || !normals_xyz) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (!ctx->sym_valid || ctx->state_prec < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no deformed state yet");
+    CK(cudaSetDevice(ctx->device));
+    const int rc = enqueue_positions_normals(ctx, true);
+    if (rc != ARAP_OK) return rc;
+    CK(cudaMemcpyAsync(normals_xyz, ctx->vnorm.p, (size_t)3 * ctx->topo.V * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ARAP_OK;
+}
+
+int arap_device_positions(arap_ctx *ctx, int32_t with_normals, const double **positions_device,
+                          const double **normals_device) {
+    if (check_ctx(ctx) || !positions_device) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (!ctx->sym_valid || ctx->state_prec < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no deformed state yet");
+    CK(cudaSetDevice(ctx->device));
+    const int rc = enqueue_positions_normals(ctx, with_normals != 0);
+    if (rc != ARAP_OK) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    *positions_device = ctx->out.as<double>();
+    if (normals_device) *normals_device = with_normals ? ctx->vnorm.as<double>() : nullptr;
     return ARAP_OK;
 }
 

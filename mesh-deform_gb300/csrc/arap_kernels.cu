@@ -1429,6 +1429,52 @@ __global__ void __launch_bounds__(kEnergyThreads) k_sum_partials(int n, const do
     if (threadIdx.x == 0) out[0] = buf[0];
 }
 
+// Vertex normals of a triangle mesh as OpenMesh's update_normals computes them
+// for display after a deform (examples/osg_viewer.cpp:53,60-62): face normal
+// = normalised (p1 - p0) x (p2 - p0), vertex normal = normalised sum of the
+// normals of the faces around the vertex (summed in face order). Degenerate
+// faces and vertices without faces give zero vectors.
+__device__ __forceinline__ void normalize3(double &x, double &y, double &z) {
+    const double n = sqrt(x * x + y * y + z * z);
+    if (n > 0.0) {
+        x /= n;
+        y /= n;
+        z /= n;
+    }
+}
+
+__global__ void k_face_normals(int F, const int32_t *__restrict__ faces, const double *__restrict__ xyz,
+                               double *__restrict__ fn) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    const double *a = xyz + 3 * (int64_t)faces[3 * f], *b = xyz + 3 * (int64_t)faces[3 * f + 1],
+                 *c = xyz + 3 * (int64_t)faces[3 * f + 2];
+    const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
+    const double vx = c[0] - a[0], vy = c[1] - a[1], vz = c[2] - a[2];
+    double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+    normalize3(nx, ny, nz);
+    fn[3 * (int64_t)f] = nx;
+    fn[3 * (int64_t)f + 1] = ny;
+    fn[3 * (int64_t)f + 2] = nz;
+}
+
+__global__ void k_vertex_normals(int V, const int32_t *__restrict__ vf_ptr, const int32_t *__restrict__ vf_face,
+                                 const double *__restrict__ fn, double *__restrict__ vn) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    double x = 0.0, y = 0.0, z = 0.0;
+    for (int q = vf_ptr[v]; q < vf_ptr[v + 1]; ++q) {
+        const double *n = fn + 3 * (int64_t)vf_face[q];
+        x += n[0];
+        y += n[1];
+        z += n[2];
+    }
+    normalize3(x, y, z);
+    vn[3 * (int64_t)v] = x;
+    vn[3 * (int64_t)v + 1] = y;
+    vn[3 * (int64_t)v + 2] = z;
+}
+
 __global__ void k_gather_positions(int V, const int32_t *__restrict__ oldidx, const Vec4<double> *__restrict__ pc64,
                                    double *__restrict__ out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1603,6 +1649,12 @@ void launch_energy(const DevSym &s, const double *w64, const Vec4<double> *p64, 
     const int nb = energy_partials(s.V);
     k_energy<<<nb, kEnergyThreads, 0, st>>>(s.V, s.drow, s.dcol, w64, p64, pc64, partial);
     k_sum_partials<<<1, kEnergyThreads, 0, st>>>(nb, partial, out);
+}
+
+void launch_vertex_normals(int V, int F, const int32_t *faces, const int32_t *vf_ptr, const int32_t *vf_face,
+                           const double *xyz, double *face_n, double *vertex_n, cudaStream_t st) {
+    if (F > 0) k_face_normals<<<blocks_for(F, 256), 256, 0, st>>>(F, faces, xyz, face_n);
+    if (V > 0) k_vertex_normals<<<blocks_for(V, 256), 256, 0, st>>>(V, vf_ptr, vf_face, face_n, vertex_n);
 }
 
 void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st) {

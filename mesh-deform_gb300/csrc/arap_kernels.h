@@ -149,6 +149,11 @@ int energy_partials(int V);
 void launch_energy(const DevSym &s, const double *w64, const Vec4<double> *p64, const Vec4<double> *pc64,
                    double *partial, double *out, cudaStream_t st);
 
+// vertex normals of positions xyz (V x 3, vertex order): face normals into
+// face_n (F x 3), then vertex_n (V x 3)
+void launch_vertex_normals(int V, int F, const int32_t *faces, const int32_t *vf_ptr, const int32_t *vf_face,
+                           const double *xyz, double *face_n, double *vertex_n, cudaStream_t st);
+
 // deformed positions back to the original vertex order as doubles (arap.h:133-135)
 void launch_gather_positions(const DevSym &s, const Vec4<double> *pc64, double *out_xyz, cudaStream_t st);
 template <typename T>

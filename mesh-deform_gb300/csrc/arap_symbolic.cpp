@@ -84,6 +84,16 @@ bool build_topology(int V, int F, const int32_t *faces, Topology &topo, std::str
         }
     }
     for (int v = 0; v < V; ++v) topo.rowptr[v + 1] += topo.rowptr[v];
+    // faces around each vertex (a face whose corners repeat is listed once per corner)
+    topo.vf_ptr.assign((size_t)V + 1, 0);
+    for (int64_t i = 0; i < (int64_t)3 * F; ++i) topo.vf_ptr[faces[i] + 1]++;
+    for (int v = 0; v < V; ++v) topo.vf_ptr[v + 1] += topo.vf_ptr[v];
+    topo.vf_face.resize((size_t)3 * F);
+    {
+        std::vector<int32_t> fill(topo.vf_ptr.begin(), topo.vf_ptr.end() - 1);
+        for (int f = 0; f < F; ++f)
+            for (int k = 0; k < 3; ++k) topo.vf_face[fill[faces[3 * f + k]]++] = f;
+    }
     return true;
 }
 

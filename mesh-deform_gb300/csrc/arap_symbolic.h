@@ -46,6 +46,8 @@ struct Topology {
     std::vector<int32_t> col;        // nnz
     std::vector<int32_t> ent_ptr;    // nnz+1
     std::vector<int32_t> ent_fc;     // face*3 + k (k: which cotangent of the face)
+    std::vector<int32_t> vf_ptr;     // V+1: faces around each vertex, in face order
+    std::vector<int32_t> vf_face;    // 3F
     int nnz() const { return (int)col.size(); }
 };
 

@@ -246,3 +246,29 @@ def test_energy_matches_oracle_and_decreases(gpu, precision, tol):
             assert eg <= prev * (1 + 1e-12)
         prev = eg
     ctx.close()
+
+
+def test_vertex_normals_and_device_positions(gpu):
+    """Vertex normals of the deformed mesh (OpenMesh's update_normals rule,
+    examples/osg_viewer.cpp:53,60-62) against numpy, and the device-resident
+    positions against the host copy of the same deform."""
+    import torch
+
+    w = W.cfg_icosphere_l4(level=3, iterations=5)
+    ctx = gpu.ArapContext(w.V, w.faces)
+    ctx.set_rest_positions(w.positions)
+    ctx.set_constraints(w.cidx, w.ctargets)
+    out = ctx.deform(w.iterations)
+    n = ctx.vertex_normals()
+    a, b, c = out[w.faces[:, 0]], out[w.faces[:, 1]], out[w.faces[:, 2]]
+    fn = np.cross(b - a, c - a)
+    fn /= np.linalg.norm(fn, axis=1, keepdims=True)
+    vn = np.zeros_like(out)
+    for k in range(3):
+        np.add.at(vn, w.faces[:, k], fn)
+    vn /= np.linalg.norm(vn, axis=1, keepdims=True)
+    np.testing.assert_allclose(n, vn, atol=1e-12)
+    pos, nrm = ctx.device_positions(with_normals=True)
+    np.testing.assert_array_equal(torch.as_tensor(pos, device="cuda").cpu().numpy(), out)
+    np.testing.assert_allclose(torch.as_tensor(nrm, device="cuda").cpu().numpy(), vn, atol=1e-12)
+    ctx.close()
