@@ -762,19 +762,64 @@ __device__ __forceinline__ void chunk_axpy(const T *buf, int ld, int cn, int c0,
     }
 }
 
-// Sums the G partial results into out (SUB: out -= sum). Ends with a barrier.
+// Work split of a GEMV phase over the CTA: thread t owns the 4-row quad
+// q = t mod NQp of the result (NQ = ceil(rows / 4) quads, NQp the next power of
+// two, at most 256) for the columns g, g + G, ... (g = t div NQp, G = 256 /
+// NQp groups). Threads with q >= NQ only take part in the reductions.
+struct Quads {
+    int NQ, NQp, G, q, g;
+    __device__ bool active() const { return q < NQ; }
+};
+
+__device__ __forceinline__ Quads quads_for(int rows) {
+    Quads Q;
+    Q.NQ = (rows + 3) >> 2;
+    Q.NQp = 1;
+    while (Q.NQp < Q.NQ) Q.NQp <<= 1;
+    Q.G = kSolveThreads / Q.NQp;
+    Q.q = threadIdx.x & (Q.NQp - 1);
+    Q.g = threadIdx.x / Q.NQp;
+    return Q;
+}
+
+// Sums the G partial results of every quad into out (SUB: out -= sum): first
+// across the lanes of a warp that share a quad (shuffles; only when NQp < 32),
+// then over at most 8 partials per quad through shared memory, in a fixed
+// order. Ends with a barrier.
 template <typename T, bool SUB>
-__device__ __forceinline__ void reduce_groups(int NQ, int G, int q, int g, const T ax[4], const T ay[4],
-                                              const T az[4], Vec4<T> *red, Vec4<T> *out) {
-    const int tid = threadIdx.x;
-    if (g < G && q < NQ)
+__device__ __forceinline__ void reduce_quads(const Quads &Q, T ax[4], T ay[4], T az[4], Vec4<T> *red,
+                                             Vec4<T> *out) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int slot, nslots;
+    bool writer;
+    if (Q.NQp < 32) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) red[g * 4 * NQ + 4 * q + k] = {ax[k], ay[k], az[k], (T)0};
+        for (int off = 16; off > 0; off >>= 1) {
+            if (off < Q.NQp) break;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                ax[k] += __shfl_xor_sync(0xffffffffu, ax[k], off);
+                ay[k] += __shfl_xor_sync(0xffffffffu, ay[k], off);
+                az[k] += __shfl_xor_sync(0xffffffffu, az[k], off);
+            }
+        }
+        slot = warp;
+        nslots = kSolveThreads / 32;
+        writer = lane < Q.NQp;
+    } else {
+        slot = Q.g;
+        nslots = Q.G;
+        writer = true;
+    }
+    if (writer && Q.active())
+#pragma unroll
+        for (int k = 0; k < 4; ++k) red[(slot * Q.NQ + Q.q) * 4 + k] = {ax[k], ay[k], az[k], (T)0};
     __syncthreads();
-    for (int rr = tid; rr < 4 * NQ; rr += kSolveThreads) {
+    for (int rr = tid; rr < 4 * Q.NQ; rr += kSolveThreads) {
+        const int qq = rr >> 2, k = rr & 3;
         T sx = 0, sy = 0, sz = 0;
-        for (int gg = 0; gg < G; ++gg) {
-            const Vec4<T> p = red[gg * 4 * NQ + rr];
+        for (int s = 0; s < nslots; ++s) {
+            const Vec4<T> p = red[(s * Q.NQ + qq) * 4 + k];
             sx += p.x; sy += p.y; sz += p.z;
         }
         Vec4<T> &o = out[rr];
@@ -782,10 +827,6 @@ __device__ __forceinline__ void reduce_groups(int NQ, int G, int q, int g, const
         else o = {sx, sy, sz, (T)0};
     }
     __syncthreads();
-}
-
-__device__ __forceinline__ int groups_for(int NQ) {
-    return NQ >= kSolveThreads ? 1 : max(1, kSolveThreads / max(NQ, 1));
 }
 
 // Ticket of the calling CTA's next task (thread 0 only). A launch of G CTAs
@@ -916,8 +957,7 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
         }
     }
     // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb)
-    const int NQa = (nc + 3) >> 2, Ga = groups_for(NQa);
-    const int NQb = (nb + 3) >> 2, Gb = groups_for(NQb);
+    const Quads Qa = quads_for(nc), Qb = quads_for(nb);
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
     for (int k = 0; k < ntot; ++k) {
         T *buf = (k & 1) ? buf1 : buf0;
@@ -926,21 +966,19 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
         const T *src;
         pl.chunk(k, c0, cn, src, ld);
         if (k < pl.nA) {
-            for (int w = tid; w < NQa * Ga; w += kSolveThreads)
-                chunk_axpy(buf, ld, cn, c0, w % NQa, w / NQa, Ga, fc, ax, ay, az);
+            if (Qa.active()) chunk_axpy(buf, ld, cn, c0, Qa.q, Qa.g, Qa.G, fc, ax, ay, az);
         } else {
-            for (int w = tid; w < NQb * Gb; w += kSolveThreads)
-                chunk_axpy(buf, ld, cn, c0, w % NQb, w / NQb, Gb, yv, ax, ay, az);
+            if (Qb.active()) chunk_axpy(buf, ld, cn, c0, Qb.q, Qb.g, Qb.G, yv, ax, ay, az);
         }
         __syncthreads();
         if (tid == 0 && k + 2 < ntot) issue_chunk(pl, k + 2, buf, &bars[k & 1]);
         if (k == pl.nA - 1) {
-            reduce_groups<T, false>(NQa, Ga, tid % NQa, tid / NQa, ax, ay, az, red, yv);
+            reduce_quads<T, false>(Qa, ax, ay, az, red, yv);
 #pragma unroll
             for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
         }
     }
-    if (pl.nB > 0) reduce_groups<T, true>(NQb, Gb, tid % max(NQb, 1), tid / max(NQb, 1), ax, ay, az, red, fb);
+    if (pl.nB > 0) reduce_quads<T, true>(Qb, ax, ay, az, red, fb);
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
     // the next ticket is taken while the stores drain; the barrier orders
@@ -1014,7 +1052,7 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     for (int i = tid + 4 * kSolveThreads; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
     __syncthreads();
     // phase A (nb > 0): z -= L21^T g; phase B: x = X^T z; both have nc rows
-    const int NQ = (nc + 3) >> 2, G = groups_for(NQ);
+    const Quads Q = quads_for(nc);
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
     for (int k = 0; k < ntot; ++k) {
         T *buf = (k & 1) ? buf1 : buf0;
@@ -1023,16 +1061,16 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
         const T *src;
         pl.chunk(k, c0, cn, src, ld);
         const Vec4<T> *v = (k < nA) ? gb : zv;
-        for (int w = tid; w < NQ * G; w += kSolveThreads) chunk_axpy(buf, ld, cn, c0, w % NQ, w / NQ, G, v, ax, ay, az);
+        if (Q.active()) chunk_axpy(buf, ld, cn, c0, Q.q, Q.g, Q.G, v, ax, ay, az);
         __syncthreads();
         if (tid == 0 && k + 2 < ntot) issue_chunk(pl, k + 2, buf, &bars[k & 1]);
         if (k == nA - 1) {
-            reduce_groups<T, true>(NQ, G, tid % NQ, tid / NQ, ax, ay, az, red, zv);
+            reduce_quads<T, true>(Q, ax, ay, az, red, zv);
 #pragma unroll
             for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
         }
     }
-    reduce_groups<T, false>(NQ, G, tid % NQ, tid / NQ, ax, ay, az, red, xv);
+    reduce_quads<T, false>(Q, ax, ay, az, red, xv);
     for (int i = tid; i < nc; i += kSolveThreads) {
         const Vec4<T> x = xv[i];
         const int k = d.first + i;
@@ -1168,15 +1206,14 @@ k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict
             }
             __syncthreads();
         }
-        const int NQa = (nc + 3) >> 2, Ga = groups_for(NQa);
-        const int NQb = (nb + 3) >> 2, Gb = groups_for(NQb);
+        const Quads Qa = quads_for(nc), Qb = quads_for(nb);
         T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
         bool a_done = false;
         for (int j = 0; j <= mine; ++j) {
             const int k = rank + j * CL;
             if (!a_done && (j == mine || k >= pl.nA)) {
                 // my part of y = X fc, then the sum over the ranks
-                reduce_groups<T, false>(NQa, Ga, tid % NQa, tid / NQa, ax, ay, az, red, ypart);
+                reduce_quads<T, false>(Qa, ax, ay, az, red, ypart);
 #pragma unroll
                 for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
                 cluster.sync();
@@ -1200,16 +1237,14 @@ k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict
             const T *src;
             pl.chunk(k, c0, cn, src, ld);
             if (k < pl.nA) {
-                for (int w = tid; w < NQa * Ga; w += kSolveThreads)
-                    chunk_axpy(buf, ld, cn, c0, w % NQa, w / NQa, Ga, fc, ax, ay, az);
+                if (Qa.active()) chunk_axpy(buf, ld, cn, c0, Qa.q, Qa.g, Qa.G, fc, ax, ay, az);
             } else {
-                for (int w = tid; w < NQb * Gb; w += kSolveThreads)
-                    chunk_axpy(buf, ld, cn, c0, w % NQb, w / NQb, Gb, yv, ax, ay, az);
+                if (Qb.active()) chunk_axpy(buf, ld, cn, c0, Qb.q, Qb.g, Qb.G, yv, ax, ay, az);
             }
             __syncthreads();
             if (tid == 0) top_issue<T, CL>(pl, rank, j + 2, buf0, buf1, bars);
         }
-        if (nb > 0) reduce_groups<T, false>(NQb, Gb, tid % max(NQb, 1), tid / max(NQb, 1), ax, ay, az, red, upart);
+        if (nb > 0) reduce_quads<T, false>(Qb, ax, ay, az, red, upart);
         cluster.sync();  // every rank's part of L21 y is in its shared memory
         for (int i = rank * kSolveThreads + tid; i < nb; i += CL * kSolveThreads) {
             Vec4<T> u = fb[i];
@@ -1291,7 +1326,7 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
         const int32_t *rs = rows + d.rows_off;
         for (int i = tid; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
         __syncthreads();
-        const int NQ = (nc + 3) >> 2, G = groups_for(NQ);
+        const Quads Q = quads_for(nc);
         T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
         bool a_done = false;
         for (int j = 0; j <= mine; ++j) {
@@ -1299,7 +1334,7 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
             if (!a_done && (j == mine || k >= nA)) {
                 // z = y - sum over the ranks of their part of L21^T g
                 if (nb > 0) {
-                    reduce_groups<T, false>(NQ, G, tid % NQ, tid / NQ, ax, ay, az, red, zpart);
+                    reduce_quads<T, false>(Q, ax, ay, az, red, zpart);
 #pragma unroll
                     for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
                     cluster.sync();
@@ -1325,11 +1360,11 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
             const T *src;
             pl.chunk(k, c0, cn, src, ld);
             const Vec4<T> *v = (k < nA) ? gb : zf;
-            for (int w = tid; w < NQ * G; w += kSolveThreads) chunk_axpy(buf, ld, cn, c0, w % NQ, w / NQ, G, v, ax, ay, az);
+            if (Q.active()) chunk_axpy(buf, ld, cn, c0, Q.q, Q.g, Q.G, v, ax, ay, az);
             __syncthreads();
             if (tid == 0) top_issue<T, CL>(pl, rank, j + 2, buf0, buf1, bars);
         }
-        reduce_groups<T, false>(NQ, G, tid % NQ, tid / NQ, ax, ay, az, red, xpart);
+        reduce_quads<T, false>(Q, ax, ay, az, red, xpart);
         cluster.sync();  // every rank's part of X^T z is in its shared memory
         for (int i = rank * kSolveThreads + tid; i < nc; i += CL * kSolveThreads) {
             Vec4<T> x = {(T)0, (T)0, (T)0, (T)0};
