@@ -170,12 +170,13 @@ def _f64(a):
 
 class DeviceArray:
     """A V x 3 float64 array in device memory owned by a context, exposed
-    through __cuda_array_interface__ (read-only view, no copy)."""
+    through __cuda_array_interface__ (a view, no copy; the context rewrites it
+    on its next call, so treat it as read-only)."""
 
     def __init__(self, ptr: int, shape):
         self.ptr = int(ptr)
         self.shape = tuple(shape)
-        self.__cuda_array_interface__ = {"shape": self.shape, "typestr": "<f8", "data": (self.ptr, True),
+        self.__cuda_array_interface__ = {"shape": self.shape, "typestr": "<f8", "data": (self.ptr, False),
                                          "version": 3, "strides": None}
 
 
