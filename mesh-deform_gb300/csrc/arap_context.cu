@@ -627,13 +627,15 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
         ctx->launches += 1;
         for (int r = 0; r <= ctx->refine; ++r) {
             {
-                // the forward sweep forms the FP64 residual of its own rows
+                Prof pr(ctx, ARAP_K_RESIDUAL);
+                launch_residual(d, ctx->w64.as<double>(), ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<double>>(),
+                                ctx->b.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(), ctx->sol.as<Vec4<float>>(), st);
+            }
+            {
                 Prof pr(ctx, ARAP_K_SOLVE_FWD);
                 launch_solve_fwd<float>(d, ctx->Xinv.as<float>(), ctx->L21.as<float>(),
                                         ctx->sol.as<Vec4<float>>(), ctx->uvec.as<Vec4<float>>(), tk, fl,
-                                        ctx->errw.as<int>(), st, ctx->w64.as<double>(), ctx->diag64.as<double>(),
-                                        ctx->bfixed.as<Vec4<double>>(), ctx->b.as<Vec4<float>>(),
-                                        ctx->pc64.as<Vec4<double>>());
+                                        ctx->errw.as<int>(), st);
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_BWD);
@@ -641,7 +643,7 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
                                         ctx->sol.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(),
                                         ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(), st);
             }
-            ctx->launches += solve_launches(d);
+            ctx->launches += solve_launches(d) + 1;
         }
     }
     CK(cudaGetLastError());
@@ -1655,10 +1657,6 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
     case ARAP_K_SOLVE_BWD:  // matrices once per pose tile, vectors once per pose
         B = T * (xlow + l21) * sz + P * (m * 3 * sz * 2 + nbsum * 3 * sz * 2);
         if (kernel_class == ARAP_K_SOLVE_BWD && ctx->state_prec != ARAP_PRECISION_FP64) B += P * m * (24 * 2 + 12);
-        // the single mixed forward sweep forms its right-hand side: FP64 residual
-        // inputs (x, b, bFixed, diagonal, adjacency with FP64 weights)
-        if (kernel_class == ARAP_K_SOLVE_FWD && ctx->state_prec != ARAP_PRECISION_FP64 && P == 1)
-            B += m * (24 + 12 + 24 + 8) + 4 * (m + 1) + nnz * (4 + 8);
         FL = P * (xlow + l21) * 6;
         break;
     case ARAP_K_GATHER:

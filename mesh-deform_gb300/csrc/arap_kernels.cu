@@ -850,39 +850,6 @@ struct SolveSmem {
     int ldx_max, ld21_max;
 };
 
-// Right-hand side of the forward sweep of the mixed form, computed by the
-// sweep itself: the FP64 residual r = (bFixed + b) - A x of the task's own rows
-// (x: the FP64 positions, A: the constrained Laplacian; as k_residual). With
-// drow == nullptr the sweep reads its right-hand side from sol instead.
-struct ResidualIn {
-    const int32_t *drow = nullptr, *dcol = nullptr;
-    const double *w64 = nullptr, *diag64 = nullptr;
-    const Vec4<double> *bfixed = nullptr, *x = nullptr;
-    const Vec4<float> *b = nullptr;
-    int m = 0;
-};
-
-template <typename T>
-__device__ __forceinline__ Vec4<T> residual_row(const ResidualIn &ri, int i) {
-    const Vec4<double> xi = ri.x[i];
-    const double dg = ri.diag64[i];
-    double ax = dg * xi.x, ay = dg * xi.y, az = dg * xi.z;
-    const int e1 = ri.drow[i + 1];
-    for (int e = ri.drow[i]; e < e1; ++e) {
-        const int j = ri.dcol[e];
-        if (j == i || j >= ri.m) continue;
-        const double wj = ri.w64[e];
-        const Vec4<double> xj = ri.x[j];
-        ax -= wj * xj.x;
-        ay -= wj * xj.y;
-        az -= wj * xj.z;
-    }
-    const Vec4<float> bi = ri.b[i];
-    const Vec4<double> bf = ri.bfixed[i];
-    return {(T)(float)((bf.x + (double)bi.x) - ax), (T)(float)((bf.y + (double)bi.y) - ay),
-            (T)(float)((bf.z + (double)bi.z) - az), (T)0};
-}
-
 // Forward: for supernode s (children first), f = [b(cols); 0] plus the
 // children's update vectors; y = X f(cols); u_s = f(struct) - L21 y goes to
 // the parent. Tickets follow `order` (level by level, leaves first), so a CTA
@@ -892,7 +859,7 @@ __global__ void __launch_bounds__(kSolveThreads, 3)
 k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
             const int32_t *__restrict__ child, const int32_t *__restrict__ relind, const T *__restrict__ Xall,
             const T *__restrict__ L21all, Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec,
-            unsigned long long *ticket, unsigned *flags, int *err, ResidualIn res) {
+            unsigned long long *ticket, unsigned *flags, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T *buf0 = reinterpret_cast<T *>(smem_raw);
     T *buf1 = reinterpret_cast<T *>(smem_raw + kChunkBytes);
@@ -927,8 +894,7 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
         for (int k = 2; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     for (int i = tid; i < d.ldx; i += kSolveThreads)
-        fc[i] = i >= nc ? Vec4<T>{(T)0, (T)0, (T)0, (T)0}
-                        : (res.drow ? residual_row<T>(res, d.first + i) : sol[d.first + i]);
+        fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
     for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
     // the children's entries of this thread (child-major list, kPull per thread):
     // positions are read before waiting, update vectors in one round trip after
@@ -1174,7 +1140,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kSolveThreads, 1)
 k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ order,
                 const SnInfo *__restrict__ sn, const int32_t *__restrict__ child, const int32_t *__restrict__ relind,
                 const T *__restrict__ Xall, const T *__restrict__ L21all, Vec4<T> *__restrict__ sol,
-                Vec4<T> *__restrict__ uvec, unsigned long long *ticket, unsigned *flags, int *err, ResidualIn res) {
+                Vec4<T> *__restrict__ uvec, unsigned long long *ticket, unsigned *flags, int *err) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
@@ -1218,8 +1184,7 @@ k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict
             for (int j = 2; j < mine; ++j) prefetch_chunk_l2(pl, rank + j * CL);
         }
         for (int i = tid; i < d.ldx; i += kSolveThreads)
-            fc[i] = i >= nc ? Vec4<T>{(T)0, (T)0, (T)0, (T)0}
-                            : (res.drow ? residual_row<T>(res, d.first + i) : sol[d.first + i]);
+            fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
         for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
         if (rank == 0 && tid == 0)
             for (int ci = d.child_begin; ci < d.child_end; ++ci) {
@@ -1677,32 +1642,19 @@ size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
 
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
-                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st,
-                      const double *w64, const double *diag64, const Vec4<double> *bfixed, const Vec4<float> *b,
-                      const Vec4<double> *x64) {
-    ResidualIn res;
-    if (b) {
-        res.drow = s.drow;
-        res.dcol = s.dcol;
-        res.w64 = w64;
-        res.diag64 = diag64;
-        res.bfixed = bfixed;
-        res.x = x64;
-        res.b = b;
-        res.m = s.m;
-    }
+                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st) {
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
     if (s.s_low > 0)
         k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(s.s_low, s.s_low + G, lay, s.level_sn, s.sn, s.child, s.relind,
-                                                       X, L21, sol, uvec, ticket, flags, err, res);
+                                                       X, L21, sol, uvec, ticket, flags, err);
     if (s.s_top > 0) {
         const size_t tsmem = top_smem_bytes_impl(s.max_ldx, s.max_ld21, sizeof(T));
         k_solve_fwd_top<T, kTopCluster><<<s.top_clusters * kTopCluster, kSolveThreads, tsmem, st>>>(
             s.s_top, s.s_top + s.top_clusters, s.ltop, lay, s.level_sn + s.s_low, s.sn, s.child, s.relind, X, L21, sol,
-            uvec, ticket + 2, flags, err, res);
+            uvec, ticket + 2, flags, err);
     }
 }
 
@@ -1841,14 +1793,10 @@ template void launch_rhs<float>(const DevSym &, const float *, const Vec4<float>
                                 const Vec4<float> *, Vec4<float> *, cudaStream_t);
 template void launch_rhs<double>(const DevSym &, const double *, const Vec4<double> *, const Vec4<double> *,
                                  const Vec4<double> *, Vec4<double> *, cudaStream_t);
-template void launch_solve_fwd<float>(const DevSym &, const float *, const float *, Vec4<float> *,
-                                        Vec4<float> *, unsigned long long *, unsigned *, int *, cudaStream_t,
-                                        const double *, const double *, const Vec4<double> *,
-                                        const Vec4<float> *, const Vec4<double> *);
+template void launch_solve_fwd<float>(const DevSym &, const float *, const float *, Vec4<float> *, Vec4<float> *,
+                                      unsigned long long *, unsigned *, int *, cudaStream_t);
 template void launch_solve_fwd<double>(const DevSym &, const double *, const double *, Vec4<double> *,
-                                        Vec4<double> *, unsigned long long *, unsigned *, int *, cudaStream_t,
-                                        const double *, const double *, const Vec4<double> *,
-                                        const Vec4<float> *, const Vec4<double> *);
+                                       Vec4<double> *, unsigned long long *, unsigned *, int *, cudaStream_t);
 template void launch_solve_bwd<float>(const DevSym &, const float *, const float *, Vec4<float> *, Vec4<double> *,
                                       Vec4<float> *, int, unsigned long long *, unsigned *, int *, cudaStream_t);
 template void launch_solve_bwd<double>(const DevSym &, const double *, const double *, Vec4<double> *,

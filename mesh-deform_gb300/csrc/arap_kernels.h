@@ -111,15 +111,9 @@ cudaError_t configure_top_smem(int bytes_f32, int bytes_f64);
 #endif
 constexpr int kTopTaskBytes = ARAP_TOP_TASK_KB * 1024;
 constexpr int kTopMaxClusters = 16;
-// With b != nullptr (mixed form) the forward sweep computes its right-hand
-// side itself: the FP64 residual (bFixed + b) - A x64 of every row it solves
-// (k_residual's arithmetic); otherwise it reads the right-hand side from sol.
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
-                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st,
-                      const double *w64 = nullptr, const double *diag64 = nullptr,
-                      const Vec4<double> *bfixed = nullptr, const Vec4<float> *b = nullptr,
-                      const Vec4<double> *x64 = nullptr);
+                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st);
 template <typename T>
 void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
