@@ -923,6 +923,9 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     }
     if (tid == 0)
         for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
+    // the next ticket is taken once this task is ready to run, so its round
+    // trip overlaps the work below
+    if (tid == 32) next_task(ticket, S, Z, order, false, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
     __syncthreads();
     if (total_children_rows <= kPull * kSolveThreads) {
         Vec4<T> pu[kPull];
@@ -981,10 +984,8 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     if (pl.nB > 0) reduce_quads<T, true>(Qb, ax, ay, az, red, fb);
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
-    // the next ticket is taken while the stores drain; the barrier orders
-    // every thread's writes before thread 0's release, which is cumulative: a
-    // CTA that acquires the flag sees them all
-    if (tid == 32) next_task(ticket, S, Z, order, false, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
+    // the barrier orders every thread's writes before thread 0's release,
+    // which is cumulative: a CTA that acquires the flag sees them all
     __syncthreads();
     if (tid == 0) st_release(flags + s, epoch);
     ph[0] += (unsigned)(ntot + 1) / 2u;
@@ -1045,6 +1046,7 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     for (int u = 0; u < 4; ++u) myrow[u] = (tid + u * kSolveThreads < nb) ? rs[tid + u * kSolveThreads] : 0;
     // a parent in the top levels was finished by the launch before this one
     if (tid == 0 && d.parent >= 0 && sn[d.parent].level < ltop) wait_flag(flags + d.parent, epoch, err);
+    if (tid == 32) next_task(ticket, S, Z, order, true, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < 4; ++u)
@@ -1086,10 +1088,8 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
             pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
         }
     }
-    // the next ticket is taken while the stores drain; the barrier orders
-    // every thread's writes before thread 0's release, which is cumulative: a
-    // CTA that acquires the flag sees them all
-    if (tid == 32) next_task(ticket, S, Z, order, true, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
+    // the barrier orders every thread's writes before thread 0's release,
+    // which is cumulative: a CTA that acquires the flag sees them all
     __syncthreads();
     if (tid == 0) st_release(flags + s, epoch);
     ph[0] += (unsigned)(ntot + 1) / 2u;
@@ -1191,6 +1191,7 @@ k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict
                 const int c = child[ci];
                 if (sn[c].level >= ltop) wait_flag(flags + c, epoch, err);
             }
+        if (rank == 0 && tid == 32) next_task(ticket, S, Z, order, false, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
         cluster.sync();  // the children's update vectors are complete for every rank
         for (int ci = d.child_begin; ci < d.child_end; ++ci) {
             const SnInfo c = sn[child[ci]];
@@ -1257,9 +1258,8 @@ k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict
             uvec[d.uvec_off + i] = u;
         }
         for (int i = rank * kSolveThreads + tid; i < nc; i += CL * kSolveThreads) sol[d.first + i] = yv[i];
-        // rank 0 takes the next ticket meanwhile; the cluster barrier orders every
-        // rank's writes before rank 0's (cumulative) release
-        if (rank == 0 && tid == 32) next_task(ticket, S, Z, order, false, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
+        // the cluster barrier orders every rank's writes before rank 0's
+        // (cumulative) release
         cluster.sync();
         if (rank == 0 && tid == 0) st_release(flags + s, epoch);
         ph[0] += (unsigned)(mine + 1) / 2u;
@@ -1322,6 +1322,7 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
         for (int i = tid; i < d.ldx; i += kSolveThreads)
             zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
         if (rank == 0 && tid == 0 && d.parent >= 0) wait_flag(flags + d.parent, epoch, err);
+        if (rank == 0 && tid == 32) next_task(ticket, S, Z, order, true, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
         cluster.sync();  // the parent's solution is complete for every rank
         const int32_t *rs = rows + d.rows_off;
         for (int i = tid; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
@@ -1387,9 +1388,8 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
                 pc32[kk] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
             }
         }
-        // rank 0 takes the next ticket meanwhile; the cluster barrier orders every
-        // rank's writes before rank 0's (cumulative) release
-        if (rank == 0 && tid == 32) next_task(ticket, S, Z, order, true, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
+        // the cluster barrier orders every rank's writes before rank 0's
+        // (cumulative) release
         cluster.sync();
         if (rank == 0 && tid == 0) st_release(flags + s, epoch);
         ph[0] += (unsigned)(mine + 1) / 2u;
