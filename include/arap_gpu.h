@@ -171,7 +171,7 @@ int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas);
    split each supernode's matrices, and the levels below with one CTA per
    supernode. A level goes to the clusters when one of its supernodes holds at
    least `bytes` of X = inv(L11) and L21 (as FP32) and every level above it does
-   too. 0 (the default): 64 KiB; negative: no cluster levels. The split changes
+   too. 0 (the default): 128 KiB; negative: no cluster levels. The split changes
    only the order of some sums. Takes effect at the next deform (which sets the
    problem up again). */
 int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes);

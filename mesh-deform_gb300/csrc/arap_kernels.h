@@ -107,7 +107,7 @@ cudaError_t configure_top_smem(int bytes_f32, int bytes_f64);
 // a tree level goes to the cluster solves when one of its supernodes holds at
 // least this many bytes of X and L21 (FP32), and every level above does too
 #ifndef ARAP_TOP_TASK_KB
-#define ARAP_TOP_TASK_KB 64
+#define ARAP_TOP_TASK_KB 128
 #endif
 constexpr int kTopTaskBytes = ARAP_TOP_TASK_KB * 1024;
 constexpr int kTopMaxClusters = 16;
