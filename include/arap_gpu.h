@@ -350,8 +350,8 @@ typedef struct arap_server_config {
     int32_t device;
     int32_t precision;           /* arap_precision of every request (ARAP_PRECISION_MIXED) */
     int32_t refine_steps;        /* MIXED refinement solves per iteration (1) */
-    int32_t max_in_flight;       /* launches on the device at once (0: 4; more in flight made the
-                                    measured serving stream slower, not faster) */
+    int32_t max_in_flight;       /* launches on the device at once (0: 8; beyond that the measured
+                                    serving stream got no faster) */
     int64_t device_budget_bytes; /* resident device memory limit (0: 80% of the free memory) */
     int32_t prep_threads;        /* host threads for analysis and first launches (0: 4) */
     int32_t max_batch;           /* most requests per multi-pose launch (0: 64; 1: no batching) */

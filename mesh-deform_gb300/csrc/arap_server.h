@@ -122,7 +122,7 @@ class Server {
 
   public:
     Server(B backend, const arap_server_config &cfg) : b_(std::move(backend)), cfg_(cfg) {
-        if (cfg_.max_in_flight <= 0) cfg_.max_in_flight = 4;
+        if (cfg_.max_in_flight <= 0) cfg_.max_in_flight = 8;
         if (cfg_.prep_threads <= 0) cfg_.prep_threads = 4;
         if (cfg_.max_batch <= 0) cfg_.max_batch = 64;
         if (cfg_.max_queue <= 0) cfg_.max_queue = 65536;
