@@ -371,7 +371,14 @@ class Server {
         auto &v = cache_[s->key];
         v.erase(std::remove(v.begin(), v.end(), s), v.end());
         if (v.empty()) cache_.erase(s->key);
+        // destroying the context waits for its stream, so a completion
+        // callback of it has run by now: drop any notice it left
         destroy_slot_resources(s);
+        notified_.erase(std::remove(notified_.begin(), notified_.end(), s), notified_.end());
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            done_slots_.erase(std::remove(done_slots_.begin(), done_slots_.end(), s), done_slots_.end());
+        }
         for (auto it = slots_.begin(); it != slots_.end(); ++it)
             if (it->get() == s) {
                 slots_.erase(it);
@@ -627,7 +634,6 @@ class Server {
             } else {
                 // a failed factorisation (or an expired wait) leaves nothing worth keeping
                 fail_key(s, rc, err);
-                notified_.erase(std::remove(notified_.begin(), notified_.end(), s), notified_.end());
                 remove_slot(s);
             }
         }
