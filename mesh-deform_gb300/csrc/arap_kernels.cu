@@ -317,48 +317,55 @@ template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
 k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF *__restrict__ Lval,
       TF *__restrict__ Dinv, int *err) {
-    __shared__ TF Db[NB][NB + 1];  // row-major
-    __shared__ TF Di[NB][NB + 1];
-    __shared__ TF s_inv;
+    __shared__ TF Db[NB][NB + 1];  // the factored block, row-major
+    __shared__ TF Di[NB][NB + 1];  // its inverse
     const SnInfo d = sn[items[blockIdx.x].sn];
     const int n = d.nrow, nc = d.ncol;
     const int j0 = jb * NB, w = min(NB, nc - j0);
     TF *P = Lval + d.panel_off;
-    const int tid = threadIdx.x;
-    for (int q = tid; q < NB * NB; q += kFactorThreads) {
-        const int r = q % NB, c = q / NB;
-        Db[r][c] = (r < w && c < w && c <= r) ? P[(int64_t)(j0 + c) * n + j0 + r] : (TF)0;
-    }
-    __syncthreads();
-    for (int k = 0; k < w; ++k) {
-        if (tid == 0) {
-            TF dk = Db[k][k];
-            if (!(dk > (TF)0)) { atomicOr(err, kErrNotSpd); dk = (TF)1; }
-            dk = tsqrt(dk);
-            Db[k][k] = dk;
-            s_inv = (TF)1 / dk;
-        }
-        __syncthreads();
-        if (tid > k && tid < w) Db[tid][k] *= s_inv;
-        __syncthreads();
-        const int m = w - k - 1;
-        for (int q = tid; q < m * m; q += kFactorThreads) {
-            const int r = k + 1 + q / m, c = k + 1 + q % m;
-            if (c <= r) Db[r][c] -= Db[r][k] * Db[c][k];
-        }
-        __syncthreads();
-    }
-    if (tid < NB) {  // inverse of the lower-triangular block, column tid
-        const int c = tid;
-        for (int i = 0; i < NB; ++i) {
-            TF v = (TF)0;
-            if (i >= c && i < w) {
-                TF acc = (i == c) ? (TF)1 : (TF)0;
-                for (int t = c; t < i; ++t) acc -= Db[i][t] * Di[t][c];
-                v = acc / Db[i][i];
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid < 32) {
+        // one warp: row `lane` of the block in registers, right-looking
+        // Cholesky with the pivot column broadcast by shuffles (the same
+        // operations in the same order as a column-by-column update)
+        TF a[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) a[c] = (lane < w && c <= lane) ? P[(int64_t)(j0 + c) * n + j0 + lane] : (TF)0;
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            if (k < w) {
+                TF akk = __shfl_sync(0xffffffffu, a[k], k);
+                if (!(akk > (TF)0)) {
+                    bad = true;
+                    akk = (TF)1;
+                }
+                const TF dk = tsqrt(akk), inv = (TF)1 / dk;
+                if (lane == k) a[k] = dk;
+                else if (lane > k) a[k] *= inv;
+#pragma unroll
+                for (int c = k + 1; c < NB; ++c) {
+                    const TF lck = __shfl_sync(0xffffffffu, a[k], c);  // L(c, k)
+                    if (lane >= c) a[c] -= a[k] * lck;
+                }
             }
-            Di[i][c] = v;
         }
+        if (bad && lane == 0) atomicOr(err, kErrNotSpd);
+#pragma unroll
+        for (int c = 0; c < NB; ++c) Db[lane][c] = (lane < w && c <= lane) ? a[c] : (TF)0;
+        __syncwarp();
+        // inverse of the lower-triangular block: lane c forms column c by
+        // forward substitution (entries above the diagonal stay zero)
+        TF x[NB];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            TF acc = (i == lane) ? (TF)1 : (TF)0;
+#pragma unroll
+            for (int t = 0; t < i; ++t) acc -= Db[i][t] * x[t];
+            x[i] = (i < w && i >= lane) ? acc / Db[i][i] : (TF)0;
+        }
+#pragma unroll
+        for (int i = 0; i < NB; ++i) Di[i][lane] = x[i];
     }
     __syncthreads();
     for (int q = tid; q < NB * NB; q += kFactorThreads) {
