@@ -244,19 +244,28 @@ k_fea(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const int3
         const SnInfo c = sn[child[ci]];
         const int nbc = c.nrow - c.ncol;
         const int32_t *ri = relind + c.relind_off;
-        if (tid == 0) {  // child columns whose parent column lies in [a, b) (ri increases)
-            int lo = 0, hi = nbc;
-            while (lo < hi) { const int m = (lo + hi) >> 1; if (ri[m] < it.a) lo = m + 1; else hi = m; }
-            s_k0 = lo;
-            hi = nbc;
-            while (lo < hi) { const int m = (lo + hi) >> 1; if (ri[m] < it.b) lo = m + 1; else hi = m; }
-            s_k1 = lo;
-        }
+        // child columns whose parent column lies in [a, b): ri increases, so
+        // they are [k0, k1) with k0 = #{ri < a}, k1 = #{ri < b}, counted by all threads
+        if (tid == 0) s_k0 = s_k1 = 0;
         __syncthreads();
+        int n0 = 0, n1 = 0;
+        for (int m = tid; m < nbc; m += kFactorThreads) {
+            const int v = ri[m];
+            n0 += v < it.a;
+            n1 += v < it.b;
+        }
+        if (n0) atomicAdd(&s_k0, n0);
+        if (n1) atomicAdd(&s_k1, n1);
+        __syncthreads();
+        const int k0 = s_k0, k1 = s_k1;
         const TF *Uc = Upd + c.upd_off;
-        for (int k = s_k0; k < s_k1; ++k) {
-            const int pk = ri[k];
-            for (int i = k + tid; i < nbc; i += kFactorThreads) front(P, U, n, nc, nb, ri[i], pk) += Uc[(int64_t)k * nbc + i];
+        // every (column k, row i >= k) pair of the slice in one sweep: distinct
+        // targets within one child, so no two threads meet
+        const int64_t cnt = (int64_t)(k1 - k0) * nbc;
+        for (int64_t q = tid; q < cnt; q += kFactorThreads) {
+            const int k = k0 + (int)(q / nbc), i = (int)(q % nbc);
+            if (i < k) continue;
+            front(P, U, n, nc, nb, ri[i], ri[k]) += Uc[(int64_t)k * nbc + i];
         }
         __syncthreads();
     }
@@ -459,6 +468,7 @@ k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *_
     extern __shared__ __align__(16) unsigned char fx_raw[];
     TF *Xc = reinterpret_cast<TF *>(fx_raw);  // [row][NB + 1]
     __shared__ TF Ts[NB][NB + 1];
+    __shared__ TF Ds[NB][NB + 1];  // inverse of the current diagonal block, [t][r]
     const FItem it = items[blockIdx.x];
     const SnInfo d = sn[it.sn];
     const int n = d.nrow, nc = d.ncol, nb = n - nc;
@@ -477,9 +487,14 @@ k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *_
     const int r = tid % NB, cg = tid / NB;  // row in block, group of 4 columns
     for (int ib = jb + 1; ib < nblk; ++ib) {
         const int i0 = ib * NB, wi = min(NB, nc - i0);
+        {
+            // the block's inverse into shared memory (read 32 times per column below)
+            const TF *Dii = Dinv + d.dinv_off + (int64_t)ib * NB * NB;
+            for (int q = tid; q < NB * NB; q += kFactorThreads) Ds[q / NB][q % NB] = Dii[q];
+        }
         TF acc[4] = {(TF)0, (TF)0, (TF)0, (TF)0};
         if (r < wi) {
-#pragma unroll 4
+#pragma unroll 8
             for (int k = j0; k < i0; ++k) {
                 const TF l = P[(int64_t)k * n + i0 + r];
 #pragma unroll
@@ -489,13 +504,12 @@ k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *_
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) Ts[cg * 4 + cc][r] = acc[cc];
         __syncthreads();
-        const TF *Dii = Dinv + d.dinv_off + (int64_t)ib * NB * NB;
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
             const int c = cg * 4 + cc;
             TF v = (TF)0;
             if (r < wi)
-                for (int t = 0; t <= r; ++t) v += Dii[(int64_t)t * NB + r] * Ts[c][t];
+                for (int t = 0; t <= r; ++t) v += Ds[t][r] * Ts[c][t];
             Xc[(i0 + r) * (NB + 1) + c] = (r < wi && c < wj) ? -v : (TF)0;
         }
         __syncthreads();
