@@ -166,6 +166,14 @@ int arap_query(arap_ctx *ctx, int32_t *done);
    next deform (which sets the problem up again). */
 int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas);
 
+/* Poses per task of the batched triangular solves of arap_deform_poses: 1, 2,
+   4, 8 or 16 (0, the default: the largest the mesh's biggest supernode
+   allows). A larger tile streams each factor block once for more poses; a
+   smaller one gives more tasks to run at once. Any value gives the same
+   result. ARAP_ERR_UNSUPPORTED at the next arap_deform_poses when the tile
+   does not fit; ARAP_ERR_INVALID_ARGUMENT for other values. */
+int arap_set_pose_tile(arap_ctx *ctx, int32_t poses);
+
 /* The triangular solves take the top levels of the elimination tree (large
    fronts, one or a few supernodes per level) with clusters of 8 CTAs that
    split each supernode's matrices, and the levels below with one CTA per

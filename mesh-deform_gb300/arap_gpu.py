@@ -103,6 +103,7 @@ SIGNATURES = {
     "arap_wait": (C.c_int, [_P]),
     "arap_set_graphs": (C.c_int, [_P, _I32]),
     "arap_set_solve_ctas": (C.c_int, [_P, _I32]),
+    "arap_set_pose_tile": (C.c_int, [_P, _I32]),
     "arap_energy": (C.c_int, [_P, _dp]),
     "arap_set_cluster_threshold": (C.c_int, [_P, _I32]),
     "arap_set_ordering": (C.c_int, [_P, _I32]),
@@ -309,6 +310,10 @@ class ArapContext:
 
     def set_solve_ctas(self, n: int):
         self._check(self.lib.arap_set_solve_ctas(self.h, int(n)))
+
+    def set_pose_tile(self, poses: int):
+        """Poses per batched-solve task of deform_poses (0: automatic)."""
+        self._check(self.lib.arap_set_pose_tile(self.h, int(poses)))
 
     def set_targets(self, xyz):
         x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)

@@ -10,6 +10,8 @@
 // 16 KB chunk of a supernode's matrices streamed into shared memory (TMA bulk
 // copies) serves PT poses.
 #include "arap_kernels.h"
+
+#include <algorithm>
 #include "arap_device.cuh"
 
 namespace arapgpu {
@@ -60,6 +62,30 @@ __device__ __forceinline__ void wait_chunk(uint64_t *bar, unsigned parity, int *
     if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
     for (unsigned it = 0; it < kSpinLimit; ++it)
         if (mbar_try_wait(bar, parity)) return;
+}
+
+// Next task of a persistent batched solve (thread 0): tasks are (supernode,
+// pose tile) pairs, supernodes in `order` (reversed for the backward sweep),
+// tiles inner. A launch of G CTAs over N = S*T tasks consumes exactly
+// Z = N + G tickets (one per task, one per CTA that finds none left); launch e
+// owns [e*Z, (e+1)*Z) and publishes epoch e + 1. After an expired wait every
+// CTA leaves at its next ticket.
+__device__ __forceinline__ void next_btask(unsigned long long *ticket, int S, int T, unsigned long long Z,
+                                           const int32_t *order, bool reverse, const int *err, int &task,
+                                           int &tile, unsigned &epoch) {
+    const unsigned long long n = (unsigned long long)S * T;
+    const unsigned long long t = atomicAdd(ticket, 1ull);
+    const unsigned long long r = t % Z;
+    const bool stop = (*(volatile const int *)err & kErrTimeout) != 0;
+    if (r < n && !stop) {
+        const int idx = (int)(reverse ? n - 1 - r : r);
+        task = order[idx / T];
+        tile = idx % T;
+    } else {
+        task = -1;
+        tile = 0;
+    }
+    epoch = (unsigned)(t / Z) + 1u;
 }
 
 // Column chunks of matrix A then matrix B (both column-major, 16-byte aligned
@@ -147,7 +173,7 @@ struct BLayout {
 // Forward solve for a tile of PT poses of one supernode (children first).
 template <int PT>
 __global__ void __launch_bounds__(kThreads)
-k_bsolve_fwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+k_bsolve_fwd(int S, int T, int P, unsigned long long nz, BLayout lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
              const int32_t *__restrict__ child, const int32_t *__restrict__ relind, const float *__restrict__ Xall,
              const float *__restrict__ L21all, Vec4<float> *__restrict__ sol, Vec4<float> *__restrict__ uvec,
              unsigned long long *ticket, unsigned *flags, int *err) {
@@ -157,23 +183,21 @@ k_bsolve_fwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
     Vec4<float> *Y = F + lay.ldx_max * PT;
     Vec4<float> *Fb = Y + lay.ldx_max * PT;
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_task, s_tile;
-    __shared__ unsigned s_epoch;
+    __shared__ int s_task[2], s_tile[2];  // this task's and the next one's ticket
+    __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
-    const unsigned long long ntask = (unsigned long long)S * T;
     if (tid == 0) {
-        const unsigned long long t = atomicAdd(ticket, 1ull);
-        const int r = (int)(t % ntask);
-        s_task = order[r / T];
-        s_tile = r % T;
-        s_epoch = (unsigned)(t / ntask) + 1u;
         mbar_init(&bars[0]);
         mbar_init(&bars[1]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        next_btask(ticket, S, T, nz, order, false, err, s_task[0], s_tile[0], s_epoch[0]);
     }
     __syncthreads();
-    const int s = s_task, tile = s_tile, p0 = tile * PT;
-    const unsigned epoch = s_epoch;
+    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
+    for (int slot = 0;; slot ^= 1) {
+    const int s = s_task[slot], tile = s_tile[slot], p0 = tile * PT;
+    if (s < 0) break;
+    const unsigned epoch = s_epoch[slot];
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
     Chunks pl;
@@ -191,6 +215,7 @@ k_bsolve_fwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
     for (int e = tid; e < d.ld21 * PT; e += kThreads) Fb[e] = {0.f, 0.f, 0.f, 0.f};
     if (tid == 0)
         for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + (int64_t)child[ci] * T + tile, epoch, err);
+    if (tid == 32) next_btask(ticket, S, T, nz, order, false, err, s_task[slot ^ 1], s_tile[slot ^ 1], s_epoch[slot ^ 1]);
     __syncthreads();
     for (int ci = d.child_begin; ci < d.child_end; ++ci) {
         const SnInfo c = sn[child[ci]];
@@ -215,7 +240,7 @@ k_bsolve_fwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
 #pragma unroll
         for (int k = 0; k < 4; ++k) acc[i][k][0] = acc[i][k][1] = acc[i][k][2] = 0.f;
     for (int k = 0; k < ntot; ++k) {
-        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        wait_chunk(&bars[k & 1], (ph[k & 1] + (unsigned)(k >> 1)) & 1u, err);
         int c0, cn, ld;
         const float *src;
         pl.chunk(k, c0, cn, src, ld);
@@ -244,13 +269,16 @@ k_bsolve_fwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
     // which is cumulative: a CTA that acquires the flag sees them all
     __syncthreads();
     if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
+    ph[0] += (unsigned)(ntot + 1) / 2u;
+    ph[1] += (unsigned)ntot / 2u;
+    }
 }
 
 // Backward solve for a tile of PT poses of one supernode (root first); adds the
 // correction to the FP64 positions and refreshes their FP32 copy.
 template <int PT>
 __global__ void __launch_bounds__(kThreads)
-k_bsolve_bwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+k_bsolve_bwd(int S, int T, int P, unsigned long long nz, BLayout lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
              const int32_t *__restrict__ rows, const float *__restrict__ Xall, const float *__restrict__ L21Tall,
              Vec4<float> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32,
              unsigned long long *ticket, unsigned *flags, int *err) {
@@ -260,23 +288,21 @@ k_bsolve_bwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
     Vec4<float> *Xv = Z + lay.ldx_max * PT;
     Vec4<float> *G = Xv + lay.ldx_max * PT;
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_task, s_tile;
-    __shared__ unsigned s_epoch;
+    __shared__ int s_task[2], s_tile[2];  // this task's and the next one's ticket
+    __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
-    const unsigned long long ntask = (unsigned long long)S * T;
     if (tid == 0) {
-        const unsigned long long t = atomicAdd(ticket, 1ull);
-        const int r = (int)(ntask - 1 - t % ntask);
-        s_task = order[r / T];
-        s_tile = r % T;
-        s_epoch = (unsigned)(t / ntask) + 1u;
         mbar_init(&bars[0]);
         mbar_init(&bars[1]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        next_btask(ticket, S, T, nz, order, true, err, s_task[0], s_tile[0], s_epoch[0]);
     }
     __syncthreads();
-    const int s = s_task, tile = s_tile, p0 = tile * PT;
-    const unsigned epoch = s_epoch;
+    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
+    for (int slot = 0;; slot ^= 1) {
+    const int s = s_task[slot], tile = s_tile[slot], p0 = tile * PT;
+    if (s < 0) break;
+    const unsigned epoch = s_epoch[slot];
     const SnInfo d = sn[s];
     const int nc = d.ncol, nb = d.nrow - d.ncol;
     Chunks pl;
@@ -295,6 +321,7 @@ k_bsolve_bwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
     }
     const int32_t *rs = rows + d.rows_off;
     if (tid == 0 && d.parent >= 0) wait_flag(flags + (int64_t)d.parent * T + tile, epoch, err);
+    if (tid == 32) next_btask(ticket, S, T, nz, order, true, err, s_task[slot ^ 1], s_tile[slot ^ 1], s_epoch[slot ^ 1]);
     __syncthreads();
     for (int e = tid; e < nb * PT; e += kThreads) {
         const int i = e / PT, p = e % PT;
@@ -308,7 +335,7 @@ k_bsolve_bwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
 #pragma unroll
         for (int k = 0; k < 4; ++k) acc[i][k][0] = acc[i][k][1] = acc[i][k][2] = 0.f;
     for (int k = 0; k < ntot; ++k) {
-        wait_chunk(&bars[k & 1], (unsigned)((k >> 1) & 1), err);
+        wait_chunk(&bars[k & 1], (ph[k & 1] + (unsigned)(k >> 1)) & 1u, err);
         int c0, cn, ld;
         const float *src;
         pl.chunk(k, c0, cn, src, ld);
@@ -339,6 +366,9 @@ k_bsolve_bwd(int S, int T, int P, BLayout lay, const int32_t *__restrict__ order
     // which is cumulative: a CTA that acquires the flag sees them all
     __syncthreads();
     if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
+    ph[0] += (unsigned)(ntot + 1) / 2u;
+    ph[1] += (unsigned)ntot / 2u;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -481,12 +511,16 @@ inline int nblocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
 // ---------------------------------------------------------------------------
 
-int batch_pose_tile(int max_ldx, int max_ld21) {
+bool batch_pose_tile_fits(int max_ldx, int max_ld21, int pt) {
+    if (pt != 1 && pt != 2 && pt != 4 && pt != 8 && pt != 16) return false;
     const int rows = max_ldx > max_ld21 ? max_ldx : max_ld21;
-    for (int pt = 16; pt >= 1; pt /= 2) {
-        const size_t smem = batch_solve_smem_bytes(max_ldx, max_ld21, pt);
-        if ((rows / 4) * pt <= kMaxItems * kThreads && smem <= 200 * 1024) return pt;
-    }
+    const size_t smem = batch_solve_smem_bytes(max_ldx, max_ld21, pt);
+    return ((rows + 3) / 4) * pt <= kMaxItems * kThreads && smem <= 200 * 1024;
+}
+
+int batch_pose_tile(int max_ldx, int max_ld21) {
+    for (int pt = 16; pt >= 1; pt /= 2)
+        if (batch_pose_tile_fits(max_ldx, max_ld21, pt)) return pt;
     return 0;
 }
 
@@ -579,32 +613,60 @@ void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *ou
     if (n) k_bgather<<<nblocks(n, 256), 256, 0, st>>>(s.V, P, s.oldidx, pc64, out);
 }
 
+// CTAs of a persistent batched solve: the tasks, at most what fits on the
+// device at once (both sweeps' occupancy at this pose tile's shared memory).
 template <int PT>
-static void bsolve(const DevSym &s, int P, const float *X, const float *L21, const float *L21T, Vec4<float> *sol,
+static int resident_bsolve(size_t smem) {
+    int dev = 0, sms = 0, a = 0, b = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        return 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_bsolve_fwd<PT>, kThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bsolve_bwd<PT>, kThreads, smem);
+    return std::max(1, std::min(a, b) * sms);
+}
+
+int batch_grid(const DevSym &s, int P, int pt) {
+    const size_t smem = batch_solve_smem_bytes(s.max_ldx, s.max_ld21, pt);
+    const int T = (P + pt - 1) / pt;
+    int res = 1;
+    switch (pt) {
+    case 16: res = resident_bsolve<16>(smem); break;
+    case 8: res = resident_bsolve<8>(smem); break;
+    case 4: res = resident_bsolve<4>(smem); break;
+    case 2: res = resident_bsolve<2>(smem); break;
+    default: res = resident_bsolve<1>(smem); break;
+    }
+    const long long ntask = (long long)s.S * T;
+    return (int)std::max(1LL, std::min<long long>(ntask, res));
+}
+
+template <int PT>
+static void bsolve(const DevSym &s, int P, int grid, const float *X, const float *L21, const float *L21T, Vec4<float> *sol,
                    Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32, unsigned long long *ticket,
                    unsigned *flags, int *err, bool forward, cudaStream_t st) {
     const int T = (P + PT - 1) / PT;
     const BLayout lay{s.max_ldx, s.max_ld21};
     const size_t smem = batch_solve_smem_bytes(s.max_ldx, s.max_ld21, PT);
-    const int grid = s.S * T;
+    const unsigned long long Z = (unsigned long long)s.S * T + grid;
     if (forward)
-        k_bsolve_fwd<PT><<<grid, kThreads, smem, st>>>(s.S, T, P, lay, s.level_sn, s.sn, s.child, s.relind, X, L21,
-                                                       sol, uvec, ticket, flags, err);
+        k_bsolve_fwd<PT><<<grid, kThreads, smem, st>>>(s.S, T, P, Z, lay, s.level_sn, s.sn, s.child, s.relind, X,
+                                                       L21, sol, uvec, ticket, flags, err);
     else
-        k_bsolve_bwd<PT><<<grid, kThreads, smem, st>>>(s.S, T, P, lay, s.level_sn, s.sn, s.rows, X, L21T, sol, pc64,
-                                                       pc32, ticket, flags, err);
+        k_bsolve_bwd<PT><<<grid, kThreads, smem, st>>>(s.S, T, P, Z, lay, s.level_sn, s.sn, s.rows, X, L21T, sol,
+                                                       pc64, pc32, ticket, flags, err);
 }
 
-void launch_bsolve(const DevSym &s, int P, int pt, const float *X, const float *L21, const float *L21T,
+void launch_bsolve(const DevSym &s, int P, int pt, int grid, const float *X, const float *L21, const float *L21T,
                    Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
                    unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st) {
     if (s.S == 0) return;
     switch (pt) {
-    case 16: bsolve<16>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
-    case 8: bsolve<8>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
-    case 4: bsolve<4>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
-    case 2: bsolve<2>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
-    default: bsolve<1>(s, P, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    case 16: bsolve<16>(s, P, grid, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    case 8: bsolve<8>(s, P, grid, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    case 4: bsolve<4>(s, P, grid, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    case 2: bsolve<2>(s, P, grid, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
+    default: bsolve<1>(s, P, grid, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
     }
 }
 

@@ -139,17 +139,19 @@ struct arap_ctx {
     DevBuf vf_ptr, vf_face, fnorm, vnorm;    // vertex normals
     // many-pose state (arap_deform_poses)
     DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
-    int bP = 0, bT = 0, bS = -1, bpt = 0;
-    int tP = -1;  // poses whose targets arap_pose_targets left in btargets (-1: none)
+    int bP = 0, bT = 0, bpt = 0, bgrid = 0;
+    int64_t bgen = -1;  // gen the many-pose buffers and counters were set up for (-1: redo)
+    int pose_tile = 0;  // poses per batched-solve task (0: the largest that fits)
+    int tP = -1;  // poses whose targets btargets holds (-1: none)
     int model_P = 1, model_T = 1;  // poses / pose tiles of the last deform (cost model)
     // CUDA graphs of the setup and of 2^k iterations (k < kIterGraphs); a deform
     // of n iterations replays the graphs of n's binary digits, so any count
     // reuses them. Replayed while nothing they reference changes (direct
     // launches when profiling).
     static constexpr int kIterGraphs = 8;
-    cudaGraphExec_t g_setup = nullptr, g_iter[kIterGraphs] = {};
-    int64_t g_setup_key[4] = {0, 0, 0, 0}, g_iter_key[kIterGraphs][4] = {};
-    int64_t g_setup_launches = 0, g_iter_launches[kIterGraphs] = {};
+    cudaGraphExec_t g_setup = nullptr, g_iter[kIterGraphs] = {}, g_biter[kIterGraphs] = {};
+    int64_t g_setup_key[4] = {0, 0, 0, 0}, g_iter_key[kIterGraphs][4] = {}, g_biter_key[kIterGraphs][4] = {};
+    int64_t g_setup_launches = 0, g_iter_launches[kIterGraphs] = {}, g_biter_launches[kIterGraphs] = {};
     int64_t gen = 1;  // bumped when the symbolic analysis or any device buffer changes
     bool use_graphs = true;
     int solve_cap = 0;  // most CTAs per triangular-solve launch (0: as many as fit the device)
@@ -650,6 +652,57 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
     return ARAP_OK;
 }
 
+// `iterations` local/global iterations of P poses at once (the loop of
+// arap.h:122-129 per pose), the two triangular solves each one persistent
+// launch over all (supernode, pose tile) tasks.
+int run_batch_iterations(arap_ctx *ctx, int P, int iterations) {
+    const Symbolic &s = ctx->sym;
+    const DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    const int m = s.m;
+    unsigned long long *tk = ctx->bticket.as<unsigned long long>();
+    unsigned *fl = ctx->bflags.as<unsigned>();
+    const size_t fhalf = (size_t)std::max(s.S, 1) * ctx->bT;
+    for (int it = 0; it < iterations; ++it) {
+        {
+            Prof pr(ctx, ARAP_K_LOCAL);
+            launch_blocal(d, P, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
+                          ctx->bR.as<Vec4<float>>(), st);
+        }
+        ctx->launches += 1;
+        if (m == 0) continue;
+        {
+            Prof pr(ctx, ARAP_K_RHS);
+            launch_brhs(d, P, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(), ctx->bR.as<Vec4<float>>(),
+                        ctx->bb.as<Vec4<float>>(), st);
+        }
+        ctx->launches += 1;
+        for (int r = 0; r <= ctx->refine; ++r) {
+            {
+                Prof pr(ctx, ARAP_K_RESIDUAL);
+                launch_bresidual(d, P, ctx->w64.as<double>(), ctx->diag64.as<double>(),
+                                 ctx->bbfixed.as<Vec4<double>>(), ctx->bb.as<Vec4<float>>(),
+                                 ctx->bpc64.as<Vec4<double>>(), ctx->bsol.as<Vec4<float>>(), st);
+            }
+            {
+                Prof pr(ctx, ARAP_K_SOLVE_FWD);
+                launch_bsolve(d, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
+                              ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), nullptr, nullptr, tk, fl,
+                              ctx->errw.as<int>(), true, st);
+            }
+            {
+                Prof pr(ctx, ARAP_K_SOLVE_BWD);
+                launch_bsolve(d, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
+                              ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
+                              ctx->bpc32.as<Vec4<float>>(), tk + 1, fl + fhalf, ctx->errw.as<int>(), false, st);
+            }
+            ctx->launches += 3;
+        }
+    }
+    CK(cudaGetLastError());
+    return ARAP_OK;
+}
+
 int check_ctx(const arap_ctx *ctx) { return ctx ? ARAP_OK : ARAP_ERR_INVALID_ARGUMENT; }
 
 }  // namespace
@@ -802,6 +855,8 @@ void arap_destroy(arap_ctx *ctx) {
     if (ctx->g_setup) cudaGraphExecDestroy(ctx->g_setup);
     for (cudaGraphExec_t g : ctx->g_iter)
         if (g) cudaGraphExecDestroy(g);
+    for (cudaGraphExec_t g : ctx->g_biter)
+        if (g) cudaGraphExecDestroy(g);
     if (ctx->herr_host) pinned_words().put(ctx->herr_host);
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -921,42 +976,61 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
     const Symbolic &s = ctx->sym;
     const DevSym &d = ctx->ds;
     const int V = s.V, m = s.m, P = n_poses, nc = V - m;
-    if (ctx->bS != s.S || ctx->bP != P) {
-        const int pt = batch_pose_tile(s.max_ldx, s.max_ld21);
-        if (pt == 0) return fail(ctx, ARAP_ERR_UNSUPPORTED, "supernode fronts too large for the batched solves");
+    int pt = ctx->pose_tile;
+    if (pt == 0) pt = batch_pose_tile(s.max_ldx, s.max_ld21);
+    else if (!batch_pose_tile_fits(s.max_ldx, s.max_ld21, pt))
+        return fail(ctx, ARAP_ERR_UNSUPPORTED,
+                    "pose tile " + std::to_string(pt) + " does not fit this mesh's largest supernode");
+    if (pt == 0) return fail(ctx, ARAP_ERR_UNSUPPORTED, "supernode fronts too large for the batched solves");
+    if (ctx->bgen != ctx->gen || ctx->bP != P || ctx->bpt != pt) {
         const size_t smem = batch_solve_smem_bytes(s.max_ldx, s.max_ld21, pt);
         if (pt != ctx->bpt || smem > ctx->bsmem) {
             CK(configure_batch_smem(s.max_ldx, s.max_ld21, pt));
             ctx->bsmem = smem;
         }
-        ctx->bpt = pt;
-        ctx->bT = (P + pt - 1) / pt;
+        const int T = (P + pt - 1) / pt;
         const size_t VP = (size_t)V * P, MP = (size_t)std::max(m, 1) * P;
-        CK(ctx->bpc64.ensure(VP * sizeof(Vec4<double>)));
-        CK(ctx->bpc32.ensure(VP * sizeof(Vec4<float>)));
-        CK(ctx->bR.ensure(VP * 3 * sizeof(Vec4<float>)));
-        CK(ctx->bbfixed.ensure(MP * sizeof(Vec4<double>)));
-        CK(ctx->bb.ensure(MP * sizeof(Vec4<float>)));
-        CK(ctx->bsol.ensure(MP * sizeof(Vec4<float>)));
-        CK(ctx->buvec.ensure((size_t)std::max<int64_t>(s.uvec_size, 1) * P * sizeof(Vec4<float>)));
-        CK(ctx->bout.ensure(VP * 3 * sizeof(double)));
-        CK(ctx->btargets.ensure((size_t)P * nc * 3 * sizeof(double)));
-        const size_t nflags = (size_t)2 * std::max(s.S, 1) * ctx->bT;
-        CK(ctx->bticket.ensure(2 * sizeof(unsigned long long)));
-        CK(ctx->bflags.ensure(nflags * sizeof(unsigned)));
+        const size_t nflags = (size_t)2 * std::max(s.S, 1) * T;
+        const std::pair<DevBuf *, size_t> plan[] = {
+            {&ctx->bpc64, VP * sizeof(Vec4<double>)},
+            {&ctx->bpc32, VP * sizeof(Vec4<float>)},
+            {&ctx->bR, VP * 3 * sizeof(Vec4<float>)},
+            {&ctx->bbfixed, MP * sizeof(Vec4<double>)},
+            {&ctx->bb, MP * sizeof(Vec4<float>)},
+            {&ctx->bsol, MP * sizeof(Vec4<float>)},
+            {&ctx->buvec, (size_t)std::max<int64_t>(s.uvec_size, 1) * P * sizeof(Vec4<float>)},
+            {&ctx->bout, VP * 3 * sizeof(double)},
+            {&ctx->btargets, (size_t)P * nc * 3 * sizeof(double)},
+            {&ctx->bticket, 2 * sizeof(unsigned long long)},
+            {&ctx->bflags, nflags * sizeof(unsigned)}};
+        bool moved = false;
+        void *const old_targets = ctx->btargets.p;
+        for (const auto &pb : plan) {
+            void *before = pb.first->p;
+            CK(pb.first->ensure(pb.second));
+            moved |= before != pb.first->p;
+        }
+        if (moved) ctx->gen++;  // captured graphs hold the old addresses
+        if (ctx->btargets.p != old_targets) ctx->tP = -1;
+        // scheduling counters restart: each launch then consumes a fixed
+        // number of tickets (tasks + CTAs), so the grid is fixed with them
         CK(cudaMemsetAsync(ctx->bticket.p, 0, 2 * sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(ctx->bflags.p, 0, nflags * sizeof(unsigned), st));
-        ctx->bS = s.S;
+        int grid = batch_grid(d, P, pt);
+        if (ctx->solve_cap > 0) grid = std::min(grid, ctx->solve_cap);
+        ctx->bpt = pt;
+        ctx->bT = T;
+        ctx->bgrid = grid;
         ctx->bP = P;
-    } else if (!targets && !ctx->btargets.p) {
-        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no targets uploaded yet");
+        ctx->bgen = ctx->gen;
     }
-    if (!targets && ctx->tP >= 0 && ctx->tP != P)
-        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "arap_pose_targets computed targets for another pose count");
+    if (!targets && ctx->tP < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no targets on the device yet");
+    if (!targets && ctx->tP != P)
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "the targets on the device are for another pose count");
     if (targets) {
         CK(cudaMemcpyAsync(ctx->btargets.p, targets, (size_t)P * nc * 3 * sizeof(double), cudaMemcpyHostToDevice,
                            st));
-        ctx->tP = -1;
+        ctx->tP = P;
     }
     {
         Prof pr(ctx, ARAP_K_ASSEMBLE);
@@ -969,44 +1043,16 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
     CK(cudaEventRecord(ctx->ev1, st));
     ctx->model_P = P;
     ctx->model_T = ctx->bT;
-    unsigned long long *tk = ctx->bticket.as<unsigned long long>();
-    unsigned *fl = ctx->bflags.as<unsigned>();
-    const size_t fhalf = (size_t)std::max(s.S, 1) * ctx->bT;
-    for (int it = 0; it < iterations; ++it) {
-        {
-            Prof pr(ctx, ARAP_K_LOCAL);
-            launch_blocal(d, P, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
-                          ctx->bR.as<Vec4<float>>(), st);
-        }
-        ctx->launches += 1;
-        if (m == 0) continue;
-        {
-            Prof pr(ctx, ARAP_K_RHS);
-            launch_brhs(d, P, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(), ctx->bR.as<Vec4<float>>(),
-                        ctx->bb.as<Vec4<float>>(), st);
-        }
-        ctx->launches += 1;
-        for (int r = 0; r <= ctx->refine; ++r) {
-            {
-                Prof pr(ctx, ARAP_K_RESIDUAL);
-                launch_bresidual(d, P, ctx->w64.as<double>(), ctx->diag64.as<double>(),
-                                 ctx->bbfixed.as<Vec4<double>>(), ctx->bb.as<Vec4<float>>(),
-                                 ctx->bpc64.as<Vec4<double>>(), ctx->bsol.as<Vec4<float>>(), st);
-            }
-            {
-                Prof pr(ctx, ARAP_K_SOLVE_FWD);
-                launch_bsolve(d, P, ctx->bpt, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
-                              ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), nullptr, nullptr, tk, fl,
-                              ctx->errw.as<int>(), true, st);
-            }
-            {
-                Prof pr(ctx, ARAP_K_SOLVE_BWD);
-                launch_bsolve(d, P, ctx->bpt, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
-                              ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
-                              ctx->bpc32.as<Vec4<float>>(), tk + 1, fl + fhalf, ctx->errw.as<int>(), false, st);
-            }
-            ctx->launches += 3;
-        }
+    for (int left = iterations; left > 0;) {
+        int k = 0;
+        while (k + 1 < arap_ctx::kIterGraphs && (2 << k) <= left) ++k;
+        const int n = 1 << k;
+        const int64_t key[4] = {ctx->gen, P, n + ((int64_t)ctx->refine << 32),
+                                ctx->bpt + ((int64_t)ctx->bgrid << 32)};
+        const int rc = graph_or_direct(ctx, ctx->g_biter[k], ctx->g_biter_key[k], key, ctx->g_biter_launches[k],
+                                       [&] { return run_batch_iterations(ctx, P, n); });
+        if (rc != ARAP_OK) return rc;
+        left -= n;
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev2, st));
@@ -1253,7 +1299,7 @@ int arap_wait(arap_ctx *ctx) {
         // scheduling counters may be inconsistent now: rebuild them next time
         ctx->sym_valid = false;
         ctx->dirty = true;
-        ctx->bS = -1;
+        ctx->bgen = -1;
         return fail(ctx, ARAP_ERR_TIMEOUT, "a bounded in-kernel wait expired");
     }
     return ARAP_OK;
@@ -1301,6 +1347,18 @@ int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas) {
         ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
         ctx->dirty = true;
     }
+    return ARAP_OK;
+}
+
+int arap_set_pose_tile(arap_ctx *ctx, int32_t poses) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (poses != 0 && poses != 1 && poses != 2 && poses != 4 && poses != 8 && poses != 16)
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "pose tile must be 0, 1, 2, 4, 8 or 16");
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    ctx->pose_tile = poses;  // a changed tile resets the batched solves' counters at the next call
     return ARAP_OK;
 }
 

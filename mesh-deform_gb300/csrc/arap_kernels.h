@@ -124,7 +124,11 @@ size_t batch_solve_smem_bytes(int max_ldx, int max_ld21, int pt);
 // largest pose tile (16, 8, 4, 2, 1) the batched solves support for these
 // front sizes, 0 when none fits
 int batch_pose_tile(int max_ldx, int max_ld21);
+// whether tiles of pt poses (1, 2, 4, 8 or 16) fit the batched solve kernels
+bool batch_pose_tile_fits(int max_ldx, int max_ld21, int pt);
 cudaError_t configure_batch_smem(int max_ldx, int max_ld21, int pt);
+// CTAs of one persistent batched solve launch for P poses in tiles of pt
+int batch_grid(const DevSym &s, int P, int pt);
 void launch_bsetup(const DevSym &s, int P, const Vec4<double> *p64, const double *targets, Vec4<double> *pc64,
                    Vec4<float> *pc32, Vec4<float> *R, cudaStream_t st);
 void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double> *pc64, Vec4<double> *bfixed,
@@ -135,7 +139,9 @@ void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *re
                  Vec4<float> *b, cudaStream_t st);
 void launch_bresidual(const DevSym &s, int P, const double *w64, const double *diag64, const Vec4<double> *bfixed,
                       const Vec4<float> *b, const Vec4<double> *x, Vec4<float> *r, cudaStream_t st);
-void launch_bsolve(const DevSym &s, int P, int pt, const float *X, const float *L21, const float *L21T,
+// one persistent launch of `grid` CTAs (batch_grid) over all (supernode, pose
+// tile) tasks; the grid must stay fixed while the ticket counter is not reset
+void launch_bsolve(const DevSym &s, int P, int pt, int grid, const float *X, const float *L21, const float *L21T,
                    Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
                    unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st);
 void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *out, cudaStream_t st);

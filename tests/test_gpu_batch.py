@@ -85,3 +85,50 @@ def test_pose_targets_rejects_unconstrained_handle(gpu):
         with pytest.raises(gpu.ArapError) as e:
             ctx.pose_targets([int(free)], w.info["transforms"], w.info["origin"])
         assert e.value.code == gpu.ARAP_ERR_BAD_INDEX
+
+
+def test_pose_tile_and_launch_shape_give_identical_results(gpu):
+    """Each (supernode, pose tile) task sums its columns in the same order
+    whatever the tile or the number of persistent CTAs, so every launch shape
+    gives bit-identical poses; repeated calls (graph capture on the second
+    call, replay on the third) and graphs switched off repeat them too. 19
+    poses leave a ragged last tile for every tile size; 7 iterations run
+    through the 4-, 2- and 1-iteration graphs."""
+    w = W.cfg_pose_batch(level=4, n_poses=19, iterations=7)
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.poses[0])
+        ref = ctx.deform_poses(w.poses, 7)
+        for _ in range(2):
+            np.testing.assert_array_equal(ctx.deform_poses(None, 7), ref)
+        for pt in (1, 2, 4, 8, 16):
+            ctx.set_pose_tile(pt)
+            for _ in range(3):
+                np.testing.assert_array_equal(ctx.deform_poses(None, 7), ref, err_msg=f"pose tile {pt}")
+        ctx.set_pose_tile(0)
+        for ctas in (1, 5, 0):
+            ctx.set_solve_ctas(ctas)
+            for _ in range(3):
+                np.testing.assert_array_equal(ctx.deform_poses(w.poses, 7), ref, err_msg=f"{ctas} CTAs")
+        ctx.set_graphs(False)
+        np.testing.assert_array_equal(ctx.deform_poses(None, 7), ref)
+        with pytest.raises(gpu.ArapError) as e:
+            ctx.set_pose_tile(3)
+        assert e.value.code == gpu.ARAP_ERR_INVALID_ARGUMENT
+
+
+def test_pose_batch_pose_count_change_resets_schedule(gpu):
+    """Changing the pose count between calls (new tiles, new grid, new
+    scheduling counters) keeps every call exact against the per-pose batch."""
+    w = W.cfg_pose_batch(level=3, n_poses=9, iterations=4)
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.poses[0])
+        full = ctx.deform_poses(w.poses, 4)
+        for n in (1, 5, 9, 3, 9):
+            for _ in range(2):
+                np.testing.assert_array_equal(ctx.deform_poses(w.poses[:n], 4), full[:n])
+        # the device holds targets for 9 poses, not for 5
+        assert ctx.lib.arap_deform_poses(ctx.h, 5, None, 4, None) == gpu.ARAP_ERR_INVALID_ARGUMENT
