@@ -208,6 +208,16 @@ def run_batch(args):
     ctx.set_rest_positions(w.positions)
     ctx.set_constraints(w.cidx, w.poses[0])
     first = ctx.deform_poses(w.poses, w.iterations)
+    tuned = None
+    if args.pose_tile < 0:
+        import arap_tune
+
+        best, times = arap_tune.tune_pose_tile(ctx, w.iterations)
+        tuned = {"pose_tile": best, "ms_per_call": {str(k): round(v, 3) for k, v in times.items()}}
+        log(f"autotuned pose tile: {best} {tuned['ms_per_call']}")
+        args.pose_tile = best
+    else:
+        ctx.set_pose_tile(args.pose_tile)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -321,7 +331,8 @@ def run_batch(args):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": config_of(w, args, {"poses": P, "step": f"dirty deform of {P} poses (one shared factor)",
-                                      "precision": "mixed"}),
+                                      "precision": "mixed", "pose_tile": args.pose_tile,
+                                      "pose_tile_autotune": tuned}),
         "e2e": {"value": its_total / e2e_total if e2e_s else None, "unit": UNIT,
                 "h2d_bytes_per_step": int(tf_h.nbytes + handles.nbytes + 96), "d2h_bytes_per_step": int(out_h.nbytes),
                 "inputs": "P rigid transforms, targets mapped on the device"},
@@ -512,6 +523,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: skip the end-to-end pass")
     ap.add_argument("--poses", type=int, default=256, help="pose_batch: handle poses per step")
+    ap.add_argument("--pose-tile", type=int, default=-1,
+                    help="pose_batch: poses per batched-solve task (0: largest that fits; -1: autotuned)")
     ap.add_argument("--solve-ctas", type=int, default=-1,
                     help="CTAs per triangular-solve launch (0: as many as fit; -1: autotuned for the concurrency)")
     ap.add_argument("--concurrent", type=int, default=os.cpu_count() or 1,

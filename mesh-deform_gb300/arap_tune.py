@@ -1,6 +1,7 @@
 """Launch-shape autotuner: picks the number of CTAs per triangular-solve
 launch (arap_set_solve_ctas) for a workload and a number of requests in
-flight, by timing short trial runs through the C ABI.
+flight, and the pose tile of the batched solves (arap_set_pose_tile), by
+timing short trial runs through the C ABI.
 
 One request alone is fastest with as many CTAs as fit on the device (the
 default, 0); several requests in flight share the SMs, and a smaller count
@@ -79,3 +80,39 @@ def tune_solve_ctas(positions, faces, cidx, ctargets, iterations: int, precision
         except Exception:
             pass
     return best, rates
+
+
+POSE_TILES = (1, 2, 4, 8, 16)
+
+
+def tune_pose_tile(ctx, iterations: int, candidates=POSE_TILES, trials: int = 2, dirty: bool = True):
+    """Returns (best_tile, {tile: ms per call}) for arap_deform_poses on a
+    context whose pose targets are already on the device (a previous
+    deform_poses or pose_targets). Tiles the mesh's fronts do not allow are
+    skipped. dirty=True times a full dirty call (weights and factor included),
+    as DeformationUtil's loop of dirty deforms does. Leaves the best tile set."""
+    times = {}
+    for pt in candidates:
+        try:
+            ctx.set_pose_tile(int(pt))
+            ctx.deform_poses(None, iterations)  # schedule reset and first launch, untimed
+            ctx.deform_poses(None, iterations)  # graph capture, untimed
+        except G.ArapError as e:
+            if e.code == G.ARAP_ERR_UNSUPPORTED:
+                continue
+            raise
+        best = float("inf")
+        for _ in range(max(1, trials)):
+            if dirty:
+                ctx.invalidate()
+            t0 = time.perf_counter()
+            rc = ctx.deform_poses_rc(None, iterations, None)
+            if rc != G.ARAP_OK:
+                raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+            best = min(best, time.perf_counter() - t0)
+        times[int(pt)] = 1e3 * best
+    if not times:
+        raise G.ArapError(G.ARAP_ERR_UNSUPPORTED, "no pose tile fits this mesh")
+    best_pt = min(times, key=times.get)
+    ctx.set_pose_tile(best_pt)
+    return best_pt, times

@@ -257,10 +257,6 @@ k_bsolve_fwd(int S, int T, int P, unsigned long long nz, BLayout lay, const int3
         store_items<PT, 1>(NQb, acc, Fb);
         __syncthreads();
     }
-    for (int e = tid; e < nc * PT; e += kThreads) {
-        const int i = e / PT, p = e % PT;
-        if (p0 + p < P) sol[(int64_t)(d.first + i) * P + p0 + p] = Y[e];
-    }
     for (int e = tid; e < nb * PT; e += kThreads) {
         const int i = e / PT, p = e % PT;
         if (p0 + p < P) uvec[(d.uvec_off + i) * P + p0 + p] = Fb[e];
@@ -269,6 +265,12 @@ k_bsolve_fwd(int S, int T, int P, unsigned long long nz, BLayout lay, const int3
     // which is cumulative: a CTA that acquires the flag sees them all
     __syncthreads();
     if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
+    // y of the columns is read only by the backward sweep (a later launch):
+    // stored after the release; Y is next written after a barrier
+    for (int e = tid; e < nc * PT; e += kThreads) {
+        const int i = e / PT, p = e % PT;
+        if (p0 + p < P) sol[(int64_t)(d.first + i) * P + p0 + p] = Y[e];
+    }
     ph[0] += (unsigned)(ntot + 1) / 2u;
     ph[1] += (unsigned)ntot / 2u;
     }
@@ -351,10 +353,19 @@ k_bsolve_bwd(int S, int T, int P, unsigned long long nz, BLayout lay, const int3
     __syncthreads();
     for (int e = tid; e < nc * PT; e += kThreads) {
         const int i = e / PT, p = e % PT;
+        if (p0 + p < P) sol[(int64_t)(d.first + i) * P + p0 + p] = Xv[e];
+    }
+    // the barrier orders every thread's writes before thread 0's release,
+    // which is cumulative: a CTA that acquires the flag sees them all
+    __syncthreads();
+    if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
+    // the positions are read by no other task of this sweep: updated after
+    // the release; Xv is next written after a barrier
+    for (int e = tid; e < nc * PT; e += kThreads) {
+        const int i = e / PT, p = e % PT;
         if (p0 + p >= P) continue;
         const int64_t k = (int64_t)(d.first + i) * P + p0 + p;
         const Vec4<float> x = Xv[e];
-        sol[k] = x;
         Vec4<double> v = pc64[k];
         v.x += (double)x.x;
         v.y += (double)x.y;
@@ -362,10 +373,6 @@ k_bsolve_bwd(int S, int T, int P, unsigned long long nz, BLayout lay, const int3
         pc64[k] = v;
         pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
     }
-    // the barrier orders every thread's writes before thread 0's release,
-    // which is cumulative: a CTA that acquires the flag sees them all
-    __syncthreads();
-    if (tid == 0) st_release(flags + (int64_t)s * T + tile, epoch);
     ph[0] += (unsigned)(ntot + 1) / 2u;
     ph[1] += (unsigned)ntot / 2u;
     }

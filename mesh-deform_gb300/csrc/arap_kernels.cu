@@ -1003,12 +1003,15 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
         }
     }
     if (pl.nB > 0) reduce_quads<T, true>(Qb, ax, ay, az, red, fb);
-    for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
     // the barrier orders every thread's writes before thread 0's release,
     // which is cumulative: a CTA that acquires the flag sees them all
     __syncthreads();
     if (tid == 0) st_release(flags + s, epoch);
+    // y of this supernode's columns is read only by the backward sweep (a
+    // later launch): stored after the release, off the parent's critical
+    // path. yv is next written after a barrier of the next task.
+    for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
     ph[0] += (unsigned)(ntot + 1) / 2u;
     ph[1] += (unsigned)ntot / 2u;
     }
@@ -1094,10 +1097,17 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
         }
     }
     reduce_quads<T, false>(Q, ax, ay, az, red, xv);
+    for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = xv[i];
+    // the barrier orders every thread's writes before thread 0's release,
+    // which is cumulative: a CTA that acquires the flag sees them all
+    __syncthreads();
+    if (tid == 0) st_release(flags + s, epoch);
+    // the positions are read by no other task of this sweep: updated after
+    // the release, off the children's critical path. xv is next written
+    // after a barrier of the next task.
     for (int i = tid; i < nc; i += kSolveThreads) {
         const Vec4<T> x = xv[i];
         const int k = d.first + i;
-        sol[k] = x;
         if (mode == 0) {
             pc64[k] = {(double)x.x, (double)x.y, (double)x.z, 0.0};
         } else {
@@ -1109,10 +1119,6 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
             pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
         }
     }
-    // the barrier orders every thread's writes before thread 0's release,
-    // which is cumulative: a CTA that acquires the flag sees them all
-    __syncthreads();
-    if (tid == 0) st_release(flags + s, epoch);
     ph[0] += (unsigned)(ntot + 1) / 2u;
     ph[1] += (unsigned)ntot / 2u;
     }
