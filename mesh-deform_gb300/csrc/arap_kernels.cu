@@ -320,81 +320,99 @@ k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, T
     }
 }
 
-// Diagonal block jb of a front: Cholesky and inverse in shared memory, then the
-// rows below are solved against it (L_ib = A_ib inv(L_bb)^T), one row per thread.
+// Diagonal block jb of a front: Cholesky and inverse by one warp in registers,
+// then the rows below are solved against it (L_ib = A_ib inv(L_bb)^T), one row
+// per thread of warps 1-7, which load their first rows while warp 0 factors.
+// Every step is written without divergent branches (selects instead), so the
+// shuffles of a step issue back to back and their latencies overlap; the row
+// solve runs column by column over 32 independent sums.
 template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
 k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF *__restrict__ Lval,
       TF *__restrict__ Dinv, int *err) {
-    __shared__ TF Db[NB][NB + 1];  // the factored block, row-major
-    __shared__ TF Di[NB][NB + 1];  // its inverse
+    __shared__ __align__(16) TF Xc[NB][NB];  // inverse of the factored block, column-major: Xc[c][r] = X(r, c)
     const SnInfo d = sn[items[blockIdx.x].sn];
     const int n = d.nrow, nc = d.ncol;
     const int j0 = jb * NB, w = min(NB, nc - j0);
     TF *P = Lval + d.panel_off;
     const int tid = threadIdx.x, lane = tid & 31;
+    constexpr int kRowThreads = kFactorThreads - 32;
+    const int i_first = j0 + w + (tid - 32);  // warps 1-7: first trailing row
+    TF a[NB];
     if (tid < 32) {
-        // one warp: row `lane` of the block in registers, right-looking
-        // Cholesky with the pivot column broadcast by shuffles (the same
-        // operations in the same order as a column-by-column update)
-        TF a[NB];
+        // row `lane` of the block, right-looking Cholesky (the operations of a
+        // column-by-column update, in the same order)
 #pragma unroll
         for (int c = 0; c < NB; ++c) a[c] = (lane < w && c <= lane) ? P[(int64_t)(j0 + c) * n + j0 + lane] : (TF)0;
         bool bad = false;
+        TF myinv = (TF)0;  // 1 / L(lane, lane)
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
             if (k < w) {
                 TF akk = __shfl_sync(0xffffffffu, a[k], k);
-                if (!(akk > (TF)0)) {
-                    bad = true;
-                    akk = (TF)1;
-                }
+                bad |= !(akk > (TF)0);
+                akk = (akk > (TF)0) ? akk : (TF)1;
                 const TF dk = tsqrt(akk), inv = (TF)1 / dk;
-                if (lane == k) a[k] = dk;
-                else if (lane > k) a[k] *= inv;
+                a[k] = (lane == k) ? dk : a[k] * inv;  // zero above the diagonal stays zero
+                myinv = (lane == k) ? inv : myinv;
+                TF l[NB];
 #pragma unroll
-                for (int c = k + 1; c < NB; ++c) {
-                    const TF lck = __shfl_sync(0xffffffffu, a[k], c);  // L(c, k)
-                    if (lane >= c) a[c] -= a[k] * lck;
-                }
+                for (int c = k + 1; c < NB; ++c) l[c] = __shfl_sync(0xffffffffu, a[k], c);  // L(c, k)
+                const TF lk = a[k];
+#pragma unroll
+                for (int c = k + 1; c < NB; ++c) a[c] -= ((lane >= c) ? lk : (TF)0) * l[c];
             }
         }
         if (bad && lane == 0) atomicOr(err, kErrNotSpd);
+        // X = inv(L), lane = row, right-looking: at step t row t of X lacks
+        // only the division by L(t, t); it is broadcast and every later row i
+        // subtracts L(i, t) X(t, :)
+        TF y[NB];
 #pragma unroll
-        for (int c = 0; c < NB; ++c) Db[lane][c] = (lane < w && c <= lane) ? a[c] : (TF)0;
-        __syncwarp();
-        // inverse of the lower-triangular block: lane c forms column c by
-        // forward substitution (entries above the diagonal stay zero)
-        TF x[NB];
+        for (int j = 0; j < NB; ++j) y[j] = (j == lane && lane < w) ? (TF)1 : (TF)0;
 #pragma unroll
-        for (int i = 0; i < NB; ++i) {
-            TF acc = (i == lane) ? (TF)1 : (TF)0;
+        for (int t = 0; t < NB; ++t) {
+            if (t < w) {
+                TF xt[NB];
 #pragma unroll
-            for (int t = 0; t < i; ++t) acc -= Db[i][t] * x[t];
-            x[i] = (i < w && i >= lane) ? acc / Db[i][i] : (TF)0;
+                for (int j = 0; j <= t; ++j) {
+                    y[j] = (lane == t) ? y[j] * myinv : y[j];
+                    xt[j] = __shfl_sync(0xffffffffu, y[j], t);
+                }
+                const TF m = (lane > t) ? a[t] : (TF)0;
+#pragma unroll
+                for (int j = 0; j <= t; ++j) y[j] -= m * xt[j];
+            }
         }
 #pragma unroll
-        for (int i = 0; i < NB; ++i) Di[i][lane] = x[i];
+        for (int c = 0; c < NB; ++c) {
+            Xc[c][lane] = y[c];  // zero above the diagonal and outside the block
+            if (lane < w && c <= lane) P[(int64_t)(j0 + c) * n + j0 + lane] = a[c];
+        }
+    } else if (i_first < n) {
+#pragma unroll
+        for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i_first] : (TF)0;
     }
     __syncthreads();
-    for (int q = tid; q < NB * NB; q += kFactorThreads) {
-        const int r = q % NB, c = q / NB;
-        if (r < w && c < w && c <= r) P[(int64_t)(j0 + c) * n + j0 + r] = Db[r][c];
-        Dinv[d.dinv_off + (int64_t)jb * NB * NB + (int64_t)c * NB + r] = Di[r][c];
-    }
-    for (int i = j0 + w + tid; i < n; i += kFactorThreads) {
-        TF a[NB];
+    for (int q = tid; q < NB * NB; q += kFactorThreads)
+        Dinv[d.dinv_off + (int64_t)jb * NB * NB + q] = (&Xc[0][0])[q];  // column-major, as stored
+    if (tid < 32) return;
+    for (int i = i_first; i < n; i += kRowThreads) {
+        if (i != i_first) {
 #pragma unroll
-        for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i] : (TF)0;
-#pragma unroll 4
-        for (int r = 0; r < NB; ++r) {
-            if (r >= w) break;
-            TF acc = (TF)0;
-#pragma unroll
-            for (int c = 0; c < NB; ++c)
-                if (c <= r) acc += a[c] * Di[r][c];
-            P[(int64_t)(j0 + r) * n + i] = acc;
+            for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i] : (TF)0;
         }
+        TF acc[NB];
+#pragma unroll
+        for (int r = 0; r < NB; ++r) acc[r] = (TF)0;
+        // L(i, r) = sum_{c <= r} a[c] X(r, c), summed in increasing c as before
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+#pragma unroll
+            for (int r = c; r < NB; ++r) acc[r] += a[c] * Xc[c][r];
+#pragma unroll
+        for (int r = 0; r < NB; ++r)
+            if (r < w) P[(int64_t)(j0 + r) * n + i] = acc[r];
     }
 }
 
