@@ -702,8 +702,13 @@ k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ 
 #ifndef ARAP_SOLVE_CHUNK_KB
 #define ARAP_SOLVE_CHUNK_KB 16
 #endif
+#ifndef ARAP_SOLVE_BUFS
+#define ARAP_SOLVE_BUFS 2
+#endif
 constexpr int kSolveThreads = 256;
-constexpr int kChunkBytes = ARAP_SOLVE_CHUNK_KB * 1024;  // bytes per TMA chunk buffer (two buffers)
+constexpr int kChunkBytes = ARAP_SOLVE_CHUNK_KB * 1024;  // bytes per TMA chunk buffer
+constexpr int kSolveBufs = ARAP_SOLVE_BUFS;  // chunk buffers of a lower-level solve CTA (a ring)
+static_assert((kSolveBufs & (kSolveBufs - 1)) == 0 && kSolveBufs >= 2, "ring of 2, 4 or 8 buffers");
 constexpr int kRedRows = 4 * kSolveThreads;  // G * 4 * NQ <= 4 * threads
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -774,6 +779,13 @@ __device__ __forceinline__ void issue_chunk(const ChunkPlan<T> &pl, int k, T *bu
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // buffer reads done before the async write
     mbar_expect_tx(bar, bytes);
     tma_load_1d(buf, src, bytes, bar);
+}
+
+// Chunk buffer b of a lower-level solve CTA (the ring at the start of its
+// dynamic shared memory).
+template <typename T>
+__device__ __forceinline__ T *sbuf(unsigned char *raw, int b) {
+    return reinterpret_cast<T *>(raw + b * kChunkBytes);
 }
 
 // Bounded wait for a buffer's bytes. On expiry it records kErrTimeout and
@@ -900,24 +912,23 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
             const T *__restrict__ L21all, Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec,
             unsigned long long *ticket, unsigned *flags, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    T *buf0 = reinterpret_cast<T *>(smem_raw);
-    T *buf1 = reinterpret_cast<T *>(smem_raw + kChunkBytes);
-    Vec4<T> *fc = reinterpret_cast<Vec4<T> *>(smem_raw + 2 * kChunkBytes);
+    Vec4<T> *fc = reinterpret_cast<Vec4<T> *>(smem_raw + kSolveBufs * kChunkBytes);
     Vec4<T> *yv = fc + lay.ldx_max;
     Vec4<T> *fb = yv + lay.ldx_max;
     Vec4<T> *red = fb + lay.ld21_max;
-    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ __align__(8) uint64_t bars[kSolveBufs];
     __shared__ int s_task[2];  // this task's and the next one's ticket (taken early)
     __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int b = 0; b < kSolveBufs; ++b) mbar_init(&bars[b], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         next_task(ticket, S, Z, order, false, err, s_task[0], s_epoch[0]);
     }
     __syncthreads();
-    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
+    unsigned ph[kSolveBufs];  // phases each chunk buffer completed in earlier tasks
+#pragma unroll
+    for (int b = 0; b < kSolveBufs; ++b) ph[b] = 0u;
     for (int slot = 0;; slot ^= 1) {
     const int s = s_task[slot];
     if (s < 0) break;
@@ -928,9 +939,8 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     pl.init(Xall + d.x_off, d.ldx, nc, L21all + d.l21_off, d.ld21, nb > 0 ? nc : 0);
     const int ntot = pl.total();
     if (tid == 0) {
-        issue_chunk(pl, 0, buf0, &bars[0]);
-        if (ntot > 1) issue_chunk(pl, 1, buf1, &bars[1]);
-        for (int k = 2; k < ntot; ++k) prefetch_chunk_l2(pl, k);
+        for (int k = 0; k < ntot && k < kSolveBufs; ++k) issue_chunk(pl, k, sbuf<T>(smem_raw, k), &bars[k]);
+        for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
@@ -1002,8 +1012,9 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     const Quads Qa = quads_for(nc), Qb = quads_for(nb);
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
     for (int k = 0; k < ntot; ++k) {
-        T *buf = (k & 1) ? buf1 : buf0;
-        wait_chunk(&bars[k & 1], (ph[k & 1] + (unsigned)(k >> 1)) & 1u, err);
+        const int kb = k & (kSolveBufs - 1);
+        T *buf = sbuf<T>(smem_raw, kb);
+        wait_chunk(&bars[kb], (ph[kb] + (unsigned)(k / kSolveBufs)) & 1u, err);
         int c0, cn, ld;
         const T *src;
         pl.chunk(k, c0, cn, src, ld);
@@ -1013,7 +1024,7 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
             if (Qb.active()) chunk_axpy(buf, ld, cn, c0, Qb.q, Qb.g, Qb.G, yv, ax, ay, az);
         }
         __syncthreads();
-        if (tid == 0 && k + 2 < ntot) issue_chunk(pl, k + 2, buf, &bars[k & 1]);
+        if (tid == 0 && k + kSolveBufs < ntot) issue_chunk(pl, k + kSolveBufs, buf, &bars[kb]);
         if (k == pl.nA - 1) {
             reduce_quads<T, false>(Qa, ax, ay, az, red, yv);
 #pragma unroll
@@ -1030,8 +1041,8 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     // later launch): stored after the release, off the parent's critical
     // path. yv is next written after a barrier of the next task.
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
-    ph[0] += (unsigned)(ntot + 1) / 2u;
-    ph[1] += (unsigned)ntot / 2u;
+#pragma unroll
+    for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((ntot - b + kSolveBufs - 1) / kSolveBufs);
     }
 }
 
@@ -1046,24 +1057,23 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
             Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode,
             unsigned long long *ticket, unsigned *flags, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    T *buf0 = reinterpret_cast<T *>(smem_raw);
-    T *buf1 = reinterpret_cast<T *>(smem_raw + kChunkBytes);
-    Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw + 2 * kChunkBytes);
+    Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw + kSolveBufs * kChunkBytes);
     Vec4<T> *xv = zv + lay.ldx_max;
     Vec4<T> *gb = xv + lay.ldx_max;
     Vec4<T> *red = gb + lay.ld21_max;
-    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ __align__(8) uint64_t bars[kSolveBufs];
     __shared__ int s_task[2];  // this task's and the next one's ticket (taken early)
     __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int b = 0; b < kSolveBufs; ++b) mbar_init(&bars[b], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         next_task(ticket, S, Z, order, true, err, s_task[0], s_epoch[0]);
     }
     __syncthreads();
-    unsigned ph[2] = {0u, 0u};  // phases each chunk buffer completed in earlier tasks
+    unsigned ph[kSolveBufs];  // phases each chunk buffer completed in earlier tasks
+#pragma unroll
+    for (int b = 0; b < kSolveBufs; ++b) ph[b] = 0u;
     for (int slot = 0;; slot ^= 1) {
     const int s = s_task[slot];
     if (s < 0) break;
@@ -1076,9 +1086,8 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     const int ntot = pl.total();
     const int nA = nb > 0 ? pl.nA : 0;  // chunks of L21^T
     if (tid == 0) {
-        issue_chunk(pl, 0, buf0, &bars[0]);
-        if (ntot > 1) issue_chunk(pl, 1, buf1, &bars[1]);
-        for (int k = 2; k < ntot; ++k) prefetch_chunk_l2(pl, k);
+        for (int k = 0; k < ntot && k < kSolveBufs; ++k) issue_chunk(pl, k, sbuf<T>(smem_raw, k), &bars[k]);
+        for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     const int32_t *rs = rows + d.rows_off;
     for (int i = tid; i < d.ldx; i += kSolveThreads)
@@ -1099,15 +1108,16 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     const Quads Q = quads_for(nc);
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
     for (int k = 0; k < ntot; ++k) {
-        T *buf = (k & 1) ? buf1 : buf0;
-        wait_chunk(&bars[k & 1], (ph[k & 1] + (unsigned)(k >> 1)) & 1u, err);
+        const int kb = k & (kSolveBufs - 1);
+        T *buf = sbuf<T>(smem_raw, kb);
+        wait_chunk(&bars[kb], (ph[kb] + (unsigned)(k / kSolveBufs)) & 1u, err);
         int c0, cn, ld;
         const T *src;
         pl.chunk(k, c0, cn, src, ld);
         const Vec4<T> *v = (k < nA) ? gb : zv;
         if (Q.active()) chunk_axpy(buf, ld, cn, c0, Q.q, Q.g, Q.G, v, ax, ay, az);
         __syncthreads();
-        if (tid == 0 && k + 2 < ntot) issue_chunk(pl, k + 2, buf, &bars[k & 1]);
+        if (tid == 0 && k + kSolveBufs < ntot) issue_chunk(pl, k + kSolveBufs, buf, &bars[kb]);
         if (k == nA - 1) {
             reduce_quads<T, true>(Q, ax, ay, az, red, zv);
 #pragma unroll
@@ -1137,8 +1147,8 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
             pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
         }
     }
-    ph[0] += (unsigned)(ntot + 1) / 2u;
-    ph[1] += (unsigned)ntot / 2u;
+#pragma unroll
+    for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((ntot - b + kSolveBufs - 1) / kSolveBufs);
     }
 }
 
@@ -1682,7 +1692,7 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 }
 
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
-    return (size_t)2 * kChunkBytes + (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
+    return (size_t)kSolveBufs * kChunkBytes + (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
 }
 
 template <typename T>
