@@ -813,13 +813,16 @@ __device__ __forceinline__ void chunk_axpy(const T *buf, int ld, int cn, int c0,
     }
 }
 
-// Work split of a GEMV phase over the CTA: thread t owns the 4-row quad
-// q = t mod NQp of the result (NQ = ceil(rows / 4) quads, NQp the next power of
-// two, at most 256) for the columns g, g + G, ... (g = t div NQp, G = 256 /
-// NQp groups). Threads with q >= NQ only take part in the reductions.
+// Work split of a GEMV phase over the CTA: thread t owns the 4-row quad q of
+// the result (NQ = ceil(rows / 4) quads, at most 256) for the columns g,
+// g + G, ... Below 32 quads, q = t mod NQp and g = t div NQp with NQp the next
+// power of two (a warp's partial sums then meet by shuffles); from 32 quads
+// on, q = t mod NQ and g = t div NQ with G = 256 div NQ groups, so that all
+// but 256 mod NQ threads work. Inactive threads only take part in the
+// reductions.
 struct Quads {
     int NQ, NQp, G, q, g;
-    __device__ bool active() const { return q < NQ; }
+    __device__ bool active() const { return q < NQ && g < G; }
 };
 
 __device__ __forceinline__ Quads quads_for(int rows) {
@@ -827,9 +830,15 @@ __device__ __forceinline__ Quads quads_for(int rows) {
     Q.NQ = (rows + 3) >> 2;
     Q.NQp = 1;
     while (Q.NQp < Q.NQ) Q.NQp <<= 1;
-    Q.G = kSolveThreads / Q.NQp;
-    Q.q = threadIdx.x & (Q.NQp - 1);
-    Q.g = threadIdx.x / Q.NQp;
+    if (Q.NQ < 32) {
+        Q.G = kSolveThreads / Q.NQp;
+        Q.q = threadIdx.x & (Q.NQp - 1);
+        Q.g = threadIdx.x / Q.NQp;
+    } else {
+        Q.G = kSolveThreads / Q.NQ;
+        Q.q = threadIdx.x % Q.NQ;
+        Q.g = threadIdx.x / Q.NQ;
+    }
     return Q;
 }
 
