@@ -260,12 +260,34 @@ k_fea(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const int3
         const int k0 = s_k0, k1 = s_k1;
         const TF *Uc = Upd + c.upd_off;
         // every (column k, row i >= k) pair of the slice in one sweep: distinct
-        // targets within one child, so no two threads meet
+        // targets within one child, so no two threads meet. A thread takes
+        // kEa pairs at a time and issues all their loads (child entries, row
+        // maps, front entries) before its stores, so the round trips of a
+        // batch overlap instead of queueing behind each other's stores.
+        constexpr int kEa = 8;
         const int64_t cnt = (int64_t)(k1 - k0) * nbc;
-        for (int64_t q = tid; q < cnt; q += kFactorThreads) {
-            const int k = k0 + (int)(q / nbc), i = (int)(q % nbc);
-            if (i < k) continue;
-            front(P, U, n, nc, nb, ri[i], ri[k]) += Uc[(int64_t)k * nbc + i];
+        for (int64_t q0 = tid; q0 < cnt; q0 += (int64_t)kEa * kFactorThreads) {
+            TF val[kEa];
+            TF *dst[kEa];
+#pragma unroll
+            for (int u = 0; u < kEa; ++u) {
+                const int64_t q = q0 + (int64_t)u * kFactorThreads;
+                dst[u] = nullptr;
+                if (q < cnt) {
+                    const int k = k0 + (int)(q / nbc), i = (int)(q % nbc);
+                    if (i >= k) {
+                        val[u] = Uc[(int64_t)k * nbc + i];
+                        dst[u] = &front(P, U, n, nc, nb, ri[i], ri[k]);
+                    }
+                }
+            }
+            TF cur[kEa];
+#pragma unroll
+            for (int u = 0; u < kEa; ++u)
+                if (dst[u]) cur[u] = *dst[u];
+#pragma unroll
+            for (int u = 0; u < kEa; ++u)
+                if (dst[u]) *dst[u] = cur[u] + val[u];
         }
         __syncthreads();
     }
@@ -286,16 +308,36 @@ k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, T
     TF *P = Lval + d.panel_off;
     const int tid = threadIdx.x, tx = tid % 8, ty = tid / 8;  // 4 columns x 2 rows per thread
     TF acc[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-    for (int k0 = 0; k0 < j0; k0 += NB) {
-        for (int q = tid; q < NB * kTile; q += kFactorThreads) {
-            const int t = q / kTile, r = q % kTile;
-            As[t][r] = (r0 + r < n) ? P[(int64_t)(k0 + t) * n + r0 + r] : (TF)0;
+    // the next k-slice is loaded into registers while the current one is
+    // multiplied, so its global round trip overlaps the products
+    constexpr int kPa = NB * kTile / kFactorThreads, kPb = NB * NB / kFactorThreads;
+    TF pa[kPa], pb[kPb];
+    auto load_slice = [&](int k0) {
+#pragma unroll
+        for (int u = 0; u < kPa; ++u) {
+            const int q = tid + u * kFactorThreads, t = q / kTile, r = q % kTile;
+            pa[u] = (r0 + r < n) ? P[(int64_t)(k0 + t) * n + r0 + r] : (TF)0;
         }
-        for (int q = tid; q < NB * NB; q += kFactorThreads) {
-            const int t = q / NB, c = q % NB;
-            Bs[t][c] = (c < w) ? P[(int64_t)(k0 + t) * n + j0 + c] : (TF)0;
+#pragma unroll
+        for (int u = 0; u < kPb; ++u) {
+            const int q = tid + u * kFactorThreads, t = q / NB, c = q % NB;
+            pb[u] = (c < w) ? P[(int64_t)(k0 + t) * n + j0 + c] : (TF)0;
+        }
+    };
+    if (j0 > 0) load_slice(0);
+    for (int k0 = 0; k0 < j0; k0 += NB) {
+#pragma unroll
+        for (int u = 0; u < kPa; ++u) {
+            const int q = tid + u * kFactorThreads;
+            As[q / kTile][q % kTile] = pa[u];
+        }
+#pragma unroll
+        for (int u = 0; u < kPb; ++u) {
+            const int q = tid + u * kFactorThreads;
+            Bs[q / NB][q % NB] = pb[u];
         }
         __syncthreads();
+        if (k0 + NB < j0) load_slice(k0 + NB);
 #pragma unroll 8
         for (int t = 0; t < NB; ++t) {
             const TF a0 = As[t][ty], a1 = As[t][ty + 32];
@@ -320,17 +362,19 @@ k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, T
     }
 }
 
-// Diagonal block jb of a front: Cholesky and inverse by one warp in registers,
-// then the rows below are solved against it (L_ib = A_ib inv(L_bb)^T), one row
-// per thread of warps 1-7, which load their first rows while warp 0 factors.
-// Every step is written without divergent branches (selects instead), so the
-// shuffles of a step issue back to back and their latencies overlap; the row
-// solve runs column by column over 32 independent sums.
+// Diagonal block jb of a front: Cholesky by one warp in registers; then warp 0
+// forms the block's inverse (for X = inv(L11) and the solves) while warps 1-7
+// solve the rows below against the block by forward substitution
+// (L_ib L_bb^T = A_ib), one row per thread, their first rows loaded while
+// warp 0 factors. Every step is written without divergent branches (selects
+// instead), so the shuffles of a step issue back to back and their latencies
+// overlap.
 template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
 k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF *__restrict__ Lval,
       TF *__restrict__ Dinv, int *err) {
-    __shared__ __align__(16) TF Xc[NB][NB];  // inverse of the factored block, column-major: Xc[c][r] = X(r, c)
+    __shared__ TF Lb[NB][NB + 1];  // the factored block, row-major: Lb[r][c] = L(r, c)
+    __shared__ TF rinv[NB];        // 1 / L(r, r)
     const SnInfo d = sn[items[blockIdx.x].sn];
     const int n = d.nrow, nc = d.ncol;
     const int j0 = jb * NB, w = min(NB, nc - j0);
@@ -339,13 +383,13 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
     constexpr int kRowThreads = kFactorThreads - 32;
     const int i_first = j0 + w + (tid - 32);  // warps 1-7: first trailing row
     TF a[NB];
+    TF myinv = (TF)0;  // warp 0: 1 / L(lane, lane)
     if (tid < 32) {
         // row `lane` of the block, right-looking Cholesky (the operations of a
         // column-by-column update, in the same order)
 #pragma unroll
         for (int c = 0; c < NB; ++c) a[c] = (lane < w && c <= lane) ? P[(int64_t)(j0 + c) * n + j0 + lane] : (TF)0;
         bool bad = false;
-        TF myinv = (TF)0;  // 1 / L(lane, lane)
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
             if (k < w) {
@@ -355,15 +399,25 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
                 const TF dk = tsqrt(akk), inv = (TF)1 / dk;
                 a[k] = (lane == k) ? dk : a[k] * inv;  // zero above the diagonal stays zero
                 myinv = (lane == k) ? inv : myinv;
-                TF l[NB];
-#pragma unroll
-                for (int c = k + 1; c < NB; ++c) l[c] = __shfl_sync(0xffffffffu, a[k], c);  // L(c, k)
                 const TF lk = a[k];
 #pragma unroll
-                for (int c = k + 1; c < NB; ++c) a[c] -= ((lane >= c) ? lk : (TF)0) * l[c];
+                for (int c = k + 1; c < NB; ++c)  // L(c, k) from lane c
+                    a[c] -= ((lane >= c) ? lk : (TF)0) * __shfl_sync(0xffffffffu, lk, c);
             }
         }
         if (bad && lane == 0) atomicOr(err, kErrNotSpd);
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            Lb[lane][c] = a[c];  // zero above the diagonal and outside the block
+            if (lane < w && c <= lane) P[(int64_t)(j0 + c) * n + j0 + lane] = a[c];
+        }
+        rinv[lane] = myinv;
+    } else if (i_first < n) {
+#pragma unroll
+        for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i_first] : (TF)0;
+    }
+    __syncthreads();
+    if (tid < 32) {
         // X = inv(L), lane = row, right-looking: at step t row t of X lacks
         // only the division by L(t, t); it is broadcast and every later row i
         // subtracts L(i, t) X(t, :)
@@ -373,46 +427,36 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
 #pragma unroll
         for (int t = 0; t < NB; ++t) {
             if (t < w) {
-                TF xt[NB];
-#pragma unroll
-                for (int j = 0; j <= t; ++j) {
-                    y[j] = (lane == t) ? y[j] * myinv : y[j];
-                    xt[j] = __shfl_sync(0xffffffffu, y[j], t);
-                }
                 const TF m = (lane > t) ? a[t] : (TF)0;
 #pragma unroll
-                for (int j = 0; j <= t; ++j) y[j] -= m * xt[j];
+                for (int j = 0; j <= t; ++j) {
+                    const TF yj = (lane == t) ? y[j] * myinv : y[j];
+                    y[j] = yj - m * __shfl_sync(0xffffffffu, yj, t);  // X(t, j) from lane t
+                }
             }
         }
+        // column-major: Dinv[c * NB + r] = X(r, c); zero above the diagonal
+        TF *D = Dinv + d.dinv_off + (int64_t)jb * NB * NB;
 #pragma unroll
-        for (int c = 0; c < NB; ++c) {
-            Xc[c][lane] = y[c];  // zero above the diagonal and outside the block
-            if (lane < w && c <= lane) P[(int64_t)(j0 + c) * n + j0 + lane] = a[c];
-        }
-    } else if (i_first < n) {
-#pragma unroll
-        for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i_first] : (TF)0;
+        for (int c = 0; c < NB; ++c) D[c * NB + lane] = y[c];
+        return;
     }
-    __syncthreads();
-    for (int q = tid; q < NB * NB; q += kFactorThreads)
-        Dinv[d.dinv_off + (int64_t)jb * NB * NB + q] = (&Xc[0][0])[q];  // column-major, as stored
-    if (tid < 32) return;
     for (int i = i_first; i < n; i += kRowThreads) {
         if (i != i_first) {
 #pragma unroll
             for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i] : (TF)0;
         }
-        TF acc[NB];
+        // L(i, r) = (A(i, r) - sum_{c < r} L(i, c) L(r, c)) / L(r, r)
 #pragma unroll
-        for (int r = 0; r < NB; ++r) acc[r] = (TF)0;
-        // L(i, r) = sum_{c <= r} a[c] X(r, c), summed in increasing c as before
+        for (int r = 0; r < NB; ++r) {
+            TF acc = a[r];
 #pragma unroll
-        for (int c = 0; c < NB; ++c)
-#pragma unroll
-            for (int r = c; r < NB; ++r) acc[r] += a[c] * Xc[c][r];
+            for (int c = 0; c < r; ++c) acc -= a[c] * Lb[r][c];
+            a[r] = acc * rinv[r];  // zero for r >= w (rinv and the row are zero there)
+        }
 #pragma unroll
         for (int r = 0; r < NB; ++r)
-            if (r < w) P[(int64_t)(j0 + r) * n + i] = acc[r];
+            if (r < w) P[(int64_t)(j0 + r) * n + i] = a[r];
     }
 }
 
@@ -436,20 +480,33 @@ k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) acc[a][b] = (TF)0;
-    for (int k0 = 0; k0 < nc; k0 += NB) {
+    // the next k-slice is loaded into registers while the current one is
+    // multiplied, so its global round trip overlaps the products
+    constexpr int kPer = NB * kTile / kFactorThreads;
+    TF pa[kPer], pb[kPer];
+    auto load_slice = [&](int k0) {
         const int kw = min(NB, nc - k0);
-        for (int q = tid; q < NB * kTile; q += kFactorThreads) {
-            const int t = q / kTile, r = q % kTile;
-            TF av = (TF)0, bv = (TF)0;
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const int q = tid + u * kFactorThreads, t = q / kTile, r = q % kTile;
+            pa[u] = pb[u] = (TF)0;
             if (t < kw) {
                 const TF *col = P + (int64_t)(k0 + t) * n + nc;
-                if (rb + r < nb) av = col[rb + r];
-                if (cb + r < nb) bv = col[cb + r];
+                if (rb + r < nb) pa[u] = col[rb + r];
+                if (cb + r < nb) pb[u] = col[cb + r];
             }
-            As[t][r] = av;
-            Bs[t][r] = bv;
+        }
+    };
+    if (nc > 0) load_slice(0);
+    for (int k0 = 0; k0 < nc; k0 += NB) {
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const int q = tid + u * kFactorThreads;
+            As[q / kTile][q % kTile] = pa[u];
+            Bs[q / kTile][q % kTile] = pb[u];
         }
         __syncthreads();
+        if (k0 + NB < nc) load_slice(k0 + NB);
 #pragma unroll 8
         for (int t = 0; t < NB; ++t) {
             TF av[4], bv[4];
@@ -487,6 +544,8 @@ k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *_
     TF *Xc = reinterpret_cast<TF *>(fx_raw);  // [row][NB + 1]
     __shared__ TF Ts[NB][NB + 1];
     __shared__ TF Ds[NB][NB + 1];  // inverse of the current diagonal block, [t][r]
+    constexpr int KC = 64;         // columns of L staged per pass
+    __shared__ TF Ls[NB][KC + 1];  // rows of the current block row, columns [k0, k0 + KC)
     const FItem it = items[blockIdx.x];
     const SnInfo d = sn[it.sn];
     const int n = d.nrow, nc = d.ncol, nb = n - nc;
@@ -510,25 +569,46 @@ k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *_
             const TF *Dii = Dinv + d.dinv_off + (int64_t)ib * NB * NB;
             for (int q = tid; q < NB * NB; q += kFactorThreads) Ds[q / NB][q % NB] = Dii[q];
         }
+        // sum_k L(i0 + r, k) X(k, j0 + c) over k in [j0, i0), in increasing k:
+        // the block row is staged KC columns at a time by all threads (every
+        // load of a pass in flight at once) instead of each thread walking
+        // its row through global memory
         TF acc[4] = {(TF)0, (TF)0, (TF)0, (TF)0};
-        if (r < wi) {
-#pragma unroll 8
-            for (int k = j0; k < i0; ++k) {
-                const TF l = P[(int64_t)k * n + i0 + r];
-#pragma unroll
-                for (int cc = 0; cc < 4; ++cc) acc[cc] += l * Xc[k * (NB + 1) + cg * 4 + cc];
+        for (int k0 = j0; k0 < i0; k0 += KC) {
+            const int kw = min(KC, i0 - k0);
+            for (int q = tid; q < NB * KC; q += kFactorThreads) {
+                const int rr = q % NB, kk = q / NB;
+                Ls[rr][kk] = (rr < wi && kk < kw) ? P[(int64_t)(k0 + kk) * n + i0 + rr] : (TF)0;
             }
+            __syncthreads();
+            if (r < wi) {
+#pragma unroll 8
+                for (int kk = 0; kk < kw; ++kk) {
+                    const TF l = Ls[r][kk];
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) acc[cc] += l * Xc[(k0 + kk) * (NB + 1) + cg * 4 + cc];
+                }
+            }
+            __syncthreads();
         }
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) Ts[cg * 4 + cc][r] = acc[cc];
         __syncthreads();
+        // X(i0 + r, c) = -sum_{t <= r} inv(L_ii)(r, t) T(t, c), in increasing t
+        // (a fixed-length loop with the bound as a predicate: the loads of
+        // all terms issue ahead of the sums)
+        TF v[4] = {(TF)0, (TF)0, (TF)0, (TF)0};
+#pragma unroll
+        for (int t = 0; t < NB; ++t) {
+            const TF dt = Ds[t][r];
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc)
+                if (t <= r) v[cc] += dt * Ts[cg * 4 + cc][t];
+        }
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
             const int c = cg * 4 + cc;
-            TF v = (TF)0;
-            if (r < wi)
-                for (int t = 0; t <= r; ++t) v += Ds[t][r] * Ts[c][t];
-            Xc[(i0 + r) * (NB + 1) + c] = (r < wi && c < wj) ? -v : (TF)0;
+            Xc[(i0 + r) * (NB + 1) + c] = (r < wi && c < wj) ? -v[cc] : (TF)0;
         }
         __syncthreads();
     }
