@@ -308,6 +308,13 @@ def run_batch(args):
     # factor once per pose tile and the per-pose vectors once per pose
     dom_bytes = kmodel[dom][0]
     achieved = dom_bytes / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "ncu_traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get(w.name, {}).get(dom)
+        except Exception:
+            traffic = None
     cpu = None
     err = None
     if rank == 0 and not args.no_cpu_baseline and e2e_s:
@@ -340,7 +347,7 @@ def run_batch(args):
                                  "h2d_bytes_per_step": int(tg_h.nbytes), "d2h_bytes_per_step": int(out_h.nbytes)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "bytes_per_launch": dom_bytes,
+                     "frac": achieved / hbm_peak, "traffic": traffic, "bytes_per_launch": dom_bytes,
                      "ms_per_launch": per_launch_ms},
         "cpu_baseline": cpu,
         "error_vs_fp64_oracle": err,
