@@ -447,7 +447,7 @@ def run_serving(args):
                "stats": {k: st[k] for k in ("factor_hits", "factor_misses", "evictions", "launches",
                                              "batched_launches", "batched_requests", "peak_resident_bytes",
                                              "budget_bytes", "scheduler_busy_ms", "worker_busy_ms", "analyze_ms",
-                                             "staging_ms", "device_ms")},
+                                             "staging_ms", "device_ms", "launch_ms", "launch_host_ms")},
                "device_spans_in_flight_avg": st["device_ms"] / (1e3 * wall),
                "scheduler_busy_frac": st["scheduler_busy_ms"] / (1e3 * wall),
                "clocks": clk}

@@ -399,6 +399,10 @@ typedef struct arap_server_stats {
     double analyze_ms;         /* of which: contexts created, constraint sets analysed */
     double staging_ms;         /* scheduler time allocating pinned result buffers */
     double device_ms;          /* sum over launches of their device time (set-up + iterations) */
+    double launch_ms;          /* host time in the launch calls (arap_deform[_poses]_async and the
+                                  re-pose before it) */
+    double launch_host_ms[5];  /* of which, summed arap_get_host_timing phases: analysis and uploads,
+                                  allocation, set-up enqueue, iteration enqueue, rest */
 } arap_server_stats;
 
 int arap_srv_create(const arap_server_config *cfg, arap_server **out);

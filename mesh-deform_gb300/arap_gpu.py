@@ -70,7 +70,8 @@ class ServerStats(C.Structure):
                                          "peak_resident_bytes", "budget_bytes")] + \
         [(n, C.c_int32) for n in ("resident_factors", "queue_depth", "in_flight", "pad")] + \
         [(n, C.c_double) for n in ("scheduler_busy_ms", "worker_busy_ms", "analyze_ms", "staging_ms",
-                                             "device_ms")]
+                                             "device_ms", "launch_ms")] + \
+        [("launch_host_ms", C.c_double * 5)]
 
 
 SIGNATURES = {
@@ -475,7 +476,9 @@ class ArapServer:
     def stats(self) -> dict:
         st = ServerStats()
         self._check(self.lib.arap_srv_stats(self.h, C.byref(st)))
-        return {n: getattr(st, n) for n, _ in ServerStats._fields_ if n != "pad"}
+        out = {n: getattr(st, n) for n, _ in ServerStats._fields_ if n != "pad"}
+        out["launch_host_ms"] = list(st.launch_host_ms)
+        return out
 
     def close(self):
         if getattr(self, "h", None):

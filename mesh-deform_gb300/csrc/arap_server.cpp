@@ -35,6 +35,10 @@ struct CtxBackend {
     }
     int query(Handle h, int32_t *done) { return arap_query(h, done); }
     int set_done_callback(Handle h, void (*fn)(void *), void *user) { return arap_set_done_callback(h, fn, user); }
+    void host_timing(Handle h, double *ms5) {
+        if (arap_get_host_timing(h, ms5) != ARAP_OK)
+            for (int i = 0; i < 5; ++i) ms5[i] = 0.0;
+    }
     double device_ms(Handle h) {
         double a = 0.0, b = 0.0;
         return arap_get_timing(h, &a, &b) == ARAP_OK ? a + b : 0.0;

@@ -426,6 +426,7 @@ class Server {
     int launch(Slot *s, std::string &err) {
         const int P = (int)s->running.size();
         const int iters = s->running[0]->iterations;
+        const auto t0 = Clock::now();
         int rc;
         if (P == 1) {
             const Req *q = s->running[0];
@@ -435,6 +436,12 @@ class Server {
             rc = b_.deform_poses_async(s->ctx, P, s->batch_targets.data(), iters, s->staging);
         }
         if (rc != ARAP_OK) err = b_.last_error(s->ctx);
+        double ph[5] = {0, 0, 0, 0, 0};
+        if (rc == ARAP_OK) b_.host_timing(s->ctx, ph);
+        const double ms = ms_between(t0, Clock::now());
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.launch_ms += ms;
+        for (int i = 0; i < 5; ++i) st_.launch_host_ms[i] += ph[i];
         return rc;
     }
 
