@@ -540,7 +540,8 @@ def main():
                     help="serving: Poisson arrival rates in requests/s (0: all requests at once)")
     ap.add_argument("--serve-requests", type=int, default=400)
     ap.add_argument("--serve-in-flight", type=int, default=8)
-    ap.add_argument("--serve-prep-threads", type=int, default=min(12, os.cpu_count() or 4))
+    ap.add_argument("--serve-prep-threads", type=int, default=4,
+                    help="serving: preparation threads (measured best at saturation: 4 of 2/4/6/8)")
     ap.add_argument("--serve-max-batch", type=int, default=64)
     ap.add_argument("--serve-check", type=int, default=40, help="serving: results checked against the oracle")
     ap.add_argument("--serve-fp64-requests", type=int, default=100)
