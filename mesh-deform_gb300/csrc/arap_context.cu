@@ -16,7 +16,6 @@
 
 namespace arapgpu {
 cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64);
-cudaError_t configure_factor_smem(int max_ncol);
 }
 
 using namespace arapgpu;
@@ -124,6 +123,7 @@ struct arap_ctx {
     bool sym_host = false;   // analysed (host only)
     Symbolic sym;
     size_t smem_f32 = 0, smem_f64 = 0;  // dynamic shared memory the solve kernels are configured for
+    bool fp64_solves = true;             // the FP64 solves fit this symbolic analysis's fronts
     size_t top_smem_f32 = 0, top_smem_f64 = 0;
     // which precision the iteration state was set up for
     int state_prec = -1;
@@ -132,7 +132,6 @@ struct arap_ctx {
     DevBuf faces, ent_ptr, ent_fc, hc, w_orig;
     DevBuf rest, targets, out;
     DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn, fitems;
-    int factor_smem_ncol = 0;
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T, redge;
     DevBuf errw, ticket, flags, energy;
     DevBuf cidx_dev, handle_dev, tabs_dev;  // arap_pose_targets inputs
@@ -352,31 +351,28 @@ int prepare_symbolic(arap_ctx *ctx) {
     CK(upload(ctx->child, s.child, st));
     CK(upload(ctx->level_sn, s.level_sn, st));
     CK(upload(ctx->fitems, s.fitems, st));
-    if (s.max_ncol > ctx->factor_smem_ncol) {
-        CK(configure_factor_smem(s.max_ncol));
-        ctx->factor_smem_ncol = s.max_ncol;
-    }
     // solve scheduling state: ticket counters and per-supernode flags start at 0
     // counters: forward / backward of the lower levels, then of the top levels
     CK(ctx->ticket.ensure(4 * sizeof(unsigned long long)));
     CK(ctx->flags.ensure(2 * sizeof(unsigned) * (size_t)std::max(s.S, 1)));
     CK(cudaMemsetAsync(ctx->ticket.p, 0, 4 * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
-    // the solve kernels give each thread one 4-row quad of a front (at most
-    // 1024 rows) and stream whole columns through 16 KB chunks
-    if (s.max_ldx > 1024 || s.max_ld21 > 1024)
-        return fail(ctx, ARAP_ERR_UNSUPPORTED,
-                    "supernode front of " + std::to_string(std::max(s.max_ldx, s.max_ld21)) +
-                        " rows exceeds the solve kernels' limit of 1024");
+    // the solve kernels stream whole columns through chunk buffers (a column
+    // must fit one) and keep a front's vectors in shared memory; fronts of
+    // more than kSolveBlockRows rows take several passes. The FP64 form needs
+    // twice the bytes: when only the mixed form fits, FP64 deforms are refused.
+    const int max_rows = std::max(s.max_ldx, s.max_ld21);
     const size_t b32 = solve_smem_bytes(s.max_ldx, s.max_ld21, 4), b64 = solve_smem_bytes(s.max_ldx, s.max_ld21, 8);
-    if (b64 > 227 * 1024)
+    constexpr size_t kSmemMax = 227 * 1024;
+    if ((size_t)max_rows * 4 > (size_t)solve_chunk_bytes() || b32 > kSmemMax)
         return fail(ctx, ARAP_ERR_UNSUPPORTED,
-                    "supernode of " + std::to_string(s.max_ncol) + " columns and " +
-                        std::to_string(s.max_ld21) + " struct rows exceeds the solve kernel's shared memory");
-    if (b32 > ctx->smem_f32 || b64 > ctx->smem_f64) {
-        CK(configure_solve_smem((int)b32, (int)b64));
+                    "supernode front of " + std::to_string(max_rows) + " rows (" + std::to_string(s.max_ncol) +
+                        " columns) exceeds the solve kernels' shared memory");
+    ctx->fp64_solves = (size_t)max_rows * 8 <= (size_t)solve_chunk_bytes() && b64 <= kSmemMax;
+    if (b32 > ctx->smem_f32 || (ctx->fp64_solves && b64 > ctx->smem_f64)) {
+        CK(configure_solve_smem((int)b32, ctx->fp64_solves ? (int)b64 : 0));
         ctx->smem_f32 = b32;
-        ctx->smem_f64 = b64;
+        if (ctx->fp64_solves) ctx->smem_f64 = b64;
     }
     DevSym &d = ctx->ds;
     {
@@ -390,6 +386,9 @@ int prepare_symbolic(arap_ctx *ctx) {
         }
         int ltop = nlev;
         while (ltop > 0 && big[ltop - 1]) --ltop;
+        // the cluster solves take fronts of at most kSolveBlockRows rows
+        for (const SnInfo &q : s.sn)
+            if (q.level >= ltop && std::max(q.ldx, q.ld21) > kSolveBlockRows) ltop = std::max(ltop, q.level + 1);
         d.ltop = ltop;
         d.s_low = nlev > 0 ? s.level_ptr[ltop] : 0;
         d.s_top = s.S - d.s_low;
@@ -401,14 +400,23 @@ int prepare_symbolic(arap_ctx *ctx) {
         const int nl = std::max(d.s_low, 1);
         d.solve_grid32 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res32) : res32));
         d.solve_grid64 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res64) : res64));
+        // the cluster solves size their shared memory by the largest front of
+        // the cluster levels
+        d.top_ldx = d.top_ld21 = 0;
+        for (const SnInfo &q : s.sn)
+            if (q.level >= ltop) {
+                d.top_ldx = std::max(d.top_ldx, (int)q.ldx);
+                d.top_ld21 = std::max(d.top_ld21, (int)q.ld21);
+            }
         if (d.s_top > 0) {
-            const size_t t32 = top_smem_bytes(s.max_ldx, s.max_ld21, 4), t64 = top_smem_bytes(s.max_ldx, s.max_ld21, 8);
-            if (t64 > 227 * 1024)
+            const size_t t32 = top_smem_bytes(d.top_ldx, d.top_ld21, 4), t64 = top_smem_bytes(d.top_ldx, d.top_ld21, 8);
+            if (t32 > kSmemMax)
                 return fail(ctx, ARAP_ERR_UNSUPPORTED, "top supernode fronts exceed the cluster solve's shared memory");
-            if (t32 > ctx->top_smem_f32 || t64 > ctx->top_smem_f64) {
-                CK(configure_top_smem((int)t32, (int)t64));
+            if (t64 > kSmemMax) ctx->fp64_solves = false;
+            if (t32 > ctx->top_smem_f32 || (t64 <= kSmemMax && t64 > ctx->top_smem_f64)) {
+                CK(configure_top_smem((int)t32, t64 <= kSmemMax ? (int)t64 : 0));
                 ctx->top_smem_f32 = t32;
-                ctx->top_smem_f64 = t64;
+                if (t64 <= kSmemMax) ctx->top_smem_f64 = t64;
             }
         }
     }
@@ -462,6 +470,11 @@ int setup_enqueue(arap_ctx *ctx) {
     const DevSym &d = ctx->ds;
     cudaStream_t st = ctx->stream;
     const int m = s.m;
+    // the solves' scheduling counters and flags restart with every set-up: a
+    // launch consumes tickets in proportion to its grid, which differs
+    // between the precisions
+    CK(cudaMemsetAsync(ctx->ticket.p, 0, 4 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
     // cotan weights (arap.h:182-239)
     {
         Prof pr(ctx, ARAP_K_WEIGHTS);
@@ -1211,6 +1224,9 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         }
         int rc = prepare_symbolic(ctx);
         if (rc != ARAP_OK) return rc;
+        if (fp64 && !ctx->fp64_solves)
+            return fail(ctx, ARAP_ERR_UNSUPPORTED,
+                        "supernode fronts too large for the FP64 solves' shared memory (the mixed form handles them)");
         h1 = HClock::now();
         rc = fp64 ? setup_alloc<double>(ctx) : setup_alloc<float>(ctx);
         if (rc != ARAP_OK) return rc;

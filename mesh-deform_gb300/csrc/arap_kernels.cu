@@ -533,35 +533,49 @@ k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF
 }
 
 // Column block jb of X = inv(L11): X_jj = inv(L_jj) and, block row by block
-// row, X_ij = -inv(L_ii) sum_{k=j..i-1} L_ik X_kj, with the column block kept in
-// shared memory (dynamic, max_ncol x 33). Writes X, its transpose, and the
-// aligned L21 / L21^T copies of the block's columns.
+// row, X_ij = -inv(L_ii) sum_{k=j..i-1} L_ik X_kj. Each block row is written
+// to X (and X^T) as soon as it is known; later block rows read the rows above
+// back from X (the CTA's own writes, visible after a barrier), staged with the
+// matching columns of L through shared memory KC rows at a time, so the front
+// may have any number of columns. Also writes the aligned L21 / L21^T copies
+// of the block's columns.
 template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
 k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *__restrict__ Lval,
      const TF *__restrict__ Dinv, TF *__restrict__ Xall, TF *__restrict__ L21all, TF *__restrict__ L21Tall) {
-    extern __shared__ __align__(16) unsigned char fx_raw[];
-    TF *Xc = reinterpret_cast<TF *>(fx_raw);  // [row][NB + 1]
+    constexpr int KC = sizeof(TF) == 4 ? 64 : 32;  // rows of the sum staged per pass
     __shared__ TF Ts[NB][NB + 1];
     __shared__ TF Ds[NB][NB + 1];  // inverse of the current diagonal block, [t][r]
-    constexpr int KC = 64;         // columns of L staged per pass
-    __shared__ TF Ls[NB][KC + 1];  // rows of the current block row, columns [k0, k0 + KC)
+    __shared__ TF Ls[NB][KC + 1];  // L(i0 + r, k0 + kk)
+    __shared__ TF Xs[KC][NB + 1];  // X(k0 + kk, j0 + c)
     const FItem it = items[blockIdx.x];
     const SnInfo d = sn[it.sn];
     const int n = d.nrow, nc = d.ncol, nb = n - nc;
     const int jb = it.a, j0 = jb * NB, wj = min(NB, nc - j0);
     const TF *P = Lval + d.panel_off;
+    TF *X = Xall + d.x_off, *XT = Xall + d.xt_off;
+    const int ldx = d.ldx;
     const int tid = threadIdx.x;
     const int nblk = (nc + NB - 1) / NB;
-    {
-        const TF *Djj = Dinv + d.dinv_off + (int64_t)jb * NB * NB;
-        for (int q = tid; q < NB * NB; q += kFactorThreads) {
-            const int r = q % NB, c = q / NB;
-            Xc[(j0 + r) * (NB + 1) + c] = (r < wj && c < wj) ? Djj[(int64_t)c * NB + r] : (TF)0;
-        }
-    }
-    __syncthreads();
     const int r = tid % NB, cg = tid / NB;  // row in block, group of 4 columns
+    // X(i0 + r, j0 + c) for c < wj into X and X^T (X^T keeps the lower part)
+    auto store_rows = [&](int i0, int wi, const TF v[4]) {
+        if (r >= wi) return;
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            const int c = cg * 4 + cc, i = i0 + r;
+            if (c >= wj) continue;
+            X[(int64_t)(j0 + c) * ldx + i] = v[cc];
+            if (i >= j0 + c) XT[(int64_t)i * ldx + j0 + c] = v[cc];
+        }
+    };
+    {
+        const TF *Djj = Dinv + d.dinv_off + (int64_t)jb * NB * NB;  // column-major
+        TF v[4];
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) v[cc] = Djj[(int64_t)(cg * 4 + cc) * NB + r];
+        store_rows(j0, wj, v);
+    }
     for (int ib = jb + 1; ib < nblk; ++ib) {
         const int i0 = ib * NB, wi = min(NB, nc - i0);
         {
@@ -569,16 +583,18 @@ k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *_
             const TF *Dii = Dinv + d.dinv_off + (int64_t)ib * NB * NB;
             for (int q = tid; q < NB * NB; q += kFactorThreads) Ds[q / NB][q % NB] = Dii[q];
         }
-        // sum_k L(i0 + r, k) X(k, j0 + c) over k in [j0, i0), in increasing k:
-        // the block row is staged KC columns at a time by all threads (every
-        // load of a pass in flight at once) instead of each thread walking
-        // its row through global memory
+        // sum_k L(i0 + r, k) X(k, j0 + c) over k in [j0, i0), in increasing k
         TF acc[4] = {(TF)0, (TF)0, (TF)0, (TF)0};
         for (int k0 = j0; k0 < i0; k0 += KC) {
             const int kw = min(KC, i0 - k0);
+            __syncthreads();  // the rows of X read below were written before it
             for (int q = tid; q < NB * KC; q += kFactorThreads) {
                 const int rr = q % NB, kk = q / NB;
                 Ls[rr][kk] = (rr < wi && kk < kw) ? P[(int64_t)(k0 + kk) * n + i0 + rr] : (TF)0;
+            }
+            for (int q = tid; q < KC * NB; q += kFactorThreads) {
+                const int kk = q % KC, c = q / KC;
+                Xs[kk][c] = (kk < kw && c < wj) ? X[(int64_t)(j0 + c) * ldx + k0 + kk] : (TF)0;
             }
             __syncthreads();
             if (r < wi) {
@@ -586,10 +602,9 @@ k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *_
                 for (int kk = 0; kk < kw; ++kk) {
                     const TF l = Ls[r][kk];
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) acc[cc] += l * Xc[(k0 + kk) * (NB + 1) + cg * 4 + cc];
+                    for (int cc = 0; cc < 4; ++cc) acc[cc] += l * Xs[kk][cg * 4 + cc];
                 }
             }
-            __syncthreads();
         }
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) Ts[cg * 4 + cc][r] = acc[cc];
@@ -606,21 +621,11 @@ k_fx(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *_
                 if (t <= r) v[cc] += dt * Ts[cg * 4 + cc][t];
         }
 #pragma unroll
-        for (int cc = 0; cc < 4; ++cc) {
-            const int c = cg * 4 + cc;
-            Xc[(i0 + r) * (NB + 1) + c] = (r < wi && c < wj) ? -v[cc] : (TF)0;
-        }
-        __syncthreads();
+        for (int cc = 0; cc < 4; ++cc) v[cc] = -v[cc];
+        store_rows(i0, wi, v);
+        __syncthreads();  // Ts and Ds are rewritten by the next block row
     }
-    TF *X = Xall + d.x_off, *XT = Xall + d.xt_off;
-    const int ldx = d.ldx;
-    for (int q = tid; q < (nc - j0) * NB; q += kFactorThreads) {
-        const int i = j0 + q / NB, c = q % NB;
-        if (c >= wj) continue;
-        const TF v = Xc[i * (NB + 1) + c];
-        X[(int64_t)(j0 + c) * ldx + i] = v;                 // X(i, j0+c)
-        if (i >= j0 + c) XT[(int64_t)i * ldx + j0 + c] = v;  // X^T stored column i
-    }
+    // rows of X above the block column stay as set up: zero (X is lower triangular)
     TF *L21 = L21all + d.l21_off, *L21T = L21Tall + d.l21t_off;
     const int ld21 = d.ld21;
     for (int q = tid; q < wj * nb; q += kFactorThreads) {
@@ -868,6 +873,37 @@ __device__ __forceinline__ T *sbuf(unsigned char *raw, int b) {
     return reinterpret_cast<T *>(raw + b * kChunkBytes);
 }
 
+// A task's chunk stream when a GEMV phase has more rows than one pass covers
+// (kSolveBlockRows, one 4-row quad per thread): phase A's chunks once per row
+// block of its rows, then phase B's chunks once per row block of theirs (B's
+// chunks follow A's in the ChunkPlan). With fronts of at most kSolveBlockRows
+// rows this is the plain chunk sequence.
+struct VPlan {
+    int nA, nB, rbA, rbB;
+    __device__ int total() const { return nA * rbA + nB * rbB; }
+    // chunk index in the ChunkPlan, phase (0: A, 1: B) and row block of
+    // stream position e
+    __device__ void decode(int e, int &k, int &phase, int &rb) const {
+        if (e < nA * rbA) {
+            phase = 0;
+            rb = e / nA;
+            k = e - rb * nA;
+        } else {
+            const int f = e - nA * rbA;
+            phase = 1;
+            rb = f / nB;
+            k = nA + (f - rb * nB);
+        }
+    }
+    __device__ int real(int e) const {
+        int k, phase, rb;
+        decode(e, k, phase, rb);
+        return k;
+    }
+};
+
+__device__ __forceinline__ int row_blocks(int rows) { return (rows + kSolveBlockRows - 1) / kSolveBlockRows; }
+
 // Bounded wait for a buffer's bytes. On expiry it records kErrTimeout and
 // waits once more (bounded) so that no copy is still writing into shared
 // memory when the CTA moves on.
@@ -1027,8 +1063,10 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     ChunkPlan<T> pl;
     pl.init(Xall + d.x_off, d.ldx, nc, L21all + d.l21_off, d.ld21, nb > 0 ? nc : 0);
     const int ntot = pl.total();
+    const VPlan vp{pl.nA, pl.nB, row_blocks(nc), pl.nB > 0 ? row_blocks(nb) : 0};
+    const int vtot = vp.total();
     if (tid == 0) {
-        for (int k = 0; k < ntot && k < kSolveBufs; ++k) issue_chunk(pl, k, sbuf<T>(smem_raw, k), &bars[k]);
+        for (int e = 0; e < vtot && e < kSolveBufs; ++e) issue_chunk(pl, vp.real(e), sbuf<T>(smem_raw, e), &bars[e]);
         for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     for (int i = tid; i < d.ldx; i += kSolveThreads)
@@ -1097,30 +1135,30 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
             __syncthreads();
         }
     }
-    // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb)
-    const Quads Qa = quads_for(nc), Qb = quads_for(nb);
+    // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb), each in
+    // passes of at most kSolveBlockRows rows
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-    for (int k = 0; k < ntot; ++k) {
-        const int kb = k & (kSolveBufs - 1);
+    for (int e = 0; e < vtot; ++e) {
+        int k, phase, rb;
+        vp.decode(e, k, phase, rb);
+        const int row0 = rb * kSolveBlockRows;
+        const Quads Q = quads_for(min(kSolveBlockRows, (phase == 0 ? nc : nb) - row0));
+        const int kb = e & (kSolveBufs - 1);
         T *buf = sbuf<T>(smem_raw, kb);
-        wait_chunk(&bars[kb], (ph[kb] + (unsigned)(k / kSolveBufs)) & 1u, err);
+        wait_chunk(&bars[kb], (ph[kb] + (unsigned)(e / kSolveBufs)) & 1u, err);
         int c0, cn, ld;
         const T *src;
         pl.chunk(k, c0, cn, src, ld);
-        if (k < pl.nA) {
-            if (Qa.active()) chunk_axpy(buf, ld, cn, c0, Qa.q, Qa.g, Qa.G, fc, ax, ay, az);
-        } else {
-            if (Qb.active()) chunk_axpy(buf, ld, cn, c0, Qb.q, Qb.g, Qb.G, yv, ax, ay, az);
-        }
+        if (Q.active()) chunk_axpy(buf + row0, ld, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? fc : yv, ax, ay, az);
         __syncthreads();
-        if (tid == 0 && k + kSolveBufs < ntot) issue_chunk(pl, k + kSolveBufs, buf, &bars[kb]);
-        if (k == pl.nA - 1) {
-            reduce_quads<T, false>(Qa, ax, ay, az, red, yv);
+        if (tid == 0 && e + kSolveBufs < vtot) issue_chunk(pl, vp.real(e + kSolveBufs), buf, &bars[kb]);
+        if (k == (phase == 0 ? pl.nA - 1 : ntot - 1)) {
+            if (phase == 0) reduce_quads<T, false>(Q, ax, ay, az, red, yv + row0);
+            else reduce_quads<T, true>(Q, ax, ay, az, red, fb + row0);
 #pragma unroll
             for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
         }
     }
-    if (pl.nB > 0) reduce_quads<T, true>(Qb, ax, ay, az, red, fb);
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
     // the barrier orders every thread's writes before thread 0's release,
     // which is cumulative: a CTA that acquires the flag sees them all
@@ -1131,7 +1169,7 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     // path. yv is next written after a barrier of the next task.
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
 #pragma unroll
-    for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((ntot - b + kSolveBufs - 1) / kSolveBufs);
+    for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((vtot - b + kSolveBufs - 1) / kSolveBufs);
     }
 }
 
@@ -1174,8 +1212,10 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     else pl.init(Xall + d.xt_off, d.ldx, nc, nullptr, 0, 0);
     const int ntot = pl.total();
     const int nA = nb > 0 ? pl.nA : 0;  // chunks of L21^T
+    const VPlan vp{nA, ntot - nA, row_blocks(nc), row_blocks(nc)};
+    const int vtot = vp.total();
     if (tid == 0) {
-        for (int k = 0; k < ntot && k < kSolveBufs; ++k) issue_chunk(pl, k, sbuf<T>(smem_raw, k), &bars[k]);
+        for (int e = 0; e < vtot && e < kSolveBufs; ++e) issue_chunk(pl, vp.real(e), sbuf<T>(smem_raw, e), &bars[e]);
         for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     const int32_t *rs = rows + d.rows_off;
@@ -1193,27 +1233,30 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
         if (tid + u * kSolveThreads < nb) gb[tid + u * kSolveThreads] = ldcg4(sol + myrow[u]);
     for (int i = tid + 4 * kSolveThreads; i < nb; i += kSolveThreads) gb[i] = ldcg4(sol + rs[i]);
     __syncthreads();
-    // phase A (nb > 0): z -= L21^T g; phase B: x = X^T z; both have nc rows
-    const Quads Q = quads_for(nc);
+    // phase A (nb > 0): z -= L21^T g; phase B: x = X^T z; both have nc rows,
+    // in passes of at most kSolveBlockRows rows
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-    for (int k = 0; k < ntot; ++k) {
-        const int kb = k & (kSolveBufs - 1);
+    for (int e = 0; e < vtot; ++e) {
+        int k, phase, rb;
+        vp.decode(e, k, phase, rb);
+        const int row0 = rb * kSolveBlockRows;
+        const Quads Q = quads_for(min(kSolveBlockRows, nc - row0));
+        const int kb = e & (kSolveBufs - 1);
         T *buf = sbuf<T>(smem_raw, kb);
-        wait_chunk(&bars[kb], (ph[kb] + (unsigned)(k / kSolveBufs)) & 1u, err);
+        wait_chunk(&bars[kb], (ph[kb] + (unsigned)(e / kSolveBufs)) & 1u, err);
         int c0, cn, ld;
         const T *src;
         pl.chunk(k, c0, cn, src, ld);
-        const Vec4<T> *v = (k < nA) ? gb : zv;
-        if (Q.active()) chunk_axpy(buf, ld, cn, c0, Q.q, Q.g, Q.G, v, ax, ay, az);
+        if (Q.active()) chunk_axpy(buf + row0, ld, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? gb : zv, ax, ay, az);
         __syncthreads();
-        if (tid == 0 && k + kSolveBufs < ntot) issue_chunk(pl, k + kSolveBufs, buf, &bars[kb]);
-        if (k == nA - 1) {
-            reduce_quads<T, true>(Q, ax, ay, az, red, zv);
+        if (tid == 0 && e + kSolveBufs < vtot) issue_chunk(pl, vp.real(e + kSolveBufs), buf, &bars[kb]);
+        if (k == (phase == 0 ? nA - 1 : ntot - 1)) {
+            if (phase == 0) reduce_quads<T, true>(Q, ax, ay, az, red, zv + row0);
+            else reduce_quads<T, false>(Q, ax, ay, az, red, xv + row0);
 #pragma unroll
             for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
         }
     }
-    reduce_quads<T, false>(Q, ax, ay, az, red, xv);
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = xv[i];
     // the barrier orders every thread's writes before thread 0's release,
     // which is cumulative: a CTA that acquires the flag sees them all
@@ -1237,7 +1280,7 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
         }
     }
 #pragma unroll
-    for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((ntot - b + kSolveBufs - 1) / kSolveBufs);
+    for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((vtot - b + kSolveBufs - 1) / kSolveBufs);
     }
 }
 
@@ -1752,11 +1795,7 @@ void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *it
     case kFupd: k_fupd<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval); break;
     case kFdt: k_fdt<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv, err); break;
     case kFsyrk: k_fsyrk<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Upd); break;
-    case kFx: {
-        const size_t smem = (size_t)((s.max_ncol + NB - 1) / NB * NB) * (NB + 1) * sizeof(TF);
-        k_fx<TF><<<fl.count, kFactorThreads, smem, st>>>(it, s.sn, Lval, Dinv, X, L21, L21T);
-        break;
-    }
+    case kFx: k_fx<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Dinv, X, L21, L21T); break;
     }
 }
 
@@ -1780,6 +1819,8 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
     k_residual<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, bfixed, b, x64, r);
 }
 
+int solve_chunk_bytes() { return kChunkBytes; }
+
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
     return (size_t)kSolveBufs * kChunkBytes + (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
 }
@@ -1795,10 +1836,11 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
         k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(s.s_low, s.s_low + G, lay, s.level_sn, s.sn, s.child, s.relind,
                                                        X, L21, sol, uvec, ticket, flags, err);
     if (s.s_top > 0) {
-        const size_t tsmem = top_smem_bytes_impl(s.max_ldx, s.max_ld21, sizeof(T));
+        const SolveSmem tlay{s.top_ldx, s.top_ld21};
+        const size_t tsmem = top_smem_bytes_impl(s.top_ldx, s.top_ld21, sizeof(T));
         k_solve_fwd_top<T, kTopCluster><<<s.top_clusters * kTopCluster, kSolveThreads, tsmem, st>>>(
-            s.s_top, s.s_top + s.top_clusters, s.ltop, lay, s.level_sn + s.s_low, s.sn, s.child, s.relind, X, L21, sol,
-            uvec, ticket + 2, flags, err);
+            s.s_top, s.s_top + s.top_clusters, s.ltop, tlay, s.level_sn + s.s_low, s.sn, s.child, s.relind, X, L21,
+            sol, uvec, ticket + 2, flags, err);
     }
 }
 
@@ -1811,10 +1853,11 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
     if (s.s_top > 0) {
-        const size_t tsmem = top_smem_bytes_impl(s.max_ldx, s.max_ld21, sizeof(T));
+        const SolveSmem tlay{s.top_ldx, s.top_ld21};
+        const size_t tsmem = top_smem_bytes_impl(s.top_ldx, s.top_ld21, sizeof(T));
         k_solve_bwd_top<T, kTopCluster><<<s.top_clusters * kTopCluster, kSolveThreads, tsmem, st>>>(
-            s.s_top, s.s_top + s.top_clusters, lay, s.level_sn + s.s_low, s.sn, s.rows, X, L21T, sol, pc64, pc32, mode,
-            ticket + 2, flags, err);
+            s.s_top, s.s_top + s.top_clusters, tlay, s.level_sn + s.s_low, s.sn, s.rows, X, L21T, sol, pc64, pc32,
+            mode, ticket + 2, flags, err);
     }
     if (s.s_low > 0)
         k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(s.s_low, s.s_low + G, s.ltop, lay, s.level_sn, s.sn, s.rows, X,
@@ -1865,12 +1908,6 @@ cudaError_t raise_smem_limit(const void *func, int bytes) {
     return e;
 }
 
-cudaError_t configure_factor_smem(int max_ncol) {
-    const int rows = (max_ncol + NB - 1) / NB * NB;
-    cudaError_t e = raise_smem_limit((const void *)k_fx<float>, (int)(rows * (NB + 1) * sizeof(float)));
-    if (e != cudaSuccess) return e;
-    return raise_smem_limit((const void *)k_fx<double>, (int)(rows * (NB + 1) * sizeof(double)));
-}
 
 // CTAs of the solve kernels that fit on the device at once for this dynamic
 // shared memory (precision T), at least 1.
@@ -1894,7 +1931,7 @@ cudaError_t configure_solve_smem(int bytes_f32, int bytes_f64) {
     cudaError_t e = raise_smem_limit((const void *)k_solve_fwd<float>, bytes_f32);
     if (e != cudaSuccess) return e;
     e = raise_smem_limit((const void *)k_solve_bwd<float>, bytes_f32);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || bytes_f64 <= 0) return e;
     e = raise_smem_limit((const void *)k_solve_fwd<double>, bytes_f64);
     if (e != cudaSuccess) return e;
     return raise_smem_limit((const void *)k_solve_bwd<double>, bytes_f64);
@@ -1908,7 +1945,7 @@ cudaError_t configure_top_smem(int bytes_f32, int bytes_f64) {
     cudaError_t e = raise_smem_limit((const void *)k_solve_fwd_top<float, kTopCluster>, bytes_f32);
     if (e != cudaSuccess) return e;
     e = raise_smem_limit((const void *)k_solve_bwd_top<float, kTopCluster>, bytes_f32);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || bytes_f64 <= 0) return e;
     e = raise_smem_limit((const void *)k_solve_fwd_top<double, kTopCluster>, bytes_f64);
     if (e != cudaSuccess) return e;
     return raise_smem_limit((const void *)k_solve_bwd_top<double, kTopCluster>, bytes_f64);

@@ -41,6 +41,7 @@ struct DevSym {
     // the solves split the tree: levels [0, ltop) by single CTAs (s_low tasks),
     // levels [ltop, top) by clusters (s_top tasks, top_clusters clusters)
     int ltop, s_low, s_top, top_clusters;
+    int top_ldx, top_ld21;  // largest front of the cluster levels (their shared-memory layout)
     const int32_t *drow, *dcol, *dent, *oldidx;
     const int64_t *amap, *dmap;
     const SnInfo *sn;
@@ -98,6 +99,12 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 // supernodal triangular solves L y = b (forward) and L^T x = y (backward),
 // one launch each, supernodes scheduled by a ticket counter with bounded waits.
 // mode 0: pc64[k] = x_k; mode 1: pc64[k] += x_k and pc32[k] = float(pc64[k]).
+// rows of one pass of a solve GEMV phase (one 4-row quad per thread); the
+// single-CTA solves take larger fronts in several passes, the cluster solves
+// take fronts of at most this many rows
+constexpr int kSolveBlockRows = 1024;
+// bytes of one chunk buffer of the solves (a matrix column must fit one)
+int solve_chunk_bytes();
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
 // solve CTAs resident on the device at once (occupancy x SMs) for that shared memory
 int solve_resident_ctas(int smem_bytes, int scalar_bytes);
