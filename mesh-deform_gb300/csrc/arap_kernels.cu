@@ -881,28 +881,37 @@ __device__ __forceinline__ T *sbuf(unsigned char *raw, int b) {
 struct VPlan {
     int nA, nB, rbA, rbB;
     __device__ int total() const { return nA * rbA + nB * rbB; }
-    // chunk index in the ChunkPlan, phase (0: A, 1: B) and row block of
-    // stream position e
-    __device__ void decode(int e, int &k, int &phase, int &rb) const {
-        if (e < nA * rbA) {
-            phase = 0;
-            rb = e / nA;
-            k = e - rb * nA;
-        } else {
-            const int f = e - nA * rbA;
-            phase = 1;
-            rb = f / nB;
-            k = nA + (f - rb * nB);
-        }
-    }
-    __device__ int real(int e) const {
-        int k, phase, rb;
-        decode(e, k, phase, rb);
-        return k;
-    }
 };
 
 __device__ __forceinline__ int row_blocks(int rows) { return (rows + kSolveBlockRows - 1) / kSolveBlockRows; }
+
+// Walks a VPlan's stream one chunk at a time without divisions: k is the
+// chunk's index in the ChunkPlan, phase and rb its phase and row block.
+struct VCursor {
+    int k, phase, rb;
+    __device__ void start(const VPlan &v) {
+        rb = 0;
+        phase = v.nA * v.rbA > 0 ? 0 : 1;
+        k = phase == 0 ? 0 : v.nA;
+    }
+    __device__ void step(const VPlan &v) {
+        ++k;
+        if (phase == 0) {
+            if (k == v.nA) {
+                k = 0;
+                if (++rb == v.rbA) {
+                    phase = 1;
+                    rb = 0;
+                    k = v.nA;
+                }
+            }
+        } else if (k == v.nA + v.nB) {
+            k = v.nA;
+            ++rb;
+        }
+    }
+    __device__ bool first_of_pass(const VPlan &v) const { return k == (phase == 0 ? 0 : v.nA); }
+};
 
 // Bounded wait for a buffer's bytes. On expiry it records kErrTimeout and
 // waits once more (bounded) so that no copy is still writing into shared
@@ -1065,8 +1074,10 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     const int ntot = pl.total();
     const VPlan vp{pl.nA, pl.nB, row_blocks(nc), pl.nB > 0 ? row_blocks(nb) : 0};
     const int vtot = vp.total();
+    VCursor iss;  // next stream position to issue (thread 0)
+    iss.start(vp);
     if (tid == 0) {
-        for (int e = 0; e < vtot && e < kSolveBufs; ++e) issue_chunk(pl, vp.real(e), sbuf<T>(smem_raw, e), &bars[e]);
+        for (int e = 0; e < vtot && e < kSolveBufs; ++e, iss.step(vp)) issue_chunk(pl, iss.k, sbuf<T>(smem_raw, e), &bars[e]);
         for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     for (int i = tid; i < d.ldx; i += kSolveThreads)
@@ -1138,25 +1149,55 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb), each in
     // passes of at most kSolveBlockRows rows
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-    for (int e = 0; e < vtot; ++e) {
-        int k, phase, rb;
-        vp.decode(e, k, phase, rb);
-        const int row0 = rb * kSolveBlockRows;
-        const Quads Q = quads_for(min(kSolveBlockRows, (phase == 0 ? nc : nb) - row0));
-        const int kb = e & (kSolveBufs - 1);
-        T *buf = sbuf<T>(smem_raw, kb);
-        wait_chunk(&bars[kb], (ph[kb] + (unsigned)(e / kSolveBufs)) & 1u, err);
-        int c0, cn, ld;
-        const T *src;
-        pl.chunk(k, c0, cn, src, ld);
-        if (Q.active()) chunk_axpy(buf + row0, ld, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? fc : yv, ax, ay, az);
-        __syncthreads();
-        if (tid == 0 && e + kSolveBufs < vtot) issue_chunk(pl, vp.real(e + kSolveBufs), buf, &bars[kb]);
-        if (k == (phase == 0 ? pl.nA - 1 : ntot - 1)) {
-            if (phase == 0) reduce_quads<T, false>(Q, ax, ay, az, red, yv + row0);
-            else reduce_quads<T, true>(Q, ax, ay, az, red, fb + row0);
+    if (vtot == ntot) {
+        // every phase in one pass: the plain chunk sequence
+        const Quads Qa = quads_for(nc), Qb = quads_for(nb);
+        for (int k = 0; k < ntot; ++k) {
+            const int kb = k & (kSolveBufs - 1);
+            T *buf = sbuf<T>(smem_raw, kb);
+            wait_chunk(&bars[kb], (ph[kb] + (unsigned)(k / kSolveBufs)) & 1u, err);
+            int c0, cn, ld;
+            const T *src;
+            pl.chunk(k, c0, cn, src, ld);
+            if (k < pl.nA) {
+                if (Qa.active()) chunk_axpy(buf, ld, cn, c0, Qa.q, Qa.g, Qa.G, fc, ax, ay, az);
+            } else {
+                if (Qb.active()) chunk_axpy(buf, ld, cn, c0, Qb.q, Qb.g, Qb.G, yv, ax, ay, az);
+            }
+            __syncthreads();
+            if (tid == 0 && k + kSolveBufs < ntot) issue_chunk(pl, k + kSolveBufs, buf, &bars[kb]);
+            if (k == pl.nA - 1) {
+                reduce_quads<T, false>(Qa, ax, ay, az, red, yv);
 #pragma unroll
-            for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+                for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+            }
+        }
+        if (pl.nB > 0) reduce_quads<T, true>(Qb, ax, ay, az, red, fb);
+    } else {
+        VCursor cur;
+        cur.start(vp);
+        Quads Q;
+        for (int e = 0; e < vtot; ++e, cur.step(vp)) {
+            const int k = cur.k, phase = cur.phase, row0 = cur.rb * kSolveBlockRows;
+            if (cur.first_of_pass(vp)) Q = quads_for(min(kSolveBlockRows, (phase == 0 ? nc : nb) - row0));
+            const int kb = e & (kSolveBufs - 1);
+            T *buf = sbuf<T>(smem_raw, kb);
+            wait_chunk(&bars[kb], (ph[kb] + (unsigned)(e / kSolveBufs)) & 1u, err);
+            int c0, cn, ld;
+            const T *src;
+            pl.chunk(k, c0, cn, src, ld);
+            if (Q.active()) chunk_axpy(buf + row0, ld, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? fc : yv, ax, ay, az);
+            __syncthreads();
+            if (tid == 0 && e + kSolveBufs < vtot) {
+                issue_chunk(pl, iss.k, buf, &bars[kb]);
+                iss.step(vp);
+            }
+            if (k == (phase == 0 ? pl.nA - 1 : ntot - 1)) {
+                if (phase == 0) reduce_quads<T, false>(Q, ax, ay, az, red, yv + row0);
+                else reduce_quads<T, true>(Q, ax, ay, az, red, fb + row0);
+#pragma unroll
+                for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+            }
         }
     }
     for (int i = tid; i < nb; i += kSolveThreads) uvec[d.uvec_off + i] = fb[i];
@@ -1214,8 +1255,10 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     const int nA = nb > 0 ? pl.nA : 0;  // chunks of L21^T
     const VPlan vp{nA, ntot - nA, row_blocks(nc), row_blocks(nc)};
     const int vtot = vp.total();
+    VCursor iss;  // next stream position to issue (thread 0)
+    iss.start(vp);
     if (tid == 0) {
-        for (int e = 0; e < vtot && e < kSolveBufs; ++e) issue_chunk(pl, vp.real(e), sbuf<T>(smem_raw, e), &bars[e]);
+        for (int e = 0; e < vtot && e < kSolveBufs; ++e, iss.step(vp)) issue_chunk(pl, iss.k, sbuf<T>(smem_raw, e), &bars[e]);
         for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     const int32_t *rs = rows + d.rows_off;
@@ -1236,25 +1279,52 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     // phase A (nb > 0): z -= L21^T g; phase B: x = X^T z; both have nc rows,
     // in passes of at most kSolveBlockRows rows
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-    for (int e = 0; e < vtot; ++e) {
-        int k, phase, rb;
-        vp.decode(e, k, phase, rb);
-        const int row0 = rb * kSolveBlockRows;
-        const Quads Q = quads_for(min(kSolveBlockRows, nc - row0));
-        const int kb = e & (kSolveBufs - 1);
-        T *buf = sbuf<T>(smem_raw, kb);
-        wait_chunk(&bars[kb], (ph[kb] + (unsigned)(e / kSolveBufs)) & 1u, err);
-        int c0, cn, ld;
-        const T *src;
-        pl.chunk(k, c0, cn, src, ld);
-        if (Q.active()) chunk_axpy(buf + row0, ld, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? gb : zv, ax, ay, az);
-        __syncthreads();
-        if (tid == 0 && e + kSolveBufs < vtot) issue_chunk(pl, vp.real(e + kSolveBufs), buf, &bars[kb]);
-        if (k == (phase == 0 ? nA - 1 : ntot - 1)) {
-            if (phase == 0) reduce_quads<T, true>(Q, ax, ay, az, red, zv + row0);
-            else reduce_quads<T, false>(Q, ax, ay, az, red, xv + row0);
+    if (vtot == ntot) {
+        // both phases in one pass: the plain chunk sequence
+        const Quads Q = quads_for(nc);
+        for (int k = 0; k < ntot; ++k) {
+            const int kb = k & (kSolveBufs - 1);
+            T *buf = sbuf<T>(smem_raw, kb);
+            wait_chunk(&bars[kb], (ph[kb] + (unsigned)(k / kSolveBufs)) & 1u, err);
+            int c0, cn, ld;
+            const T *src;
+            pl.chunk(k, c0, cn, src, ld);
+            const Vec4<T> *v = (k < nA) ? gb : zv;
+            if (Q.active()) chunk_axpy(buf, ld, cn, c0, Q.q, Q.g, Q.G, v, ax, ay, az);
+            __syncthreads();
+            if (tid == 0 && k + kSolveBufs < ntot) issue_chunk(pl, k + kSolveBufs, buf, &bars[kb]);
+            if (k == nA - 1) {
+                reduce_quads<T, true>(Q, ax, ay, az, red, zv);
 #pragma unroll
-            for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+                for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+            }
+        }
+        reduce_quads<T, false>(Q, ax, ay, az, red, xv);
+    } else {
+        VCursor cur;
+        cur.start(vp);
+        Quads Q;
+        for (int e = 0; e < vtot; ++e, cur.step(vp)) {
+            const int k = cur.k, phase = cur.phase, row0 = cur.rb * kSolveBlockRows;
+            if (cur.first_of_pass(vp)) Q = quads_for(min(kSolveBlockRows, nc - row0));
+            const int kb = e & (kSolveBufs - 1);
+            T *buf = sbuf<T>(smem_raw, kb);
+            wait_chunk(&bars[kb], (ph[kb] + (unsigned)(e / kSolveBufs)) & 1u, err);
+            int c0, cn, ld;
+            const T *src;
+            pl.chunk(k, c0, cn, src, ld);
+            if (Q.active()) chunk_axpy(buf + row0, ld, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? gb : zv, ax, ay, az);
+            __syncthreads();
+            if (tid == 0 && e + kSolveBufs < vtot) {
+                issue_chunk(pl, iss.k, buf, &bars[kb]);
+                iss.step(vp);
+            }
+            if (k == (phase == 0 ? nA - 1 : ntot - 1)) {
+                if (phase == 0) reduce_quads<T, true>(Q, ax, ay, az, red, zv + row0);
+                else reduce_quads<T, false>(Q, ax, ay, az, red, xv + row0);
+#pragma unroll
+                for (int z = 0; z < 4; ++z) ax[z] = ay[z] = az[z] = (T)0;
+            }
         }
     }
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = xv[i];
