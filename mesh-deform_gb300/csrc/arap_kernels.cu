@@ -972,8 +972,9 @@ __device__ __forceinline__ Quads quads_for(int rows) {
 // then over at most 8 partials per quad through shared memory, in a fixed
 // order. Ends with a barrier.
 template <typename T, bool SUB>
-__device__ __forceinline__ void reduce_quads(const Quads &Q, T ax[4], T ay[4], T az[4], Vec4<T> *red,
-                                             Vec4<T> *out) {
+__device__ __forceinline__ void reduce_quads(const Quads &Q, T ax[4], T ay[4], T az[4], T *red, Vec4<T> *out) {
+    // scratch: three arrays of kRedRows scalars (x, y, z)
+    T *rx = red, *ry = red + kRedRows, *rz = red + 2 * kRedRows;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int slot, nslots;
     bool writer;
@@ -998,14 +999,19 @@ __device__ __forceinline__ void reduce_quads(const Quads &Q, T ax[4], T ay[4], T
     }
     if (writer && Q.active())
 #pragma unroll
-        for (int k = 0; k < 4; ++k) red[(slot * Q.NQ + Q.q) * 4 + k] = {ax[k], ay[k], az[k], (T)0};
+        for (int k = 0; k < 4; ++k) {
+            const int i = (slot * Q.NQ + Q.q) * 4 + k;
+            rx[i] = ax[k];
+            ry[i] = ay[k];
+            rz[i] = az[k];
+        }
     __syncthreads();
     for (int rr = tid; rr < 4 * Q.NQ; rr += kSolveThreads) {
         const int qq = rr >> 2, k = rr & 3;
         T sx = 0, sy = 0, sz = 0;
         for (int s = 0; s < nslots; ++s) {
-            const Vec4<T> p = red[(s * Q.NQ + qq) * 4 + k];
-            sx += p.x; sy += p.y; sz += p.z;
+            const int i = (s * Q.NQ + qq) * 4 + k;
+            sx += rx[i]; sy += ry[i]; sz += rz[i];
         }
         Vec4<T> &o = out[rr];
         if (SUB) { o.x -= sx; o.y -= sy; o.z -= sz; }
@@ -1047,9 +1053,12 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
             unsigned long long *ticket, unsigned *flags, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Vec4<T> *fc = reinterpret_cast<Vec4<T> *>(smem_raw + kSolveBufs * kChunkBytes);
-    Vec4<T> *yv = fc + lay.ldx_max;
+    // y takes f's place once phase A's sums are reduced, unless a front needs
+    // several passes (later passes still read all of f)
+    const bool y_in_f = lay.ldx_max <= kSolveBlockRows;
+    Vec4<T> *yv = y_in_f ? fc : fc + lay.ldx_max;
     Vec4<T> *fb = yv + lay.ldx_max;
-    Vec4<T> *red = fb + lay.ld21_max;
+    T *red = reinterpret_cast<T *>(fb + lay.ld21_max);
     __shared__ __align__(8) uint64_t bars[kSolveBufs];
     __shared__ int s_task[2];  // this task's and the next one's ticket (taken early)
     __shared__ unsigned s_epoch[2];
@@ -1207,8 +1216,9 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
     if (tid == 0) st_release(flags + s, epoch);
     // y of this supernode's columns is read only by the backward sweep (a
     // later launch): stored after the release, off the parent's critical
-    // path. yv is next written after a barrier of the next task.
+    // path.
     for (int i = tid; i < nc; i += kSolveThreads) sol[d.first + i] = yv[i];
+    if (y_in_f) __syncthreads();  // the next task loads its f over y
 #pragma unroll
     for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((vtot - b + kSolveBufs - 1) / kSolveBufs);
     }
@@ -1226,9 +1236,9 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
             unsigned long long *ticket, unsigned *flags, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Vec4<T> *zv = reinterpret_cast<Vec4<T> *>(smem_raw + kSolveBufs * kChunkBytes);
-    Vec4<T> *xv = zv + lay.ldx_max;
-    Vec4<T> *gb = xv + lay.ldx_max;
-    Vec4<T> *red = gb + lay.ld21_max;
+    Vec4<T> *gb = zv + lay.ldx_max;
+    Vec4<T> *xv = gb;  // x takes the place of the gathered rows, read by phase A only
+    T *red = reinterpret_cast<T *>(gb + max(lay.ldx_max, lay.ld21_max));
     __shared__ __align__(8) uint64_t bars[kSolveBufs];
     __shared__ int s_task[2];  // this task's and the next one's ticket (taken early)
     __shared__ unsigned s_epoch[2];
@@ -1407,7 +1417,7 @@ k_solve_fwd_top(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict
     Vec4<T> *fc = TopSmem<T, CL>::vec(smem_raw, 0, lay.ldx_max, lay.ld21_max);
     Vec4<T> *yv = TopSmem<T, CL>::vec(smem_raw, 1, lay.ldx_max, lay.ld21_max);
     Vec4<T> *fb = TopSmem<T, CL>::vec(smem_raw, 2, lay.ldx_max, lay.ld21_max);
-    Vec4<T> *red = TopSmem<T, CL>::vec(smem_raw, 3, lay.ldx_max, lay.ld21_max);
+    T *red = reinterpret_cast<T *>(TopSmem<T, CL>::vec(smem_raw, 3, lay.ldx_max, lay.ld21_max));
     Vec4<T> *ypart = TopSmem<T, CL>::vec(smem_raw, 4, lay.ldx_max, lay.ld21_max);
     Vec4<T> *upart = TopSmem<T, CL>::vec(smem_raw, 5, lay.ldx_max, lay.ld21_max);
     __shared__ __align__(8) uint64_t bars[2];
@@ -1541,7 +1551,7 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
     Vec4<T> *zv = TopSmem<T, CL>::vec(smem_raw, 0, lay.ldx_max, lay.ld21_max);
     Vec4<T> *zf = TopSmem<T, CL>::vec(smem_raw, 1, lay.ldx_max, lay.ld21_max);
     Vec4<T> *gb = TopSmem<T, CL>::vec(smem_raw, 2, lay.ldx_max, lay.ld21_max);
-    Vec4<T> *red = TopSmem<T, CL>::vec(smem_raw, 3, lay.ldx_max, lay.ld21_max);
+    T *red = reinterpret_cast<T *>(TopSmem<T, CL>::vec(smem_raw, 3, lay.ldx_max, lay.ld21_max));
     Vec4<T> *zpart = TopSmem<T, CL>::vec(smem_raw, 4, lay.ldx_max, lay.ld21_max);
     Vec4<T> *xpart = TopSmem<T, CL>::vec(smem_raw, 5, lay.ldx_max, lay.ld21_max);
     __shared__ __align__(8) uint64_t bars[2];
@@ -1892,7 +1902,11 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 int solve_chunk_bytes() { return kChunkBytes; }
 
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
-    return (size_t)kSolveBufs * kChunkBytes + (size_t)(2 * ldx_max + ld21_max + kRedRows) * 4 * scalar_bytes;
+    // forward: f [y] f_b; backward: z, then g and x in one place; then the
+    // reduction scratch (3 x kRedRows scalars)
+    const size_t fwd = (size_t)ldx_max + (ldx_max > kSolveBlockRows ? ldx_max : 0) + ld21_max;
+    const size_t bwd = (size_t)ldx_max + std::max(ldx_max, ld21_max);
+    return (size_t)kSolveBufs * kChunkBytes + (std::max(fwd, bwd) * 4 + 3 * (size_t)kRedRows) * scalar_bytes;
 }
 
 template <typename T>
