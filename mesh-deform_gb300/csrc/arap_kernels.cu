@@ -380,8 +380,11 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
     const int j0 = jb * NB, w = min(NB, nc - j0);
     TF *P = Lval + d.panel_off;
     const int tid = threadIdx.x, lane = tid & 31;
-    constexpr int kRowThreads = kFactorThreads - 32;
-    const int i_first = j0 + w + (tid - 32);  // warps 1-7: first trailing row
+    // the rows below the block: warps 1.. of the CTA, or warp 0 itself after
+    // the inverse when the CTA is a single warp
+    const bool solo = blockDim.x == 32;
+    const int row_threads = solo ? 32 : (int)blockDim.x - 32;
+    const int i_first = j0 + w + (solo ? lane : tid - 32);
     TF a[NB];
     TF myinv = (TF)0;  // warp 0: 1 / L(lane, lane)
     if (tid < 32) {
@@ -439,10 +442,10 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
         TF *D = Dinv + d.dinv_off + (int64_t)jb * NB * NB;
 #pragma unroll
         for (int c = 0; c < NB; ++c) D[c * NB + lane] = y[c];
-        return;
+        if (!solo) return;
     }
-    for (int i = i_first; i < n; i += kRowThreads) {
-        if (i != i_first) {
+    for (int i = i_first; i < n; i += row_threads) {
+        if (solo || i != i_first) {
 #pragma unroll
             for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i] : (TF)0;
         }
@@ -1873,7 +1876,21 @@ void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *it
     switch (fl.kind) {
     case kFea: k_fea<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, s.child, s.relind, Lval, Upd); break;
     case kFupd: k_fupd<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval); break;
-    case kFdt: k_fdt<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv, err); break;
+    case kFdt: {
+        // many small fronts (the wide lower levels): one-warp CTAs, so that
+        // more of the register-heavy blocks fit on an SM at once; few large
+        // fronts: 256 threads for the rows below the block
+        static int sms = 0;
+        if (sms == 0) {
+            int dev = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                          cudaSuccess)
+                sms = 1;
+        }
+        const int threads = fl.count > 2 * sms ? 32 : kFactorThreads;
+        k_fdt<TF><<<fl.count, threads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv, err);
+        break;
+    }
     case kFsyrk: k_fsyrk<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Upd); break;
     case kFx: k_fx<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Dinv, X, L21, L21T); break;
     }
