@@ -214,7 +214,7 @@ int arap_energy(arap_ctx *ctx, double *energy);
 /* Host time of the last arap_deform_async, in ms, by phase: symbolic
    analysis and its upload, device allocation, set-up enqueue, iteration
    enqueue, the rest (gather, copies). The phases of a non-dirty deform are 0
-   but for the last two. */
+   but for the last two; after an arap_deform_poses_async all five are 0. */
 int arap_get_host_timing(arap_ctx *ctx, double *ms5);
 
 /* Vertex normals of the current deformed positions, computed on the device

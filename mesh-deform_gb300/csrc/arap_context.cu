@@ -953,6 +953,7 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
         const int rc_ = arap_wait(ctx);
         if (rc_ != ARAP_OK) return rc_;
     }
+    std::fill(ctx->host_ms, ctx->host_ms + 5, 0.0);  // phases are timed for arap_deform_async only
     if (n_poses <= 0 || iterations < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "n_poses must be positive");
     if (ctx->precision != ARAP_PRECISION_MIXED)
         return fail(ctx, ARAP_ERR_UNSUPPORTED, "arap_deform_poses runs the mixed-precision form only");

@@ -132,3 +132,22 @@ def test_pose_batch_pose_count_change_resets_schedule(gpu):
                 np.testing.assert_array_equal(ctx.deform_poses(w.poses[:n], 4), full[:n])
         # the device holds targets for 9 poses, not for 5
         assert ctx.lib.arap_deform_poses(ctx.h, 5, None, 4, None) == gpu.ARAP_ERR_INVALID_ARGUMENT
+
+
+def test_pose_tile_that_does_not_fit_is_refused(gpu):
+    """The twisted bar's largest front has 544 rows: 136 quads x 16 poses is
+    more than the 1,024 items a batched-solve CTA holds, so tile 16 is refused
+    (ARAP_ERR_UNSUPPORTED) and the automatic choice still runs."""
+    w = W.cfg_twisted_bar(iterations=2)
+    poses = np.stack([w.ctargets, w.ctargets + 0.01])
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.ctargets)
+        ctx.set_pose_tile(16)
+        with pytest.raises(gpu.ArapError) as e:
+            ctx.deform_poses(poses, 2)
+        assert e.value.code == gpu.ARAP_ERR_UNSUPPORTED
+        ctx.set_pose_tile(0)
+        out = ctx.deform_poses(poses, 2)
+        assert np.isfinite(out).all()

@@ -100,6 +100,9 @@ def test_results_same_alone_and_in_the_mix(gpu, precision):
     srv.close()
     assert st["completed"] == len(reqs) and st["failed"] == 0
     assert st["factor_hits"] > 0
+    # host time of the launch calls, and its phases (the struct layout matches the C ABI)
+    assert st["launch_ms"] > 0 and len(st["launch_host_ms"]) == 5
+    assert 0 < sum(st["launch_host_ms"]) <= st["launch_ms"] * 1.01
     if precision == "mixed":
         assert st["batched_launches"] > 0
     # the oracle pins a sample of them
