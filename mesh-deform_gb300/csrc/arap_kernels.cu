@@ -1880,13 +1880,13 @@ void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *it
         // many small fronts (the wide lower levels): one-warp CTAs, so that
         // more of the register-heavy blocks fit on an SM at once; few large
         // fronts: 256 threads for the rows below the block
-        static int sms = 0;
-        if (sms == 0) {
-            int dev = 0;
-            if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
-                                                          cudaSuccess)
-                sms = 1;
-        }
+        static const int sms = [] {  // initialised once, thread-safe
+            int dev = 0, n = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess ||
+                cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+                return 1;
+            return n;
+        }();
         const int threads = fl.count > 2 * sms ? 32 : kFactorThreads;
         k_fdt<TF><<<fl.count, threads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv, err);
         break;
