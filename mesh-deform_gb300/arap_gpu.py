@@ -107,6 +107,7 @@ SIGNATURES = {
     "arap_set_pose_tile": (C.c_int, [_P, _I32]),
     "arap_energy": (C.c_int, [_P, _dp]),
     "arap_set_cluster_threshold": (C.c_int, [_P, _I32]),
+    "arap_set_dense_top": (C.c_int, [_P, _I32]),
     "arap_set_ordering": (C.c_int, [_P, _I32]),
     "arap_set_done_callback": (C.c_int, [_P, _P, _P]),
     "arap_get_host_timing": (C.c_int, [_P, _dp]),
@@ -308,6 +309,10 @@ class ArapContext:
 
     def set_cluster_threshold(self, nbytes: int):
         self._check(self.lib.arap_set_cluster_threshold(self.h, int(nbytes)))
+
+    def set_dense_top(self, max_columns: int):
+        """Columns of the tree's top solved through an explicit inverse (0: default, <0: none)."""
+        self._check(self.lib.arap_set_dense_top(self.h, int(max_columns)))
 
     def set_solve_ctas(self, n: int):
         self._check(self.lib.arap_set_solve_ctas(self.h, int(n)))

@@ -155,6 +155,9 @@ struct arap_ctx {
     bool use_graphs = true;
     int solve_cap = 0;  // most CTAs per triangular-solve launch (0: as many as fit the device)
     int top_bytes = 0;  // supernode size from which tree levels go to the cluster solves (0: default, <0: never)
+    int dense_cols = 0;  // most columns of the dense top of the tree (0: default, <0: none)
+    size_t dense_inv_smem[2] = {0, 0}, dense_vec_smem[2] = {0, 0};  // configured limits (FP32, FP64)
+    DevBuf top_col, top_gptr, top_gidx, tdpos, top_items, Ttop, ytop;
     int ordering = ARAP_ORDER_PER_CONSTRAINT_SET;
     arap_done_fn done_fn = nullptr;  // called from a CUDA thread when an async deform finished
     void *done_user = nullptr;
@@ -186,7 +189,7 @@ struct arap_ctx {
                 &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
                 &errw, &ticket, &flags, &energy, &cidx_dev, &handle_dev, &tabs_dev, &vf_ptr, &vf_face, &fnorm,
                 &vnorm, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
-                &bticket, &bflags};
+                &bticket, &bflags, &top_col, &top_gptr, &top_gidx, &tdpos, &top_items, &Ttop, &ytop};
     }
 };
 
@@ -268,6 +271,36 @@ int analyze_symbolic(arap_ctx *ctx) {
     return ARAP_OK;
 }
 
+// The dense top of the tree: the most top levels whose supernodes hold at most
+// `cap` columns together (at least two levels, or none). Returns its first
+// level (nlev when empty) and its column count.
+struct DenseTopChoice {
+    int level = 0, ncols = 0;
+};
+DenseTopChoice choose_dense_top(const Symbolic &s, int cap) {
+    const int nlev = (int)s.level_ptr.size() - 1;
+    DenseTopChoice t;
+    t.level = std::max(nlev, 0);
+    if (cap <= 0 || nlev <= 0) return t;
+    int cols = 0, level = nlev;
+    for (int l = nlev - 1; l >= 0; --l) {
+        int c = 0;
+        for (int q = s.level_ptr[l]; q < s.level_ptr[l + 1]; ++q) c += s.sn[s.level_sn[q]].ncol;
+        if (cols + c > cap) break;
+        cols += c;
+        level = l;
+    }
+    if (nlev - level >= 2) {
+        t.level = level;
+        t.ncols = cols;
+    }
+    return t;
+}
+
+int dense_cap(const arap_ctx *ctx) {
+    return ctx->dense_cols < 0 ? 0 : (ctx->dense_cols == 0 ? kDenseTopCols : std::min(ctx->dense_cols, kDenseTopCols));
+}
+
 // Bytes of every device buffer the setup of precision T (and, for n_poses > 0,
 // arap_deform_poses with that many poses) holds, buffer by buffer.
 template <typename T>
@@ -314,6 +347,11 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     add(ctx->Xinv, (size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T));
     add(ctx->L21, (size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T));
     add(ctx->L21T, (size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T));
+    {
+        const size_t nt = (size_t)choose_dense_top(s, dense_cap(ctx)).ncols;
+        add(ctx->Ttop, std::max<size_t>(nt * nt, 1) * sizeof(T));
+        add(ctx->ytop, std::max<size_t>(nt, 1) * sizeof(Vec4<T>));
+    }
     if (n_poses > 0) {
         const size_t P = (size_t)n_poses, VP = V * P, MP = m1 * P, nc = V - (size_t)s.m;
         const int pt = std::max(batch_pose_tile(s.max_ldx, s.max_ld21), 1);
@@ -330,6 +368,62 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
         add(ctx->bticket, 2 * sizeof(unsigned long long));
         add(ctx->bflags, 2 * S1 * T_ * sizeof(unsigned));
     }
+}
+
+// Index maps of the dense top (levels >= level, n columns) uploaded to the
+// device: each top supernode's dense offset, each dense index's device column,
+// the update-vector entries of the top supernodes' children in the lower
+// levels that land on each dense row (children in child-list order), and the
+// work items of the inversion (supernode, first of 16 columns).
+int prepare_dense_top(arap_ctx *ctx, int level, int n) {
+    const Symbolic &s = ctx->sym;
+    DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    const int nlev = (int)s.level_ptr.size() - 1;
+    std::vector<int32_t> tdpos(std::max(s.S, 1), -1), col(n), items;
+    std::vector<int32_t> col2d(std::max(s.m, 1), -1);
+    int off = 0;
+    for (int j = 0; j < s.S; ++j) {  // supernode order is the elimination order
+        const SnInfo &x = s.sn[j];
+        if (x.level < level) continue;
+        tdpos[j] = off;
+        for (int c = 0; c < x.ncol; ++c) {
+            col[off + c] = x.first + c;
+            col2d[x.first + c] = off + c;
+        }
+        for (int c0 = 0; c0 < x.ncol; c0 += kTopRhs) items.insert(items.end(), {j, c0});
+        off += x.ncol;
+    }
+    if (off != n) return fail(ctx, ARAP_ERR_CUDA, "dense top: column count mismatch");
+    std::vector<int32_t> cnt(n + 1, 0);
+    std::vector<std::pair<int32_t, int64_t>> entries;
+    for (int q = s.level_ptr[level]; q < s.level_ptr[nlev]; ++q) {
+        const SnInfo &a = s.sn[s.level_sn[q]];
+        for (int ci = a.child_begin; ci < a.child_end; ++ci) {
+            const SnInfo &c = s.sn[s.child[ci]];
+            if (c.level >= level) continue;
+            for (int i = 0; i < c.nrow - c.ncol; ++i) {
+                const int dd = col2d[s.rows[c.rows_off + i]];
+                if (dd < 0) return fail(ctx, ARAP_ERR_CUDA, "dense top: update row outside the top");
+                entries.push_back({dd, c.uvec_off + i});
+            }
+        }
+    }
+    for (const auto &e : entries) ++cnt[e.first + 1];
+    for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int64_t> gidx(std::max<size_t>(entries.size(), 1), 0);
+    {
+        std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+        for (const auto &e : entries) gidx[fill[e.first]++] = e.second;  // stable: entries keep their order per row
+    }
+    CK(upload(ctx->tdpos, tdpos, st));
+    CK(upload(ctx->top_col, col, st));
+    CK(upload(ctx->top_gptr, cnt, st));
+    CK(upload(ctx->top_gidx, gidx, st));
+    CK(upload(ctx->top_items, items, st));
+    d.n_top = n;
+    d.n_top_items = (int)items.size() / 2;
+    return ARAP_OK;
 }
 
 int prepare_symbolic(arap_ctx *ctx) {
@@ -389,9 +483,38 @@ int prepare_symbolic(arap_ctx *ctx) {
         // the cluster solves take fronts of at most kSolveBlockRows rows
         for (const SnInfo &q : s.sn)
             if (q.level >= ltop && std::max(q.ldx, q.ld21) > kSolveBlockRows) ltop = std::max(ltop, q.level + 1);
+        // the dense top, where its inversion's and its solves' shared memory
+        // fit, takes the top levels instead of the clusters
+        d.n_top = d.n_top_items = d.dense_ldx = d.dense_ld21 = 0;
+        const DenseTopChoice dtop = choose_dense_top(s, dense_cap(ctx));
+        if (dtop.ncols > 0) {
+            int ldxm = 0, ld21m = 0;
+            for (int q = s.level_ptr[dtop.level]; q < s.level_ptr[nlev]; ++q) {
+                const SnInfo &x = s.sn[s.level_sn[q]];
+                ldxm = std::max(ldxm, (int)x.ldx);
+                ld21m = std::max(ld21m, (int)x.ld21);
+            }
+            const size_t i32 = dense_inverse_smem_bytes(ldxm, ld21m, 4), i64 = dense_inverse_smem_bytes(ldxm, ld21m, 8);
+            const size_t v32 = (size_t)dtop.ncols * 16, v64 = (size_t)dtop.ncols * 32;
+            if (i64 <= kSmemMax && v64 <= kSmemMax) {
+                const int rc_d = prepare_dense_top(ctx, dtop.level, dtop.ncols);
+                if (rc_d != ARAP_OK) return rc_d;
+                if (i32 > ctx->dense_inv_smem[0] || i64 > ctx->dense_inv_smem[1] || v32 > ctx->dense_vec_smem[0] ||
+                    v64 > ctx->dense_vec_smem[1]) {
+                    CK(configure_dense_smem((int)i32, (int)i64, (int)v32, (int)v64));
+                    ctx->dense_inv_smem[0] = std::max(ctx->dense_inv_smem[0], i32);
+                    ctx->dense_inv_smem[1] = std::max(ctx->dense_inv_smem[1], i64);
+                    ctx->dense_vec_smem[0] = std::max(ctx->dense_vec_smem[0], v32);
+                    ctx->dense_vec_smem[1] = std::max(ctx->dense_vec_smem[1], v64);
+                }
+                d.dense_ldx = ldxm;
+                d.dense_ld21 = ld21m;
+                ltop = dtop.level;
+            }
+        }
         d.ltop = ltop;
         d.s_low = nlev > 0 ? s.level_ptr[ltop] : 0;
-        d.s_top = s.S - d.s_low;
+        d.s_top = d.n_top > 0 ? 0 : s.S - d.s_low;
         int width = 0;
         for (int l = ltop; l < nlev; ++l) width = std::max(width, s.level_ptr[l + 1] - s.level_ptr[l]);
         d.top_clusters = std::max(1, std::min(width, kTopMaxClusters));
@@ -404,7 +527,7 @@ int prepare_symbolic(arap_ctx *ctx) {
         // the cluster levels
         d.top_ldx = d.top_ld21 = 0;
         for (const SnInfo &q : s.sn)
-            if (q.level >= ltop) {
+            if (q.level >= ltop && d.s_top > 0) {
                 d.top_ldx = std::max(d.top_ldx, (int)q.ldx);
                 d.top_ld21 = std::max(d.top_ld21, (int)q.ld21);
             }
@@ -438,6 +561,11 @@ int prepare_symbolic(arap_ctx *ctx) {
     d.relind = ctx->relind.as<int32_t>();
     d.child = ctx->child.as<int32_t>();
     d.level_sn = ctx->level_sn.as<int32_t>();
+    d.top_col = ctx->top_col.as<int32_t>();
+    d.top_gptr = ctx->top_gptr.as<int32_t>();
+    d.top_gidx = ctx->top_gidx.as<int64_t>();
+    d.tdpos = ctx->tdpos.as<int32_t>();
+    d.top_items = ctx->top_items.as<int32_t>();
     ctx->sym_valid = true;
     return ARAP_OK;
 }
@@ -510,6 +638,11 @@ int setup_enqueue(arap_ctx *ctx) {
                                   ctx->errw.as<int>(), st);
             ctx->launches += 1;
         }
+        if (d.n_top > 0) {
+            Prof pr(ctx, ARAP_K_FACTOR);
+            launch_top_inverse<T>(d, ctx->Xinv.as<T>(), ctx->L21.as<T>(), ctx->Ttop.as<T>(), st);
+            ctx->launches += 1;
+        }
     }
     CK(cudaGetLastError());
     return ARAP_OK;
@@ -579,7 +712,7 @@ template <typename T>
 int run_iterations(arap_ctx *ctx, int iterations);
 
 // kernels of one forward + backward sweep (lower levels and cluster levels)
-int solve_launches(const DevSym &d) { return 2 * ((d.s_low > 0) + (d.s_top > 0)); }
+int solve_launches(const DevSym &d) { return 2 * ((d.s_low > 0) + (d.s_top > 0) + (d.n_top > 0)); }
 
 template <>
 int run_iterations<double>(arap_ctx *ctx, int iterations) {
@@ -605,13 +738,14 @@ int run_iterations<double>(arap_ctx *ctx, int iterations) {
             Prof pr(ctx, ARAP_K_SOLVE_FWD);
             launch_solve_fwd<double>(d, ctx->Xinv.as<double>(), ctx->L21.as<double>(),
                                      ctx->sol.as<Vec4<double>>(), ctx->uvec.as<Vec4<double>>(), tk, fl,
-                                     ctx->errw.as<int>(), st);
+                                     ctx->errw.as<int>(), st, ctx->Ttop.as<double>(), ctx->ytop.as<Vec4<double>>());
         }
         {
             Prof pr(ctx, ARAP_K_SOLVE_BWD);
             launch_solve_bwd<double>(d, ctx->Xinv.as<double>(), ctx->L21T.as<double>(),
                                      ctx->sol.as<Vec4<double>>(), ctx->pc64.as<Vec4<double>>(), nullptr, 0, tk + 1,
-                                     fl + s.S, ctx->errw.as<int>(), st);
+                                     fl + s.S, ctx->errw.as<int>(), st, ctx->Ttop.as<double>(),
+                                     ctx->ytop.as<Vec4<double>>());
         }
         ctx->launches += solve_launches(d) + 1;
     }
@@ -650,13 +784,14 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
                 Prof pr(ctx, ARAP_K_SOLVE_FWD);
                 launch_solve_fwd<float>(d, ctx->Xinv.as<float>(), ctx->L21.as<float>(),
                                         ctx->sol.as<Vec4<float>>(), ctx->uvec.as<Vec4<float>>(), tk, fl,
-                                        ctx->errw.as<int>(), st);
+                                        ctx->errw.as<int>(), st, ctx->Ttop.as<float>(), ctx->ytop.as<Vec4<float>>());
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_BWD);
                 launch_solve_bwd<float>(d, ctx->Xinv.as<float>(), ctx->L21T.as<float>(),
                                         ctx->sol.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(),
-                                        ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(), st);
+                                        ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(), st,
+                                        ctx->Ttop.as<float>(), ctx->ytop.as<Vec4<float>>());
             }
             ctx->launches += solve_launches(d) + 1;
         }
@@ -855,6 +990,7 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->use_graphs = src->use_graphs;
     ctx->solve_cap = src->solve_cap;
     ctx->top_bytes = src->top_bytes;
+    ctx->dense_cols = src->dense_cols;
     ctx->ordering = src->ordering;
     return finish_create(ctx, src->device, src, out);
 }
@@ -1404,6 +1540,20 @@ int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes) {
     }
     if (bytes != ctx->top_bytes) {
         ctx->top_bytes = bytes;
+        ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
+        ctx->dirty = true;
+    }
+    return ARAP_OK;
+}
+
+int arap_set_dense_top(arap_ctx *ctx, int32_t max_columns) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (max_columns != ctx->dense_cols) {
+        ctx->dense_cols = max_columns;
         ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
         ctx->dirty = true;
     }

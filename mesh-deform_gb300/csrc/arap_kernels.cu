@@ -1668,6 +1668,196 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
 }
 
 // ---------------------------------------------------------------------------
+// Dense top of the elimination tree. The top levels hold few supernodes, and
+// each is one CTA's task on the sweeps' critical path. For them the factor's
+// restriction L_top (n_top <= a few thousand columns, in elimination order)
+// is inverted once per factorisation, T = inv(L_top) dense; a sweep then
+// solves the top in one wide launch: forward y_top = T f_top, where f_top is
+// the top columns' right-hand side plus the update vectors of their children
+// in the lower levels, and backward x_top = T^T y_top.
+
+// Column block [c0, c0 + 16) of supernode j's columns of T: the forward solve
+// of L_top Y = E (E the identity columns) restricted to j and its ancestors,
+// supernode by supernode: Y_a = X_a F_a, U_a = F_b - L21_a Y_a, with F the
+// update rows scattered into the parent's front (Y_j = X_j at the start).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, const int32_t *__restrict__ relind,
+              const int32_t *__restrict__ tdpos, const T *__restrict__ Xall, const T *__restrict__ L21all, int n_top,
+              int ldx_max, int ld21_max, T *__restrict__ Tt) {
+    extern __shared__ __align__(16) unsigned char top_raw[];
+    constexpr int RC = kTopRhs;
+    T *Y = reinterpret_cast<T *>(top_raw);  // [row][RC], rows of the current supernode's columns
+    T *U = Y + (size_t)ldx_max * RC;       // [row][RC], its struct rows
+    T *F = U + (size_t)ld21_max * RC;      // the parent's front: columns
+    T *Fb = F + (size_t)ldx_max * RC;      // and struct rows
+    const int tid = threadIdx.x;
+    const int j = items[2 * blockIdx.x], c0 = items[2 * blockIdx.x + 1];
+    const SnInfo dj = sn[j];
+    const int w = min(RC, dj.ncol - c0);
+    const int64_t dcol0 = (int64_t)tdpos[j] + c0;  // dense column of the block's first column
+    // supernode j: Y = X_j[:, c0 + c]
+    {
+        const T *X = Xall + dj.x_off;
+        for (int q = tid; q < dj.ncol * RC; q += 256) {
+            const int r = q / RC, c = q % RC;
+            const T v = c < w ? X[(int64_t)(c0 + c) * dj.ldx + r] : (T)0;
+            Y[q] = v;
+            if (c < w) Tt[((int64_t)tdpos[j] + r) * n_top + dcol0 + c] = v;
+        }
+    }
+    __syncthreads();
+    int node = j;
+    SnInfo dn = dj;
+    for (;;) {
+        // U = -L21 Y (or F_b - L21 Y below), the update rows of `node`
+        const int nbn = dn.nrow - dn.ncol;
+        const T *L21 = L21all + dn.l21_off;
+        const bool first = node == j;
+        for (int r = tid; r < nbn; r += 256) {
+            T acc[RC];
+#pragma unroll
+            for (int c = 0; c < RC; ++c) acc[c] = first ? (T)0 : Fb[r * RC + c];
+            for (int k = 0; k < dn.ncol; ++k) {
+                const T l = L21[(int64_t)k * dn.ld21 + r];
+#pragma unroll
+                for (int c = 0; c < RC; ++c) acc[c] -= l * Y[k * RC + c];
+            }
+#pragma unroll
+            for (int c = 0; c < RC; ++c) U[r * RC + c] = acc[c];
+        }
+        __syncthreads();
+        if (dn.parent < 0) break;
+        const int a = dn.parent;
+        const SnInfo da = sn[a];
+        const int nca = da.ncol, nba = da.nrow - da.ncol;
+        for (int q = tid; q < (nca + nba) * RC; q += 256) (q < nca * RC ? F[q] : Fb[q - nca * RC]) = (T)0;
+        __syncthreads();
+        const int32_t *ri = relind + dn.relind_off;
+        for (int q = tid; q < nbn * RC; q += 256) {
+            const int i = q / RC, c = q % RC;
+            const int pos = ri[i];
+            (pos < nca ? F[pos * RC + c] : Fb[(pos - nca) * RC + c]) = U[q];
+        }
+        __syncthreads();
+        // Y = X_a F
+        const T *X = Xall + da.x_off;
+        for (int r = tid; r < nca; r += 256) {
+            T acc[RC];
+#pragma unroll
+            for (int c = 0; c < RC; ++c) acc[c] = (T)0;
+            for (int k = 0; k <= r; ++k) {  // X_a is lower triangular
+                const T x = X[(int64_t)k * da.ldx + r];
+#pragma unroll
+                for (int c = 0; c < RC; ++c) acc[c] += x * F[k * RC + c];
+            }
+            T *trow = Tt + ((int64_t)tdpos[a] + r) * n_top + dcol0;
+#pragma unroll
+            for (int c = 0; c < RC; ++c) {
+                Y[r * RC + c] = acc[c];
+                if (c < w) trow[c] = acc[c];
+            }
+        }
+        __syncthreads();
+        node = a;
+        dn = da;
+    }
+}
+
+// f_top (right-hand side of the top columns plus their lower children's
+// update vectors, in a fixed order) into shared memory; then one warp per row:
+// y_i = sum_{j <= i} T(i, j) f_j, lanes over j, sums in a fixed order.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_top_fwd(int n, const int32_t *__restrict__ col, const int32_t *__restrict__ gptr, const int64_t *__restrict__ gidx,
+          const T *__restrict__ Tt, const Vec4<T> *__restrict__ sol, const Vec4<T> *__restrict__ uvec,
+          Vec4<T> *__restrict__ ytop) {
+    extern __shared__ __align__(16) unsigned char top_raw[];
+    Vec4<T> *f = reinterpret_cast<Vec4<T> *>(top_raw);
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int d = tid; d < n; d += 256) {
+        Vec4<T> v = sol[col[d]];
+        for (int k = gptr[d]; k < gptr[d + 1]; ++k) {
+            const Vec4<T> u = ldcg4(uvec + gidx[k]);
+            v.x += u.x;
+            v.y += u.y;
+            v.z += u.z;
+        }
+        f[d] = v;
+    }
+    __syncthreads();
+    const int nw = gridDim.x * 8;
+    for (int i = blockIdx.x * 8 + (tid >> 5); i < n; i += nw) {
+        const T *trow = Tt + (int64_t)i * n;
+        T ax = 0, ay = 0, az = 0;
+        for (int jj = lane; jj <= i; jj += 32) {
+            const T t = trow[jj];
+            const Vec4<T> v = f[jj];
+            ax += t * v.x;
+            ay += t * v.y;
+            az += t * v.z;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, off);
+            ay += __shfl_xor_sync(0xffffffffu, ay, off);
+            az += __shfl_xor_sync(0xffffffffu, az, off);
+        }
+        if (lane == 0) ytop[i] = {ax, ay, az, (T)0};
+    }
+}
+
+// x_j = sum_{i >= j} T(i, j) y_i for 32 columns per CTA (lanes over j, the
+// eight warps over interleaved rows, partial sums added in warp order); x is
+// stored into the solution and the positions (mode 0: pc64 = x; mode 1:
+// pc64 += x, pc32 = float(pc64)), as the backward sweep does.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_top_bwd(int n, const int32_t *__restrict__ col, const T *__restrict__ Tt, const Vec4<T> *__restrict__ ytop,
+          Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode) {
+    extern __shared__ __align__(16) unsigned char top_raw[];
+    Vec4<T> *yv = reinterpret_cast<Vec4<T> *>(top_raw);
+    __shared__ T part[3][8][33];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int j0 = blockIdx.x * 32, j = j0 + lane;
+    for (int d = j0 + tid; d < n; d += 256) yv[d] = ytop[d];
+    __syncthreads();
+    T ax = 0, ay = 0, az = 0;
+    for (int i = j0 + warp; i < n; i += 8) {
+        const T t = (j <= i) ? Tt[(int64_t)i * n + j] : (T)0;  // j <= i < n
+        const Vec4<T> v = yv[i];
+        ax += t * v.x;
+        ay += t * v.y;
+        az += t * v.z;
+    }
+    part[0][warp][lane] = ax;
+    part[1][warp][lane] = ay;
+    part[2][warp][lane] = az;
+    __syncthreads();
+    if (warp == 0 && j < n) {
+        T sx = 0, sy = 0, sz = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            sx += part[0][q][lane];
+            sy += part[1][q][lane];
+            sz += part[2][q][lane];
+        }
+        const int k = col[j];
+        sol[k] = {sx, sy, sz, (T)0};
+        if (mode == 0) {
+            pc64[k] = {(double)sx, (double)sy, (double)sz, 0.0};
+        } else {
+            Vec4<double> v = pc64[k];
+            v.x += (double)sx;
+            v.y += (double)sy;
+            v.z += (double)sz;
+            pc64[k] = v;
+            pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // ARAP energy (FP64): per vertex the rotation the local step would fit to its
 // one-ring now, then sum over its entries of w |(p'_k - p'_l) - R_k (p_k - p_l)|^2.
 // One partial sum per block (warp shuffles, then the warps in order), summed
@@ -1928,7 +2118,8 @@ size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
 
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
-                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st) {
+                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st, const T *Ttop,
+                      Vec4<T> *ytop) {
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
@@ -1943,14 +2134,22 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
             s.s_top, s.s_top + s.top_clusters, s.ltop, tlay, s.level_sn + s.s_low, s.sn, s.child, s.relind, X, L21,
             sol, uvec, ticket + 2, flags, err);
     }
+    if (s.n_top > 0) {
+        const int grid = (s.n_top + 15) / 16;  // eight warps, two rows each
+        k_top_fwd<T><<<grid, 256, (size_t)s.n_top * sizeof(Vec4<T>), st>>>(s.n_top, s.top_col, s.top_gptr, s.top_gidx,
+                                                                           Ttop, sol, uvec, ytop);
+    }
 }
 
 template <typename T>
 void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
-                      cudaStream_t st) {
+                      cudaStream_t st, const T *Ttop, const Vec4<T> *ytop) {
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
+    if (s.n_top > 0)
+        k_top_bwd<T><<<(s.n_top + 31) / 32, 256, (size_t)s.n_top * sizeof(Vec4<T>), st>>>(s.n_top, s.top_col, Ttop,
+                                                                                         ytop, sol, pc64, pc32, mode);
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
     if (s.s_top > 0) {
@@ -1963,6 +2162,28 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
     if (s.s_low > 0)
         k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(s.s_low, s.s_low + G, s.ltop, lay, s.level_sn, s.sn, s.rows, X,
                                                        L21T, sol, pc64, pc32, mode, ticket, flags, err);
+}
+
+template <typename T>
+void launch_top_inverse(const DevSym &s, const T *X, const T *L21, T *Tt, cudaStream_t st) {
+    if (s.n_top == 0) return;
+    cudaMemsetAsync(Tt, 0, (size_t)s.n_top * s.n_top * sizeof(T), st);
+    k_top_inverse<T><<<s.n_top_items, 256, dense_inverse_smem_bytes(s.dense_ldx, s.dense_ld21, sizeof(T)), st>>>(
+        s.top_items, s.sn, s.relind, s.tdpos, X, L21, s.n_top, s.dense_ldx, s.dense_ld21, Tt);
+}
+
+size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
+    return (size_t)2 * (ldx_max + ld21_max) * kTopRhs * scalar_bytes;
+}
+
+cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64) {
+    cudaError_t e = raise_smem_limit((const void *)k_top_inverse<float>, inv32);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_inverse<double>, inv64);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_fwd<float>, vec32);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_fwd<double>, vec64);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_bwd<float>, vec32);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_bwd<double>, vec64);
+    return e;
 }
 
 int energy_partials(int V) { return std::max(1, blocks_for(V, kEnergyThreads)); }
@@ -2076,14 +2297,19 @@ template void launch_rhs<float>(const DevSym &, const float *, const Vec4<float>
 template void launch_rhs<double>(const DevSym &, const double *, const Vec4<double> *, const Vec4<double> *,
                                  const Vec4<double> *, Vec4<double> *, cudaStream_t);
 template void launch_solve_fwd<float>(const DevSym &, const float *, const float *, Vec4<float> *, Vec4<float> *,
-                                      unsigned long long *, unsigned *, int *, cudaStream_t);
+                                      unsigned long long *, unsigned *, int *, cudaStream_t, const float *,
+                                      Vec4<float> *);
 template void launch_solve_fwd<double>(const DevSym &, const double *, const double *, Vec4<double> *,
-                                       Vec4<double> *, unsigned long long *, unsigned *, int *, cudaStream_t);
+                                       Vec4<double> *, unsigned long long *, unsigned *, int *, cudaStream_t,
+                                       const double *, Vec4<double> *);
 template void launch_solve_bwd<float>(const DevSym &, const float *, const float *, Vec4<float> *, Vec4<double> *,
-                                      Vec4<float> *, int, unsigned long long *, unsigned *, int *, cudaStream_t);
+                                      Vec4<float> *, int, unsigned long long *, unsigned *, int *, cudaStream_t,
+                                      const float *, const Vec4<float> *);
 template void launch_solve_bwd<double>(const DevSym &, const double *, const double *, Vec4<double> *,
                                        Vec4<double> *, Vec4<float> *, int, unsigned long long *, unsigned *, int *,
-                                       cudaStream_t);
+                                       cudaStream_t, const double *, const Vec4<double> *);
+template void launch_top_inverse<float>(const DevSym &, const float *, const float *, float *, cudaStream_t);
+template void launch_top_inverse<double>(const DevSym &, const double *, const double *, double *, cudaStream_t);
 template void launch_gather_rotations<float>(const DevSym &, const Vec4<float> *, double *, cudaStream_t);
 template void launch_gather_rotations<double>(const DevSym &, const Vec4<double> *, double *, cudaStream_t);
 

@@ -42,6 +42,14 @@ struct DevSym {
     // levels [ltop, top) by clusters (s_top tasks, top_clusters clusters)
     int ltop, s_low, s_top, top_clusters;
     int top_ldx, top_ld21;  // largest front of the cluster levels (their shared-memory layout)
+    // dense top (levels [ltop, top) when n_top > 0, instead of cluster levels):
+    // n_top columns, T = inv(L_top) formed by n_top_items CTAs
+    int n_top, n_top_items, dense_ldx, dense_ld21;
+    const int32_t *top_col;    // n_top: device column of each dense index
+    const int32_t *top_gptr;   // n_top + 1: update-vector entries added to each dense row
+    const int64_t *top_gidx;   // their offsets in the update-vector array
+    const int32_t *tdpos;      // S: dense index of a top supernode's first column (-1 elsewhere)
+    const int32_t *top_items;  // 2 per CTA: supernode, first column
     const int32_t *drow, *dcol, *dent, *oldidx;
     const int64_t *amap, *dmap;
     const SnInfo *sn;
@@ -120,11 +128,20 @@ constexpr int kTopTaskBytes = ARAP_TOP_TASK_KB * 1024;
 constexpr int kTopMaxClusters = 16;
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
-                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st);
+                      unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st, const T *Ttop,
+                      Vec4<T> *ytop);
 template <typename T>
 void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
-                      cudaStream_t st);
+                      cudaStream_t st, const T *Ttop, const Vec4<T> *ytop);
+// T = inv(L_top) of the dense top (n_top x n_top, row-major, zero above the diagonal)
+template <typename T>
+void launch_top_inverse(const DevSym &s, const T *X, const T *L21, T *Tt, cudaStream_t st);
+size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
+cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64);
+// most columns of the dense top (its T and f vectors must fit the device and shared memory)
+constexpr int kDenseTopCols = 2048;
+constexpr int kTopRhs = 16;  // columns of T one CTA of the inversion forms
 // ---- many poses of one mesh and constraint set (arap_batch.cu); arrays of
 // (vertex, pose) pairs are vertex-major, element (k, p) at k * P + p
 size_t batch_solve_smem_bytes(int max_ldx, int max_ld21, int pt);
