@@ -348,9 +348,9 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     add(ctx->L21, (size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T));
     add(ctx->L21T, (size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T));
     {
-        const size_t nt = (size_t)choose_dense_top(s, dense_cap(ctx)).ncols;
-        add(ctx->Ttop, std::max<size_t>(nt * nt, 1) * sizeof(T));
-        add(ctx->ytop, std::max<size_t>(nt, 1) * sizeof(Vec4<T>));
+        const int nt = choose_dense_top(s, dense_cap(ctx)).ncols;
+        add(ctx->Ttop, std::max<size_t>(nt > 0 ? dense_top_elems(nt) : 0, 1) * sizeof(T));
+        add(ctx->ytop, std::max<size_t>(2 * (size_t)dense_ld(nt), 1) * sizeof(Vec4<T>));  // y_top, then f_top
     }
     if (n_poses > 0) {
         const size_t P = (size_t)n_poses, VP = V * P, MP = m1 * P, nc = V - (size_t)s.m;
@@ -495,7 +495,7 @@ int prepare_symbolic(arap_ctx *ctx) {
                 ld21m = std::max(ld21m, (int)x.ld21);
             }
             const size_t i32 = dense_inverse_smem_bytes(ldxm, ld21m, 4), i64 = dense_inverse_smem_bytes(ldxm, ld21m, 8);
-            const size_t v32 = (size_t)dtop.ncols * 16, v64 = (size_t)dtop.ncols * 32;
+            const size_t v32 = (size_t)dense_ld(dtop.ncols) * 16, v64 = (size_t)dense_ld(dtop.ncols) * 32;
             if (i64 <= kSmemMax && v64 <= kSmemMax) {
                 const int rc_d = prepare_dense_top(ctx, dtop.level, dtop.ncols);
                 if (rc_d != ARAP_OK) return rc_d;

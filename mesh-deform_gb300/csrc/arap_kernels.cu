@@ -1683,8 +1683,8 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, const int32_t *__restrict__ relind,
-              const int32_t *__restrict__ tdpos, const T *__restrict__ Xall, const T *__restrict__ L21all, int n_top,
-              int ldx_max, int ld21_max, T *__restrict__ Tt) {
+              const int32_t *__restrict__ tdpos, const T *__restrict__ Xall, const T *__restrict__ L21all, int ldt,
+              int ldx_max, int ld21_max, T *__restrict__ Tt, T *__restrict__ TTt) {
     extern __shared__ __align__(16) unsigned char top_raw[];
     constexpr int RC = kTopRhs;
     T *Y = reinterpret_cast<T *>(top_raw);  // [row][RC], rows of the current supernode's columns
@@ -1703,7 +1703,10 @@ k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, 
             const int r = q / RC, c = q % RC;
             const T v = c < w ? X[(int64_t)(c0 + c) * dj.ldx + r] : (T)0;
             Y[q] = v;
-            if (c < w) Tt[((int64_t)tdpos[j] + r) * n_top + dcol0 + c] = v;
+            if (c < w) {
+                Tt[((int64_t)tdpos[j] + r) * ldt + dcol0 + c] = v;
+                TTt[(dcol0 + c) * ldt + tdpos[j] + r] = v;
+            }
         }
     }
     __syncthreads();
@@ -1751,11 +1754,14 @@ k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, 
 #pragma unroll
                 for (int c = 0; c < RC; ++c) acc[c] += x * F[k * RC + c];
             }
-            T *trow = Tt + ((int64_t)tdpos[a] + r) * n_top + dcol0;
+            T *trow = Tt + ((int64_t)tdpos[a] + r) * ldt + dcol0;
 #pragma unroll
             for (int c = 0; c < RC; ++c) {
                 Y[r * RC + c] = acc[c];
-                if (c < w) trow[c] = acc[c];
+                if (c < w) {
+                    trow[c] = acc[c];
+                    TTt[(dcol0 + c) * ldt + tdpos[a] + r] = acc[c];
+                }
             }
         }
         __syncthreads();
@@ -1764,38 +1770,55 @@ k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, 
     }
 }
 
-// f_top (right-hand side of the top columns plus their lower children's
-// update vectors, in a fixed order) into shared memory; then one warp per row:
-// y_i = sum_{j <= i} T(i, j) f_j, lanes over j, sums in a fixed order.
+// f_top: the right-hand side of the top columns plus the update vectors of
+// their children in the lower levels (in a fixed order), one thread per row.
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_top_fwd(int n, const int32_t *__restrict__ col, const int32_t *__restrict__ gptr, const int64_t *__restrict__ gidx,
-          const T *__restrict__ Tt, const Vec4<T> *__restrict__ sol, const Vec4<T> *__restrict__ uvec,
-          Vec4<T> *__restrict__ ytop) {
-    extern __shared__ __align__(16) unsigned char top_raw[];
-    Vec4<T> *f = reinterpret_cast<Vec4<T> *>(top_raw);
-    const int tid = threadIdx.x, lane = tid & 31;
-    for (int d = tid; d < n; d += 256) {
-        Vec4<T> v = sol[col[d]];
-        for (int k = gptr[d]; k < gptr[d + 1]; ++k) {
-            const Vec4<T> u = ldcg4(uvec + gidx[k]);
-            v.x += u.x;
-            v.y += u.y;
-            v.z += u.z;
-        }
-        f[d] = v;
+k_top_gather(int n, const int32_t *__restrict__ col, const int32_t *__restrict__ gptr,
+             const int64_t *__restrict__ gidx, const Vec4<T> *__restrict__ sol, const Vec4<T> *__restrict__ uvec,
+             Vec4<T> *__restrict__ ftop) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    Vec4<T> v = sol[col[d]];
+    for (int k = gptr[d]; k < gptr[d + 1]; ++k) {
+        const Vec4<T> u = ldcg4(uvec + gidx[k]);
+        v.x += u.x;
+        v.y += u.y;
+        v.z += u.z;
     }
+    ftop[d] = v;
+}
+
+// out_r = sum_c M(r, c) in_c over the nonzero part of row r of a dense
+// triangular matrix (row-major, leading dimension ldt a multiple of 4, zeros
+// outside the triangle): the lower part c <= r (UPPER false, forward: M = T)
+// or the upper part c >= r (UPPER true, backward: M = T^T). One warp per row,
+// lanes over groups of four columns, sums in a fixed order. Forward: out to
+// ytop. Backward: out is x of the top columns, stored into the solution and
+// the positions (mode 0: pc64 = x; mode 1: pc64 += x, pc32 = float(pc64)).
+template <typename T, bool UPPER>
+__global__ void __launch_bounds__(256)
+k_top_gemv(int n, int ldt, const T *__restrict__ M, const Vec4<T> *__restrict__ in, Vec4<T> *__restrict__ ytop,
+           const int32_t *__restrict__ col, Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64,
+           Vec4<float> *__restrict__ pc32, int mode) {
+    extern __shared__ __align__(16) unsigned char top_raw[];
+    Vec4<T> *v = reinterpret_cast<Vec4<T> *>(top_raw);
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int d = tid; d < n; d += 256) v[d] = in[d];
+    for (int d = n + tid; d < ldt; d += 256) v[d] = {(T)0, (T)0, (T)0, (T)0};
     __syncthreads();
     const int nw = gridDim.x * 8;
-    for (int i = blockIdx.x * 8 + (tid >> 5); i < n; i += nw) {
-        const T *trow = Tt + (int64_t)i * n;
+    for (int r = blockIdx.x * 8 + (tid >> 5); r < n; r += nw) {
+        const T *row = M + (int64_t)r * ldt;
+        const int g0 = UPPER ? (r >> 2) : 0, g1 = UPPER ? (ldt >> 2) : (r >> 2) + 1;  // column groups of four
         T ax = 0, ay = 0, az = 0;
-        for (int jj = lane; jj <= i; jj += 32) {
-            const T t = trow[jj];
-            const Vec4<T> v = f[jj];
-            ax += t * v.x;
-            ay += t * v.y;
-            az += t * v.z;
+#pragma unroll 4
+        for (int g = g0 + lane; g < g1; g += 32) {
+            const Vec4<T> m = *reinterpret_cast<const Vec4<T> *>(row + 4 * g);
+            const Vec4<T> f0 = v[4 * g], f1 = v[4 * g + 1], f2 = v[4 * g + 2], f3 = v[4 * g + 3];
+            ax += m.x * f0.x + m.y * f1.x + m.z * f2.x + m.w * f3.x;
+            ay += m.x * f0.y + m.y * f1.y + m.z * f2.y + m.w * f3.y;
+            az += m.x * f0.z + m.y * f1.z + m.z * f2.z + m.w * f3.z;
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
@@ -1803,56 +1826,22 @@ k_top_fwd(int n, const int32_t *__restrict__ col, const int32_t *__restrict__ gp
             ay += __shfl_xor_sync(0xffffffffu, ay, off);
             az += __shfl_xor_sync(0xffffffffu, az, off);
         }
-        if (lane == 0) ytop[i] = {ax, ay, az, (T)0};
-    }
-}
-
-// x_j = sum_{i >= j} T(i, j) y_i for 32 columns per CTA (lanes over j, the
-// eight warps over interleaved rows, partial sums added in warp order); x is
-// stored into the solution and the positions (mode 0: pc64 = x; mode 1:
-// pc64 += x, pc32 = float(pc64)), as the backward sweep does.
-template <typename T>
-__global__ void __launch_bounds__(256)
-k_top_bwd(int n, const int32_t *__restrict__ col, const T *__restrict__ Tt, const Vec4<T> *__restrict__ ytop,
-          Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32, int mode) {
-    extern __shared__ __align__(16) unsigned char top_raw[];
-    Vec4<T> *yv = reinterpret_cast<Vec4<T> *>(top_raw);
-    __shared__ T part[3][8][33];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int j0 = blockIdx.x * 32, j = j0 + lane;
-    for (int d = j0 + tid; d < n; d += 256) yv[d] = ytop[d];
-    __syncthreads();
-    T ax = 0, ay = 0, az = 0;
-    for (int i = j0 + warp; i < n; i += 8) {
-        const T t = (j <= i) ? Tt[(int64_t)i * n + j] : (T)0;  // j <= i < n
-        const Vec4<T> v = yv[i];
-        ax += t * v.x;
-        ay += t * v.y;
-        az += t * v.z;
-    }
-    part[0][warp][lane] = ax;
-    part[1][warp][lane] = ay;
-    part[2][warp][lane] = az;
-    __syncthreads();
-    if (warp == 0 && j < n) {
-        T sx = 0, sy = 0, sz = 0;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            sx += part[0][q][lane];
-            sy += part[1][q][lane];
-            sz += part[2][q][lane];
-        }
-        const int k = col[j];
-        sol[k] = {sx, sy, sz, (T)0};
-        if (mode == 0) {
-            pc64[k] = {(double)sx, (double)sy, (double)sz, 0.0};
+        if (lane != 0) continue;
+        if (!UPPER) {
+            ytop[r] = {ax, ay, az, (T)0};
         } else {
-            Vec4<double> v = pc64[k];
-            v.x += (double)sx;
-            v.y += (double)sy;
-            v.z += (double)sz;
-            pc64[k] = v;
-            pc32[k] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
+            const int k = col[r];
+            sol[k] = {ax, ay, az, (T)0};
+            if (mode == 0) {
+                pc64[k] = {(double)ax, (double)ay, (double)az, 0.0};
+            } else {
+                Vec4<double> p = pc64[k];
+                p.x += (double)ax;
+                p.y += (double)ay;
+                p.z += (double)az;
+                pc64[k] = p;
+                pc32[k] = {(float)p.x, (float)p.y, (float)p.z, 0.f};
+            }
         }
     }
 }
@@ -2135,9 +2124,13 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
             sol, uvec, ticket + 2, flags, err);
     }
     if (s.n_top > 0) {
-        const int grid = (s.n_top + 15) / 16;  // eight warps, two rows each
-        k_top_fwd<T><<<grid, 256, (size_t)s.n_top * sizeof(Vec4<T>), st>>>(s.n_top, s.top_col, s.top_gptr, s.top_gidx,
-                                                                           Ttop, sol, uvec, ytop);
+        // f_top into the second half of ytop, then y_top = T f_top
+        const int ldt = dense_ld(s.n_top);
+        Vec4<T> *ftop = ytop + ldt;
+        k_top_gather<T><<<(s.n_top + 255) / 256, 256, 0, st>>>(s.n_top, s.top_col, s.top_gptr, s.top_gidx, sol, uvec,
+                                                               ftop);
+        k_top_gemv<T, false><<<(s.n_top + 7) / 8, 256, (size_t)ldt * sizeof(Vec4<T>), st>>>(
+            s.n_top, ldt, Ttop, ftop, ytop, nullptr, nullptr, nullptr, nullptr, 0);
     }
 }
 
@@ -2147,9 +2140,12 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
                       cudaStream_t st, const T *Ttop, const Vec4<T> *ytop) {
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
-    if (s.n_top > 0)
-        k_top_bwd<T><<<(s.n_top + 31) / 32, 256, (size_t)s.n_top * sizeof(Vec4<T>), st>>>(s.n_top, s.top_col, Ttop,
-                                                                                         ytop, sol, pc64, pc32, mode);
+    if (s.n_top > 0) {
+        // x_top = T^T y_top (T^T stored after T)
+        const int ldt = dense_ld(s.n_top);
+        k_top_gemv<T, true><<<(s.n_top + 7) / 8, 256, (size_t)ldt * sizeof(Vec4<T>), st>>>(
+            s.n_top, ldt, Ttop + (size_t)ldt * s.n_top, ytop, nullptr, s.top_col, sol, pc64, pc32, mode);
+    }
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
     if (s.s_top > 0) {
@@ -2167,10 +2163,14 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
 template <typename T>
 void launch_top_inverse(const DevSym &s, const T *X, const T *L21, T *Tt, cudaStream_t st) {
     if (s.n_top == 0) return;
-    cudaMemsetAsync(Tt, 0, (size_t)s.n_top * s.n_top * sizeof(T), st);
+    const int ldt = dense_ld(s.n_top);
+    cudaMemsetAsync(Tt, 0, dense_top_elems(s.n_top) * sizeof(T), st);
     k_top_inverse<T><<<s.n_top_items, 256, dense_inverse_smem_bytes(s.dense_ldx, s.dense_ld21, sizeof(T)), st>>>(
-        s.top_items, s.sn, s.relind, s.tdpos, X, L21, s.n_top, s.dense_ldx, s.dense_ld21, Tt);
+        s.top_items, s.sn, s.relind, s.tdpos, X, L21, ldt, s.dense_ldx, s.dense_ld21, Tt, Tt + (size_t)ldt * s.n_top);
 }
+
+int dense_ld(int n) { return (n + 3) & ~3; }
+size_t dense_top_elems(int n) { return (size_t)2 * dense_ld(n) * n; }
 
 size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
     return (size_t)2 * (ldx_max + ld21_max) * kTopRhs * scalar_bytes;
@@ -2179,10 +2179,10 @@ size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
 cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64) {
     cudaError_t e = raise_smem_limit((const void *)k_top_inverse<float>, inv32);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_inverse<double>, inv64);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_fwd<float>, vec32);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_fwd<double>, vec64);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_bwd<float>, vec32);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_bwd<double>, vec64);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<float, false>, vec32);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<double, false>, vec64);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<float, true>, vec32);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<double, true>, vec64);
     return e;
 }
 

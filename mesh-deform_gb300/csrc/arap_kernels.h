@@ -134,10 +134,14 @@ template <typename T>
 void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, Vec4<double> *pc64,
                       Vec4<float> *pc32, int mode, unsigned long long *ticket, unsigned *flags, int *err,
                       cudaStream_t st, const T *Ttop, const Vec4<T> *ytop);
-// T = inv(L_top) of the dense top (n_top x n_top, row-major, zero above the diagonal)
+// T = inv(L_top) of the dense top (n_top rows of dense_ld(n_top), row-major, zero
+// above the diagonal), followed by T^T in the same layout
 template <typename T>
 void launch_top_inverse(const DevSym &s, const T *X, const T *L21, T *Tt, cudaStream_t st);
 size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
+// leading dimension of the dense top's T and T^T rows, and the elements of both
+int dense_ld(int n);
+size_t dense_top_elems(int n);
 cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64);
 // most columns of the dense top (its T and f vectors must fit the device and shared memory)
 constexpr int kDenseTopCols = 2048;
