@@ -298,7 +298,7 @@ DenseTopChoice choose_dense_top(const Symbolic &s, int cap) {
 }
 
 int dense_cap(const arap_ctx *ctx) {
-    return ctx->dense_cols < 0 ? 0 : (ctx->dense_cols == 0 ? kDenseTopCols : std::min(ctx->dense_cols, kDenseTopCols));
+    return ctx->dense_cols < 0 ? 0 : (ctx->dense_cols == 0 ? kDenseTopDefault : std::min(ctx->dense_cols, kDenseTopCols));
 }
 
 // Bytes of every device buffer the setup of precision T (and, for n_poses > 0,
@@ -494,9 +494,11 @@ int prepare_symbolic(arap_ctx *ctx) {
                 ldxm = std::max(ldxm, (int)x.ldx);
                 ld21m = std::max(ld21m, (int)x.ld21);
             }
-            const size_t i32 = dense_inverse_smem_bytes(ldxm, ld21m, 4), i64 = dense_inverse_smem_bytes(ldxm, ld21m, 8);
+            const int rc32 = dense_inverse_rhs(ldxm, ld21m, 4), rc64 = dense_inverse_rhs(ldxm, ld21m, 8);
+            const size_t i32 = rc32 > 0 ? dense_inverse_smem_bytes(ldxm, ld21m, 4, rc32) : 0;
+            const size_t i64 = rc64 > 0 ? dense_inverse_smem_bytes(ldxm, ld21m, 8, rc64) : 0;
             const size_t v32 = (size_t)dense_ld(dtop.ncols) * 16, v64 = (size_t)dense_ld(dtop.ncols) * 32;
-            if (i64 <= kSmemMax && v64 <= kSmemMax) {
+            if (rc32 > 0 && rc64 > 0 && v64 <= kSmemMax) {
                 const int rc_d = prepare_dense_top(ctx, dtop.level, dtop.ncols);
                 if (rc_d != ARAP_OK) return rc_d;
                 if (i32 > ctx->dense_inv_smem[0] || i64 > ctx->dense_inv_smem[1] || v32 > ctx->dense_vec_smem[0] ||

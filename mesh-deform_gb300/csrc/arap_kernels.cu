@@ -1680,20 +1680,23 @@ k_solve_bwd_top(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, 
 // of L_top Y = E (E the identity columns) restricted to j and its ancestors,
 // supernode by supernode: Y_a = X_a F_a, U_a = F_b - L21_a Y_a, with F the
 // update rows scattered into the parent's front (Y_j = X_j at the start).
-template <typename T>
+template <typename T, int RC>
 __global__ void __launch_bounds__(256)
 k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, const int32_t *__restrict__ relind,
               const int32_t *__restrict__ tdpos, const T *__restrict__ Xall, const T *__restrict__ L21all, int ldt,
               int ldx_max, int ld21_max, T *__restrict__ Tt, T *__restrict__ TTt) {
     extern __shared__ __align__(16) unsigned char top_raw[];
-    constexpr int RC = kTopRhs;
+    // the item's kTopRhs columns in passes of RC (fewer columns per pass for
+    // fronts whose buffers would not fit shared memory otherwise)
+    for (int pass = 0; pass < kTopRhs / RC; ++pass) {
     T *Y = reinterpret_cast<T *>(top_raw);  // [row][RC], rows of the current supernode's columns
     T *U = Y + (size_t)ldx_max * RC;       // [row][RC], its struct rows
     T *F = U + (size_t)ld21_max * RC;      // the parent's front: columns
     T *Fb = F + (size_t)ldx_max * RC;      // and struct rows
     const int tid = threadIdx.x;
-    const int j = items[2 * blockIdx.x], c0 = items[2 * blockIdx.x + 1];
+    const int j = items[2 * blockIdx.x], c0 = items[2 * blockIdx.x + 1] + pass * RC;
     const SnInfo dj = sn[j];
+    if (c0 >= dj.ncol) break;
     const int w = min(RC, dj.ncol - c0);
     const int64_t dcol0 = (int64_t)tdpos[j] + c0;  // dense column of the block's first column
     // supernode j: Y = X_j[:, c0 + c]
@@ -1767,6 +1770,8 @@ k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, 
         __syncthreads();
         node = a;
         dn = da;
+    }
+    __syncthreads();  // the buffers are reused by the next pass
     }
 }
 
@@ -2165,20 +2170,46 @@ void launch_top_inverse(const DevSym &s, const T *X, const T *L21, T *Tt, cudaSt
     if (s.n_top == 0) return;
     const int ldt = dense_ld(s.n_top);
     cudaMemsetAsync(Tt, 0, dense_top_elems(s.n_top) * sizeof(T), st);
-    k_top_inverse<T><<<s.n_top_items, 256, dense_inverse_smem_bytes(s.dense_ldx, s.dense_ld21, sizeof(T)), st>>>(
-        s.top_items, s.sn, s.relind, s.tdpos, X, L21, ldt, s.dense_ldx, s.dense_ld21, Tt, Tt + (size_t)ldt * s.n_top);
+    const int rc = dense_inverse_rhs(s.dense_ldx, s.dense_ld21, sizeof(T));
+    const size_t smem = dense_inverse_smem_bytes(s.dense_ldx, s.dense_ld21, sizeof(T), rc);
+    T *TT = Tt + (size_t)ldt * s.n_top;
+#define ARAP_TOPINV(R)                                                                                               \
+    k_top_inverse<T, R><<<s.n_top_items, 256, smem, st>>>(s.top_items, s.sn, s.relind, s.tdpos, X, L21, ldt,       \
+                                                          s.dense_ldx, s.dense_ld21, Tt, TT)
+    switch (rc) {
+    case 16: ARAP_TOPINV(16); break;
+    case 8: ARAP_TOPINV(8); break;
+    case 4: ARAP_TOPINV(4); break;
+    default: ARAP_TOPINV(2); break;
+    }
+#undef ARAP_TOPINV
+}
+
+int dense_inverse_rhs(int ldx_max, int ld21_max, int scalar_bytes) {
+    for (int rc = kTopRhs; rc >= 2; rc /= 2)
+        if (dense_inverse_smem_bytes(ldx_max, ld21_max, scalar_bytes, rc) <= 227 * 1024) return rc;
+    return 0;
 }
 
 int dense_ld(int n) { return (n + 3) & ~3; }
 size_t dense_top_elems(int n) { return (size_t)2 * dense_ld(n) * n; }
 
-size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
-    return (size_t)2 * (ldx_max + ld21_max) * kTopRhs * scalar_bytes;
+size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes, int rc) {
+    return (size_t)2 * (ldx_max + ld21_max) * rc * scalar_bytes;
+}
+
+template <typename T>
+static cudaError_t raise_inverse(int bytes) {
+    cudaError_t e = raise_smem_limit((const void *)k_top_inverse<T, 16>, bytes);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_inverse<T, 8>, bytes);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_inverse<T, 4>, bytes);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_inverse<T, 2>, bytes);
+    return e;
 }
 
 cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64) {
-    cudaError_t e = raise_smem_limit((const void *)k_top_inverse<float>, inv32);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_inverse<double>, inv64);
+    cudaError_t e = raise_inverse<float>(inv32);
+    if (e == cudaSuccess) e = raise_inverse<double>(inv64);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<float, false>, vec32);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<double, false>, vec64);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<float, true>, vec32);

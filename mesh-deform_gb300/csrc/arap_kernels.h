@@ -138,13 +138,16 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
 // above the diagonal), followed by T^T in the same layout
 template <typename T>
 void launch_top_inverse(const DevSym &s, const T *X, const T *L21, T *Tt, cudaStream_t st);
-size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
+size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes, int rc);
+// columns per pass of the inversion whose buffers fit shared memory (0: none)
+int dense_inverse_rhs(int ldx_max, int ld21_max, int scalar_bytes);
 // leading dimension of the dense top's T and T^T rows, and the elements of both
 int dense_ld(int n);
 size_t dense_top_elems(int n);
 cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64);
 // most columns of the dense top (its T and f vectors must fit the device and shared memory)
-constexpr int kDenseTopCols = 2048;
+constexpr int kDenseTopCols = 4096;
+constexpr int kDenseTopDefault = 2048;  // the default column cap
 constexpr int kTopRhs = 16;  // columns of T one CTA of the inversion forms
 // ---- many poses of one mesh and constraint set (arap_batch.cu); arrays of
 // (vertex, pose) pairs are vertex-major, element (k, p) at k * P + p
