@@ -143,6 +143,7 @@ struct arap_ctx {
     int pose_tile = 0;  // poses per batched-solve task (0: the largest that fits)
     int tP = -1;  // poses whose targets btargets holds (-1: none)
     int model_P = 1, model_T = 1;  // poses / pose tiles of the last deform (cost model)
+    bool model_batched = false;    // the last deform was arap_deform_poses (its solves cover the whole tree)
     // CUDA graphs of the setup and of 2^k iterations (k < kIterGraphs); a deform
     // of n iterations replays the graphs of n's binary digits, so any count
     // reuses them. Replayed while nothing they reference changes (direct
@@ -1195,6 +1196,7 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
     CK(cudaEventRecord(ctx->ev1, st));
     ctx->model_P = P;
     ctx->model_T = ctx->bT;
+    ctx->model_batched = true;
     for (int left = iterations; left > 0;) {
         int k = 0;
         while (k + 1 < arap_ctx::kIterGraphs && (2 << k) <= left) ++k;
@@ -1337,6 +1339,7 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
     ctx->launches = 0;
     ctx->setup_ms = ctx->iter_ms = 0.0;
     ctx->model_P = ctx->model_T = 1;
+    ctx->model_batched = false;
     const bool fp64 = ctx->precision == ARAP_PRECISION_FP64;
     using HClock = std::chrono::steady_clock;
     auto hms = [](HClock::time_point a, HClock::time_point b) {
@@ -1840,12 +1843,20 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
     // panel entries below the diagonal blocks and lower-triangular entries of the
     // inverted diagonal blocks, read once per solve sweep
     // per solve sweep: the lower triangle of X = inv(L11) and L21, once each
-    double xlow = 0.0, l21 = 0.0, nbsum = 0.0;
+    double xlow = 0.0, l21 = 0.0, nbsum = 0.0, xlow_lo = 0.0, l21_lo = 0.0;
     for (const SnInfo &d : s.sn) {
         xlow += (double)d.ncol * (d.ncol + 1) / 2;
         l21 += (double)(d.nrow - d.ncol) * d.ncol;
         nbsum += d.nrow - d.ncol;
+        if (ctx->ds.n_top == 0 || d.level < ctx->ds.ltop) {
+            xlow_lo += (double)d.ncol * (d.ncol + 1) / 2;
+            l21_lo += (double)(d.nrow - d.ncol) * d.ncol;
+        }
     }
+    // one request's sweeps: the lower levels' matrices, then the dense top's
+    // triangle of T (or T^T) and its vectors
+    const double nt = ctx->ds.n_top;
+    const double dense_mat = xlow_lo + l21_lo + nt * (nt + 1) / 2;
     double B = 0.0, FL = 0.0;
     const double P = ctx->model_P, T = ctx->model_T;  // poses, pose tiles of the last deform
     switch (kernel_class) {
@@ -1881,10 +1892,15 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
         FL = P * nnz * 6;
         break;
     case ARAP_K_SOLVE_FWD:
-    case ARAP_K_SOLVE_BWD:  // matrices once per pose tile, vectors once per pose
-        B = T * (xlow + l21) * sz + P * (m * 3 * sz * 2 + nbsum * 3 * sz * 2);
+    case ARAP_K_SOLVE_BWD:
+        if (ctx->model_batched) {  // matrices once per pose tile, vectors once per pose
+            B = T * (xlow + l21) * sz + P * (m * 3 * sz * 2 + nbsum * 3 * sz * 2);
+            FL = P * (xlow + l21) * 6;
+        } else {
+            B = dense_mat * sz + m * 3 * sz * 2 + nbsum * 3 * sz * 2 + nt * 3 * sz * 2;
+            FL = dense_mat * 6;
+        }
         if (kernel_class == ARAP_K_SOLVE_BWD && ctx->state_prec != ARAP_PRECISION_FP64) B += P * m * (24 * 2 + 12);
-        FL = P * (xlow + l21) * 6;
         break;
     case ARAP_K_GATHER:
         B = P * V * (24 + 24) + V * 4;
