@@ -92,3 +92,30 @@ def test_cluster_levels_match_single_cta_levels(gpu, precision, tol, threshold):
     assert W.bbox_rel_error(got2, ref2, w.positions) <= tol
     ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, 6)
     assert ok and W.bbox_rel_error(got, o, w.positions) <= (1e-10 if precision == "fp64" else 1e-6)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-6)])
+@pytest.mark.parametrize("cols", [-1, 256, 0, 4096])
+def test_dense_top_matches_supernodal_top(gpu, precision, tol, cols):
+    """The top levels solved through T = inv(L_top) (any column cap, none with
+    -1) give the positions of the supernodal sweeps up to the order of sums,
+    and stay within the oracle tolerance; repeated deforms (graph replay) are
+    bit-identical."""
+    from oracle import oracle as O
+
+    w = W.cfg_twisted_bar(h=0.1, iterations=6)
+    with make(gpu, w, precision) as ctx:
+        ctx.set_dense_top(-1)
+        ref = ctx.deform(6)
+    with make(gpu, w, precision) as ctx:
+        ctx.set_dense_top(cols)
+        got = ctx.deform(6)
+        ctx.invalidate()
+        again = ctx.deform(6)
+        ctx.invalidate()
+        third = ctx.deform(6)
+    np.testing.assert_array_equal(got, again)
+    np.testing.assert_array_equal(got, third)
+    assert W.bbox_rel_error(got, ref, w.positions) <= tol
+    ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, 6)
+    assert ok and W.bbox_rel_error(got, o, w.positions) <= (1e-10 if precision == "fp64" else 1e-6)
