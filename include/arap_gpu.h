@@ -188,9 +188,10 @@ int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes);
    (0, the default: 2,048; negative: none), are solved through the explicit
    inverse of the factor restricted to them: formed once per factorisation
    (n x n dense), it turns the top of each triangular sweep, a chain of
-   single-supernode steps, into one wide matrix-vector product. Takes effect
-   at the next deform (which sets the problem up again); it changes the order
-   of sums. */
+   single-supernode steps, into one wide matrix-vector product (in
+   arap_deform_poses: one matrix product over all poses). Takes effect at the
+   next deform (which sets the problem up again); it changes the order of
+   sums. */
 int arap_set_dense_top(arap_ctx *ctx, int32_t max_columns);
 
 /* arap_ordering of the next symbolic analysis (marks the context dirty). */

@@ -137,8 +137,8 @@ struct arap_ctx {
     DevBuf cidx_dev, handle_dev, tabs_dev;  // arap_pose_targets inputs
     DevBuf vf_ptr, vf_face, fnorm, vnorm;    // vertex normals
     // many-pose state (arap_deform_poses)
-    DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags;
-    int bP = 0, bT = 0, bpt = 0, bgrid = 0;
+    DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags, bftop, bytop, bws;
+    int bP = 0, bT = 0, bpt = 0, bgrid = 0, bntop = -1;
     int64_t bgen = -1;  // gen the many-pose buffers and counters were set up for (-1: redo)
     int pose_tile = 0;  // poses per batched-solve task (0: the largest that fits)
     int tP = -1;  // poses whose targets btargets holds (-1: none)
@@ -189,7 +189,7 @@ struct arap_ctx {
                 &amap, &dmap, &sn, &rows, &relind, &child, &level_sn, &fitems, &w64, &w32, &p64, &pc64, &p32,
                 &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
                 &errw, &ticket, &flags, &energy, &cidx_dev, &handle_dev, &tabs_dev, &vf_ptr, &vf_face, &fnorm,
-                &vnorm, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout,
+                &vnorm, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout, &bftop, &bytop, &bws,
                 &bticket, &bflags, &top_col, &top_gptr, &top_gidx, &tdpos, &top_items, &Ttop, &ytop};
     }
 };
@@ -348,11 +348,9 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     add(ctx->Xinv, (size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T));
     add(ctx->L21, (size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T));
     add(ctx->L21T, (size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T));
-    {
-        const int nt = choose_dense_top(s, dense_cap(ctx)).ncols;
-        add(ctx->Ttop, std::max<size_t>(nt > 0 ? dense_top_elems(nt) : 0, 1) * sizeof(T));
-        add(ctx->ytop, std::max<size_t>(2 * (size_t)dense_ld(nt), 1) * sizeof(Vec4<T>));  // y_top, then f_top
-    }
+    const int nt = choose_dense_top(s, dense_cap(ctx)).ncols;
+    add(ctx->Ttop, std::max<size_t>(nt > 0 ? dense_top_elems(nt) : 0, 1) * sizeof(T));
+    add(ctx->ytop, std::max<size_t>(2 * (size_t)dense_ld(nt), 1) * sizeof(Vec4<T>));  // y_top, then f_top
     if (n_poses > 0) {
         const size_t P = (size_t)n_poses, VP = V * P, MP = m1 * P, nc = V - (size_t)s.m;
         const int pt = std::max(batch_pose_tile(s.max_ldx, s.max_ld21), 1);
@@ -368,6 +366,9 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
         add(ctx->btargets, P * nc * 3 * sizeof(double));
         add(ctx->bticket, 2 * sizeof(unsigned long long));
         add(ctx->bflags, 2 * S1 * T_ * sizeof(unsigned));
+        add(ctx->bftop, std::max<size_t>(btop_matrix_floats(nt, (int)P), 1) * sizeof(float));
+        add(ctx->bytop, std::max<size_t>(btop_matrix_floats(nt, (int)P), 1) * sizeof(float));
+        add(ctx->bws, std::max<size_t>(btop_workspace_floats(nt, (int)P), 1) * sizeof(float));
     }
 }
 
@@ -839,15 +840,18 @@ int run_batch_iterations(arap_ctx *ctx, int P, int iterations) {
                 Prof pr(ctx, ARAP_K_SOLVE_FWD);
                 launch_bsolve(d, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
                               ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), nullptr, nullptr, tk, fl,
-                              ctx->errw.as<int>(), true, st);
+                              ctx->errw.as<int>(), true, st, ctx->Ttop.as<float>(), ctx->bftop.as<float>(),
+                              ctx->bytop.as<float>(), ctx->bws.as<float>());
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_BWD);
                 launch_bsolve(d, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
                               ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
-                              ctx->bpc32.as<Vec4<float>>(), tk + 1, fl + fhalf, ctx->errw.as<int>(), false, st);
+                              ctx->bpc32.as<Vec4<float>>(), tk + 1, fl + fhalf, ctx->errw.as<int>(), false, st,
+                              ctx->Ttop.as<float>(), ctx->bftop.as<float>(), ctx->bytop.as<float>(),
+                              ctx->bws.as<float>());
             }
-            ctx->launches += 3;
+            ctx->launches += 1 + (batch_tasks(d) > 0 ? 2 : 0) + batch_top_launches(d);
         }
     }
     CK(cudaGetLastError());
@@ -1135,7 +1139,7 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
         return fail(ctx, ARAP_ERR_UNSUPPORTED,
                     "pose tile " + std::to_string(pt) + " does not fit this mesh's largest supernode");
     if (pt == 0) return fail(ctx, ARAP_ERR_UNSUPPORTED, "supernode fronts too large for the batched solves");
-    if (ctx->bgen != ctx->gen || ctx->bP != P || ctx->bpt != pt) {
+    if (ctx->bgen != ctx->gen || ctx->bP != P || ctx->bpt != pt || ctx->bntop != d.n_top) {
         const size_t smem = batch_solve_smem_bytes(s.max_ldx, s.max_ld21, pt);
         if (pt != ctx->bpt || smem > ctx->bsmem) {
             CK(configure_batch_smem(s.max_ldx, s.max_ld21, pt));
@@ -1155,7 +1159,10 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
             {&ctx->bout, VP * 3 * sizeof(double)},
             {&ctx->btargets, (size_t)P * nc * 3 * sizeof(double)},
             {&ctx->bticket, 2 * sizeof(unsigned long long)},
-            {&ctx->bflags, nflags * sizeof(unsigned)}};
+            {&ctx->bflags, nflags * sizeof(unsigned)},
+            {&ctx->bftop, std::max<size_t>(btop_matrix_floats(d.n_top, P), 1) * sizeof(float)},
+            {&ctx->bytop, std::max<size_t>(btop_matrix_floats(d.n_top, P), 1) * sizeof(float)},
+            {&ctx->bws, std::max<size_t>(btop_workspace_floats(d.n_top, P), 1) * sizeof(float)}};
         bool moved = false;
         void *const old_targets = ctx->btargets.p;
         for (const auto &pb : plan) {
@@ -1175,6 +1182,7 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
         ctx->bT = T;
         ctx->bgrid = grid;
         ctx->bP = P;
+        ctx->bntop = d.n_top;
         ctx->bgen = ctx->gen;
     }
     if (!targets && ctx->tP < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no targets on the device yet");
@@ -1843,20 +1851,23 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
     // panel entries below the diagonal blocks and lower-triangular entries of the
     // inverted diagonal blocks, read once per solve sweep
     // per solve sweep: the lower triangle of X = inv(L11) and L21, once each
-    double xlow = 0.0, l21 = 0.0, nbsum = 0.0, xlow_lo = 0.0, l21_lo = 0.0;
+    // (the levels below the dense top, where there is one: the _lo sums)
+    double xlow = 0.0, l21 = 0.0, xlow_lo = 0.0, l21_lo = 0.0, nbsum_lo = 0.0;
     for (const SnInfo &d : s.sn) {
         xlow += (double)d.ncol * (d.ncol + 1) / 2;
         l21 += (double)(d.nrow - d.ncol) * d.ncol;
-        nbsum += d.nrow - d.ncol;
         if (ctx->ds.n_top == 0 || d.level < ctx->ds.ltop) {
             xlow_lo += (double)d.ncol * (d.ncol + 1) / 2;
             l21_lo += (double)(d.nrow - d.ncol) * d.ncol;
+            nbsum_lo += d.nrow - d.ncol;
         }
     }
-    // one request's sweeps: the lower levels' matrices, then the dense top's
-    // triangle of T (or T^T) and its vectors
+    // one sweep: the lower levels' matrices, then the dense top's triangle of
+    // T (or T^T); per pose the solution, the update vectors and the top's
+    // vector, each written and read once
     const double nt = ctx->ds.n_top;
-    const double dense_mat = xlow_lo + l21_lo + nt * (nt + 1) / 2;
+    const double tri = nt * (nt + 1) / 2;
+    const double vec = m * 3 * sz * 2 + nbsum_lo * 3 * sz * 2 + nt * 3 * sz * 2;
     double B = 0.0, FL = 0.0;
     const double P = ctx->model_P, T = ctx->model_T;  // poses, pose tiles of the last deform
     switch (kernel_class) {
@@ -1893,12 +1904,12 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
         break;
     case ARAP_K_SOLVE_FWD:
     case ARAP_K_SOLVE_BWD:
-        if (ctx->model_batched) {  // matrices once per pose tile, vectors once per pose
-            B = T * (xlow + l21) * sz + P * (m * 3 * sz * 2 + nbsum * 3 * sz * 2);
-            FL = P * (xlow + l21) * 6;
+        if (ctx->model_batched) {  // lower matrices once per pose tile, T once, vectors once per pose
+            B = (T * (xlow_lo + l21_lo) + tri) * sz + P * vec;
+            FL = P * (xlow_lo + l21_lo + tri) * 6;
         } else {
-            B = dense_mat * sz + m * 3 * sz * 2 + nbsum * 3 * sz * 2 + nt * 3 * sz * 2;
-            FL = dense_mat * 6;
+            B = (xlow_lo + l21_lo + tri) * sz + vec;
+            FL = (xlow_lo + l21_lo + tri) * 6;
         }
         if (kernel_class == ARAP_K_SOLVE_BWD && ctx->state_prec != ARAP_PRECISION_FP64) B += P * m * (24 * 2 + 12);
         break;

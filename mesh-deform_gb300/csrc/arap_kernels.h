@@ -174,7 +174,16 @@ void launch_bresidual(const DevSym &s, int P, const double *w64, const double *d
 // tile) tasks; the grid must stay fixed while the ticket counter is not reset
 void launch_bsolve(const DevSym &s, int P, int pt, int grid, const float *X, const float *L21, const float *L21T,
                    Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
-                   unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st);
+                   unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st,
+                   const float *Ttop, float *bftop, float *bytop, float *bws);
+// supernode tasks of the batched sweeps (the dense top's levels excluded)
+int batch_tasks(const DevSym &s);
+// launches of the dense top in one forward + backward pair of batched sweeps
+int batch_top_launches(const DevSym &s);
+// the dense top's n x 3P right-hand sides (rows padded to a multiple of 4
+// floats) and the partial products of one sweep, in floats
+size_t btop_matrix_floats(int n, int P);
+size_t btop_workspace_floats(int n, int P);
 void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *out, cudaStream_t st);
 // handle targets of P rigid poses (P x nc x 3, ascending constrained order)
 void launch_pose_targets(int P, int nc, const int32_t *cidx, const uint8_t *handle, const double *rest,

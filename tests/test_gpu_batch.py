@@ -151,3 +151,30 @@ def test_pose_tile_that_does_not_fit_is_refused(gpu):
         ctx.set_pose_tile(0)
         out = ctx.deform_poses(poses, 2)
         assert np.isfinite(out).all()
+
+
+@pytest.mark.parametrize("cols", [256, 0, 4096])
+def test_pose_batch_dense_top_matches_supernodal_top(gpu, cols):
+    """The batched sweeps with the tree's top levels through T = inv(L_top)
+    (a matrix product over all poses) agree with the sweeps over the whole
+    tree to the mixed tolerance and with the oracle pose by pose, for caps
+    from a few levels up to most of this mesh's tree."""
+    w = W.cfg_pose_batch(level=4, n_poses=7, iterations=6)
+
+    def run(c):
+        with gpu.ArapContext(w.V, w.faces) as ctx:
+            ctx.set_precision("mixed", 1)
+            ctx.set_dense_top(c)
+            ctx.set_rest_positions(w.positions)
+            ctx.set_constraints(w.cidx, w.poses[0])
+            out = ctx.deform_poses(w.poses, 6)
+            again = ctx.deform_poses(None, 6)
+            np.testing.assert_array_equal(out, again)
+            return out
+
+    ref, got = run(-1), run(cols)
+    for p in range(len(w.poses)):
+        assert W.bbox_rel_error(got[p], ref[p], w.positions) <= 1e-6, p
+        ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.poses[p], 6)
+        assert ok and W.bbox_rel_error(got[p], o, w.positions) <= 1e-6, p
+        np.testing.assert_array_equal(got[p][w.cidx], w.poses[p])
