@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <climits>
+#include "arap_btop.cuh"
 #include "arap_device.cuh"
 
 namespace arapgpu {
@@ -544,7 +545,21 @@ static cudaError_t configure_pt(size_t bytes) {
     return raise_smem_limit((const void *)k_bsolve_bwd<PT>, (int)bytes);
 }
 
+// the tensor-core products of the dense top: shared memory above the default
+static cudaError_t configure_btop() {
+    static const cudaError_t e = [] {
+        const cudaError_t a = cudaFuncSetAttribute((const void *)btop::k_btop_mma<false>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, btop::kSmemBytes);
+        if (a != cudaSuccess) return a;
+        return cudaFuncSetAttribute((const void *)btop::k_btop_mma<true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, btop::kSmemBytes);
+    }();
+    return e;
+}
+
 cudaError_t configure_batch_smem(int max_ldx, int max_ld21, int pt) {
+    const cudaError_t eb = configure_btop();
+    if (eb != cudaSuccess) return eb;
     const size_t bytes = batch_solve_smem_bytes(max_ldx, max_ld21, pt);
     switch (pt) {
     case 16: return configure_pt<16>(bytes);
@@ -669,210 +684,15 @@ static void bsolve(const DevSym &s, int P, int grid, const float *X, const float
 }
 
 // ---------------------------------------------------------------------------
-// dense top for many poses. The top's right-hand sides form an n x 3P matrix
-// (row d: the xyz of every pose, packed; rows padded to ldb floats). The
-// forward sweep's Y = T F and the backward's X = T^T Y are products with the
-// triangular T = inv(L_top). Each row tile of 64 rows reads only the columns
-// of T inside the triangle, cut into splits of at most kTSplit columns; one
-// CTA computes one (row tile, split, 128 columns) partial product, and a
-// second kernel sums a row's partials in split order (the same order for
-// every run, pose tile and pose count) and applies the sweep's epilogue.
-
-#ifndef ARAP_BTOP_SPLIT
-#define ARAP_BTOP_SPLIT 128
-#endif
-constexpr int kTM = 64, kTN = 128, kTK = 16, kTSplit = ARAP_BTOP_SPLIT;
-
-__host__ __device__ inline int btop_ldb(int P) { return (3 * P + 3) & ~3; }
-
-// columns [kb, ke) of T's rows in row tile rt that the product reads
-__host__ __device__ inline void btop_krange(bool upper, int n, int rt, int &kb, int &ke) {
-    kb = upper ? rt * kTM : 0;
-    ke = upper ? n : ((rt + 1) * kTM < n ? (rt + 1) * kTM : n);
-}
-
-__host__ __device__ inline int btop_splits(bool upper, int n, int rt) {
-    int kb, ke;
-    btop_krange(upper, n, rt, kb, ke);
-    return (ke - kb + kTSplit - 1) / kTSplit;
-}
-
-// partial products of one sweep, and the first one of row tile rt
-__host__ __device__ inline int btop_tasks(bool upper, int n, int rt_end) {
-    int t = 0;
-    for (int rt = 0; rt < rt_end && rt * kTM < n; ++rt) t += btop_splits(upper, n, rt);
-    return t;
-}
+// dense top for many poses (arap_btop.cuh)
 
 size_t btop_workspace_floats(int n, int P) {
     if (n <= 0) return 0;
-    const int nrt = (n + kTM - 1) / kTM;
-    return (size_t)std::max(btop_tasks(false, n, nrt), btop_tasks(true, n, nrt)) * kTM * btop_ldb(P);
+    const int nrt = btop::row_tiles(n);
+    return (size_t)std::max(btop::tasks(false, n, nrt), btop::tasks(true, n, nrt)) * btop::kRows * btop::ldb_of(P);
 }
 
-size_t btop_matrix_floats(int n, int P) { return (size_t)std::max(n, 0) * btop_ldb(P); }
-
-// F[d][3p + c] = the top's right-hand side of pose p: its solution entry plus
-// the update vectors of the lower children (gptr/gidx, a CSR per top row)
-__global__ void __launch_bounds__(256)
-k_btop_gather(int n, int P, int ldb, const int32_t *__restrict__ col, const int32_t *__restrict__ gptr,
-              const int64_t *__restrict__ gidx, const Vec4<float> *__restrict__ sol,
-              const Vec4<float> *__restrict__ uvec, float *__restrict__ F) {
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= (int64_t)n * P) return;
-    const int d = (int)(q / P), p = (int)(q % P);
-    Vec4<float> v = sol[(int64_t)col[d] * P + p];
-    for (int k = gptr[d]; k < gptr[d + 1]; ++k) {
-        const Vec4<float> u = uvec[gidx[k] * P + p];
-        v.x += u.x;
-        v.y += u.y;
-        v.z += u.z;
-    }
-    float *row = F + (int64_t)d * ldb;
-    row[3 * p] = v.x;
-    row[3 * p + 1] = v.y;
-    row[3 * p + 2] = v.z;
-    if (p == P - 1)
-        for (int c = 3 * P; c < ldb; ++c) row[c] = 0.f;
-}
-
-// One partial product: rows [i0, i0+64) of M (n x n, row-major, leading
-// dimension ldt, a multiple of 4, zero past column n) times rows [k_lo, k_hi)
-// of B (n x ldb), columns [c0, c0+128). 256 threads, 4 rows x 8 columns each;
-// the next 16-deep slice goes from registers to the other shared buffer while
-// the current one is multiplied (one barrier per slice). Every entry sums its
-// k in increasing order.
-template <bool UPPER>
-__global__ void __launch_bounds__(256)
-k_btop_gemm(int n, int ldt, int ldb, const float *__restrict__ M, const float *__restrict__ B,
-            float *__restrict__ ws) {
-    __shared__ __align__(16) float As[2][kTK][kTM + 4];  // As[k][i] = M(i0 + i, k0 + k)
-    __shared__ __align__(16) float Bs[2][kTK][kTN];      // Bs[k][c] = B(k0 + k, c0 + c)
-    const int task = blockIdx.y;
-    int rt = 0, t = task;
-    for (int c = btop_splits(UPPER, n, 0); t >= c; c = btop_splits(UPPER, n, rt)) {
-        t -= c;
-        ++rt;
-    }
-    int kb, ke;
-    btop_krange(UPPER, n, rt, kb, ke);
-    const int k_lo = kb + t * kTSplit, k_hi = min(ke, k_lo + kTSplit);
-    const int i0 = rt * kTM, c0 = blockIdx.x * kTN;
-    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-    const int ar = tid / 4, ak = (tid % 4) * 4;    // A: row ar, columns ak..ak+3 of the slice
-    const int br = tid / 32, bc = (tid % 32) * 4;  // B: rows br and br+8, columns bc..bc+3
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 pa, pb0, pb1;
-    auto load = [&](int k0) {
-        const int ka = k0 + ak, i = i0 + ar;
-        pa = zero;
-        if (i < n && ka < k_hi) {  // ka + 3 < ldt: ka and ldt are multiples of 4
-            const float4 v = *reinterpret_cast<const float4 *>(M + (int64_t)i * ldt + ka);
-            pa.x = v.x;
-            if (ka + 1 < k_hi) pa.y = v.y;
-            if (ka + 2 < k_hi) pa.z = v.z;
-            if (ka + 3 < k_hi) pa.w = v.w;
-        }
-        const int kb0 = k0 + br, kb1 = kb0 + 8;
-        const bool cin = c0 + bc < ldb;  // a whole float4: ldb is a multiple of 4
-        pb0 = (cin && kb0 < k_hi) ? *reinterpret_cast<const float4 *>(B + (int64_t)kb0 * ldb + c0 + bc) : zero;
-        pb1 = (cin && kb1 < k_hi) ? *reinterpret_cast<const float4 *>(B + (int64_t)kb1 * ldb + c0 + bc) : zero;
-    };
-    auto store = [&](int buf) {
-        As[buf][ak][ar] = pa.x;
-        As[buf][ak + 1][ar] = pa.y;
-        As[buf][ak + 2][ar] = pa.z;
-        As[buf][ak + 3][ar] = pa.w;
-        *reinterpret_cast<float4 *>(&Bs[buf][br][bc]) = pb0;
-        *reinterpret_cast<float4 *>(&Bs[buf][br + 8][bc]) = pb1;
-    };
-    float acc[4][8];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int c = 0; c < 8; ++c) acc[a][c] = 0.f;
-    int buf = 0;
-    load(k_lo);
-    store(0);
-    __syncthreads();
-    for (int k0 = k_lo; k0 < k_hi; k0 += kTK) {
-        const bool more = k0 + kTK < k_hi;
-        if (more) load(k0 + kTK);
-#pragma unroll
-        for (int k = 0; k < kTK; ++k) {
-            const float4 av = *reinterpret_cast<const float4 *>(&As[buf][k][ty * 4]);
-            const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][k][tx * 4]);
-            const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][k][64 + tx * 4]);
-            const float a4[4] = {av.x, av.y, av.z, av.w};
-            const float b8[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int c = 0; c < 8; ++c) acc[a][c] = fmaf(a4[a], b8[c], acc[a][c]);
-        }
-        // the other buffer was last read before the previous barrier
-        if (more) store(buf ^ 1);
-        __syncthreads();
-        buf ^= 1;
-    }
-    float *w = ws + (int64_t)task * kTM * ldb;
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        float *row = w + (int64_t)(ty * 4 + a) * ldb + c0;
-        if (c0 + tx * 4 < ldb)
-            *reinterpret_cast<float4 *>(row + tx * 4) = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
-        if (c0 + 64 + tx * 4 < ldb)
-            *reinterpret_cast<float4 *>(row + 64 + tx * 4) = make_float4(acc[a][4], acc[a][5], acc[a][6], acc[a][7]);
-    }
-}
-
-// Sums a row's partial products in split order. Forward: Y (n x ldb), one
-// float4 per thread.
-__global__ void __launch_bounds__(256)
-k_btop_reduce_fwd(int n, int ldb, const float *__restrict__ ws, float *__restrict__ Y) {
-    const int g4 = ldb / 4;
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= (int64_t)n * g4) return;
-    const int i = (int)(q / g4), c = (int)(q % g4) * 4, rt = i / kTM;
-    const int t0 = btop_tasks(false, n, rt), ns = btop_splits(false, n, rt);
-    const float *w = ws + ((int64_t)t0 * kTM + (i - rt * kTM)) * ldb + c;
-    float4 acc = *reinterpret_cast<const float4 *>(w);
-    for (int k = 1; k < ns; ++k) {
-        const float4 v = *reinterpret_cast<const float4 *>(w + (int64_t)k * kTM * ldb);
-        acc.x += v.x;
-        acc.y += v.y;
-        acc.z += v.z;
-        acc.w += v.w;
-    }
-    *reinterpret_cast<float4 *>(Y + (int64_t)i * ldb + c) = acc;
-}
-
-// Backward, one (top row, pose) per thread: x of that top column stored
-// into the solution and added to the positions (pc32 = float(pc64)).
-__global__ void __launch_bounds__(256)
-k_btop_reduce_bwd(int n, int P, int ldb, const float *__restrict__ ws, const int32_t *__restrict__ col,
-                  Vec4<float> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32) {
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= (int64_t)n * P) return;
-    const int i = (int)(q / P), p = (int)(q % P), rt = i / kTM;
-    const int t0 = btop_tasks(true, n, rt), ns = btop_splits(true, n, rt);
-    const float *w = ws + ((int64_t)t0 * kTM + (i - rt * kTM)) * ldb + 3 * p;
-    float x = w[0], y = w[1], z = w[2];
-    for (int k = 1; k < ns; ++k) {
-        const float *v = w + (int64_t)k * kTM * ldb;
-        x += v[0];
-        y += v[1];
-        z += v[2];
-    }
-    const int64_t e = (int64_t)col[i] * P + p;
-    sol[e] = {x, y, z, 0.f};
-    Vec4<double> v = pc64[e];
-    v.x += (double)x;
-    v.y += (double)y;
-    v.z += (double)z;
-    pc64[e] = v;
-    pc32[e] = {(float)v.x, (float)v.y, (float)v.z, 0.f};
-}
+size_t btop_matrix_floats(int n, int P) { return (size_t)std::max(n, 0) * btop::ldb_of(P); }
 
 int batch_tasks(const DevSym &s) { return s.n_top > 0 ? s.s_low : s.S; }
 
@@ -883,14 +703,14 @@ void launch_bsolve(const DevSym &s, int P, int pt, int grid, const float *X, con
                    unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st,
                    const float *Ttop, float *bftop, float *bytop, float *bws) {
     if (s.S == 0) return;
-    const int n = s.n_top, ldt = n > 0 ? dense_ld(n) : 0, ldb = btop_ldb(P);
-    const int nrt = (n + kTM - 1) / kTM, nct = (ldb + kTN - 1) / kTN;
+    const int n = s.n_top, ldt = n > 0 ? dense_ld(n) : 0, ldb = btop::ldb_of(P);
+    const int nrt = btop::row_tiles(n), nct = (ldb + btop::kCols - 1) / btop::kCols;
     const unsigned rblocks = (unsigned)(((int64_t)n * (ldb / 4) + 255) / 256);
     const unsigned pblocks = (unsigned)(((int64_t)n * P + 255) / 256);
     if (!forward && n > 0) {
-        k_btop_gemm<true><<<dim3(nct, btop_tasks(true, n, nrt)), 256, 0, st>>>(n, ldt, ldb, Ttop + (size_t)ldt * n,
-                                                                                bytop, bws);
-        k_btop_reduce_bwd<<<pblocks, 256, 0, st>>>(n, P, ldb, bws, s.top_col, sol, pc64, pc32);
+        btop::k_btop_mma<true><<<dim3(nct, btop::tasks(true, n, nrt)), btop::kThreads, btop::kSmemBytes, st>>>(
+            n, ldt, ldb, Ttop + (size_t)ldt * n, bytop, bws, btop::kCoreK, btop::kCoreMN, err);
+        btop::k_btop_reduce_bwd<<<pblocks, 256, 0, st>>>(n, P, ldb, bws, s.top_col, sol, pc64, pc32);
     }
     switch (pt) {
     case 16: bsolve<16>(s, P, grid, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
@@ -900,10 +720,10 @@ void launch_bsolve(const DevSym &s, int P, int pt, int grid, const float *X, con
     default: bsolve<1>(s, P, grid, X, L21, L21T, sol, uvec, pc64, pc32, ticket, flags, err, forward, st); break;
     }
     if (forward && n > 0) {
-        k_btop_gather<<<pblocks, 256, 0, st>>>(n, P, ldb, s.top_col, s.top_gptr, s.top_gidx, sol,
-                                                                     uvec, bftop);
-        k_btop_gemm<false><<<dim3(nct, btop_tasks(false, n, nrt)), 256, 0, st>>>(n, ldt, ldb, Ttop, bftop, bws);
-        k_btop_reduce_fwd<<<rblocks, 256, 0, st>>>(n, ldb, bws, bytop);
+        btop::k_btop_gather<<<pblocks, 256, 0, st>>>(n, P, ldb, s.top_col, s.top_gptr, s.top_gidx, sol, uvec, bftop);
+        btop::k_btop_mma<false><<<dim3(nct, btop::tasks(false, n, nrt)), btop::kThreads, btop::kSmemBytes, st>>>(
+            n, ldt, ldb, Ttop, bftop, bws, btop::kCoreK, btop::kCoreMN, err);
+        btop::k_btop_reduce_fwd<<<rblocks, 256, 0, st>>>(n, ldb, bws, bytop);
     }
 }
 
