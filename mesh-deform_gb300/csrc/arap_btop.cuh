@@ -66,6 +66,13 @@ __host__ __device__ inline int tasks(bool upper, int n, int rt_end) {
 
 __host__ __device__ inline int row_tiles(int n) { return (n + kRows - 1) / kRows; }
 
+// A task's partial product (kRows x ldb) is stored column-quad-major: the 4
+// columns [4q, 4q+4) of all 128 rows, then the next quad, so that a warp's
+// accumulator rows (one per lane) leave as 512 contiguous bytes.
+__host__ __device__ inline int64_t ws_at(int task, int r, int c, int ldb) {
+    return (int64_t)task * kRows * ldb + ((int64_t)(c >> 2) * kRows + r) * 4 + (c & 3);
+}
+
 // byte offset of element (r, k) of an operand tile (r: row of M or column of
 // the right-hand sides, k: column of T within the stage)
 __device__ __forceinline__ uint32_t tile_off(int r, int k) {
@@ -168,7 +175,7 @@ k_btop_gather(int n, int P, int ldb, const int32_t *__restrict__ col, const int3
 
 // One partial product: rows [i0, i0+128) of M (n x n, row-major, leading
 // dimension ldt, a multiple of 4, zero past column n) times rows [k_lo, k_hi)
-// of B (n x ldb), columns [c0, c0+256), into ws[task] (128 x ldb). Per stage
+// of B (n x ldb), columns [c0, c0+256), into ws[task] (128 x ldb, ws_at). Per stage
 // of 32 columns of M: all threads load and split the tiles into shared
 // memory, thread 0 issues 12 MMAs (4 steps of K = 8, three products each)
 // and commits them to an mbarrier; the next stage is loaded into registers
@@ -307,17 +314,18 @@ k_btop_mma(int n, int ldt, int ldb, const float *__restrict__ M, const float *__
     }
     fence_after_sync();
     if (ok) {
-        const int lane_base = 32 * (warp % 4), cbase = (warp / 4) * (kCols / 2);
-        float *w = ws + ((int64_t)task * kRows + lane_base + lane) * ldb + c0 + cbase;
+        const int lane_base = 32 * (warp % 4), cbase = (warp / 4) * (kCols / 2), r = lane_base + lane;
 #pragma unroll 1
         for (int ch = 0; ch < kCols / 2 / 16; ++ch) {
             float v[16];
             tmem_ld16(tmem + ((uint32_t)lane_base << 16) + (uint32_t)(cbase + ch * 16), v);
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (c0 + cbase + ch * 16 + 4 * q < ldb)
-                    *reinterpret_cast<float4 *>(w + ch * 16 + 4 * q) =
+            for (int q = 0; q < 4; ++q) {
+                const int c = c0 + cbase + ch * 16 + 4 * q;
+                if (c < ldb)
+                    *reinterpret_cast<float4 *>(ws + ws_at(task, r, c, ldb)) =
                         make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
         }
     } else {
         if (tid == 0) atomicOr(err, kErrTimeout);
@@ -334,18 +342,17 @@ k_btop_mma(int n, int ldt, int ldb, const float *__restrict__ M, const float *__
 }
 
 // Sums a row's partial products in split order. Forward: Y (n x ldb), one
-// float4 per thread.
+// float4 per thread, consecutive threads on consecutive rows (the partials'
+// order).
 __global__ void __launch_bounds__(256)
 k_btop_reduce_fwd(int n, int ldb, const float *__restrict__ ws, float *__restrict__ Y) {
-    const int g4 = ldb / 4;
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= (int64_t)n * g4) return;
-    const int i = (int)(q / g4), c = (int)(q % g4) * 4, rt = i / kRows;
+    if (q >= (int64_t)n * (ldb / 4)) return;
+    const int c = (int)(q / n) * 4, i = (int)(q % n), rt = i / kRows, r = i - rt * kRows;
     const int t0 = tasks(false, n, rt), ns = splits(false, n, rt);
-    const float *w = ws + ((int64_t)t0 * kRows + (i - rt * kRows)) * ldb + c;
-    float4 acc = *reinterpret_cast<const float4 *>(w);
+    float4 acc = *reinterpret_cast<const float4 *>(ws + ws_at(t0, r, c, ldb));
     for (int k = 1; k < ns; ++k) {
-        const float4 v = *reinterpret_cast<const float4 *>(w + (int64_t)k * kRows * ldb);
+        const float4 v = *reinterpret_cast<const float4 *>(ws + ws_at(t0 + k, r, c, ldb));
         acc.x += v.x;
         acc.y += v.y;
         acc.z += v.z;
@@ -354,22 +361,21 @@ k_btop_reduce_fwd(int n, int ldb, const float *__restrict__ ws, float *__restric
     *reinterpret_cast<float4 *>(Y + (int64_t)i * ldb + c) = acc;
 }
 
-// Backward, one (top row, pose) per thread: x of that top column stored into
-// the solution and added to the positions (pc32 = float(pc64)).
+// Backward, one (top row, pose) per thread, consecutive threads on
+// consecutive rows: x of that top column stored into the solution and added
+// to the positions (pc32 = float(pc64)).
 __global__ void __launch_bounds__(256)
 k_btop_reduce_bwd(int n, int P, int ldb, const float *__restrict__ ws, const int32_t *__restrict__ col,
                   Vec4<float> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= (int64_t)n * P) return;
-    const int i = (int)(q / P), p = (int)(q % P), rt = i / kRows;
+    const int p = (int)(q / n), i = (int)(q % n), rt = i / kRows, r = i - rt * kRows;
     const int t0 = tasks(true, n, rt), ns = splits(true, n, rt);
-    const float *w = ws + ((int64_t)t0 * kRows + (i - rt * kRows)) * ldb + 3 * p;
-    float x = w[0], y = w[1], z = w[2];
+    float x = ws[ws_at(t0, r, 3 * p, ldb)], y = ws[ws_at(t0, r, 3 * p + 1, ldb)], z = ws[ws_at(t0, r, 3 * p + 2, ldb)];
     for (int k = 1; k < ns; ++k) {
-        const float *v = w + (int64_t)k * kRows * ldb;
-        x += v[0];
-        y += v[1];
-        z += v[2];
+        x += ws[ws_at(t0 + k, r, 3 * p, ldb)];
+        y += ws[ws_at(t0 + k, r, 3 * p + 1, ldb)];
+        z += ws[ws_at(t0 + k, r, 3 * p + 2, ldb)];
     }
     const int64_t e = (int64_t)col[i] * P + p;
     sol[e] = {x, y, z, 0.f};
