@@ -686,11 +686,7 @@ static void bsolve(const DevSym &s, int P, int grid, const float *X, const float
 // ---------------------------------------------------------------------------
 // dense top for many poses (arap_btop.cuh)
 
-size_t btop_workspace_floats(int n, int P) {
-    if (n <= 0) return 0;
-    const int nrt = btop::row_tiles(n);
-    return (size_t)std::max(btop::tasks(false, n, nrt), btop::tasks(true, n, nrt)) * btop::kRows * btop::ldb_of(P);
-}
+size_t btop_workspace_floats(int n, int P) { return (size_t)btop::ws_floats(n, P); }
 
 size_t btop_matrix_floats(int n, int P) { return (size_t)std::max(n, 0) * btop::ldb_of(P); }
 

@@ -18,22 +18,14 @@
 
 #include <cstdint>
 
+#include "arap_btop_plan.h"
 #include "arap_kernels.h"
 
 namespace arapgpu {
 namespace btop {
 
-#ifndef ARAP_BTOP_SPLIT
-#define ARAP_BTOP_SPLIT 256
-#endif
-
-constexpr int kRows = 128;             // rows of T per task: the MMA's M
-constexpr int kCols = 256;             // columns of the right-hand sides per CTA: the MMA's N
-constexpr int kDepth = 32;             // columns of T per stage: 4 MMAs of K = 8
-constexpr int kSplit = ARAP_BTOP_SPLIT;  // columns of T per task (a multiple of kDepth)
 constexpr int kThreads = 256;
-constexpr uint32_t kTmemCols = 256;    // the fp32 accumulator: 128 lanes x 256 columns
-static_assert(kSplit % kDepth == 0, "a split is a whole number of stages");
+constexpr uint32_t kTmemCols = 256;  // the fp32 accumulator: 128 lanes x 256 columns
 
 // Operands in shared memory, K-major without swizzle: core matrices of 8 rows
 // x 16 bytes (4 floats) stored as 128 contiguous bytes; the core matrices of
@@ -42,36 +34,6 @@ static_assert(kSplit % kDepth == 0, "a split is a whole number of stages");
 constexpr uint32_t kCoreK = 128, kCoreMN = (kDepth / 4) * 128;
 constexpr int kAFloats = kRows * kDepth, kBFloats = kCols * kDepth;
 constexpr int kSmemBytes = (2 * kAFloats + 2 * kBFloats) * 4 + 1024;  // hi and lo of each, alignment slack
-
-__host__ __device__ inline int ldb_of(int P) { return (3 * P + 3) & ~3; }
-
-// columns [kb, ke) of T's rows in row tile rt that the product reads
-__host__ __device__ inline void krange(bool upper, int n, int rt, int &kb, int &ke) {
-    kb = upper ? rt * kRows : 0;
-    ke = upper ? n : ((rt + 1) * kRows < n ? (rt + 1) * kRows : n);
-}
-
-__host__ __device__ inline int splits(bool upper, int n, int rt) {
-    int kb, ke;
-    krange(upper, n, rt, kb, ke);
-    return (ke - kb + kSplit - 1) / kSplit;
-}
-
-// tasks (row tile, split) of the row tiles before rt_end
-__host__ __device__ inline int tasks(bool upper, int n, int rt_end) {
-    int t = 0;
-    for (int rt = 0; rt < rt_end && rt * kRows < n; ++rt) t += splits(upper, n, rt);
-    return t;
-}
-
-__host__ __device__ inline int row_tiles(int n) { return (n + kRows - 1) / kRows; }
-
-// A task's partial product (kRows x ldb) is stored column-quad-major: the 4
-// columns [4q, 4q+4) of all 128 rows, then the next quad, so that a warp's
-// accumulator rows (one per lane) leave as 512 contiguous bytes.
-__host__ __device__ inline int64_t ws_at(int task, int r, int c, int ldb) {
-    return (int64_t)task * kRows * ldb + ((int64_t)(c >> 2) * kRows + r) * 4 + (c & 3);
-}
 
 // byte offset of element (r, k) of an operand tile (r: row of M or column of
 // the right-hand sides, k: column of T within the stage)
@@ -193,14 +155,8 @@ k_btop_mma(int n, int ldt, int ldb, const float *__restrict__ M, const float *__
     float *Ahi = reinterpret_cast<float *>(base), *Alo = Ahi + kAFloats;
     float *Bhi = Alo + kAFloats, *Blo = Bhi + kBFloats;
     const int task = blockIdx.y;
-    int rt = 0, t = task;
-    for (int c = splits(UPPER, n, 0); t >= c; c = splits(UPPER, n, rt)) {
-        t -= c;
-        ++rt;
-    }
-    int kb, ke;
-    krange(UPPER, n, rt, kb, ke);
-    const int k_lo = kb + t * kSplit, k_hi = min(ke, k_lo + kSplit);
+    int rt, k_lo, k_hi;
+    task_of(UPPER, n, task, rt, k_lo, k_hi);
     const int i0 = rt * kRows, c0 = blockIdx.x * kCols;
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 

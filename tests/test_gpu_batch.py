@@ -178,3 +178,26 @@ def test_pose_batch_dense_top_matches_supernodal_top(gpu, cols):
         ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.poses[p], 6)
         assert ok and W.bbox_rel_error(got[p], o, w.positions) <= 1e-6, p
         np.testing.assert_array_equal(got[p][w.cidx], w.poses[p])
+
+
+def test_pose_batch_dense_top_several_column_tiles(gpu):
+    """90 poses pack into 270 right-hand-side columns: two 256-column tiles of
+    the tensor-core products, the second ragged. Every pose agrees with the
+    sweeps over the whole tree; every ninth with the oracle."""
+    w = W.cfg_pose_batch(level=4, n_poses=90, iterations=4)
+
+    def run(c):
+        with gpu.ArapContext(w.V, w.faces) as ctx:
+            ctx.set_precision("mixed", 1)
+            ctx.set_dense_top(c)
+            ctx.set_rest_positions(w.positions)
+            ctx.set_constraints(w.cidx, w.poses[0])
+            return ctx.deform_poses(w.poses, 4)
+
+    ref, got = run(-1), run(0)
+    for p in range(len(w.poses)):
+        assert W.bbox_rel_error(got[p], ref[p], w.positions) <= 1e-6, p
+        np.testing.assert_array_equal(got[p][w.cidx], w.poses[p])
+    for p in range(0, len(w.poses), 9):
+        ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.poses[p], 4)
+        assert ok and W.bbox_rel_error(got[p], o, w.positions) <= 1e-6, p
