@@ -1898,8 +1898,8 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
             B = nnz * (4 + 4 + 12) + 4 * (m + 1) + P * (V * 36 + m * 12);
         FL = P * nnz * 24;
         break;
-    case ARAP_K_RESIDUAL:
-        B = P * m * (24 + 12 + 12) + m * 8 + 4 * (m + 1) + nnz * (4 + 8);
+    case ARAP_K_RESIDUAL:  // x, bFixed (FP64), b in, r out per free vertex and pose
+        B = P * m * (24 + 24 + 12 + 12) + m * 8 + 4 * (m + 1) + nnz * (4 + 8);
         FL = P * nnz * 6;
         break;
     case ARAP_K_SOLVE_FWD:
