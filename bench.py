@@ -207,6 +207,16 @@ def run_batch(args):
     ctx.set_precision("mixed", args.refine)
     ctx.set_rest_positions(w.positions)
     ctx.set_constraints(w.cidx, w.poses[0])
+    dense_tuned = None
+    if args.dense_top == "auto":
+        import arap_tune
+
+        ctx.deform_poses(w.poses, w.iterations)  # targets on the device
+        best_cap, times = arap_tune.tune_dense_top(ctx, w.iterations, batched=True)
+        dense_tuned = {"dense_top": best_cap, "ms_per_call": {str(k): round(v, 3) for k, v in times.items()}}
+        log(f"autotuned dense top: {best_cap} {dense_tuned['ms_per_call']}")
+    else:
+        ctx.set_dense_top(int(args.dense_top))
     first = ctx.deform_poses(w.poses, w.iterations)
     tuned = None
     if args.pose_tile < 0:
@@ -339,7 +349,9 @@ def run_batch(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": config_of(w, args, {"poses": P, "step": f"dirty deform of {P} poses (one shared factor)",
                                       "precision": "mixed", "pose_tile": args.pose_tile,
-                                      "pose_tile_autotune": tuned}),
+                                      "pose_tile_autotune": tuned,
+                                      "dense_top": dense_tuned["dense_top"] if dense_tuned else int(args.dense_top),
+                                      "dense_top_autotune": dense_tuned}),
         "e2e": {"value": its_total / e2e_total if e2e_s else None, "unit": UNIT,
                 "h2d_bytes_per_step": int(tf_h.nbytes + handles.nbytes + 96), "d2h_bytes_per_step": int(out_h.nbytes),
                 "inputs": "P rigid transforms, targets mapped on the device"},
@@ -530,6 +542,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: skip the end-to-end pass")
     ap.add_argument("--poses", type=int, default=256, help="pose_batch: handle poses per step")
+    ap.add_argument("--dense-top", default="auto",
+                    help="pose_batch: column cap of the tree's dense top (-1: none; 0: the library default; "
+                         "'auto': autotuned)")
     ap.add_argument("--pose-tile", type=int, default=-1,
                     help="pose_batch: poses per batched-solve task (0: largest that fits; -1: autotuned)")
     ap.add_argument("--solve-ctas", type=int, default=-1,

@@ -1,6 +1,7 @@
 """Launch-shape autotuner: picks the number of CTAs per triangular-solve
 launch (arap_set_solve_ctas) for a workload and a number of requests in
-flight, and the pose tile of the batched solves (arap_set_pose_tile), by
+flight, the pose tile of the batched solves (arap_set_pose_tile) and the
+column cap of the elimination tree's dense top (arap_set_dense_top), by
 timing short trial runs through the C ABI.
 
 One request alone is fastest with as many CTAs as fit on the device (the
@@ -116,3 +117,42 @@ def tune_pose_tile(ctx, iterations: int, candidates=POSE_TILES, trials: int = 2,
     best_pt = min(times, key=times.get)
     ctx.set_pose_tile(best_pt)
     return best_pt, times
+
+
+DENSE_TOPS = (-1, 1024, 2048, 3072, 4096)
+
+
+def tune_dense_top(ctx, iterations: int, batched: bool, candidates=DENSE_TOPS, trials: int = 2):
+    """Returns (best_cap, {cap: ms per call}): the column cap of the tree's top
+    solved through its explicit inverse (arap_set_dense_top; -1: none), timed
+    on full dirty calls (weights, factor, inverse of the top, iterations) of
+    arap_deform_poses when batched (pose targets already on the device) or of
+    arap_deform. A wider top trades the supernodal tasks of the upper levels
+    for wider products with T, formed once per factorisation. Leaves the best
+    cap set."""
+    times = {}
+    for cap in candidates:
+        ctx.set_dense_top(int(cap))
+
+        def call():
+            if batched:
+                return ctx.deform_poses_rc(None, iterations, None)
+            return ctx.deform_rc(iterations)
+
+        for _ in range(2):  # set-up and schedule reset, then graph capture: untimed
+            ctx.invalidate()
+            rc = call()
+            if rc != G.ARAP_OK:
+                raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+        best = float("inf")
+        for _ in range(max(1, trials)):
+            ctx.invalidate()
+            t0 = time.perf_counter()
+            rc = call()
+            if rc != G.ARAP_OK:
+                raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
+            best = min(best, time.perf_counter() - t0)
+        times[int(cap)] = 1e3 * best
+    best_cap = min(times, key=times.get)
+    ctx.set_dense_top(best_cap)
+    return best_cap, times

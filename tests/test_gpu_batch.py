@@ -201,3 +201,33 @@ def test_pose_batch_dense_top_several_column_tiles(gpu):
     for p in range(0, len(w.poses), 9):
         ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.poses[p], 4)
         assert ok and W.bbox_rel_error(got[p], o, w.positions) <= 1e-6, p
+
+
+def test_dense_top_autotune(gpu):
+    """arap_tune.tune_dense_top times every candidate cap on full dirty calls,
+    leaves the fastest set, and the results stay within the mixed tolerance
+    of the default cap (batched) and of the oracle (one request)."""
+    import arap_tune
+
+    w = W.cfg_pose_batch(level=4, n_poses=6, iterations=3)
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.poses[0])
+        ref = ctx.deform_poses(w.poses, 3)
+        best, times = arap_tune.tune_dense_top(ctx, 3, batched=True, candidates=(-1, 256, 2048), trials=1)
+        assert set(times) == {-1, 256, 2048} and best in times
+        assert all(t > 0 for t in times.values())
+        got = ctx.deform_poses(None, 3)
+        for p in range(len(w.poses)):
+            assert W.bbox_rel_error(got[p], ref[p], w.positions) <= 1e-6, p
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.poses[1])
+        best, times = arap_tune.tune_dense_top(ctx, 3, batched=False, candidates=(-1, 512), trials=1)
+        assert set(times) == {-1, 512} and best in times
+        ctx.invalidate()  # a dirty deform from the rest pose, as the oracle runs
+        out = ctx.deform(3)
+    ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.poses[1], 3)
+    assert ok and W.bbox_rel_error(out, o, w.positions) <= 1e-6
