@@ -546,15 +546,11 @@ static cudaError_t configure_pt(size_t bytes) {
 }
 
 // the tensor-core products of the dense top: shared memory above the default
+// (per device)
 static cudaError_t configure_btop() {
-    static const cudaError_t e = [] {
-        const cudaError_t a = cudaFuncSetAttribute((const void *)btop::k_btop_mma<false>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, btop::kSmemBytes);
-        if (a != cudaSuccess) return a;
-        return cudaFuncSetAttribute((const void *)btop::k_btop_mma<true>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, btop::kSmemBytes);
-    }();
-    return e;
+    const cudaError_t a = raise_smem_limit((const void *)btop::k_btop_mma<false>, btop::kSmemBytes);
+    if (a != cudaSuccess) return a;
+    return raise_smem_limit((const void *)btop::k_btop_mma<true>, btop::kSmemBytes);
 }
 
 cudaError_t configure_batch_smem(int max_ldx, int max_ld21, int pt) {

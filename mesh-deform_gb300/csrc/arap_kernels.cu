@@ -2243,7 +2243,6 @@ void launch_gather_rotations(const DevSym &s, const Vec4<T> *R, double *out9, cu
     k_gather_rotations<T><<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.oldidx, R, out9);
 }
 
-// Raises the dynamic shared-memory limit of the column-block inverse kernel.
 // Raises, never lowers, a kernel's dynamic shared-memory limit on the current
 // device. The limit belongs to the kernel, not to a context: contexts of
 // different sizes in one process must not lower each other's.
