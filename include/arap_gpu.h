@@ -337,14 +337,32 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
    val (nnz doubles, overwritten). The kernels run on `stream` (a
    cudaStream_t; NULL = default stream) of the calling thread's current
    device and the call returns without waiting for them. The first call on a
-   device looks up the scratch array's device address; make that first call
-   before any stream capture. All calls on one device share the scratch array,
-   which keeps the last call's contents: calls whose kernels overlap on the GPU
-   race and must be ordered by the caller. More than 524,288 faces returns
-   ARAP_ERR_UNSUPPORTED. Values equal arap_get_edge_weights bit for bit when
-   every edge lies on at most two faces. */
+   device looks up the scratch array's device address, which under CUDA's
+   default lazy module loading also loads the library's device code on that
+   device: a one-time driver allocation of the 12 MiB array that may
+   synchronise the device. Make that first call at start-up, before any stream
+   capture and before the callbacks that must not stall; later calls allocate
+   nothing. All calls on one device share the scratch array, which keeps the
+   last call's contents: calls whose kernels overlap on the GPU race and must
+   be ordered by the caller. More than 524,288 faces returns
+   ARAP_ERR_UNSUPPORTED. The device-resident inputs are checked by the
+   kernels: a face with an index outside [0, n_vertices) is skipped (it adds
+   nothing) and an edge missing from the pattern adds nothing; both are
+   counted for arap_cotan_weights_static_status, and no kernel reads outside
+   the given arrays. A face whose corners repeat a vertex adds both halves of
+   that edge to the diagonal entry (the reference's two (a, a) triplets) when
+   the pattern holds it. Values equal arap_get_edge_weights bit for bit when no
+   entry receives more than two contributions (every edge on at most two
+   faces, no diagonal shared by two degenerate corners); otherwise the
+   additions' order, and so the last bit, may differ. */
 int arap_cotan_weights_static(int32_t n_vertices, int32_t n_faces, const int32_t *faces, const double *xyz,
                               const int32_t *rowptr, const int32_t *col, int32_t nnz, double *val, void *stream);
+/* Input-check result of the last arap_cotan_weights_static on the current
+   device: waits for `stream` (the stream that call used), stores in *skipped
+   (may be NULL) the number of faces it skipped for an out-of-range index plus
+   the edges it found missing from the pattern, and returns ARAP_ERR_BAD_INDEX
+   when that number is not zero, else ARAP_OK. Allocates nothing. */
+int arap_cotan_weights_static_status(void *stream, int32_t *skipped);
 
 /* ------------------------------------------------------------------------
    Deform server: a request loop over resident contexts (no counterpart in the

@@ -99,6 +99,7 @@ SIGNATURES = {
     "arap_get_kernel_stats": (C.c_int, [_P, _I32, _dp, _lp]),
     "arap_get_kernel_model": (C.c_int, [_P, _I32, _dp, _dp]),
     "arap_cotan_weights_static": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _I32, _P, _P]),
+    "arap_cotan_weights_static_status": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "arap_deform_poses": (C.c_int, [_P, _I32, _dp, _I32, _dp]),
     "arap_deform_async": (C.c_int, [_P, _I32, _dp]),
     "arap_wait": (C.c_int, [_P]),

@@ -15,6 +15,14 @@
 // a device share it and it keeps the last call's contents; calls whose kernels
 // overlap on the GPU (different streams, or different host threads on the same
 // device) race on it and must be ordered by the caller.
+//
+// Input checks on the device: the face indices and the weight pattern live in
+// device memory, so they are checked by the kernels, not the host. A face with
+// an index outside [0, n_vertices) is skipped (its scratch halves are zero and
+// nothing is added for it), and an edge whose entry is missing from the
+// pattern adds nothing; every such event is counted in a file-scope __device__
+// counter that arap_cotan_weights_static_status reads. No kernel reads outside
+// faces[0, 3F), xyz[0, 3V), rowptr[0, V] or col/val[0, nnz).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -34,32 +42,57 @@ constexpr int kMaxDevices = 64;
 
 // per-face cotangent halves (arap.h:212-227), three doubles per face
 static __device__ __align__(256) double g_face_cot_scratch[3 * kStaticMaxFaces];
+// faces skipped for an out-of-range index plus edges missing from the pattern,
+// in the last call on this device (zeroed at the start of every call)
+static __device__ int g_skipped;
 
 std::mutex g_setup_mutex;
 double *g_scratch_addr[kMaxDevices] = {};
+int *g_skipped_addr[kMaxDevices] = {};
 
-// Host code cannot use g_face_cot_scratch as a device address (in host code it
-// names a host-side stand-in). Its device address is looked up once per device,
-// with that device current, and passed to the kernels.
-cudaError_t scratch_address(int device, double **out) {
+// Host code cannot use g_face_cot_scratch or g_skipped as device addresses (in
+// host code their names denote host-side stand-ins). Their device addresses
+// are looked up once per device, with that device current, and passed to the
+// kernels and copies.
+cudaError_t symbol_addresses(int device, double **scratch, int **skipped) {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch_addr[device]) {
-        void *p = nullptr;
+        void *p = nullptr, *q = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_face_cot_scratch);
         if (e != cudaSuccess) return e;
+        e = cudaGetSymbolAddress(&q, g_skipped);
+        if (e != cudaSuccess) return e;
+        g_skipped_addr[device] = static_cast<int *>(q);
         g_scratch_addr[device] = static_cast<double *>(p);
     }
-    *out = g_scratch_addr[device];
+    *scratch = g_scratch_addr[device];
+    *skipped = g_skipped_addr[device];
     return cudaSuccess;
 }
 
+int current_device(int *device) {
+    if (cudaGetDevice(device) != cudaSuccess || *device < 0 || *device >= kMaxDevices) return ARAP_ERR_NO_DEVICE;
+    return ARAP_OK;
+}
+
+__device__ __forceinline__ bool in_range(int v, int n) { return v >= 0 && v < n; }
+
 // The clamped Heron cotangents of arap.h:199-218 times 1/2, each operation
-// rounded separately (no fused multiply-add), as the FP64 CPU path does.
-__global__ void k_face_cots_to_scratch(int F, const int32_t *__restrict__ faces, const double *__restrict__ xyz,
-                                       double *__restrict__ hc) {
+// rounded separately (no fused multiply-add), as the FP64 CPU path does. A
+// face with an index outside [0, V) reads no position, gets zero halves and is
+// counted.
+__global__ void k_face_cots_to_scratch(int F, int V, const int32_t *__restrict__ faces,
+                                       const double *__restrict__ xyz, double *__restrict__ hc, int *skipped) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
     const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
+    if (!in_range(i0, V) || !in_range(i1, V) || !in_range(i2, V)) {
+        hc[3 * (int64_t)f + 0] = 0.0;
+        hc[3 * (int64_t)f + 1] = 0.0;
+        hc[3 * (int64_t)f + 2] = 0.0;
+        atomicAdd(skipped, 1);
+        return;
+    }
     const double *v0 = xyz + 3 * (int64_t)i0, *v1 = xyz + 3 * (int64_t)i1, *v2 = xyz + 3 * (int64_t)i2;
     double l0 = 0.0, l1 = 0.0, l2 = 0.0, d;
     for (int c = 0; c < 3; ++c) { d = __dsub_rn(v1[c], v0[c]); l0 = __dadd_rn(l0, __dmul_rn(d, d)); }
@@ -82,13 +115,17 @@ __global__ void k_face_cots_to_scratch(int F, const int32_t *__restrict__ faces,
     hc[3 * (int64_t)f + 2] = __dmul_rn((1e-10 < c2) ? c2 : 1e-10, 0.5);
 }
 
-__global__ void k_zero(int n, double *__restrict__ v) {
+// val = 0; thread 0 also clears the skip counter of the previous call
+__global__ void k_zero(int n, double *__restrict__ v, int *skipped) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *skipped = 0;
     if (i < n) v[i] = 0.0;
 }
 
-__device__ __forceinline__ int find_entry(const int32_t *rowptr, const int32_t *col, int r, int c) {
-    int lo = rowptr[r], hi = rowptr[r + 1] - 1;
+// Entry (r, c) of the pattern, or -1. The row's range is clipped to [0, nnz),
+// so a malformed rowptr cannot send the search outside col.
+__device__ __forceinline__ int find_entry(const int32_t *rowptr, const int32_t *col, int nnz, int r, int c) {
+    int lo = max(rowptr[r], 0), hi = min(rowptr[r + 1], nnz) - 1;
     while (lo <= hi) {
         const int mid = (lo + hi) >> 1;
         const int v = col[mid];
@@ -101,19 +138,26 @@ __device__ __forceinline__ int find_entry(const int32_t *rowptr, const int32_t *
 
 // Adds each face's halves into both directions of its three edges
 // (arap.h:225-232). An edge of a manifold mesh receives at most two additions
-// onto zero, which round the same in either order.
-__global__ void k_scatter_weights(int F, const int32_t *__restrict__ faces, const int32_t *__restrict__ rowptr,
-                                  const int32_t *__restrict__ col, const double *__restrict__ hc,
-                                  double *__restrict__ val) {
+// onto zero, which round the same in either order. A face whose corners
+// repeat a vertex gives a diagonal entry both directions' halves, as the
+// reference's two triplets (a, a) do. Faces with an out-of-range index are
+// skipped (counted by k_face_cots_to_scratch); an edge missing from the
+// pattern is counted here.
+__global__ void k_scatter_weights(int F, int V, int nnz, const int32_t *__restrict__ faces,
+                                  const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+                                  const double *__restrict__ hc, double *__restrict__ val, int *skipped) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * F) return;
     const int f = t / 3, k = t - 3 * f;
+    const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
+    if (!in_range(i0, V) || !in_range(i1, V) || !in_range(i2, V)) return;
     const int a = faces[3 * f + k], b = faces[3 * f + (k + 1) % 3];
     const double h = hc[t];
-    const int e1 = find_entry(rowptr, col, a, b);
-    const int e2 = find_entry(rowptr, col, b, a);
+    const int e1 = find_entry(rowptr, col, nnz, a, b);
+    const int e2 = find_entry(rowptr, col, nnz, b, a);
     if (e1 >= 0) atomicAdd(val + e1, h);
     if (e2 >= 0) atomicAdd(val + e2, h);
+    if (e1 < 0 || e2 < 0) atomicAdd(skipped, 1);
 }
 
 }  // namespace
@@ -132,27 +176,54 @@ extern "C" int arap_cotan_weights_static(int32_t n_vertices, int32_t n_faces, co
         return ARAP_ERR_UNSUPPORTED;
     }
     int device = 0;
-    cudaError_t e = cudaGetDevice(&device);
-    if (e != cudaSuccess || device < 0 || device >= kMaxDevices) {
+    if (current_device(&device) != ARAP_OK) {
         arapgpu::set_global_error("arap_cotan_weights_static: no usable current device");
         return ARAP_ERR_NO_DEVICE;
     }
     double *hc = nullptr;
-    e = scratch_address(device, &hc);
+    int *skipped = nullptr;
+    cudaError_t e = symbol_addresses(device, &hc, &skipped);
     if (e != cudaSuccess) {
         arapgpu::set_global_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         return ARAP_ERR_CUDA;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (nnz > 0) k_zero<<<(nnz + 255) / 256, 256, 0, st>>>(nnz, val);
+    k_zero<<<(nnz + 255) / 256 + (nnz == 0), 256, 0, st>>>(nnz, val, skipped);
     if (n_faces > 0) {
-        k_face_cots_to_scratch<<<(n_faces + 255) / 256, 256, 0, st>>>(n_faces, faces, xyz, hc);
-        k_scatter_weights<<<(3 * n_faces + 255) / 256, 256, 0, st>>>(n_faces, faces, rowptr, col, hc, val);
+        k_face_cots_to_scratch<<<(n_faces + 255) / 256, 256, 0, st>>>(n_faces, n_vertices, faces, xyz, hc, skipped);
+        k_scatter_weights<<<(3 * n_faces + 255) / 256, 256, 0, st>>>(n_faces, n_vertices, nnz, faces, rowptr, col,
+                                                                      hc, val, skipped);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         arapgpu::set_global_error(std::string("arap_cotan_weights_static launch: ") + cudaGetErrorString(e));
         return ARAP_ERR_CUDA;
+    }
+    return ARAP_OK;
+}
+
+extern "C" int arap_cotan_weights_static_status(void *stream, int32_t *skipped) {
+    int device = 0;
+    if (current_device(&device) != ARAP_OK) {
+        arapgpu::set_global_error("arap_cotan_weights_static_status: no usable current device");
+        return ARAP_ERR_NO_DEVICE;
+    }
+    double *hc = nullptr;
+    int *counter = nullptr;
+    cudaError_t e = symbol_addresses(device, &hc, &counter);
+    int n = 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&n, counter, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        arapgpu::set_global_error(std::string("arap_cotan_weights_static_status: ") + cudaGetErrorString(e));
+        return ARAP_ERR_CUDA;
+    }
+    if (skipped) *skipped = n;
+    if (n > 0) {
+        arapgpu::set_global_error("arap_cotan_weights_static: " + std::to_string(n) +
+                                  " faces with an index outside [0, n_vertices) or edges missing from the pattern");
+        return ARAP_ERR_BAD_INDEX;
     }
     return ARAP_OK;
 }
