@@ -78,10 +78,9 @@ def config_of(w, args, extra=None):
         "free": int(w.V - len(w.cidx)),
         "iterations_per_step": w.iterations,
         "precision": args.precision,
-        "refine_steps": args.refine,
         "step": "dirty deform (weights + factor + iterations)",
         "l2": "flushed before every step (256 MB write)",
-        "parallelism": f"replicas{args.gpus}",
+        "parallelism": f"replicas{int(os.environ.get('WORLD_SIZE', '1'))}",
     }
     if extra:
         c.update(extra)
@@ -205,6 +204,7 @@ def run_batch(args):
     P = w.poses.shape[0]
     ctx = G.ArapContext(w.V, w.faces, device=local)
     ctx.set_precision("mixed", args.refine)
+    ctx.set_factor_precision(args.factor_bits)
     ctx.set_rest_positions(w.positions)
     ctx.set_constraints(w.cidx, w.poses[0])
     dense_tuned = None
@@ -237,6 +237,7 @@ def run_batch(args):
         if rc != G.ARAP_OK:
             raise G.ArapError(rc, ctx.lib.arap_last_error(ctx.h).decode())
 
+    ctx.set_symbolic_cache(args.cached_analysis)
     for _ in range(args.warmup):
         flush.zero_()
         torch.cuda.synchronize()
@@ -258,6 +259,27 @@ def run_batch(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
+    repose = None
+    if not args.cached_analysis:  # the same step with the symbolic analysis kept
+        ctx.set_symbolic_cache(True)
+        for _ in range(args.warmup):
+            flush.zero_()
+            torch.cuda.synchronize()
+            step()
+        rms = []
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            rms.append(a.elapsed_time(b))
+        repose = {"value": P * w.iterations * args.steps / (sum(rms) / 1e3), "unit": UNIT,
+                  "ms_per_step": sum(rms) / len(rms),
+                  "step": "the same step with the symbolic analysis of the unchanged constraint set kept"}
+        ctx.set_symbolic_cache(args.cached_analysis)
     ctx.set_profiling(True)
     ctx.reset_kernel_stats()
     for k in range(args.steps):
@@ -347,7 +369,12 @@ def run_batch(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": config_of(w, args, {"poses": P, "step": f"dirty deform of {P} poses (one shared factor)",
+        "config": config_of(w, args, {"poses": P,
+                                      "step": f"dirty deform of {P} poses (symbolic analysis "
+                                              f"{'kept' if args.cached_analysis else 'redone'}, one shared "
+                                              f"factorisation, {w.iterations} iterations)",
+                                      "factor": f"fp{args.factor_bits}",
+                                      "fp64_residual_solves_per_iteration": 1 + args.refine,
                                       "precision": "mixed", "pose_tile": args.pose_tile,
                                       "pose_tile_autotune": tuned,
                                       "dense_top": dense_tuned["dense_top"] if dense_tuned else int(args.dense_top),
@@ -355,6 +382,7 @@ def run_batch(args):
         "e2e": {"value": its_total / e2e_total if e2e_s else None, "unit": UNIT,
                 "h2d_bytes_per_step": int(tf_h.nbytes + handles.nbytes + 96), "d2h_bytes_per_step": int(out_h.nbytes),
                 "inputs": "P rigid transforms, targets mapped on the device"},
+        "repose_refactor": repose,
         "e2e_explicit_targets": {"value": its_total / sum(e2e_x) if e2e_x else None, "unit": UNIT,
                                  "h2d_bytes_per_step": int(tg_h.nbytes), "d2h_bytes_per_step": int(out_h.nbytes)},
         "gpu_launches": int(launches),
@@ -527,6 +555,31 @@ def run_serving(args):
     return 0
 
 
+def reduce_max(x: float, dist, device=None) -> float:
+    """Largest x over the ranks of the process group (x itself without one):
+    the step time of a replica run is the slowest rank's."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def spawn_replicas(args) -> int:
+    """bench.py --gpus N (N > 1) started without torchrun: one replica process
+    per GPU through torch.distributed.run on this node, rank 0 prints."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve())] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -537,7 +590,13 @@ def main():
     ap.add_argument("--h", type=float, default=0.025)
     ap.add_argument("--iterations", type=int, default=30)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--refine", type=int, default=1)
+    ap.add_argument("--refine", type=int, default=1,
+                    help="mixed form: refinement solves per iteration beyond the first (every solve corrects the "
+                         "positions from an FP64 residual; 1 gives two per iteration)")
+    ap.add_argument("--factor-bits", type=int, default=64, choices=[32, 64],
+                    help="mixed form: numeric factorisation in FP64 (default) or FP32")
+    ap.add_argument("--cached-analysis", action="store_true",
+                    help="headline step keeps the symbolic analysis of the unchanged constraint set")
     ap.add_argument("--cpu-requests", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: skip the end-to-end pass")
@@ -564,24 +623,33 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return spawn_replicas(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "pose_batch":
         return run_batch(args)
     if args.workload == "serving":
         return run_serving(args)
+    return run_requests(args)
 
+
+def run_requests(args):
+    """N concurrent single-request dirty deforms per step (the default
+    workload): one host thread per request, as the reference arm runs one
+    request per host thread."""
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
     dist = None
     if world > 1:
         import torch.distributed as dist
 
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist.init_process_group("nccl", device_id=dev)
 
     def barrier():
         torch.cuda.synchronize()
@@ -594,6 +662,7 @@ def main():
 
     w = workload(args)
     N = max(1, args.concurrent)
+    mixed = args.precision == "mixed"
     tuned = None
     if args.solve_ctas < 0:
         import arap_tune
@@ -610,71 +679,111 @@ def main():
     for _ in range(N):
         c = G.ArapContext(w.V, w.faces, device=local)
         c.set_precision(args.precision, args.refine)
+        if mixed:
+            c.set_factor_precision(args.factor_bits)
         c.set_solve_ctas(args.solve_ctas)
         c.set_rest_positions(w.positions)
         c.set_constraints(w.cidx, w.ctargets)
         ctxs.append(c)
-    first = ctxs[0].deform(w.iterations)  # symbolic analysis + allocation + graph capture, untimed
+    first = ctxs[0].deform(w.iterations)  # allocation and graph capture, untimed
     for c in ctxs[1:]:
         c.deform(w.iterations, want_output=False)
-    streams = [torch.cuda.ExternalStream(c.stream(), device=torch.device("cuda", local)) for c in ctxs]
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    streams = [torch.cuda.ExternalStream(c.stream(), device=dev) for c in ctxs]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    pool = ThreadPoolExecutor(max_workers=N)
 
-    def step(out=None):
+    def set_analysis(cached: bool):
         for c in ctxs:
-            c.invalidate()
-            rc = c.lib.arap_deform_async(c.h, w.iterations, None)
-            if rc != G.ARAP_OK:
-                raise G.ArapError(rc, c.lib.arap_last_error(c.h).decode())
+            c.set_symbolic_cache(cached)
 
-    def wait_all():
-        for c in ctxs:
-            c.wait()
-
-    for _ in range(args.warmup):
+    def device_step():
+        """One step with inputs resident on the device: every request is a
+        dirty deform started by its own host thread. Device time = the union
+        of the requests' spans on their streams (first start event to last end
+        event), each start recorded before the request's first enqueue."""
         flush.zero_()
         torch.cuda.synchronize()
-        step()
-        wait_all()
-    # ---- timed region (device-resident inputs) ----
+        ref = torch.cuda.Event(enable_timing=True)
+        ref.record(streams[0])
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(N)]
+
+        def one(i):
+            c = ctxs[i]
+            c.invalidate()
+            ev[i][0].record(streams[i])
+            rc = c.lib.arap_deform_async(c.h, w.iterations, None)
+            ev[i][1].record(streams[i])
+            if rc != G.ARAP_OK:
+                raise G.ArapError(rc, c.lib.arap_last_error(c.h).decode())
+            c.wait()
+            return c.launch_count()
+
+        launches = sum(pool.map(one, range(N)))
+        torch.cuda.synchronize()
+        t0 = min(ref.elapsed_time(a) for a, _ in ev)
+        t1 = max(ref.elapsed_time(b) for _, b in ev)
+        return t1 - t0, launches
+
+    # ---- timed region: dirty deforms with inputs resident on the device ----
+    set_analysis(args.cached_analysis)
+    for _ in range(args.warmup):
+        device_step()
     clocks = ClockSampler(local)
     launches = 0
-    t_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    t_end = [[torch.cuda.Event(enable_timing=True) for _ in ctxs] for _ in range(args.steps)]
+    step_ms = []
     barrier()
     clocks.start()
     for k in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t_start[k].record(streams[0])
-        step()
-        for i, st in enumerate(streams):
-            t_end[k][i].record(st)
-        wait_all()
-        launches += sum(c.launch_count() for c in ctxs)
+        ms, nl = device_step()
+        step_ms.append(ms)
+        launches += nl
     barrier()
     clk = clocks.stop()
-    step_ms = [max(t_start[k].elapsed_time(e) for e in t_end[k]) for k in range(args.steps)]
+    total_ms = reduce_max(sum(step_ms), dist, dev)
+    its_total = N * w.iterations * args.steps * world
+    value = its_total / (total_ms / 1e3)
+    # ---- the same step with the symbolic analysis kept (re-pose + refactor) ----
+    repose = None
+    if not args.cached_analysis:
+        set_analysis(True)
+        for _ in range(args.warmup):
+            device_step()
+        rms = [device_step()[0] for _ in range(args.steps)]
+        repose = {"value": N * w.iterations * args.steps / (sum(rms) / 1e3), "unit": UNIT,
+                  "ms_per_step": sum(rms) / len(rms),
+                  "step": "the same dirty deforms with the symbolic analysis of the unchanged constraint set kept: "
+                          "weights, numeric factorisation and iterations only"}
+        set_analysis(args.cached_analysis)
     # per-request latency of a single request alone (p50/p99 over the steps),
-    # with the launch shape a lone request prefers
+    # with the launch shape a lone request prefers, with and without the
+    # symbolic analysis
+    c0 = ctxs[0]
     if args.solve_ctas != 0:
-        ctxs[0].set_solve_ctas(0)
-        ctxs[0].deform(w.iterations, want_output=False)
-    lat_single = []
-    for k in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(streams[0])
-        ctxs[0].invalidate()
-        ctxs[0].deform(w.iterations, want_output=False)
-        e1.record(streams[0])
-        torch.cuda.synchronize()
-        lat_single.append(e0.elapsed_time(e1))
+        c0.set_solve_ctas(0)
+        c0.deform(w.iterations, want_output=False)
+    lat_alone = {}
+    for cached in ((True,) if args.cached_analysis else (False, True)):
+        c0.set_symbolic_cache(cached)
+        c0.deform(w.iterations, want_output=False)
+        lat = []
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(streams[0])
+            c0.invalidate()
+            c0.deform(w.iterations, want_output=False)
+            e1.record(streams[0])
+            torch.cuda.synchronize()
+            lat.append(e0.elapsed_time(e1))
+        lat.sort()
+        key = "cached_analysis" if cached else "with_analysis"
+        lat_alone[key] = {"p50": lat[len(lat) // 2], "p99": float(np.percentile(lat, 99)),
+                          "host_ms_last": c0.host_timing()}
     # ---- per-kernel device time of one request, every launch bracketed by
     # CUDA events on its stream (a separate pass: the events do not inflate
     # the timed region above) ----
-    c0 = ctxs[0]
+    c0.set_symbolic_cache(True)
     c0.set_profiling(True)
     c0.reset_kernel_stats()
     for k in range(args.steps):
@@ -685,39 +794,37 @@ def main():
     kstats = c0.kernel_stats()
     kmodel = c0.kernel_model()
     c0.set_profiling(False)
+    setup_ms, iter_ms = c0.timing()
     if args.solve_ctas != 0:
         c0.set_solve_ctas(args.solve_ctas)
-    total_ms = sum(step_ms)
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    its_total = N * w.iterations * args.steps * world
-    value = its_total / (total_ms / 1e3)
+    c0.set_symbolic_cache(args.cached_analysis)
 
-    # ---- end to end through the C ABI with pinned host buffers ----
+    # ---- end to end through the C ABI with pinned host buffers: rest pose,
+    # constraint indices and targets in, deformed positions out, per request
+    # on its own host thread; wall clock around the whole step ----
     rest_h = torch.from_numpy(np.ascontiguousarray(w.positions)).pin_memory().numpy()
     idx_h = torch.from_numpy(np.ascontiguousarray(w.cidx, dtype=np.int32)).pin_memory().numpy()
     tgt_h = torch.from_numpy(np.ascontiguousarray(w.ctargets)).pin_memory().numpy()
     outs_h = [torch.empty((w.V, 3), dtype=torch.float64).pin_memory().numpy() for _ in ctxs]
+
+    def e2e_one(i):
+        c = ctxs[i]
+        c.set_rest_positions(rest_h)
+        c.set_constraints(idx_h, tgt_h)
+        c.deform_async(w.iterations, outs_h[i])
+        c.wait()
+
     e2e_s = []
     for k in range(0 if args.skip_e2e else args.warmup + args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for c, o in zip(ctxs, outs_h):
-            c.set_rest_positions(rest_h)
-            c.set_constraints(idx_h, tgt_h)
-            c.deform_async(w.iterations, o)
-        wait_all()
+        list(pool.map(e2e_one, range(N)))
         t1 = time.perf_counter()
         if k >= args.warmup:
             e2e_s.append(t1 - t0)
-    e2e_total = sum(e2e_s) if e2e_s else float("nan")
-    if dist is not None and e2e_s:
-        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    pool.shutdown()
+    e2e_total = reduce_max(sum(e2e_s), dist, dev) if e2e_s else float("nan")
     e2e_value = its_total / e2e_total if e2e_s else None
     h2d = N * (w.positions.nbytes + idx_h.nbytes + tgt_h.nbytes)
     d2h = N * outs_h[0].nbytes
@@ -764,26 +871,36 @@ def main():
         err = max([W.bbox_rel_error(o, ref, w.positions) for o in outs_h] if e2e_s else [err_first])
         log(f"error vs FP64 oracle: {err:.3e} (first deform {err_first:.3e})")
 
-    setup_ms, iter_ms = c0.timing()
-    lat = sorted(lat_single)
+    analysis = "kept for the unchanged constraint set" if args.cached_analysis else \
+        "redone on every request (ordering, elimination tree, supernodes, plan), as SimplicialLDLT::compute"
+    extra = {"requests_per_step": N, "solve_ctas": args.solve_ctas, "solve_ctas_autotune": tuned,
+             "symbolic_analysis": analysis,
+             "step": f"{N} concurrent dirty deform requests, one host thread each (symbolic analysis "
+                     f"{'kept' if args.cached_analysis else 'redone'}, weights, numeric factorisation, "
+                     f"{w.iterations} iterations)",
+             "timing": "union of the requests' device spans (CUDA events on each request's stream, the start "
+                       "recorded before its first enqueue)"}
+    if mixed:
+        extra.update({"factor": f"fp{args.factor_bits}",
+                      "fp64_residual_solves_per_iteration": 1 + args.refine})
+    else:
+        extra.update({"factor": "fp64"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": config_of(w, args, {"requests_per_step": N, "solve_ctas": args.solve_ctas,
-                                      "solve_ctas_autotune": tuned,
-                                      "step": f"{N} concurrent dirty deform requests (weights + factor + "
-                                              f"{w.iterations} iterations each)"}),
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
+        "config": config_of(w, args, extra),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "timing": "host wall clock around each step (uploads, enqueues, waits, result copies)"},
+        "repose_refactor": repose,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
                      "bytes_per_launch": dom_bytes, "ms_per_launch": per_launch_ms},
         "cpu_baseline": cpu,
         "error_vs_fp64_oracle": err,
-        "latency_ms": {"request_alone_p50": lat[len(lat) // 2], "request_alone_p99": float(np.percentile(lat, 99)),
-                       "step_p50": sorted(step_ms)[len(step_ms) // 2]},
+        "latency_ms": {"request_alone": lat_alone, "step_p50": sorted(step_ms)[len(step_ms) // 2]},
         "kernel_ms_per_request": {k: v[0] / args.steps for k, v in kstats.items()},
         "last_request_ms": {"setup": setup_ms, "iterations": iter_ms},
         "clocks": clk,

@@ -41,9 +41,11 @@ typedef enum arap_precision {
        factor, triangular solves. Matches the FP64 CPU path to <= 1e-10 of the
        bounding-box diagonal. */
     ARAP_PRECISION_FP64 = 0,
-    /* FP32 local step, RHS and triangular solves on an FP32 Cholesky factor;
-       the global system's residual is taken in FP64 and refined
-       (refine_steps extra solves per iteration). */
+    /* FP32 local step, RHS and triangular solves; the Cholesky factor is
+       computed in FP64 and rounded to FP32 for the solves
+       (arap_set_factor_precision); every solve corrects the positions from
+       the global system's residual taken in FP64, 1 + refine_steps such
+       refinement solves per iteration. */
     ARAP_PRECISION_MIXED = 1
 } arap_precision;
 
@@ -81,6 +83,14 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out);
    (MIXED only; 0..8). The default is ARAP_PRECISION_FP64. Marks the context
    dirty. */
 int arap_set_precision(arap_ctx *ctx, int32_t precision, int32_t refine_steps);
+
+/* Numeric factorisation of the MIXED form: bits = 64 (the default) factors
+   the constrained Laplacian in FP64, as SimplicialLDLT<SparseMatrix<double>>
+   does (arap.h:337,462), and rounds the factor's solve arrays to FP32 for the
+   triangular solves; bits = 32 factors in FP32 (cheaper set-up; the FP64
+   residual refinement still carries the accuracy). The FP64 form always
+   factors in FP64. Marks the context dirty. */
+int arap_set_factor_precision(arap_ctx *ctx, int32_t bits);
 
 /* Replaces initializeMeshGeometry (arap.h:162-168): the rest pose _p, read
    from the mesh on every dirty deform. 3*V doubles. Marks the context dirty. */
@@ -196,6 +206,14 @@ int arap_set_dense_top(arap_ctx *ctx, int32_t max_columns);
 
 /* arap_ordering of the next symbolic analysis (marks the context dirty). */
 int arap_set_ordering(arap_ctx *ctx, int32_t mode);
+
+/* enable != 0 (the default) keeps the symbolic analysis (ordering,
+   elimination tree, supernodes, factorisation plan) of a constrained-vertex
+   set for later dirty deforms of the same set, which then only refactor
+   numerically. 0 redoes and re-uploads it on every dirty deform, as the
+   reference's SimplicialLDLT::compute (arap.h:337) analyses the pattern on
+   every call; the CUDA graphs are then captured anew too. */
+int arap_set_symbolic_cache(arap_ctx *ctx, int32_t enable);
 
 /* enable != 0 (the default) runs the setup and the iteration sequence as CUDA
    graphs captured on first use and replayed while the problem's size,

@@ -80,6 +80,7 @@ SIGNATURES = {
     "arap_create": (C.c_int, [_I32, _I32, _ip, _I32, C.POINTER(_P)]),
     "arap_destroy": (None, [_P]),
     "arap_set_precision": (C.c_int, [_P, _I32, _I32]),
+    "arap_set_factor_precision": (C.c_int, [_P, _I32]),
     "arap_set_rest_positions": (C.c_int, [_P, _dp]),
     "arap_set_constraints": (C.c_int, [_P, _I32, _ip, _dp]),
     "arap_deform": (C.c_int, [_P, _I32, _dp]),
@@ -104,6 +105,7 @@ SIGNATURES = {
     "arap_deform_async": (C.c_int, [_P, _I32, _dp]),
     "arap_wait": (C.c_int, [_P]),
     "arap_set_graphs": (C.c_int, [_P, _I32]),
+    "arap_set_symbolic_cache": (C.c_int, [_P, _I32]),
     "arap_set_solve_ctas": (C.c_int, [_P, _I32]),
     "arap_set_pose_tile": (C.c_int, [_P, _I32]),
     "arap_energy": (C.c_int, [_P, _dp]),
@@ -223,6 +225,16 @@ class ArapContext:
 
     def set_precision(self, precision: str = "fp64", refine_steps: int = 1):
         self._check(self.lib.arap_set_precision(self.h, PRECISION[precision], int(refine_steps)))
+
+    def set_symbolic_cache(self, enable: bool = True):
+        """False: every dirty deform redoes the symbolic analysis, as the
+        reference's SimplicialLDLT::compute does."""
+        self._check(self.lib.arap_set_symbolic_cache(self.h, 1 if enable else 0))
+
+    def set_factor_precision(self, bits: int = 64):
+        """Mixed form: 64 = FP64 numeric factor rounded to FP32 for the solves
+        (default), 32 = FP32 factor."""
+        self._check(self.lib.arap_set_factor_precision(self.h, int(bits)))
 
     def set_rest_positions(self, xyz: np.ndarray):
         a = np.ascontiguousarray(xyz, dtype=np.float64).reshape(self.V, 3)

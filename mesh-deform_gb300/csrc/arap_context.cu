@@ -116,8 +116,12 @@ struct arap_ctx {
     std::vector<uint8_t> cmask;   // V
     int precision = ARAP_PRECISION_FP64;
     int refine = 1;
+    // numeric factorisation of the mixed form: 64 (FP64 factor, rounded to FP32
+    // copies for the solves) or 32 (FP32 factor)
+    int factor_bits = 64;
     bool dirty = true;
     bool retarget = false;  // same constrained set, new targets: reuse weights and factor
+    bool sym_cache = true;  // keep the symbolic analysis while the constrained set is unchanged
     // symbolic cache (keyed by the constrained-vertex mask)
     bool sym_valid = false;  // analysed and uploaded
     bool sym_host = false;   // analysed (host only)
@@ -133,6 +137,7 @@ struct arap_ctx {
     DevBuf rest, targets, out;
     DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn, fitems;
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T, redge;
+    DevBuf X64, L21_64, L21T_64, Ttop64;  // the mixed form's FP64 factor outputs (rounded into Xinv, L21, L21T, Ttop)
     DevBuf errw, ticket, flags, energy;
     DevBuf cidx_dev, handle_dev, tabs_dev;  // arap_pose_targets inputs
     DevBuf vf_ptr, vf_face, fnorm, vnorm;    // vertex normals
@@ -190,7 +195,8 @@ struct arap_ctx {
                 &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
                 &errw, &ticket, &flags, &energy, &cidx_dev, &handle_dev, &tabs_dev, &vf_ptr, &vf_face, &fnorm,
                 &vnorm, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout, &bftop, &bytop, &bws,
-                &bticket, &bflags, &top_col, &top_gptr, &top_gidx, &tdpos, &top_items, &Ttop, &ytop};
+                &bticket, &bflags, &top_col, &top_gptr, &top_gidx, &tdpos, &top_items, &Ttop, &ytop, &X64, &L21_64,
+                &L21T_64, &Ttop64};
     }
 };
 
@@ -342,14 +348,24 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     add(ctx->b, m1 * sizeof(Vec4<T>));
     add(ctx->sol, m1 * sizeof(Vec4<T>));
     add(ctx->uvec, (size_t)std::max<int64_t>(s.uvec_size, 1) * sizeof(Vec4<T>));
-    add(ctx->Lval, (size_t)std::max<int64_t>(s.panel_size, 1) * sizeof(T));
-    add(ctx->Dinv, (size_t)std::max<int64_t>(s.dinv_size, 1) * sizeof(T));
-    add(ctx->Upd, (size_t)std::max<int64_t>(s.upd_size, 1) * sizeof(T));
+    // the factor's working arrays in the factor's precision; an FP64 factor of
+    // the mixed form also keeps FP64 solve arrays, rounded into the FP32 ones
+    const bool f64f = f32 && ctx->factor_bits == 64;
+    const size_t fs = f64f ? sizeof(double) : sizeof(T);
+    add(ctx->Lval, (size_t)std::max<int64_t>(s.panel_size, 1) * fs);
+    add(ctx->Dinv, (size_t)std::max<int64_t>(s.dinv_size, 1) * fs);
+    add(ctx->Upd, (size_t)std::max<int64_t>(s.upd_size, 1) * fs);
     add(ctx->Xinv, (size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T));
     add(ctx->L21, (size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T));
     add(ctx->L21T, (size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T));
     const int nt = choose_dense_top(s, dense_cap(ctx)).ncols;
     add(ctx->Ttop, std::max<size_t>(nt > 0 ? dense_top_elems(nt) : 0, 1) * sizeof(T));
+    if (f64f) {
+        add(ctx->X64, (size_t)std::max<int64_t>(s.x_size, 1) * sizeof(double));
+        add(ctx->L21_64, (size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(double));
+        add(ctx->L21T_64, (size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(double));
+        add(ctx->Ttop64, std::max<size_t>(nt > 0 ? dense_top_elems(nt) : 0, 1) * sizeof(double));
+    }
     add(ctx->ytop, std::max<size_t>(2 * (size_t)dense_ld(nt), 1) * sizeof(Vec4<T>));  // y_top, then f_top
     if (n_poses > 0) {
         const size_t P = (size_t)n_poses, VP = V * P, MP = m1 * P, nc = V - (size_t)s.m;
@@ -591,8 +607,43 @@ int setup_alloc(arap_ctx *ctx) {
     return ARAP_OK;
 }
 
+// Enqueues the numeric factorisation in precision TF: the constrained
+// Laplacian assembled into the supernodal panels (and bFixed), the
+// multifrontal Cholesky plan level by level, the solve arrays X = inv(L11),
+// L21, L21^T, and the dense top's T = inv(L_top).
+template <typename TF>
+int factor_enqueue(arap_ctx *ctx, TF *Lval, TF *Upd, TF *Dinv, TF *X, TF *L21, TF *L21T, TF *Ttop) {
+    const Symbolic &s = ctx->sym;
+    const DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemsetAsync(Lval, 0, (size_t)s.panel_size * sizeof(TF), st));
+    if (s.upd_size > 0) CK(cudaMemsetAsync(Upd, 0, (size_t)s.upd_size * sizeof(TF), st));
+    CK(cudaMemsetAsync(X, 0, (size_t)s.x_size * sizeof(TF), st));
+    if (s.l21_size > 0) CK(cudaMemsetAsync(L21, 0, (size_t)s.l21_size * sizeof(TF), st));
+    if (s.l21t_size > 0) CK(cudaMemsetAsync(L21T, 0, (size_t)s.l21t_size * sizeof(TF), st));
+    {
+        Prof pr(ctx, ARAP_K_ASSEMBLE);
+        launch_assemble<TF>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), Lval, ctx->diag64.as<double>(),
+                            ctx->bfixed.as<Vec4<double>>(), st);
+    }
+    ctx->launches += 1;
+    for (const FactorLaunch &fl : s.fplan) {
+        Prof pr(ctx, ARAP_K_FACTOR);
+        launch_factor_step<TF>(d, fl, ctx->fitems.as<FItem>(), Lval, Upd, Dinv, X, L21, L21T, ctx->errw.as<int>(), st);
+        ctx->launches += 1;
+    }
+    if (d.n_top > 0) {
+        Prof pr(ctx, ARAP_K_FACTOR);
+        launch_top_inverse<TF>(d, X, L21, Ttop, st);
+        ctx->launches += 1;
+    }
+    CK(cudaGetLastError());
+    return ARAP_OK;
+}
+
 // Enqueues the dirty-deform setup in precision T (FP64: T = double for
-// everything; MIXED: T = float for the local step, RHS, factor and solves):
+// everything; MIXED: T = float for the local step, RHS and solves, with the
+// factor in FP64 unless factor_bits is 32):
 // cotan weights, geometry and constraint snap, rotations reset, Laplacian and
 // bFixed assembly, the factorisation plan. No host synchronisation; a failed
 // pivot shows up in the device error word.
@@ -624,28 +675,27 @@ int setup_enqueue(arap_ctx *ctx) {
     }
     ctx->launches += sizeof(T) == 4 ? 3 : 2;
     if (m > 0) {
-        CK(cudaMemsetAsync(ctx->Lval.p, 0, (size_t)s.panel_size * sizeof(T), st));
-        if (s.upd_size > 0) CK(cudaMemsetAsync(ctx->Upd.p, 0, (size_t)s.upd_size * sizeof(T), st));
-        CK(cudaMemsetAsync(ctx->Xinv.p, 0, (size_t)s.x_size * sizeof(T), st));
-        if (s.l21_size > 0) CK(cudaMemsetAsync(ctx->L21.p, 0, (size_t)s.l21_size * sizeof(T), st));
-        if (s.l21t_size > 0) CK(cudaMemsetAsync(ctx->L21T.p, 0, (size_t)s.l21t_size * sizeof(T), st));
-        {
-            Prof pr(ctx, ARAP_K_ASSEMBLE);
-            launch_assemble<T>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), ctx->Lval.as<T>(),
-                               ctx->diag64.as<double>(), ctx->bfixed.as<Vec4<double>>(), st);
-        }
-        ctx->launches += 1;
-        for (const FactorLaunch &fl : s.fplan) {
+        int rc;
+        if (sizeof(T) == 4 && ctx->factor_bits == 64) {
+            // FP64 numeric factorisation (arap.h:337 factors in double), then
+            // its solve arrays rounded to the FP32 copies the sweeps stream
+            rc = factor_enqueue<double>(ctx, ctx->Lval.as<double>(), ctx->Upd.as<double>(), ctx->Dinv.as<double>(),
+                                        ctx->X64.as<double>(), ctx->L21_64.as<double>(), ctx->L21T_64.as<double>(),
+                                        ctx->Ttop64.as<double>());
+            if (rc != ARAP_OK) return rc;
+            const double *src[4] = {ctx->X64.as<double>(), ctx->L21_64.as<double>(), ctx->L21T_64.as<double>(),
+                                    ctx->Ttop64.as<double>()};
+            float *dst[4] = {ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
+                             ctx->Ttop.as<float>()};
+            const int64_t n[4] = {s.x_size, s.l21_size, s.l21t_size,
+                                  d.n_top > 0 ? (int64_t)dense_top_elems(d.n_top) : 0};
             Prof pr(ctx, ARAP_K_FACTOR);
-            launch_factor_step<T>(d, fl, ctx->fitems.as<FItem>(), ctx->Lval.as<T>(), ctx->Upd.as<T>(),
-                                  ctx->Dinv.as<T>(), ctx->Xinv.as<T>(), ctx->L21.as<T>(), ctx->L21T.as<T>(),
-                                  ctx->errw.as<int>(), st);
+            launch_demote(4, src, dst, n, st);
             ctx->launches += 1;
-        }
-        if (d.n_top > 0) {
-            Prof pr(ctx, ARAP_K_FACTOR);
-            launch_top_inverse<T>(d, ctx->Xinv.as<T>(), ctx->L21.as<T>(), ctx->Ttop.as<T>(), st);
-            ctx->launches += 1;
+        } else {
+            rc = factor_enqueue<T>(ctx, ctx->Lval.as<T>(), ctx->Upd.as<T>(), ctx->Dinv.as<T>(), ctx->Xinv.as<T>(),
+                                   ctx->L21.as<T>(), ctx->L21T.as<T>(), ctx->Ttop.as<T>());
+            if (rc != ARAP_OK) return rc;
         }
     }
     CK(cudaGetLastError());
@@ -994,6 +1044,8 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->topo = src->topo;
     ctx->precision = src->precision;
     ctx->refine = src->refine;
+    ctx->factor_bits = src->factor_bits;
+    ctx->sym_cache = src->sym_cache;
     ctx->use_graphs = src->use_graphs;
     ctx->solve_cap = src->solve_cap;
     ctx->top_bytes = src->top_bytes;
@@ -1034,6 +1086,20 @@ int arap_set_precision(arap_ctx *ctx, int32_t precision, int32_t refine_steps) {
     ctx->precision = precision;
     ctx->refine = refine_steps;
     ctx->dirty = true;
+    return ARAP_OK;
+}
+
+int arap_set_factor_precision(arap_ctx *ctx, int32_t bits) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (bits != 32 && bits != 64) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "factor precision must be 32 or 64 bits");
+    if (bits != ctx->factor_bits) {
+        ctx->factor_bits = bits;
+        ctx->dirty = true;
+    }
     return ARAP_OK;
 }
 
@@ -1118,6 +1184,7 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
             launch_face_cots(ctx->dt, ctx->rest.as<double>(), ctx->hc.as<double>(), st);
         }
         ctx->launches += 1;
+        if (!ctx->sym_cache) ctx->sym_host = ctx->sym_valid = false;  // analyse again, as SimplicialLDLT::compute
         int rc = prepare_symbolic(ctx);
         if (rc != ARAP_OK) return rc;
         rc = setup_alloc<float>(ctx);
@@ -1372,6 +1439,7 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
             ctx->have_rotations = false;
             return ARAP_OK;
         }
+        if (!ctx->sym_cache) ctx->sym_host = ctx->sym_valid = false;  // analyse again, as SimplicialLDLT::compute
         int rc = prepare_symbolic(ctx);
         if (rc != ARAP_OK) return rc;
         if (fp64 && !ctx->fp64_solves)
@@ -1381,7 +1449,7 @@ int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz) {
         rc = fp64 ? setup_alloc<double>(ctx) : setup_alloc<float>(ctx);
         if (rc != ARAP_OK) return rc;
         h2 = HClock::now();
-        const int64_t key[4] = {ctx->gen, fp64 ? 1 : 2, 0, 0};
+        const int64_t key[4] = {ctx->gen, fp64 ? 1 : 2, fp64 ? 64 : ctx->factor_bits, 0};
         rc = graph_or_direct(ctx, ctx->g_setup, ctx->g_setup_key, key, ctx->g_setup_launches, [&] {
             return fp64 ? setup_enqueue<double>(ctx) : setup_enqueue<float>(ctx);
         });
@@ -1570,6 +1638,16 @@ int arap_set_dense_top(arap_ctx *ctx, int32_t max_columns) {
         ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
         ctx->dirty = true;
     }
+    return ARAP_OK;
+}
+
+int arap_set_symbolic_cache(arap_ctx *ctx, int32_t enable) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    ctx->sym_cache = enable != 0;
     return ARAP_OK;
 }
 
@@ -1879,11 +1957,17 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
         B = V * (24 + 24 + 3 * sz * 2 + 9 * sz) + m * (8 + 3 * sz) + nnz * (4 + 8 + 8);
         FL = nnz * 4;
         break;
-    case ARAP_K_FACTOR:
-        B = (double)s.panel_size * sz * 2 + (double)s.upd_size * sz * 2 + (double)s.dinv_size * sz +
-            (xlow + l21) * sz;
+    case ARAP_K_FACTOR: {
+        // in the factor's precision; an FP64 factor of the mixed form also
+        // writes the FP32 solve copies (and reads the FP64 ones back once)
+        const bool f64f = ctx->state_prec == ARAP_PRECISION_MIXED && ctx->factor_bits == 64;
+        const double fz = f64f ? 8.0 : sz;
+        B = (double)s.panel_size * fz * 2 + (double)s.upd_size * fz * 2 + (double)s.dinv_size * fz +
+            (xlow + l21) * fz;
+        if (f64f) B += (double)(s.x_size + s.l21_size + s.l21t_size) * (8 + 4) + 2 * nt * nt * (8 + 4);
         FL = s.factor_flops;
         break;
+    }
     case ARAP_K_LOCAL:
         if (sz == 8.0)  // rest + current positions, rotations out, adjacency + weights
             B = V * 3 * sz + P * V * (3 * sz + 9 * sz) + 4 * (V + 1) + nnz * (4 + sz);

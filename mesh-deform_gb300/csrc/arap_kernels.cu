@@ -1991,6 +1991,31 @@ __global__ void k_gather_rotations(int V, const int32_t *__restrict__ oldidx, co
 
 inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
+// FP64 factor outputs rounded to FP32 for the solves: up to four arrays in
+// one launch, four elements per thread and step (32-byte loads, 16-byte
+// stores; the allocations are 256-byte aligned), grid-stride over each array.
+struct DemoteJob {
+    const double *src[4];
+    float *dst[4];
+    int64_t n[4];
+};
+
+__global__ void __launch_bounds__(256) k_demote(DemoteJob job) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll 1
+    for (int a = 0; a < 4; ++a) {
+        const double *__restrict__ src = job.src[a];
+        float *__restrict__ dst = job.dst[a];
+        const int64_t n = job.n[a], n4 = n / 4;
+        for (int64_t q = t0; q < n4; q += stride) {
+            const Vec4<double> v = reinterpret_cast<const Vec4<double> *>(src)[q];
+            reinterpret_cast<float4 *>(dst)[q] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+        }
+        for (int64_t i = 4 * n4 + t0; i < n; i += stride) dst[i] = (float)src[i];
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -2098,6 +2123,27 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
                      const Vec4<float> *b, const Vec4<double> *x64, Vec4<float> *r, cudaStream_t st) {
     if (s.m == 0) return;
     k_residual<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, bfixed, b, x64, r);
+}
+
+void launch_demote(int count, const double *const *src, float *const *dst, const int64_t *n, cudaStream_t st) {
+    DemoteJob job{};
+    int64_t most = 0;
+    for (int a = 0; a < 4; ++a) {
+        const bool use = a < count && n[a] > 0 && src[a] && dst[a];
+        job.src[a] = use ? src[a] : nullptr;
+        job.dst[a] = use ? dst[a] : nullptr;
+        job.n[a] = use ? n[a] : 0;
+        most = std::max(most, job.n[a]);
+    }
+    if (most == 0) return;
+    static const int sms = [] {  // initialised once, thread-safe
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 1;
+        return v;
+    }();
+    const int grid = std::max(1, std::min(blocks_for((most + 3) / 4, 256), 8 * sms));
+    k_demote<<<grid, 256, 0, st>>>(job);
 }
 
 int solve_chunk_bytes() { return kChunkBytes; }

@@ -93,6 +93,9 @@ void launch_rhs_mixed(const DevSym &s, const float *w32, const Vec4<float> *redg
 template <typename TF>
 void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *items, TF *Lval, TF *Upd, TF *Dinv,
                         TF *X, TF *L21, TF *L21T, int *err, cudaStream_t st);
+// FP64 factor outputs (X, L21, L21^T, the dense top's T) rounded to the FP32
+// copies the mixed form's solves read: count <= 4 arrays of n[a] elements
+void launch_demote(int count, const double *const *src, float *const *dst, const int64_t *n, cudaStream_t st);
 // local step: covariance + rotation fit (estimateRotations arap.h:354-384)
 template <typename T>
 void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *pc, Vec4<T> *R,

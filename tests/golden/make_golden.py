@@ -1,8 +1,8 @@
 """Regenerates the golden fixtures in tests/golden/ from the reference tree.
 
-Run in a checkout that has the reference mounted (default /root/reference):
+Run with the path of a checkout of the reference (a required argument):
 
-    python tests/golden/make_golden.py [/path/to/mesh-deform]
+    python tests/golden/make_golden.py /path/to/mesh-deform
 
 It reads, as text, without compiling or running anything of the reference:
   * tests/test_cotan.cpp:26-51   the cotan known-answer test (unit square in
@@ -127,4 +127,6 @@ def write_oracle_deforms():
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py /path/to/mesh-deform")
+    main(Path(sys.argv[1]))
