@@ -207,6 +207,17 @@ int arap_set_dense_top(arap_ctx *ctx, int32_t max_columns);
 /* arap_ordering of the next symbolic analysis (marks the context dirty). */
 int arap_set_ordering(arap_ctx *ctx, int32_t mode);
 
+/* Failure detection: the most polls a triangular-solve task makes while it
+   waits for another task's completion flag (0, the default: 2^24 polls of
+   20-200 ns, a few seconds). When a wait runs out, the kernel records it,
+   every CTA of the launch leaves at its next task, the rest of the deform's
+   solve launches leave at once, and arap_wait (arap_deform) returns
+   ARAP_ERR_TIMEOUT; the context rebuilds its scheduling state, so the next
+   deform is correct. Waits of a CTA for its own bulk copies are not limited
+   by this value. No counterpart in the reference (whose solves are
+   sequential). */
+int arap_set_wait_limit(arap_ctx *ctx, int32_t polls);
+
 /* enable != 0 (the default) keeps the symbolic analysis (ordering,
    elimination tree, supernodes, factorisation plan) of a constrained-vertex
    set for later dirty deforms of the same set, which then only refactor

@@ -106,6 +106,7 @@ SIGNATURES = {
     "arap_wait": (C.c_int, [_P]),
     "arap_set_graphs": (C.c_int, [_P, _I32]),
     "arap_set_symbolic_cache": (C.c_int, [_P, _I32]),
+    "arap_set_wait_limit": (C.c_int, [_P, _I32]),
     "arap_set_solve_ctas": (C.c_int, [_P, _I32]),
     "arap_set_pose_tile": (C.c_int, [_P, _I32]),
     "arap_energy": (C.c_int, [_P, _dp]),
@@ -225,6 +226,10 @@ class ArapContext:
 
     def set_precision(self, precision: str = "fp64", refine_steps: int = 1):
         self._check(self.lib.arap_set_precision(self.h, PRECISION[precision], int(refine_steps)))
+
+    def set_wait_limit(self, polls: int = 0):
+        """Poll limit of the solves' waits for another task (0: the default)."""
+        self._check(self.lib.arap_set_wait_limit(self.h, int(polls)))
 
     def set_symbolic_cache(self, enable: bool = True):
         """False: every dirty deform redoes the symbolic analysis, as the

@@ -33,8 +33,10 @@ __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ void wait_flag(const unsigned *p, unsigned target, int *err) {
-    for (unsigned it = 0; it < kSpinLimit; ++it) {
+    const unsigned lim = flag_wait_limit(err);
+    for (unsigned it = 0;; ++it) {
         if (ld_acquire(p) >= target) return;
+        if (it >= lim) break;
         __nanosleep(it < 64 ? 20 : 200);
     }
     atomicOr(err, kErrTimeout);

@@ -983,7 +983,9 @@ int finish_create(arap_ctx *ctx, int device, const arap_ctx *src, arap_ctx **out
         return bail(e, "alloc");
     if ((e = ctx->out.ensure((size_t)9 * std::max(n_vertices, 1) * sizeof(double))) != cudaSuccess)
         return bail(e, "alloc");
-    if ((e = ctx->errw.ensure(sizeof(int))) != cudaSuccess) return bail(e, "alloc");
+    // status word: error bits, then the flag-wait poll limit (0: the default)
+    if ((e = ctx->errw.ensure(2 * sizeof(int))) != cudaSuccess) return bail(e, "alloc");
+    if ((e = cudaMemsetAsync(ctx->errw.p, 0, 2 * sizeof(int), ctx->stream)) != cudaSuccess) return bail(e, "memset");
     if (!(ctx->herr_host = pinned_words().get())) return bail(cudaErrorMemoryAllocation, "pinned error word");
     *ctx->herr_host = 0;
     if (src && src->have_rest) {
@@ -1638,6 +1640,20 @@ int arap_set_dense_top(arap_ctx *ctx, int32_t max_columns) {
         ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
         ctx->dirty = true;
     }
+    return ARAP_OK;
+}
+
+int arap_set_wait_limit(arap_ctx *ctx, int32_t polls) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (polls < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "negative poll limit");
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    CK(cudaSetDevice(ctx->device));
+    const int v = polls;
+    CK(cudaMemcpyAsync(ctx->errw.as<int>() + 1, &v, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return ARAP_OK;
 }
 

@@ -27,6 +27,17 @@ constexpr int kErrTimeout = 2;
 // the bound is a few seconds).
 constexpr unsigned kSpinLimit = 1u << 24;
 
+// The context's device status word is two ints: err[0] collects the error
+// bits of a deform, err[1] is the poll limit of the waits for another task's
+// flag (0: kSpinLimit), set by arap_set_wait_limit. The waits for a CTA's own
+// bulk copies always use kSpinLimit, so that no copy is left in flight.
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned flag_wait_limit(const int *err) {
+    const unsigned v = (unsigned)__ldcg(err + 1);
+    return v == 0u ? kSpinLimit : v;
+}
+#endif
+
 struct DevTopo {
     int V, F, nnz;
     const int32_t *faces;    // 3F (original vertex ids)

@@ -21,30 +21,63 @@
  *   - the result is written back through the adapter, cast to Mesh::Scalar
  *     (arap.h:133-135).
  * Precision: PrecisionType = double runs the FP64 GPU form; float runs the
- * mixed form (FP32 local step and solves with FP64-residual refinement), which
- * is more accurate than the reference's all-float path.
+ * mixed form (FP64 factor, FP32 local step and solves with FP64-residual
+ * refinement), which is more accurate than the reference's all-float path.
+ *
+ * Test access: as in the reference (arap.h:28,141,445,453), the private
+ * typedef SparseMatrix and the member _edgeWeights are reachable from the
+ * friend template PrivateAccessor<ARAP>, so an accessor that returns
+ * `typename ARAP::SparseMatrix` from `a._edgeWeights` works unchanged.
+ * SparseMatrix is Eigen::SparseMatrix<Scalar, Eigen::RowMajor> when Eigen's
+ * headers are on the include path (define DEFORM_NO_EIGEN to opt out), else
+ * deform::SparseRowMatrix<Scalar>. _edgeWeights reads the weights from the
+ * device when it is converted to SparseMatrix; before the first deform it is
+ * an empty matrix, as the reference's member is.
+ *
+ * No device: the constructor does not throw (the reference's cannot fail);
+ * deform then returns false and lastError() says why.
  */
 #ifndef DEFORM_ARAP_H
 #define DEFORM_ARAP_H
 
 #include <arap_gpu.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <map>
-#include <stdexcept>
 #include <string>
 #include <type_traits>
 #include <vector>
+
+#if !defined(DEFORM_NO_EIGEN) && defined(__has_include)
+#if __has_include(<Eigen/Sparse>)
+#include <Eigen/Sparse>
+#define DEFORM_HAVE_EIGEN 1
+#endif
+#endif
 
 namespace deform {
 
 /** Forward declaration of a class with access to internals (tests), as arap.h:28. */
 template <class T> class PrivateAccessor;
 
-/** Compressed sparse rows of _edgeWeights. */
-struct EdgeWeightsCSR {
-    std::vector<int32_t> rowptr, col;
-    std::vector<double> val;
+/** Row-major compressed sparse matrix: the form of _edgeWeights when Eigen is
+    not available. Columns are sorted within each row. */
+template <class S>
+struct SparseRowMatrix {
+    typedef S Scalar;
+    int32_t n = 0;
+    std::vector<int32_t> rowptr{0}, col;
+    std::vector<S> val;
+    int rows() const { return n; }
+    int cols() const { return n; }
+    int nonZeros() const { return (int)col.size(); }
+    /** Entry (r, c), zero where the pattern has none. */
+    S coeff(int r, int c) const {
+        const auto b = col.begin() + rowptr[r], e = col.begin() + rowptr[r + 1];
+        const auto it = std::lower_bound(b, e, c);
+        return (it != e && *it == c) ? val[it - col.begin()] : S(0);
+    }
 };
 
 template <class MeshType, class PrecisionType = typename MeshType::Scalar>
@@ -58,7 +91,7 @@ public:
     typedef int Index;
 
     /** Construct from mesh; the mesh must outlive this object. device: CUDA ordinal. */
-    AsRigidAsPossibleDeformation(Mesh &mesh, int device = 0) : _mesh(mesh), _dirty(true) {
+    AsRigidAsPossibleDeformation(Mesh &mesh, int device = 0) : _mesh(mesh), _edgeWeights(this), _dirty(true) {
         initializeMeshTopology(device);
     }
 
@@ -77,6 +110,8 @@ public:
     /** Run numberOfIterations local/global iterations (arap.h:101-138). */
     bool deform(Index numberOfIterations) {
         const Index V = _mesh.numberOfVertices();
+        if (!_ctx) return false;  // no device (lastError() says why)
+        const bool was_dirty = _dirty;
         if (_dirty) {
             std::vector<double> xyz((size_t)3 * V);
             for (Index v = 0; v < V; ++v) {
@@ -100,6 +135,7 @@ public:
             _lastError = arap_last_error(_ctx);
             return false;
         }
+        if (was_dirty) _weightsValid = true;
         if (_constrainedLocations.empty()) return true;  // arap.h:113-114
         _dirty = false;
         typedef typename std::decay<decltype(_mesh.vertexLocation(0))>::type VertexType;
@@ -114,9 +150,10 @@ public:
     /** Message of the last failed deform (empty when none). */
     const std::string &lastError() const { return _lastError; }
 
-    /** Extension: refinement solves per iteration of the mixed form (default 2). */
+    /** Extension: refinement solves per iteration of the mixed form beyond the
+        first (default 2). */
     void setRefinementSteps(int steps) {
-        arap_set_precision(_ctx, precision(), steps);
+        if (_ctx) arap_set_precision(_ctx, precision(), steps);
         _dirty = true;
     }
 
@@ -124,6 +161,51 @@ private:
     template <class> friend class PrivateAccessor;
 
     struct Point { Scalar v[3]; };
+
+#ifdef DEFORM_HAVE_EIGEN
+    typedef Eigen::SparseMatrix<Scalar, Eigen::RowMajor> SparseMatrix;
+#else
+    typedef SparseRowMatrix<Scalar> SparseMatrix;
+#endif
+
+    /** _edgeWeights: the cotan weights of the last dirty deform
+        (computeCotanWeights, arap.h:182-239), read from the device when
+        converted to SparseMatrix. */
+    class EdgeWeights {
+    public:
+        explicit EdgeWeights(const AsRigidAsPossibleDeformation *owner) : _owner(owner) {}
+        operator SparseMatrix() const {
+            const int n = _owner->_weightsValid ? _owner->_mesh.numberOfVertices() : 0;
+            std::vector<int32_t> rowptr((size_t)n + 1, 0), col;
+            std::vector<double> val;
+            if (n > 0) {
+                int32_t nnz = 0;
+                arap_edge_weights_nnz(_owner->_ctx, &nnz);
+                col.resize(nnz);
+                val.resize(nnz);
+                arap_get_edge_weights(_owner->_ctx, rowptr.data(), col.data(), val.data());
+            }
+#ifdef DEFORM_HAVE_EIGEN
+            SparseMatrix m(n, n);
+            std::vector<Eigen::Triplet<Scalar>> t;
+            t.reserve(col.size());
+            for (int r = 0; r < n; ++r)
+                for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) t.emplace_back(r, col[q], Scalar(val[q]));
+            m.setFromTriplets(t.begin(), t.end());
+            return m;
+#else
+            SparseMatrix m;
+            m.n = n;
+            m.rowptr = rowptr;
+            m.col = col;
+            m.val.assign(val.begin(), val.end());
+            return m;
+#endif
+        }
+
+    private:
+        const AsRigidAsPossibleDeformation *_owner;
+    };
 
     static int precision() {
         return std::is_same<Scalar, double>::value ? ARAP_PRECISION_FP64 : ARAP_PRECISION_MIXED;
@@ -137,25 +219,17 @@ private:
             for (int c = 0; c < 3; ++c) faces[(size_t)3 * f + c] = static_cast<int32_t>(t(c));
         }
         const int rc = arap_create(_mesh.numberOfVertices(), F, faces.data(), device, &_ctx);
-        if (rc != ARAP_OK)
-            throw std::runtime_error(std::string("arap_create: ") + arap_status_string(rc) + ": " +
-                                     arap_last_error(nullptr));
+        if (rc != ARAP_OK) {
+            _ctx = nullptr;
+            _lastError = std::string("arap_create: ") + arap_status_string(rc) + ": " + arap_last_error(nullptr);
+            return;
+        }
         arap_set_precision(_ctx, precision(), 2);
     }
 
-    /** _edgeWeights (arap.h:453) as CSR, for PrivateAccessor. */
-    EdgeWeightsCSR edgeWeights() const {
-        EdgeWeightsCSR w;
-        int32_t nnz = 0;
-        arap_edge_weights_nnz(_ctx, &nnz);
-        w.rowptr.resize((size_t)_mesh.numberOfVertices() + 1);
-        w.col.resize(nnz);
-        w.val.resize(nnz);
-        arap_get_edge_weights(_ctx, w.rowptr.data(), w.col.data(), w.val.data());
-        return w;
-    }
-
     Mesh &_mesh;
+    EdgeWeights _edgeWeights;
+    bool _weightsValid = false;
     arap_ctx *_ctx = nullptr;
     std::map<Index, Point> _constrainedLocations;
     bool _dirty;

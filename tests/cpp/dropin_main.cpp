@@ -6,6 +6,15 @@
 //   dropin_main run <in> <out> <float|double>
 //                                        reads a mesh + constraints + iteration count,
 //                                        deforms through the template, writes positions
+//   dropin_main nodevice                 construction and the accessor without a GPU:
+//                                        no exception, an empty weight matrix before the
+//                                        first deform, deform() false with a message
+//
+// The weights are read through PrivateAccessor<ARAP>::cotanWeights, which
+// returns `typename ARAP::SparseMatrix` from `a._edgeWeights`, the contract of
+// the reference's tests/accessor.h. Built with -DDEFORM_REFERENCE_ACCESSOR and
+// the reference's tests/ directory on the include path, that file itself is
+// used; otherwise an accessor of the same shape is defined here.
 #include <deform/arap.h>
 #include <deform/array_adapter.h>
 
@@ -14,13 +23,17 @@
 #include <cstring>
 #include <vector>
 
+#ifdef DEFORM_REFERENCE_ACCESSOR
+#include <accessor.h>
+#else
 namespace deform {
 template <class ARAP>
 class PrivateAccessor {
 public:
-    static EdgeWeightsCSR cotanWeights(const ARAP &a) { return a.edgeWeights(); }
+    static typename ARAP::SparseMatrix cotanWeights(const ARAP &a) { return a._edgeWeights; }
 };
 }  // namespace deform
+#endif
 
 static int kat() {
     typedef deform::ArrayMeshAdapter<float> Mesh;
@@ -34,11 +47,11 @@ static int kat() {
     typedef deform::AsRigidAsPossibleDeformation<Mesh> ARAP;
     ARAP arap(m);
     if (!arap.deform(0)) { std::printf("deform(0) failed\n"); return 1; }
-    deform::EdgeWeightsCSR w = deform::PrivateAccessor<ARAP>::cotanWeights(arap);
-    if (w.rowptr.size() != 5) { std::printf("rows %zu\n", w.rowptr.size()); return 1; }
+    const auto w = deform::PrivateAccessor<ARAP>::cotanWeights(arap);
+    if (w.rows() != 4 || w.cols() != 4) { std::printf("size %d x %d\n", (int)w.rows(), (int)w.cols()); return 1; }
     double sp[4][4] = {{0}};
     for (int i = 0; i < 4; ++i)
-        for (int q = w.rowptr[i]; q < w.rowptr[i + 1]; ++q) sp[i][w.col[q]] = w.val[q];
+        for (int j = 0; j < 4; ++j) sp[i][j] = w.coeff(i, j);
     const double expected[4][4] = {{0, .5, 0, .5}, {.5, 0, .5, 0}, {0, .5, 0, .5}, {.5, 0, .5, 0}};
     double d2 = 0, a2 = 0, b2 = 0;
     for (int i = 0; i < 4; ++i)
@@ -82,8 +95,26 @@ static int run(const char *in, const char *out) {
     return 0;
 }
 
+static int nodevice() {
+    typedef deform::ArrayMeshAdapter<double> Mesh;
+    Mesh m;
+    m.addVertex(0., 0., 0.);
+    m.addVertex(1., 0., 0.);
+    m.addVertex(0., 1., 0.);
+    m.addFace(0, 1, 2);
+    typedef deform::AsRigidAsPossibleDeformation<Mesh> ARAP;
+    ARAP arap(m);  // must not throw
+    const auto w = deform::PrivateAccessor<ARAP>::cotanWeights(arap);
+    if (w.rows() != 0 || w.nonZeros() != 0) { std::printf("weights before deform not empty\n"); return 1; }
+    arap.setConstraint(0, deform::Vec3<double>(0., 0., 1.));
+    const bool ok = arap.deform(1);
+    std::printf("nodevice deform=%d error=%s\n", ok ? 1 : 0, arap.lastError().c_str());
+    return ok ? 3 : 0;
+}
+
 int main(int argc, char **argv) {
     if (argc >= 2 && std::strcmp(argv[1], "kat") == 0) return kat();
+    if (argc >= 2 && std::strcmp(argv[1], "nodevice") == 0) return nodevice();
     if (argc >= 5 && std::strcmp(argv[1], "run") == 0)
         return std::strcmp(argv[4], "float") == 0 ? run<float>(argv[2], argv[3]) : run<double>(argv[2], argv[3]);
     std::printf("usage: dropin_main kat | run <in> <out> <float|double>\n");

@@ -16,23 +16,60 @@ SRC = ROOT / "tests" / "cpp" / "dropin_main.cpp"
 OUT = ROOT / "tests" / "cpp" / "_build"
 
 
-def build_dropin() -> Path:
+def build_dropin(reference_tests: Path | None = None) -> Path:
+    """Compiles tests/cpp/dropin_main.cpp against the drop-in; with
+    reference_tests, the reference's own tests/accessor.h is used unchanged."""
     import build_lib
 
     lib = build_lib.build()
     OUT.mkdir(exist_ok=True)
-    exe = OUT / "dropin_main"
-    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", f"-I{PKG}", f"-I{ROOT / 'include'}", str(SRC),
-           f"-L{PKG}", "-larap_gb300", f"-Wl,-rpath,{PKG}", "-o", str(exe)]
+    exe = OUT / ("dropin_main_refaccessor" if reference_tests else "dropin_main")
+    extra = ["-DDEFORM_REFERENCE_ACCESSOR", f"-I{reference_tests}"] if reference_tests else []
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", f"-I{PKG}", f"-I{ROOT / 'include'}"] + extra + \
+        [str(SRC), f"-L{PKG}", "-larap_gb300", f"-Wl,-rpath,{PKG}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert lib.exists()
     return exe
 
 
+def _has_gpu() -> bool:
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
 def test_dropin_header_compiles_and_links(built):
     exe = build_dropin()
     assert exe.exists()
+
+
+def test_dropin_with_the_reference_accessor(built):
+    """The reference's tests/accessor.h (PrivateAccessor returning
+    typename ARAP::SparseMatrix from a._edgeWeights) compiles unchanged
+    against the drop-in. Needs a checkout of the reference: ARAP_REFERENCE_DIR,
+    else a directory named `reference` beside this repository."""
+    import os
+
+    ref = Path(os.environ.get("ARAP_REFERENCE_DIR", str(ROOT.parent / "reference"))) / "tests"
+    if not (ref / "accessor.h").exists():
+        pytest.skip("no reference checkout")
+    exe = build_dropin(ref)
+    if not _has_gpu():
+        r = subprocess.run([str(exe), "nodevice"], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_dropin_without_device_does_not_throw(built):
+    if _has_gpu():
+        pytest.skip("a GPU is present")
+    exe = build_dropin()
+    r = subprocess.run([str(exe), "nodevice"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "deform=0" in r.stdout and "arap_create" in r.stdout
 
 
 @pytest.mark.gpu
