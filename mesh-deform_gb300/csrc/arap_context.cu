@@ -1815,7 +1815,7 @@ int arap_get_symbolic_sizes(arap_ctx *ctx, int32_t *n_free, int32_t *n_blocks, i
     if (!ctx->sym_valid) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "no symbolic analysis yet");
     if (n_free) *n_free = ctx->sym.m;
     if (n_blocks) *n_blocks = ctx->sym.S;
-    if (factor_nnz) *factor_nnz = ctx->sym.factor_nnz;
+    if (factor_nnz) *factor_nnz = symbolic_factor_nnz(ctx->sym);
     return ARAP_OK;
 }
 
@@ -1860,7 +1860,7 @@ int arap_analyze_pattern(int32_t n_vertices, int32_t n_faces, const int32_t *fac
     }
     if (n_free) *n_free = s.m;
     if (n_blocks) *n_blocks = s.S;
-    if (factor_nnz) *factor_nnz = s.factor_nnz;
+    if (factor_nnz) *factor_nnz = symbolic_factor_nnz(s);
     if (perm && s.m) std::memcpy(perm, s.perm.data(), (size_t)s.m * sizeof(int32_t));
     if (etree && s.m) std::memcpy(etree, s.etree.data(), (size_t)s.m * sizeof(int32_t));
     if (block_ptr) std::memcpy(block_ptr, s.block_ptr.data(), s.block_ptr.size() * sizeof(int32_t));

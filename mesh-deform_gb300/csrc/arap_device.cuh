@@ -16,51 +16,59 @@ template <typename T> struct Eps;
 template <> struct Eps<float> { static constexpr float v = 1.1920929e-07f; };
 template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; };
 
-// Classical cyclic Jacobi on a symmetric 3x3 (Golub & Van Loan, Alg. 8.5.3):
-// a -> diag(lambda), v = eigenvectors (columns).
+// One-sided (Hestenes) Jacobi on a 3x3 matrix (Golub & Van Loan, Sec. 8.6.3;
+// Demmel & Veselic 1992): plane rotations from the right orthogonalise the
+// columns of B = S J1 J2 ..., V accumulates the rotations. On exit the columns
+// of B are sigma_i u_i and those of V the right singular vectors. Working on S
+// itself, not on S^T S, keeps the small singular directions accurate in FP32
+// (the one-rings stretched close to rank one in the first iterations of a
+// large handle move).
 template <typename T>
-__device__ __forceinline__ void jacobi_eig3(T a[3][3], T v[3][3]) {
+__device__ __forceinline__ void hestenes3(T B[3][3], T V[3][3]) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? (T)1 : (T)0;
-    const int sweeps = sizeof(T) == 4 ? 6 : 10;
+        for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? (T)1 : (T)0;
+    const int sweeps = sizeof(T) == 4 ? 8 : 12;
     for (int sw = 0; sw < sweeps; ++sw) {
-        const T off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
-        const T dia = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
-        if (off <= Eps<T>::v * Eps<T>::v * dia) break;
+        bool rotated = false;
 #pragma unroll
         for (int pq = 0; pq < 3; ++pq) {
             const int p = pq == 2 ? 1 : 0;
             const int q = pq == 0 ? 1 : 2;
-            const int r = 3 - p - q;
-            const T apq = a[p][q];
-            if (apq == (T)0) continue;
-            const T theta = (a[q][q] - a[p][p]) / ((T)2 * apq);
-            T t = (T)1 / (fabs(theta) + tsqrt(theta * theta + (T)1));
-            if (theta < (T)0) t = -t;
-            const T c = (T)1 / tsqrt(t * t + (T)1);
-            const T s = t * c;
-            const T tau = s / ((T)1 + c);
-            a[p][p] -= t * apq;
-            a[q][q] += t * apq;
-            a[p][q] = a[q][p] = (T)0;
-            const T arp = a[r][p], arq = a[r][q];
-            a[r][p] = a[p][r] = arp - s * (arq + tau * arp);
-            a[r][q] = a[q][r] = arq + s * (arp - tau * arq);
+            const T a = B[0][p] * B[0][p] + B[1][p] * B[1][p] + B[2][p] * B[2][p];
+            const T b = B[0][q] * B[0][q] + B[1][q] * B[1][q] + B[2][q] * B[2][q];
+            const T g = B[0][p] * B[0][q] + B[1][p] * B[1][q] + B[2][p] * B[2][q];
+            if (fabs(g) <= Eps<T>::v * tsqrt(a * b)) continue;  // columns orthogonal to working precision
+            rotated = true;
+            // t = tan of the angle that makes the new columns orthogonal, the
+            // root of t^2 + 2 zeta t - 1 = 0 of smaller magnitude
+            const T zeta = (b - a) / ((T)2 * g);
+            const T az = fabs(zeta);
+            const T r = az > (T)1 ? az * tsqrt((T)1 + (T)1 / (az * az)) : tsqrt((T)1 + az * az);
+            const T t = (zeta < (T)0 ? (T)-1 : (T)1) / (az + r);
+            const T c = (T)1 / tsqrt((T)1 + t * t);
+            const T sn = c * t;
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                const T vip = v[i][p], viq = v[i][q];
-                v[i][p] = vip - s * (viq + tau * vip);
-                v[i][q] = viq + s * (vip - tau * viq);
+                const T bp = B[i][p], bq = B[i][q];
+                B[i][p] = c * bp - sn * bq;
+                B[i][q] = sn * bp + c * bq;
+                const T vp = V[i][p], vq = V[i][q];
+                V[i][p] = c * vp - sn * vq;
+                V[i][q] = sn * vp + c * vq;
             }
         }
+        if (!rotated) break;
     }
 }
 
 // Best rotation R = V diag(1,1,det(V U^T)) U^T for cov = U S V^T (arap.h:376-382),
-// from the eigenvectors V of cov^T cov (proper, v3 = v1 x v2) and the proper
-// left factor u1 = cov v1/|.|, u2 = Gram-Schmidt(cov v2), u3 = u1 x u2.
+// from the one-sided Jacobi SVD of cov: the right singular vectors v1, v2 of
+// the two largest singular values and v3 = v1 x v2 (proper), the left ones
+// u1 = b1/|b1|, u2 = Gram-Schmidt(b2) and u3 = u1 x u2 (proper). With both
+// factors proper the sign of det(V U^T) lands on the smallest singular value,
+// as the reference's reflection fix puts it.
 template <typename T>
 __device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3]) {
     T f2 = (T)0;
@@ -76,36 +84,36 @@ __device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3])
         return;
     }
     const T sc = (T)1 / tsqrt(f2);
-    T S[3][3];
+    T B[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) S[i][j] = S_in[i][j] * sc;
-    T C[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) C[i][j] = S[0][i] * S[0][j] + S[1][i] * S[1][j] + S[2][i] * S[2][j];
+        for (int j = 0; j < 3; ++j) B[i][j] = S_in[i][j] * sc;
     T Vm[3][3];
-    jacobi_eig3(C, Vm);
-    // order eigenpairs descending
-    T lam[3] = {C[0][0], C[1][1], C[2][2]};
-    int o0 = 0, o1 = 1, o2 = 2;
-    if (lam[o1] > lam[o0]) { int t = o0; o0 = o1; o1 = t; }
-    if (lam[o2] > lam[o0]) { int t = o0; o0 = o2; o2 = t; }
-    if (lam[o2] > lam[o1]) { int t = o1; o1 = o2; o2 = t; }
-    T v1[3], v2[3], v3[3];
+    hestenes3(B, Vm);
+    // singular values (column norms of B), ordered descending
+    T nrm[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) { v1[i] = Vm[i][o0]; v2[i] = Vm[i][o1]; }
+    for (int j = 0; j < 3; ++j) nrm[j] = B[0][j] * B[0][j] + B[1][j] * B[1][j] + B[2][j] * B[2][j];
+    // indices of the largest and second largest (ties keep the lower index)
+    const int o0 = (nrm[1] > nrm[0]) ? ((nrm[2] > nrm[1]) ? 2 : 1) : ((nrm[2] > nrm[0]) ? 2 : 0);
+    const int lo = o0 == 0 ? 1 : 0, hi = o0 == 2 ? 1 : 2;  // the other two, lo < hi
+    const T nlo = lo == 0 ? nrm[0] : nrm[1], nhi = hi == 1 ? nrm[1] : nrm[2];
+    const int o1 = (nhi > nlo) ? hi : lo;
+    T v1[3], v2[3], v3[3];
+    T u1[3], u2[3], u3[3];
+    // columns picked by selects, not by indexing with o0/o1 (keeps every
+    // array in registers)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        v1[i] = o0 == 0 ? Vm[i][0] : (o0 == 1 ? Vm[i][1] : Vm[i][2]);
+        v2[i] = o1 == 0 ? Vm[i][0] : (o1 == 1 ? Vm[i][1] : Vm[i][2]);
+        u1[i] = o0 == 0 ? B[i][0] : (o0 == 1 ? B[i][1] : B[i][2]);
+        u2[i] = o1 == 0 ? B[i][0] : (o1 == 1 ? B[i][1] : B[i][2]);
+    }
     v3[0] = v1[1] * v2[2] - v1[2] * v2[1];
     v3[1] = v1[2] * v2[0] - v1[0] * v2[2];
     v3[2] = v1[0] * v2[1] - v1[1] * v2[0];
-    T u1[3], u2[3], u3[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        u1[i] = S[i][0] * v1[0] + S[i][1] * v1[1] + S[i][2] * v1[2];
-        u2[i] = S[i][0] * v2[0] + S[i][1] * v2[1] + S[i][2] * v2[2];
-    }
     const T n1 = tsqrt(u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) u1[i] /= n1;
@@ -115,14 +123,11 @@ __device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3])
     T n2 = tsqrt(u2[0] * u2[0] + u2[1] * u2[1] + u2[2] * u2[2]);
     if (!(n2 > (T)64 * Eps<T>::v * n1)) {
         // rank one: any unit vector orthogonal to u1
-        int mi = 0;
-        if (fabs(u1[1]) < fabs(u1[mi])) mi = 1;
-        if (fabs(u1[2]) < fabs(u1[mi])) mi = 2;
-        T e[3] = {(T)0, (T)0, (T)0};
-        e[mi] = (T)1;
-        const T d2 = u1[mi];
+        const T a0 = fabs(u1[0]), a1 = fabs(u1[1]), a2 = fabs(u1[2]);
+        const int mi = (a1 < a0) ? ((a2 < a1) ? 2 : 1) : ((a2 < a0) ? 2 : 0);
+        const T d2 = mi == 0 ? u1[0] : (mi == 1 ? u1[1] : u1[2]);
 #pragma unroll
-        for (int i = 0; i < 3; ++i) u2[i] = e[i] - d2 * u1[i];
+        for (int i = 0; i < 3; ++i) u2[i] = (i == mi ? (T)1 : (T)0) - d2 * u1[i];
         n2 = tsqrt(u2[0] * u2[0] + u2[1] * u2[1] + u2[2] * u2[2]);
     }
 #pragma unroll

@@ -255,6 +255,26 @@ void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int3
 
 // ---------------------------------------------------------------------------
 
+int64_t symbolic_factor_nnz(Symbolic &sym) {
+    if (sym.factor_nnz >= 0) return sym.factor_nnz;
+    // row subtrees of the elimination tree: row k of L holds column i < k for
+    // every i on the tree path from a neighbour of k (in the permuted free
+    // graph, which is the device-order adjacency restricted to [0, m)) up to k
+    const int m = sym.m;
+    std::vector<int32_t> mark(m, -1);
+    int64_t nz = m;
+    for (int k = 0; k < m; ++k) {
+        mark[k] = k;
+        for (int32_t e = sym.drow[k]; e < sym.drow[k + 1]; ++e) {
+            int32_t i = sym.dcol[e];
+            if (i >= k) continue;
+            while (mark[i] != k) { mark[i] = k; ++nz; i = sym.etree[i]; }
+        }
+    }
+    sym.factor_nnz = nz;
+    return nz;
+}
+
 bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
                     std::string &err, bool &singular, bool mesh_order) {
     singular = false;
@@ -382,18 +402,10 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
                 }
             }
         }
-        std::vector<int32_t> mark(m, -1);
-        int64_t nz = m;
-        for (int k = 0; k < m; ++k) {
-            mark[k] = k;
-            for (int32_t q = prow[k]; q < prow[k + 1]; ++q) {
-                int32_t i = pcol[q];
-                if (i >= k) continue;
-                while (mark[i] != k) { mark[i] = k; ++nz; i = sym.etree[i]; }
-            }
-        }
-        sym.factor_nnz = nz;
     }
+    // the factor's nonzero count is only reported, so it is counted on demand
+    // (symbolic_factor_nnz) rather than on every analysis
+    sym.factor_nnz = -1;
     // supernodes = the dissection's blocks
     const int S = (int)sym.block_ptr.size() - 1;
     sym.S = S;

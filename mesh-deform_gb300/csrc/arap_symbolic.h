@@ -117,7 +117,7 @@ struct Symbolic {
     int max_nrow = 0, max_ncol = 0, max_children = 0, max_ldx = 0, max_ld21 = 0;
     int64_t panel_size = 0, dinv_size = 0, upd_size = 0, uvec_size = 0, x_size = 0, l21_size = 0;
     int64_t l21t_size = 0;
-    int64_t factor_nnz = 0;           // nonzeros of the scalar factor (from the etree)
+    int64_t factor_nnz = -1;          // nonzeros of the scalar factor (-1: not counted yet)
     double factor_flops = 0.0;        // dense flops of the supernodal factorisation
     std::vector<FItem> fitems;
     std::vector<FactorLaunch> fplan;
@@ -134,6 +134,10 @@ struct Symbolic {
 // left empty are dropped) instead of dissecting the free graph.
 bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
                     std::string &err, bool &singular, bool mesh_order = false);
+
+// Nonzeros of the scalar Cholesky factor (diagonal included), counted from the
+// elimination tree on first use and kept in sym.factor_nnz.
+int64_t symbolic_factor_nnz(Symbolic &sym);
 
 // Nested-dissection order of a symmetric graph (no self loops); exposed for tests.
 void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int32_t> &perm,

@@ -9,8 +9,10 @@ uses, so the timed numbers rest on a tested result:
 * noisy icosphere L7 (163,842 vertices), 16 handle caps and an anchor cap,
   50 iterations, mixed form with the FP64 factor: <= 1e-6;
 * icosphere L5 x 256 poses, 20 iterations, one factor for all poses, the
-  dense top's column cap and the pose tile autotuned as bench.py does: 32
-  poses spread over the batch against the oracle, <= 1e-6;
+  dense top's column cap and the pose tile autotuned as bench.py does: every
+  pose against the oracle, <= 1e-6 (the hardest poses stretch one-rings close
+  to rank one in the first iterations, which the FP32 rotation fit must
+  handle without squaring the covariance);
 * icosphere L4, FP64 form, 10 iterations: <= 1e-10.
 
 A dirty deform that redoes the symbolic analysis on every call (the
@@ -35,7 +37,7 @@ def oracle_many(w, targets_list, iterations):
         assert ok
         return ref
 
-    with ThreadPoolExecutor(max_workers=8) as ex:
+    with ThreadPoolExecutor(max_workers=16) as ex:
         return list(ex.map(one, targets_list))
 
 
@@ -101,7 +103,7 @@ def test_pose_batch_l5x256_autotuned_matches_oracle(gpu):
         arap_tune.tune_pose_tile(ctx, w.iterations, trials=1)
         ctx.invalidate()
         out = ctx.deform_poses(None, w.iterations)
-    picks = np.linspace(0, P - 1, 32).round().astype(int)
+    picks = np.arange(P)  # every pose
     refs = oracle_many(w, [w.poses[p] for p in picks], w.iterations)
     errs = [W.bbox_rel_error(out[p], r, w.positions) for p, r in zip(picks, refs)]
     assert max(errs) <= 1e-6, max(errs)
