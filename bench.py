@@ -724,19 +724,48 @@ def run_requests(args):
         t1 = max(ref.elapsed_time(b) for _, b in ev)
         return t1 - t0, launches
 
-    # ---- timed region: dirty deforms with inputs resident on the device ----
+    # ---- end to end through the C ABI with pinned host buffers: rest pose,
+    # constraint indices and targets in, deformed positions out, per request
+    # on its own host thread; wall clock around the whole step ----
+    rest_h = torch.from_numpy(np.ascontiguousarray(w.positions)).pin_memory().numpy()
+    idx_h = torch.from_numpy(np.ascontiguousarray(w.cidx, dtype=np.int32)).pin_memory().numpy()
+    tgt_h = torch.from_numpy(np.ascontiguousarray(w.ctargets)).pin_memory().numpy()
+    outs_h = [torch.empty((w.V, 3), dtype=torch.float64).pin_memory().numpy() for _ in ctxs]
+
+    def e2e_one(i):
+        c = ctxs[i]
+        c.set_rest_positions(rest_h)
+        c.set_constraints(idx_h, tgt_h)
+        c.deform_async(w.iterations, outs_h[i])
+        c.wait()
+
+    def e2e_step():
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        list(pool.map(e2e_one, range(N)))
+        return time.perf_counter() - t0
+
+    # ---- timed region: dirty deforms with inputs resident on the device.
+    # Each one is followed by one end-to-end step (not counted in `value`), so
+    # both measures see the same conditions over the run ----
     set_analysis(args.cached_analysis)
     for _ in range(args.warmup):
         device_step()
+        if not args.skip_e2e:
+            e2e_step()
     clocks = ClockSampler(local)
     launches = 0
     step_ms = []
+    e2e_s = []
     barrier()
     clocks.start()
     for k in range(args.steps):
         ms, nl = device_step()
         step_ms.append(ms)
         launches += nl
+        if not args.skip_e2e:
+            e2e_s.append(e2e_step())
     barrier()
     clk = clocks.stop()
     total_ms = reduce_max(sum(step_ms), dist, dev)
@@ -799,30 +828,6 @@ def run_requests(args):
         c0.set_solve_ctas(args.solve_ctas)
     c0.set_symbolic_cache(args.cached_analysis)
 
-    # ---- end to end through the C ABI with pinned host buffers: rest pose,
-    # constraint indices and targets in, deformed positions out, per request
-    # on its own host thread; wall clock around the whole step ----
-    rest_h = torch.from_numpy(np.ascontiguousarray(w.positions)).pin_memory().numpy()
-    idx_h = torch.from_numpy(np.ascontiguousarray(w.cidx, dtype=np.int32)).pin_memory().numpy()
-    tgt_h = torch.from_numpy(np.ascontiguousarray(w.ctargets)).pin_memory().numpy()
-    outs_h = [torch.empty((w.V, 3), dtype=torch.float64).pin_memory().numpy() for _ in ctxs]
-
-    def e2e_one(i):
-        c = ctxs[i]
-        c.set_rest_positions(rest_h)
-        c.set_constraints(idx_h, tgt_h)
-        c.deform_async(w.iterations, outs_h[i])
-        c.wait()
-
-    e2e_s = []
-    for k in range(0 if args.skip_e2e else args.warmup + args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        list(pool.map(e2e_one, range(N)))
-        t1 = time.perf_counter()
-        if k >= args.warmup:
-            e2e_s.append(t1 - t0)
     pool.shutdown()
     e2e_total = reduce_max(sum(e2e_s), dist, dev) if e2e_s else float("nan")
     e2e_value = its_total / e2e_total if e2e_s else None
@@ -892,7 +897,8 @@ def run_requests(args):
         "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
         "config": config_of(w, args, extra),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "timing": "host wall clock around each step (uploads, enqueues, waits, result copies)"},
+                "timing": "host wall clock around each step (uploads, enqueues, waits, result copies); one "
+                          "end-to-end step after each timed device step"},
         "repose_refactor": repose,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

@@ -194,6 +194,14 @@ int arap_set_pose_tile(arap_ctx *ctx, int32_t poses);
    problem up again). */
 int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes);
 
+/* The bottom levels of the elimination tree whose supernode fronts all have
+   at most `rows` rows (0: none; at most 256; the default is 128) are solved
+   one warp per supernode, many supernodes per CTA, before the CTA-per-
+   supernode sweep of the levels above (after it, backward). Any value gives
+   a correct result; it changes the order of some sums. Takes effect at the
+   next deform (which sets the problem up again). */
+int arap_set_warp_rows(arap_ctx *ctx, int32_t rows);
+
 /* The top levels of the elimination tree, up to `max_columns` columns in all
    (0, the default: 2,048; negative: none), are solved through the explicit
    inverse of the factor restricted to them: formed once per factorisation

@@ -112,6 +112,7 @@ SIGNATURES = {
     "arap_energy": (C.c_int, [_P, _dp]),
     "arap_set_cluster_threshold": (C.c_int, [_P, _I32]),
     "arap_set_dense_top": (C.c_int, [_P, _I32]),
+    "arap_set_warp_rows": (C.c_int, [_P, _I32]),
     "arap_set_ordering": (C.c_int, [_P, _I32]),
     "arap_set_done_callback": (C.c_int, [_P, _P, _P]),
     "arap_get_host_timing": (C.c_int, [_P, _dp]),
@@ -327,6 +328,10 @@ class ArapContext:
 
     def set_cluster_threshold(self, nbytes: int):
         self._check(self.lib.arap_set_cluster_threshold(self.h, int(nbytes)))
+
+    def set_warp_rows(self, rows: int):
+        """Largest front (rows) of the warp-per-supernode solves of the bottom levels (0: none)."""
+        self._check(self.lib.arap_set_warp_rows(self.h, int(rows)))
 
     def set_dense_top(self, max_columns: int):
         """Columns of the tree's top solved through an explicit inverse (0: default, <0: none)."""

@@ -22,6 +22,13 @@ using namespace arapgpu;
 
 namespace {
 
+// ticket counters of the single-request solves: forward / backward of the CTA
+// sweep (0, 1), of the cluster sweep (2, 3), of the warp sweep (4, 6)
+constexpr int kTickets = 8;
+// fronts of at most this many rows at the bottom of the tree are solved one
+// warp per supernode (arap_set_warp_rows; 0: none)
+constexpr int kWarpRowsDefault = 128;
+
 // Device buffer from the device's stream-ordered memory pool, allocated and
 // freed on the owning context's stream: growing or dropping a buffer never
 // waits for work on other streams (a plain cudaFree would wait for the whole
@@ -162,6 +169,7 @@ struct arap_ctx {
     int solve_cap = 0;  // most CTAs per triangular-solve launch (0: as many as fit the device)
     int top_bytes = 0;  // supernode size from which tree levels go to the cluster solves (0: default, <0: never)
     int dense_cols = 0;  // most columns of the dense top of the tree (0: default, <0: none)
+    int warp_rows = kWarpRowsDefault;  // largest front of the warp-per-supernode solves (0: none)
     size_t dense_inv_smem[2] = {0, 0}, dense_vec_smem[2] = {0, 0};  // configured limits (FP32, FP64)
     DevBuf top_col, top_gptr, top_gidx, tdpos, top_items, Ttop, ytop;
     int ordering = ARAP_ORDER_PER_CONSTRAINT_SET;
@@ -329,7 +337,7 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     add(ctx->child, s.child.size() * 4);
     add(ctx->level_sn, s.level_sn.size() * 4);
     add(ctx->fitems, s.fitems.size() * sizeof(FItem));
-    add(ctx->ticket, 4 * sizeof(unsigned long long));
+    add(ctx->ticket, kTickets * sizeof(unsigned long long));
     add(ctx->flags, 2 * sizeof(unsigned) * S1);
     // iteration state and factor (setup_alloc)
     const bool f32 = sizeof(T) == 4;
@@ -465,9 +473,9 @@ int prepare_symbolic(arap_ctx *ctx) {
     CK(upload(ctx->fitems, s.fitems, st));
     // solve scheduling state: ticket counters and per-supernode flags start at 0
     // counters: forward / backward of the lower levels, then of the top levels
-    CK(ctx->ticket.ensure(4 * sizeof(unsigned long long)));
+    CK(ctx->ticket.ensure(kTickets * sizeof(unsigned long long)));
     CK(ctx->flags.ensure(2 * sizeof(unsigned) * (size_t)std::max(s.S, 1)));
-    CK(cudaMemsetAsync(ctx->ticket.p, 0, 4 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(ctx->ticket.p, 0, kTickets * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
     // the solve kernels stream whole columns through chunk buffers (a column
     // must fit one) and keep a front's vectors in shared memory; fronts of
@@ -534,13 +542,34 @@ int prepare_symbolic(arap_ctx *ctx) {
         }
         d.ltop = ltop;
         d.s_low = nlev > 0 ? s.level_ptr[ltop] : 0;
+        // the bottom levels whose fronts all fit a warp task
+        int lwarp = 0;
+        const int wrows = std::min(ctx->warp_rows, wsolve_max_rows());
+        while (wrows > 0 && lwarp < ltop) {
+            int mx = 0;
+            for (int q = s.level_ptr[lwarp]; q < s.level_ptr[lwarp + 1]; ++q) mx = std::max(mx, (int)s.sn[s.level_sn[q]].nrow);
+            if (mx > wrows) break;
+            ++lwarp;
+        }
+        d.lwarp = lwarp;
+        d.s_warp = nlev > 0 ? s.level_ptr[lwarp] : 0;
+        if (d.s_warp > 0) {
+            CK(configure_wsolve());
+            const int cap = ctx->solve_cap;
+            const int need = (d.s_warp + 7) / 8;
+            const int r32 = wsolve_resident_ctas(4), r64 = wsolve_resident_ctas(8);
+            d.wgrid32 = std::max(1, std::min(need, cap > 0 ? std::min(cap, r32) : r32));
+            d.wgrid64 = std::max(1, std::min(need, cap > 0 ? std::min(cap, r64) : r64));
+        } else {
+            d.wgrid32 = d.wgrid64 = 0;
+        }
         d.s_top = d.n_top > 0 ? 0 : s.S - d.s_low;
         int width = 0;
         for (int l = ltop; l < nlev; ++l) width = std::max(width, s.level_ptr[l + 1] - s.level_ptr[l]);
         d.top_clusters = std::max(1, std::min(width, kTopMaxClusters));
         const int res32 = solve_resident_ctas((int)b32, 4), res64 = solve_resident_ctas((int)b64, 8);
         const int cap = ctx->solve_cap;
-        const int nl = std::max(d.s_low, 1);
+        const int nl = std::max(d.s_low - d.s_warp, 1);
         d.solve_grid32 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res32) : res32));
         d.solve_grid64 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res64) : res64));
         // the cluster solves size their shared memory by the largest front of
@@ -656,7 +685,7 @@ int setup_enqueue(arap_ctx *ctx) {
     // the solves' scheduling counters and flags restart with every set-up: a
     // launch consumes tickets in proportion to its grid, which differs
     // between the precisions
-    CK(cudaMemsetAsync(ctx->ticket.p, 0, 4 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(ctx->ticket.p, 0, kTickets * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
     // cotan weights (arap.h:182-239)
     {
@@ -766,7 +795,9 @@ template <typename T>
 int run_iterations(arap_ctx *ctx, int iterations);
 
 // kernels of one forward + backward sweep (lower levels and cluster levels)
-int solve_launches(const DevSym &d) { return 2 * ((d.s_low > 0) + (d.s_top > 0) + (d.n_top > 0)); }
+int solve_launches(const DevSym &d) {
+    return 2 * ((d.s_warp > 0) + (d.s_low > d.s_warp) + (d.s_top > 0) + (d.n_top > 0));
+}
 
 template <>
 int run_iterations<double>(arap_ctx *ctx, int iterations) {
@@ -1052,6 +1083,7 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->solve_cap = src->solve_cap;
     ctx->top_bytes = src->top_bytes;
     ctx->dense_cols = src->dense_cols;
+    ctx->warp_rows = src->warp_rows;
     ctx->ordering = src->ordering;
     return finish_create(ctx, src->device, src, out);
 }
@@ -1610,6 +1642,21 @@ int arap_set_ordering(arap_ctx *ctx, int32_t mode) {
         ctx->ordering = mode;
         ctx->sym_host = false;
         ctx->sym_valid = false;
+        ctx->dirty = true;
+    }
+    return ARAP_OK;
+}
+
+int arap_set_warp_rows(arap_ctx *ctx, int32_t rows) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (rows < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "negative row count");
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (rows != ctx->warp_rows) {
+        ctx->warp_rows = rows;
+        ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
         ctx->dirty = true;
     }
     return ARAP_OK;

@@ -218,7 +218,15 @@ __global__ void k_rest_edges(int V, const int32_t *__restrict__ drow, const int3
 // multifrontal Cholesky, level by level, many CTAs per front
 
 constexpr int kFactorThreads = 256;
-constexpr int kTile = 64;   // rows of an update tile
+// Tile shapes of the factorisation plan (arap_symbolic.cpp builds the items
+// with the same sizes): rows of a block-column update tile, rows of a tile of
+// the solve below a diagonal block, and the square tiles of the Schur
+// complement. Small tiles spread a front's work over many CTAs, which the
+// FP64 factor needs: a GB300 SM issues about two FP64 FMAs per clock.
+constexpr int kUpdRows = kFactorUpdRows;
+constexpr int kRowsTile = kFactorRowsTile;
+constexpr int kSyrkTile = kFactorSyrkTile;
+static_assert(kUpdRows == 32 && kRowsTile == 64 && kSyrkTile == 32, "thread mappings below assume these sizes");
 
 // Front of supernode d: the nrow x ncol panel P (column-major, ld nrow; rows are
 // the supernode's columns then its struct rows) and the nb x nb update matrix U.
@@ -295,29 +303,29 @@ k_fea(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const int3
     }
 }
 
-// Left-looking update of block column jb: rows [j0 + 64 rt, +64) of columns
+// Left-looking update of block column jb: rows [j0 + 32 rt, +32) of columns
 // [j0, j0+w) lose sum_{k < j0} P(r, k) P(j0+c, k).
 template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
 k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF *__restrict__ Lval) {
-    __shared__ TF As[NB][kTile];
+    __shared__ TF As[NB][kUpdRows];
     __shared__ TF Bs[NB][NB + 1];
     const FItem it = items[blockIdx.x];
     const SnInfo d = sn[it.sn];
     const int n = d.nrow, nc = d.ncol;
     const int j0 = jb * NB, w = min(NB, nc - j0);
-    const int r0 = j0 + it.a * kTile;
+    const int r0 = j0 + it.a * kUpdRows;
     TF *P = Lval + d.panel_off;
-    const int tid = threadIdx.x, tx = tid % 8, ty = tid / 8;  // 4 columns x 2 rows per thread
-    TF acc[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    const int tid = threadIdx.x, tx = tid % 8, ty = tid / 8;  // 4 columns x 1 row per thread
+    TF acc[4] = {0, 0, 0, 0};
     // the next k-slice is loaded into registers while the current one is
     // multiplied, so its global round trip overlaps the products
-    constexpr int kPa = NB * kTile / kFactorThreads, kPb = NB * NB / kFactorThreads;
+    constexpr int kPa = NB * kUpdRows / kFactorThreads, kPb = NB * NB / kFactorThreads;
     TF pa[kPa], pb[kPb];
     auto load_slice = [&](int k0) {
 #pragma unroll
         for (int u = 0; u < kPa; ++u) {
-            const int q = tid + u * kFactorThreads, t = q / kTile, r = q % kTile;
+            const int q = tid + u * kFactorThreads, t = q / kUpdRows, r = q % kUpdRows;
             pa[u] = (r0 + r < n) ? P[(int64_t)(k0 + t) * n + r0 + r] : (TF)0;
         }
 #pragma unroll
@@ -331,7 +339,7 @@ k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, T
 #pragma unroll
         for (int u = 0; u < kPa; ++u) {
             const int q = tid + u * kFactorThreads;
-            As[q / kTile][q % kTile] = pa[u];
+            As[q / kUpdRows][q % kUpdRows] = pa[u];
         }
 #pragma unroll
         for (int u = 0; u < kPb; ++u) {
@@ -342,24 +350,18 @@ k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, T
         if (k0 + NB < j0) load_slice(k0 + NB);
 #pragma unroll 8
         for (int t = 0; t < NB; ++t) {
-            const TF a0 = As[t][ty], a1 = As[t][ty + 32];
+            const TF a0 = As[t][ty];
 #pragma unroll
-            for (int cc = 0; cc < 4; ++cc) {
-                const TF bv = Bs[t][tx * 4 + cc];
-                acc[0][cc] += a0 * bv;
-                acc[1][cc] += a1 * bv;
-            }
+            for (int cc = 0; cc < 4; ++cc) acc[cc] += a0 * Bs[t][tx * 4 + cc];
         }
         __syncthreads();
     }
-#pragma unroll
-    for (int rr = 0; rr < 2; ++rr) {
-        const int r = r0 + ty + 32 * rr;
-        if (r >= n) continue;
+    const int r = r0 + ty;
+    if (r < n) {
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
             const int c = tx * 4 + cc;
-            if (c < w) P[(int64_t)(j0 + c) * n + r] -= acc[rr][cc];
+            if (c < w) P[(int64_t)(j0 + c) * n + r] -= acc[cc];
         }
     }
 }
@@ -377,16 +379,18 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
       TF *__restrict__ Dinv, int *err) {
     __shared__ TF Lb[NB][NB + 1];  // the factored block, row-major: Lb[r][c] = L(r, c)
     __shared__ TF rinv[NB];        // 1 / L(r, r)
-    const SnInfo d = sn[items[blockIdx.x].sn];
+    const FItem it = items[blockIdx.x];
+    const SnInfo d = sn[it.sn];
     const int n = d.nrow, nc = d.ncol;
     const int j0 = jb * NB, w = min(NB, nc - j0);
     TF *P = Lval + d.panel_off;
     const int tid = threadIdx.x, lane = tid & 31;
     // the rows below the block: warps 1.. of the CTA, or warp 0 itself after
-    // the inverse when the CTA is a single warp
+    // the inverse when the CTA is a single warp; none when the item leaves
+    // them to k_frows (it.a != 0)
     const bool solo = blockDim.x == 32;
     const int row_threads = solo ? 32 : (int)blockDim.x - 32;
-    const int i_first = j0 + w + (solo ? lane : tid - 32);
+    const int i_first = it.a ? n : j0 + w + (solo ? lane : tid - 32);
     TF a[NB];
     TF myinv = (TF)0;  // warp 0: 1 / L(lane, lane)
     if (tid < 32) {
@@ -465,35 +469,79 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
     }
 }
 
-// Schur complement of a front: the 64x64 tile (rt, ct), rt >= ct, of U loses
+// The rows below diagonal block jb of a front, 64 rows per CTA, when the plan
+// takes them out of k_fdt (fronts with many rows): L(i, j0 + c) =
+// sum_k A(i, j0 + k) X(c, k) with X = inv(L_bb) from Dinv, written in place.
+// One matrix product per tile, so the rows spread over many CTAs instead of
+// one CTA's forward substitution.
+template <typename TF>
+__global__ void __launch_bounds__(kFactorThreads)
+k_frows(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF *__restrict__ Lval,
+        const TF *__restrict__ Dinv) {
+    __shared__ TF As[NB][kRowsTile];
+    __shared__ TF Bs[NB][NB + 1];
+    const FItem it = items[blockIdx.x];
+    const SnInfo d = sn[it.sn];
+    const int n = d.nrow, nc = d.ncol;
+    const int j0 = jb * NB, w = min(NB, nc - j0);
+    const int r0 = j0 + w + it.a * kRowsTile;
+    TF *P = Lval + d.panel_off;
+    const TF *D = Dinv + d.dinv_off + (int64_t)jb * NB * NB;  // column-major: D[k * NB + c] = X(c, k)
+    const int tid = threadIdx.x, tx = tid % 8, ty = tid / 8;  // 4 columns x 2 rows per thread
+    for (int q = tid; q < NB * kRowsTile; q += kFactorThreads) {
+        const int t = q / kRowsTile, r = q % kRowsTile;
+        As[t][r] = (t < w && r0 + r < n) ? P[(int64_t)(j0 + t) * n + r0 + r] : (TF)0;
+    }
+    for (int q = tid; q < NB * NB; q += kFactorThreads) Bs[q / NB][q % NB] = D[q];
+    __syncthreads();
+    TF acc[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+#pragma unroll 8
+    for (int t = 0; t < NB; ++t) {
+        const TF a0 = As[t][ty], a1 = As[t][ty + 32];
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            const TF bv = Bs[t][tx * 4 + cc];
+            acc[0][cc] += a0 * bv;
+            acc[1][cc] += a1 * bv;
+        }
+    }
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+        const int r = r0 + ty + 32 * rr;
+        if (r >= n) continue;
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            const int c = tx * 4 + cc;
+            if (c < w) P[(int64_t)(j0 + c) * n + r] = acc[rr][cc];
+        }
+    }
+}
+
+// Schur complement of a front: the 32x32 tile (rt, ct), rt >= ct, of U loses
 // sum_{k < nc} L21(r, k) L21(c, k); each entry is read and written once.
 template <typename TF>
 __global__ void __launch_bounds__(kFactorThreads)
 k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF *__restrict__ Lval,
         TF *__restrict__ Upd) {
-    __shared__ TF As[NB][kTile];
-    __shared__ TF Bs[NB][kTile];
+    __shared__ TF As[NB][kSyrkTile];
+    __shared__ TF Bs[NB][kSyrkTile];
     const FItem it = items[blockIdx.x];
     const SnInfo d = sn[it.sn];
     const int n = d.nrow, nc = d.ncol, nb = n - nc;
     const TF *P = Lval + d.panel_off;
     TF *U = Upd + d.upd_off;
-    const int rb = it.a * kTile, cb = it.b * kTile;  // within U
-    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-    TF acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = (TF)0;
+    const int rb = it.a * kSyrkTile, cb = it.b * kSyrkTile;  // within U
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;  // 2 x 2 entries per thread
+    TF acc[2][2] = {{(TF)0, (TF)0}, {(TF)0, (TF)0}};
     // the next k-slice is loaded into registers while the current one is
     // multiplied, so its global round trip overlaps the products
-    constexpr int kPer = NB * kTile / kFactorThreads;
+    constexpr int kPer = NB * kSyrkTile / kFactorThreads;
     TF pa[kPer], pb[kPer];
     auto load_slice = [&](int k0) {
         const int kw = min(NB, nc - k0);
 #pragma unroll
         for (int u = 0; u < kPer; ++u) {
-            const int q = tid + u * kFactorThreads, t = q / kTile, r = q % kTile;
+            const int q = tid + u * kFactorThreads, t = q / kSyrkTile, r = q % kSyrkTile;
             pa[u] = pb[u] = (TF)0;
             if (t < kw) {
                 const TF *col = P + (int64_t)(k0 + t) * n + nc;
@@ -507,30 +555,27 @@ k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF
 #pragma unroll
         for (int u = 0; u < kPer; ++u) {
             const int q = tid + u * kFactorThreads;
-            As[q / kTile][q % kTile] = pa[u];
-            Bs[q / kTile][q % kTile] = pb[u];
+            As[q / kSyrkTile][q % kSyrkTile] = pa[u];
+            Bs[q / kSyrkTile][q % kSyrkTile] = pb[u];
         }
         __syncthreads();
         if (k0 + NB < nc) load_slice(k0 + NB);
 #pragma unroll 8
         for (int t = 0; t < NB; ++t) {
-            TF av[4], bv[4];
-#pragma unroll
-            for (int a = 0; a < 4; ++a) av[a] = As[t][ty + 16 * a];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) bv[b] = Bs[t][tx + 16 * b];
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+            const TF a0 = As[t][ty], a1 = As[t][ty + 16];
+            const TF b0 = Bs[t][tx], b1 = Bs[t][tx + 16];
+            acc[0][0] += a0 * b0;
+            acc[0][1] += a0 * b1;
+            acc[1][0] += a1 * b0;
+            acc[1][1] += a1 * b1;
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
+    for (int a = 0; a < 2; ++a) {
         const int r = rb + ty + 16 * a;
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
+        for (int b = 0; b < 2; ++b) {
             const int c = cb + tx + 16 * b;
             if (r < nb && c < nb && r >= c) U[(int64_t)c * nb + r] -= acc[a][b];
         }
@@ -1040,6 +1085,8 @@ __device__ __forceinline__ void next_task(unsigned long long *ticket, int S, int
     epoch = (unsigned)(t / (unsigned long long)Z) + 1u;
 }
 
+#include "arap_wsolve.cuh"
+
 // Shared memory of a solve CTA (dynamic): two chunk buffers, three vectors
 // (two of max_ldx rows, one of max_ld21 rows) and the reduction scratch.
 struct SolveSmem {
@@ -1052,7 +1099,7 @@ struct SolveSmem {
 // only waits for CTAs that started before it.
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads, 3)
-k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
+k_solve_fwd(int S, int Z, int lbeg, SolveSmem lay, const int32_t *__restrict__ order, const SnInfo *__restrict__ sn,
             const int32_t *__restrict__ child, const int32_t *__restrict__ relind, const T *__restrict__ Xall,
             const T *__restrict__ L21all, Vec4<T> *__restrict__ sol, Vec4<T> *__restrict__ uvec,
             unsigned long long *ticket, unsigned *flags, int *err) {
@@ -1123,7 +1170,8 @@ k_solve_fwd(int S, int Z, SolveSmem lay, const int32_t *__restrict__ order, cons
         total_children_rows += c.nrow - c.ncol;
     }
     if (tid == 0)
-        for (int ci = d.child_begin; ci < d.child_end; ++ci) wait_flag(flags + child[ci], epoch, err);
+        for (int ci = d.child_begin; ci < d.child_end; ++ci)
+            if (sn[child[ci]].level >= lbeg) wait_flag(flags + child[ci], epoch, err);  // lower: an earlier launch
     // the next ticket is taken once this task is ready to run, so its round
     // trip overlaps the work below
     if (tid == 32) next_task(ticket, S, Z, order, false, err, s_task[slot ^ 1], s_epoch[slot ^ 1]);
@@ -2102,6 +2150,7 @@ void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *it
         k_fdt<TF><<<fl.count, threads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv, err);
         break;
     }
+    case kFrows: k_frows<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv); break;
     case kFsyrk: k_fsyrk<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Upd); break;
     case kFx: k_fx<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Dinv, X, L21, L21T); break;
     }
@@ -2148,6 +2197,32 @@ void launch_demote(int count, const double *const *src, float *const *dst, const
     k_demote<<<grid, 256, 0, st>>>(job);
 }
 
+size_t wsolve_smem_bytes(int scalar_bytes) { return (size_t)kWarpsPerCta * kWarpRows * 4 * scalar_bytes; }
+int wsolve_max_rows() { return kWarpRows; }
+
+cudaError_t configure_wsolve() {
+    cudaError_t e = raise_smem_limit((const void *)k_wsolve_fwd<float>, (int)wsolve_smem_bytes(4));
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_wsolve_bwd<float>, (int)wsolve_smem_bytes(4));
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_wsolve_fwd<double>, (int)wsolve_smem_bytes(8));
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_wsolve_bwd<double>, (int)wsolve_smem_bytes(8));
+    return e;
+}
+
+int wsolve_resident_ctas(int scalar_bytes) {
+    int dev = 0, sms = 0, a = 0, b = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 1;
+    const size_t smem = wsolve_smem_bytes(scalar_bytes);
+    if (scalar_bytes == 4) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wsolve_fwd<float>, kWarpThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wsolve_bwd<float>, kWarpThreads, smem);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wsolve_fwd<double>, kWarpThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wsolve_bwd<double>, kWarpThreads, smem);
+    }
+    return std::max(1, std::min(a, b)) * sms;
+}
+
 int solve_chunk_bytes() { return kChunkBytes; }
 
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
@@ -2166,9 +2241,16 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
-    if (s.s_low > 0)
-        k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(s.s_low, s.s_low + G, lay, s.level_sn, s.sn, s.child, s.relind,
-                                                       X, L21, sol, uvec, ticket, flags, err);
+    if (s.s_warp > 0) {
+        const int WG = sizeof(T) == 4 ? s.wgrid32 : s.wgrid64;
+        const int W = WG * kWarpsPerCta;
+        k_wsolve_fwd<T><<<WG, kWarpThreads, wsolve_smem_bytes(sizeof(T)), st>>>(
+            s.s_warp, s.s_warp + W, s.level_sn, s.sn, s.child, s.relind, X, L21, sol, uvec, ticket + 4, flags, err);
+    }
+    const int sb = s.s_low - s.s_warp;  // supernodes of the CTA sweep
+    if (sb > 0)
+        k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(sb, sb + G, s.lwarp, lay, s.level_sn + s.s_warp, s.sn, s.child,
+                                                       s.relind, X, L21, sol, uvec, ticket, flags, err);
     if (s.s_top > 0) {
         const SolveSmem tlay{s.top_ldx, s.top_ld21};
         const size_t tsmem = top_smem_bytes_impl(s.top_ldx, s.top_ld21, sizeof(T));
@@ -2208,9 +2290,17 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
             s.s_top, s.s_top + s.top_clusters, tlay, s.level_sn + s.s_low, s.sn, s.rows, X, L21T, sol, pc64, pc32,
             mode, ticket + 2, flags, err);
     }
-    if (s.s_low > 0)
-        k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(s.s_low, s.s_low + G, s.ltop, lay, s.level_sn, s.sn, s.rows, X,
+    const int sb = s.s_low - s.s_warp;
+    if (sb > 0)
+        k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(sb, sb + G, s.ltop, lay, s.level_sn + s.s_warp, s.sn, s.rows, X,
                                                        L21T, sol, pc64, pc32, mode, ticket, flags, err);
+    if (s.s_warp > 0) {
+        const int WG = sizeof(T) == 4 ? s.wgrid32 : s.wgrid64;
+        const int W = WG * kWarpsPerCta;
+        k_wsolve_bwd<T><<<WG, kWarpThreads, wsolve_smem_bytes(sizeof(T)), st>>>(
+            s.s_warp, s.s_warp + W, s.lwarp, s.level_sn, s.sn, s.rows, X, L21T, sol, pc64, pc32, mode, ticket + 5,
+            flags, err);
+    }
 }
 
 template <typename T>

@@ -52,6 +52,11 @@ struct DevSym {
     // the solves split the tree: levels [0, ltop) by single CTAs (s_low tasks),
     // levels [ltop, top) by clusters (s_top tasks, top_clusters clusters)
     int ltop, s_low, s_top, top_clusters;
+    // the bottom levels [0, lwarp) (s_warp supernodes, fronts of at most
+    // wsolve_max_rows() rows) are solved one warp per supernode, in wgrid
+    // CTAs, before (forward) / after (backward) the CTA sweep of the levels
+    // [lwarp, ltop)
+    int lwarp, s_warp, wgrid32, wgrid64;
     int top_ldx, top_ld21;  // largest front of the cluster levels (their shared-memory layout)
     // dense top (levels [ltop, top) when n_top > 0, instead of cluster levels):
     // n_top columns, T = inv(L_top) formed by n_top_items CTAs
@@ -127,6 +132,12 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
 constexpr int kSolveBlockRows = 1024;
 // bytes of one chunk buffer of the solves (a matrix column must fit one)
 int solve_chunk_bytes();
+// warp-per-supernode solves of the bottom levels: largest front, dynamic shared
+// memory per CTA, shared-memory limits, CTAs resident on the device
+int wsolve_max_rows();
+size_t wsolve_smem_bytes(int scalar_bytes);
+cudaError_t configure_wsolve();
+int wsolve_resident_ctas(int scalar_bytes);
 size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes);
 // solve CTAs resident on the device at once (occupancy x SMs) for that shared memory
 int solve_resident_ctas(int smem_bytes, int scalar_bytes);

@@ -528,7 +528,7 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
             sym.fplan.push_back({kind, jb, (int32_t)sym.fitems.size(), (int32_t)items.size()});
             sym.fitems.insert(sym.fitems.end(), items.begin(), items.end());
         };
-        constexpr int kSlice = 32, kRowTile = 64, kTileU = 64;
+        constexpr int kSlice = 32, kRowTile = kFactorUpdRows, kTileU = kFactorSyrkTile;
         for (int l = 0; l < nlev; ++l) {
             std::vector<FItem> it;
             int nblk_max = 0;
@@ -541,18 +541,23 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
             }
             add(kFea, 0, it);
             for (int jb = 0; jb < nblk_max; ++jb) {
-                std::vector<FItem> up, dt;
+                std::vector<FItem> up, dt, rw;
                 for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; ++q) {
                     const int sidx = sym.level_sn[q];
                     const SnInfo &d = sym.sn[sidx];
                     const int j0 = jb * kDiagBlock;
                     if (j0 >= d.ncol) continue;
-                    dt.push_back({sidx, 0, 0, 0});
+                    const int below = d.nrow - std::min(d.ncol, j0 + kDiagBlock);
+                    const bool tiled = below > kFactorRowsInline;
+                    dt.push_back({sidx, tiled ? 1 : 0, 0, 0});
+                    if (tiled)
+                        for (int rt = 0; rt * kFactorRowsTile < below; ++rt) rw.push_back({sidx, rt, 0, 0});
                     if (jb > 0)
                         for (int rt = 0; j0 + rt * kRowTile < d.nrow; ++rt) up.push_back({sidx, rt, 0, 0});
                 }
                 add(kFupd, jb, up);
                 add(kFdt, jb, dt);
+                add(kFrows, jb, rw);
             }
             std::vector<FItem> sy, fx;
             for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; ++q) {

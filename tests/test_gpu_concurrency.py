@@ -119,3 +119,28 @@ def test_dense_top_matches_supernodal_top(gpu, precision, tol, cols):
     assert W.bbox_rel_error(got, ref, w.positions) <= tol
     ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, 6)
     assert ok and W.bbox_rel_error(got, o, w.positions) <= (1e-10 if precision == "fp64" else 1e-6)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-6)])
+def test_warp_solves_match_cta_solves(gpu, precision, tol):
+    """The bottom levels solved one warp per supernode (arap_set_warp_rows)
+    against the CTA-per-supernode sweep of every level and against the
+    oracle: any front limit gives the same positions up to the order of sums,
+    and repeated calls repeat bit for bit."""
+    w = W.cfg_twisted_bar(h=0.05, iterations=8)
+    ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, w.iterations)
+    assert ok
+    outs = {}
+    for rows in (0, 64, 128, 256):
+        with gpu.ArapContext(w.V, w.faces) as ctx:
+            ctx.set_precision(precision, 1)
+            ctx.set_warp_rows(rows)
+            ctx.set_rest_positions(w.positions)
+            ctx.set_constraints(w.cidx, w.ctargets)
+            out = ctx.deform(w.iterations)
+            ctx.invalidate()
+            np.testing.assert_array_equal(ctx.deform(w.iterations), out)
+        outs[rows] = out
+        assert W.bbox_rel_error(out, ref, w.positions) <= (1e-10 if precision == "fp64" else 1e-6)
+    for rows in (64, 128, 256):
+        assert W.bbox_rel_error(outs[rows], outs[0], w.positions) <= tol

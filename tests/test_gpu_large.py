@@ -19,15 +19,10 @@ def test_bar_with_fronts_beyond_one_pass_matches_oracle(gpu):
         ctx.set_constraints(w.cidx, w.ctargets)
         got = ctx.deform(w.iterations)
         assert max(int(np.diff(ctx.symbolic()["block_ptr"]).max()), 0) > 0
-        # the FP64 form either runs (within its tolerance) or is refused as too large
+        # the plain FP64 form runs on the same fronts, within its tolerance
         ctx.set_precision("fp64", 0)
-        try:
-            got64 = ctx.deform(w.iterations)
-        except gpu.ArapError as e:
-            assert e.code == gpu.ARAP_ERR_UNSUPPORTED
-            got64 = None
+        got64 = ctx.deform(w.iterations)
     ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, w.iterations)
     assert ok
     assert W.bbox_rel_error(got, ref, w.positions) <= 1e-6
-    if got64 is not None:
-        assert W.bbox_rel_error(got64, ref, w.positions) <= 1e-10
+    assert W.bbox_rel_error(got64, ref, w.positions) <= 1e-10
