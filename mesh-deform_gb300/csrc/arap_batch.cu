@@ -431,7 +431,8 @@ __global__ void k_bbfixed(int m, int P, const int32_t *__restrict__ drow, const 
 // rest edges and the pose's current edges differenced in FP64
 __global__ void __launch_bounds__(256)
 k_blocal(int V, int P, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const float *__restrict__ w,
-         const Vec4<float> *__restrict__ redge, const Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ R) {
+         const Vec4<float> *__restrict__ redge, const Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ R,
+         const double *__restrict__ w64, const Vec4<double> *__restrict__ p64) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)V * P) return;
     const int i = (int)(t / P), p = (int)(t % P);
@@ -447,8 +448,9 @@ k_blocal(int V, int P, const int32_t *__restrict__ drow, const int32_t *__restri
         S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
         S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
     }
-    float Rm[3][3];
-    dev::rotation_from_cov<float>(S, Rm);
+    float Rm[3][3], spread;
+    dev::rotation_from_cov<float>(S, Rm, &spread);
+    if (!(spread >= dev::kPolarFallback)) dev::rotation_fp64(i, drow[i], drow[i + 1], dcol, w64, p64, pc64, P, p, Rm);
     R[3 * t + 0] = {Rm[0][0], Rm[0][1], Rm[0][2], 0.f};
     R[3 * t + 1] = {Rm[1][0], Rm[1][1], Rm[1][2], 0.f};
     R[3 * t + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], 0.f};
@@ -613,9 +615,9 @@ void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double
 }
 
 void launch_blocal(const DevSym &s, int P, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
-                   Vec4<float> *R, cudaStream_t st) {
+                   Vec4<float> *R, const double *w64, const Vec4<double> *p64, cudaStream_t st) {
     const int64_t n = (int64_t)s.V * P;
-    if (n) k_blocal<<<nblocks(n, 256), 256, 0, st>>>(s.V, P, s.drow, s.dcol, w32, redge, pc64, R);
+    if (n) k_blocal<<<nblocks(n, 256), 256, 0, st>>>(s.V, P, s.drow, s.dcol, w32, redge, pc64, R, w64, p64);
 }
 
 void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,

@@ -849,7 +849,8 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
         {
             Prof pr(ctx, ARAP_K_LOCAL);
             launch_local_step_mixed(d, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(),
-                                    ctx->pc64.as<Vec4<double>>(), ctx->R.as<Vec4<float>>(), st);
+                                    ctx->pc64.as<Vec4<double>>(), ctx->R.as<Vec4<float>>(), ctx->w64.as<double>(),
+                                    ctx->p64.as<Vec4<double>>(), st);
         }
         ctx->launches += 1;
         if (s.m == 0) continue;
@@ -900,7 +901,7 @@ int run_batch_iterations(arap_ctx *ctx, int P, int iterations) {
         {
             Prof pr(ctx, ARAP_K_LOCAL);
             launch_blocal(d, P, ctx->w32.as<float>(), ctx->redge.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
-                          ctx->bR.as<Vec4<float>>(), st);
+                          ctx->bR.as<Vec4<float>>(), ctx->w64.as<double>(), ctx->p64.as<Vec4<double>>(), st);
         }
         ctx->launches += 1;
         if (m == 0) continue;

@@ -5,6 +5,8 @@
 
 #include <cuda_runtime.h>
 
+#include "arap_kernels.h"
+
 namespace arapgpu {
 namespace dev {
 
@@ -69,8 +71,12 @@ __device__ __forceinline__ void hestenes3(T B[3][3], T V[3][3]) {
 // u1 = b1/|b1|, u2 = Gram-Schmidt(b2) and u3 = u1 x u2 (proper). With both
 // factors proper the sign of det(V U^T) lands on the smallest singular value,
 // as the reference's reflection fix puts it.
+// spread (optional): (sigma_2 + sigma_3) / sigma_1 of cov, which bounds how
+// well R is determined by it (the polar factor's condition number is about
+// its inverse); 0 for a zero covariance.
 template <typename T>
-__device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3]) {
+__device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3], T *spread = nullptr) {
+    if (spread) *spread = (T)0;
     T f2 = (T)0;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -100,6 +106,10 @@ __device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3])
     const int lo = o0 == 0 ? 1 : 0, hi = o0 == 2 ? 1 : 2;  // the other two, lo < hi
     const T nlo = lo == 0 ? nrm[0] : nrm[1], nhi = hi == 1 ? nrm[1] : nrm[2];
     const int o1 = (nhi > nlo) ? hi : lo;
+    if (spread) {
+        const T n0 = o0 == 0 ? nrm[0] : (o0 == 1 ? nrm[1] : nrm[2]);
+        *spread = (tsqrt(nlo) + tsqrt(nhi)) / tsqrt(n0);
+    }
     T v1[3], v2[3], v3[3];
     T u1[3], u2[3], u3[3];
     // columns picked by selects, not by indexing with o0/o1 (keeps every
@@ -141,6 +151,42 @@ __device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3])
         for (int j = 0; j < 3; ++j) R[i][j] = v1[i] * u1[j] + v2[i] * u2[j] + v3[i] * u3[j];
 }
 
+
+// The mixed form's rotation fit runs in FP32. Where the one-ring's covariance
+// is close to rank one ((sigma_2 + sigma_3) / sigma_1 below this bound, which
+// happens where a large handle move stretches a one-ring in the first
+// iterations), the FP32 rounding of the covariance is amplified by about the
+// inverse of that ratio, so the fit is redone in FP64 from the FP64 rest and
+// current positions: the FP64 arithmetic goes only where the stability needs
+// it (a fraction of a percent of the vertices).
+constexpr float kPolarFallback = 0.1f;
+
+// FP64 covariance of vertex i's one-ring (estimateRotations, arap.h:358-374)
+// and its rotation, from the rest positions p, current positions pc (element
+// k of vertex k's pose at k * stride + off) and the FP64 weights.
+__device__ __forceinline__ void rotation_fp64(int i, int e0, int e1, const int32_t *__restrict__ dcol,
+                                              const double *__restrict__ w64, const Vec4<double> *__restrict__ p,
+                                              const Vec4<double> *__restrict__ pc, int64_t stride, int64_t off,
+                                              float Rm[3][3]) {
+    const Vec4<double> pi = p[i], ci = pc[(int64_t)i * stride + off];
+    double S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int e = e0; e < e1; ++e) {
+        const int j = dcol[e];
+        const double wj = w64[e];
+        const Vec4<double> pj = p[j], cj = pc[(int64_t)j * stride + off];
+        const double ex = wj * (pi.x - pj.x), ey = wj * (pi.y - pj.y), ez = wj * (pi.z - pj.z);
+        const double fx = ci.x - cj.x, fy = ci.y - cj.y, fz = ci.z - cj.z;
+        S[0][0] += ex * fx; S[0][1] += ex * fy; S[0][2] += ex * fz;
+        S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
+        S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
+    }
+    double R[3][3];
+    rotation_from_cov<double>(S, R);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) Rm[a][b] = (float)R[a][b];
+}
 
 }  // namespace dev
 }  // namespace arapgpu

@@ -725,7 +725,8 @@ k_local_step(int V, const int32_t *__restrict__ drow, const int32_t *__restrict_
 __global__ void __launch_bounds__(256)
 k_local_step_mixed(int V, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
                    const float *__restrict__ w, const Vec4<float> *__restrict__ redge,
-                   const Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ R) {
+                   const Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ R,
+                   const double *__restrict__ w64, const Vec4<double> *__restrict__ p64) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     const Vec4<double> ci = pc64[i];
@@ -741,8 +742,9 @@ k_local_step_mixed(int V, const int32_t *__restrict__ drow, const int32_t *__res
         S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
         S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
     }
-    float Rm[3][3];
-    rotation_from_cov(S, Rm);
+    float Rm[3][3], spread;
+    rotation_from_cov(S, Rm, &spread);
+    if (!(spread >= dev::kPolarFallback)) dev::rotation_fp64(i, drow[i], e1, dcol, w64, p64, pc64, 1, 0, Rm);
     R[3 * (int64_t)i + 0] = {Rm[0][0], Rm[0][1], Rm[0][2], 0.f};
     R[3 * (int64_t)i + 1] = {Rm[1][0], Rm[1][1], Rm[1][2], 0.f};
     R[3 * (int64_t)i + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], 0.f};
@@ -2116,9 +2118,9 @@ void launch_rest_edges(const DevSym &s, const Vec4<double> *p64, Vec4<float> *re
 }
 
 void launch_local_step_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
-                             Vec4<float> *R, cudaStream_t st) {
+                             Vec4<float> *R, const double *w64, const Vec4<double> *p64, cudaStream_t st) {
     if (s.V == 0) return;
-    k_local_step_mixed<<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.drow, s.dcol, w32, redge, pc64, R);
+    k_local_step_mixed<<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.drow, s.dcol, w32, redge, pc64, R, w64, p64);
 }
 
 void launch_rhs_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,

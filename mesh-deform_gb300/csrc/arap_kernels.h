@@ -97,9 +97,11 @@ void launch_bfixed(const DevSym &s, const double *w64, const Vec4<double> *pc64,
                    cudaStream_t st);
 // FP32 rest edge vectors per adjacency entry, differenced in FP64
 void launch_rest_edges(const DevSym &s, const Vec4<double> *p64, Vec4<float> *redge, cudaStream_t st);
-// mixed form: FP32 covariance from FP32 rest edges and FP64-differenced current edges
+// mixed form: FP32 covariance from FP32 rest edges and FP64-differenced current edges;
+// one-rings whose covariance is close to rank one are fitted again in FP64
+// from the FP64 weights and rest positions p64
 void launch_local_step_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
-                             Vec4<float> *R, cudaStream_t st);
+                             Vec4<float> *R, const double *w64, const Vec4<double> *p64, cudaStream_t st);
 // mixed form: the RHS terms sum 1/2 w (Ri+Rj)(pi-pj) without bFixed
 void launch_rhs_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,
                       Vec4<float> *b, cudaStream_t st);
@@ -190,7 +192,7 @@ void launch_bsetup(const DevSym &s, int P, const Vec4<double> *p64, const double
 void launch_bbfixed(const DevSym &s, int P, const double *w64, const Vec4<double> *pc64, Vec4<double> *bfixed,
                     cudaStream_t st);
 void launch_blocal(const DevSym &s, int P, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
-                   Vec4<float> *R, cudaStream_t st);
+                   Vec4<float> *R, const double *w64, const Vec4<double> *p64, cudaStream_t st);
 void launch_brhs(const DevSym &s, int P, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,
                  Vec4<float> *b, cudaStream_t st);
 void launch_bresidual(const DevSym &s, int P, const double *w64, const double *diag64, const Vec4<double> *bfixed,

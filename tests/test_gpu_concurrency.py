@@ -127,6 +127,8 @@ def test_warp_solves_match_cta_solves(gpu, precision, tol):
     against the CTA-per-supernode sweep of every level and against the
     oracle: any front limit gives the same positions up to the order of sums,
     and repeated calls repeat bit for bit."""
+    from oracle import oracle as O
+
     w = W.cfg_twisted_bar(h=0.05, iterations=8)
     ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, w.iterations)
     assert ok
