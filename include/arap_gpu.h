@@ -195,11 +195,12 @@ int arap_set_pose_tile(arap_ctx *ctx, int32_t poses);
 int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes);
 
 /* The bottom levels of the elimination tree whose supernode fronts all have
-   at most `rows` rows (0: none; at most 256; the default is 128) are solved
-   one warp per supernode, many supernodes per CTA, before the CTA-per-
-   supernode sweep of the levels above (after it, backward). Any value gives
-   a correct result; it changes the order of some sums. Takes effect at the
-   next deform (which sets the problem up again). */
+   at most `rows` rows (0, the default: none; at most 256) are solved one warp
+   per supernode, many supernodes per CTA, before the CTA-per-supernode sweep
+   of the levels above (after it, backward). Any value gives a correct
+   result; it changes the order of some sums. Takes effect at the next deform
+   (which sets the problem up again). On the measured meshes a warp's task
+   takes longer than a CTA's, so the default leaves it off. */
 int arap_set_warp_rows(arap_ctx *ctx, int32_t rows);
 
 /* The top levels of the elimination tree, up to `max_columns` columns in all

@@ -27,7 +27,7 @@ namespace {
 constexpr int kTickets = 8;
 // fronts of at most this many rows at the bottom of the tree are solved one
 // warp per supernode (arap_set_warp_rows; 0: none)
-constexpr int kWarpRowsDefault = 128;
+constexpr int kWarpRowsDefault = 0;
 
 // Device buffer from the device's stream-ordered memory pool, allocated and
 // freed on the owning context's stream: growing or dropping a buffer never
