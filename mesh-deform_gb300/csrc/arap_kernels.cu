@@ -366,107 +366,110 @@ k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, T
     }
 }
 
-// Diagonal block jb of a front: Cholesky by one warp in registers; then warp 0
-// forms the block's inverse (for X = inv(L11) and the solves) while warps 1-7
-// solve the rows below against the block by forward substitution
-// (L_ib L_bb^T = A_ib), one row per thread, their first rows loaded while
-// warp 0 factors. Every step is written without divergent branches (selects
-// instead), so the shuffles of a step issue back to back and their latencies
-// overlap.
+// 1/sqrt(a) for the pivots: an FP32 seed refined by two Newton steps in the
+// working precision (a double's 53 bits from the seed's 22), which on GB300
+// costs far fewer FP64 instructions than a correctly rounded sqrt and a
+// division. Pivots outside the FP32 range take the plain route.
+template <typename TF> __device__ __forceinline__ TF pivot_rsqrt(TF a);
+template <> __device__ __forceinline__ float pivot_rsqrt(float a) { return rsqrtf(a); }
+template <> __device__ __forceinline__ double pivot_rsqrt(double a) {
+    if (!(a > 1e-30 && a < 1e30)) return 1.0 / sqrt(a);
+    double r = (double)rsqrtf((float)a);
+    r = r * (1.5 - 0.5 * a * r * r);
+    r = r * (1.5 - 0.5 * a * r * r);
+    return r;
+}
+
+constexpr int kFdtThreads = 128;
+constexpr int kTri = NB * (NB + 1) / 2;  // entries of a block's lower triangle
+
+// Diagonal block jb of a front: its Cholesky factor and that factor's inverse
+// (written to Dinv for k_frows, which solves the rows below, and for k_fx).
+// Four warps share each step through shared memory, every lane with a useful
+// entry, so the FP64 form's arithmetic uses all four schedulers of the SM (a
+// GB300 SM issues about two FP64 FMAs per clock; a single warp's FP64 chain
+// runs at a quarter of that). Right-looking: step k takes the pivot, scales
+// column k and updates the trailing lower triangle, the operations of a
+// column-by-column Cholesky in the same order. The trailing entries of step k
+// are the first (31-k)(32-k)/2 of a table of the triangle ordered by column,
+// last column first. The inverse X = inv(L) is formed row by row: row i is
+// -rinv(i) times row i of L times the rows above, with the sum over k split
+// in four quarters (one per warp) added in a fixed order.
 template <typename TF>
-__global__ void __launch_bounds__(kFactorThreads)
+__global__ void __launch_bounds__(kFdtThreads)
 k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF *__restrict__ Lval,
       TF *__restrict__ Dinv, int *err) {
-    __shared__ TF Lb[NB][NB + 1];  // the factored block, row-major: Lb[r][c] = L(r, c)
+    __shared__ TF A[NB][NB + 1];   // the block, A[r][c] = L(r, c) once factored
+    __shared__ TF X[NB][NB + 1];   // its inverse, X[r][c]
+    __shared__ TF part[4][NB];     // quarter sums of the inverse's current row
     __shared__ TF rinv[NB];        // 1 / L(r, r)
-    const FItem it = items[blockIdx.x];
-    const SnInfo d = sn[it.sn];
+    __shared__ uint8_t tri_i[kTri], tri_j[kTri];
+    __shared__ int s_bad;
+    const SnInfo d = sn[items[blockIdx.x].sn];
     const int n = d.nrow, nc = d.ncol;
     const int j0 = jb * NB, w = min(NB, nc - j0);
     TF *P = Lval + d.panel_off;
-    const int tid = threadIdx.x, lane = tid & 31;
-    // the rows below the block: warps 1.. of the CTA, or warp 0 itself after
-    // the inverse when the CTA is a single warp; none when the item leaves
-    // them to k_frows (it.a != 0)
-    const bool solo = blockDim.x == 32;
-    const int row_threads = solo ? 32 : (int)blockDim.x - 32;
-    const int i_first = it.a ? n : j0 + w + (solo ? lane : tid - 32);
-    TF a[NB];
-    TF myinv = (TF)0;  // warp 0: 1 / L(lane, lane)
-    if (tid < 32) {
-        // row `lane` of the block, right-looking Cholesky (the operations of a
-        // column-by-column update, in the same order)
-#pragma unroll
-        for (int c = 0; c < NB; ++c) a[c] = (lane < w && c <= lane) ? P[(int64_t)(j0 + c) * n + j0 + lane] : (TF)0;
-        bool bad = false;
-#pragma unroll
-        for (int k = 0; k < NB; ++k) {
-            if (k < w) {
-                TF akk = __shfl_sync(0xffffffffu, a[k], k);
-                bad |= !(akk > (TF)0);
-                akk = (akk > (TF)0) ? akk : (TF)1;
-                const TF dk = tsqrt(akk), inv = (TF)1 / dk;
-                a[k] = (lane == k) ? dk : a[k] * inv;  // zero above the diagonal stays zero
-                myinv = (lane == k) ? inv : myinv;
-                const TF lk = a[k];
-#pragma unroll
-                for (int c = k + 1; c < NB; ++c)  // L(c, k) from lane c
-                    a[c] -= ((lane >= c) ? lk : (TF)0) * __shfl_sync(0xffffffffu, lk, c);
-            }
+    const int tid = threadIdx.x;
+    if (tid == 0) s_bad = 0;
+    for (int q = tid; q < NB * NB; q += kFdtThreads) {
+        const int r = q % NB, c = q / NB;
+        A[r][c] = (r < w && c <= r) ? P[(int64_t)(j0 + c) * n + j0 + r] : (TF)0;
+        X[r][c] = (TF)0;
+    }
+    // triangle table: column jj from NB-1 down to 0, rows jj..NB-1
+    for (int t = tid; t < kTri; t += kFdtThreads) {
+        int jj = NB - 1, base = 0;
+        while (t >= base + (NB - jj)) {
+            base += NB - jj;
+            --jj;
         }
-        if (bad && lane == 0) atomicOr(err, kErrNotSpd);
-#pragma unroll
-        for (int c = 0; c < NB; ++c) {
-            Lb[lane][c] = a[c];  // zero above the diagonal and outside the block
-            if (lane < w && c <= lane) P[(int64_t)(j0 + c) * n + j0 + lane] = a[c];
-        }
-        rinv[lane] = myinv;
-    } else if (i_first < n) {
-#pragma unroll
-        for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i_first] : (TF)0;
+        tri_j[t] = (uint8_t)jj;
+        tri_i[t] = (uint8_t)(jj + (t - base));
     }
     __syncthreads();
-    if (tid < 32) {
-        // X = inv(L), lane = row, right-looking: at step t row t of X lacks
-        // only the division by L(t, t); it is broadcast and every later row i
-        // subtracts L(i, t) X(t, :)
-        TF y[NB];
-#pragma unroll
-        for (int j = 0; j < NB; ++j) y[j] = (j == lane && lane < w) ? (TF)1 : (TF)0;
-#pragma unroll
-        for (int t = 0; t < NB; ++t) {
-            if (t < w) {
-                const TF m = (lane > t) ? a[t] : (TF)0;
-#pragma unroll
-                for (int j = 0; j <= t; ++j) {
-                    const TF yj = (lane == t) ? y[j] * myinv : y[j];
-                    y[j] = yj - m * __shfl_sync(0xffffffffu, yj, t);  // X(t, j) from lane t
-                }
+    for (int k = 0; k < w; ++k) {
+        if (tid == 0) {
+            TF a = A[k][k];
+            if (!(a > (TF)0)) {
+                s_bad = 1;
+                a = (TF)1;
             }
+            const TF r = pivot_rsqrt(a);
+            A[k][k] = a * r;
+            rinv[k] = r;
         }
-        // column-major: Dinv[c * NB + r] = X(r, c); zero above the diagonal
-        TF *D = Dinv + d.dinv_off + (int64_t)jb * NB * NB;
-#pragma unroll
-        for (int c = 0; c < NB; ++c) D[c * NB + lane] = y[c];
-        if (!solo) return;
+        __syncthreads();
+        const TF r = rinv[k];
+        for (int i = k + 1 + tid; i < w; i += kFdtThreads) A[i][k] *= r;
+        __syncthreads();
+        const int T = (NB - 1 - k) * (NB - k) / 2;  // entries of columns k+1..NB-1
+        for (int t = tid; t < T; t += kFdtThreads) {
+            const int i = tri_i[t], jj = tri_j[t];
+            if (i < w) A[i][jj] -= A[i][k] * A[jj][k];
+        }
+        __syncthreads();
     }
-    for (int i = i_first; i < n; i += row_threads) {
-        if (solo || i != i_first) {
-#pragma unroll
-            for (int c = 0; c < NB; ++c) a[c] = (c < w) ? P[(int64_t)(j0 + c) * n + i] : (TF)0;
-        }
-        // L(i, r) = (A(i, r) - sum_{c < r} L(i, c) L(r, c)) / L(r, r)
-#pragma unroll
-        for (int r = 0; r < NB; ++r) {
-            TF acc = a[r];
-#pragma unroll
-            for (int c = 0; c < r; ++c) acc -= a[c] * Lb[r][c];
-            a[r] = acc * rinv[r];  // zero for r >= w (rinv and the row are zero there)
-        }
-#pragma unroll
-        for (int r = 0; r < NB; ++r)
-            if (r < w) P[(int64_t)(j0 + r) * n + i] = a[r];
+    if (s_bad && tid == 0) atomicOr(err, kErrNotSpd);
+    // the factored block back into the panel
+    for (int q = tid; q < NB * NB; q += kFdtThreads) {
+        const int r = q % NB, c = q / NB;
+        if (r < w && c <= r) P[(int64_t)(j0 + c) * n + j0 + r] = A[r][c];
     }
+    // X row by row: X(i, c) = -rinv(i) sum_{c <= k < i} L(i, k) X(k, c), X(i, i) = rinv(i)
+    const int c = tid & 31, qk = tid >> 5;  // column, quarter of the k range
+    for (int i = 0; i < w; ++i) {
+        TF acc = (TF)0;
+        for (int k = c + ((qk - c) & 3); k < i; k += 4) acc += A[i][k] * X[k][c];  // k >= c, k = qk mod 4
+        part[qk][c] = acc;
+        __syncthreads();
+        if (tid < NB && c <= i) {
+            const TF sum = (part[0][c] + part[1][c]) + (part[2][c] + part[3][c]);
+            X[i][c] = (c == i) ? rinv[i] : -sum * rinv[i];
+        }
+        __syncthreads();
+    }
+    TF *D = Dinv + d.dinv_off + (int64_t)jb * NB * NB;  // column-major: D[c * NB + r] = X(r, c)
+    for (int q = tid; q < NB * NB; q += kFdtThreads) D[q] = X[q % NB][q / NB];
 }
 
 // The rows below diagonal block jb of a front, 64 rows per CTA, when the plan
@@ -2137,21 +2140,7 @@ void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *it
     switch (fl.kind) {
     case kFea: k_fea<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, s.child, s.relind, Lval, Upd); break;
     case kFupd: k_fupd<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval); break;
-    case kFdt: {
-        // many small fronts (the wide lower levels): one-warp CTAs, so that
-        // more of the register-heavy blocks fit on an SM at once; few large
-        // fronts: 256 threads for the rows below the block
-        static const int sms = [] {  // initialised once, thread-safe
-            int dev = 0, n = 0;
-            if (cudaGetDevice(&dev) != cudaSuccess ||
-                cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-                return 1;
-            return n;
-        }();
-        const int threads = fl.count > 2 * sms ? 32 : kFactorThreads;
-        k_fdt<TF><<<fl.count, threads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv, err);
-        break;
-    }
+    case kFdt: k_fdt<TF><<<fl.count, kFdtThreads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv, err); break;
     case kFrows: k_frows<TF><<<fl.count, kFactorThreads, 0, st>>>(it, fl.jb, s.sn, Lval, Dinv); break;
     case kFsyrk: k_fsyrk<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Upd); break;
     case kFx: k_fx<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Dinv, X, L21, L21T); break;

@@ -175,7 +175,7 @@ cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64);
 // most columns of the dense top (its T and f vectors must fit the device and shared memory)
 constexpr int kDenseTopCols = 4096;
 constexpr int kDenseTopDefault = 2048;  // the default column cap
-constexpr int kTopRhs = 16;  // columns of T one CTA of the inversion forms
+constexpr int kTopRhs = 8;   // columns of T one CTA of the inversion forms
 // ---- many poses of one mesh and constraint set (arap_batch.cu); arrays of
 // (vertex, pose) pairs are vertex-major, element (k, p) at k * P + p
 size_t batch_solve_smem_bytes(int max_ldx, int max_ld21, int pt);

@@ -20,8 +20,10 @@
 #include "arap_symbolic.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <numeric>
+#include <thread>
 
 namespace arapgpu {
 
@@ -102,26 +104,61 @@ bool build_topology(int V, int F, const int32_t *faces, Topology &topo, std::str
 
 namespace {
 
-struct NestedDissection {
+// State shared by every worker of one dissection: the graph and the arrays
+// indexed by vertex. A worker only writes the entries of the vertices of its
+// own set; it reads `inset` of neighbours outside the set, which another
+// worker may be writing at the same time, so those accesses are relaxed
+// atomics. Stamps come from one atomic counter, so a set's stamp is never
+// seen on a vertex outside the set: the result does not depend on timing.
+struct NdShared {
     const int32_t *rowptr, *col;
     int n;
-    // two BFS buffers (queue + level per vertex): a trial BFS from a new root
-    // fills the spare one, which becomes current when the trial is kept
-    std::vector<int32_t> inset, seen, lev_buf[2], queue_buf[2];
-    int cur = 0;
-    int32_t stamp = 0;
-    std::vector<int32_t> *perm, *block_ptr;
+    std::vector<int32_t> inset, seen, lev_buf[2];
+    std::atomic<int32_t> stamp{0};
+    int32_t next_stamp() { return stamp.fetch_add(1, std::memory_order_relaxed) + 1; }
+};
 
+inline int32_t load_rlx(const int32_t *p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
+inline void store_rlx(int32_t *p, int32_t v) { __atomic_store_n(p, v, __ATOMIC_RELAXED); }
+
+// Output of a recursion: the vertices in elimination order and the sizes of
+// the blocks (leaves and separators) they form.
+struct NdOut {
+    std::vector<int32_t> perm, sizes;
     void emit(const std::vector<int32_t> &S) {
-        perm->insert(perm->end(), S.begin(), S.end());
-        block_ptr->push_back((int32_t)perm->size());
+        perm.insert(perm.end(), S.begin(), S.end());
+        sizes.push_back((int32_t)S.size());
+    }
+    void append(const NdOut &o) {
+        perm.insert(perm.end(), o.perm.begin(), o.perm.end());
+        sizes.insert(sizes.end(), o.sizes.begin(), o.sizes.end());
+    }
+};
+
+// Sets of at least this many vertices dissect their two sides on two threads
+// (down to a depth of kNdParallelDepth: at most 2^depth threads at once).
+constexpr int kNdParallelMin = 16384;
+constexpr int kNdParallelDepth = 3;
+
+struct NdWorker {
+    NdShared *sh;
+    // two BFS queues (indexed by position): a trial BFS from a new root
+    // fills the spare one, which becomes current when the trial is kept
+    std::vector<int32_t> queue_buf[2];
+    int cur = 0;
+
+    NdWorker(NdShared *s, size_t cap) : sh(s) {
+        queue_buf[0].resize(cap);
+        queue_buf[1].resize(cap);
     }
 
     // BFS inside the stamped set into buffer `buf`; neighbours visited in CSR
     // order. Returns the number of levels, level offsets into the queue in levptr.
     int bfs(int32_t setstamp, int32_t root, std::vector<int32_t> &levptr, int buf) {
-        int32_t *queue = queue_buf[buf].data(), *lev = lev_buf[buf].data();
-        const int32_t bs = ++stamp;
+        const int32_t *rowptr = sh->rowptr, *col = sh->col;
+        int32_t *queue = queue_buf[buf].data(), *lev = sh->lev_buf[buf].data();
+        int32_t *inset = sh->inset.data(), *seen = sh->seen.data();
+        const int32_t bs = sh->next_stamp();
         int head = 0, tail = 0;
         queue[tail++] = root;
         seen[root] = bs;
@@ -133,7 +170,7 @@ struct NestedDissection {
             ++head;
             for (int32_t q = rowptr[v]; q < rowptr[v + 1]; ++q) {
                 const int32_t u = col[q];
-                if (inset[u] != setstamp || seen[u] == bs) continue;
+                if (load_rlx(inset + u) != setstamp || seen[u] == bs) continue;
                 seen[u] = bs;
                 lev[u] = lev[v] + 1;
                 queue[tail++] = u;
@@ -146,17 +183,19 @@ struct NestedDissection {
     // S arrives in any order; only the blocks emitted are sorted, and the
     // smallest vertex of S is the first BFS root, so the result is that of
     // recursing on sorted sets.
-    void recurse(std::vector<int32_t> S) {
+    void recurse(std::vector<int32_t> S, NdOut &out, int depth) {
         const int ns = (int)S.size();
         if (ns <= kNdLeaf) {
             std::sort(S.begin(), S.end());
-            emit(S);
+            out.emit(S);
             return;
         }
-        const int32_t setstamp = ++stamp;
+        int32_t *inset = sh->inset.data();
+        const int32_t *rowptr = sh->rowptr, *col = sh->col;
+        const int32_t setstamp = sh->next_stamp();
         int32_t smin = S[0];
         for (int32_t v : S) {
-            inset[v] = setstamp;
+            store_rlx(inset + v, setstamp);
             smin = std::min(smin, v);
         }
         std::vector<int32_t> levptr;
@@ -165,12 +204,12 @@ struct NestedDissection {
             // several components, each in order of its smallest vertex
             std::sort(S.begin(), S.end());
             for (int32_t v : S) {
-                if (inset[v] != setstamp) continue;
+                if (load_rlx(inset + v) != setstamp) continue;
                 const int hl = bfs(setstamp, v, levptr, cur);
                 std::vector<int32_t> comp(queue_buf[cur].begin(), queue_buf[cur].begin() + levptr[hl]);
-                const int32_t cs = ++stamp;
-                for (int32_t u : comp) inset[u] = cs;
-                recurse(std::move(comp));
+                const int32_t cs = sh->next_stamp();
+                for (int32_t u : comp) store_rlx(inset + u, cs);
+                recurse(std::move(comp), out, depth);
             }
             return;
         }
@@ -182,27 +221,27 @@ struct NestedDissection {
             for (int q = levptr[h - 1]; q < levptr[h]; ++q) {
                 const int32_t v = queue[q];
                 int32_t deg = 0;
-                for (int32_t e = rowptr[v]; e < rowptr[v + 1]; ++e) deg += (inset[col[e]] == setstamp);
+                for (int32_t e = rowptr[v]; e < rowptr[v + 1]; ++e) deg += (load_rlx(inset + col[e]) == setstamp);
                 if (best < 0 || deg < bestdeg || (deg == bestdeg && v < best)) { best = v; bestdeg = deg; }
             }
             const int h2 = bfs(setstamp, best, lp2, cur ^ 1);
             if (h2 > h) { h = h2; levptr.swap(lp2); cur ^= 1; }
             else break;
         }
-        const int32_t *queue = queue_buf[cur].data(), *lev = lev_buf[cur].data();
+        const int32_t *queue = queue_buf[cur].data(), *lev = sh->lev_buf[cur].data();
         if (h < 3) {
             std::sort(S.begin(), S.end());
-            emit(S);
+            out.emit(S);
             return;
         }
         int bestk = -1;
         int64_t bsz = 0, bdiff = 0;
         for (int k = 1; k <= h - 2; ++k) {
-            const int64_t a = levptr[k], s = levptr[k + 1] - levptr[k], b = (int64_t)ns - a - s;
+            const int64_t a = levptr[k], sz = levptr[k + 1] - levptr[k], b = (int64_t)ns - a - sz;
             const int64_t mn = std::min(a, b);
             if (mn * kNdBalDen < (int64_t)kNdBalNum * ns) continue;
             const int64_t d = a > b ? a - b : b - a;
-            if (bestk < 0 || s < bsz || (s == bsz && d < bdiff)) { bestk = k; bsz = s; bdiff = d; }
+            if (bestk < 0 || sz < bsz || (sz == bsz && d < bdiff)) { bestk = k; bsz = sz; bdiff = d; }
         }
         if (bestk < 0) {
             bestk = h - 2;
@@ -217,15 +256,30 @@ struct NestedDissection {
             bool touches = false;
             for (int32_t e = rowptr[v]; e < rowptr[v + 1] && !touches; ++e) {
                 const int32_t u = col[e];
-                touches = (inset[u] == setstamp && lev[u] == k + 1);
+                touches = (load_rlx(inset + u) == setstamp && lev[u] == k + 1);
             }
             (touches ? Sep : A).push_back(v);
         }
         B.assign(queue + levptr[k + 1], queue + levptr[h]);
         std::sort(Sep.begin(), Sep.end());
-        recurse(std::move(A));
-        recurse(std::move(B));
-        emit(Sep);
+        if (ns >= kNdParallelMin && depth < kNdParallelDepth) {
+            // the near side on a second thread, the far side here; blocks are
+            // emitted in the sequential order (near, far, separator)
+            NdOut outA, outB;
+            const size_t capA = A.size() + 1;
+            std::thread th([this, &outA, capA, depth](std::vector<int32_t> a) {
+                NdWorker w(sh, capA);
+                w.recurse(std::move(a), outA, depth + 1);
+            }, std::move(A));
+            recurse(std::move(B), outB, depth + 1);
+            th.join();
+            out.append(outA);
+            out.append(outB);
+        } else {
+            recurse(std::move(A), out, depth);
+            recurse(std::move(B), out, depth);
+        }
+        out.emit(Sep);
     }
 };
 
@@ -236,21 +290,22 @@ void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int3
     perm.clear();
     block_ptr.assign(1, 0);
     if (n <= 0) return;
-    NestedDissection nd;
-    nd.rowptr = rowptr;
-    nd.col = col;
-    nd.n = n;
-    nd.inset.assign(n, 0);
-    nd.seen.assign(n, 0);
-    for (int b = 0; b < 2; ++b) {
-        nd.lev_buf[b].assign(n, 0);
-        nd.queue_buf[b].assign(n, 0);
-    }
-    nd.perm = &perm;
-    nd.block_ptr = &block_ptr;
+    NdShared sh;
+    sh.rowptr = rowptr;
+    sh.col = col;
+    sh.n = n;
+    sh.inset.assign(n, 0);
+    sh.seen.assign(n, 0);
+    for (int b = 0; b < 2; ++b) sh.lev_buf[b].assign(n, 0);
+    NdWorker w(&sh, (size_t)n);
     std::vector<int32_t> S(n);
     std::iota(S.begin(), S.end(), 0);
-    nd.recurse(std::move(S));
+    NdOut out;
+    out.perm.reserve(n);
+    w.recurse(std::move(S), out, 0);
+    perm.swap(out.perm);
+    block_ptr.reserve(out.sizes.size() + 1);
+    for (int32_t sz : out.sizes) block_ptr.push_back(block_ptr.back() + sz);
 }
 
 // ---------------------------------------------------------------------------
@@ -548,10 +603,8 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
                     const int j0 = jb * kDiagBlock;
                     if (j0 >= d.ncol) continue;
                     const int below = d.nrow - std::min(d.ncol, j0 + kDiagBlock);
-                    const bool tiled = below > kFactorRowsInline;
-                    dt.push_back({sidx, tiled ? 1 : 0, 0, 0});
-                    if (tiled)
-                        for (int rt = 0; rt * kFactorRowsTile < below; ++rt) rw.push_back({sidx, rt, 0, 0});
+                    dt.push_back({sidx, 0, 0, 0});
+                    for (int rt = 0; rt * kFactorRowsTile < below; ++rt) rw.push_back({sidx, rt, 0, 0});
                     if (jb > 0)
                         for (int rt = 0; j0 + rt * kRowTile < d.nrow; ++rt) up.push_back({sidx, rt, 0, 0});
                 }

@@ -86,19 +86,16 @@ struct FItem {
 // Factorisation launch plan, level by level (leaves first):
 //   kFea   extend-add, item = (sn, first parent column, end parent column)
 //   kFupd  left-looking update of block column jb, item = (sn, row tile)
-//   kFdt   diagonal block jb: factor, invert, solve the rows below, item = (sn)
+//   kFdt   diagonal block jb: factor and invert, item = (sn)
 //   kFsyrk Schur complement U -= L21 L21^T, item = (sn, row tile, column tile)
 //   kFx    X = inv(L11) column block jb and the solve copies, item = (sn, jb)
-//   kFrows the rows below diagonal block jb, item = (sn, row tile); kFdt items
-//          of such fronts have a = 1 (their rows below are left to kFrows)
+//   kFrows the rows below diagonal block jb, item = (sn, row tile)
 enum FactorKind { kFea = 0, kFupd = 1, kFdt = 2, kFsyrk = 3, kFx = 4, kFrows = 5 };
 // Tile sizes of the plan's items: rows of a kFupd tile, rows of a kFrows
-// tile, side of a kFsyrk tile; fronts with more than kFactorRowsInline rows
-// below a diagonal block get kFrows items
+// tile, side of a kFsyrk tile
 constexpr int kFactorUpdRows = 32;
 constexpr int kFactorRowsTile = 64;
 constexpr int kFactorSyrkTile = 32;
-constexpr int kFactorRowsInline = 224;
 struct FactorLaunch {
     int32_t kind, jb, item_off, count;
 };

@@ -63,6 +63,9 @@ CASES = [
     lambda: W.cfg_twisted_bar(h=0.05),
     lambda: W.cfg_noisy_sphere(level=5),
     lambda: W.cfg_pose_batch(level=4, n_poses=1),
+    # large enough that the dissection runs its two sides on threads
+    lambda: W.cfg_twisted_bar(h=0.025),
+    lambda: W.cfg_noisy_sphere(level=7),
 ]
 
 
@@ -142,3 +145,14 @@ def test_workload_sizes():
     p = W.cfg_pose_batch(level=5, n_poses=4)
     assert p.V == 10242 and p.poses.shape == (4, 2058, 3)
     assert W.icosphere(7)[0].shape == (163842, 3)
+
+
+def test_threaded_dissection_is_deterministic(gpu):
+    """The dissection of a large free graph splits over threads; repeated
+    analyses give the same ordering, tree and blocks every time."""
+    w = W.cfg_twisted_bar(h=0.025)
+    first = gpu.analyze_pattern(w.V, w.faces, w.cidx)
+    for _ in range(3):
+        again = gpu.analyze_pattern(w.V, w.faces, w.cidx)
+        for key in ("perm", "etree", "block_ptr"):
+            np.testing.assert_array_equal(first[key], again[key])
