@@ -1,20 +1,28 @@
 #!/usr/bin/env python
 """ARAP deformation benchmark: ARAP iterations/s on one GB300.
 
-Workload (one "step"): one dirty deform of the twisted bar -- the 10x1x1 box
-surface at 0.025 spacing (67,202 vertices, 134,400 triangles), anchors x<0.2
-(2,801), handles x>9.8 (2,801) turned 90 deg about the bar axis and shifted
-(0,0.5,0) -- in the mixed-precision form, 30 local/global iterations. A dirty
-deform is what the reference does after setConstraint (inc/deform/arap.h:102-129):
-cotan weights, constrained Laplacian and its factorisation, then the iterations.
-Inputs are seeded synthetic meshes (the reference publishes no data set).
+Workload (one "step"): 16 concurrent dirty deforms (one per host thread, as
+the reference arm runs one request per host thread) of the twisted bar -- the
+10x1x1 box surface at 0.025 spacing (67,202 vertices, 134,400 triangles),
+anchors x<0.2 (2,801), handles x>9.8 (2,801) turned 90 deg about the bar axis
+and shifted (0,0.5,0) -- in the mixed-precision form (FP64 numeric factor,
+FP32 local steps and solves, two FP64-residual refinement solves per
+iteration), 30 local/global iterations each. A dirty deform is what the
+reference does after setConstraint (inc/deform/arap.h:102-129): the symbolic
+analysis of the constrained Laplacian (redone on every request, as
+SimplicialLDLT::compute does), cotan weights, numeric factorisation, then the
+iterations. Inputs are seeded synthetic meshes (the reference publishes no
+data set).
 
-value: iterations/s with the rest pose and targets already in device memory
-       (arap_invalidate + arap_deform, output left on the device), timed with
-       CUDA events on the library's stream; L2 (129 MB) is flushed before each
-       step by writing a 256 MB buffer, outside the timed events.
+value: iterations/s with the rest pose and targets already in device memory,
+       timed with CUDA events from a start event on the idle device to the
+       last request's end event; L2 (129 MB) is flushed before each step by
+       writing a 256 MB buffer, outside the timed events.
 e2e:   the same steps through the C ABI with host buffers: pinned rest
-       positions and targets copied in, deformed positions copied out.
+       positions and targets copied in, deformed positions copied out, wall
+       clock; one end-to-end step follows each timed device step.
+repose_refactor: the same steps with the symbolic analysis kept (the
+       constrained set does not change), reported beside the headline.
 cpu_baseline: the FP64 C restatement of arap.h (the oracle) on one host core,
        full requests of the same workload; its output also gives the error of
        the GPU result (bbox-diagonal-relative, stated on every line).
@@ -22,7 +30,8 @@ cpu_baseline: the FP64 C restatement of arap.h (the oracle) on one host core,
 --impl reference times the reference's CPU path (the oracle restatement,
 since the reference needs Eigen and cannot be built) with one independent
 request per host thread.
-Multi-GPU: replicas only (one independent replica per rank, no collective).
+Multi-GPU: replicas only (one independent replica per rank, no collective);
+--gpus N without torchrun starts N replicas through torch.distributed.run.
 """
 from __future__ import annotations
 
@@ -698,21 +707,22 @@ def run_requests(args):
 
     def device_step():
         """One step with inputs resident on the device: every request is a
-        dirty deform started by its own host thread. Device time = the union
-        of the requests' spans on their streams (first start event to last end
-        event), each start recorded before the request's first enqueue."""
+        dirty deform started by its own host thread. Device time = from a
+        start event recorded on the first request's stream before the threads
+        are dispatched (the device is idle then) to the last request's end
+        event, recorded on its stream after its enqueue: the union of the
+        requests' spans, host analysis and enqueue gaps included."""
         flush.zero_()
         torch.cuda.synchronize()
-        ref = torch.cuda.Event(enable_timing=True)
-        ref.record(streams[0])
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(N)]
+        start = torch.cuda.Event(enable_timing=True)
+        start.record(streams[0])
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(N)]
 
         def one(i):
             c = ctxs[i]
             c.invalidate()
-            ev[i][0].record(streams[i])
             rc = c.lib.arap_deform_async(c.h, w.iterations, None)
-            ev[i][1].record(streams[i])
+            ends[i].record(streams[i])
             if rc != G.ARAP_OK:
                 raise G.ArapError(rc, c.lib.arap_last_error(c.h).decode())
             c.wait()
@@ -720,9 +730,7 @@ def run_requests(args):
 
         launches = sum(pool.map(one, range(N)))
         torch.cuda.synchronize()
-        t0 = min(ref.elapsed_time(a) for a, _ in ev)
-        t1 = max(ref.elapsed_time(b) for _, b in ev)
-        return t1 - t0, launches
+        return max(start.elapsed_time(e) for e in ends), launches
 
     # ---- end to end through the C ABI with pinned host buffers: rest pose,
     # constraint indices and targets in, deformed positions out, per request
@@ -883,8 +891,9 @@ def run_requests(args):
              "step": f"{N} concurrent dirty deform requests, one host thread each (symbolic analysis "
                      f"{'kept' if args.cached_analysis else 'redone'}, weights, numeric factorisation, "
                      f"{w.iterations} iterations)",
-             "timing": "union of the requests' device spans (CUDA events on each request's stream, the start "
-                       "recorded before its first enqueue)"}
+             "timing": "CUDA events: a start event on the idle device before the requests' threads are "
+                       "dispatched, an end event on each request's stream after its enqueue; the step is the "
+                       "latest end"}
     if mixed:
         extra.update({"factor": f"fp{args.factor_bits}",
                       "fp64_residual_solves_per_iteration": 1 + args.refine})

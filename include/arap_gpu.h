@@ -86,10 +86,11 @@ int arap_set_precision(arap_ctx *ctx, int32_t precision, int32_t refine_steps);
 
 /* Numeric factorisation of the MIXED form: bits = 64 (the default) factors
    the constrained Laplacian in FP64, as SimplicialLDLT<SparseMatrix<double>>
-   does (arap.h:337,462), and rounds the factor's solve arrays to FP32 for the
-   triangular solves; bits = 32 factors in FP32 (cheaper set-up; the FP64
-   residual refinement still carries the accuracy). The FP64 form always
-   factors in FP64. Marks the context dirty. */
+   does (arap.h:337,462), rounds the factor to FP32 and forms from it, in
+   FP32, the inverted blocks the FP32 triangular solves multiply by; bits = 32
+   factors in FP32 (cheaper set-up; the FP64 residual refinement still
+   carries the accuracy). The FP64 form always factors in FP64. Marks the
+   context dirty. */
 int arap_set_factor_precision(arap_ctx *ctx, int32_t bits);
 
 /* Replaces initializeMeshGeometry (arap.h:162-168): the rest pose _p, read

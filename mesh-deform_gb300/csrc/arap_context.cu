@@ -144,7 +144,7 @@ struct arap_ctx {
     DevBuf rest, targets, out;
     DevBuf drow, dcol, dent, oldidx, amap, dmap, sn, rows, relind, child, level_sn, fitems;
     DevBuf w64, w32, p64, pc64, p32, pc32, R, diag64, bfixed, b, sol, uvec, Lval, Dinv, Upd, Xinv, L21, L21T, redge;
-    DevBuf X64, L21_64, L21T_64, Ttop64;  // the mixed form's FP64 factor outputs (rounded into Xinv, L21, L21T, Ttop)
+    DevBuf Lval32, Dinv32;  // the mixed form's FP64 factor rounded to FP32 (the inverses for the solves are formed from it)
     DevBuf errw, ticket, flags, energy;
     DevBuf cidx_dev, handle_dev, tabs_dev;  // arap_pose_targets inputs
     DevBuf vf_ptr, vf_face, fnorm, vnorm;    // vertex normals
@@ -203,8 +203,8 @@ struct arap_ctx {
                 &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
                 &errw, &ticket, &flags, &energy, &cidx_dev, &handle_dev, &tabs_dev, &vf_ptr, &vf_face, &fnorm,
                 &vnorm, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout, &bftop, &bytop, &bws,
-                &bticket, &bflags, &top_col, &top_gptr, &top_gidx, &tdpos, &top_items, &Ttop, &ytop, &X64, &L21_64,
-                &L21T_64, &Ttop64};
+                &bticket, &bflags, &top_col, &top_gptr, &top_gidx, &tdpos, &top_items, &Ttop, &ytop, &Lval32,
+                &Dinv32};
     }
 };
 
@@ -369,10 +369,8 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     const int nt = choose_dense_top(s, dense_cap(ctx)).ncols;
     add(ctx->Ttop, std::max<size_t>(nt > 0 ? dense_top_elems(nt) : 0, 1) * sizeof(T));
     if (f64f) {
-        add(ctx->X64, (size_t)std::max<int64_t>(s.x_size, 1) * sizeof(double));
-        add(ctx->L21_64, (size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(double));
-        add(ctx->L21T_64, (size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(double));
-        add(ctx->Ttop64, std::max<size_t>(nt > 0 ? dense_top_elems(nt) : 0, 1) * sizeof(double));
+        add(ctx->Lval32, (size_t)std::max<int64_t>(s.panel_size, 1) * sizeof(float));
+        add(ctx->Dinv32, (size_t)std::max<int64_t>(s.dinv_size, 1) * sizeof(float));
     }
     add(ctx->ytop, std::max<size_t>(2 * (size_t)dense_ld(nt), 1) * sizeof(Vec4<T>));  // y_top, then f_top
     if (n_poses > 0) {
@@ -637,19 +635,15 @@ int setup_alloc(arap_ctx *ctx) {
 }
 
 // Enqueues the numeric factorisation in precision TF: the constrained
-// Laplacian assembled into the supernodal panels (and bFixed), the
-// multifrontal Cholesky plan level by level, the solve arrays X = inv(L11),
-// L21, L21^T, and the dense top's T = inv(L_top).
+// Laplacian assembled into the supernodal panels (and bFixed) and the
+// multifrontal Cholesky plan level by level (every launch but the inverses').
 template <typename TF>
-int factor_enqueue(arap_ctx *ctx, TF *Lval, TF *Upd, TF *Dinv, TF *X, TF *L21, TF *L21T, TF *Ttop) {
+int factor_numeric(arap_ctx *ctx, TF *Lval, TF *Upd, TF *Dinv) {
     const Symbolic &s = ctx->sym;
     const DevSym &d = ctx->ds;
     cudaStream_t st = ctx->stream;
     CK(cudaMemsetAsync(Lval, 0, (size_t)s.panel_size * sizeof(TF), st));
     if (s.upd_size > 0) CK(cudaMemsetAsync(Upd, 0, (size_t)s.upd_size * sizeof(TF), st));
-    CK(cudaMemsetAsync(X, 0, (size_t)s.x_size * sizeof(TF), st));
-    if (s.l21_size > 0) CK(cudaMemsetAsync(L21, 0, (size_t)s.l21_size * sizeof(TF), st));
-    if (s.l21t_size > 0) CK(cudaMemsetAsync(L21T, 0, (size_t)s.l21t_size * sizeof(TF), st));
     {
         Prof pr(ctx, ARAP_K_ASSEMBLE);
         launch_assemble<TF>(d, ctx->w64.as<double>(), ctx->pc64.as<Vec4<double>>(), Lval, ctx->diag64.as<double>(),
@@ -657,13 +651,38 @@ int factor_enqueue(arap_ctx *ctx, TF *Lval, TF *Upd, TF *Dinv, TF *X, TF *L21, T
     }
     ctx->launches += 1;
     for (const FactorLaunch &fl : s.fplan) {
+        if (fl.kind == kFx) continue;
         Prof pr(ctx, ARAP_K_FACTOR);
-        launch_factor_step<TF>(d, fl, ctx->fitems.as<FItem>(), Lval, Upd, Dinv, X, L21, L21T, ctx->errw.as<int>(), st);
+        launch_factor_step<TF>(d, fl, ctx->fitems.as<FItem>(), Lval, Upd, Dinv, nullptr, nullptr, nullptr,
+                               ctx->errw.as<int>(), st);
+        ctx->launches += 1;
+    }
+    CK(cudaGetLastError());
+    return ARAP_OK;
+}
+
+// Enqueues the arrays the triangular solves multiply by, in precision TI,
+// from a factor (panels and inverted diagonal blocks) in that precision:
+// X = inv(L11) and X^T per supernode, the aligned L21 / L21^T copies, and the
+// dense top's T = inv(L_top). The factor no longer changes when they run.
+template <typename TI>
+int factor_inverses(arap_ctx *ctx, const TI *Lval, const TI *Dinv, TI *X, TI *L21, TI *L21T, TI *Ttop) {
+    const Symbolic &s = ctx->sym;
+    const DevSym &d = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemsetAsync(X, 0, (size_t)s.x_size * sizeof(TI), st));
+    if (s.l21_size > 0) CK(cudaMemsetAsync(L21, 0, (size_t)s.l21_size * sizeof(TI), st));
+    if (s.l21t_size > 0) CK(cudaMemsetAsync(L21T, 0, (size_t)s.l21t_size * sizeof(TI), st));
+    for (const FactorLaunch &fl : s.fplan) {
+        if (fl.kind != kFx) continue;
+        Prof pr(ctx, ARAP_K_FACTOR);
+        launch_factor_step<TI>(d, fl, ctx->fitems.as<FItem>(), const_cast<TI *>(Lval), nullptr, const_cast<TI *>(Dinv),
+                               X, L21, L21T, ctx->errw.as<int>(), st);
         ctx->launches += 1;
     }
     if (d.n_top > 0) {
         Prof pr(ctx, ARAP_K_FACTOR);
-        launch_top_inverse<TF>(d, X, L21, Ttop, st);
+        launch_top_inverse<TI>(d, X, L21, Ttop, st);
         ctx->launches += 1;
     }
     CK(cudaGetLastError());
@@ -706,24 +725,29 @@ int setup_enqueue(arap_ctx *ctx) {
     if (m > 0) {
         int rc;
         if (sizeof(T) == 4 && ctx->factor_bits == 64) {
-            // FP64 numeric factorisation (arap.h:337 factors in double), then
-            // its solve arrays rounded to the FP32 copies the sweeps stream
-            rc = factor_enqueue<double>(ctx, ctx->Lval.as<double>(), ctx->Upd.as<double>(), ctx->Dinv.as<double>(),
-                                        ctx->X64.as<double>(), ctx->L21_64.as<double>(), ctx->L21T_64.as<double>(),
-                                        ctx->Ttop64.as<double>());
+            // FP64 numeric factorisation (arap.h:337 factors in double); the
+            // factor is then rounded to FP32, and the arrays the FP32 solves
+            // multiply by (the supernodes' X = inv(L11), the dense top's T)
+            // are formed from it in FP32: they carry FP32 accuracy either way,
+            // and the FP64 residual refinement restores the rest
+            rc = factor_numeric<double>(ctx, ctx->Lval.as<double>(), ctx->Upd.as<double>(), ctx->Dinv.as<double>());
             if (rc != ARAP_OK) return rc;
-            const double *src[4] = {ctx->X64.as<double>(), ctx->L21_64.as<double>(), ctx->L21T_64.as<double>(),
-                                    ctx->Ttop64.as<double>()};
-            float *dst[4] = {ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
-                             ctx->Ttop.as<float>()};
-            const int64_t n[4] = {s.x_size, s.l21_size, s.l21t_size,
-                                  d.n_top > 0 ? (int64_t)dense_top_elems(d.n_top) : 0};
-            Prof pr(ctx, ARAP_K_FACTOR);
-            launch_demote(4, src, dst, n, st);
-            ctx->launches += 1;
+            {
+                const double *src[2] = {ctx->Lval.as<double>(), ctx->Dinv.as<double>()};
+                float *dst[2] = {ctx->Lval32.as<float>(), ctx->Dinv32.as<float>()};
+                const int64_t n[2] = {s.panel_size, s.dinv_size};
+                Prof pr(ctx, ARAP_K_FACTOR);
+                launch_demote(2, src, dst, n, st);
+                ctx->launches += 1;
+            }
+            rc = factor_inverses<float>(ctx, ctx->Lval32.as<float>(), ctx->Dinv32.as<float>(), ctx->Xinv.as<float>(),
+                                        ctx->L21.as<float>(), ctx->L21T.as<float>(), ctx->Ttop.as<float>());
+            if (rc != ARAP_OK) return rc;
         } else {
-            rc = factor_enqueue<T>(ctx, ctx->Lval.as<T>(), ctx->Upd.as<T>(), ctx->Dinv.as<T>(), ctx->Xinv.as<T>(),
-                                   ctx->L21.as<T>(), ctx->L21T.as<T>(), ctx->Ttop.as<T>());
+            rc = factor_numeric<T>(ctx, ctx->Lval.as<T>(), ctx->Upd.as<T>(), ctx->Dinv.as<T>());
+            if (rc != ARAP_OK) return rc;
+            rc = factor_inverses<T>(ctx, ctx->Lval.as<T>(), ctx->Dinv.as<T>(), ctx->Xinv.as<T>(), ctx->L21.as<T>(),
+                                    ctx->L21T.as<T>(), ctx->Ttop.as<T>());
             if (rc != ARAP_OK) return rc;
         }
     }
@@ -2027,8 +2051,8 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
         const bool f64f = ctx->state_prec == ARAP_PRECISION_MIXED && ctx->factor_bits == 64;
         const double fz = f64f ? 8.0 : sz;
         B = (double)s.panel_size * fz * 2 + (double)s.upd_size * fz * 2 + (double)s.dinv_size * fz +
-            (xlow + l21) * fz;
-        if (f64f) B += (double)(s.x_size + s.l21_size + s.l21t_size) * (8 + 4) + 2 * nt * nt * (8 + 4);
+            (xlow + l21) * sz;
+        if (f64f) B += (double)(s.panel_size + s.dinv_size) * (8 + 4);  // rounded to FP32 for the inverses
         FL = s.factor_flops;
         break;
     }
