@@ -20,7 +20,7 @@ value: iterations/s with the rest pose and targets already in device memory,
        writing a 256 MB buffer, outside the timed events.
 e2e:   the same steps through the C ABI with host buffers: pinned rest
        positions and targets copied in, deformed positions copied out, wall
-       clock; one end-to-end step follows each timed device step.
+       clock; one end-to-end step precedes each timed device step.
 repose_refactor: the same steps with the symbolic analysis kept (the
        constrained set does not change), reported beside the headline.
 cpu_baseline: the FP64 C restatement of arap.h (the oracle) on one host core,
@@ -193,6 +193,53 @@ def run_reference(args):
     return 0
 
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal (the measured peaks hold no FP64 figure)
+
+
+def roofline_of(kstats, kmodel, steps, peaks, wname, factorisations):
+    """Roofline of the dominant kernel class and of the factorisation.
+
+    The dominant class is the one with the most device time among the
+    classes that run one kernel kind per launch (local step, RHS, residual,
+    the two sweeps, ...): HBM-bound, algorithmic bytes of one launch over its
+    average CUDA-event duration against the measured copy bandwidth. The
+    factorisation is a sequence of seven kernel kinds over the tree's levels
+    (none of them alone as long as a sweep class) and is bound by the FP64
+    units: its algorithmic flops (the dense Cholesky's, sum over supernodes of
+    c^3/3 + c^2 b + c b^2) over its time per factorisation, against the
+    nominal FP64 rate."""
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    cands = {k: v for k, v in kstats.items() if k != "factor" and v[1] > 0}
+    dom = max(cands, key=lambda k: cands[k][0])
+    dom_ms, dom_n = kstats[dom]
+    per_launch_ms = dom_ms / max(dom_n, 1)
+    dom_bytes = kmodel[dom][0]
+    achieved = dom_bytes / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "ncu_traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get(wname, {}).get(dom)
+        except Exception:
+            traffic = None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "traffic": traffic,
+            "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+            "bytes_per_launch": dom_bytes, "ms_per_launch": per_launch_ms,
+            "dominant_by": "device time among the single-kernel classes; the factorisation is in factor_roofline"}
+    fms = kstats.get("factor", (0.0, 0))[0] / max(factorisations, 1)
+    ffl = kmodel.get("factor", (0.0, 0.0))[1]
+    froof = None
+    if fms > 0:
+        tf = ffl / (fms * 1e-3) / 1e12
+        froof = {"bound": "fp64", "achieved": tf, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                 "frac": tf / FP64_NOMINAL_TFLOPS, "peak_source": "nominal",
+                 "flops_per_factorisation": ffl, "ms_per_factorisation": fms,
+                 "share_of_request_kernel_time": kstats["factor"][0] / max(sum(v[0] for v in kstats.values()), 1e-9)}
+    return roof, froof
+
+
+
 def run_batch(args):
     """Many poses of one mesh per step (arap_deform_poses): one factorisation
     shared by all poses, P x 3 right-hand sides per triangular solve."""
@@ -339,23 +386,7 @@ def run_batch(args):
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
     except Exception:
         pass
-    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    dom = max(kstats, key=lambda k: kstats[k][0])
-    dom_ms, dom_n = kstats[dom]
-    per_launch_ms = dom_ms / max(dom_n, 1)
-    if dom == "factor":
-        per_launch_ms = dom_ms / max(args.steps, 1)
-    # the model covers one right-hand side; the batched solves stream the
-    # factor once per pose tile and the per-pose vectors once per pose
-    dom_bytes = kmodel[dom][0]
-    achieved = dom_bytes / (per_launch_ms * 1e-3) / 1e9
-    traffic = None
-    tfile = ROOT / "profiles" / "ncu_traffic.json"
-    if tfile.exists():
-        try:
-            traffic = json.loads(tfile.read_text()).get(w.name, {}).get(dom)
-        except Exception:
-            traffic = None
+    roof, froof = roofline_of(kstats, kmodel, args.steps, peaks, w.name, args.steps)
     cpu = None
     err = None
     if rank == 0 and not args.no_cpu_baseline and e2e_s:
@@ -395,9 +426,8 @@ def run_batch(args):
         "e2e_explicit_targets": {"value": its_total / sum(e2e_x) if e2e_x else None, "unit": UNIT,
                                  "h2d_bytes_per_step": int(tg_h.nbytes), "d2h_bytes_per_step": int(out_h.nbytes)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic, "bytes_per_launch": dom_bytes,
-                     "ms_per_launch": per_launch_ms},
+        "roofline": roof,
+        "factor_roofline": froof,
         "cpu_baseline": cpu,
         "error_vs_fp64_oracle": err,
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": float(np.percentile(lat, 99))},
@@ -755,7 +785,7 @@ def run_requests(args):
         return time.perf_counter() - t0
 
     # ---- timed region: dirty deforms with inputs resident on the device.
-    # Each one is followed by one end-to-end step (not counted in `value`), so
+    # Each one is preceded by one end-to-end step (not counted in `value`), so
     # both measures see the same conditions over the run ----
     set_analysis(args.cached_analysis)
     for _ in range(args.warmup):
@@ -769,11 +799,11 @@ def run_requests(args):
     barrier()
     clocks.start()
     for k in range(args.steps):
+        if not args.skip_e2e:
+            e2e_s.append(e2e_step())
         ms, nl = device_step()
         step_ms.append(ms)
         launches += nl
-        if not args.skip_e2e:
-            e2e_s.append(e2e_step())
     barrier()
     clk = clocks.stop()
     total_ms = reduce_max(sum(step_ms), dist, dev)
@@ -848,22 +878,7 @@ def run_requests(args):
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
     except Exception:
         pass
-    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    dom = max(kstats, key=lambda k: kstats[k][0])
-    dom_ms, dom_n = kstats[dom]
-    dom_bytes = kmodel[dom][0]
-    per_launch_ms = dom_ms / max(dom_n, 1)
-    if dom == "factor":  # model bytes cover a whole factorisation (all levels)
-        per_launch_ms = dom_ms / max(args.steps, 1)
-    achieved = dom_bytes / (per_launch_ms * 1e-3) / 1e9
-    traffic = None
-    tfile = ROOT / "profiles" / "ncu_traffic.json"
-    if tfile.exists():
-        try:
-            traffic = json.loads(tfile.read_text()).get(w.name, {}).get(dom)
-        except Exception:
-            traffic = None
+    roof, froof = roofline_of(kstats, kmodel, args.steps, peaks, w.name, args.steps)
 
     # ---- CPU baseline (oracle, one core) + error of the GPU result ----
     cpu = None
@@ -907,15 +922,16 @@ def run_requests(args):
         "config": config_of(w, args, extra),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "timing": "host wall clock around each step (uploads, enqueues, waits, result copies); one "
-                          "end-to-end step after each timed device step"},
+                          "end-to-end step before each timed device step"},
         "repose_refactor": repose,
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
-                     "bytes_per_launch": dom_bytes, "ms_per_launch": per_launch_ms},
+        "roofline": roof,
+        "factor_roofline": froof,
         "cpu_baseline": cpu,
         "error_vs_fp64_oracle": err,
-        "latency_ms": {"request_alone": lat_alone, "step_p50": sorted(step_ms)[len(step_ms) // 2]},
+        "latency_ms": {"request_alone": lat_alone, "step_p50": sorted(step_ms)[len(step_ms) // 2],
+                       "steps": [round(x, 3) for x in step_ms],
+                       "e2e_steps": [round(1e3 * x, 3) for x in e2e_s]},
         "kernel_ms_per_request": {k: v[0] / args.steps for k, v in kstats.items()},
         "last_request_ms": {"setup": setup_ms, "iterations": iter_ms},
         "clocks": clk,
