@@ -161,9 +161,77 @@ __device__ __forceinline__ void rotation_from_cov(const T S_in[3][3], T R[3][3],
 // it (a fraction of a percent of the vertices).
 constexpr float kPolarFallback = 0.1f;
 
+// Newton steps towards the rotation R of rotation_from_cov (the maximiser of
+// tr(R S) over proper rotations, so V diag(1,1,det) U^T for S = U Sigma V^T)
+// from a nearby R. With R = R0 exp([w]x) the objective's gradient at w = 0
+// is g, the axial vector of the skew part of Q = (S R0)^T, and its Hessian
+// -(tr(Q) I - sym(Q)); the step w = (tr(Q) I - sym(Q))^-1 g is applied
+// through the Cayley map, which keeps R orthogonal. Quadratic convergence:
+// from an FP32 fit, two steps reach FP64 accuracy.
+template <typename T>
+__device__ __forceinline__ void polar_newton(const T S[3][3], T R[3][3], int iters) {
+    // R orthogonal to working precision first (the Cayley steps keep R's
+    // deviation from orthogonality): Newton-Schulz, R <- R (3 I - R^T R) / 2
+    for (int it = 0; it < 2; ++it) {
+        T G[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+                G[a][b] = (a == b ? (T)1.5 : (T)0) - (T)0.5 * (R[0][a] * R[0][b] + R[1][a] * R[1][b] + R[2][a] * R[2][b]);
+        T Rn[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) Rn[a][b] = R[a][0] * G[0][b] + R[a][1] * G[1][b] + R[a][2] * G[2][b];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) R[a][b] = Rn[a][b];
+    }
+    for (int it = 0; it < iters; ++it) {
+        T Q[3][3];  // Q = (S R)^T: Q[a][b] = sum_k S[b][k] R[k][a]
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) Q[a][b] = S[b][0] * R[0][a] + S[b][1] * R[1][a] + S[b][2] * R[2][a];
+        const T g0 = Q[2][1] - Q[1][2], g1 = Q[0][2] - Q[2][0], g2 = Q[1][0] - Q[0][1];
+        const T tr = Q[0][0] + Q[1][1] + Q[2][2];
+        // H = tr I - sym(Q), symmetric
+        const T h00 = tr - Q[0][0], h11 = tr - Q[1][1], h22 = tr - Q[2][2];
+        const T h01 = -(T)0.5 * (Q[0][1] + Q[1][0]), h02 = -(T)0.5 * (Q[0][2] + Q[2][0]),
+                h12 = -(T)0.5 * (Q[1][2] + Q[2][1]);
+        // w = adj(H) g / det(H)
+        const T c00 = h11 * h22 - h12 * h12, c01 = h02 * h12 - h01 * h22, c02 = h01 * h12 - h02 * h11;
+        const T c11 = h00 * h22 - h02 * h02, c12 = h01 * h02 - h00 * h12, c22 = h00 * h11 - h01 * h01;
+        const T det = h00 * c00 + h01 * c01 + h02 * c02;
+        const T scale = fabs(h00) + fabs(h11) + fabs(h22);
+        if (!(det > Eps<T>::v * scale * scale * scale)) break;  // not a maximum's neighbourhood: keep R
+        const T id = (T)1 / det;
+        const T w0 = (c00 * g0 + c01 * g1 + c02 * g2) * id, w1 = (c01 * g0 + c11 * g1 + c12 * g2) * id,
+                w2 = (c02 * g0 + c12 * g1 + c22 * g2) * id;
+        // Cayley: C = I + 2/(1+|a|^2) ([a]x + [a]x^2), a = w/2
+        const T a0 = (T)0.5 * w0, a1 = (T)0.5 * w1, a2 = (T)0.5 * w2;
+        const T f = (T)2 / ((T)1 + a0 * a0 + a1 * a1 + a2 * a2);
+        const T C[3][3] = {{(T)1 - f * (a1 * a1 + a2 * a2), f * (a0 * a1 - a2), f * (a0 * a2 + a1)},
+                           {f * (a0 * a1 + a2), (T)1 - f * (a0 * a0 + a2 * a2), f * (a1 * a2 - a0)},
+                           {f * (a0 * a2 - a1), f * (a1 * a2 + a0), (T)1 - f * (a0 * a0 + a1 * a1)}};
+        T Rn[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) Rn[a][b] = R[a][0] * C[0][b] + R[a][1] * C[1][b] + R[a][2] * C[2][b];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) R[a][b] = Rn[a][b];
+    }
+}
+
 // FP64 covariance of vertex i's one-ring (estimateRotations, arap.h:358-374)
-// and its rotation, from the rest positions p, current positions pc (element
-// k of vertex k's pose at k * stride + off) and the FP64 weights.
+// and its rotation refined from the FP32 fit Rm (in place), from the rest
+// positions p, current positions pc (element k of vertex k's pose at
+// k * stride + off) and the FP64 weights.
 __device__ __forceinline__ void rotation_fp64(int i, int e0, int e1, const int32_t *__restrict__ dcol,
                                               const double *__restrict__ w64, const Vec4<double> *__restrict__ p,
                                               const Vec4<double> *__restrict__ pc, int64_t stride, int64_t off,
@@ -180,8 +248,15 @@ __device__ __forceinline__ void rotation_fp64(int i, int e0, int e1, const int32
         S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
         S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
     }
+    // Newton's method on the rotation group from the FP32 fit, which is close
+    // (a few 1e-6 at worst): a FP64 SVD would take an order of magnitude more
+    // FP64 instructions, the scarce kind on this GPU.
     double R[3][3];
-    rotation_from_cov<double>(S, R);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) R[a][b] = (double)Rm[a][b];
+    polar_newton(S, R, 2);
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
