@@ -645,6 +645,12 @@ def main():
                          "'auto': autotuned)")
     ap.add_argument("--pose-tile", type=int, default=-1,
                     help="pose_batch: poses per batched-solve task (0: largest that fits; -1: autotuned)")
+    ap.add_argument("--solve-schedule", default="auto", choices=["auto", "persistent", "levels"],
+                    help="single-request solves: persistent CTAs per sweep or one launch per tree level "
+                         "(auto: autotuned with the CTA count when requests run concurrently)")
+    ap.add_argument("--warp-rows", type=int, default=-1,
+                    help="single-request solves: fronts of at most this many rows solved one warp per supernode "
+                         "(-1: autotuned with the CTA count when requests run concurrently, else 0)")
     ap.add_argument("--solve-ctas", type=int, default=-1,
                     help="CTAs per triangular-solve launch (0: as many as fit; -1: autotuned for the concurrency)")
     ap.add_argument("--concurrent", type=int, default=os.cpu_count() or 1,
@@ -703,17 +709,33 @@ def run_requests(args):
     N = max(1, args.concurrent)
     mixed = args.precision == "mixed"
     tuned = None
-    if args.solve_ctas < 0:
+    # the persistent schedule is the faster one on every measured mesh, alone
+    # and concurrent; the level schedule is tried only when asked for
+    schedules = ("persistent",) if args.solve_schedule == "auto" else (args.solve_schedule,)
+    warps = (0, 128, 256) if args.warp_rows < 0 else (args.warp_rows,)
+    if args.solve_ctas < 0 and N > 1:
         import arap_tune
 
-        if N > 1:
-            best, rates = arap_tune.tune_solve_ctas(w.positions, w.faces, w.cidx, w.ctargets, w.iterations,
-                                                    args.precision, args.refine, N, device=local)
-            tuned = {"solve_ctas": best, "iterations_per_s": {str(k): round(v, 1) for k, v in rates.items()}}
-            log(f"autotuned solve CTAs for {N} requests in flight: {best} {tuned['iterations_per_s']}")
-            args.solve_ctas = best
-        else:
+        tuned = {}
+        pick = None
+        for sch in schedules:
+            for wr in warps:
+                best, rates = arap_tune.tune_solve_ctas(w.positions, w.faces, w.cidx, w.ctargets, w.iterations,
+                                                        args.precision, args.refine, N, device=local, schedule=sch,
+                                                        warp_rows=wr)
+                key = f"{sch}/warp_rows={wr}"
+                tuned[key] = {"solve_ctas": best, "iterations_per_s": {str(k): round(v, 1) for k, v in rates.items()}}
+                log(f"autotuned solve CTAs for {N} requests in flight, {key}: {best} {tuned[key]}")
+                if pick is None or rates[best] > pick[3]:
+                    pick = (sch, wr, best, rates[best])
+        args.solve_schedule, args.warp_rows, args.solve_ctas = pick[0], pick[1], pick[2]
+    else:
+        if args.solve_ctas < 0:
             args.solve_ctas = 0
+        if args.solve_schedule == "auto":
+            args.solve_schedule = "persistent"
+        if args.warp_rows < 0:
+            args.warp_rows = 0
     ctxs = []
     for _ in range(N):
         c = G.ArapContext(w.V, w.faces, device=local)
@@ -721,6 +743,8 @@ def run_requests(args):
         if mixed:
             c.set_factor_precision(args.factor_bits)
         c.set_solve_ctas(args.solve_ctas)
+        c.set_solve_schedule(args.solve_schedule)
+        c.set_warp_rows(args.warp_rows)
         c.set_rest_positions(w.positions)
         c.set_constraints(w.cidx, w.ctargets)
         ctxs.append(c)
@@ -825,8 +849,9 @@ def run_requests(args):
     # with the launch shape a lone request prefers, with and without the
     # symbolic analysis
     c0 = ctxs[0]
-    if args.solve_ctas != 0:
+    if args.solve_ctas != 0 or args.warp_rows != 0:
         c0.set_solve_ctas(0)
+        c0.set_warp_rows(0)
         c0.deform(w.iterations, want_output=False)
     lat_alone = {}
     for cached in ((True,) if args.cached_analysis else (False, True)):
@@ -862,8 +887,9 @@ def run_requests(args):
     kmodel = c0.kernel_model()
     c0.set_profiling(False)
     setup_ms, iter_ms = c0.timing()
-    if args.solve_ctas != 0:
+    if args.solve_ctas != 0 or args.warp_rows != 0:
         c0.set_solve_ctas(args.solve_ctas)
+        c0.set_warp_rows(args.warp_rows)
     c0.set_symbolic_cache(args.cached_analysis)
 
     pool.shutdown()
@@ -901,7 +927,9 @@ def run_requests(args):
 
     analysis = "kept for the unchanged constraint set" if args.cached_analysis else \
         "redone on every request (ordering, elimination tree, supernodes, plan), as SimplicialLDLT::compute"
-    extra = {"requests_per_step": N, "solve_ctas": args.solve_ctas, "solve_ctas_autotune": tuned,
+    extra = {"requests_per_step": N, "solve_schedule": args.solve_schedule, "warp_rows": args.warp_rows,
+             "solve_ctas": args.solve_ctas,
+             "solve_ctas_autotune": tuned,
              "symbolic_analysis": analysis,
              "step": f"{N} concurrent dirty deform requests, one host thread each (symbolic analysis "
                      f"{'kept' if args.cached_analysis else 'redone'}, weights, numeric factorisation, "

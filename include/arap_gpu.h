@@ -204,6 +204,19 @@ int arap_set_cluster_threshold(arap_ctx *ctx, int32_t bytes);
    takes longer than a CTA's, so the default leaves it off. */
 int arap_set_warp_rows(arap_ctx *ctx, int32_t rows);
 
+/* Schedule of the CTA-per-supernode levels of a single request's triangular
+   solves (arap.h:417-429). ARAP_SOLVE_PERSISTENT: one launch of persistent
+   CTAs per sweep that take supernodes in dependency order and wait (bounded)
+   for their children's or parent's completion flags. ARAP_SOLVE_LEVELS: one
+   launch per level of the elimination tree, sized to the level, in which no
+   task waits; CTAs only occupy SMs while they have work, so concurrent
+   requests share the device better. Trees of more than 48 levels keep the
+   persistent schedule. Both give identical results. Takes effect at the next
+   deform (which sets the problem up again). */
+#define ARAP_SOLVE_PERSISTENT 0
+#define ARAP_SOLVE_LEVELS 1
+int arap_set_solve_schedule(arap_ctx *ctx, int32_t schedule);
+
 /* The top levels of the elimination tree, up to `max_columns` columns in all
    (0, the default: 2,048; negative: none), are solved through the explicit
    inverse of the factor restricted to them: formed once per factorisation

@@ -34,6 +34,8 @@ ARAP_ERR_ADMISSION_REFUSED = 7
 ARAP_ERR_NO_DEVICE = 8
 ARAP_ERR_UNSUPPORTED = 9
 ARAP_PENDING = 10
+ARAP_SOLVE_PERSISTENT = 0
+ARAP_SOLVE_LEVELS = 1
 
 PRECISION = {"fp64": 0, "mixed": 1}
 
@@ -113,6 +115,7 @@ SIGNATURES = {
     "arap_set_cluster_threshold": (C.c_int, [_P, _I32]),
     "arap_set_dense_top": (C.c_int, [_P, _I32]),
     "arap_set_warp_rows": (C.c_int, [_P, _I32]),
+    "arap_set_solve_schedule": (C.c_int, [_P, _I32]),
     "arap_set_ordering": (C.c_int, [_P, _I32]),
     "arap_set_done_callback": (C.c_int, [_P, _P, _P]),
     "arap_get_host_timing": (C.c_int, [_P, _dp]),
@@ -332,6 +335,12 @@ class ArapContext:
     def set_warp_rows(self, rows: int):
         """Largest front (rows) of the warp-per-supernode solves of the bottom levels (0: none)."""
         self._check(self.lib.arap_set_warp_rows(self.h, int(rows)))
+
+    def set_solve_schedule(self, schedule):
+        """'persistent' (one launch of persistent CTAs per sweep) or 'levels'
+        (one launch per tree level, no waits) for the single-CTA solve levels."""
+        code = {"persistent": ARAP_SOLVE_PERSISTENT, "levels": ARAP_SOLVE_LEVELS}.get(schedule, schedule)
+        self._check(self.lib.arap_set_solve_schedule(self.h, int(code)))
 
     def set_dense_top(self, max_columns: int):
         """Columns of the tree's top solved through an explicit inverse (0: default, <0: none)."""

@@ -26,16 +26,19 @@ CANDIDATES = (0, 64, 96, 128, 192, 256)
 _cache: dict = {}
 
 
-def _key(device: int, V: int, n_constrained: int, precision: str, concurrency: int, iterations: int) -> str:
-    return f"dev{device}:V{V}:c{n_constrained}:{precision}:x{concurrency}:it{iterations}"
+def _key(device: int, V: int, n_constrained: int, precision: str, concurrency: int, iterations: int,
+         schedule: str = "persistent") -> str:
+    return f"dev{device}:V{V}:c{n_constrained}:{precision}:x{concurrency}:it{iterations}:{schedule}"
 
 
 def tune_solve_ctas(positions, faces, cidx, ctargets, iterations: int, precision: str = "mixed",
                     refine: int = 1, concurrency: int = 1, device: int = 0, candidates=CANDIDATES,
-                    trials: int = 2, cache_file: str | Path | None = None):
+                    trials: int = 2, cache_file: str | Path | None = None, schedule: str = "persistent",
+                    warp_rows: int = 0):
     """Returns (best_count, {count: iterations/s}) for `concurrency` concurrent
-    dirty deforms of the given problem."""
-    key = _key(device, len(positions), len(cidx), precision, concurrency, iterations)
+    dirty deforms of the given problem under the given solve schedule
+    ('persistent' or 'levels', arap_set_solve_schedule)."""
+    key = _key(device, len(positions), len(cidx), precision, concurrency, iterations, f"{schedule}:w{warp_rows}")
     if cache_file and Path(cache_file).exists():
         try:
             _cache.update(json.loads(Path(cache_file).read_text()))
@@ -49,6 +52,8 @@ def tune_solve_ctas(positions, faces, cidx, ctargets, iterations: int, precision
     for _ in range(max(1, concurrency)):
         c = G.ArapContext(len(positions), faces, device=device)
         c.set_precision(precision, refine)
+        c.set_solve_schedule(schedule)
+        c.set_warp_rows(warp_rows)
         c.set_rest_positions(positions)
         c.set_constraints(cidx, ctargets)
         ctxs.append(c)

@@ -23,8 +23,12 @@ using namespace arapgpu;
 namespace {
 
 // ticket counters of the single-request solves: forward / backward of the CTA
-// sweep (0, 1), of the cluster sweep (2, 3), of the warp sweep (4, 6)
-constexpr int kTickets = 8;
+// sweep (0, 1), of the cluster sweep (2, 3), of the warp sweep (4, 6), then
+// forward / backward per tree level of the level schedule
+// (kLevelTicket0 + 2 l, kLevelTicket0 + 2 l + 1)
+constexpr int kTickets = kLevelTicket0 + 2 * kMaxLevelLaunch;
+// schedule of the single-CTA solve levels (arap_set_solve_schedule)
+constexpr int kSolveScheduleDefault = ARAP_SOLVE_PERSISTENT;
 // fronts of at most this many rows at the bottom of the tree are solved one
 // warp per supernode (arap_set_warp_rows; 0: none)
 constexpr int kWarpRowsDefault = 0;
@@ -170,6 +174,7 @@ struct arap_ctx {
     int top_bytes = 0;  // supernode size from which tree levels go to the cluster solves (0: default, <0: never)
     int dense_cols = 0;  // most columns of the dense top of the tree (0: default, <0: none)
     int warp_rows = kWarpRowsDefault;  // largest front of the warp-per-supernode solves (0: none)
+    int solve_schedule = kSolveScheduleDefault;  // ARAP_SOLVE_PERSISTENT or ARAP_SOLVE_LEVELS
     size_t dense_inv_smem[2] = {0, 0}, dense_vec_smem[2] = {0, 0};  // configured limits (FP32, FP64)
     DevBuf top_col, top_gptr, top_gidx, tdpos, top_items, Ttop, ytop;
     int ordering = ARAP_ORDER_PER_CONSTRAINT_SET;
@@ -570,6 +575,25 @@ int prepare_symbolic(arap_ctx *ctx) {
         const int nl = std::max(d.s_low - d.s_warp, 1);
         d.solve_grid32 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res32) : res32));
         d.solve_grid64 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res64) : res64));
+        // level schedule: per level its supernodes, the shared memory its
+        // largest front needs and a grid of at most one CTA per supernode
+        d.level_launch = ctx->solve_schedule == ARAP_SOLVE_LEVELS && nlev <= kMaxLevelLaunch;
+        for (int l = 0; l <= kMaxLevelLaunch; ++l) d.lev_ptr[l] = nlev > 0 ? s.level_ptr[std::min(l, nlev)] : 0;
+        for (int l = 0; l < kMaxLevelLaunch; ++l) {
+            int lx = 0, l21 = 0;
+            for (int q = d.lev_ptr[l]; q < d.lev_ptr[l + 1]; ++q) {
+                const SnInfo &x = s.sn[s.level_sn[q]];
+                lx = std::max(lx, (int)x.ldx);
+                l21 = std::max(l21, (int)x.ld21);
+            }
+            d.lev_ldx[l] = lx;
+            d.lev_ld21[l] = l21;
+            const int n = std::max(d.lev_ptr[l + 1] - d.lev_ptr[l], 1);
+            const int r32 = solve_resident_ctas((int)solve_smem_bytes(lx, l21, 4), 4);
+            const int r64 = solve_resident_ctas((int)solve_smem_bytes(lx, l21, 8), 8);
+            d.lev_grid32[l] = std::max(1, std::min(n, cap > 0 ? std::min(cap, r32) : r32));
+            d.lev_grid64[l] = std::max(1, std::min(n, cap > 0 ? std::min(cap, r64) : r64));
+        }
         // the cluster solves size their shared memory by the largest front of
         // the cluster levels
         d.top_ldx = d.top_ld21 = 0;
@@ -820,7 +844,13 @@ int run_iterations(arap_ctx *ctx, int iterations);
 
 // kernels of one forward + backward sweep (lower levels and cluster levels)
 int solve_launches(const DevSym &d) {
-    return 2 * ((d.s_warp > 0) + (d.s_low > d.s_warp) + (d.s_top > 0) + (d.n_top > 0));
+    int cta = d.s_low > d.s_warp;
+    if (cta && d.level_launch) {
+        cta = 0;
+        for (int l = d.lwarp; l < d.ltop; ++l) cta += d.lev_ptr[l + 1] > d.lev_ptr[l];
+    }
+    // the dense top: gather + GEMV forward, GEMV backward
+    return 2 * ((d.s_warp > 0) + cta + (d.s_top > 0)) + (d.n_top > 0 ? 3 : 0);
 }
 
 template <>
@@ -1109,6 +1139,7 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->top_bytes = src->top_bytes;
     ctx->dense_cols = src->dense_cols;
     ctx->warp_rows = src->warp_rows;
+    ctx->solve_schedule = src->solve_schedule;
     ctx->ordering = src->ordering;
     return finish_create(ctx, src->device, src, out);
 }
@@ -1681,6 +1712,22 @@ int arap_set_warp_rows(arap_ctx *ctx, int32_t rows) {
     }
     if (rows != ctx->warp_rows) {
         ctx->warp_rows = rows;
+        ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
+        ctx->dirty = true;
+    }
+    return ARAP_OK;
+}
+
+int arap_set_solve_schedule(arap_ctx *ctx, int32_t schedule) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (schedule != ARAP_SOLVE_PERSISTENT && schedule != ARAP_SOLVE_LEVELS)
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "unknown solve schedule");
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (schedule != ctx->solve_schedule) {
+        ctx->solve_schedule = schedule;
         ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
         ctx->dirty = true;
     }

@@ -753,6 +753,8 @@ k_local_step_mixed(int V, const int32_t *__restrict__ drow, const int32_t *__res
     R[3 * (int64_t)i + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], 0.f};
 }
 
+
+
 // RHS of the mixed form without bFixed (added in FP64 by the residual):
 // sum_j 1/2 w (R_i + R_j)(p_i - p_j) over the FP32 rest edges.
 __global__ void __launch_bounds__(256)
@@ -2239,9 +2241,22 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
             s.s_warp, s.s_warp + W, s.level_sn, s.sn, s.child, s.relind, X, L21, sol, uvec, ticket + 4, flags, err);
     }
     const int sb = s.s_low - s.s_warp;  // supernodes of the CTA sweep
-    if (sb > 0)
+    if (sb > 0 && s.level_launch) {
+        // one launch per level: every child was solved by an earlier launch,
+        // so no task waits (lbeg = l)
+        for (int l = s.lwarp; l < s.ltop; ++l) {
+            const int b = s.lev_ptr[l], n = s.lev_ptr[l + 1] - b;
+            if (n == 0) continue;
+            const SolveSmem ll{s.lev_ldx[l], s.lev_ld21[l]};
+            const int Gl = sizeof(T) == 4 ? s.lev_grid32[l] : s.lev_grid64[l];
+            k_solve_fwd<T><<<Gl, kSolveThreads, solve_smem_bytes(ll.ldx_max, ll.ld21_max, sizeof(T)), st>>>(
+                n, n + Gl, l, ll, s.level_sn + b, s.sn, s.child, s.relind, X, L21, sol, uvec,
+                ticket + kLevelTicket0 + 2 * l, flags, err);
+        }
+    } else if (sb > 0) {
         k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(sb, sb + G, s.lwarp, lay, s.level_sn + s.s_warp, s.sn, s.child,
                                                        s.relind, X, L21, sol, uvec, ticket, flags, err);
+    }
     if (s.s_top > 0) {
         const SolveSmem tlay{s.top_ldx, s.top_ld21};
         const size_t tsmem = top_smem_bytes_impl(s.top_ldx, s.top_ld21, sizeof(T));
@@ -2282,9 +2297,22 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
             mode, ticket + 2, flags, err);
     }
     const int sb = s.s_low - s.s_warp;
-    if (sb > 0)
+    if (sb > 0 && s.level_launch) {
+        // one launch per level, root side first: every parent was solved by
+        // an earlier launch, so no task waits (ltop = l + 1)
+        for (int l = s.ltop - 1; l >= s.lwarp; --l) {
+            const int b = s.lev_ptr[l], n = s.lev_ptr[l + 1] - b;
+            if (n == 0) continue;
+            const SolveSmem ll{s.lev_ldx[l], s.lev_ld21[l]};
+            const int Gl = sizeof(T) == 4 ? s.lev_grid32[l] : s.lev_grid64[l];
+            k_solve_bwd<T><<<Gl, kSolveThreads, solve_smem_bytes(ll.ldx_max, ll.ld21_max, sizeof(T)), st>>>(
+                n, n + Gl, l + 1, ll, s.level_sn + b, s.sn, s.rows, X, L21T, sol, pc64, pc32, mode,
+                ticket + kLevelTicket0 + 2 * l, flags, err);
+        }
+    } else if (sb > 0) {
         k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(sb, sb + G, s.ltop, lay, s.level_sn + s.s_warp, s.sn, s.rows, X,
                                                        L21T, sol, pc64, pc32, mode, ticket, flags, err);
+    }
     if (s.s_warp > 0) {
         const int WG = sizeof(T) == 4 ? s.wgrid32 : s.wgrid64;
         const int W = WG * kWarpsPerCta;

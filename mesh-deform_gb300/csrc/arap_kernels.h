@@ -38,6 +38,14 @@ __device__ __forceinline__ unsigned flag_wait_limit(const int *err) {
 }
 #endif
 
+// level schedule of the single-request solves: at most this many tree levels
+// (deeper trees keep the persistent schedule). The forward sweep's launch for
+// level l takes its tickets from counter kLevelTicket0 + 2 l of the counter
+// array it is given, the backward sweep's from the same index of its array
+// (the backward sweeps are given the array one counter further on).
+constexpr int kMaxLevelLaunch = 48;
+constexpr int kLevelTicket0 = 8;
+
 struct DevTopo {
     int V, F, nnz;
     const int32_t *faces;    // 3F (original vertex ids)
@@ -58,6 +66,13 @@ struct DevSym {
     // [lwarp, ltop)
     int lwarp, s_warp, wgrid32, wgrid64;
     int top_ldx, top_ld21;  // largest front of the cluster levels (their shared-memory layout)
+    // level schedule (arap_set_solve_schedule): the CTA sweep of the levels
+    // [lwarp, ltop) as one launch per level instead of one persistent launch;
+    // level l holds the supernodes level_sn[lev_ptr[l], lev_ptr[l+1]), its
+    // fronts fit lev_ldx[l] / lev_ld21[l] rows, lev_grid32/64[l] CTAs
+    int level_launch;
+    int lev_ptr[kMaxLevelLaunch + 1], lev_ldx[kMaxLevelLaunch], lev_ld21[kMaxLevelLaunch];
+    int lev_grid32[kMaxLevelLaunch], lev_grid64[kMaxLevelLaunch];
     // dense top (levels [ltop, top) when n_top > 0, instead of cluster levels):
     // n_top columns, T = inv(L_top) formed by n_top_items CTAs
     int n_top, n_top_items, dense_ldx, dense_ld21;

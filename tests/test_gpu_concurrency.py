@@ -146,3 +146,42 @@ def test_warp_solves_match_cta_solves(gpu, precision, tol):
         assert W.bbox_rel_error(out, ref, w.positions) <= (1e-10 if precision == "fp64" else 1e-6)
     for rows in (64, 128, 256):
         assert W.bbox_rel_error(outs[rows], outs[0], w.positions) <= tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("workload", ["bar", "sphere"])
+def test_level_schedule_matches_persistent(gpu, precision, workload):
+    """One solve launch per tree level (arap_set_solve_schedule) runs the same
+    tasks with the same sums as the persistent sweep: positions bit for bit
+    equal, with and without the dense top, and with a capped grid."""
+    from oracle import oracle as O
+
+    w = (W.cfg_twisted_bar(h=0.05, iterations=8) if workload == "bar"
+         else W.cfg_noisy_sphere(level=4, iterations=8))
+    ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, w.iterations)
+    assert ok
+    for dense in (0, -1):
+        outs = []
+        for schedule, cap in (("persistent", 0), ("levels", 0), ("levels", 7)):
+            with gpu.ArapContext(w.V, w.faces) as ctx:
+                ctx.set_precision(precision, 1)
+                ctx.set_dense_top(dense)
+                ctx.set_solve_schedule(schedule)
+                ctx.set_solve_ctas(cap)
+                ctx.set_rest_positions(w.positions)
+                ctx.set_constraints(w.cidx, w.ctargets)
+                out = ctx.deform(w.iterations)
+                ctx.invalidate()
+                np.testing.assert_array_equal(ctx.deform(w.iterations), out)
+            outs.append(out)
+        np.testing.assert_array_equal(outs[1], outs[0])
+        np.testing.assert_array_equal(outs[2], outs[0])
+        assert W.bbox_rel_error(outs[1], ref, w.positions) <= (1e-10 if precision == "fp64" else 1e-6)
+
+
+def test_level_schedule_rejects_unknown(gpu):
+    w = W.cfg_icosphere_l4(level=2, iterations=1)
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        with pytest.raises(gpu.ArapError) as e:
+            ctx.set_solve_schedule(7)
+        assert e.value.code == gpu.ARAP_ERR_INVALID_ARGUMENT
