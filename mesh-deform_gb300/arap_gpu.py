@@ -430,6 +430,69 @@ class ArapContext:
         return out
 
 
+class MeshBatch:
+    """Several meshes of uneven sizes deformed together in one set of launches.
+
+    The meshes are packed into one block-diagonal problem over their disjoint
+    union (mesh k's vertices at offset[k], its faces and constrained indices
+    shifted by it): one context, so every kernel launch covers all meshes.
+    The nested dissection orders each mesh (a connected component of the
+    union) on its own, in parallel threads, so the elimination forest is the
+    meshes' trees side by side; the persistent triangular solves take
+    (mesh, supernode) tasks from one ticket queue, and the factorisation's
+    launches of one tree level cover that level of every mesh. Each mesh is
+    the reference's per-object problem (inc/deform/arap.h:101-138) and gets
+    the result a context of its own would give up to the order of sums (the
+    dense top of the union may differ from a lone mesh's). Every mesh needs
+    a constrained vertex in each of its components, as a lone deform does.
+    """
+
+    def __init__(self, meshes, device: int = 0):
+        """meshes: sequence of (n_vertices, faces)."""
+        self.sizes = [int(v) for v, _ in meshes]
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        faces = [np.ascontiguousarray(f, dtype=np.int64).reshape(-1, 3) + self.offsets[k]
+                 for k, (_, f) in enumerate(meshes)]
+        self.ctx = ArapContext(int(self.offsets[-1]), np.concatenate(faces).astype(np.int32), device=device)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def close(self):
+        self.ctx.close()
+
+    def set_rest_positions(self, positions):
+        """positions: one (n_k, 3) array per mesh."""
+        self.ctx.set_rest_positions(np.concatenate([np.asarray(p, dtype=np.float64).reshape(-1, 3)
+                                                    for p in positions]))
+
+    def _union_indices(self, idx):
+        return np.concatenate([np.asarray(i, dtype=np.int64).reshape(-1) + self.offsets[k]
+                               for k, i in enumerate(idx)]).astype(np.int32)
+
+    def set_constraints(self, idx, targets):
+        """idx, targets: one index array and one (c_k, 3) target array per mesh."""
+        self._order = [np.argsort(np.asarray(i).reshape(-1), kind="stable") for i in idx]
+        self.ctx.set_constraints(self._union_indices(idx),
+                                 np.concatenate([np.asarray(t, dtype=np.float64).reshape(-1, 3) for t in targets]))
+
+    def set_targets(self, targets):
+        """New targets for the same constrained sets (no refactorisation), one
+        (c_k, 3) array per mesh in the order of its set_constraints indices."""
+        self.ctx.set_targets(np.concatenate([np.asarray(t, dtype=np.float64).reshape(-1, 3)[o]
+                                             for t, o in zip(targets, self._order)]))
+
+    def split(self, union_xyz: np.ndarray):
+        return [union_xyz[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.sizes))]
+
+    def deform(self, iterations: int):
+        """One deform of every mesh; returns one (n_k, 3) array per mesh."""
+        return self.split(self.ctx.deform(iterations))
+
+
 def analyze_pattern(n_vertices: int, faces: np.ndarray, constrained) -> dict:
     """Host-only symbolic analysis (no GPU needed), see arap_analyze_pattern."""
     lib = load()

@@ -203,14 +203,36 @@ struct NdWorker {
         if (levptr[h] < ns) {
             // several components, each in order of its smallest vertex
             std::sort(S.begin(), S.end());
+            std::vector<std::vector<int32_t>> comps;
             for (int32_t v : S) {
                 if (load_rlx(inset + v) != setstamp) continue;
                 const int hl = bfs(setstamp, v, levptr, cur);
-                std::vector<int32_t> comp(queue_buf[cur].begin(), queue_buf[cur].begin() + levptr[hl]);
+                comps.emplace_back(queue_buf[cur].begin(), queue_buf[cur].begin() + levptr[hl]);
                 const int32_t cs = sh->next_stamp();
-                for (int32_t u : comp) store_rlx(inset + u, cs);
-                recurse(std::move(comp), out, depth);
+                for (int32_t u : comps.back()) store_rlx(inset + u, cs);
             }
+            const int nt = std::min<int>((int)comps.size(), (int)std::max(1u, std::thread::hardware_concurrency()));
+            if (ns < kNdParallelMin || depth >= kNdParallelDepth || nt < 2) {
+                for (auto &c : comps) recurse(std::move(c), out, depth);
+                return;
+            }
+            // components (the meshes of a batch) on a pool of threads, output
+            // in component order; with many components each recursion stays
+            // on its thread
+            const int sub_depth = (int)comps.size() >= nt ? kNdParallelDepth : depth + 1;
+            std::vector<NdOut> outs(comps.size());
+            std::atomic<int> next{0};
+            auto work = [&]() {
+                for (int c = next.fetch_add(1); c < (int)comps.size(); c = next.fetch_add(1)) {
+                    NdWorker w(sh, comps[c].size() + 1);
+                    w.recurse(std::move(comps[c]), outs[c], sub_depth);
+                }
+            };
+            std::vector<std::thread> pool;
+            for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+            work();
+            for (auto &t : pool) t.join();
+            for (const NdOut &o : outs) out.append(o);
             return;
         }
         // pseudo-peripheral vertex

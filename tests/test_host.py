@@ -156,3 +156,33 @@ def test_threaded_dissection_is_deterministic(gpu):
         again = gpu.analyze_pattern(w.V, w.faces, w.cidx)
         for key in ("perm", "etree", "block_ptr"):
             np.testing.assert_array_equal(first[key], again[key])
+
+
+def test_dissection_of_a_mesh_batch_orders_each_mesh_as_alone(gpu):
+    """A batch of meshes (their disjoint union) is dissected one mesh per
+    component, the components on a pool of threads: each mesh gets the
+    ordering, elimination tree and blocks it gets alone, shifted by the free
+    vertices of the meshes before it, and repeated analyses agree."""
+    parts = [W.cfg_twisted_bar(h=0.05, iterations=1), W.cfg_icosphere_l4(level=5, iterations=1),
+             W.cfg_twisted_bar(h=0.04, iterations=1, length=6.0)]
+    offs = np.cumsum([0] + [p.V for p in parts])
+    faces = np.concatenate([p.faces + offs[k] for k, p in enumerate(parts)])
+    cidx = np.concatenate([np.asarray(p.cidx) + offs[k] for k, p in enumerate(parts)])
+    union = gpu.analyze_pattern(int(offs[-1]), faces, cidx)
+    assert len(union["perm"]) >= 16384  # large enough for the threaded path
+    M = 0
+    perm, etree, bptr = [], [], [0]
+    for p in parts:
+        a = gpu.analyze_pattern(p.V, p.faces, p.cidx)
+        perm.append(np.asarray(a["perm"]) + M)
+        e = np.asarray(a["etree"]).copy()
+        e[e >= 0] += M
+        etree.append(e)
+        bptr.extend((np.asarray(a["block_ptr"])[1:] + M).tolist())
+        M += len(a["perm"])
+    np.testing.assert_array_equal(union["perm"], np.concatenate(perm))
+    np.testing.assert_array_equal(union["etree"], np.concatenate(etree))
+    np.testing.assert_array_equal(union["block_ptr"], np.asarray(bptr))
+    again = gpu.analyze_pattern(int(offs[-1]), faces, cidx)
+    for key in ("perm", "etree", "block_ptr"):
+        np.testing.assert_array_equal(union[key], again[key])
