@@ -810,6 +810,9 @@ def main():
     ap.add_argument("--solve-schedule", default="auto", choices=["auto", "persistent", "levels"],
                     help="single-request solves: persistent CTAs per sweep or one launch per tree level "
                          "(auto: autotuned with the CTA count when requests run concurrently)")
+    ap.add_argument("--vertex-launch", default="auto", choices=["auto", "default"],
+                    help="threads per vertex and block size of the local step, RHS and residual "
+                         "(auto: autotuned per kernel before the timed region)")
     ap.add_argument("--warp-rows", type=int, default=-1,
                     help="single-request solves: fronts of at most this many rows solved one warp per supernode "
                          "(-1: autotuned with the CTA count when requests run concurrently, else 0)")
@@ -913,6 +916,16 @@ def run_requests(args):
         c.set_constraints(w.cidx, w.ctargets)
         ctxs.append(c)
     first = ctxs[0].deform(w.iterations)  # allocation and graph capture, untimed
+    vtuned = None
+    if args.vertex_launch == "auto" and mixed:
+        import arap_tune
+
+        res = arap_tune.tune_vertex_launch(ctxs[0], w.iterations)
+        vtuned = {k: {"threads_per_vertex": sh[0], "block": sh[1], "us_per_launch": t} for k, (sh, t) in res.items()}
+        log(f"autotuned vertex kernels: {vtuned}")
+        for c in ctxs[1:]:
+            for k, (sh, _) in res.items():
+                c.set_vertex_launch(k, *sh)
     for c in ctxs[1:]:
         c.deform(w.iterations, want_output=False)
     streams = [torch.cuda.ExternalStream(c.stream(), device=dev) for c in ctxs]
@@ -1091,7 +1104,8 @@ def run_requests(args):
 
     analysis = "kept for the unchanged constraint set" if args.cached_analysis else \
         "redone on every request (ordering, elimination tree, supernodes, plan), as SimplicialLDLT::compute"
-    extra = {"requests_per_step": N, "solve_schedule": args.solve_schedule, "warp_rows": args.warp_rows,
+    extra = {"requests_per_step": N, "vertex_launch": vtuned or "1 thread per vertex, 256-thread blocks",
+             "solve_schedule": args.solve_schedule, "warp_rows": args.warp_rows,
              "solve_ctas": args.solve_ctas,
              "solve_ctas_autotune": tuned,
              "symbolic_analysis": analysis,

@@ -213,6 +213,18 @@ int arap_set_warp_rows(arap_ctx *ctx, int32_t rows);
    requests share the device better. Trees of more than 48 levels keep the
    persistent schedule. Both give identical results. Takes effect at the next
    deform (which sets the problem up again). */
+/* Launch shape of a per-vertex kernel of a single request's iterations:
+   kernel = ARAP_K_LOCAL (covariance + rotation fit, arap.h:354-384), ARAP_K_RHS
+   (arap.h:395-414) or ARAP_K_RESIDUAL (the FP64 residual of the mixed form).
+   threads_per_vertex = 1, 2, 4, 8 or 32 lanes of one warp per vertex, which
+   split the vertex's adjacency entries and sum by shuffles (32: a warp per
+   vertex); block_threads a multiple of 32, at most 256 for ARAP_K_LOCAL and
+   1024 for the others. Default 1 and 256 for all three. Any shape gives the
+   same result up to the order of sums. The batched kernels of
+   arap_deform_poses take one thread per (vertex, pose) and keep their shape.
+   mesh-deform_gb300/arap_tune.py measures the best shape per kernel. */
+int arap_set_vertex_launch(arap_ctx *ctx, int32_t kernel, int32_t threads_per_vertex, int32_t block_threads);
+
 #define ARAP_SOLVE_PERSISTENT 0
 #define ARAP_SOLVE_LEVELS 1
 int arap_set_solve_schedule(arap_ctx *ctx, int32_t schedule);

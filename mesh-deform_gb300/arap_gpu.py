@@ -116,6 +116,7 @@ SIGNATURES = {
     "arap_set_dense_top": (C.c_int, [_P, _I32]),
     "arap_set_warp_rows": (C.c_int, [_P, _I32]),
     "arap_set_solve_schedule": (C.c_int, [_P, _I32]),
+    "arap_set_vertex_launch": (C.c_int, [_P, _I32, _I32, _I32]),
     "arap_set_ordering": (C.c_int, [_P, _I32]),
     "arap_set_done_callback": (C.c_int, [_P, _P, _P]),
     "arap_get_host_timing": (C.c_int, [_P, _dp]),
@@ -139,6 +140,7 @@ SIGNATURES = {
 }
 
 KERNEL_CLASSES = ["weights", "assemble", "factor", "local", "rhs", "residual", "solve_fwd", "solve_bwd", "gather"]
+ARAP_K_LOCAL, ARAP_K_RHS, ARAP_K_RESIDUAL = 3, 4, 5
 
 _lib = None
 
@@ -335,6 +337,11 @@ class ArapContext:
     def set_warp_rows(self, rows: int):
         """Largest front (rows) of the warp-per-supernode solves of the bottom levels (0: none)."""
         self._check(self.lib.arap_set_warp_rows(self.h, int(rows)))
+
+    def set_vertex_launch(self, kernel, threads_per_vertex: int, block_threads: int = 256):
+        """Launch shape of 'local', 'rhs' or 'residual' (or an ARAP_K_* code)."""
+        code = {"local": ARAP_K_LOCAL, "rhs": ARAP_K_RHS, "residual": ARAP_K_RESIDUAL}.get(kernel, kernel)
+        self._check(self.lib.arap_set_vertex_launch(self.h, int(code), int(threads_per_vertex), int(block_threads)))
 
     def set_solve_schedule(self, schedule):
         """'persistent' (one launch of persistent CTAs per sweep) or 'levels'

@@ -1,8 +1,9 @@
 """Launch-shape autotuner: picks the number of CTAs per triangular-solve
 launch (arap_set_solve_ctas) for a workload and a number of requests in
-flight, the pose tile of the batched solves (arap_set_pose_tile) and the
-column cap of the elimination tree's dense top (arap_set_dense_top), by
-timing short trial runs through the C ABI.
+flight, the pose tile of the batched solves (arap_set_pose_tile), the
+column cap of the elimination tree's dense top (arap_set_dense_top) and the
+threads per vertex and block size of the per-vertex kernels
+(arap_set_vertex_launch), by timing short trial runs through the C ABI.
 
 One request alone is fastest with as many CTAs as fit on the device (the
 default, 0); several requests in flight share the SMs, and a smaller count
@@ -161,3 +162,47 @@ def tune_dense_top(ctx, iterations: int, batched: bool, candidates=DENSE_TOPS, t
     best_cap = min(times, key=times.get)
     ctx.set_dense_top(best_cap)
     return best_cap, times
+
+
+# (threads per vertex, block threads) candidates of the per-vertex kernels
+VERTEX_SHAPES = {
+    "local": ((1, 64), (1, 128), (1, 256), (2, 128), (2, 256), (4, 256)),
+    "rhs": ((1, 128), (1, 256), (1, 512), (2, 256), (4, 256), (8, 256), (32, 256)),
+    "residual": ((1, 128), (1, 256), (1, 512), (2, 256), (4, 256), (8, 256), (32, 256)),
+}
+
+
+def tune_vertex_launch(ctx, iterations: int, shapes=None, trials: int = 2):
+    """Per-vertex kernels of the single-request iterations (local step, RHS,
+    FP64 residual): threads per vertex (lanes of a warp splitting a vertex's
+    adjacency entries, up to a warp per vertex) and block size, each timed by
+    the per-launch profiler over `iterations` iterations of the context's
+    current problem (set up and deformed once before). Returns
+    {kernel: ((tpv, block), {"tpv x block": us per launch})} and leaves the
+    best shapes set."""
+    shapes = shapes or VERTEX_SHAPES
+    out = {}
+    ctx.set_profiling(True)
+    try:
+        for name, cands in shapes.items():
+            times = {}
+            for tpv, blk in cands:
+                ctx.set_vertex_launch(name, tpv, blk)
+                best = float("inf")
+                for _ in range(max(1, trials)):
+                    ctx.reset_kernel_stats()
+                    ctx.deform(iterations, want_output=False)
+                    ms, n = ctx.kernel_stats()[name]
+                    if n:
+                        best = min(best, ms / n)
+                if best < float("inf"):
+                    times[(tpv, blk)] = best
+            if not times:  # the kernel does not run in this precision
+                ctx.set_vertex_launch(name, 1, 256)
+                continue
+            pick = min(times, key=times.get)
+            ctx.set_vertex_launch(name, *pick)
+            out[name] = (pick, {f"{t}x{b}": round(v * 1e3, 2) for (t, b), v in times.items()})
+    finally:
+        ctx.set_profiling(False)
+    return out

@@ -688,7 +688,18 @@ static void bsolve(const DevSym &s, int P, int grid, const float *X, const float
 
 size_t btop_workspace_floats(int n, int P) { return (size_t)btop::ws_floats(n, P); }
 
-size_t btop_matrix_floats(int n, int P) { return (size_t)std::max(n, 0) * btop::ldb_of(P); }
+size_t btop_matrix_floats(int n, int P) { return (size_t)btop::b_tile_floats(n, btop::ldb_of(P)); }
+size_t btop_atile_floats(int n) { return (size_t)btop::a_tile_floats(n); }
+
+void launch_btop_pack(const DevSym &s, const float *Ttop, float *atiles, cudaStream_t st) {
+    const int n = s.n_top;
+    if (n <= 0) return;
+    const int ldt = dense_ld(n), nrt = btop::row_tiles(n);
+    const unsigned max_stages = (unsigned)((n + btop::kDepth - 1) / btop::kDepth);
+    btop::k_btop_pack<false><<<dim3(max_stages, nrt), 256, 0, st>>>(n, ldt, Ttop, atiles);
+    btop::k_btop_pack<true><<<dim3(max_stages, nrt), 256, 0, st>>>(
+        n, ldt, Ttop + (size_t)ldt * n, atiles + (size_t)btop::stages_before(false, n, nrt) * btop::kATileFloats);
+}
 
 int batch_tasks(const DevSym &s) { return s.n_top > 0 ? s.s_low : s.S; }
 
@@ -697,15 +708,15 @@ int batch_top_launches(const DevSym &s) { return s.n_top > 0 ? 5 : 0; }
 void launch_bsolve(const DevSym &s, int P, int pt, int grid, const float *X, const float *L21, const float *L21T,
                    Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
                    unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st,
-                   const float *Ttop, float *bftop, float *bytop, float *bws) {
+                   const float *atiles, float *bftop, float *bytop, float *bws) {
     if (s.S == 0) return;
-    const int n = s.n_top, ldt = n > 0 ? dense_ld(n) : 0, ldb = btop::ldb_of(P);
+    const int n = s.n_top, ldb = btop::ldb_of(P);
     const int nrt = btop::row_tiles(n), nct = (ldb + btop::kCols - 1) / btop::kCols;
     const unsigned rblocks = (unsigned)(((int64_t)n * (ldb / 4) + 255) / 256);
     const unsigned pblocks = (unsigned)(((int64_t)n * P + 255) / 256);
     if (!forward && n > 0) {
         btop::k_btop_mma<true><<<dim3(nct, btop::tasks(true, n, nrt)), btop::kThreads, btop::kSmemBytes, st>>>(
-            n, ldt, ldb, Ttop + (size_t)ldt * n, bytop, bws, btop::kCoreK, btop::kCoreMN, err);
+            n, ldb, atiles, bytop, bws, btop::kCoreK, btop::kCoreMN, err);
         btop::k_btop_reduce_bwd<<<pblocks, 256, 0, st>>>(n, P, ldb, bws, s.top_col, sol, pc64, pc32);
     }
     switch (pt) {
@@ -718,7 +729,7 @@ void launch_bsolve(const DevSym &s, int P, int pt, int grid, const float *X, con
     if (forward && n > 0) {
         btop::k_btop_gather<<<pblocks, 256, 0, st>>>(n, P, ldb, s.top_col, s.top_gptr, s.top_gidx, sol, uvec, bftop);
         btop::k_btop_mma<false><<<dim3(nct, btop::tasks(false, n, nrt)), btop::kThreads, btop::kSmemBytes, st>>>(
-            n, ldt, ldb, Ttop, bftop, bws, btop::kCoreK, btop::kCoreMN, err);
+            n, ldb, atiles, bftop, bws, btop::kCoreK, btop::kCoreMN, err);
         btop::k_btop_reduce_fwd<<<rblocks, 256, 0, st>>>(n, ldb, bws, bytop);
     }
 }

@@ -14,6 +14,13 @@
 // product, and a second kernel sums a row's partials in split order (the same
 // order for every run, pose tile and pose count) and applies the sweep's
 // epilogue.
+//
+// Both operands reach shared memory by TMA bulk copies, already split and in
+// the MMA's layout: T's tiles are split and laid out once per batched deform
+// (k_btop_pack, T changes only with the factorisation), the right-hand sides
+// are written split and tiled by the kernels that produce them (the gather
+// and the forward reduction). A CTA's stages go through two buffers: the copy
+// of stage s + 1 runs while the tensor cores multiply stage s.
 #pragma once
 
 #include <cstdint>
@@ -32,8 +39,8 @@ constexpr uint32_t kTmemCols = 256;  // the fp32 accumulator: 128 lanes x 256 co
 // one 8-row group follow each other along k (kCoreK bytes apart), the 8-row
 // groups are kCoreMN bytes apart.
 constexpr uint32_t kCoreK = 128, kCoreMN = (kDepth / 4) * 128;
-constexpr int kAFloats = kRows * kDepth, kBFloats = kCols * kDepth;
-constexpr int kSmemBytes = (2 * kAFloats + 2 * kBFloats) * 4 + 1024;  // hi and lo of each, alignment slack
+constexpr int kStageBytes = (kATileFloats + kBTileFloats) * 4;  // A and B tiles, head and rest of each
+constexpr int kSmemBytes = 2 * kStageBytes + 1024;                // two stage buffers, alignment slack
 
 // byte offset of element (r, k) of an operand tile (r: row of M or column of
 // the right-hand sides, k: column of T within the stage)
@@ -105,14 +112,39 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+__device__ __forceinline__ void bar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_addr(bar)), "r"(bytes) : "memory");
+}
+
+// bulk copy global -> shared (16-byte aligned, bytes a multiple of 16) counted on bar
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     s_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(s_addr(bar))
+                 : "memory");
+}
+
 // x = hi + lo, hi = x with the low 13 mantissa bits cleared (exact in TF32)
 __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
     hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
     lo = x - hi;
 }
 
+// Entry (d, c) of an n x ldb right-hand side matrix into its B tile, split:
+// head at the MMA layout's offset, rest kBFloats further. Entries never
+// written (rows past n, columns past 3P) stay zero from the buffer's clearing.
+__device__ __forceinline__ void put_b(float *Bt, int ldb, int d, int c, float x) {
+    float *tile = Bt + b_tile_at(d / kDepth, c / kCols, ldb);
+    const uint32_t o = tile_off(c % kCols, d % kDepth) / 4u;
+    float h, l;
+    split_tf32(x, h, l);
+    tile[o] = h;
+    tile[kBFloats + o] = l;
+}
+
 // F[d][3p + c] = the top's right-hand side of pose p: its solution entry plus
-// the update vectors of the lower children (gptr/gidx, a CSR per top row)
+// the update vectors of the lower children (gptr/gidx, a CSR per top row),
+// written split into F's B tiles
 __global__ void __launch_bounds__(256)
 k_btop_gather(int n, int P, int ldb, const int32_t *__restrict__ col, const int32_t *__restrict__ gptr,
               const int64_t *__restrict__ gidx, const Vec4<float> *__restrict__ sol,
@@ -127,37 +159,74 @@ k_btop_gather(int n, int P, int ldb, const int32_t *__restrict__ col, const int3
         v.y += u.y;
         v.z += u.z;
     }
-    float *row = F + (int64_t)d * ldb;
-    row[3 * p] = v.x;
-    row[3 * p + 1] = v.y;
-    row[3 * p + 2] = v.z;
-    if (p == P - 1)
-        for (int c = 3 * P; c < ldb; ++c) row[c] = 0.f;
+    put_b(F, ldb, d, 3 * p, v.x);
+    put_b(F, ldb, d, 3 * p + 1, v.y);
+    put_b(F, ldb, d, 3 * p + 2, v.z);
 }
 
-// One partial product: rows [i0, i0+128) of M (n x n, row-major, leading
-// dimension ldt, a multiple of 4, zero past column n) times rows [k_lo, k_hi)
-// of B (n x ldb), columns [c0, c0+256), into ws[task] (128 x ldb, ws_at). Per stage
-// of 32 columns of M: all threads load and split the tiles into shared
-// memory, thread 0 issues 12 MMAs (4 steps of K = 8, three products each)
-// and commits them to an mbarrier; the next stage is loaded into registers
-// meanwhile, and the tiles are rewritten once that phase completes.
-// lbo / sbo: kCoreK / kCoreMN. Waits are bounded: on expiry the CTA records
-// kErrTimeout, writes nothing, frees its tensor memory and returns.
+// T (UPPER: T^T) split and laid out as A tiles, row tile by row tile, the
+// stages of a row tile in column order: CTA (stage, row tile), columns past
+// the row tile's range zero.
 template <bool UPPER>
-__global__ void __launch_bounds__(kThreads, 2)
-k_btop_mma(int n, int ldt, int ldb, const float *__restrict__ M, const float *__restrict__ B, float *__restrict__ ws,
+__global__ void __launch_bounds__(256)
+k_btop_pack(int n, int ldt, const float *__restrict__ M, float *__restrict__ At) {
+    const int rt = blockIdx.y;
+    int kb, ke;
+    krange(UPPER, n, rt, kb, ke);
+    const int st = blockIdx.x;
+    if (kb + st * kDepth >= ke) return;
+    const int k0 = kb + st * kDepth;
+    float *tile = At + (int64_t)(stages_before(UPPER, n, rt) + st) * kATileFloats;
+    for (int q = threadIdx.x; q < kRows * (kDepth / 4); q += blockDim.x) {
+        const int r = q / (kDepth / 4), k4 = q % (kDepth / 4);
+        const int i = rt * kRows + r, ka = k0 + 4 * k4;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < n && ka < ke) {  // ka + 3 < ldt: ka and ldt are multiples of 4
+            v = *reinterpret_cast<const float4 *>(M + (int64_t)i * ldt + ka);
+            if (ka + 1 >= ke) v.y = 0.f;
+            if (ka + 2 >= ke) v.z = 0.f;
+            if (ka + 3 >= ke) v.w = 0.f;
+        }
+        float4 h, l;
+        split_tf32(v.x, h.x, l.x);
+        split_tf32(v.y, h.y, l.y);
+        split_tf32(v.z, h.z, l.z);
+        split_tf32(v.w, h.w, l.w);
+        const uint32_t o = tile_off(r, 4 * k4) / 4u;
+        *reinterpret_cast<float4 *>(tile + o) = h;
+        *reinterpret_cast<float4 *>(tile + kAFloats + o) = l;
+    }
+}
+
+// One partial product: rows [i0, i0+128) of T (UPPER: T^T) times rows
+// [k_lo, k_hi) of B, columns [c0, c0+256), into ws[task] (128 x ldb, ws_at).
+// Thread 0 drives the pipeline: the bulk copies of each stage's A tile
+// (32 KB) and B tile (64 KB) into one of two buffers, counted on that
+// buffer's `full` barrier; once they land, 12 MMAs (4 steps of K = 8, three
+// products each) committed to the buffer's `done` barrier, whose completion
+// frees the buffer for the stage after next. At: both directions' A tiles
+// (forward first); Bt: B's tiles. lbo / sbo: kCoreK / kCoreMN. Waits are
+// bounded: on expiry the CTA records kErrTimeout, waits (bounded) for its
+// copies and products in flight, writes nothing, frees its tensor memory and
+// returns.
+template <bool UPPER>
+__global__ void __launch_bounds__(kThreads, 1)
+k_btop_mma(int n, int ldb, const float *__restrict__ At, const float *__restrict__ Bt, float *__restrict__ ws,
            uint32_t lbo, uint32_t sbo, int *err) {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar;
+    __shared__ __align__(8) uint64_t full[2], done[2], drain;
     __shared__ uint32_t tmem_slot;
+    __shared__ int s_ok;
     unsigned char *base = smem_raw + ((1024u - (s_addr(smem_raw) & 1023u)) & 1023u);
-    float *Ahi = reinterpret_cast<float *>(base), *Alo = Ahi + kAFloats;
-    float *Bhi = Alo + kAFloats, *Blo = Bhi + kBFloats;
     const int task = blockIdx.y;
     int rt, k_lo, k_hi;
     task_of(UPPER, n, task, rt, k_lo, k_hi);
-    const int i0 = rt * kRows, c0 = blockIdx.x * kCols;
+    int kb_rt, ke_rt;
+    krange(UPPER, n, rt, kb_rt, ke_rt);
+    const int ns = (k_hi - k_lo + kDepth - 1) / kDepth;
+    const int ct = blockIdx.x, c0 = ct * kCols;
+    const float *Ad = At + (UPPER ? (int64_t)stages_before(false, n, row_tiles(n)) * kATileFloats : 0) +
+                      (int64_t)(stages_before(UPPER, n, rt) + (k_lo - kb_rt) / kDepth) * kATileFloats;
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 
     if (warp == 0) {
@@ -167,109 +236,78 @@ k_btop_mma(int n, int ldt, int ldb, const float *__restrict__ M, const float *__
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(s_addr(&bar)) : "memory");
+        for (uint64_t *b : {&full[0], &full[1], &done[0], &done[1], &drain})
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(s_addr(b)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = tmem_slot;
-    constexpr uint32_t idesc = idesc_tf32(kRows, kCols);
 
-    // the next stage's tiles are loaded into registers while the tensor cores
-    // multiply the current one
-    constexpr int kAU = kAFloats / 4 / kThreads, kBU = kBFloats / 4 / kThreads;
-    float4 ra[kAU], rb[kBU];
-    auto gload = [&](int k0) {
-        // M: 8 rows x 4 float4 per warp and step (64 contiguous bytes per row)
-#pragma unroll
-        for (int u = 0; u < kAU; ++u) {
-            const int idx = tid + u * kThreads, wc = idx / 32, ln = idx % 32;
-            const int r = (wc % (kRows / 8)) * 8 + (ln % 8), k4 = ln / 8 + 4 * (wc / (kRows / 8));
-            const int i = i0 + r, ka = k0 + 4 * k4;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (i < n && ka < k_hi) {  // ka + 3 < ldt: ka and ldt are multiples of 4
-                v = *reinterpret_cast<const float4 *>(M + (int64_t)i * ldt + ka);
-                if (ka + 1 >= k_hi) v.y = 0.f;
-                if (ka + 2 >= k_hi) v.z = 0.f;
-                if (ka + 3 >= k_hi) v.w = 0.f;
+    if (tid == 0) {
+        constexpr uint32_t idesc = idesc_tf32(kRows, kCols);
+        auto load = [&](int st, int b) {
+            unsigned char *buf = base + b * kStageBytes;
+            bar_expect_tx(&full[b], (uint32_t)kStageBytes);
+            bulk_load(buf, Ad + (int64_t)st * kATileFloats, kATileFloats * 4u, &full[b]);
+            bulk_load(buf + kATileFloats * 4, Bt + b_tile_at(k_lo / kDepth + st, ct, ldb), kBTileFloats * 4u,
+                      &full[b]);
+        };
+        bool ok = true;
+        int loaded = 0, multiplied = 0;  // stages whose copies / products were issued
+        load(0, 0);
+        loaded = 1;
+        if (ns > 1) {
+            load(1, 1);
+            loaded = 2;
+        }
+        for (int st = 0; st < ns; ++st) {
+            const int b = st & 1;
+            if (!bar_wait(&full[b], (unsigned)(st >> 1) & 1u)) {
+                ok = false;
+                break;
             }
-            ra[u] = v;
-        }
-        // B: column c0 + tid, 4 rows per step (coalesced along the columns)
-        const int c = c0 + tid;
-#pragma unroll
-        for (int u = 0; u < kBU; ++u) {
-            const int kr = k0 + 4 * u;
-            const float *src = B + (int64_t)kr * ldb + c;
-            const bool cin = c < ldb;
-            rb[u].x = (cin && kr < k_hi) ? src[0] : 0.f;
-            rb[u].y = (cin && kr + 1 < k_hi) ? src[ldb] : 0.f;
-            rb[u].z = (cin && kr + 2 < k_hi) ? src[2 * (int64_t)ldb] : 0.f;
-            rb[u].w = (cin && kr + 3 < k_hi) ? src[3 * (int64_t)ldb] : 0.f;
-        }
-    };
-    // split into TF32 heads and rests, stored in the MMA layout (a quarter
-    // warp stores one 128-byte core matrix)
-    auto sstore = [&] {
-#pragma unroll
-        for (int u = 0; u < kAU; ++u) {
-            const int idx = tid + u * kThreads, wc = idx / 32, ln = idx % 32;
-            const int r = (wc % (kRows / 8)) * 8 + (ln % 8), k4 = ln / 8 + 4 * (wc / (kRows / 8));
-            float4 h, l;
-            split_tf32(ra[u].x, h.x, l.x);
-            split_tf32(ra[u].y, h.y, l.y);
-            split_tf32(ra[u].z, h.z, l.z);
-            split_tf32(ra[u].w, h.w, l.w);
-            const uint32_t o = tile_off(r, 4 * k4);
-            *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(Ahi) + o) = h;
-            *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(Alo) + o) = l;
-        }
-#pragma unroll
-        for (int u = 0; u < kBU; ++u) {
-            float4 h, l;
-            split_tf32(rb[u].x, h.x, l.x);
-            split_tf32(rb[u].y, h.y, l.y);
-            split_tf32(rb[u].z, h.z, l.z);
-            split_tf32(rb[u].w, h.w, l.w);
-            const uint32_t o = tile_off(tid, 4 * u);
-            *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(Bhi) + o) = h;
-            *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(Blo) + o) = l;
-        }
-    };
-
-    bool ok = true;
-    int stage = 0;
-    gload(k_lo);
-    for (int k0 = k_lo; k0 < k_hi; k0 += kDepth, ++stage) {
-        sstore();
-        // the tensor cores read shared memory through the async proxy
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
             fence_after_sync();
-            const uint32_t ah = s_addr(Ahi), al = s_addr(Alo), bh = s_addr(Bhi), bl = s_addr(Blo);
+            const uint32_t ah = s_addr(base + b * kStageBytes), al = ah + kAFloats * 4u;
+            const uint32_t bh = ah + kATileFloats * 4u, bl = bh + kBFloats * 4u;
 #pragma unroll
             for (int j = 0; j < kDepth / 8; ++j) {
                 const uint32_t o = (uint32_t)j * 2u * kCoreK;  // K = 8: two core matrices along k
                 mma_tf32(tmem, smem_desc(al + o, lbo, sbo), smem_desc(bh + o, lbo, sbo), idesc,
-                         (stage > 0 || j > 0) ? 1u : 0u);
+                         (st > 0 || j > 0) ? 1u : 0u);
                 mma_tf32(tmem, smem_desc(ah + o, lbo, sbo), smem_desc(bl + o, lbo, sbo), idesc, 1u);
                 mma_tf32(tmem, smem_desc(ah + o, lbo, sbo), smem_desc(bh + o, lbo, sbo), idesc, 1u);
             }
-            mma_commit(&bar);
+            mma_commit(&done[b]);
+            multiplied = st + 1;
+            if (st + 2 < ns) {
+                // the buffer is free once this stage's products are done
+                if (!bar_wait(&done[b], (unsigned)(st >> 1) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                load(st + 2, b);
+                loaded = st + 3;
+            }
         }
-        if (k0 + kDepth < k_hi) gload(k0 + kDepth);
-        // every thread waits for this stage's products before the tiles are
-        // rewritten (or the accumulator read)
-        const bool done = bar_wait(&bar, (unsigned)stage & 1u);
-        if (__syncthreads_or(!done)) {
-            ok = false;
-            break;
+        // the last stage's products (a commit covers every earlier MMA too)
+        if (ok && !bar_wait(&done[(ns - 1) & 1], (unsigned)((ns - 1) >> 1) & 1u)) ok = false;
+        if (!ok) {
+            atomicOr(err, kErrTimeout);
+            // no copy or product may still run when the CTA leaves: wait
+            // (bounded) for every copy issued and for all products issued
+            for (int st = multiplied; st < loaded; ++st) bar_wait(&full[st & 1], (unsigned)(st >> 1) & 1u);
+            if (multiplied > 0) {
+                mma_commit(&drain);
+                bar_wait(&drain, 0u);
+            }
         }
+        s_ok = ok ? 1 : 0;
     }
+    __syncthreads();
     fence_after_sync();
-    if (ok) {
+    if (s_ok) {
         const int lane_base = 32 * (warp % 4), cbase = (warp / 4) * (kCols / 2), r = lane_base + lane;
 #pragma unroll 1
         for (int ch = 0; ch < kCols / 2 / 16; ++ch) {
@@ -283,11 +321,6 @@ k_btop_mma(int n, int ldt, int ldb, const float *__restrict__ M, const float *__
                         make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
             }
         }
-    } else {
-        if (tid == 0) atomicOr(err, kErrTimeout);
-        // one more bounded wait, so that no product is still running when the
-        // tensor memory is freed
-        if (tid == 0) bar_wait(&bar, (unsigned)(stage & 1));
     }
     fence_before_sync();
     __syncthreads();
@@ -297,7 +330,8 @@ k_btop_mma(int n, int ldt, int ldb, const float *__restrict__ M, const float *__
     }
 }
 
-// Sums a row's partial products in split order. Forward: Y (n x ldb), one
+// Sums a row's partial products in split order. Forward: Y (n x ldb, the
+// backward product's right-hand sides, written split into its B tiles), one
 // float4 per thread, consecutive threads on consecutive rows (the partials'
 // order).
 __global__ void __launch_bounds__(256)
@@ -314,7 +348,10 @@ k_btop_reduce_fwd(int n, int ldb, const float *__restrict__ ws, float *__restric
         acc.z += v.z;
         acc.w += v.w;
     }
-    *reinterpret_cast<float4 *>(Y + (int64_t)i * ldb + c) = acc;
+    put_b(Y, ldb, i, c, acc.x);
+    put_b(Y, ldb, i, c + 1, acc.y);
+    put_b(Y, ldb, i, c + 2, acc.z);
+    put_b(Y, ldb, i, c + 3, acc.w);
 }
 
 // Backward, one (top row, pose) per thread, consecutive threads on

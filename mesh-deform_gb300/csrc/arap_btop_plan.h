@@ -74,6 +74,42 @@ ARAP_BTOP_HD inline int64_t ws_at(int task, int r, int c, int ldb) {
     return (int64_t)task * kRows * ldb + ((int64_t)(c >> 2) * kRows + r) * 4 + (c & 3);
 }
 
+// Operand tiles, stored in global memory exactly as the MMA reads them from
+// shared memory (K-major core matrices, arap_btop.cuh's tile_off), TF32 head
+// then rest, so that one bulk copy moves a stage's tile. A tile: 128 rows of
+// T x 32 of its columns (kRows x kDepth floats per part); B tile: 32 rows of
+// the right-hand sides x 256 of their columns (kCols x kDepth per part).
+constexpr int kAFloats = kRows * kDepth, kBFloats = kCols * kDepth;
+constexpr int kATileFloats = 2 * kAFloats, kBTileFloats = 2 * kBFloats;
+
+// A tiles of direction `upper` for the row tiles before rt: each row tile's
+// columns [kb, ke) in stages of kDepth
+ARAP_BTOP_HD inline int stages_before(bool upper, int n, int rt) {
+    int t = 0;
+    for (int r = 0; r < rt && r * kRows < n; ++r) {
+        int kb, ke;
+        krange(upper, n, r, kb, ke);
+        t += (ke - kb + kDepth - 1) / kDepth;
+    }
+    return t;
+}
+
+// floats of both directions' A tiles of an n-column top
+inline int64_t a_tile_floats(int n) {
+    if (n <= 0) return 0;
+    const int nrt = row_tiles(n);
+    return (int64_t)(stages_before(false, n, nrt) + stages_before(true, n, nrt)) * kATileFloats;
+}
+
+// B tile (stage kb, column tile ct) of an n x ldb right-hand side matrix
+ARAP_BTOP_HD inline int col_tiles(int ldb) { return (ldb + kCols - 1) / kCols; }
+ARAP_BTOP_HD inline int64_t b_tile_at(int kb, int ct, int ldb) {
+    return ((int64_t)kb * col_tiles(ldb) + ct) * kBTileFloats;
+}
+inline int64_t b_tile_floats(int n, int ldb) {
+    return n <= 0 ? 0 : (int64_t)((n + kDepth - 1) / kDepth) * col_tiles(ldb) * kBTileFloats;
+}
+
 // floats of the partial products of one sweep (the larger of the two
 // directions' task counts)
 inline int64_t ws_floats(int n, int P) {

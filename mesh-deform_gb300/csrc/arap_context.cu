@@ -153,7 +153,7 @@ struct arap_ctx {
     DevBuf cidx_dev, handle_dev, tabs_dev;  // arap_pose_targets inputs
     DevBuf vf_ptr, vf_face, fnorm, vnorm;    // vertex normals
     // many-pose state (arap_deform_poses)
-    DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags, bftop, bytop, bws;
+    DevBuf btargets, bpc64, bpc32, bR, bbfixed, bb, bsol, buvec, bout, bticket, bflags, bftop, bytop, bws, batile;
     int bP = 0, bT = 0, bpt = 0, bgrid = 0, bntop = -1;
     int64_t bgen = -1;  // gen the many-pose buffers and counters were set up for (-1: redo)
     int pose_tile = 0;  // poses per batched-solve task (0: the largest that fits)
@@ -175,6 +175,8 @@ struct arap_ctx {
     int dense_cols = 0;  // most columns of the dense top of the tree (0: default, <0: none)
     int warp_rows = kWarpRowsDefault;  // largest front of the warp-per-supernode solves (0: none)
     int solve_schedule = kSolveScheduleDefault;  // ARAP_SOLVE_PERSISTENT or ARAP_SOLVE_LEVELS
+    // launch shape of the local step, RHS and residual (arap_set_vertex_launch)
+    VertexLaunch vlaunch[kVertexKernels] = {{1, 256}, {1, 256}, {1, 256}};
     size_t dense_inv_smem[2] = {0, 0}, dense_vec_smem[2] = {0, 0};  // configured limits (FP32, FP64)
     DevBuf top_col, top_gptr, top_gidx, tdpos, top_items, Ttop, ytop;
     int ordering = ARAP_ORDER_PER_CONSTRAINT_SET;
@@ -208,6 +210,7 @@ struct arap_ctx {
                 &pc32, &R, &diag64, &bfixed, &b, &sol, &uvec, &Lval, &Dinv, &Upd, &Xinv, &L21, &L21T, &redge,
                 &errw, &ticket, &flags, &energy, &cidx_dev, &handle_dev, &tabs_dev, &vf_ptr, &vf_face, &fnorm,
                 &vnorm, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout, &bftop, &bytop, &bws,
+                &batile,
                 &bticket, &bflags, &top_col, &top_gptr, &top_gidx, &tdpos, &top_items, &Ttop, &ytop, &Lval32,
                 &Dinv32};
     }
@@ -396,6 +399,7 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
         add(ctx->bftop, std::max<size_t>(btop_matrix_floats(nt, (int)P), 1) * sizeof(float));
         add(ctx->bytop, std::max<size_t>(btop_matrix_floats(nt, (int)P), 1) * sizeof(float));
         add(ctx->bws, std::max<size_t>(btop_workspace_floats(nt, (int)P), 1) * sizeof(float));
+        add(ctx->batile, std::max<size_t>(btop_atile_floats(nt), 1) * sizeof(float));
     }
 }
 
@@ -480,18 +484,19 @@ int prepare_symbolic(arap_ctx *ctx) {
     CK(ctx->flags.ensure(2 * sizeof(unsigned) * (size_t)std::max(s.S, 1)));
     CK(cudaMemsetAsync(ctx->ticket.p, 0, kTickets * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
-    // the solve kernels stream whole columns through chunk buffers (a column
-    // must fit one) and keep a front's vectors in shared memory; fronts of
-    // more than kSolveBlockRows rows take several passes. The FP64 form needs
-    // twice the bytes: when only the mixed form fits, FP64 deforms are refused.
+    // the solve kernels stream a front's matrices through chunk buffers
+    // (whole columns for fronts of one pass, row segments of each pass for
+    // larger ones, so columns may have any length) and keep the front's
+    // vectors in shared memory. The FP64 form needs twice the bytes: when
+    // only the mixed form fits, FP64 deforms are refused.
     const int max_rows = std::max(s.max_ldx, s.max_ld21);
     const size_t b32 = solve_smem_bytes(s.max_ldx, s.max_ld21, 4), b64 = solve_smem_bytes(s.max_ldx, s.max_ld21, 8);
     constexpr size_t kSmemMax = 227 * 1024;
-    if ((size_t)max_rows * 4 > (size_t)solve_chunk_bytes() || b32 > kSmemMax)
+    if (b32 > kSmemMax)
         return fail(ctx, ARAP_ERR_UNSUPPORTED,
                     "supernode front of " + std::to_string(max_rows) + " rows (" + std::to_string(s.max_ncol) +
                         " columns) exceeds the solve kernels' shared memory");
-    ctx->fp64_solves = (size_t)max_rows * 8 <= (size_t)solve_chunk_bytes() && b64 <= kSmemMax;
+    ctx->fp64_solves = b64 <= kSmemMax;
     if (b32 > ctx->smem_f32 || (ctx->fp64_solves && b64 > ctx->smem_f64)) {
         CK(configure_solve_smem((int)b32, ctx->fp64_solves ? (int)b64 : 0));
         ctx->smem_f32 = b32;
@@ -617,6 +622,7 @@ int prepare_symbolic(arap_ctx *ctx) {
     d.V = s.V;
     d.m = s.m;
     d.S = s.S;
+    for (int k = 0; k < kVertexKernels; ++k) d.vlaunch[k] = ctx->vlaunch[k];
     d.nnz = (int)s.dcol.size();
     d.max_ldx = s.max_ldx;
     d.max_ld21 = s.max_ld21;
@@ -951,6 +957,11 @@ int run_batch_iterations(arap_ctx *ctx, int P, int iterations) {
     unsigned long long *tk = ctx->bticket.as<unsigned long long>();
     unsigned *fl = ctx->bflags.as<unsigned>();
     const size_t fhalf = (size_t)std::max(s.S, 1) * ctx->bT;
+    if (d.n_top > 0 && m > 0 && iterations > 0) {
+        // T of this factorisation as the tensor-core products' operand tiles
+        launch_btop_pack(d, ctx->Ttop.as<float>(), ctx->batile.as<float>(), st);
+        ctx->launches += 2;
+    }
     for (int it = 0; it < iterations; ++it) {
         {
             Prof pr(ctx, ARAP_K_LOCAL);
@@ -976,7 +987,7 @@ int run_batch_iterations(arap_ctx *ctx, int P, int iterations) {
                 Prof pr(ctx, ARAP_K_SOLVE_FWD);
                 launch_bsolve(d, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
                               ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), nullptr, nullptr, tk, fl,
-                              ctx->errw.as<int>(), true, st, ctx->Ttop.as<float>(), ctx->bftop.as<float>(),
+                              ctx->errw.as<int>(), true, st, ctx->batile.as<float>(), ctx->bftop.as<float>(),
                               ctx->bytop.as<float>(), ctx->bws.as<float>());
             }
             {
@@ -984,7 +995,7 @@ int run_batch_iterations(arap_ctx *ctx, int P, int iterations) {
                 launch_bsolve(d, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
                               ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
                               ctx->bpc32.as<Vec4<float>>(), tk + 1, fl + fhalf, ctx->errw.as<int>(), false, st,
-                              ctx->Ttop.as<float>(), ctx->bftop.as<float>(), ctx->bytop.as<float>(),
+                              ctx->batile.as<float>(), ctx->bftop.as<float>(), ctx->bytop.as<float>(),
                               ctx->bws.as<float>());
             }
             ctx->launches += 1 + (batch_tasks(d) > 0 ? 2 : 0) + batch_top_launches(d);
@@ -1140,6 +1151,7 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->dense_cols = src->dense_cols;
     ctx->warp_rows = src->warp_rows;
     ctx->solve_schedule = src->solve_schedule;
+    for (int k = 0; k < kVertexKernels; ++k) ctx->vlaunch[k] = src->vlaunch[k];
     ctx->ordering = src->ordering;
     return finish_create(ctx, src->device, src, out);
 }
@@ -1319,7 +1331,8 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
             {&ctx->bflags, nflags * sizeof(unsigned)},
             {&ctx->bftop, std::max<size_t>(btop_matrix_floats(d.n_top, P), 1) * sizeof(float)},
             {&ctx->bytop, std::max<size_t>(btop_matrix_floats(d.n_top, P), 1) * sizeof(float)},
-            {&ctx->bws, std::max<size_t>(btop_workspace_floats(d.n_top, P), 1) * sizeof(float)}};
+            {&ctx->bws, std::max<size_t>(btop_workspace_floats(d.n_top, P), 1) * sizeof(float)},
+            {&ctx->batile, std::max<size_t>(btop_atile_floats(d.n_top), 1) * sizeof(float)}};
         bool moved = false;
         void *const old_targets = ctx->btargets.p;
         for (const auto &pb : plan) {
@@ -1333,6 +1346,10 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
         // number of tickets (tasks + CTAs), so the grid is fixed with them
         CK(cudaMemsetAsync(ctx->bticket.p, 0, 2 * sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(ctx->bflags.p, 0, nflags * sizeof(unsigned), st));
+        // the products' B tiles: entries past the top's rows and the poses'
+        // columns are never written and must read as zero
+        CK(cudaMemsetAsync(ctx->bftop.p, 0, ctx->bftop.cap, st));
+        CK(cudaMemsetAsync(ctx->bytop.p, 0, ctx->bytop.cap, st));
         int grid = batch_grid(d, P, pt);
         if (ctx->solve_cap > 0) grid = std::min(grid, ctx->solve_cap);
         ctx->bpt = pt;
@@ -1714,6 +1731,29 @@ int arap_set_warp_rows(arap_ctx *ctx, int32_t rows) {
         ctx->warp_rows = rows;
         ctx->sym_valid = false;  // new launch shape: scheduling counters restart with the next setup
         ctx->dirty = true;
+    }
+    return ARAP_OK;
+}
+
+int arap_set_vertex_launch(arap_ctx *ctx, int32_t kernel, int32_t threads_per_vertex, int32_t block_threads) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    const int k = kernel == ARAP_K_LOCAL ? kVertexLocal
+                  : kernel == ARAP_K_RHS ? kVertexRhs
+                  : kernel == ARAP_K_RESIDUAL ? kVertexResidual : -1;
+    if (k < 0) return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "kernel class without a vertex launch shape");
+    const int t = threads_per_vertex, b = block_threads;
+    if (t != 1 && t != 2 && t != 4 && t != 8 && t != 32)
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "threads per vertex must be 1, 2, 4, 8 or 32");
+    if (b < 32 || b % 32 != 0 || b > (k == kVertexLocal ? kLocalMaxBlock : 1024))
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "block threads must be a multiple of 32 up to the kernel's limit");
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (ctx->vlaunch[k].tpv != t || ctx->vlaunch[k].block != b) {
+        ctx->vlaunch[k] = {t, b};
+        ctx->ds.vlaunch[k] = ctx->vlaunch[k];
+        ctx->gen++;  // captured iteration graphs hold the old launch shape
     }
     return ARAP_OK;
 }

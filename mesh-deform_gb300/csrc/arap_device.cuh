@@ -263,5 +263,37 @@ __device__ __forceinline__ void rotation_fp64(int i, int e0, int e1, const int32
         for (int b = 0; b < 3; ++b) Rm[a][b] = (float)R[a][b];
 }
 
+// FP64 rotation fit of the FP64 form: the FP32 fit of the covariance
+// (scaled to unit Frobenius norm before rounding), orthonormalised and
+// refined to FP64 accuracy by Newton's method on the rotation group
+// (polar_newton); near rank-one covariances, where the FP32 fit is a poor
+// seed, take the FP64 one-sided Jacobi fit. About a quarter of the FP64
+// instructions of the FP64 Jacobi fit, the same rotation to FP64 accuracy.
+__device__ __forceinline__ void rotation_fit_fp64(const double S[3][3], double R[3][3]) {
+    double f2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) f2 += S[a][b] * S[a][b];
+    if (f2 > 0.0 && f2 < 1e300) {
+        const double sc = 1.0 / sqrt(f2);
+        float Sf[3][3], Rf[3][3], spread;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) Sf[a][b] = (float)(S[a][b] * sc);
+        rotation_from_cov<float>(Sf, Rf, &spread);
+        if (spread >= kPolarFallback) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) R[a][b] = (double)Rf[a][b];
+            polar_newton(S, R, 2);
+            return;
+        }
+    }
+    rotation_from_cov<double>(S, R);
+}
+
 }  // namespace dev
 }  // namespace arapgpu

@@ -716,7 +716,8 @@ k_local_step(int V, const int32_t *__restrict__ drow, const int32_t *__restrict_
         S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
     }
     T Rm[3][3];
-    rotation_from_cov(S, Rm);
+    if constexpr (sizeof(T) == 8) dev::rotation_fit_fp64(S, Rm);
+    else rotation_from_cov(S, Rm);
     R[3 * (int64_t)i + 0] = {Rm[0][0], Rm[0][1], Rm[0][2], (T)0};
     R[3 * (int64_t)i + 1] = {Rm[1][0], Rm[1][1], Rm[1][2], (T)0};
     R[3 * (int64_t)i + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], (T)0};
@@ -725,26 +726,54 @@ k_local_step(int V, const int32_t *__restrict__ drow, const int32_t *__restrict_
 // Local step of the mixed form: the covariance in FP32 from the FP32 rest
 // edges and the current edges differenced in FP64 (the positions are kept in
 // FP64), then the FP32 rotation fit.
-__global__ void __launch_bounds__(256)
+template <int G>
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <int G>
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Threads per vertex: a group of G lanes of one warp takes a vertex, lane l
+// its adjacency entries l, l + G, ...; the partial sums meet by shuffles
+// (G = 1: one thread per vertex). Every lane of a warp reaches the shuffles.
+template <int G>
+__global__ void __launch_bounds__(kLocalMaxBlock)
 k_local_step_mixed(int V, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
                    const float *__restrict__ w, const Vec4<float> *__restrict__ redge,
                    const Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ R,
                    const double *__restrict__ w64, const Vec4<double> *__restrict__ p64) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= V) return;
-    const Vec4<double> ci = pc64[i];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / G, l = t % G;
+    const bool live = i < V;
     float S[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    const int e1 = drow[i + 1];
-    for (int e = drow[i]; e < e1; ++e) {
-        const float wj = w[e];
-        const Vec4<float> re = redge[e];
-        const Vec4<double> cj = pc64[dcol[e]];
-        const float ex = wj * re.x, ey = wj * re.y, ez = wj * re.z;
-        const float fx = (float)(ci.x - cj.x), fy = (float)(ci.y - cj.y), fz = (float)(ci.z - cj.z);
-        S[0][0] += ex * fx; S[0][1] += ex * fy; S[0][2] += ex * fz;
-        S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
-        S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
+    int e1 = 0;
+    if (live) {
+        const Vec4<double> ci = pc64[i];
+        e1 = drow[i + 1];
+        for (int e = drow[i] + l; e < e1; e += G) {
+            const float wj = w[e];
+            const Vec4<float> re = redge[e];
+            const Vec4<double> cj = pc64[dcol[e]];
+            const float ex = wj * re.x, ey = wj * re.y, ez = wj * re.z;
+            const float fx = (float)(ci.x - cj.x), fy = (float)(ci.y - cj.y), fz = (float)(ci.z - cj.z);
+            S[0][0] += ex * fx; S[0][1] += ex * fy; S[0][2] += ex * fz;
+            S[1][0] += ey * fx; S[1][1] += ey * fy; S[1][2] += ey * fz;
+            S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
+        }
     }
+    if (G > 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) S[a][b] = group_sum<G>(S[a][b]);
+    }
+    if (!live || l != 0) return;
     float Rm[3][3], spread;
     rotation_from_cov(S, Rm, &spread);
     if (!(spread >= dev::kPolarFallback)) dev::rotation_fp64(i, drow[i], e1, dcol, w64, p64, pc64, 1, 0, Rm);
@@ -757,25 +786,34 @@ k_local_step_mixed(int V, const int32_t *__restrict__ drow, const int32_t *__res
 
 // RHS of the mixed form without bFixed (added in FP64 by the residual):
 // sum_j 1/2 w (R_i + R_j)(p_i - p_j) over the FP32 rest edges.
-__global__ void __launch_bounds__(256)
+template <int G>
+__global__ void __launch_bounds__(1024)
 k_rhs_mixed(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const float *__restrict__ w,
             const Vec4<float> *__restrict__ redge, const Vec4<float> *__restrict__ R, Vec4<float> *__restrict__ b) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    const Vec4<float> r0 = R[3 * (int64_t)i], r1 = R[3 * (int64_t)i + 1], r2 = R[3 * (int64_t)i + 2];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / G, l = t % G;
+    const bool live = i < m;
     float ax = 0.f, ay = 0.f, az = 0.f;
-    const int e1 = drow[i + 1];
-    for (int e = drow[i]; e < e1; ++e) {
-        const int j = dcol[e];
-        if (j == i) continue;
-        const float h = w[e] * 0.5f;
-        const Vec4<float> d = redge[e];
-        const Vec4<float> q0 = R[3 * (int64_t)j], q1 = R[3 * (int64_t)j + 1], q2 = R[3 * (int64_t)j + 2];
-        ax += ((r0.x + q0.x) * d.x + (r0.y + q0.y) * d.y + (r0.z + q0.z) * d.z) * h;
-        ay += ((r1.x + q1.x) * d.x + (r1.y + q1.y) * d.y + (r1.z + q1.z) * d.z) * h;
-        az += ((r2.x + q2.x) * d.x + (r2.y + q2.y) * d.y + (r2.z + q2.z) * d.z) * h;
+    if (live) {
+        const Vec4<float> r0 = R[3 * (int64_t)i], r1 = R[3 * (int64_t)i + 1], r2 = R[3 * (int64_t)i + 2];
+        const int e1 = drow[i + 1];
+        for (int e = drow[i] + l; e < e1; e += G) {
+            const int j = dcol[e];
+            if (j == i) continue;
+            const float h = w[e] * 0.5f;
+            const Vec4<float> d = redge[e];
+            const Vec4<float> q0 = R[3 * (int64_t)j], q1 = R[3 * (int64_t)j + 1], q2 = R[3 * (int64_t)j + 2];
+            ax += ((r0.x + q0.x) * d.x + (r0.y + q0.y) * d.y + (r0.z + q0.z) * d.z) * h;
+            ay += ((r1.x + q1.x) * d.x + (r1.y + q1.y) * d.y + (r1.z + q1.z) * d.z) * h;
+            az += ((r2.x + q2.x) * d.x + (r2.y + q2.y) * d.y + (r2.z + q2.z) * d.z) * h;
+        }
     }
-    b[i] = {ax, ay, az, 0.f};
+    if (G > 1) {
+        ax = group_sum<G>(ax);
+        ay = group_sum<G>(ay);
+        az = group_sum<G>(az);
+    }
+    if (live && l == 0) b[i] = {ax, ay, az, 0.f};
 }
 
 // estimatePositions RHS, arap.h:395-414
@@ -805,25 +843,38 @@ k_rhs(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol,
 }
 
 // r = b - A x in FP64 over the free vertices (A = constrained Laplacian)
-__global__ void __launch_bounds__(256)
+template <int G>
+__global__ void __launch_bounds__(1024)
 k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const double *__restrict__ w64,
            const double *__restrict__ diag64, const Vec4<double> *__restrict__ bfixed,
            const Vec4<float> *__restrict__ b, const Vec4<double> *__restrict__ x, Vec4<float> *__restrict__ r) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / G, l = t % G;
+    const bool live = i < m;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (live) {
+        const int e1 = drow[i + 1];
+        for (int e = drow[i] + l; e < e1; e += G) {
+            const int j = dcol[e];
+            if (j == i || j >= m) continue;
+            const double wj = w64[e];
+            const Vec4<double> xj = x[j];
+            ax -= wj * xj.x;
+            ay -= wj * xj.y;
+            az -= wj * xj.z;
+        }
+    }
+    if (G > 1) {
+        ax = group_sum<G>(ax);
+        ay = group_sum<G>(ay);
+        az = group_sum<G>(az);
+    }
+    if (!live || l != 0) return;
     const Vec4<double> xi = x[i];
     const double d = diag64[i];
-    double ax = d * xi.x, ay = d * xi.y, az = d * xi.z;
-    const int e1 = drow[i + 1];
-    for (int e = drow[i]; e < e1; ++e) {
-        const int j = dcol[e];
-        if (j == i || j >= m) continue;
-        const double wj = w64[e];
-        const Vec4<double> xj = x[j];
-        ax -= wj * xj.x;
-        ay -= wj * xj.y;
-        az -= wj * xj.z;
-    }
+    ax += d * xi.x;
+    ay += d * xi.y;
+    az += d * xi.z;
     const Vec4<float> bi = b[i];
     const Vec4<double> bf = bfixed[i];
     r[i] = {(float)((bf.x + (double)bi.x) - ax), (float)((bf.y + (double)bi.y) - ay),
@@ -882,17 +933,36 @@ __device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned
 
 // The chunks of one task: matrix A (columns [0, CA), leading dimension ldA)
 // then matrix B (columns [0, CB), ldB), each cut into column ranges of at most
-// kChunkBytes.
+// kChunkBytes (fronts of one pass: a column has at most kSolveBlockRows rows).
+// Fronts of several passes stream segments instead: segment j of pass rb
+// holds rows [rb * kSolveBlockRows, +kSolveBlockRows) of kSegCols columns,
+// packed with the segment's row count as leading dimension, so a column may
+// have any length and each pass reads only its own rows.
 template <typename T>
 struct ChunkPlan {
+    static constexpr int kSegCols = kChunkBytes / (kSolveBlockRows * (int)sizeof(T));
     const T *A, *B;
-    int ldA, ldB, CA, CB, cwA, cwB, nA, nB;
+    int ldA, ldB, CA, CB, cwA, cwB, nA, nB, sA, sB;
     __device__ void init(const T *a, int lda, int ca, const T *b, int ldb, int cb) {
         A = a; B = b; ldA = lda; ldB = ldb; CA = ca; CB = cb;
         cwA = max(1, kChunkBytes / (lda * (int)sizeof(T)));
         cwB = ldb > 0 ? max(1, kChunkBytes / (ldb * (int)sizeof(T))) : 1;
         nA = (CA + cwA - 1) / cwA;
         nB = CB > 0 ? (CB + cwB - 1) / cwB : 0;
+        sA = (CA + kSegCols - 1) / kSegCols;
+        sB = CB > 0 ? (CB + kSegCols - 1) / kSegCols : 0;
+    }
+    // segment j (j < sA: of A, else of B) of pass rb: first column, columns,
+    // source of its first column's rows, the matrix's leading dimension and
+    // the segment's rows
+    __device__ void seg(int j, int rb, int &c0, int &cn, const T *&src, int &ld, int &rows) const {
+        const bool a = j < sA;
+        const int jj = a ? j : j - sA, C = a ? CA : CB, row0 = rb * kSolveBlockRows;
+        ld = a ? ldA : ldB;
+        c0 = jj * kSegCols;
+        cn = min(kSegCols, C - c0);
+        rows = min(kSolveBlockRows, ld - row0);
+        src = (a ? A : B) + (int64_t)c0 * ld + row0;
     }
     __device__ int total() const { return nA + nB; }
     // first column, number of columns and source of chunk k
@@ -921,6 +991,33 @@ __device__ __forceinline__ void issue_chunk(const ChunkPlan<T> &pl, int k, T *bu
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // buffer reads done before the async write
     mbar_expect_tx(bar, bytes);
     tma_load_1d(buf, src, bytes, bar);
+}
+
+// Segment j of pass rb into buf: one bulk copy per column (16-byte aligned:
+// leading dimensions are multiples of 4 and passes start at multiples of
+// kSolveBlockRows), all counted on `bar`.
+template <typename T>
+__device__ __forceinline__ void issue_seg(const ChunkPlan<T> &pl, int j, int rb, T *buf, uint64_t *bar) {
+    int c0, cn, ld, rows;
+    const T *src;
+    pl.seg(j, rb, c0, cn, src, ld, rows);
+    const unsigned bytes = (unsigned)(rows * (int)sizeof(T));
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // buffer reads done before the async write
+    mbar_expect_tx(bar, bytes * (unsigned)cn);
+    for (int i = 0; i < cn; ++i) tma_load_1d(buf + i * rows, src + (int64_t)i * ld, bytes, bar);
+}
+
+// Both matrices of a task of several passes into L2, in pieces of at most 1 MiB.
+template <typename T>
+__device__ __forceinline__ void prefetch_mats_l2(const ChunkPlan<T> &pl) {
+    for (int m = 0; m < 2; ++m) {
+        const char *p = reinterpret_cast<const char *>(m == 0 ? pl.A : pl.B);
+        const int64_t total = (int64_t)(m == 0 ? pl.CA * pl.ldA : pl.CB * pl.ldB) * (int64_t)sizeof(T);
+        for (int64_t o = 0; o < total; o += (1 << 20)) {
+            const unsigned n = (unsigned)min((int64_t)(1 << 20), total - o);
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p + o), "r"(n) : "memory");
+        }
+    }
 }
 
 // Chunk buffer b of a lower-level solve CTA (the ring at the start of its
@@ -1140,13 +1237,20 @@ k_solve_fwd(int S, int Z, int lbeg, SolveSmem lay, const int32_t *__restrict__ o
     ChunkPlan<T> pl;
     pl.init(Xall + d.x_off, d.ldx, nc, L21all + d.l21_off, d.ld21, nb > 0 ? nc : 0);
     const int ntot = pl.total();
-    const VPlan vp{pl.nA, pl.nB, row_blocks(nc), pl.nB > 0 ? row_blocks(nb) : 0};
+    // one pass (chunks of whole columns) or several (segments of each pass's rows)
+    const int rbA = row_blocks(nc), rbB = pl.nB > 0 ? row_blocks(nb) : 0;
+    const bool multi = rbA > 1 || rbB > 1;
+    const VPlan vp = multi ? VPlan{pl.sA, pl.sB, rbA, rbB} : VPlan{pl.nA, pl.nB, rbA, rbB};
     const int vtot = vp.total();
     VCursor iss;  // next stream position to issue (thread 0)
     iss.start(vp);
     if (tid == 0) {
-        for (int e = 0; e < vtot && e < kSolveBufs; ++e, iss.step(vp)) issue_chunk(pl, iss.k, sbuf<T>(smem_raw, e), &bars[e]);
-        for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
+        for (int e = 0; e < vtot && e < kSolveBufs; ++e, iss.step(vp)) {
+            if (multi) issue_seg(pl, iss.k, iss.rb, sbuf<T>(smem_raw, e), &bars[e]);
+            else issue_chunk(pl, iss.k, sbuf<T>(smem_raw, e), &bars[e]);
+        }
+        if (multi) prefetch_mats_l2(pl);
+        else for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
@@ -1218,7 +1322,7 @@ k_solve_fwd(int S, int Z, int lbeg, SolveSmem lay, const int32_t *__restrict__ o
     // phase A: y = X fc (rows nc), phase B: fb -= L21 y (rows nb), each in
     // passes of at most kSolveBlockRows rows
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-    if (vtot == ntot) {
+    if (!multi) {
         // every phase in one pass: the plain chunk sequence
         const Quads Qa = quads_for(nc), Qb = quads_for(nb);
         for (int k = 0; k < ntot; ++k) {
@@ -1252,16 +1356,16 @@ k_solve_fwd(int S, int Z, int lbeg, SolveSmem lay, const int32_t *__restrict__ o
             const int kb = e & (kSolveBufs - 1);
             T *buf = sbuf<T>(smem_raw, kb);
             wait_chunk(&bars[kb], (ph[kb] + (unsigned)(e / kSolveBufs)) & 1u, err);
-            int c0, cn, ld;
+            int c0, cn, ld, rows;
             const T *src;
-            pl.chunk(k, c0, cn, src, ld);
-            if (Q.active()) chunk_axpy(buf + row0, ld, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? fc : yv, ax, ay, az);
+            pl.seg(k, cur.rb, c0, cn, src, ld, rows);
+            if (Q.active()) chunk_axpy(buf, rows, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? fc : yv, ax, ay, az);
             __syncthreads();
             if (tid == 0 && e + kSolveBufs < vtot) {
-                issue_chunk(pl, iss.k, buf, &bars[kb]);
+                issue_seg(pl, iss.k, iss.rb, buf, &bars[kb]);
                 iss.step(vp);
             }
-            if (k == (phase == 0 ? pl.nA - 1 : ntot - 1)) {
+            if (k == (phase == 0 ? vp.nA - 1 : vp.nA + vp.nB - 1)) {
                 if (phase == 0) reduce_quads<T, false>(Q, ax, ay, az, red, yv + row0);
                 else reduce_quads<T, true>(Q, ax, ay, az, red, fb + row0);
 #pragma unroll
@@ -1323,13 +1427,21 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     else pl.init(Xall + d.xt_off, d.ldx, nc, nullptr, 0, 0);
     const int ntot = pl.total();
     const int nA = nb > 0 ? pl.nA : 0;  // chunks of L21^T
-    const VPlan vp{nA, ntot - nA, row_blocks(nc), row_blocks(nc)};
+    // one pass (chunks of whole columns) or several (segments of each pass's rows)
+    const int rbs = row_blocks(nc);
+    const bool multi = rbs > 1;
+    const int sAv = nb > 0 ? pl.sA : 0;
+    const VPlan vp = multi ? VPlan{sAv, pl.sA + pl.sB - sAv, rbs, rbs} : VPlan{nA, ntot - nA, rbs, rbs};
     const int vtot = vp.total();
     VCursor iss;  // next stream position to issue (thread 0)
     iss.start(vp);
     if (tid == 0) {
-        for (int e = 0; e < vtot && e < kSolveBufs; ++e, iss.step(vp)) issue_chunk(pl, iss.k, sbuf<T>(smem_raw, e), &bars[e]);
-        for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
+        for (int e = 0; e < vtot && e < kSolveBufs; ++e, iss.step(vp)) {
+            if (multi) issue_seg(pl, iss.k, iss.rb, sbuf<T>(smem_raw, e), &bars[e]);
+            else issue_chunk(pl, iss.k, sbuf<T>(smem_raw, e), &bars[e]);
+        }
+        if (multi) prefetch_mats_l2(pl);
+        else for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
     const int32_t *rs = rows + d.rows_off;
     for (int i = tid; i < d.ldx; i += kSolveThreads)
@@ -1349,7 +1461,7 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
     // phase A (nb > 0): z -= L21^T g; phase B: x = X^T z; both have nc rows,
     // in passes of at most kSolveBlockRows rows
     T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
-    if (vtot == ntot) {
+    if (!multi) {
         // both phases in one pass: the plain chunk sequence
         const Quads Q = quads_for(nc);
         for (int k = 0; k < ntot; ++k) {
@@ -1380,16 +1492,16 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
             const int kb = e & (kSolveBufs - 1);
             T *buf = sbuf<T>(smem_raw, kb);
             wait_chunk(&bars[kb], (ph[kb] + (unsigned)(e / kSolveBufs)) & 1u, err);
-            int c0, cn, ld;
+            int c0, cn, ld, rows;
             const T *src;
-            pl.chunk(k, c0, cn, src, ld);
-            if (Q.active()) chunk_axpy(buf + row0, ld, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? gb : zv, ax, ay, az);
+            pl.seg(k, cur.rb, c0, cn, src, ld, rows);
+            if (Q.active()) chunk_axpy(buf, rows, cn, c0, Q.q, Q.g, Q.G, phase == 0 ? gb : zv, ax, ay, az);
             __syncthreads();
             if (tid == 0 && e + kSolveBufs < vtot) {
-                issue_chunk(pl, iss.k, buf, &bars[kb]);
+                issue_seg(pl, iss.k, iss.rb, buf, &bars[kb]);
                 iss.step(vp);
             }
-            if (k == (phase == 0 ? nA - 1 : ntot - 1)) {
+            if (k == (phase == 0 ? vp.nA - 1 : vp.nA + vp.nB - 1)) {
                 if (phase == 0) reduce_quads<T, true>(Q, ax, ay, az, red, zv + row0);
                 else reduce_quads<T, false>(Q, ax, ay, az, red, xv + row0);
 #pragma unroll
@@ -2125,13 +2237,34 @@ void launch_rest_edges(const DevSym &s, const Vec4<double> *p64, Vec4<float> *re
 void launch_local_step_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
                              Vec4<float> *R, const double *w64, const Vec4<double> *p64, cudaStream_t st) {
     if (s.V == 0) return;
-    k_local_step_mixed<<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.drow, s.dcol, w32, redge, pc64, R, w64, p64);
+    const VertexLaunch vl = s.vlaunch[kVertexLocal];
+    const int grid = (int)(((int64_t)s.V * vl.tpv + vl.block - 1) / vl.block);
+#define ARAP_LOCAL(G) \
+    k_local_step_mixed<G><<<grid, vl.block, 0, st>>>(s.V, s.drow, s.dcol, w32, redge, pc64, R, w64, p64)
+    switch (vl.tpv) {
+    case 2: ARAP_LOCAL(2); break;
+    case 4: ARAP_LOCAL(4); break;
+    case 8: ARAP_LOCAL(8); break;
+    case 32: ARAP_LOCAL(32); break;
+    default: ARAP_LOCAL(1); break;
+    }
+#undef ARAP_LOCAL
 }
 
 void launch_rhs_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<float> *R,
                       Vec4<float> *b, cudaStream_t st) {
     if (s.m == 0) return;
-    k_rhs_mixed<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w32, redge, R, b);
+    const VertexLaunch vl = s.vlaunch[kVertexRhs];
+    const int grid = (int)(((int64_t)s.m * vl.tpv + vl.block - 1) / vl.block);
+#define ARAP_RHS(G) k_rhs_mixed<G><<<grid, vl.block, 0, st>>>(s.m, s.drow, s.dcol, w32, redge, R, b)
+    switch (vl.tpv) {
+    case 2: ARAP_RHS(2); break;
+    case 4: ARAP_RHS(4); break;
+    case 8: ARAP_RHS(8); break;
+    case 32: ARAP_RHS(32); break;
+    default: ARAP_RHS(1); break;
+    }
+#undef ARAP_RHS
 }
 
 template <typename TF>
@@ -2166,7 +2299,17 @@ void launch_rhs(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *R,
 void launch_residual(const DevSym &s, const double *w64, const double *diag64, const Vec4<double> *bfixed,
                      const Vec4<float> *b, const Vec4<double> *x64, Vec4<float> *r, cudaStream_t st) {
     if (s.m == 0) return;
-    k_residual<<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, bfixed, b, x64, r);
+    const VertexLaunch vl = s.vlaunch[kVertexResidual];
+    const int grid = (int)(((int64_t)s.m * vl.tpv + vl.block - 1) / vl.block);
+#define ARAP_RES(G) k_residual<G><<<grid, vl.block, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, bfixed, b, x64, r)
+    switch (vl.tpv) {
+    case 2: ARAP_RES(2); break;
+    case 4: ARAP_RES(4); break;
+    case 8: ARAP_RES(8); break;
+    case 32: ARAP_RES(32); break;
+    default: ARAP_RES(1); break;
+    }
+#undef ARAP_RES
 }
 
 void launch_demote(int count, const double *const *src, float *const *dst, const int64_t *n, cudaStream_t st) {

@@ -46,6 +46,17 @@ __device__ __forceinline__ unsigned flag_wait_limit(const int *err) {
 constexpr int kMaxLevelLaunch = 48;
 constexpr int kLevelTicket0 = 8;
 
+// launch shape of a per-vertex kernel of the single-request iterations
+// (arap_set_vertex_launch): tpv lanes of one warp per vertex (1, 2, 4, 8 or
+// 32), block threads a multiple of 32 (and of tpv) up to 1024
+struct VertexLaunch {
+    int tpv, block;
+};
+enum { kVertexLocal = 0, kVertexRhs = 1, kVertexResidual = 2, kVertexKernels = 3 };
+// largest block of the local step (its FP64 refit needs the registers of at
+// most 256 threads per block); the RHS and the residual take up to 1024
+constexpr int kLocalMaxBlock = 256;
+
 struct DevTopo {
     int V, F, nnz;
     const int32_t *faces;    // 3F (original vertex ids)
@@ -70,6 +81,7 @@ struct DevSym {
     // [lwarp, ltop) as one launch per level instead of one persistent launch;
     // level l holds the supernodes level_sn[lev_ptr[l], lev_ptr[l+1]), its
     // fronts fit lev_ldx[l] / lev_ld21[l] rows, lev_grid32/64[l] CTAs
+    VertexLaunch vlaunch[kVertexKernels];
     int level_launch;
     int lev_ptr[kMaxLevelLaunch + 1], lev_ldx[kMaxLevelLaunch], lev_ld21[kMaxLevelLaunch];
     int lev_grid32[kMaxLevelLaunch], lev_grid64[kMaxLevelLaunch];
@@ -217,14 +229,19 @@ void launch_bresidual(const DevSym &s, int P, const double *w64, const double *d
 void launch_bsolve(const DevSym &s, int P, int pt, int grid, const float *X, const float *L21, const float *L21T,
                    Vec4<float> *sol, Vec4<float> *uvec, Vec4<double> *pc64, Vec4<float> *pc32,
                    unsigned long long *ticket, unsigned *flags, int *err, bool forward, cudaStream_t st,
-                   const float *Ttop, float *bftop, float *bytop, float *bws);
+                   const float *atiles, float *bftop, float *bytop, float *bws);
+// the dense top's T and T^T (row-major, FP32) split into TF32 head and rest
+// and laid out as the tensor-core products' A tiles (btop_atile_floats)
+void launch_btop_pack(const DevSym &s, const float *Ttop, float *atiles, cudaStream_t st);
 // supernode tasks of the batched sweeps (the dense top's levels excluded)
 int batch_tasks(const DevSym &s);
 // launches of the dense top in one forward + backward pair of batched sweeps
 int batch_top_launches(const DevSym &s);
-// the dense top's n x 3P right-hand sides (rows padded to a multiple of 4
-// floats) and the partial products of one sweep, in floats
+// the dense top's n x 3P right-hand sides as the products' B tiles (split,
+// zero padding: clear them when allocated), its A tiles and the partial
+// products of one sweep, in floats
 size_t btop_matrix_floats(int n, int P);
+size_t btop_atile_floats(int n);
 size_t btop_workspace_floats(int n, int P);
 void launch_bgather(const DevSym &s, int P, const Vec4<double> *pc64, double *out, cudaStream_t st);
 // handle targets of P rigid poses (P x nc x 3, ascending constrained order)

@@ -2,6 +2,7 @@
 // arap_server.h over the library's device contexts.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <new>
 #include <string>
 
@@ -49,6 +50,26 @@ struct CtxBackend {
         return cudaMallocHost(&p, bytes) == cudaSuccess ? p : nullptr;
     }
     void free_host(void *p) { cudaFreeHost(p); }
+    // Grows the device's stream-ordered pool by `bytes` once (allocated and
+    // freed again; freed pool memory stays with the process): the contexts of
+    // new constraint sets then take their buffers from memory the process
+    // already holds instead of mapping more from the driver (measured ~6.7 ms
+    // of buffer allocation per new set on a growing pool).
+    void reserve_pool(int64_t bytes) {
+        if (bytes <= 0) return;
+        cudaSetDevice(device);
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return;
+        uint64_t thr = ~0ull;
+        if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr) != cudaSuccess) return;
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return;
+        void *p = nullptr;
+        if (cudaMallocAsync(&p, (size_t)bytes, st) == cudaSuccess) cudaFreeAsync(p, st);
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+        cudaGetLastError();  // a reservation that did not fit is not an error of the server
+    }
     int64_t default_budget() {
         size_t free_b = 0, total_b = 0;
         cudaSetDevice(device);
@@ -84,6 +105,12 @@ int arap_srv_create(const arap_server_config *cfg, arap_server **out) {
     }
     CtxBackend b;
     b.device = cfg->device;
+    {
+        // pool memory for the contexts to come: a quarter of the budget, at
+        // most 32 GiB
+        const int64_t budget = cfg->device_budget_bytes > 0 ? cfg->device_budget_bytes : b.default_budget();
+        b.reserve_pool(std::min<int64_t>(budget / 4, (int64_t)32 << 30));
+    }
     arap_server *s = new (std::nothrow) arap_server();
     if (!s) return ARAP_ERR_OUT_OF_MEMORY;
     s->impl = new arapsrv::Server<CtxBackend>(b, *cfg);

@@ -185,3 +185,37 @@ def test_level_schedule_rejects_unknown(gpu):
         with pytest.raises(gpu.ArapError) as e:
             ctx.set_solve_schedule(7)
         assert e.value.code == gpu.ARAP_ERR_INVALID_ARGUMENT
+
+
+def test_vertex_launch_shapes_match(gpu):
+    """Every launch shape of the local step, RHS and residual (threads per
+    vertex up to a warp per vertex, block sizes) gives the default's result up
+    to the order of sums, and the oracle's within the mixed tolerance; the
+    autotuner leaves a valid shape set."""
+    import arap_tune
+    from oracle import oracle as O
+
+    w = W.cfg_twisted_bar(h=0.05, iterations=6)
+    ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, w.iterations)
+    assert ok
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        ctx.set_precision("mixed", 1)
+        ctx.set_rest_positions(w.positions)
+        ctx.set_constraints(w.cidx, w.ctargets)
+        base = ctx.deform(w.iterations)
+        for name, shapes in arap_tune.VERTEX_SHAPES.items():
+            for tpv, blk in shapes:
+                ctx.set_vertex_launch(name, tpv, blk)
+                ctx.invalidate()
+                got = ctx.deform(w.iterations)
+                assert W.bbox_rel_error(got, base, w.positions) <= 1e-6, (name, tpv, blk)
+                assert W.bbox_rel_error(got, ref, w.positions) <= 1e-6, (name, tpv, blk)
+            ctx.set_vertex_launch(name, 1, 256)
+        res = arap_tune.tune_vertex_launch(ctx, w.iterations)
+        assert set(res) == {"local", "rhs", "residual"}
+        ctx.invalidate()
+        assert W.bbox_rel_error(ctx.deform(w.iterations), ref, w.positions) <= 1e-6
+        with pytest.raises(gpu.ArapError):
+            ctx.set_vertex_launch("local", 3, 256)
+        with pytest.raises(gpu.ArapError):
+            ctx.set_vertex_launch("local", 1, 512)
