@@ -789,7 +789,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="twisted_bar")
     ap.add_argument("--h", type=float, default=0.025)
-    ap.add_argument("--iterations", type=int, default=30)
+    ap.add_argument("--iterations", type=int, default=None,
+                    help="local/global iterations per deform (default: the configuration's own: twisted bar 30, "
+                         "icosphere L4 10, noisy sphere 50, pose batch 20, mesh batch 30)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--refine", type=int, default=1,
                     help="mixed form: refinement solves per iteration beyond the first (every solve corrects the "
@@ -832,6 +834,8 @@ def main():
     ap.add_argument("--serve-solve-ctas", type=int, default=0, help="serving: CTAs per solve launch (0: auto)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.iterations is None:
+        args.iterations = {"icosphere_l4": 10, "noisy_sphere": 50, "pose_batch": 20}.get(args.workload, 30)
 
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         return spawn_replicas(args)

@@ -450,7 +450,7 @@ k_blocal(int V, int P, const int32_t *__restrict__ drow, const int32_t *__restri
     }
     float Rm[3][3], spread;
     dev::rotation_from_cov<float>(S, Rm, &spread);
-    if (!(spread >= dev::kPolarFallback)) dev::rotation_fp64(i, drow[i], drow[i + 1], dcol, w64, p64, pc64, P, p, Rm);
+    if (!(spread >= dev::kPolarFallback)) dev::rotation_fp64<false>(i, drow[i], drow[i + 1], dcol, w64, p64, pc64, P, p, Rm);
     R[3 * t + 0] = {Rm[0][0], Rm[0][1], Rm[0][2], 0.f};
     R[3 * t + 1] = {Rm[1][0], Rm[1][1], Rm[1][2], 0.f};
     R[3 * t + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], 0.f};

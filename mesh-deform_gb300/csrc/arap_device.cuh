@@ -167,12 +167,14 @@ constexpr float kPolarFallback = 0.1f;
 // is g, the axial vector of the skew part of Q = (S R0)^T, and its Hessian
 // -(tr(Q) I - sym(Q)); the step w = (tr(Q) I - sym(Q))^-1 g is applied
 // through the Cayley map, which keeps R orthogonal. Quadratic convergence:
-// from an FP32 fit, two steps reach FP64 accuracy.
+// from an FP32 fit (error e), one step leaves about e^2, two reach FP64
+// accuracy.
 template <typename T>
-__device__ __forceinline__ void polar_newton(const T S[3][3], T R[3][3], int iters) {
+__device__ __forceinline__ void polar_newton(const T S[3][3], T R[3][3], int ns_iters, int iters) {
     // R orthogonal to working precision first (the Cayley steps keep R's
-    // deviation from orthogonality): Newton-Schulz, R <- R (3 I - R^T R) / 2
-    for (int it = 0; it < 2; ++it) {
+    // deviation from orthogonality): Newton-Schulz, R <- R (3 I - R^T R) / 2,
+    // which squares the deviation (1e-7 of an FP32 fit -> 1e-14 -> 1e-28)
+    for (int it = 0; it < ns_iters; ++it) {
         T G[3][3];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -232,6 +234,10 @@ __device__ __forceinline__ void polar_newton(const T S[3][3], T R[3][3], int ite
 // and its rotation refined from the FP32 fit Rm (in place), from the rest
 // positions p, current positions pc (element k of vertex k's pose at
 // k * stride + off) and the FP64 weights.
+// NEWTON: the refinement below; else the FP64 one-sided Jacobi fit of the
+// FP64 covariance (measured faster in the batched local step, where the 32
+// lanes of a warp are 32 poses of one vertex, slower for one request).
+template <bool NEWTON>
 __device__ __forceinline__ void rotation_fp64(int i, int e0, int e1, const int32_t *__restrict__ dcol,
                                               const double *__restrict__ w64, const Vec4<double> *__restrict__ p,
                                               const Vec4<double> *__restrict__ pc, int64_t stride, int64_t off,
@@ -249,14 +255,19 @@ __device__ __forceinline__ void rotation_fp64(int i, int e0, int e1, const int32
         S[2][0] += ez * fx; S[2][1] += ez * fy; S[2][2] += ez * fz;
     }
     // Newton's method on the rotation group from the FP32 fit, which is close
-    // (a few 1e-6 at worst): a FP64 SVD would take an order of magnitude more
-    // FP64 instructions, the scarce kind on this GPU.
+    // (a few 1e-6 at worst): one orthonormalisation and one Newton step leave
+    // an error of about 1e-12, far below what the mixed form's FP32 rotations
+    // carry anyway, for ~300 FP64 instructions (the scarce kind on this GPU).
     double R[3][3];
+    if constexpr (NEWTON) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+        for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) R[a][b] = (double)Rm[a][b];
-    polar_newton(S, R, 2);
+            for (int b = 0; b < 3; ++b) R[a][b] = (double)Rm[a][b];
+        polar_newton(S, R, 1, 1);
+    } else {
+        rotation_from_cov<double>(S, R);
+    }
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -288,7 +299,7 @@ __device__ __forceinline__ void rotation_fit_fp64(const double S[3][3], double R
             for (int a = 0; a < 3; ++a)
 #pragma unroll
                 for (int b = 0; b < 3; ++b) R[a][b] = (double)Rf[a][b];
-            polar_newton(S, R, 2);
+            polar_newton(S, R, 2, 2);
             return;
         }
     }

@@ -303,6 +303,63 @@ k_fea(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const int3
     }
 }
 
+// The entries of a factor tile of vr rows x vc columns that are needed
+// (tri: only rows r >= c, the tile on the diagonal), column by column, dealt
+// to the CTA's threads in turn: at most four per thread, all lanes of a warp
+// busy but in the last one. Factor kernels built on it issue no FP64
+// instruction for padding or for the upper triangle (GB300 issues about two
+// FP64 FMAs per clock per SM, so every wasted lane costs).
+// acc[q] += sum_t A(t, er[q]) B(t, ec[q]) over t < kw for the thread's ne
+// entries (A, B row-major in shared memory, rows t). One branch per count,
+// so a warp whose lanes all hold fewer entries issues fewer FP64
+// instructions (predicated-off instructions still take issue slots).
+template <int NE, typename TF>
+__device__ __forceinline__ void tile_fma_n(int kw, const TF *A, int lda, const TF *B, int ldb, const int er[4],
+                                           const int ec[4], TF acc[4]) {
+    for (int t = 0; t < kw; ++t)
+#pragma unroll
+        for (int q = 0; q < NE; ++q) acc[q] += A[t * lda + er[q]] * B[t * ldb + ec[q]];
+}
+template <typename TF>
+__device__ __forceinline__ void tile_fma(int ne, int kw, const TF *A, int lda, const TF *B, int ldb, const int er[4],
+                                         const int ec[4], TF acc[4]) {
+    switch (ne) {
+    case 4: tile_fma_n<4>(kw, A, lda, B, ldb, er, ec, acc); break;
+    case 3: tile_fma_n<3>(kw, A, lda, B, ldb, er, ec, acc); break;
+    case 2: tile_fma_n<2>(kw, A, lda, B, ldb, er, ec, acc); break;
+    case 1: tile_fma_n<1>(kw, A, lda, B, ldb, er, ec, acc); break;
+    default: break;
+    }
+}
+
+__device__ __forceinline__ int tile_entries(int vr, int vc, bool tri, int er[4], int ec[4]) {
+    int ne = 0;
+    if (vr <= 0 || vc <= 0) return 0;
+    if (!tri) {
+        const int tot = vr * vc;
+        for (int e = threadIdx.x; e < tot && ne < 4; e += blockDim.x) {
+            er[ne] = e % vr;
+            ec[ne] = e / vr;
+            ++ne;
+        }
+    } else {
+        int tot = 0;
+        for (int c = 0; c < vc; ++c) tot += max(vr - c, 0);
+        for (int e = threadIdx.x; e < tot && ne < 4; e += blockDim.x) {
+            // column c holds rows c..vr-1 (vr - c entries)
+            int c = 0, base = 0;
+            while (e >= base + (vr - c)) {
+                base += vr - c;
+                ++c;
+            }
+            er[ne] = c + (e - base);
+            ec[ne] = c;
+            ++ne;
+        }
+    }
+    return ne;
+}
+
 // Left-looking update of block column jb: rows [j0 + 32 rt, +32) of columns
 // [j0, j0+w) lose sum_{k < j0} P(r, k) P(j0+c, k).
 template <typename TF>
@@ -316,7 +373,12 @@ k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, T
     const int j0 = jb * NB, w = min(NB, nc - j0);
     const int r0 = j0 + it.a * kUpdRows;
     TF *P = Lval + d.panel_off;
-    const int tid = threadIdx.x, tx = tid % 8, ty = tid / 8;  // 4 columns x 1 row per thread
+    const int tid = threadIdx.x;
+    // the tile's entries: rows r0.. (at most kUpdRows, inside the front),
+    // columns of the block; the first row tile is the diagonal block, of
+    // which the lower triangle is needed
+    int er[4], ec[4];
+    const int ne = tile_entries(min(kUpdRows, n - r0), w, it.a == 0, er, ec);
     TF acc[4] = {0, 0, 0, 0};
     // the next k-slice is loaded into registers while the current one is
     // multiplied, so its global round trip overlaps the products
@@ -348,22 +410,12 @@ k_fupd(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, T
         }
         __syncthreads();
         if (k0 + NB < j0) load_slice(k0 + NB);
-#pragma unroll 8
-        for (int t = 0; t < NB; ++t) {
-            const TF a0 = As[t][ty];
-#pragma unroll
-            for (int cc = 0; cc < 4; ++cc) acc[cc] += a0 * Bs[t][tx * 4 + cc];
-        }
+        tile_fma(ne, NB, &As[0][0], kUpdRows, &Bs[0][0], NB + 1, er, ec, acc);
         __syncthreads();
     }
-    const int r = r0 + ty;
-    if (r < n) {
 #pragma unroll
-        for (int cc = 0; cc < 4; ++cc) {
-            const int c = tx * 4 + cc;
-            if (c < w) P[(int64_t)(j0 + c) * n + r] -= acc[cc];
-        }
-    }
+    for (int q = 0; q < 4; ++q)
+        if (q < ne) P[(int64_t)(j0 + ec[q]) * n + r0 + er[q]] -= acc[q];
 }
 
 // 1/sqrt(a) for the pivots: an FP32 seed refined by two Newton steps in the
@@ -490,31 +542,40 @@ k_frows(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, 
     const int r0 = j0 + w + it.a * kRowsTile;
     TF *P = Lval + d.panel_off;
     const TF *D = Dinv + d.dinv_off + (int64_t)jb * NB * NB;  // column-major: D[k * NB + c] = X(c, k)
-    const int tid = threadIdx.x, tx = tid % 8, ty = tid / 8;  // 4 columns x 2 rows per thread
+    // warp wp: columns 4wp..4wp+3; lane: rows lane and lane + 32. X is lower
+    // triangular, so column c needs k <= c only: a warp's k range ends at its
+    // last column (the same bound for all its lanes), and warps past the
+    // block's columns or rows skip their work, which saves FP64 instructions,
+    // the scarce kind on this GPU
+    const int tid = threadIdx.x, wp = tid >> 5, lane = tid & 31;
     for (int q = tid; q < NB * kRowsTile; q += kFactorThreads) {
         const int t = q / kRowsTile, r = q % kRowsTile;
         As[t][r] = (t < w && r0 + r < n) ? P[(int64_t)(j0 + t) * n + r0 + r] : (TF)0;
     }
     for (int q = tid; q < NB * NB; q += kFactorThreads) Bs[q / NB][q % NB] = D[q];
     __syncthreads();
+    const int c0 = 4 * wp;
+    if (c0 >= w) return;
+    const int kend = min(c0 + 4, w);
+    const bool two = r0 + 32 < n;  // rows lane + 32 hold entries for some lane
     TF acc[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-#pragma unroll 8
-    for (int t = 0; t < NB; ++t) {
-        const TF a0 = As[t][ty], a1 = As[t][ty + 32];
+    for (int t = 0; t < kend; ++t) {
+        const TF a0 = As[t][lane];
 #pragma unroll
-        for (int cc = 0; cc < 4; ++cc) {
-            const TF bv = Bs[t][tx * 4 + cc];
-            acc[0][cc] += a0 * bv;
-            acc[1][cc] += a1 * bv;
+        for (int cc = 0; cc < 4; ++cc) acc[0][cc] += a0 * Bs[t][c0 + cc];
+        if (two) {
+            const TF a1 = As[t][lane + 32];
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) acc[1][cc] += a1 * Bs[t][c0 + cc];
         }
     }
 #pragma unroll
     for (int rr = 0; rr < 2; ++rr) {
-        const int r = r0 + ty + 32 * rr;
+        const int r = r0 + lane + 32 * rr;
         if (r >= n) continue;
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
-            const int c = tx * 4 + cc;
+            const int c = c0 + cc;
             if (c < w) P[(int64_t)(j0 + c) * n + r] = acc[rr][cc];
         }
     }
@@ -534,8 +595,13 @@ k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF
     const TF *P = Lval + d.panel_off;
     TF *U = Upd + d.upd_off;
     const int rb = it.a * kSyrkTile, cb = it.b * kSyrkTile;  // within U
-    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;  // 2 x 2 entries per thread
-    TF acc[2][2] = {{(TF)0, (TF)0}, {(TF)0, (TF)0}};
+    const int vr = min(kSyrkTile, nb - rb), vc = min(kSyrkTile, nb - cb);
+    const bool diag = rb == cb;
+    const int tid = threadIdx.x;
+    // only the tile's entries inside U and its lower triangle are computed
+    int er[4], ec[4];
+    const int ne = tile_entries(vr, vc, diag, er, ec);
+    TF acc[4] = {(TF)0, (TF)0, (TF)0, (TF)0};
     // the next k-slice is loaded into registers while the current one is
     // multiplied, so its global round trip overlaps the products
     constexpr int kPer = NB * kSyrkTile / kFactorThreads;
@@ -555,6 +621,7 @@ k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF
     };
     if (nc > 0) load_slice(0);
     for (int k0 = 0; k0 < nc; k0 += NB) {
+        const int kw = min(NB, nc - k0);
 #pragma unroll
         for (int u = 0; u < kPer; ++u) {
             const int q = tid + u * kFactorThreads;
@@ -563,26 +630,12 @@ k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF
         }
         __syncthreads();
         if (k0 + NB < nc) load_slice(k0 + NB);
-#pragma unroll 8
-        for (int t = 0; t < NB; ++t) {
-            const TF a0 = As[t][ty], a1 = As[t][ty + 16];
-            const TF b0 = Bs[t][tx], b1 = Bs[t][tx + 16];
-            acc[0][0] += a0 * b0;
-            acc[0][1] += a0 * b1;
-            acc[1][0] += a1 * b0;
-            acc[1][1] += a1 * b1;
-        }
+        tile_fma(ne, kw, &As[0][0], kSyrkTile, &Bs[0][0], kSyrkTile, er, ec, acc);
         __syncthreads();
     }
 #pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        const int r = rb + ty + 16 * a;
-#pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            const int c = cb + tx + 16 * b;
-            if (r < nb && c < nb && r >= c) U[(int64_t)c * nb + r] -= acc[a][b];
-        }
-    }
+    for (int q = 0; q < 4; ++q)
+        if (q < ne) U[(int64_t)(cb + ec[q]) * nb + rb + er[q]] -= acc[q];
 }
 
 // Column block jb of X = inv(L11): X_jj = inv(L_jj) and, block row by block
@@ -776,7 +829,7 @@ k_local_step_mixed(int V, const int32_t *__restrict__ drow, const int32_t *__res
     if (!live || l != 0) return;
     float Rm[3][3], spread;
     rotation_from_cov(S, Rm, &spread);
-    if (!(spread >= dev::kPolarFallback)) dev::rotation_fp64(i, drow[i], e1, dcol, w64, p64, pc64, 1, 0, Rm);
+    if (!(spread >= dev::kPolarFallback)) dev::rotation_fp64<true>(i, drow[i], e1, dcol, w64, p64, pc64, 1, 0, Rm);
     R[3 * (int64_t)i + 0] = {Rm[0][0], Rm[0][1], Rm[0][2], 0.f};
     R[3 * (int64_t)i + 1] = {Rm[1][0], Rm[1][1], Rm[1][2], 0.f};
     R[3 * (int64_t)i + 2] = {Rm[2][0], Rm[2][1], Rm[2][2], 0.f};
