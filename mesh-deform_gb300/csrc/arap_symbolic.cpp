@@ -332,6 +332,81 @@ void nd_order(int n, const int32_t *rowptr, const int32_t *col, std::vector<int3
 
 // ---------------------------------------------------------------------------
 
+bool build_solve_blocks(const Symbolic &sym, int max_cols, SolveBlocks &out) {
+    out = SolveBlocks();
+    const int S = sym.S;
+    if (S == 0) return false;
+    SolveBlocks b;
+    b.sn = sym.sn;
+    b.x_size = sym.x_size;
+    b.l21_size = sym.l21_size;
+    b.l21t_size = sym.l21t_size;
+    std::vector<char> absorbed(S, 0);
+    for (int s = 0; s < S; ++s) {
+        const SnInfo &d = sym.sn[s];
+        if (d.level != 1) continue;
+        // the subtree: the leaf children (all leaves, the node being of level
+        // 1), contiguous before the node in the elimination order
+        int first = d.first, cols = d.ncol;
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+            const SnInfo &c = sym.sn[sym.child[ci]];
+            first = std::min(first, (int)c.first);
+            cols += c.ncol;
+        }
+        if (first + cols != d.first + d.ncol || cols > max_cols) return false;
+        b.items.push_back(s);
+        b.items.push_back((int32_t)b.members.size());
+        for (int ci = d.child_begin; ci < d.child_end; ++ci) {
+            b.members.push_back(sym.child[ci]);
+            absorbed[sym.child[ci]] = 1;
+        }
+        b.members.push_back(s);
+        b.items.push_back((int32_t)b.members.size());
+        SnInfo &e = b.sn[s];
+        const int nb = d.nrow - d.ncol;
+        e.first = first;
+        e.ncol = cols;
+        e.nrow = cols + nb;
+        e.child_begin = e.child_end = d.child_begin;  // no children left
+        e.ldx = (cols + 3) & ~3;
+        e.x_off = b.x_size;
+        b.x_size += (int64_t)e.ldx * cols;
+        e.xt_off = b.x_size;
+        b.x_size += (int64_t)e.ldx * cols;
+        e.l21t_off = b.l21t_size;
+        b.l21t_size += (int64_t)e.ldx * nb;
+        e.l21_off = b.l21_size;
+        b.l21_size += (int64_t)e.ld21 * cols;
+        ++b.nblocks;
+    }
+    if (b.nblocks == 0) return false;
+    // levels of the solve tree (children come before parents in the array)
+    int maxlev = 0;
+    for (int s = 0; s < S; ++s) {
+        SnInfo &e = b.sn[s];
+        int lv = 0;
+        for (int ci = e.child_begin; ci < e.child_end; ++ci) lv = std::max(lv, b.sn[sym.child[ci]].level + 1);
+        e.level = lv;
+        if (!absorbed[s]) maxlev = std::max(maxlev, lv);
+    }
+    b.level_ptr.assign(maxlev + 2, 0);
+    for (int s = 0; s < S; ++s)
+        if (!absorbed[s]) b.level_ptr[b.sn[s].level + 1]++;
+    for (int l = 0; l <= maxlev; ++l) b.level_ptr[l + 1] += b.level_ptr[l];
+    b.level_sn.assign(b.level_ptr.back(), 0);
+    std::vector<int32_t> fill(b.level_ptr.begin(), b.level_ptr.end() - 1);
+    for (int s = 0; s < S; ++s)
+        if (!absorbed[s]) b.level_sn[fill[b.sn[s].level]++] = s;
+    for (int s = 0; s < S; ++s) {
+        if (absorbed[s]) continue;
+        b.max_ldx = std::max(b.max_ldx, (int)b.sn[s].ldx);
+        b.max_ld21 = std::max(b.max_ld21, (int)b.sn[s].ld21);
+        b.max_ncol = std::max(b.max_ncol, (int)b.sn[s].ncol);
+    }
+    out = std::move(b);
+    return true;
+}
+
 int64_t symbolic_factor_nnz(Symbolic &sym) {
     if (sym.factor_nnz >= 0) return sym.factor_nnz;
     // row subtrees of the elimination tree: row k of L holds column i < k for

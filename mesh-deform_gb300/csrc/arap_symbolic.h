@@ -141,6 +141,29 @@ struct Symbolic {
 bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
                     std::string &err, bool &singular, bool mesh_order = false);
 
+// Solve-time amalgamation: every supernode of level 1 (whose children are all
+// leaves) is solved together with its leaf children as one block, the subtree's
+// columns being contiguous in the elimination order. A block keeps its node's
+// index, parent, rows below, relative indices and update vector, so the rest of
+// the tree sees no difference; it has no children, ncol = the subtree's
+// columns, a dense X = inv(L) of the subtree and L21 = L(rows below, subtree
+// columns), stored after the supernodes' solve arrays. Every level of the
+// solve tree is then one below the supernodal level (uniform shift). The
+// factorisation keeps the supernodal tree.
+struct SolveBlocks {
+    std::vector<SnInfo> sn;               // S entries: sym.sn with the blocks in place of their nodes
+    std::vector<int32_t> level_ptr;       // solve levels (leaves and blocks = 0)
+    std::vector<int32_t> level_sn;        // scheduled entries by level (absorbed leaves left out)
+    std::vector<int32_t> items;           // per block: node, first member, end member (into members)
+    std::vector<int32_t> members;         // leaf children in order, then the node
+    int64_t x_size = 0, l21_size = 0, l21t_size = 0;  // solve arrays with the blocks
+    int max_ldx = 0, max_ld21 = 0, max_ncol = 0, nblocks = 0;
+};
+
+// Builds the solve blocks; false (and out empty) when the tree has no level-1
+// supernode or a subtree has more than max_cols columns.
+bool build_solve_blocks(const Symbolic &sym, int max_cols, SolveBlocks &out);
+
 // Nonzeros of the scalar Cholesky factor (diagonal included), counted from the
 // elimination tree on first use and kept in sym.factor_nnz.
 int64_t symbolic_factor_nnz(Symbolic &sym);
