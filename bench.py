@@ -815,6 +815,8 @@ def main():
     ap.add_argument("--vertex-launch", default="auto", choices=["auto", "default"],
                     help="threads per vertex and block size of the local step, RHS and residual "
                          "(auto: autotuned per kernel before the timed region)")
+    ap.add_argument("--solve-blocks", type=int, default=512,
+                    help="single-request solves: level-1 subtrees of at most this many columns as one block (0: none)")
     ap.add_argument("--warp-rows", type=int, default=-1,
                     help="single-request solves: fronts of at most this many rows solved one warp per supernode "
                          "(-1: autotuned with the CTA count when requests run concurrently, else 0)")
@@ -893,7 +895,7 @@ def run_requests(args):
             for wr in warps:
                 best, rates = arap_tune.tune_solve_ctas(w.positions, w.faces, w.cidx, w.ctargets, w.iterations,
                                                         args.precision, args.refine, N, device=local, schedule=sch,
-                                                        warp_rows=wr)
+                                                        warp_rows=wr, solve_blocks=args.solve_blocks)
                 key = f"{sch}/warp_rows={wr}"
                 tuned[key] = {"solve_ctas": best, "iterations_per_s": {str(k): round(v, 1) for k, v in rates.items()}}
                 log(f"autotuned solve CTAs for {N} requests in flight, {key}: {best} {tuned[key]}")
@@ -916,6 +918,7 @@ def run_requests(args):
         c.set_solve_ctas(args.solve_ctas)
         c.set_solve_schedule(args.solve_schedule)
         c.set_warp_rows(args.warp_rows)
+        c.set_solve_blocks(args.solve_blocks)
         c.set_rest_positions(w.positions)
         c.set_constraints(w.cidx, w.ctargets)
         ctxs.append(c)
@@ -1108,7 +1111,8 @@ def run_requests(args):
 
     analysis = "kept for the unchanged constraint set" if args.cached_analysis else \
         "redone on every request (ordering, elimination tree, supernodes, plan), as SimplicialLDLT::compute"
-    extra = {"requests_per_step": N, "vertex_launch": vtuned or "1 thread per vertex, 256-thread blocks",
+    extra = {"requests_per_step": N, "solve_blocks": args.solve_blocks,
+             "vertex_launch": vtuned or "1 thread per vertex, 256-thread blocks",
              "solve_schedule": args.solve_schedule, "warp_rows": args.warp_rows,
              "solve_ctas": args.solve_ctas,
              "solve_ctas_autotune": tuned,

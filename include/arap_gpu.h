@@ -225,6 +225,16 @@ int arap_set_warp_rows(arap_ctx *ctx, int32_t rows);
    mesh-deform_gb300/arap_tune.py measures the best shape per kernel. */
 int arap_set_vertex_launch(arap_ctx *ctx, int32_t kernel, int32_t threads_per_vertex, int32_t block_threads);
 
+/* Solve blocks of a single request's triangular sweeps (arap.h:417-429):
+   every supernode of level 1 of the elimination tree is solved together with
+   its leaf children as one task, through the dense inverse of the subtree's
+   diagonal block (formed once per factorisation) and the subtree's rows
+   below, when every such subtree has at most `max_columns` columns (default
+   512; 0: none; at most 1,024). Half the tasks of a sweep and one level less on its chain,
+   for more bytes per task. Results equal up to the order of sums. Takes
+   effect at the next deform (which analyses the problem again). */
+int arap_set_solve_blocks(arap_ctx *ctx, int32_t max_columns);
+
 #define ARAP_SOLVE_PERSISTENT 0
 #define ARAP_SOLVE_LEVELS 1
 int arap_set_solve_schedule(arap_ctx *ctx, int32_t schedule);

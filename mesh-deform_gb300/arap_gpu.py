@@ -116,6 +116,7 @@ SIGNATURES = {
     "arap_set_dense_top": (C.c_int, [_P, _I32]),
     "arap_set_warp_rows": (C.c_int, [_P, _I32]),
     "arap_set_solve_schedule": (C.c_int, [_P, _I32]),
+    "arap_set_solve_blocks": (C.c_int, [_P, _I32]),
     "arap_set_vertex_launch": (C.c_int, [_P, _I32, _I32, _I32]),
     "arap_set_ordering": (C.c_int, [_P, _I32]),
     "arap_set_done_callback": (C.c_int, [_P, _P, _P]),
@@ -342,6 +343,11 @@ class ArapContext:
         """Launch shape of 'local', 'rhs' or 'residual' (or an ARAP_K_* code)."""
         code = {"local": ARAP_K_LOCAL, "rhs": ARAP_K_RHS, "residual": ARAP_K_RESIDUAL}.get(kernel, kernel)
         self._check(self.lib.arap_set_vertex_launch(self.h, int(code), int(threads_per_vertex), int(block_threads)))
+
+    def set_solve_blocks(self, max_columns: int):
+        """Largest level-1 subtree (columns) solved as one block by the
+        single-request sweeps (0: none)."""
+        self._check(self.lib.arap_set_solve_blocks(self.h, int(max_columns)))
 
     def set_solve_schedule(self, schedule):
         """'persistent' (one launch of persistent CTAs per sweep) or 'levels'

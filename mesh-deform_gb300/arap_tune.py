@@ -35,11 +35,12 @@ def _key(device: int, V: int, n_constrained: int, precision: str, concurrency: i
 def tune_solve_ctas(positions, faces, cidx, ctargets, iterations: int, precision: str = "mixed",
                     refine: int = 1, concurrency: int = 1, device: int = 0, candidates=CANDIDATES,
                     trials: int = 2, cache_file: str | Path | None = None, schedule: str = "persistent",
-                    warp_rows: int = 0):
+                    warp_rows: int = 0, solve_blocks: int = 0):
     """Returns (best_count, {count: iterations/s}) for `concurrency` concurrent
     dirty deforms of the given problem under the given solve schedule
     ('persistent' or 'levels', arap_set_solve_schedule)."""
-    key = _key(device, len(positions), len(cidx), precision, concurrency, iterations, f"{schedule}:w{warp_rows}")
+    key = _key(device, len(positions), len(cidx), precision, concurrency, iterations,
+               f"{schedule}:w{warp_rows}:b{solve_blocks}")
     if cache_file and Path(cache_file).exists():
         try:
             _cache.update(json.loads(Path(cache_file).read_text()))
@@ -55,6 +56,7 @@ def tune_solve_ctas(positions, faces, cidx, ctargets, iterations: int, precision
         c.set_precision(precision, refine)
         c.set_solve_schedule(schedule)
         c.set_warp_rows(warp_rows)
+        c.set_solve_blocks(solve_blocks)
         c.set_rest_positions(positions)
         c.set_constraints(cidx, ctargets)
         ctxs.append(c)

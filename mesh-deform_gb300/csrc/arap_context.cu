@@ -29,6 +29,11 @@ namespace {
 constexpr int kTickets = kLevelTicket0 + 2 * kMaxLevelLaunch;
 // schedule of the single-CTA solve levels (arap_set_solve_schedule)
 constexpr int kSolveScheduleDefault = ARAP_SOLVE_PERSISTENT;
+// largest subtree (columns) of a level-1 supernode solved as one block by the
+// single-request sweeps (arap_set_solve_blocks; 0: none). Measured on the
+// twisted bar: iterations of one request 13.3 -> 9.7 ms, 16 requests in flight
+// 91 -> 86 ms per step.
+constexpr int kSolveBlocksDefault = 512;
 // fronts of at most this many rows at the bottom of the tree are solved one
 // warp per supernode (arap_set_warp_rows; 0: none)
 constexpr int kWarpRowsDefault = 0;
@@ -175,6 +180,11 @@ struct arap_ctx {
     int dense_cols = 0;  // most columns of the dense top of the tree (0: default, <0: none)
     int warp_rows = kWarpRowsDefault;  // largest front of the warp-per-supernode solves (0: none)
     int solve_schedule = kSolveScheduleDefault;  // ARAP_SOLVE_PERSISTENT or ARAP_SOLVE_LEVELS
+    int solve_blocks = kSolveBlocksDefault;      // largest solve block (columns), 0: none
+    SolveBlocks sb;                              // the blocks of the current analysis (use_sb)
+    bool use_sb = false;
+    DevSym dss;                                  // the single-request sweeps' layout with the blocks
+    DevBuf ssn, slevel_sn, sbitems, sbmembers;
     // launch shape of the local step, RHS and residual (arap_set_vertex_launch)
     VertexLaunch vlaunch[kVertexKernels] = {{1, 256}, {1, 256}, {1, 256}};
     size_t dense_inv_smem[2] = {0, 0}, dense_vec_smem[2] = {0, 0};  // configured limits (FP32, FP64)
@@ -212,7 +222,7 @@ struct arap_ctx {
                 &vnorm, &btargets, &bpc64, &bpc32, &bR, &bbfixed, &bb, &bsol, &buvec, &bout, &bftop, &bytop, &bws,
                 &batile,
                 &bticket, &bflags, &top_col, &top_gptr, &top_gidx, &tdpos, &top_items, &Ttop, &ytop, &Lval32,
-                &Dinv32};
+                &Dinv32, &ssn, &slevel_sn, &sbitems, &sbmembers};
     }
 };
 
@@ -290,6 +300,8 @@ int analyze_symbolic(arap_ctx *ctx) {
     bool singular = false;
     if (!build_symbolic(ctx->topo, ctx->cmask, ctx->sym, err, singular, ctx->ordering == ARAP_ORDER_MESH))
         return fail(ctx, singular ? ARAP_ERR_NOT_SPD : ARAP_ERR_CUDA, err);
+    ctx->use_sb = ctx->solve_blocks > 0 && build_solve_blocks(ctx->sym, ctx->solve_blocks, ctx->sb);
+    if (!ctx->use_sb) ctx->sb = SolveBlocks();
     ctx->sym_host = true;
     return ARAP_OK;
 }
@@ -371,9 +383,12 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     add(ctx->Lval, (size_t)std::max<int64_t>(s.panel_size, 1) * fs);
     add(ctx->Dinv, (size_t)std::max<int64_t>(s.dinv_size, 1) * fs);
     add(ctx->Upd, (size_t)std::max<int64_t>(s.upd_size, 1) * fs);
-    add(ctx->Xinv, (size_t)std::max<int64_t>(s.x_size, 1) * sizeof(T));
-    add(ctx->L21, (size_t)std::max<int64_t>(s.l21_size, 1) * sizeof(T));
-    add(ctx->L21T, (size_t)std::max<int64_t>(s.l21t_size, 1) * sizeof(T));
+    // the solve arrays, with the solve blocks after the supernodes' own
+    const int64_t xs = ctx->use_sb ? ctx->sb.x_size : s.x_size, l21s = ctx->use_sb ? ctx->sb.l21_size : s.l21_size,
+                  l21ts = ctx->use_sb ? ctx->sb.l21t_size : s.l21t_size;
+    add(ctx->Xinv, (size_t)std::max<int64_t>(xs, 1) * sizeof(T));
+    add(ctx->L21, (size_t)std::max<int64_t>(l21s, 1) * sizeof(T));
+    add(ctx->L21T, (size_t)std::max<int64_t>(l21ts, 1) * sizeof(T));
     const int nt = choose_dense_top(s, dense_cap(ctx)).ncols;
     add(ctx->Ttop, std::max<size_t>(nt > 0 ? dense_top_elems(nt) : 0, 1) * sizeof(T));
     if (f64f) {
@@ -456,6 +471,88 @@ int prepare_dense_top(arap_ctx *ctx, int level, int n) {
     CK(upload(ctx->top_items, items, st));
     d.n_top = n;
     d.n_top_items = (int)items.size() / 2;
+    return ARAP_OK;
+}
+
+// The single-request sweeps' layout with the solve blocks (SolveBlocks): the
+// supernodal layout ds with the blocks' array and solve levels. Every level of
+// the solve tree is one below the supernodal level, so the top's split moves
+// down by one; the blocks need the top to start at supernodal level 2 or
+// above (else they are not used).
+int prepare_solve_blocks(arap_ctx *ctx) {
+    const SolveBlocks &b = ctx->sb;
+    const DevSym &f = ctx->ds;
+    cudaStream_t st = ctx->stream;
+    if (f.ltop < 2) {
+        ctx->use_sb = false;
+        return ARAP_OK;
+    }
+    CK(upload(ctx->ssn, b.sn, st));
+    CK(upload(ctx->slevel_sn, b.level_sn, st));
+    CK(upload(ctx->sbitems, b.items, st));
+    CK(upload(ctx->sbmembers, b.members, st));
+    DevSym d = f;
+    d.sn = ctx->ssn.as<SnInfo>();
+    d.level_sn = ctx->slevel_sn.as<int32_t>();
+    const int nlev = (int)b.level_ptr.size() - 1;
+    d.ltop = f.ltop - 1;
+    d.s_low = b.level_ptr[d.ltop];
+    d.max_ldx = std::max(f.max_ldx, b.max_ldx);
+    d.max_ld21 = std::max(f.max_ld21, b.max_ld21);
+    d.max_ncol = std::max(f.max_ncol, b.max_ncol);
+    const size_t b32 = solve_smem_bytes(d.max_ldx, d.max_ld21, 4), b64 = solve_smem_bytes(d.max_ldx, d.max_ld21, 8);
+    constexpr size_t kSmemMax = 227 * 1024;
+    if (b32 > kSmemMax || (ctx->fp64_solves && b64 > kSmemMax)) {
+        ctx->use_sb = false;
+        return ARAP_OK;
+    }
+    if (b32 > ctx->smem_f32 || (ctx->fp64_solves && b64 > ctx->smem_f64)) {
+        CK(configure_solve_smem((int)b32, ctx->fp64_solves ? (int)b64 : 0));
+        ctx->smem_f32 = std::max(ctx->smem_f32, b32);
+        if (ctx->fp64_solves) ctx->smem_f64 = std::max(ctx->smem_f64, b64);
+    }
+    // warp-per-supernode levels at the bottom of the solve tree
+    int lwarp = 0;
+    const int wrows = std::min(ctx->warp_rows, wsolve_max_rows());
+    while (wrows > 0 && lwarp < d.ltop) {
+        int mx = 0;
+        for (int q = b.level_ptr[lwarp]; q < b.level_ptr[lwarp + 1]; ++q) mx = std::max(mx, (int)b.sn[b.level_sn[q]].nrow);
+        if (mx > wrows) break;
+        ++lwarp;
+    }
+    d.lwarp = lwarp;
+    d.s_warp = b.level_ptr[lwarp];
+    const int cap = ctx->solve_cap;
+    if (d.s_warp > 0) {
+        CK(configure_wsolve());
+        const int need = (d.s_warp + 7) / 8;
+        const int r32 = wsolve_resident_ctas(4), r64 = wsolve_resident_ctas(8);
+        d.wgrid32 = std::max(1, std::min(need, cap > 0 ? std::min(cap, r32) : r32));
+        d.wgrid64 = std::max(1, std::min(need, cap > 0 ? std::min(cap, r64) : r64));
+    }
+    d.s_top = f.n_top > 0 ? 0 : b.level_ptr[nlev] - d.s_low;
+    const int res32 = solve_resident_ctas((int)b32, 4), res64 = solve_resident_ctas((int)b64, 8);
+    const int nl = std::max(d.s_low - d.s_warp, 1);
+    d.solve_grid32 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res32) : res32));
+    d.solve_grid64 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res64) : res64));
+    d.level_launch = ctx->solve_schedule == ARAP_SOLVE_LEVELS && nlev <= kMaxLevelLaunch;
+    for (int l = 0; l <= kMaxLevelLaunch; ++l) d.lev_ptr[l] = nlev > 0 ? b.level_ptr[std::min(l, nlev)] : 0;
+    for (int l = 0; l < kMaxLevelLaunch; ++l) {
+        int lx = 0, l21 = 0;
+        for (int q = d.lev_ptr[l]; q < d.lev_ptr[l + 1]; ++q) {
+            const SnInfo &x = b.sn[b.level_sn[q]];
+            lx = std::max(lx, (int)x.ldx);
+            l21 = std::max(l21, (int)x.ld21);
+        }
+        d.lev_ldx[l] = lx;
+        d.lev_ld21[l] = l21;
+        const int n = std::max(d.lev_ptr[l + 1] - d.lev_ptr[l], 1);
+        const int r32 = solve_resident_ctas((int)solve_smem_bytes(lx, l21, 4), 4);
+        const int r64 = solve_resident_ctas((int)solve_smem_bytes(lx, l21, 8), 8);
+        d.lev_grid32[l] = std::max(1, std::min(n, cap > 0 ? std::min(cap, r32) : r32));
+        d.lev_grid64[l] = std::max(1, std::min(n, cap > 0 ? std::min(cap, r64) : r64));
+    }
+    ctx->dss = d;
     return ARAP_OK;
 }
 
@@ -643,6 +740,10 @@ int prepare_symbolic(arap_ctx *ctx) {
     d.top_gidx = ctx->top_gidx.as<int64_t>();
     d.tdpos = ctx->tdpos.as<int32_t>();
     d.top_items = ctx->top_items.as<int32_t>();
+    if (ctx->use_sb) {
+        const int rc_b = prepare_solve_blocks(ctx);
+        if (rc_b != ARAP_OK) return rc_b;
+    }
     ctx->sym_valid = true;
     return ARAP_OK;
 }
@@ -703,11 +804,18 @@ int factor_inverses(arap_ctx *ctx, const TI *Lval, const TI *Dinv, TI *X, TI *L2
     CK(cudaMemsetAsync(X, 0, (size_t)s.x_size * sizeof(TI), st));
     if (s.l21_size > 0) CK(cudaMemsetAsync(L21, 0, (size_t)s.l21_size * sizeof(TI), st));
     if (s.l21t_size > 0) CK(cudaMemsetAsync(L21T, 0, (size_t)s.l21t_size * sizeof(TI), st));
+    // (the solve blocks' arrays after them are written whole by their kernel)
     for (const FactorLaunch &fl : s.fplan) {
         if (fl.kind != kFx) continue;
         Prof pr(ctx, ARAP_K_FACTOR);
         launch_factor_step<TI>(d, fl, ctx->fitems.as<FItem>(), const_cast<TI *>(Lval), nullptr, const_cast<TI *>(Dinv),
                                X, L21, L21T, ctx->errw.as<int>(), st);
+        ctx->launches += 1;
+    }
+    if (ctx->use_sb) {
+        Prof pr(ctx, ARAP_K_FACTOR);
+        launch_solve_blocks<TI>(ctx->sb.nblocks, ctx->sbitems.as<int32_t>(), ctx->sbmembers.as<int32_t>(), d.sn,
+                                ctx->ssn.as<SnInfo>(), d.relind, Lval, X, L21, L21T, st);
         ctx->launches += 1;
     }
     if (d.n_top > 0) {
@@ -863,6 +971,7 @@ template <>
 int run_iterations<double>(arap_ctx *ctx, int iterations) {
     const Symbolic &s = ctx->sym;
     const DevSym &d = ctx->ds;
+    const DevSym &dv = ctx->use_sb ? ctx->dss : d;  // the sweeps' layout (with the solve blocks)
     cudaStream_t st = ctx->stream;
     unsigned long long *tk = ctx->ticket.as<unsigned long long>();
     unsigned *fl = ctx->flags.as<unsigned>();
@@ -881,18 +990,18 @@ int run_iterations<double>(arap_ctx *ctx, int iterations) {
         }
         {
             Prof pr(ctx, ARAP_K_SOLVE_FWD);
-            launch_solve_fwd<double>(d, ctx->Xinv.as<double>(), ctx->L21.as<double>(),
+            launch_solve_fwd<double>(dv, ctx->Xinv.as<double>(), ctx->L21.as<double>(),
                                      ctx->sol.as<Vec4<double>>(), ctx->uvec.as<Vec4<double>>(), tk, fl,
                                      ctx->errw.as<int>(), st, ctx->Ttop.as<double>(), ctx->ytop.as<Vec4<double>>());
         }
         {
             Prof pr(ctx, ARAP_K_SOLVE_BWD);
-            launch_solve_bwd<double>(d, ctx->Xinv.as<double>(), ctx->L21T.as<double>(),
+            launch_solve_bwd<double>(dv, ctx->Xinv.as<double>(), ctx->L21T.as<double>(),
                                      ctx->sol.as<Vec4<double>>(), ctx->pc64.as<Vec4<double>>(), nullptr, 0, tk + 1,
                                      fl + s.S, ctx->errw.as<int>(), st, ctx->Ttop.as<double>(),
                                      ctx->ytop.as<Vec4<double>>());
         }
-        ctx->launches += solve_launches(d) + 1;
+        ctx->launches += solve_launches(dv) + 1;
     }
     CK(cudaGetLastError());
     return ARAP_OK;
@@ -902,6 +1011,7 @@ template <>
 int run_iterations<float>(arap_ctx *ctx, int iterations) {
     const Symbolic &s = ctx->sym;
     const DevSym &d = ctx->ds;
+    const DevSym &dv = ctx->use_sb ? ctx->dss : d;  // the sweeps' layout (with the solve blocks)
     cudaStream_t st = ctx->stream;
     unsigned long long *tk = ctx->ticket.as<unsigned long long>();
     unsigned *fl = ctx->flags.as<unsigned>();
@@ -928,18 +1038,18 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_FWD);
-                launch_solve_fwd<float>(d, ctx->Xinv.as<float>(), ctx->L21.as<float>(),
+                launch_solve_fwd<float>(dv, ctx->Xinv.as<float>(), ctx->L21.as<float>(),
                                         ctx->sol.as<Vec4<float>>(), ctx->uvec.as<Vec4<float>>(), tk, fl,
                                         ctx->errw.as<int>(), st, ctx->Ttop.as<float>(), ctx->ytop.as<Vec4<float>>());
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_BWD);
-                launch_solve_bwd<float>(d, ctx->Xinv.as<float>(), ctx->L21T.as<float>(),
+                launch_solve_bwd<float>(dv, ctx->Xinv.as<float>(), ctx->L21T.as<float>(),
                                         ctx->sol.as<Vec4<float>>(), ctx->pc64.as<Vec4<double>>(),
                                         ctx->pc32.as<Vec4<float>>(), 1, tk + 1, fl + s.S, ctx->errw.as<int>(), st,
                                         ctx->Ttop.as<float>(), ctx->ytop.as<Vec4<float>>());
             }
-            ctx->launches += solve_launches(d) + 1;
+            ctx->launches += solve_launches(dv) + 1;
         }
     }
     CK(cudaGetLastError());
@@ -1151,6 +1261,7 @@ int arap_create_like(const arap_ctx *src, arap_ctx **out) {
     ctx->dense_cols = src->dense_cols;
     ctx->warp_rows = src->warp_rows;
     ctx->solve_schedule = src->solve_schedule;
+    ctx->solve_blocks = src->solve_blocks;
     for (int k = 0; k < kVertexKernels; ++k) ctx->vlaunch[k] = src->vlaunch[k];
     ctx->ordering = src->ordering;
     return finish_create(ctx, src->device, src, out);
@@ -1758,6 +1869,22 @@ int arap_set_vertex_launch(arap_ctx *ctx, int32_t kernel, int32_t threads_per_ve
     return ARAP_OK;
 }
 
+int arap_set_solve_blocks(arap_ctx *ctx, int32_t max_columns) {
+    if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
+    if (max_columns < 0 || max_columns > kMaxSolveBlock)
+        return fail(ctx, ARAP_ERR_INVALID_ARGUMENT, "solve block columns out of range (0..1024)");
+    if (ctx->in_flight) {
+        const int rc_ = arap_wait(ctx);
+        if (rc_ != ARAP_OK) return rc_;
+    }
+    if (max_columns != ctx->solve_blocks) {
+        ctx->solve_blocks = max_columns;
+        ctx->sym_host = ctx->sym_valid = false;  // the analysis decides the blocks
+        ctx->dirty = true;
+    }
+    return ARAP_OK;
+}
+
 int arap_set_solve_schedule(arap_ctx *ctx, int32_t schedule) {
     if (check_ctx(ctx)) return ARAP_ERR_INVALID_ARGUMENT;
     if (schedule != ARAP_SOLVE_PERSISTENT && schedule != ARAP_SOLVE_LEVELS)
@@ -2106,10 +2233,16 @@ int arap_get_kernel_model(arap_ctx *ctx, int32_t kernel_class, double *bytes, do
     // per solve sweep: the lower triangle of X = inv(L11) and L21, once each
     // (the levels below the dense top, where there is one: the _lo sums)
     double xlow = 0.0, l21 = 0.0, xlow_lo = 0.0, l21_lo = 0.0, nbsum_lo = 0.0;
-    for (const SnInfo &d : s.sn) {
+    // the supernodes (or, with solve blocks, the blocks and the supernodes
+    // above them) the single-request sweeps read
+    const std::vector<int32_t> &sched = ctx->use_sb ? ctx->sb.level_sn : s.level_sn;
+    const std::vector<SnInfo> &snv = ctx->use_sb ? ctx->sb.sn : s.sn;
+    const int ltop_m = ctx->use_sb ? ctx->dss.ltop : ctx->ds.ltop;
+    for (const int32_t q : sched) {
+        const SnInfo &d = snv[q];
         xlow += (double)d.ncol * (d.ncol + 1) / 2;
         l21 += (double)(d.nrow - d.ncol) * d.ncol;
-        if (ctx->ds.n_top == 0 || d.level < ctx->ds.ltop) {
+        if (ctx->ds.n_top == 0 || d.level < ltop_m) {
             xlow_lo += (double)d.ncol * (d.ncol + 1) / 2;
             l21_lo += (double)(d.nrow - d.ncol) * d.ncol;
             nbsum_lo += d.nrow - d.ncol;

@@ -638,6 +638,109 @@ k_fsyrk(const FItem *__restrict__ items, const SnInfo *__restrict__ sn, const TF
         if (q < ne) U[(int64_t)(cb + ec[q]) * nb + rb + er[q]] -= acc[q];
 }
 
+// Solve block of a level-1 supernode s and its leaf children (SolveBlocks):
+// X_b = inv(L_bb) of the subtree and L21_b = L(rows below s, subtree columns),
+// with their transposes, from the supernodes' inverses (k_fx) and panels. With
+// leaves l_i (columns at o_i) and s (at o_s), L_bb has the leaves' diagonal
+// blocks, s's diagonal block and A_i = L(s columns, l_i columns), so X_b has
+// X_{l_i} and X_s on its diagonal, -X_s A_i X_{l_i} below them and zeros
+// elsewhere (written too: the sweeps stream whole columns). One CTA per block;
+// the products are small (s has a few dozen columns), staged in shared memory
+// kBlkRows rows at a time.
+constexpr int kBlkCols = 64;  // leaf columns per pass of the products
+template <typename TF>
+__global__ void __launch_bounds__(kFactorThreads)
+k_fx_block(const int32_t *__restrict__ items, const int32_t *__restrict__ members, const SnInfo *__restrict__ sn,
+           const SnInfo *__restrict__ bsn, const int32_t *__restrict__ relind, const TF *__restrict__ Lval,
+           TF *__restrict__ X, TF *__restrict__ L21, TF *__restrict__ L21T) {
+    __shared__ TF Ms[kBlkCols][kBlkCols + 1];  // M = A X_l for up to 64 rows of s x 64 leaf columns
+    __shared__ int tmap[kMaxSolveBlock];        // per column of s: the leaf's row below landing there (-1: none)
+    const int node = items[3 * blockIdx.x], mb = items[3 * blockIdx.x + 1], me = items[3 * blockIdx.x + 2];
+    const SnInfo ns = sn[node], b = bsn[node];
+    const int nb = ns.nrow - ns.ncol, nbk = b.ncol, ldb = b.ldx, ld21 = b.ld21;
+    const int os = ns.first - b.first;
+    TF *Xb = X + b.x_off, *XbT = X + b.xt_off, *Lb = L21 + b.l21_off, *LbT = L21T + b.l21t_off;
+    const int tid = threadIdx.x;
+    // zeros, then the diagonal blocks and s's rows below
+    for (int64_t q = tid; q < (int64_t)ldb * nbk; q += kFactorThreads) Xb[q] = (TF)0;
+    for (int64_t q = tid; q < (int64_t)ld21 * nbk; q += kFactorThreads) Lb[q] = (TF)0;
+    __syncthreads();
+    for (int m = mb; m < me; ++m) {
+        const SnInfo d = sn[members[m]];
+        const int o = d.first - b.first;
+        const TF *Xd = X + d.x_off;
+        for (int q = tid; q < d.ncol * d.ncol; q += kFactorThreads) {
+            const int r = q % d.ncol, c = q / d.ncol;
+            if (r >= c) Xb[(int64_t)(o + c) * ldb + o + r] = Xd[(int64_t)c * d.ldx + r];
+        }
+    }
+    {
+        const TF *P = Lval + ns.panel_off;
+        for (int q = tid; q < nb * ns.ncol; q += kFactorThreads) {
+            const int r = q % nb, c = q / nb;
+            Lb[(int64_t)(os + c) * ld21 + r] = P[(int64_t)c * ns.nrow + ns.ncol + r];
+        }
+    }
+    __syncthreads();
+    // per leaf: its rows below go to s's columns (A_i) or below s (L21_b)
+    const TF *Xs = X + ns.x_off;
+    for (int m = mb; m < me - 1; ++m) {
+        const SnInfo d = sn[members[m]];
+        const int o = d.first - b.first, nbl = d.nrow - d.ncol;
+        const TF *P = Lval + d.panel_off;
+        const int32_t *ri = relind + d.relind_off;
+        for (int q = tid; q < nbl * d.ncol; q += kFactorThreads) {
+            const int t = q % nbl, c = q / nbl, pos = ri[t];
+            if (pos >= ns.ncol) Lb[(int64_t)(o + c) * ld21 + pos - ns.ncol] = P[(int64_t)c * d.nrow + d.ncol + t];
+        }
+        for (int k = tid; k < ns.ncol; k += kFactorThreads) tmap[k] = -1;
+        __syncthreads();
+        for (int t = tid; t < nbl; t += kFactorThreads)
+            if (ri[t] < ns.ncol) tmap[ri[t]] = t;
+        __syncthreads();
+        // X_b(s rows, leaf columns) = -X_s (A_i X_l), in tiles of kBlkCols
+        // rows of s x kBlkCols leaf columns
+        for (int r0 = 0; r0 < ns.ncol; r0 += kBlkCols)
+            for (int c0 = 0; c0 < d.ncol; c0 += kBlkCols) {
+                const int rn = min(kBlkCols, ns.ncol - r0), cn = min(kBlkCols, d.ncol - c0);
+                // M(r, c) = sum_t A(r0 + r, t) X_l(t, c0 + c), A(k, t) = the leaf's row
+                // below that lands on s's column k
+                for (int q = tid; q < kBlkCols * kBlkCols; q += kFactorThreads) Ms[q / kBlkCols][q % kBlkCols] = (TF)0;
+                __syncthreads();
+                for (int q = tid; q < rn * cn; q += kFactorThreads) {
+                    const int r = q % rn, c = q / rn, t = tmap[r0 + r];
+                    TF acc = (TF)0;
+                    if (t >= 0) {
+                        // row t of the leaf's rows below, times column c0 + c of X_l (rows k >= c0 + c)
+                        const TF *Pt = P + d.ncol + t;
+                        for (int k = c0 + c; k < d.ncol; ++k)
+                            acc += Pt[(int64_t)k * d.nrow] * X[d.x_off + (int64_t)(c0 + c) * d.ldx + k];
+                    }
+                    Ms[r][c] = acc;
+                }
+                __syncthreads();
+                // rows r0.. of -X_s M: X_s(i, k) for k <= i
+                for (int q = tid; q < ns.ncol * cn; q += kFactorThreads) {
+                    const int i = q % ns.ncol, c = q / ns.ncol;
+                    TF acc = (TF)0;
+                    for (int k = r0; k < r0 + rn && k <= i; ++k) acc += Xs[(int64_t)k * ns.ldx + i] * Ms[k - r0][c];
+                    Xb[(int64_t)(o + c0 + c) * ldb + os + i] -= acc;
+                }
+                __syncthreads();
+            }
+    }
+    __syncthreads();
+    // transposes: X^T (nbk columns of ldb rows) and L21^T (nb columns of ldb rows)
+    for (int64_t q = tid; q < (int64_t)ldb * nbk; q += kFactorThreads) {
+        const int r = (int)(q % ldb), c = (int)(q / ldb);  // XbT(r, c) = Xb(c, r)
+        XbT[q] = (r < nbk && c < nbk) ? Xb[(int64_t)r * ldb + c] : (TF)0;
+    }
+    for (int64_t q = tid; q < (int64_t)ldb * nb; q += kFactorThreads) {
+        const int r = (int)(q % ldb), c = (int)(q / ldb);  // LbT(r, c) = Lb(c, r)
+        LbT[q] = r < nbk ? Lb[(int64_t)r * ld21 + c] : (TF)0;
+    }
+}
+
 // Column block jb of X = inv(L11): X_jj = inv(L_jj) and, block row by block
 // row, X_ij = -inv(L_ii) sum_{k=j..i-1} L_ik X_kj. Each block row is written
 // to X (and X^T) as soon as it is known; later block rows read the rows above
@@ -2334,6 +2437,18 @@ void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *it
     case kFx: k_fx<TF><<<fl.count, kFactorThreads, 0, st>>>(it, s.sn, Lval, Dinv, X, L21, L21T); break;
     }
 }
+
+template <typename TF>
+void launch_solve_blocks(int nblocks, const int32_t *items, const int32_t *members, const SnInfo *sn,
+                         const SnInfo *bsn, const int32_t *relind, const TF *Lval, TF *X, TF *L21, TF *L21T,
+                         cudaStream_t st) {
+    if (nblocks > 0)
+        k_fx_block<TF><<<nblocks, kFactorThreads, 0, st>>>(items, members, sn, bsn, relind, Lval, X, L21, L21T);
+}
+template void launch_solve_blocks<float>(int, const int32_t *, const int32_t *, const SnInfo *, const SnInfo *,
+                                         const int32_t *, const float *, float *, float *, float *, cudaStream_t);
+template void launch_solve_blocks<double>(int, const int32_t *, const int32_t *, const SnInfo *, const SnInfo *,
+                                          const int32_t *, const double *, double *, double *, double *, cudaStream_t);
 
 template <typename T>
 void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *pc, Vec4<T> *R,

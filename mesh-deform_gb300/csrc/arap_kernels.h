@@ -138,6 +138,15 @@ void launch_rhs_mixed(const DevSym &s, const float *w32, const Vec4<float> *redg
 template <typename TF>
 void launch_factor_step(const DevSym &s, const FactorLaunch &fl, const FItem *items, TF *Lval, TF *Upd, TF *Dinv,
                         TF *X, TF *L21, TF *L21T, int *err, cudaStream_t st);
+// largest solve block (columns; arap_set_solve_blocks)
+constexpr int kMaxSolveBlock = 1024;
+// the solve blocks (SolveBlocks: a level-1 supernode with its leaf children)
+// from the supernodes' inverses X (k_fx) and the panels: X_b, X_b^T, L21_b,
+// L21_b^T at the blocks' offsets of the same arrays (bsn: the solve array)
+template <typename TF>
+void launch_solve_blocks(int nblocks, const int32_t *items, const int32_t *members, const SnInfo *sn,
+                         const SnInfo *bsn, const int32_t *relind, const TF *Lval, TF *X, TF *L21, TF *L21T,
+                         cudaStream_t st);
 // FP64 factor outputs (X, L21, L21^T, the dense top's T) rounded to the FP32
 // copies the mixed form's solves read: count <= 4 arrays of n[a] elements
 void launch_demote(int count, const double *const *src, float *const *dst, const int64_t *n, cudaStream_t st);

@@ -219,3 +219,43 @@ def test_vertex_launch_shapes_match(gpu):
             ctx.set_vertex_launch("local", 3, 256)
         with pytest.raises(gpu.ArapError):
             ctx.set_vertex_launch("local", 1, 512)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-6)])
+@pytest.mark.parametrize("workload", ["bar", "sphere", "l4"])
+def test_solve_blocks_match_supernodal_sweeps(gpu, precision, tol, workload):
+    """Level-1 subtrees solved as blocks (arap_set_solve_blocks) through the
+    dense inverse of their diagonal block give the supernodal sweeps' positions
+    up to the order of sums, and the oracle's within the form's tolerance; with
+    and without the dense top and warp solves, repeated calls bit for bit."""
+    from oracle import oracle as O
+
+    w = {"bar": lambda: W.cfg_twisted_bar(h=0.05, iterations=8),
+         "sphere": lambda: W.cfg_noisy_sphere(level=5, iterations=8),
+         "l4": lambda: W.cfg_icosphere_l4(level=4, iterations=8)}[workload]()
+    ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, w.iterations)
+    assert ok
+    for dense, warp in ((0, 0), (-1, 0), (0, 256)):
+        outs = []
+        for blocks in (0, 512):
+            with gpu.ArapContext(w.V, w.faces) as ctx:
+                ctx.set_precision(precision, 1)
+                ctx.set_dense_top(dense)
+                ctx.set_warp_rows(warp)
+                ctx.set_solve_blocks(blocks)
+                ctx.set_rest_positions(w.positions)
+                ctx.set_constraints(w.cidx, w.ctargets)
+                out = ctx.deform(w.iterations)
+                ctx.invalidate()
+                np.testing.assert_array_equal(ctx.deform(w.iterations), out)
+            outs.append(out)
+            assert W.bbox_rel_error(out, ref, w.positions) <= (1e-10 if precision == "fp64" else 1e-6)
+        assert W.bbox_rel_error(outs[1], outs[0], w.positions) <= tol
+
+
+def test_solve_blocks_reject_negative(gpu):
+    w = W.cfg_icosphere_l4(level=2, iterations=1)
+    with gpu.ArapContext(w.V, w.faces) as ctx:
+        with pytest.raises(gpu.ArapError) as e:
+            ctx.set_solve_blocks(-1)
+        assert e.value.code == gpu.ARAP_ERR_INVALID_ARGUMENT
