@@ -701,7 +701,7 @@ void launch_btop_pack(const DevSym &s, const float *Ttop, float *atiles, cudaStr
         n, ldt, Ttop + (size_t)ldt * n, atiles + (size_t)btop::stages_before(false, n, nrt) * btop::kATileFloats);
 }
 
-int batch_tasks(const DevSym &s) { return s.n_top > 0 ? s.s_low : s.S; }
+int batch_tasks(const DevSym &s) { return s.n_top > 0 ? s.s_low : s.s_sched; }
 
 int batch_top_launches(const DevSym &s) { return s.n_top > 0 ? 5 : 0; }
 

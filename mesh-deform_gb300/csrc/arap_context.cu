@@ -398,7 +398,8 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
     add(ctx->ytop, std::max<size_t>(2 * (size_t)dense_ld(nt), 1) * sizeof(Vec4<T>));  // y_top, then f_top
     if (n_poses > 0) {
         const size_t P = (size_t)n_poses, VP = V * P, MP = m1 * P, nc = V - (size_t)s.m;
-        const int pt = std::max(batch_pose_tile(s.max_ldx, s.max_ld21), 1);
+        const int pt = std::max(batch_pose_tile(ctx->use_sb ? std::max(s.max_ldx, ctx->sb.max_ldx) : s.max_ldx,
+                                                ctx->use_sb ? std::max(s.max_ld21, ctx->sb.max_ld21) : s.max_ld21), 1);
         const size_t T_ = (P + pt - 1) / pt;
         add(ctx->bpc64, VP * sizeof(Vec4<double>));
         add(ctx->bpc32, VP * sizeof(Vec4<float>));
@@ -530,6 +531,7 @@ int prepare_solve_blocks(arap_ctx *ctx) {
         d.wgrid32 = std::max(1, std::min(need, cap > 0 ? std::min(cap, r32) : r32));
         d.wgrid64 = std::max(1, std::min(need, cap > 0 ? std::min(cap, r64) : r64));
     }
+    d.s_sched = b.level_ptr[nlev];  // the absorbed leaves are not scheduled
     d.s_top = f.n_top > 0 ? 0 : b.level_ptr[nlev] - d.s_low;
     const int res32 = solve_resident_ctas((int)b32, 4), res64 = solve_resident_ctas((int)b64, 8);
     const int nl = std::max(d.s_low - d.s_warp, 1);
@@ -719,6 +721,7 @@ int prepare_symbolic(arap_ctx *ctx) {
     d.V = s.V;
     d.m = s.m;
     d.S = s.S;
+    d.s_sched = s.S;
     for (int k = 0; k < kVertexKernels; ++k) d.vlaunch[k] = ctx->vlaunch[k];
     d.nnz = (int)s.dcol.size();
     d.max_ldx = s.max_ldx;
@@ -1062,6 +1065,7 @@ int run_iterations<float>(arap_ctx *ctx, int iterations) {
 int run_batch_iterations(arap_ctx *ctx, int P, int iterations) {
     const Symbolic &s = ctx->sym;
     const DevSym &d = ctx->ds;
+    const DevSym &dv = ctx->use_sb ? ctx->dss : d;  // the batched sweeps' layout (with the solve blocks)
     cudaStream_t st = ctx->stream;
     const int m = s.m;
     unsigned long long *tk = ctx->bticket.as<unsigned long long>();
@@ -1095,20 +1099,20 @@ int run_batch_iterations(arap_ctx *ctx, int P, int iterations) {
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_FWD);
-                launch_bsolve(d, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
+                launch_bsolve(dv, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
                               ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), nullptr, nullptr, tk, fl,
                               ctx->errw.as<int>(), true, st, ctx->batile.as<float>(), ctx->bftop.as<float>(),
                               ctx->bytop.as<float>(), ctx->bws.as<float>());
             }
             {
                 Prof pr(ctx, ARAP_K_SOLVE_BWD);
-                launch_bsolve(d, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
+                launch_bsolve(dv, P, ctx->bpt, ctx->bgrid, ctx->Xinv.as<float>(), ctx->L21.as<float>(), ctx->L21T.as<float>(),
                               ctx->bsol.as<Vec4<float>>(), ctx->buvec.as<Vec4<float>>(), ctx->bpc64.as<Vec4<double>>(),
                               ctx->bpc32.as<Vec4<float>>(), tk + 1, fl + fhalf, ctx->errw.as<int>(), false, st,
                               ctx->batile.as<float>(), ctx->bftop.as<float>(), ctx->bytop.as<float>(),
                               ctx->bws.as<float>());
             }
-            ctx->launches += 1 + (batch_tasks(d) > 0 ? 2 : 0) + batch_top_launches(d);
+            ctx->launches += 1 + (batch_tasks(dv) > 0 ? 2 : 0) + batch_top_launches(dv);
         }
     }
     CK(cudaGetLastError());
@@ -1411,18 +1415,18 @@ int arap_deform_poses_async(arap_ctx *ctx, int32_t n_poses, const double *target
         ctx->dirty = false;
     }
     const Symbolic &s = ctx->sym;
-    const DevSym &d = ctx->ds;
+    const DevSym &d = ctx->use_sb ? ctx->dss : ctx->ds;  // the batched sweeps' layout (with the solve blocks)
     const int V = s.V, m = s.m, P = n_poses, nc = V - m;
     int pt = ctx->pose_tile;
-    if (pt == 0) pt = batch_pose_tile(s.max_ldx, s.max_ld21);
-    else if (!batch_pose_tile_fits(s.max_ldx, s.max_ld21, pt))
+    if (pt == 0) pt = batch_pose_tile(d.max_ldx, d.max_ld21);
+    else if (!batch_pose_tile_fits(d.max_ldx, d.max_ld21, pt))
         return fail(ctx, ARAP_ERR_UNSUPPORTED,
                     "pose tile " + std::to_string(pt) + " does not fit this mesh's largest supernode");
     if (pt == 0) return fail(ctx, ARAP_ERR_UNSUPPORTED, "supernode fronts too large for the batched solves");
     if (ctx->bgen != ctx->gen || ctx->bP != P || ctx->bpt != pt || ctx->bntop != d.n_top) {
-        const size_t smem = batch_solve_smem_bytes(s.max_ldx, s.max_ld21, pt);
+        const size_t smem = batch_solve_smem_bytes(d.max_ldx, d.max_ld21, pt);
         if (pt != ctx->bpt || smem > ctx->bsmem) {
-            CK(configure_batch_smem(s.max_ldx, s.max_ld21, pt));
+            CK(configure_batch_smem(d.max_ldx, d.max_ld21, pt));
             ctx->bsmem = smem;
         }
         const int T = (P + pt - 1) / pt;

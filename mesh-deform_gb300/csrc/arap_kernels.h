@@ -66,6 +66,7 @@ struct DevTopo {
 
 struct DevSym {
     int V, m, S, nnz;
+    int s_sched;  // entries of level_sn (the supernodes the sweeps schedule; below S with solve blocks)
     int max_ldx, max_ld21, max_ncol;
     int solve_grid32, solve_grid64;  // CTAs per lower-level solve launch (each loops over tickets)
     // the solves split the tree: levels [0, ltop) by single CTAs (s_low tasks),

@@ -231,3 +231,19 @@ def test_dense_top_autotune(gpu):
         out = ctx.deform(3)
     ok, o = O.run_deform(w.positions, w.faces, w.cidx, w.poses[1], 3)
     assert ok and W.bbox_rel_error(out, o, w.positions) <= 1e-6
+
+
+def test_batched_sweeps_with_solve_blocks(gpu):
+    """The batched sweeps over the solve blocks (the default) and over the
+    supernodes alone give the same poses up to the order of sums."""
+    w = W.cfg_pose_batch(level=4, n_poses=24, iterations=6)
+    outs = []
+    for blocks in (512, 0):
+        with gpu.ArapContext(w.V, w.faces) as ctx:
+            ctx.set_precision("mixed", 1)
+            ctx.set_solve_blocks(blocks)
+            ctx.set_rest_positions(w.positions)
+            ctx.set_constraints(w.cidx, w.poses[0])
+            outs.append(ctx.deform_poses(w.poses, w.iterations))
+    for p in range(len(w.poses)):
+        assert W.bbox_rel_error(outs[0][p], outs[1][p], w.positions) <= 1e-6
