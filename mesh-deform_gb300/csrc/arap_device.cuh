@@ -275,9 +275,10 @@ __device__ __forceinline__ void rotation_fp64(int i, int e0, int e1, const int32
 }
 
 // FP64 rotation fit of the FP64 form: the FP32 fit of the covariance
-// (scaled to unit Frobenius norm before rounding), orthonormalised and
-// refined to FP64 accuracy by Newton's method on the rotation group
-// (polar_newton); near rank-one covariances, where the FP32 fit is a poor
+// (scaled to unit Frobenius norm before rounding), orthonormalised (one
+// Newton-Schulz step: 1e-7 -> 1e-14) and refined to FP64 accuracy by two
+// Newton steps on the rotation group (polar_newton); near rank-one
+// covariances, where the FP32 fit is a poor
 // seed, take the FP64 one-sided Jacobi fit. About a quarter of the FP64
 // instructions of the FP64 Jacobi fit, the same rotation to FP64 accuracy.
 __device__ __forceinline__ void rotation_fit_fp64(const double S[3][3], double R[3][3]) {
@@ -299,7 +300,7 @@ __device__ __forceinline__ void rotation_fit_fp64(const double S[3][3], double R
             for (int a = 0; a < 3; ++a)
 #pragma unroll
                 for (int b = 0; b < 3; ++b) R[a][b] = (double)Rf[a][b];
-            polar_newton(S, R, 2, 2);
+            polar_newton(S, R, 1, 2);
             return;
         }
     }
