@@ -187,7 +187,7 @@ struct arap_ctx {
     DevBuf ssn, slevel_sn, sbitems, sbmembers;
     // launch shape of the local step, RHS and residual (arap_set_vertex_launch)
     VertexLaunch vlaunch[kVertexKernels] = {{1, 256}, {1, 256}, {1, 256}};
-    size_t dense_inv_smem[2] = {0, 0}, dense_vec_smem[2] = {0, 0};  // configured limits (FP32, FP64)
+    size_t dense_inv_smem[2] = {0, 0};  // configured limits (FP32, FP64)
     DevBuf top_col, top_gptr, top_gidx, tdpos, top_items, Ttop, ytop;
     int ordering = ARAP_ORDER_PER_CONSTRAINT_SET;
     arap_done_fn done_fn = nullptr;  // called from a CUDA thread when an async deform finished
@@ -395,7 +395,7 @@ void planned_sizes(arap_ctx *ctx, int n_poses, std::vector<std::pair<DevBuf *, s
         add(ctx->Lval32, (size_t)std::max<int64_t>(s.panel_size, 1) * sizeof(float));
         add(ctx->Dinv32, (size_t)std::max<int64_t>(s.dinv_size, 1) * sizeof(float));
     }
-    add(ctx->ytop, std::max<size_t>(2 * (size_t)dense_ld(nt), 1) * sizeof(Vec4<T>));  // y_top, then f_top
+    add(ctx->ytop, std::max<size_t>(top_vec_bytes(nt, sizeof(T)), 16));  // y_top, the tiles' partials, counters
     if (n_poses > 0) {
         const size_t P = (size_t)n_poses, VP = V * P, MP = m1 * P, nc = V - (size_t)s.m;
         const int pt = std::max(batch_pose_tile(ctx->use_sb ? std::max(s.max_ldx, ctx->sb.max_ldx) : s.max_ldx,
@@ -537,6 +537,7 @@ int prepare_solve_blocks(arap_ctx *ctx) {
     const int nl = std::max(d.s_low - d.s_warp, 1);
     d.solve_grid32 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res32) : res32));
     d.solve_grid64 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res64) : res64));
+    d.overlap = cap <= 0;
     d.level_launch = ctx->solve_schedule == ARAP_SOLVE_LEVELS && nlev <= kMaxLevelLaunch;
     for (int l = 0; l <= kMaxLevelLaunch; ++l) d.lev_ptr[l] = nlev > 0 ? b.level_ptr[std::min(l, nlev)] : 0;
     for (int l = 0; l < kMaxLevelLaunch; ++l) {
@@ -630,17 +631,13 @@ int prepare_symbolic(arap_ctx *ctx) {
             const int rc32 = dense_inverse_rhs(ldxm, ld21m, 4), rc64 = dense_inverse_rhs(ldxm, ld21m, 8);
             const size_t i32 = rc32 > 0 ? dense_inverse_smem_bytes(ldxm, ld21m, 4, rc32) : 0;
             const size_t i64 = rc64 > 0 ? dense_inverse_smem_bytes(ldxm, ld21m, 8, rc64) : 0;
-            const size_t v32 = (size_t)dense_ld(dtop.ncols) * 16, v64 = (size_t)dense_ld(dtop.ncols) * 32;
-            if (rc32 > 0 && rc64 > 0 && v64 <= kSmemMax) {
+            if (rc32 > 0 && rc64 > 0) {
                 const int rc_d = prepare_dense_top(ctx, dtop.level, dtop.ncols);
                 if (rc_d != ARAP_OK) return rc_d;
-                if (i32 > ctx->dense_inv_smem[0] || i64 > ctx->dense_inv_smem[1] || v32 > ctx->dense_vec_smem[0] ||
-                    v64 > ctx->dense_vec_smem[1]) {
-                    CK(configure_dense_smem((int)i32, (int)i64, (int)v32, (int)v64));
+                if (i32 > ctx->dense_inv_smem[0] || i64 > ctx->dense_inv_smem[1]) {
+                    CK(configure_dense_smem((int)i32, (int)i64));
                     ctx->dense_inv_smem[0] = std::max(ctx->dense_inv_smem[0], i32);
                     ctx->dense_inv_smem[1] = std::max(ctx->dense_inv_smem[1], i64);
-                    ctx->dense_vec_smem[0] = std::max(ctx->dense_vec_smem[0], v32);
-                    ctx->dense_vec_smem[1] = std::max(ctx->dense_vec_smem[1], v64);
                 }
                 d.dense_ldx = ldxm;
                 d.dense_ld21 = ld21m;
@@ -679,6 +676,7 @@ int prepare_symbolic(arap_ctx *ctx) {
         const int nl = std::max(d.s_low - d.s_warp, 1);
         d.solve_grid32 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res32) : res32));
         d.solve_grid64 = std::max(1, std::min(nl, cap > 0 ? std::min(cap, res64) : res64));
+        d.overlap = cap <= 0;
         // level schedule: per level its supernodes, the shared memory its
         // largest front needs and a grid of at most one CTA per supernode
         d.level_launch = ctx->solve_schedule == ARAP_SOLVE_LEVELS && nlev <= kMaxLevelLaunch;
@@ -847,6 +845,8 @@ int setup_enqueue(arap_ctx *ctx) {
     // between the precisions
     CK(cudaMemsetAsync(ctx->ticket.p, 0, kTickets * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(ctx->flags.p, 0, 2 * sizeof(unsigned) * (size_t)std::max(s.S, 1), st));
+    // and the dense top's arrival counters
+    if (ctx->ytop.p) CK(cudaMemsetAsync(ctx->ytop.p, 0, ctx->ytop.cap, st));
     // cotan weights (arap.h:182-239)
     {
         Prof pr(ctx, ARAP_K_WEIGHTS);
@@ -966,8 +966,8 @@ int solve_launches(const DevSym &d) {
         cta = 0;
         for (int l = d.lwarp; l < d.ltop; ++l) cta += d.lev_ptr[l + 1] > d.lev_ptr[l];
     }
-    // the dense top: gather + GEMV forward, GEMV backward
-    return 2 * ((d.s_warp > 0) + cta + (d.s_top > 0)) + (d.n_top > 0 ? 3 : 0);
+    // the dense top: one tiled product each way
+    return 2 * ((d.s_warp > 0) + cta + (d.s_top > 0)) + (d.n_top > 0 ? 2 : 0);
 }
 
 template <>

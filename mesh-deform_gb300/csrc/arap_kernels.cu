@@ -28,6 +28,14 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     return v;
 }
 
+// Arrival count: old value of *p, incremented with acquire-release semantics
+// at device scope (the caller's CTA barrier orders its threads' writes before
+// it, cumulatively; the CTA that reads the final count sees every writer's).
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
 __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -42,6 +50,14 @@ __device__ __forceinline__ void wait_flag(const unsigned *p, unsigned target, in
     }
     atomicOr(err, kErrTimeout);
 }
+
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start once every CTA of the kernel before it has called
+// pdl_trigger (or exited); pdl_wait then blocks until that kernel has
+// finished and its memory is visible. Without the launch attribute pdl_wait
+// returns at once.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 template <typename T> __device__ __forceinline__ Vec4<T> ldcg4(const Vec4<T> *p);
 template <> __device__ __forceinline__ Vec4<float> ldcg4(const Vec4<float> *p) {
@@ -978,6 +994,7 @@ __global__ void __launch_bounds__(256)
 k_rhs(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const T *__restrict__ w,
       const Vec4<T> *__restrict__ p, const Vec4<T> *__restrict__ R, const Vec4<T> *__restrict__ bfixed,
       Vec4<T> *__restrict__ b) {
+    pdl_trigger();  // the forward sweep may take its first tasks meanwhile
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const Vec4<T> pi = p[i];
@@ -1004,6 +1021,7 @@ __global__ void __launch_bounds__(1024)
 k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const double *__restrict__ w64,
            const double *__restrict__ diag64, const Vec4<double> *__restrict__ bfixed,
            const Vec4<float> *__restrict__ b, const Vec4<double> *__restrict__ x, Vec4<float> *__restrict__ r) {
+    pdl_trigger();  // the forward sweep may take its first tasks meanwhile
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / G, l = t % G;
     const bool live = i < m;
@@ -1375,6 +1393,8 @@ k_solve_fwd(int S, int Z, int lbeg, SolveSmem lay, const int32_t *__restrict__ o
     __shared__ int s_task[2];  // this task's and the next one's ticket (taken early)
     __shared__ unsigned s_epoch[2];
     const int tid = threadIdx.x;
+    // the dense top's product may start its copies on SMs this grid leaves
+    pdl_trigger();
     if (tid == 0) {
         for (int b = 0; b < kSolveBufs; ++b) mbar_init(&bars[b], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1408,6 +1428,10 @@ k_solve_fwd(int S, int Z, int lbeg, SolveSmem lay, const int32_t *__restrict__ o
         if (multi) prefetch_mats_l2(pl);
         else for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
+    // the ticket, the task's description and its first copies (the factor does
+    // not change between factorisations) came before the kernel this launch
+    // may overlap had finished; the right-hand side and the flags come after
+    pdl_wait();
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         fc[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
     for (int i = tid; i < d.ld21; i += kSolveThreads) fb[i] = {(T)0, (T)0, (T)0, (T)0};
@@ -1542,6 +1566,7 @@ k_solve_fwd(int S, int Z, int lbeg, SolveSmem lay, const int32_t *__restrict__ o
 #pragma unroll
     for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((vtot - b + kSolveBufs - 1) / kSolveBufs);
     }
+    pdl_wait();  // a CTA without tasks still ends after the kernel it may overlap
 }
 
 // Backward: for supernode s (root first), z = y - L21^T x(struct) and
@@ -1599,6 +1624,7 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
         if (multi) prefetch_mats_l2(pl);
         else for (int k = kSolveBufs; k < ntot; ++k) prefetch_chunk_l2(pl, k);
     }
+    pdl_wait();  // as in the forward sweep
     const int32_t *rs = rows + d.rows_off;
     for (int i = tid; i < d.ldx; i += kSolveThreads)
         zv[i] = (i < nc) ? sol[d.first + i] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
@@ -1690,6 +1716,7 @@ k_solve_bwd(int S, int Z, int ltop, SolveSmem lay, const int32_t *__restrict__ o
 #pragma unroll
     for (int b = 0; b < kSolveBufs; ++b) ph[b] += (unsigned)((vtot - b + kSolveBufs - 1) / kSolveBufs);
     }
+    pdl_wait();  // a CTA without tasks still ends after the kernel it may overlap
 }
 
 
@@ -2100,80 +2127,236 @@ k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, 
     }
 }
 
-// f_top: the right-hand side of the top columns plus the update vectors of
-// their children in the lower levels (in a fixed order), one thread per row.
-template <typename T>
-__global__ void __launch_bounds__(256)
-k_top_gather(int n, const int32_t *__restrict__ col, const int32_t *__restrict__ gptr,
-             const int64_t *__restrict__ gidx, const Vec4<T> *__restrict__ sol, const Vec4<T> *__restrict__ uvec,
-             Vec4<T> *__restrict__ ftop) {
-    const int d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= n) return;
-    Vec4<T> v = sol[col[d]];
-    for (int k = gptr[d]; k < gptr[d + 1]; ++k) {
-        const Vec4<T> u = ldcg4(uvec + gidx[k]);
-        v.x += u.x;
-        v.y += u.y;
-        v.z += u.z;
-    }
-    ftop[d] = v;
+// The dense top's products with T = inv(L_top) (row-major, leading dimension
+// ldt, zeros above the diagonal and in the padding columns) run over
+// kTopTile x kTopTile tiles of T's lower triangle: one CTA per tile (rb, cb),
+// rb >= cb, numbered t = rb (rb + 1) / 2 + cb. Each CTA stores its partial
+// product into part[t] and counts its arrival on the block's counter; the CTA
+// that arrives last sums the block's partials in tile order (a fixed order:
+// results repeat bit for bit) and resets the counter for the next launch. No
+// CTA waits on another. When the launch overlaps the kernel before it
+// (pdl_wait), a CTA loads its tile of T and the gather's indices first (both
+// change only with the factorisation) and the vectors after.
+__device__ __forceinline__ void top_tile_coords(int t, int &rb, int &cb) {
+    int r = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;
+    while (r * (r + 1) / 2 > t) --r;
+    rb = r;
+    cb = t - r * (r + 1) / 2;
 }
 
-// out_r = sum_c M(r, c) in_c over the nonzero part of row r of a dense
-// triangular matrix (row-major, leading dimension ldt a multiple of 4, zeros
-// outside the triangle): the lower part c <= r (UPPER false, forward: M = T)
-// or the upper part c >= r (UPPER true, backward: M = T^T). One warp per row,
-// lanes over groups of four columns, sums in a fixed order. Forward: out to
-// ytop. Backward: out is x of the top columns, stored into the solution and
-// the positions (mode 0: pc64 = x; mode 1: pc64 += x, pc32 = float(pc64)).
-template <typename T, bool UPPER>
-__global__ void __launch_bounds__(256)
-k_top_gemv(int n, int ldt, const T *__restrict__ M, const Vec4<T> *__restrict__ in, Vec4<T> *__restrict__ ytop,
-           const int32_t *__restrict__ col, Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64,
-           Vec4<float> *__restrict__ pc32, int mode) {
-    extern __shared__ __align__(16) unsigned char top_raw[];
-    Vec4<T> *v = reinterpret_cast<Vec4<T> *>(top_raw);
-    const int tid = threadIdx.x, lane = tid & 31;
-    for (int d = tid; d < n; d += 256) v[d] = in[d];
-    for (int d = n + tid; d < ldt; d += 256) v[d] = {(T)0, (T)0, (T)0, (T)0};
-    __syncthreads();
-    const int nw = gridDim.x * 8;
-    for (int r = blockIdx.x * 8 + (tid >> 5); r < n; r += nw) {
-        const T *row = M + (int64_t)r * ldt;
-        const int g0 = UPPER ? (r >> 2) : 0, g1 = UPPER ? (ldt >> 2) : (r >> 2) + 1;  // column groups of four
-        T ax = 0, ay = 0, az = 0;
-#pragma unroll 4
-        for (int g = g0 + lane; g < g1; g += 32) {
-            const Vec4<T> m = *reinterpret_cast<const Vec4<T> *>(row + 4 * g);
-            const Vec4<T> f0 = v[4 * g], f1 = v[4 * g + 1], f2 = v[4 * g + 2], f3 = v[4 * g + 3];
-            ax += m.x * f0.x + m.y * f1.x + m.z * f2.x + m.w * f3.x;
-            ay += m.x * f0.y + m.y * f1.y + m.z * f2.y + m.w * f3.y;
-            az += m.x * f0.z + m.y * f1.z + m.z * f2.z + m.w * f3.z;
-        }
+template <typename T> __device__ __forceinline__ Vec4<T> ldg4(const T *p);
+template <> __device__ __forceinline__ Vec4<float> ldg4(const float *p) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+template <> __device__ __forceinline__ Vec4<double> ldg4(const double *p) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    return {a.x, a.y, b.x, b.y};
+}
+
+template <typename T> __device__ __forceinline__ void quad_sum(T &x, T &y, T &z) {
+    // the four lanes of an aligned quad end with the same sum, (a0 + a1) + (a2 + a3)
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            ax += __shfl_xor_sync(0xffffffffu, ax, off);
-            ay += __shfl_xor_sync(0xffffffffu, ay, off);
-            az += __shfl_xor_sync(0xffffffffu, az, off);
-        }
-        if (lane != 0) continue;
-        if (!UPPER) {
-            ytop[r] = {ax, ay, az, (T)0};
-        } else {
-            const int k = col[r];
-            sol[k] = {ax, ay, az, (T)0};
-            if (mode == 0) {
-                pc64[k] = {(double)ax, (double)ay, (double)az, 0.0};
-            } else {
-                Vec4<double> p = pc64[k];
-                p.x += (double)ax;
-                p.y += (double)ay;
-                p.z += (double)az;
-                pc64[k] = p;
-                pc32[k] = {(float)p.x, (float)p.y, (float)p.z, 0.f};
-            }
+    for (int off = 1; off <= 2; off <<= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, off);
+        y += __shfl_xor_sync(0xffffffffu, y, off);
+        z += __shfl_xor_sync(0xffffffffu, z, off);
+    }
+}
+
+// p[j kTopTile] over j = q, q + 4, ... < ntiles, in order, loads eight at a time
+template <typename T>
+__device__ __forceinline__ void top_partial_sum(const Vec4<T> *p, int q, int ntiles, T &sx, T &sy, T &sz) {
+    for (int j = q; j < ntiles; j += 32) {
+        Vec4<T> u[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            u[i] = j + 4 * i < ntiles ? ldcg4(p + (int64_t)(j + 4 * i) * kTopTile) : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            sx += u[i].x;
+            sy += u[i].y;
+            sz += u[i].z;
         }
     }
+}
+
+// Forward, y_top = T f_top: tile (rb, cb) gathers f of its columns (four
+// threads per column over every fourth update vector), multiplies its rows
+// (four threads per row, 16 columns each) and adds the row sums into block
+// row rb (rb + 1 tiles).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_top_tile_fwd(int n, int ldt, const T *__restrict__ M, const int32_t *__restrict__ col,
+               const int32_t *__restrict__ gptr, const int64_t *__restrict__ gidx, const Vec4<T> *__restrict__ sol,
+               const Vec4<T> *__restrict__ uvec, Vec4<T> *__restrict__ part, unsigned *__restrict__ cnt,
+               Vec4<T> *__restrict__ ytop) {
+    __shared__ Vec4<T> f[kTopTile];
+    __shared__ int last;
+    pdl_trigger();
+    int rb, cb;
+    top_tile_coords(blockIdx.x, rb, cb);
+    const int tid = threadIdx.x, q = tid & 3, r0 = rb * kTopTile, c0 = cb * kTopTile;
+    const int row = tid >> 2, r = r0 + row;
+    const Vec4<T> zero{(T)0, (T)0, (T)0, (T)0};
+    Vec4<T> m[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int c = c0 + 4 * q + 16 * k;  // ldt is a multiple of 4: c < ldt covers c + 3
+        m[k] = (r < n && c < ldt) ? ldg4(M + (int64_t)r * ldt + c) : zero;
+    }
+    {
+        // column d: thread q takes the right-hand side (q = 0) and the update
+        // vectors k0 + q, k0 + q + 4, ... in order; the first two indices early
+        const int d = c0 + (tid >> 2);
+        int kc = -1, k0 = 0, k1 = 0;
+        int64_t g0 = -1, g1 = -1;
+        if (d < n) {
+            if (q == 0) kc = col[d];
+            k0 = gptr[d] + q;
+            k1 = gptr[d + 1];
+            if (k0 < k1) g0 = gidx[k0];
+            if (k0 + 4 < k1) g1 = gidx[k0 + 4];
+        }
+        pdl_wait();
+        T vx = 0, vy = 0, vz = 0;
+        if (kc >= 0) {
+            const Vec4<T> v = sol[kc];
+            vx = v.x;
+            vy = v.y;
+            vz = v.z;
+        }
+        const Vec4<T> u0 = g0 >= 0 ? ldcg4(uvec + g0) : zero, u1 = g1 >= 0 ? ldcg4(uvec + g1) : zero;
+        vx += u0.x;
+        vy += u0.y;
+        vz += u0.z;
+        vx += u1.x;
+        vy += u1.y;
+        vz += u1.z;
+        for (int k = k0 + 8; k < k1; k += 4) {
+            const Vec4<T> u = ldcg4(uvec + gidx[k]);
+            vx += u.x;
+            vy += u.y;
+            vz += u.z;
+        }
+        quad_sum(vx, vy, vz);
+        if (q == 0) f[tid >> 2] = {vx, vy, vz, (T)0};
+    }
+    __syncthreads();
+    T ax = 0, ay = 0, az = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int cl = 4 * q + 16 * k;
+        const Vec4<T> f0 = f[cl], f1 = f[cl + 1], f2 = f[cl + 2], f3 = f[cl + 3];
+        ax += m[k].x * f0.x + m[k].y * f1.x + m[k].z * f2.x + m[k].w * f3.x;
+        ay += m[k].x * f0.y + m[k].y * f1.y + m[k].z * f2.y + m[k].w * f3.y;
+        az += m[k].x * f0.z + m[k].y * f1.z + m[k].z * f2.z + m[k].w * f3.z;
+    }
+    quad_sum(ax, ay, az);
+    if (q == 0) part[(int64_t)blockIdx.x * kTopTile + row] = {ax, ay, az, (T)0};
+    __syncthreads();
+    if (tid == 0) last = atom_add_acq_rel(cnt + rb, 1u) == (unsigned)rb;
+    __syncthreads();
+    if (!last) return;
+    {
+        const Vec4<T> *p = part + (int64_t)(rb * (rb + 1) / 2) * kTopTile + row;
+        T sx = 0, sy = 0, sz = 0;
+        top_partial_sum(p, q, rb + 1, sx, sy, sz);
+        quad_sum(sx, sy, sz);
+        if (q == 0 && r < n) ytop[r] = {sx, sy, sz, (T)0};
+    }
+    if (tid == 0) cnt[rb] = 0;
+}
+
+// Backward, x_top = T^T y_top, T read by columns: tile (rb, cb) adds
+// sum_r T(r, c) y_r over its rows into block column cb (nb - cb tiles), a
+// thread per column and row quarter (16 rows), the quarters combined in shared
+// memory in a fixed order; x into the solution and the positions as above.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_top_tile_bwd(int n, int ldt, int nb, const T *__restrict__ M, const Vec4<T> *__restrict__ ytop,
+               Vec4<T> *__restrict__ part, unsigned *__restrict__ cnt, const int32_t *__restrict__ col,
+               Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32,
+               int mode) {
+    __shared__ Vec4<T> y[kTopTile];
+    __shared__ Vec4<T> red[4][kTopTile];
+    __shared__ int last;
+    pdl_trigger();
+    int rb, cb;
+    top_tile_coords(blockIdx.x, rb, cb);
+    const int tid = threadIdx.x, r0 = rb * kTopTile, c0 = cb * kTopTile;
+    const int cl = tid & (kTopTile - 1), q = tid >> 6, c = c0 + cl;
+    T mv[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int r = r0 + 16 * q + i;
+        mv[i] = (r < n && c < n) ? __ldg(M + (int64_t)r * ldt + c) : (T)0;
+    }
+    const int oc = tid >> 2, j4 = tid & 3;  // the final sum's column and tile phase (see below)
+    const int kout = (j4 == 0 && c0 + oc < n) ? col[c0 + oc] : -1;
+    pdl_wait();
+    if (tid < kTopTile) y[tid] = (r0 + tid < n) ? ytop[r0 + tid] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+    __syncthreads();
+    T ax = 0, ay = 0, az = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const Vec4<T> v = y[16 * q + i];
+        ax += mv[i] * v.x;
+        ay += mv[i] * v.y;
+        az += mv[i] * v.z;
+    }
+    red[q][cl] = {ax, ay, az, (T)0};
+    __syncthreads();
+    if (tid < kTopTile) {
+        Vec4<T> v = red[0][tid];
+#pragma unroll
+        for (int j = 1; j < 4; ++j) {
+            v.x += red[j][tid].x;
+            v.y += red[j][tid].y;
+            v.z += red[j][tid].z;
+        }
+        part[(int64_t)blockIdx.x * kTopTile + tid] = v;
+    }
+    __syncthreads();
+    if (tid == 0) last = atom_add_acq_rel(cnt + cb, 1u) == (unsigned)(nb - cb - 1);
+    __syncthreads();
+    if (!last) return;
+    // four threads per column (an aligned quad), thread j4 over the block
+    // column's tiles j4, j4 + 4, ... of block rows cb, cb + 1, ..., nb - 1
+    T sx = 0, sy = 0, sz = 0;
+    for (int j = j4; j < nb - cb; j += 32) {
+        Vec4<T> u[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int rr = cb + j + 4 * i;
+            u[i] = j + 4 * i < nb - cb ? ldcg4(part + ((int64_t)rr * (rr + 1) / 2 + cb) * kTopTile + oc)
+                                       : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            sx += u[i].x;
+            sy += u[i].y;
+            sz += u[i].z;
+        }
+    }
+    quad_sum(sx, sy, sz);
+    if (kout >= 0) {
+        const int k = kout;
+        sol[k] = {sx, sy, sz, (T)0};
+        if (mode == 0) {
+            pc64[k] = {(double)sx, (double)sy, (double)sz, 0.0};
+        } else {
+            Vec4<double> p = pc64[k];
+            p.x += (double)sx;
+            p.y += (double)sy;
+            p.z += (double)sz;
+            pc64[k] = p;
+            pc32[k] = {(float)p.x, (float)p.y, (float)p.z, 0.f};
+        }
+    }
+    if (tid == 0) cnt[cb] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -2537,6 +2720,24 @@ size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
     return (size_t)kSolveBufs * kChunkBytes + (std::max(fwd, bwd) * 4 + 3 * (size_t)kRedRows) * scalar_bytes;
 }
 
+// A launch of 256-thread CTAs (kSolveThreads), with programmatic stream
+// serialization when `overlap` is set: the kernel may then start while the
+// kernel before it in the stream still runs (see pdl_wait).
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), bool overlap, int grid, size_t smem, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = overlap ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
                       unsigned long long *ticket, unsigned *flags, int *err, cudaStream_t st, const T *Ttop,
@@ -2565,8 +2766,9 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
                 ticket + kLevelTicket0 + 2 * l, flags, err);
         }
     } else if (sb > 0) {
-        k_solve_fwd<T><<<G, kSolveThreads, smem, st>>>(sb, sb + G, s.lwarp, lay, s.level_sn + s.s_warp, s.sn, s.child,
-                                                       s.relind, X, L21, sol, uvec, ticket, flags, err);
+        launch_pdl(k_solve_fwd<T>, s.overlap != 0, G, smem, st, sb, sb + G, s.lwarp, lay, (const int32_t *)(s.level_sn + s.s_warp),
+                   (const SnInfo *)s.sn, (const int32_t *)s.child, (const int32_t *)s.relind, X, L21, sol, uvec,
+                   ticket, flags, err);
     }
     if (s.s_top > 0) {
         const SolveSmem tlay{s.top_ldx, s.top_ld21};
@@ -2576,13 +2778,13 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
             sol, uvec, ticket + 2, flags, err);
     }
     if (s.n_top > 0) {
-        // f_top into the second half of ytop, then y_top = T f_top
+        // y_top = T f_top, f_top gathered by the tiles
         const int ldt = dense_ld(s.n_top);
-        Vec4<T> *ftop = ytop + ldt;
-        k_top_gather<T><<<(s.n_top + 255) / 256, 256, 0, st>>>(s.n_top, s.top_col, s.top_gptr, s.top_gidx, sol, uvec,
-                                                               ftop);
-        k_top_gemv<T, false><<<(s.n_top + 7) / 8, 256, (size_t)ldt * sizeof(Vec4<T>), st>>>(
-            s.n_top, ldt, Ttop, ftop, ytop, nullptr, nullptr, nullptr, nullptr, 0);
+        Vec4<T> *part = ytop + ldt;
+        unsigned *cnt = reinterpret_cast<unsigned *>(part + top_tiles(s.n_top) * kTopTile);
+        launch_pdl(k_top_tile_fwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 0, st, s.n_top, ldt, Ttop,
+                   (const int32_t *)s.top_col, (const int32_t *)s.top_gptr, (const int64_t *)s.top_gidx,
+                   (const Vec4<T> *)sol, (const Vec4<T> *)uvec, part, cnt, ytop);
     }
 }
 
@@ -2593,10 +2795,12 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
     if (s.S == 0) return;
     const SolveSmem lay{s.max_ldx, s.max_ld21};
     if (s.n_top > 0) {
-        // x_top = T^T y_top (T^T stored after T)
+        // x_top = T^T y_top, T read by columns
         const int ldt = dense_ld(s.n_top);
-        k_top_gemv<T, true><<<(s.n_top + 7) / 8, 256, (size_t)ldt * sizeof(Vec4<T>), st>>>(
-            s.n_top, ldt, Ttop + (size_t)ldt * s.n_top, ytop, nullptr, s.top_col, sol, pc64, pc32, mode);
+        Vec4<T> *part = const_cast<Vec4<T> *>(ytop) + ldt;
+        unsigned *cnt = reinterpret_cast<unsigned *>(part + top_tiles(s.n_top) * kTopTile);
+        launch_pdl(k_top_tile_bwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 0, st, s.n_top, ldt,
+                   top_blocks(s.n_top), Ttop, ytop, part, cnt, (const int32_t *)s.top_col, sol, pc64, pc32, mode);
     }
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
@@ -2621,8 +2825,8 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
                 ticket + kLevelTicket0 + 2 * l, flags, err);
         }
     } else if (sb > 0) {
-        k_solve_bwd<T><<<G, kSolveThreads, smem, st>>>(sb, sb + G, s.ltop, lay, s.level_sn + s.s_warp, s.sn, s.rows, X,
-                                                       L21T, sol, pc64, pc32, mode, ticket, flags, err);
+        launch_pdl(k_solve_bwd<T>, s.overlap != 0, G, smem, st, sb, sb + G, s.ltop, lay, (const int32_t *)(s.level_sn + s.s_warp),
+                   (const SnInfo *)s.sn, (const int32_t *)s.rows, X, L21T, sol, pc64, pc32, mode, ticket, flags, err);
     }
     if (s.s_warp > 0) {
         const int WG = sizeof(T) == 4 ? s.wgrid32 : s.wgrid64;
@@ -2660,6 +2864,13 @@ int dense_inverse_rhs(int ldx_max, int ld21_max, int scalar_bytes) {
 }
 
 int dense_ld(int n) { return (n + 3) & ~3; }
+int top_blocks(int n) { return (n + kTopTile - 1) / kTopTile; }
+size_t top_tiles(int n) { return (size_t)top_blocks(n) * (top_blocks(n) + 1) / 2; }
+size_t top_vec_bytes(int n, int scalar_bytes) {
+    if (n <= 0) return 0;
+    const size_t v = (size_t)4 * scalar_bytes;
+    return (dense_ld(n) + top_tiles(n) * kTopTile) * v + (((size_t)top_blocks(n) * 4 + 15) & ~(size_t)15);
+}
 size_t dense_top_elems(int n) { return (size_t)2 * dense_ld(n) * n; }
 
 size_t dense_inverse_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes, int rc) {
@@ -2675,13 +2886,9 @@ static cudaError_t raise_inverse(int bytes) {
     return e;
 }
 
-cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64) {
+cudaError_t configure_dense_smem(int inv32, int inv64) {
     cudaError_t e = raise_inverse<float>(inv32);
     if (e == cudaSuccess) e = raise_inverse<double>(inv64);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<float, false>, vec32);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<double, false>, vec64);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<float, true>, vec32);
-    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_gemv<double, true>, vec64);
     return e;
 }
 

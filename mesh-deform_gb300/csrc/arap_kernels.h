@@ -83,6 +83,11 @@ struct DevSym {
     // level l holds the supernodes level_sn[lev_ptr[l], lev_ptr[l+1]), its
     // fronts fit lev_ldx[l] / lev_ld21[l] rows, lev_grid32/64[l] CTAs
     VertexLaunch vlaunch[kVertexKernels];
+    // the persistent sweeps and the dense top's products start while the
+    // kernel before them finishes (programmatic dependent launch): set when
+    // the sweeps' grids fill the device (no CTA cap); with a cap, requests
+    // share the SMs and early-resident waiting CTAs would hold them
+    int overlap;
     int level_launch;
     int lev_ptr[kMaxLevelLaunch + 1], lev_ldx[kMaxLevelLaunch], lev_ld21[kMaxLevelLaunch];
     int lev_grid32[kMaxLevelLaunch], lev_grid64[kMaxLevelLaunch];
@@ -208,8 +213,16 @@ int dense_inverse_rhs(int ldx_max, int ld21_max, int scalar_bytes);
 // leading dimension of the dense top's T and T^T rows, and the elements of both
 int dense_ld(int n);
 size_t dense_top_elems(int n);
-cudaError_t configure_dense_smem(int inv32, int inv64, int vec32, int vec64);
-// most columns of the dense top (its T and f vectors must fit the device and shared memory)
+// the products with T (forward) and T^T (backward, T read by columns) run
+// over kTopTile x kTopTile tiles of T's lower triangle, one CTA each; the
+// vector buffer (ytop) holds y_top, the tiles' partial products and one
+// arrival counter per block of kTopTile rows (zero between launches)
+constexpr int kTopTile = 64;
+int top_blocks(int n);
+size_t top_tiles(int n);
+size_t top_vec_bytes(int n, int scalar_bytes);
+cudaError_t configure_dense_smem(int inv32, int inv64);
+// most columns of the dense top (its T must fit the device)
 constexpr int kDenseTopCols = 4096;
 constexpr int kDenseTopDefault = 2048;  // the default column cap
 constexpr int kTopRhs = 8;   // columns of T one CTA of the inversion forms
