@@ -173,8 +173,11 @@ int arap_query(arap_ctx *ctx, int32_t *done);
 /* Most CTAs one triangular-solve launch uses (0, the default: as many as fit
    on the device). Each CTA works through the supernodes in schedule order, so
    any count gives the same result; a smaller count leaves room for the
-   launches of other contexts running at the same time. Takes effect at the
-   next deform (which sets the problem up again). */
+   launches of other contexts running at the same time. With 0 the context
+   assumes it owns the device: its sweeps and dense-top products start while
+   the kernel before them finishes (programmatic dependent launch); with a cap
+   every launch waits for the previous one as usual. Takes effect at the next
+   deform (which sets the problem up again). */
 int arap_set_solve_ctas(arap_ctx *ctx, int32_t max_ctas);
 
 /* Poses per task of the batched triangular solves of arap_deform_poses: 1, 2,
