@@ -868,6 +868,8 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 k_local_step(int V, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const T *__restrict__ w,
              const Vec4<T> *__restrict__ p, const Vec4<T> *__restrict__ pc, Vec4<T> *__restrict__ R) {
+    pdl_wait();  // the positions of the kernels before (an overlapped launch)
+    pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     const Vec4<T> pi = p[i], ci = pc[i];
@@ -920,6 +922,8 @@ k_local_step_mixed(int V, const int32_t *__restrict__ drow, const int32_t *__res
                    const float *__restrict__ w, const Vec4<float> *__restrict__ redge,
                    const Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ R,
                    const double *__restrict__ w64, const Vec4<double> *__restrict__ p64) {
+    pdl_wait();  // the positions of the kernels before (an overlapped launch)
+    pdl_trigger();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / G, l = t % G;
     const bool live = i < V;
@@ -962,6 +966,8 @@ template <int G>
 __global__ void __launch_bounds__(1024)
 k_rhs_mixed(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const float *__restrict__ w,
             const Vec4<float> *__restrict__ redge, const Vec4<float> *__restrict__ R, Vec4<float> *__restrict__ b) {
+    pdl_wait();  // the rotations of the local step (an overlapped launch)
+    pdl_trigger();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / G, l = t % G;
     const bool live = i < m;
@@ -994,6 +1000,7 @@ __global__ void __launch_bounds__(256)
 k_rhs(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const T *__restrict__ w,
       const Vec4<T> *__restrict__ p, const Vec4<T> *__restrict__ R, const Vec4<T> *__restrict__ bfixed,
       Vec4<T> *__restrict__ b) {
+    pdl_wait();     // the positions and rotations of the kernels before
     pdl_trigger();  // the forward sweep may take its first tasks meanwhile
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
@@ -1021,6 +1028,7 @@ __global__ void __launch_bounds__(1024)
 k_residual(int m, const int32_t *__restrict__ drow, const int32_t *__restrict__ dcol, const double *__restrict__ w64,
            const double *__restrict__ diag64, const Vec4<double> *__restrict__ bfixed,
            const Vec4<float> *__restrict__ b, const Vec4<double> *__restrict__ x, Vec4<float> *__restrict__ r) {
+    pdl_wait();     // x and b of the kernels before
     pdl_trigger();  // the forward sweep may take its first tasks meanwhile
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / G, l = t % G;
@@ -2573,13 +2581,33 @@ void launch_rest_edges(const DevSym &s, const Vec4<double> *p64, Vec4<float> *re
     k_rest_edges<<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.drow, s.dcol, p64, redge);
 }
 
+// A launch with programmatic stream serialization when `overlap` is set: the
+// kernel may then start while the kernel before it in the stream still runs
+// (see pdl_wait); otherwise an ordinary launch.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), bool overlap, int grid, int block, size_t smem, cudaStream_t st,
+                       Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = overlap ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 void launch_local_step_mixed(const DevSym &s, const float *w32, const Vec4<float> *redge, const Vec4<double> *pc64,
                              Vec4<float> *R, const double *w64, const Vec4<double> *p64, cudaStream_t st) {
     if (s.V == 0) return;
     const VertexLaunch vl = s.vlaunch[kVertexLocal];
     const int grid = (int)(((int64_t)s.V * vl.tpv + vl.block - 1) / vl.block);
-#define ARAP_LOCAL(G) \
-    k_local_step_mixed<G><<<grid, vl.block, 0, st>>>(s.V, s.drow, s.dcol, w32, redge, pc64, R, w64, p64)
+#define ARAP_LOCAL(G)                                                                                  \
+    launch_pdl(k_local_step_mixed<G>, s.overlap != 0, grid, vl.block, 0, st, s.V, (const int32_t *)s.drow,  \
+               (const int32_t *)s.dcol, w32, redge, pc64, R, w64, p64)
     switch (vl.tpv) {
     case 2: ARAP_LOCAL(2); break;
     case 4: ARAP_LOCAL(4); break;
@@ -2595,7 +2623,9 @@ void launch_rhs_mixed(const DevSym &s, const float *w32, const Vec4<float> *redg
     if (s.m == 0) return;
     const VertexLaunch vl = s.vlaunch[kVertexRhs];
     const int grid = (int)(((int64_t)s.m * vl.tpv + vl.block - 1) / vl.block);
-#define ARAP_RHS(G) k_rhs_mixed<G><<<grid, vl.block, 0, st>>>(s.m, s.drow, s.dcol, w32, redge, R, b)
+#define ARAP_RHS(G)                                                                                    \
+    launch_pdl(k_rhs_mixed<G>, s.overlap != 0, grid, vl.block, 0, st, s.m, (const int32_t *)s.drow,         \
+               (const int32_t *)s.dcol, w32, redge, (const Vec4<float> *)R, b)
     switch (vl.tpv) {
     case 2: ARAP_RHS(2); break;
     case 4: ARAP_RHS(4); break;
@@ -2637,14 +2667,16 @@ template <typename T>
 void launch_local_step(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *pc, Vec4<T> *R,
                        cudaStream_t st) {
     if (s.V == 0) return;
-    k_local_step<T><<<blocks_for(s.V, 256), 256, 0, st>>>(s.V, s.drow, s.dcol, w, p, pc, R);
+    launch_pdl(k_local_step<T>, s.overlap != 0, blocks_for(s.V, 256), 256, 0, st, s.V, (const int32_t *)s.drow,
+               (const int32_t *)s.dcol, w, p, pc, R);
 }
 
 template <typename T>
 void launch_rhs(const DevSym &s, const T *w, const Vec4<T> *p, const Vec4<T> *R, const Vec4<T> *bfixed,
                 Vec4<T> *b, cudaStream_t st) {
     if (s.m == 0) return;
-    k_rhs<T><<<blocks_for(s.m, 256), 256, 0, st>>>(s.m, s.drow, s.dcol, w, p, R, bfixed, b);
+    launch_pdl(k_rhs<T>, s.overlap != 0, blocks_for(s.m, 256), 256, 0, st, s.m, (const int32_t *)s.drow,
+               (const int32_t *)s.dcol, w, p, R, bfixed, b);
 }
 
 void launch_residual(const DevSym &s, const double *w64, const double *diag64, const Vec4<double> *bfixed,
@@ -2652,7 +2684,9 @@ void launch_residual(const DevSym &s, const double *w64, const double *diag64, c
     if (s.m == 0) return;
     const VertexLaunch vl = s.vlaunch[kVertexResidual];
     const int grid = (int)(((int64_t)s.m * vl.tpv + vl.block - 1) / vl.block);
-#define ARAP_RES(G) k_residual<G><<<grid, vl.block, 0, st>>>(s.m, s.drow, s.dcol, w64, diag64, bfixed, b, x64, r)
+#define ARAP_RES(G)                                                                                    \
+    launch_pdl(k_residual<G>, s.overlap != 0, grid, vl.block, 0, st, s.m, (const int32_t *)s.drow,          \
+               (const int32_t *)s.dcol, w64, diag64, bfixed, b, x64, r)
     switch (vl.tpv) {
     case 2: ARAP_RES(2); break;
     case 4: ARAP_RES(4); break;
@@ -2720,23 +2754,6 @@ size_t solve_smem_bytes(int ldx_max, int ld21_max, int scalar_bytes) {
     return (size_t)kSolveBufs * kChunkBytes + (std::max(fwd, bwd) * 4 + 3 * (size_t)kRedRows) * scalar_bytes;
 }
 
-// A launch of 256-thread CTAs (kSolveThreads), with programmatic stream
-// serialization when `overlap` is set: the kernel may then start while the
-// kernel before it in the stream still runs (see pdl_wait).
-template <typename... KArgs, typename... Args>
-static void launch_pdl(void (*kern)(KArgs...), bool overlap, int grid, size_t smem, cudaStream_t st, Args... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = overlap ? 1 : 0;
-    cudaLaunchKernelEx(&cfg, kern, args...);
-}
 
 template <typename T>
 void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, Vec4<T> *uvec,
@@ -2766,7 +2783,7 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
                 ticket + kLevelTicket0 + 2 * l, flags, err);
         }
     } else if (sb > 0) {
-        launch_pdl(k_solve_fwd<T>, s.overlap != 0, G, smem, st, sb, sb + G, s.lwarp, lay, (const int32_t *)(s.level_sn + s.s_warp),
+        launch_pdl(k_solve_fwd<T>, s.overlap != 0, G, kSolveThreads, smem, st, sb, sb + G, s.lwarp, lay, (const int32_t *)(s.level_sn + s.s_warp),
                    (const SnInfo *)s.sn, (const int32_t *)s.child, (const int32_t *)s.relind, X, L21, sol, uvec,
                    ticket, flags, err);
     }
@@ -2782,7 +2799,7 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
         const int ldt = dense_ld(s.n_top);
         Vec4<T> *part = ytop + ldt;
         unsigned *cnt = reinterpret_cast<unsigned *>(part + top_tiles(s.n_top) * kTopTile);
-        launch_pdl(k_top_tile_fwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 0, st, s.n_top, ldt, Ttop,
+        launch_pdl(k_top_tile_fwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 256, 0, st, s.n_top, ldt, Ttop,
                    (const int32_t *)s.top_col, (const int32_t *)s.top_gptr, (const int64_t *)s.top_gidx,
                    (const Vec4<T> *)sol, (const Vec4<T> *)uvec, part, cnt, ytop);
     }
@@ -2799,7 +2816,7 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
         const int ldt = dense_ld(s.n_top);
         Vec4<T> *part = const_cast<Vec4<T> *>(ytop) + ldt;
         unsigned *cnt = reinterpret_cast<unsigned *>(part + top_tiles(s.n_top) * kTopTile);
-        launch_pdl(k_top_tile_bwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 0, st, s.n_top, ldt,
+        launch_pdl(k_top_tile_bwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 256, 0, st, s.n_top, ldt,
                    top_blocks(s.n_top), Ttop, ytop, part, cnt, (const int32_t *)s.top_col, sol, pc64, pc32, mode);
     }
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
@@ -2825,7 +2842,7 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
                 ticket + kLevelTicket0 + 2 * l, flags, err);
         }
     } else if (sb > 0) {
-        launch_pdl(k_solve_bwd<T>, s.overlap != 0, G, smem, st, sb, sb + G, s.ltop, lay, (const int32_t *)(s.level_sn + s.s_warp),
+        launch_pdl(k_solve_bwd<T>, s.overlap != 0, G, kSolveThreads, smem, st, sb, sb + G, s.ltop, lay, (const int32_t *)(s.level_sn + s.s_warp),
                    (const SnInfo *)s.sn, (const int32_t *)s.rows, X, L21T, sol, pc64, pc32, mode, ticket, flags, err);
     }
     if (s.s_warp > 0) {

@@ -565,19 +565,29 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     std::vector<int32_t> owner(m);
     for (int s = 0; s < S; ++s)
         for (int k = sym.block_ptr[s]; k < sym.block_ptr[s + 1]; ++k) owner[k] = s;
-    std::vector<std::vector<int32_t>> strct(S), children(S);
-    std::vector<int32_t> mark(m, -1);
+    // struct rows of each supernode (its columns' rows below it and its
+    // children's struct rows below it, sorted), written straight into
+    // sym.rows; children as linked lists in increasing order
+    std::vector<int32_t> mark(m, -1), st, chead(S, -1), ctail(S, -1), cnext(S, -1);
+    st.reserve(1024);
+    sym.rows.clear();
+    sym.rows.reserve(prow[m]);
     for (int s = 0; s < S; ++s) {
         const int f = sym.block_ptr[s], l = sym.block_ptr[s + 1];
-        std::vector<int32_t> &st = strct[s];
+        st.clear();
         for (int k = f; k < l; ++k)
             for (int32_t q = prow[k]; q < prow[k + 1]; ++q) {
                 const int32_t r = pcol[q];
                 if (r >= l && mark[r] != s) { mark[r] = s; st.push_back(r); }
             }
-        for (int32_t c : children[s])
-            for (int32_t r : strct[c])
+        for (int32_t c = chead[s]; c >= 0; c = cnext[c]) {
+            const SnInfo &cd = sym.sn[c];
+            const int32_t *cr = sym.rows.data() + cd.rows_off;
+            for (int i = 0; i < cd.nrow - cd.ncol; ++i) {
+                const int32_t r = cr[i];
                 if (r >= l && mark[r] != s) { mark[r] = s; st.push_back(r); }
+            }
+        }
         std::sort(st.begin(), st.end());
         const int p = st.empty() ? -1 : owner[st[0]];
         SnInfo &d = sym.sn[s];
@@ -585,7 +595,13 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         d.ncol = l - f;
         d.nrow = d.ncol + (int32_t)st.size();
         d.parent = p;
-        if (p >= 0) children[p].push_back(s);
+        d.rows_off = (int32_t)sym.rows.size();
+        sym.rows.insert(sym.rows.end(), st.begin(), st.end());
+        if (p >= 0) {
+            if (chead[p] < 0) chead[p] = s;
+            else cnext[ctail[p]] = s;
+            ctail[p] = s;
+        }
     }
     // levels, offsets, struct rows, children, relative indices
     int maxlev = 0;
@@ -593,8 +609,8 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     double flops = 0.0;
     for (int s = 0; s < S; ++s) {
         SnInfo &d = sym.sn[s];
-        int lv = 0;
-        for (int32_t c : children[s]) lv = std::max(lv, sym.sn[c].level + 1);
+        int lv = 0, nch = 0;
+        for (int32_t c = chead[s]; c >= 0; c = cnext[c], ++nch) lv = std::max(lv, sym.sn[c].level + 1);
         d.level = lv;
         maxlev = std::max(maxlev, lv);
         const int nb = d.nrow - d.ncol;
@@ -620,14 +636,12 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         loff += (int64_t)d.ld21 * d.ncol;
         sym.max_ldx = std::max(sym.max_ldx, (int)d.ldx);
         sym.max_ld21 = std::max(sym.max_ld21, (int)d.ld21);
-        d.rows_off = (int32_t)sym.rows.size();
-        sym.rows.insert(sym.rows.end(), strct[s].begin(), strct[s].end());
         d.child_begin = (int32_t)sym.child.size();
-        sym.child.insert(sym.child.end(), children[s].begin(), children[s].end());
+        for (int32_t c = chead[s]; c >= 0; c = cnext[c]) sym.child.push_back(c);
         d.child_end = (int32_t)sym.child.size();
         sym.max_nrow = std::max(sym.max_nrow, (int)d.nrow);
         sym.max_ncol = std::max(sym.max_ncol, (int)d.ncol);
-        sym.max_children = std::max(sym.max_children, (int)children[s].size());
+        sym.max_children = std::max(sym.max_children, nch);
         const double nc_ = d.ncol, nb_ = nb;
         flops += nc_ * nc_ * nc_ / 3.0 + nc_ * nc_ * nb_ + nc_ * nb_ * nb_;
     }
@@ -639,29 +653,45 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     sym.x_size = xoff;
     sym.l21_size = loff;
     sym.l21t_size = ltoff;
+    // front position of every row of supernode s's front: its columns, then
+    // its struct rows; filled for one supernode at a time (stamped by s), so
+    // lookups below are direct
+    std::vector<int32_t> fpos(m, 0), fstamp(m, -1);
+    auto map_front = [&](int s) {
+        const SnInfo &d = sym.sn[s];
+        for (int c = 0; c < d.ncol; ++c) {
+            fpos[d.first + c] = c;
+            fstamp[d.first + c] = s;
+        }
+        const int32_t *rs = sym.rows.data() + d.rows_off;
+        for (int i = 0; i < d.nrow - d.ncol; ++i) {
+            fpos[rs[i]] = d.ncol + i;
+            fstamp[rs[i]] = s;
+        }
+    };
     // relind: where each struct row of s sits in its parent's front
-    for (int s = 0; s < S; ++s) {
-        SnInfo &d = sym.sn[s];
-        d.relind_off = (int32_t)sym.relind.size();
-        if (d.parent < 0) continue;
-        const SnInfo &p = sym.sn[d.parent];
-        const int32_t *prs = sym.rows.data() + p.rows_off;
-        const int pnb = p.nrow - p.ncol;
-        for (int32_t r : strct[s]) {
-            int32_t pos;
-            if (r < p.first + p.ncol) {
-                pos = r - p.first;
-            } else {
-                const int32_t *it = std::lower_bound(prs, prs + pnb, r);
-                if (it == prs + pnb || *it != r) {
+    sym.relind.reserve(sym.rows.size());
+    for (int s = 0; s < S; ++s) sym.sn[s].relind_off = -1;
+    for (int p = 0; p < S; ++p) {
+        const SnInfo &pd = sym.sn[p];
+        if (pd.child_begin == pd.child_end) continue;
+        map_front(p);
+        for (int ci = pd.child_begin; ci < pd.child_end; ++ci) {
+            SnInfo &d = sym.sn[sym.child[ci]];
+            d.relind_off = (int32_t)sym.relind.size();
+            const int32_t *cr = sym.rows.data() + d.rows_off;
+            for (int i = 0; i < d.nrow - d.ncol; ++i) {
+                const int32_t r = cr[i];
+                if (fstamp[r] != p) {
                     err = "internal: struct row missing from parent front";
                     return false;
                 }
-                pos = p.ncol + (int32_t)(it - prs);
+                sym.relind.push_back(fpos[r]);
             }
-            sym.relind.push_back(pos);
         }
     }
+    for (int s = 0; s < S; ++s)
+        if (sym.sn[s].relind_off < 0) sym.sn[s].relind_off = (int32_t)sym.relind.size();
     // supernodes grouped by level
     sym.level_ptr.assign(maxlev + 2, 0);
     for (int s = 0; s < S; ++s) sym.level_ptr[sym.sn[s].level + 1]++;
@@ -726,27 +756,21 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     // assembly maps: L_kk and L_lk = -w_kl (l > k, both free) into the panels
     sym.amap.assign(nnz, -1);
     sym.dmap.assign(m, -1);
-    for (int k = 0; k < m; ++k) {
-        const SnInfo &d = sym.sn[owner[k]];
-        const int cidx = k - d.first;
-        const int32_t *rs = sym.rows.data() + d.rows_off;
-        const int nb = d.nrow - d.ncol;
-        sym.dmap[k] = d.panel_off + (int64_t)cidx * d.nrow + cidx;
-        for (int32_t e = sym.drow[k]; e < sym.drow[k + 1]; ++e) {
-            const int32_t l = sym.dcol[e];
-            if (l >= m || l <= k) continue;
-            int32_t pos;
-            if (l < d.first + d.ncol) {
-                pos = l - d.first;
-            } else {
-                const int32_t *it = std::lower_bound(rs, rs + nb, l);
-                if (it == rs + nb || *it != l) {
+    for (int s = 0; s < S; ++s) {
+        const SnInfo &d = sym.sn[s];
+        map_front(s);
+        for (int k = d.first; k < d.first + d.ncol; ++k) {
+            const int cidx = k - d.first;
+            sym.dmap[k] = d.panel_off + (int64_t)cidx * d.nrow + cidx;
+            for (int32_t e = sym.drow[k]; e < sym.drow[k + 1]; ++e) {
+                const int32_t l = sym.dcol[e];
+                if (l >= m || l <= k) continue;
+                if (fstamp[l] != s) {
                     err = "internal: matrix entry outside its supernode's front";
                     return false;
                 }
-                pos = d.ncol + (int32_t)(it - rs);
+                sym.amap[e] = d.panel_off + (int64_t)cidx * d.nrow + fpos[l];
             }
-            sym.amap[e] = d.panel_off + (int64_t)cidx * d.nrow + pos;
         }
     }
     return true;
