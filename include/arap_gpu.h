@@ -243,7 +243,10 @@ int arap_set_solve_blocks(arap_ctx *ctx, int32_t max_columns);
 int arap_set_solve_schedule(arap_ctx *ctx, int32_t schedule);
 
 /* The top levels of the elimination tree, up to `max_columns` columns in all
-   (0, the default: 2,048; negative: none), are solved through the explicit
+   (0, the default: 4,096 when the solve grid is uncapped, i.e. the request
+   owns the device, and 2,048 under an arap_set_solve_ctas cap, where the
+   wider product's SM time competes with other requests; at most 4,096;
+   negative: none), are solved through the explicit
    inverse of the factor restricted to them: formed once per factorisation
    (n x n dense), it turns the top of each triangular sweep, a chain of
    single-supernode steps, into one wide matrix-vector product (in

@@ -333,7 +333,12 @@ DenseTopChoice choose_dense_top(const Symbolic &s, int cap) {
 }
 
 int dense_cap(const arap_ctx *ctx) {
-    return ctx->dense_cols < 0 ? 0 : (ctx->dense_cols == 0 ? kDenseTopDefault : std::min(ctx->dense_cols, kDenseTopCols));
+    if (ctx->dense_cols < 0) return 0;
+    if (ctx->dense_cols > 0) return std::min(ctx->dense_cols, kDenseTopCols);
+    // a request that owns the device takes more levels into T (fewer sweep
+    // levels, one wider product); under a CTA cap the product's SM time is
+    // shared with other requests
+    return ctx->solve_cap <= 0 ? kDenseTopOwned : kDenseTopDefault;
 }
 
 // Bytes of every device buffer the setup of precision T (and, for n_poses > 0,

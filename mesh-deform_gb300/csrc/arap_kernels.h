@@ -224,7 +224,8 @@ size_t top_vec_bytes(int n, int scalar_bytes);
 cudaError_t configure_dense_smem(int inv32, int inv64);
 // most columns of the dense top (its T must fit the device)
 constexpr int kDenseTopCols = 4096;
-constexpr int kDenseTopDefault = 2048;  // the default column cap
+constexpr int kDenseTopDefault = 2048;  // the default column cap under a solve-CTA cap
+constexpr int kDenseTopOwned = 4096;    // the default with an uncapped solve grid (the device is the request's)
 constexpr int kTopRhs = 8;   // columns of T one CTA of the inversion forms
 // ---- many poses of one mesh and constraint set (arap_batch.cu); arrays of
 // (vertex, pose) pairs are vertex-major, element (k, p) at k * P + p
