@@ -476,6 +476,8 @@ int prepare_dense_top(arap_ctx *ctx, int level, int n) {
     CK(upload(ctx->top_gidx, gidx, st));
     CK(upload(ctx->top_items, items, st));
     d.n_top = n;
+    d.top_pair32 = (int64_t)top_tiles(n) > top_tile_resident_ctas(4);
+    d.top_pair64 = (int64_t)top_tiles(n) > top_tile_resident_ctas(8);
     d.n_top_items = (int)items.size() / 2;
     return ARAP_OK;
 }

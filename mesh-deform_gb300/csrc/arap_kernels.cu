@@ -2137,14 +2137,34 @@ k_top_inverse(const int32_t *__restrict__ items, const SnInfo *__restrict__ sn, 
 
 // The dense top's products with T = inv(L_top) (row-major, leading dimension
 // ldt, zeros above the diagonal and in the padding columns) run over
-// kTopTile x kTopTile tiles of T's lower triangle: one CTA per tile (rb, cb),
-// rb >= cb, numbered t = rb (rb + 1) / 2 + cb. Each CTA stores its partial
-// product into part[t] and counts its arrival on the block's counter; the CTA
-// that arrives last sums the block's partials in tile order (a fixed order:
-// results repeat bit for bit) and resets the counter for the next launch. No
-// CTA waits on another. When the launch overlaps the kernel before it
-// (pdl_wait), a CTA loads its tile of T and the gather's indices first (both
-// change only with the factorisation) and the vectors after.
+// kTopTile x kTopTile tiles of T's lower triangle, (rb, cb) with rb >= cb,
+// whose partial products are stored at tile index t = rb (rb + 1) / 2 + cb.
+// A CTA takes two tiles of one block column, (rb0, cb) and (rb0 + 1, cb)
+// (the pairs of column cb start at rb0 = cb, cb + 2, ...; the last may be a
+// single tile), so one wave covers a top of 4,096 columns. Each tile counts
+// its arrival on its block's counter; the CTA that brings a block's last tile
+// sums the block's partials in tile order (a fixed order: results repeat bit
+// for bit) and resets the counter for the next launch. No CTA waits on
+// another. When the launch overlaps the kernel before it (pdl_wait), a CTA
+// loads its tiles of T and the gather's indices first (both change only with
+// the factorisation) and the vectors after.
+
+// pairs of the block columns before cb: sum over c < cb of ceil((nb - c) / 2)
+__device__ __forceinline__ int top_pairs_before(int nb, int cb) {
+    auto S = [](int x) { return (x + 1) * (x + 1) / 4; };  // sum_{k=1..x} ceil(k / 2)
+    return S(nb) - S(nb - cb);
+}
+__device__ __forceinline__ void top_pair_coords(int t, int nb, int &cb, int &rb0) {
+    int lo = 0, hi = nb - 1;  // the last cb with top_pairs_before(nb, cb) <= t
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (top_pairs_before(nb, mid) <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    cb = lo;
+    rb0 = cb + 2 * (t - top_pairs_before(nb, cb));
+}
+
 __device__ __forceinline__ void top_tile_coords(int t, int &rb, int &cb) {
     int r = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
     while ((r + 1) * (r + 2) / 2 <= t) ++r;
@@ -2191,6 +2211,232 @@ __device__ __forceinline__ void top_partial_sum(const Vec4<T> *p, int q, int nti
     }
 }
 
+// The pair's 2 x kTopTile rows of T, columns [c0, c0 + kTopTile) clipped to
+// ldt, into shared memory by bulk copies (a thread per row, rows of kTopRow
+// words: 16-byte aligned, 4 banks apart), counted on `bar`. Thread 0 has
+// initialised `bar`; rows at or past n are not copied.
+constexpr int kTopRow = kTopTile + 4;
+template <typename T>
+__device__ __forceinline__ void top_pair_copy(const T *M, int ldt, int n, int rb0, int nsub, int c0, T *Ms,
+                                              uint64_t *bar) {
+    const int tid = threadIdx.x, w = min(kTopTile, ldt - c0);
+    const int nr = max(0, min(nsub * kTopTile, n - rb0 * kTopTile));
+    if (tid == 0) mbar_expect_tx(bar, (unsigned)(nr * w * (int)sizeof(T)));
+    __syncthreads();  // the expected bytes are set before any copy can complete
+    if (tid < nr)
+        tma_load_1d(Ms + (size_t)tid * kTopRow, M + (int64_t)(rb0 * kTopTile + tid) * ldt + c0,
+                    (unsigned)(w * (int)sizeof(T)), bar);
+}
+
+// Forward, y_top = T f_top: the pair gathers f of its columns (four threads
+// per column over every fourth update vector), each of its tiles multiplies
+// its rows (four threads per row, 16 columns each) and adds the row sums into
+// its block row (rb + 1 tiles).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_top_pair_fwd(int n, int ldt, int nb, const T *__restrict__ M, const int32_t *__restrict__ col,
+               const int32_t *__restrict__ gptr, const int64_t *__restrict__ gidx, const Vec4<T> *__restrict__ sol,
+               const Vec4<T> *__restrict__ uvec, Vec4<T> *__restrict__ part, unsigned *__restrict__ cnt,
+               Vec4<T> *__restrict__ ytop, int *err) {
+    extern __shared__ __align__(128) unsigned char top_raw[];
+    T *Ms = reinterpret_cast<T *>(top_raw);  // 2 kTopTile rows of kTopRow
+    __shared__ Vec4<T> f[kTopTile];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int last[2];
+    pdl_trigger();
+    int cb, rb0;
+    top_pair_coords(blockIdx.x, nb, cb, rb0);
+    const int nsub = min(2, nb - rb0);
+    const int tid = threadIdx.x, q = tid & 3, c0 = cb * kTopTile, row = tid >> 2;
+    const Vec4<T> zero{(T)0, (T)0, (T)0, (T)0};
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    top_pair_copy(M, ldt, n, rb0, nsub, c0, Ms, &bar);
+    {
+        // column d: thread q takes the right-hand side (q = 0) and the update
+        // vectors k0 + q, k0 + q + 4, ... in order; the first two indices early
+        const int d = c0 + (tid >> 2);
+        int kc = -1, k0 = 0, k1 = 0;
+        int64_t g0 = -1, g1 = -1;
+        if (d < n) {
+            if (q == 0) kc = col[d];
+            k0 = gptr[d] + q;
+            k1 = gptr[d + 1];
+            if (k0 < k1) g0 = gidx[k0];
+            if (k0 + 4 < k1) g1 = gidx[k0 + 4];
+        }
+        pdl_wait();
+        T vx = 0, vy = 0, vz = 0;
+        if (kc >= 0) {
+            const Vec4<T> v = sol[kc];
+            vx = v.x;
+            vy = v.y;
+            vz = v.z;
+        }
+        const Vec4<T> u0 = g0 >= 0 ? ldcg4(uvec + g0) : zero, u1 = g1 >= 0 ? ldcg4(uvec + g1) : zero;
+        vx += u0.x;
+        vy += u0.y;
+        vz += u0.z;
+        vx += u1.x;
+        vy += u1.y;
+        vz += u1.z;
+        for (int k = k0 + 8; k < k1; k += 4) {
+            const Vec4<T> u = ldcg4(uvec + gidx[k]);
+            vx += u.x;
+            vy += u.y;
+            vz += u.z;
+        }
+        quad_sum(vx, vy, vz);
+        if (q == 0) f[tid >> 2] = {vx, vy, vz, (T)0};
+    }
+    __syncthreads();
+    wait_chunk(&bar, 0, err);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const T *mr = Ms + (size_t)(h * kTopTile + row) * kTopRow;
+        T ax = 0, ay = 0, az = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int cl = 4 * q + 16 * k;
+            if (c0 + cl >= ldt) continue;  // not copied: past the matrix
+            const Vec4<T> m = *reinterpret_cast<const Vec4<T> *>(mr + cl);
+            const Vec4<T> f0 = f[cl], f1 = f[cl + 1], f2 = f[cl + 2], f3 = f[cl + 3];
+            ax += m.x * f0.x + m.y * f1.x + m.z * f2.x + m.w * f3.x;
+            ay += m.x * f0.y + m.y * f1.y + m.z * f2.y + m.w * f3.y;
+            az += m.x * f0.z + m.y * f1.z + m.z * f2.z + m.w * f3.z;
+        }
+        quad_sum(ax, ay, az);
+        const int rb = rb0 + h;
+        // rows at or past n were not copied: their sums are never read
+        if (q == 0 && h < nsub) part[((int64_t)rb * (rb + 1) / 2 + cb) * kTopTile + row] = {ax, ay, az, (T)0};
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int h = 0; h < 2; ++h)
+            last[h] = h < nsub && atom_add_acq_rel(cnt + rb0 + h, 1u) == (unsigned)(rb0 + h);
+    __syncthreads();
+    for (int h = 0; h < nsub; ++h) {
+        if (!last[h]) continue;
+        const int rb = rb0 + h, r = rb * kTopTile + row;
+        const Vec4<T> *p = part + (int64_t)(rb * (rb + 1) / 2) * kTopTile + row;
+        T sx = 0, sy = 0, sz = 0;
+        top_partial_sum(p, q, rb + 1, sx, sy, sz);
+        quad_sum(sx, sy, sz);
+        if (q == 0 && r < n) ytop[r] = {sx, sy, sz, (T)0};
+        if (tid == 0) cnt[rb] = 0;
+    }
+}
+
+// Backward, x_top = T^T y_top, T read by columns: each tile of the pair adds
+// sum_r T(r, c) y_r over its rows into block column cb (nb - cb tiles), a
+// thread per column and row quarter (16 rows), the quarters combined in
+// shared memory in a fixed order; x into the solution and the positions
+// (mode 0: pc64 = x; mode 1: pc64 += x, pc32 = float(pc64)).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_top_pair_bwd(int n, int ldt, int nb, const T *__restrict__ M, const Vec4<T> *__restrict__ ytop,
+               Vec4<T> *__restrict__ part, unsigned *__restrict__ cnt, const int32_t *__restrict__ col,
+               Vec4<T> *__restrict__ sol, Vec4<double> *__restrict__ pc64, Vec4<float> *__restrict__ pc32,
+               int mode, int *err) {
+    extern __shared__ __align__(128) unsigned char top_raw[];
+    T *Ms = reinterpret_cast<T *>(top_raw);  // 2 kTopTile rows of kTopRow
+    __shared__ Vec4<T> y[2][kTopTile];
+    __shared__ Vec4<T> red[4][kTopTile];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int last;
+    pdl_trigger();
+    int cb, rb0;
+    top_pair_coords(blockIdx.x, nb, cb, rb0);
+    const int nsub = min(2, nb - rb0);
+    const int tid = threadIdx.x, c0 = cb * kTopTile;
+    const int cl = tid & (kTopTile - 1), q = tid >> 6, c = c0 + cl;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    top_pair_copy(M, ldt, n, rb0, nsub, c0, Ms, &bar);
+    const int oc = tid >> 2, j4 = tid & 3;  // the final sum's column and tile phase (see below)
+    const int kout = (j4 == 0 && c0 + oc < n) ? col[c0 + oc] : -1;
+    pdl_wait();
+    if (tid < 2 * kTopTile) {
+        const int r = rb0 * kTopTile + tid;
+        y[tid / kTopTile][tid % kTopTile] =
+            (tid < nsub * kTopTile && r < n) ? ytop[r] : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+    }
+    __syncthreads();
+    wait_chunk(&bar, 0, err);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        T ax = 0, ay = 0, az = 0;
+        if (c < n) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int rl = h * kTopTile + 16 * q + i;
+                if (rb0 * kTopTile + rl >= n) break;  // not copied: past the matrix
+                const T m = Ms[(size_t)rl * kTopRow + cl];
+                const Vec4<T> v = y[h][16 * q + i];
+                ax += m * v.x;
+                ay += m * v.y;
+                az += m * v.z;
+            }
+        }
+        red[q][cl] = {ax, ay, az, (T)0};
+        __syncthreads();
+        if (tid < kTopTile && h < nsub) {
+            Vec4<T> v = red[0][tid];
+#pragma unroll
+            for (int j = 1; j < 4; ++j) {
+                v.x += red[j][tid].x;
+                v.y += red[j][tid].y;
+                v.z += red[j][tid].z;
+            }
+            const int rb = rb0 + h;
+            part[((int64_t)rb * (rb + 1) / 2 + cb) * kTopTile + tid] = v;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) last = atom_add_acq_rel(cnt + cb, (unsigned)nsub) + (unsigned)nsub == (unsigned)(nb - cb);
+    __syncthreads();
+    if (!last) return;
+    // four threads per column (an aligned quad), thread j4 over the block
+    // column's tiles j4, j4 + 4, ... of block rows cb, cb + 1, ..., nb - 1
+    T sx = 0, sy = 0, sz = 0;
+    for (int j = j4; j < nb - cb; j += 32) {
+        Vec4<T> u[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int rr = cb + j + 4 * i;
+            u[i] = j + 4 * i < nb - cb ? ldcg4(part + ((int64_t)rr * (rr + 1) / 2 + cb) * kTopTile + oc)
+                                       : Vec4<T>{(T)0, (T)0, (T)0, (T)0};
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            sx += u[i].x;
+            sy += u[i].y;
+            sz += u[i].z;
+        }
+    }
+    quad_sum(sx, sy, sz);
+    if (kout >= 0) {
+        const int k = kout;
+        sol[k] = {sx, sy, sz, (T)0};
+        if (mode == 0) {
+            pc64[k] = {(double)sx, (double)sy, (double)sz, 0.0};
+        } else {
+            Vec4<double> p = pc64[k];
+            p.x += (double)sx;
+            p.y += (double)sy;
+            p.z += (double)sz;
+            pc64[k] = p;
+            pc32[k] = {(float)p.x, (float)p.y, (float)p.z, 0.f};
+        }
+    }
+    if (tid == 0) cnt[cb] = 0;
+}
+
+// One tile per CTA (tops whose tiles fit one wave), tile t = rb (rb + 1) / 2 + cb.
 // Forward, y_top = T f_top: tile (rb, cb) gathers f of its columns (four
 // threads per column over every fourth update vector), multiplies its rows
 // (four threads per row, 16 columns each) and adds the row sums into block
@@ -2795,13 +3041,20 @@ void launch_solve_fwd(const DevSym &s, const T *X, const T *L21, Vec4<T> *sol, V
             sol, uvec, ticket + 2, flags, err);
     }
     if (s.n_top > 0) {
-        // y_top = T f_top, f_top gathered by the tiles
+        // y_top = T f_top, f_top gathered by the tiles: one tile per CTA while
+        // they fit one wave, else two (the same sums either way)
         const int ldt = dense_ld(s.n_top);
         Vec4<T> *part = ytop + ldt;
         unsigned *cnt = reinterpret_cast<unsigned *>(part + top_tiles(s.n_top) * kTopTile);
-        launch_pdl(k_top_tile_fwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 256, 0, st, s.n_top, ldt, Ttop,
-                   (const int32_t *)s.top_col, (const int32_t *)s.top_gptr, (const int64_t *)s.top_gidx,
-                   (const Vec4<T> *)sol, (const Vec4<T> *)uvec, part, cnt, ytop);
+        if ((sizeof(T) == 4 ? s.top_pair32 : s.top_pair64) != 0)
+            launch_pdl(k_top_pair_fwd<T>, s.overlap != 0, (int)top_pairs(s.n_top), 256, top_pair_smem(sizeof(T)),
+                       st, s.n_top, ldt, top_blocks(s.n_top), Ttop, (const int32_t *)s.top_col,
+                       (const int32_t *)s.top_gptr, (const int64_t *)s.top_gidx, (const Vec4<T> *)sol,
+                       (const Vec4<T> *)uvec, part, cnt, ytop, err);
+        else
+            launch_pdl(k_top_tile_fwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 256, 0, st, s.n_top, ldt, Ttop,
+                       (const int32_t *)s.top_col, (const int32_t *)s.top_gptr, (const int64_t *)s.top_gidx,
+                       (const Vec4<T> *)sol, (const Vec4<T> *)uvec, part, cnt, ytop);
     }
 }
 
@@ -2816,8 +3069,13 @@ void launch_solve_bwd(const DevSym &s, const T *X, const T *L21T, Vec4<T> *sol, 
         const int ldt = dense_ld(s.n_top);
         Vec4<T> *part = const_cast<Vec4<T> *>(ytop) + ldt;
         unsigned *cnt = reinterpret_cast<unsigned *>(part + top_tiles(s.n_top) * kTopTile);
-        launch_pdl(k_top_tile_bwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 256, 0, st, s.n_top, ldt,
-                   top_blocks(s.n_top), Ttop, ytop, part, cnt, (const int32_t *)s.top_col, sol, pc64, pc32, mode);
+        if ((sizeof(T) == 4 ? s.top_pair32 : s.top_pair64) != 0)
+            launch_pdl(k_top_pair_bwd<T>, s.overlap != 0, (int)top_pairs(s.n_top), 256, top_pair_smem(sizeof(T)),
+                       st, s.n_top, ldt, top_blocks(s.n_top), Ttop, ytop, part, cnt, (const int32_t *)s.top_col, sol,
+                       pc64, pc32, mode, err);
+        else
+            launch_pdl(k_top_tile_bwd<T>, s.overlap != 0, (int)top_tiles(s.n_top), 256, 0, st, s.n_top, ldt,
+                       top_blocks(s.n_top), Ttop, ytop, part, cnt, (const int32_t *)s.top_col, sol, pc64, pc32, mode);
     }
     const size_t smem = solve_smem_bytes(s.max_ldx, s.max_ld21, sizeof(T));
     const int G = sizeof(T) == 4 ? s.solve_grid32 : s.solve_grid64;
@@ -2883,6 +3141,8 @@ int dense_inverse_rhs(int ldx_max, int ld21_max, int scalar_bytes) {
 int dense_ld(int n) { return (n + 3) & ~3; }
 int top_blocks(int n) { return (n + kTopTile - 1) / kTopTile; }
 size_t top_tiles(int n) { return (size_t)top_blocks(n) * (top_blocks(n) + 1) / 2; }
+size_t top_pairs(int n) { return (size_t)(top_blocks(n) + 1) * (top_blocks(n) + 1) / 4; }
+size_t top_pair_smem(int scalar_bytes) { return (size_t)2 * kTopTile * kTopRow * scalar_bytes; }
 size_t top_vec_bytes(int n, int scalar_bytes) {
     if (n <= 0) return 0;
     const size_t v = (size_t)4 * scalar_bytes;
@@ -2906,6 +3166,10 @@ static cudaError_t raise_inverse(int bytes) {
 cudaError_t configure_dense_smem(int inv32, int inv64) {
     cudaError_t e = raise_inverse<float>(inv32);
     if (e == cudaSuccess) e = raise_inverse<double>(inv64);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_pair_fwd<float>, (int)top_pair_smem(4));
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_pair_bwd<float>, (int)top_pair_smem(4));
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_pair_fwd<double>, (int)top_pair_smem(8));
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_top_pair_bwd<double>, (int)top_pair_smem(8));
     return e;
 }
 
@@ -2966,6 +3230,21 @@ int solve_resident_ctas(int smem_bytes, int scalar_bytes) {
     } else {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_solve_fwd<double>, kSolveThreads, smem_bytes);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_solve_bwd<double>, kSolveThreads, smem_bytes);
+    }
+    return std::max(1, std::min(a, b) * sms);
+}
+
+int top_tile_resident_ctas(int scalar_bytes) {
+    int dev = 0, sms = 0, a = 0, b = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        return 1;
+    if (scalar_bytes == 4) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_top_tile_fwd<float>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_top_tile_bwd<float>, 256, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_top_tile_fwd<double>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_top_tile_bwd<double>, 256, 0);
     }
     return std::max(1, std::min(a, b) * sms);
 }

@@ -94,6 +94,9 @@ struct DevSym {
     // dense top (levels [ltop, top) when n_top > 0, instead of cluster levels):
     // n_top columns, T = inv(L_top) formed by n_top_items CTAs
     int n_top, n_top_items, dense_ldx, dense_ld21;
+    // the top's products take two tiles per CTA (T staged in shared memory)
+    // when one tile per CTA would need more than one wave (FP32 / FP64)
+    int top_pair32, top_pair64;
     const int32_t *top_col;    // n_top: device column of each dense index
     const int32_t *top_gptr;   // n_top + 1: update-vector entries added to each dense row
     const int64_t *top_gidx;   // their offsets in the update-vector array
@@ -214,12 +217,15 @@ int dense_inverse_rhs(int ldx_max, int ld21_max, int scalar_bytes);
 int dense_ld(int n);
 size_t dense_top_elems(int n);
 // the products with T (forward) and T^T (backward, T read by columns) run
-// over kTopTile x kTopTile tiles of T's lower triangle, one CTA each; the
+// over kTopTile x kTopTile tiles of T's lower triangle, two per CTA; the
 // vector buffer (ytop) holds y_top, the tiles' partial products and one
 // arrival counter per block of kTopTile rows (zero between launches)
 constexpr int kTopTile = 64;
 int top_blocks(int n);
 size_t top_tiles(int n);
+size_t top_pairs(int n);  // CTAs of one product: tile pairs of a block column
+size_t top_pair_smem(int scalar_bytes);  // dynamic shared memory of a pair's rows of T
+int top_tile_resident_ctas(int scalar_bytes);  // one-tile CTAs resident at once on the device
 size_t top_vec_bytes(int n, int scalar_bytes);
 cudaError_t configure_dense_smem(int inv32, int inv64);
 // most columns of the dense top (its T must fit the device)

@@ -97,6 +97,7 @@ def test_pose_tile_and_launch_shape_give_identical_results(gpu):
     w = W.cfg_pose_batch(level=4, n_poses=19, iterations=7)
     with gpu.ArapContext(w.V, w.faces) as ctx:
         ctx.set_precision("mixed", 1)
+        ctx.set_dense_top(2048)  # the default is wider for an uncapped grid
         ctx.set_rest_positions(w.positions)
         ctx.set_constraints(w.cidx, w.poses[0])
         ref = ctx.deform_poses(w.poses, 7)

@@ -54,11 +54,13 @@ def test_graph_replay_matches_direct_launches(gpu, precision):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_solve_cta_count_does_not_change_results(gpu, precision):
     """The triangular solves give every supernode to whichever CTA takes its
-    ticket; one CTA, a few, or as many as fit compute the same numbers."""
+    ticket; one CTA, a few, or as many as fit compute the same numbers. (The
+    default dense top is wider for an uncapped grid, so it is pinned here.)"""
     w = W.cfg_twisted_bar(h=0.1, iterations=4)
     outs = []
     for n in (0, 1, 3, 64):
         with make(gpu, w, precision) as ctx:
+            ctx.set_dense_top(2048)
             ctx.set_solve_ctas(n)
             a = ctx.deform(4)
             ctx.set_targets(w.ctargets + 0.05)   # re-pose: same launch shape, counters carry on
@@ -153,14 +155,15 @@ def test_warp_solves_match_cta_solves(gpu, precision, tol):
 def test_level_schedule_matches_persistent(gpu, precision, workload):
     """One solve launch per tree level (arap_set_solve_schedule) runs the same
     tasks with the same sums as the persistent sweep: positions bit for bit
-    equal, with and without the dense top, and with a capped grid."""
+    equal, with and without the dense top (its cap pinned: the default is
+    wider for an uncapped grid), and with a capped grid."""
     from oracle import oracle as O
 
     w = (W.cfg_twisted_bar(h=0.05, iterations=8) if workload == "bar"
          else W.cfg_noisy_sphere(level=4, iterations=8))
     ok, ref = O.run_deform(w.positions, w.faces, w.cidx, w.ctargets, w.iterations)
     assert ok
-    for dense in (0, -1):
+    for dense in (2048, -1):
         outs = []
         for schedule, cap in (("persistent", 0), ("levels", 0), ("levels", 7)):
             with gpu.ArapContext(w.V, w.faces) as ctx:

@@ -37,6 +37,7 @@ def test_wait_limit_expires_and_context_recovers(gpu, precision):
     w = W.cfg_twisted_bar(h=0.05, iterations=10)
     with gpu.ArapContext(w.V, w.faces) as ctx:
         ctx.set_precision(precision, 1)
+        ctx.set_dense_top(-1)  # every level as supernode tasks that wait for their children
         ctx.set_rest_positions(w.positions)
         ctx.set_constraints(w.cidx, w.ctargets)
         good = ctx.deform(w.iterations)
