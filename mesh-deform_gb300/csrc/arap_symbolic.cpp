@@ -453,29 +453,6 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         }
         grow[a + 1] = (int32_t)gcol.size();
     }
-    // every free component must reach a constrained vertex, else L is singular
-    {
-        std::vector<int32_t> comp(m, -1), stack;
-        for (int a = 0; a < m; ++a) {
-            if (comp[a] >= 0) continue;
-            bool anchored = false;
-            stack.assign(1, a);
-            comp[a] = a;
-            while (!stack.empty()) {
-                const int x = stack.back();
-                stack.pop_back();
-                anchored |= touches_c[x] != 0;
-                for (int32_t q = grow[x]; q < grow[x + 1]; ++q)
-                    if (comp[gcol[q]] < 0) { comp[gcol[q]] = a; stack.push_back(gcol[q]); }
-            }
-            if (!anchored) {
-                singular = true;
-                err = "free vertex " + std::to_string(fvert[a]) +
-                      " belongs to a mesh component without constrained vertices (singular Laplacian)";
-                return false;
-            }
-        }
-    }
     if (!mesh_order) {
         nd_order(m, grow.data(), gcol.data(), sym.perm, sym.block_ptr);
     } else {
@@ -552,6 +529,24 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
                     if (next == -1) { sym.etree[i] = k; break; }
                     i = next;
                 }
+            }
+        }
+    }
+    // every free component must reach a constrained vertex, else L is
+    // singular; each component of the free graph is one tree of the
+    // elimination forest, so "touches a constrained vertex" is carried up to
+    // the roots (children come before their parents)
+    {
+        std::vector<uint8_t> anchored(m, 0);
+        for (int k = 0; k < m; ++k) anchored[k] = touches_c[sym.perm[k]];
+        for (int k = 0; k < m; ++k) {
+            const int32_t p = sym.etree[k];
+            if (p >= 0) anchored[p] |= anchored[k];
+            else if (!anchored[k]) {
+                singular = true;
+                err = "free vertex " + std::to_string(fvert[sym.perm[k]]) +
+                      " belongs to a mesh component without constrained vertices (singular Laplacian)";
+                return false;
             }
         }
     }
