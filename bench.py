@@ -48,6 +48,11 @@ from pathlib import Path
 
 import numpy as np
 
+# many requests in flight, one stream each: give every stream its own hardware
+# queue (CUDA's default of 8 makes streams share queues and wait on each other);
+# read when the process's CUDA context is created, so set before any CUDA use
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = Path(__file__).resolve().parent
 PKG = ROOT / "mesh-deform_gb300"
 for p in (str(ROOT), str(PKG)):
@@ -1115,6 +1120,7 @@ def run_requests(args):
              "vertex_launch": vtuned or "1 thread per vertex, 256-thread blocks",
              "solve_schedule": args.solve_schedule, "warp_rows": args.warp_rows,
              "solve_ctas": args.solve_ctas,
+             "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
              "solve_ctas_autotune": tuned,
              "symbolic_analysis": analysis,
              "step": f"{N} concurrent dirty deform requests, one host thread each (symbolic analysis "

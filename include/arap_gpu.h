@@ -150,7 +150,10 @@ int arap_pose_targets(arap_ctx *ctx, int32_t n_handles, const int32_t *handles, 
    best pinned, until arap_wait returns); arap_wait waits for it and returns
    its status. Any other call on the context first waits for a pending
    deform. Contexts on one device run concurrently, so one host thread can
-   keep several requests in flight. */
+   keep several requests in flight. Each context has its own stream; with more
+   contexts in flight than CUDA's hardware queues (CUDA_DEVICE_MAX_CONNECTIONS,
+   8 unless set), streams share queues and wait on each other, so set it (to
+   32) in the environment before the process's first CUDA call. */
 int arap_deform_async(arap_ctx *ctx, int32_t iterations, double *out_xyz);
 int arap_wait(arap_ctx *ctx);
 /* arap_deform_poses split the same way (completed by arap_wait or
