@@ -48,11 +48,6 @@ from pathlib import Path
 
 import numpy as np
 
-# many requests in flight, one stream each: give every stream its own hardware
-# queue (CUDA's default of 8 makes streams share queues and wait on each other);
-# read when the process's CUDA context is created, so set before any CUDA use
-os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
-
 ROOT = Path(__file__).resolve().parent
 PKG = ROOT / "mesh-deform_gb300"
 for p in (str(ROOT), str(PKG)):
@@ -854,6 +849,11 @@ def main():
         return run_serving(args)
     if args.workload == "mesh_batch":
         return run_mesh_batch(args)
+    # concurrent requests, one stream each: every stream gets its own hardware
+    # queue (with CUDA's default of 8, 16 streams share queues and wait on each
+    # other); read when the process's CUDA context is created, which happens
+    # after this point. The serving stream keeps the default (slower with 32).
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     return run_requests(args)
 
 

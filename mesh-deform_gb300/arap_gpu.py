@@ -12,20 +12,11 @@ Two layers:
   adapter (arap.h:133-135). Returns False where the reference returns false.
 
 There is no CPU fallback: a missing library or device raises.
-
-Contexts deforming at the same time each own a stream; CUDA maps streams onto
-CUDA_DEVICE_MAX_CONNECTIONS hardware queues (8 unless set), and streams that
-share a queue wait on each other's work. Importing this module raises the
-default to 32 when the variable is unset; it takes effect only if no CUDA
-context exists yet in the process (import this module before other CUDA users).
 """
 from __future__ import annotations
 
 import ctypes as C
-import os
 from pathlib import Path
-
-os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np
 
