@@ -484,11 +484,12 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
         A[r][c] = (r < w && c <= r) ? P[(int64_t)(j0 + c) * n + j0 + r] : (TF)0;
         X[r][c] = (TF)0;
     }
-    // triangle table: column jj from NB-1 down to 0, rows jj..NB-1
-    for (int t = tid; t < kTri; t += kFdtThreads) {
-        int jj = NB - 1, base = 0;
-        while (t >= base + (NB - jj)) {
-            base += NB - jj;
+    // triangle table of the block's w columns: column jj from w-1 down to 0,
+    // rows jj..w-1 (a narrow block issues no FP64 work for absent rows)
+    for (int t = tid; t < w * (w + 1) / 2; t += kFdtThreads) {
+        int jj = w - 1, base = 0;
+        while (t >= base + (w - jj)) {
+            base += w - jj;
             --jj;
         }
         tri_j[t] = (uint8_t)jj;
@@ -510,10 +511,10 @@ k_fdt(const FItem *__restrict__ items, int jb, const SnInfo *__restrict__ sn, TF
         const TF r = rinv[k];
         for (int i = k + 1 + tid; i < w; i += kFdtThreads) A[i][k] *= r;
         __syncthreads();
-        const int T = (NB - 1 - k) * (NB - k) / 2;  // entries of columns k+1..NB-1
+        const int T = (w - 1 - k) * (w - k) / 2;  // entries of columns k+1..w-1
         for (int t = tid; t < T; t += kFdtThreads) {
             const int i = tri_i[t], jj = tri_j[t];
-            if (i < w) A[i][jj] -= A[i][k] * A[jj][k];
+            A[i][jj] -= A[i][k] * A[jj][k];
         }
         __syncthreads();
     }
