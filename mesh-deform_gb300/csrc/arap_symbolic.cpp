@@ -427,6 +427,16 @@ int64_t symbolic_factor_nnz(Symbolic &sym) {
     return nz;
 }
 
+namespace {
+// a thread joined when it goes out of scope (also on early returns)
+struct JoinOnExit {
+    std::thread t;
+    ~JoinOnExit() {
+        if (t.joinable()) t.join();
+    }
+};
+}  // namespace
+
 bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
                     std::string &err, bool &singular, bool mesh_order) {
     singular = false;
@@ -491,12 +501,14 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     for (int v = 0; v < V; ++v)
         if (constrained[v]) sym.newidx[v] = nc++;
     for (int v = 0; v < V; ++v) sym.oldidx[sym.newidx[v]] = v;
-    // adjacency in device order
+    // adjacency in device order, on a second thread while the elimination
+    // tree and the supernodes are built (it only writes drow, dcol, dent)
     const int nnz = topo.nnz();
-    sym.drow.assign(V + 1, 0);
-    sym.dcol.resize(nnz);
-    sym.dent.resize(nnz);
-    {
+    JoinOnExit adj;
+    adj.t = std::thread([&sym, &topo, V, nnz] {
+        sym.drow.assign(V + 1, 0);
+        sym.dcol.resize(nnz);
+        sym.dent.resize(nnz);
         int32_t e = 0;
         for (int k = 0; k < V; ++k) {
             const int v = sym.oldidx[k];
@@ -507,7 +519,7 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
             }
             sym.drow[k + 1] = e;
         }
-    }
+    });
     // permuted free graph: adjacency of device index k < m (neighbours < m)
     std::vector<int32_t> prow(m + 1, 0), pcol;
     pcol.reserve(gcol.size());
@@ -651,8 +663,7 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
     // front position of every row of supernode s's front: its columns, then
     // its struct rows; filled for one supernode at a time (stamped by s), so
     // lookups below are direct
-    std::vector<int32_t> fpos(m, 0), fstamp(m, -1);
-    auto map_front = [&](int s) {
+    auto map_front = [&sym](int s, std::vector<int32_t> &fpos, std::vector<int32_t> &fstamp) {
         const SnInfo &d = sym.sn[s];
         for (int c = 0; c < d.ncol; ++c) {
             fpos[d.first + c] = c;
@@ -664,13 +675,42 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
             fstamp[rs[i]] = s;
         }
     };
+    // assembly maps (L_kk and L_lk = -w_kl, l > k, both free, into the
+    // panels) on a second thread, with their own front map, while the
+    // relative indices and the launch plan are built here
+    adj.t.join();
+    bool amap_ok = true;
+    JoinOnExit amap_th;
+    amap_th.t = std::thread([&sym, &map_front, &amap_ok, m, S, nnz] {
+        std::vector<int32_t> fpos(m, 0), fstamp(m, -1);
+        sym.amap.assign(nnz, -1);
+        sym.dmap.assign(m, -1);
+        for (int s = 0; s < S; ++s) {
+            const SnInfo &d = sym.sn[s];
+            map_front(s, fpos, fstamp);
+            for (int k = d.first; k < d.first + d.ncol; ++k) {
+                const int cidx = k - d.first;
+                sym.dmap[k] = d.panel_off + (int64_t)cidx * d.nrow + cidx;
+                for (int32_t e = sym.drow[k]; e < sym.drow[k + 1]; ++e) {
+                    const int32_t l = sym.dcol[e];
+                    if (l >= m || l <= k) continue;
+                    if (fstamp[l] != s) {
+                        amap_ok = false;
+                        return;
+                    }
+                    sym.amap[e] = d.panel_off + (int64_t)cidx * d.nrow + fpos[l];
+                }
+            }
+        }
+    });
+    std::vector<int32_t> fpos(m, 0), fstamp(m, -1);
     // relind: where each struct row of s sits in its parent's front
     sym.relind.reserve(sym.rows.size());
     for (int s = 0; s < S; ++s) sym.sn[s].relind_off = -1;
     for (int p = 0; p < S; ++p) {
         const SnInfo &pd = sym.sn[p];
         if (pd.child_begin == pd.child_end) continue;
-        map_front(p);
+        map_front(p, fpos, fstamp);
         for (int ci = pd.child_begin; ci < pd.child_end; ++ci) {
             SnInfo &d = sym.sn[sym.child[ci]];
             d.relind_off = (int32_t)sym.relind.size();
@@ -748,25 +788,10 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
             add(kFx, 0, fx);
         }
     }
-    // assembly maps: L_kk and L_lk = -w_kl (l > k, both free) into the panels
-    sym.amap.assign(nnz, -1);
-    sym.dmap.assign(m, -1);
-    for (int s = 0; s < S; ++s) {
-        const SnInfo &d = sym.sn[s];
-        map_front(s);
-        for (int k = d.first; k < d.first + d.ncol; ++k) {
-            const int cidx = k - d.first;
-            sym.dmap[k] = d.panel_off + (int64_t)cidx * d.nrow + cidx;
-            for (int32_t e = sym.drow[k]; e < sym.drow[k + 1]; ++e) {
-                const int32_t l = sym.dcol[e];
-                if (l >= m || l <= k) continue;
-                if (fstamp[l] != s) {
-                    err = "internal: matrix entry outside its supernode's front";
-                    return false;
-                }
-                sym.amap[e] = d.panel_off + (int64_t)cidx * d.nrow + fpos[l];
-            }
-        }
+    amap_th.t.join();
+    if (!amap_ok) {
+        err = "internal: matrix entry outside its supernode's front";
+        return false;
     }
     return true;
 }
