@@ -528,9 +528,11 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         for (int32_t q = grow[a]; q < grow[a + 1]; ++q) pcol.push_back(iperm[gcol[q]]);
         prow[k + 1] = (int32_t)pcol.size();
     }
-    // elimination tree (Liu, with path compression) and factor column counts
-    sym.etree.assign(m, -1);
-    {
+    // elimination tree (Liu, with path compression), on a helper thread while
+    // the supernodes' rows are built (they follow from the dissection's blocks)
+    JoinOnExit et;
+    et.t = std::thread([&sym, &prow, &pcol, m] {
+        sym.etree.assign(m, -1);
         std::vector<int32_t> anc(m, -1);
         for (int k = 0; k < m; ++k) {
             for (int32_t q = prow[k]; q < prow[k + 1]; ++q) {
@@ -543,25 +545,7 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
                 }
             }
         }
-    }
-    // every free component must reach a constrained vertex, else L is
-    // singular; each component of the free graph is one tree of the
-    // elimination forest, so "touches a constrained vertex" is carried up to
-    // the roots (children come before their parents)
-    {
-        std::vector<uint8_t> anchored(m, 0);
-        for (int k = 0; k < m; ++k) anchored[k] = touches_c[sym.perm[k]];
-        for (int k = 0; k < m; ++k) {
-            const int32_t p = sym.etree[k];
-            if (p >= 0) anchored[p] |= anchored[k];
-            else if (!anchored[k]) {
-                singular = true;
-                err = "free vertex " + std::to_string(fvert[sym.perm[k]]) +
-                      " belongs to a mesh component without constrained vertices (singular Laplacian)";
-                return false;
-            }
-        }
-    }
+    });
     // the factor's nonzero count is only reported, so it is counted on demand
     // (symbolic_factor_nnz) rather than on every analysis
     sym.factor_nnz = -1;
@@ -608,6 +592,25 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
             if (chead[p] < 0) chead[p] = s;
             else cnext[ctail[p]] = s;
             ctail[p] = s;
+        }
+    }
+    et.t.join();
+    // every free component must reach a constrained vertex, else L is
+    // singular; each component of the free graph is one tree of the
+    // elimination forest, so "touches a constrained vertex" is carried up to
+    // the roots (children come before their parents)
+    {
+        std::vector<uint8_t> anchored(m, 0);
+        for (int k = 0; k < m; ++k) anchored[k] = touches_c[sym.perm[k]];
+        for (int k = 0; k < m; ++k) {
+            const int32_t p = sym.etree[k];
+            if (p >= 0) anchored[p] |= anchored[k];
+            else if (!anchored[k]) {
+                singular = true;
+                err = "free vertex " + std::to_string(fvert[sym.perm[k]]) +
+                      " belongs to a mesh component without constrained vertices (singular Laplacian)";
+                return false;
+            }
         }
     }
     // levels, offsets, struct rows, children, relative indices
