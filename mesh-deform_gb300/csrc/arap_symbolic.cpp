@@ -435,10 +435,36 @@ struct JoinOnExit {
         if (t.joinable()) t.join();
     }
 };
+
+// analyses running in this process (several requests prepared at once fill
+// the cores already; one alone splits its row loops over threads)
+std::atomic<int> g_analyses{0};
+struct AnalysisCount {
+    AnalysisCount() { g_analyses.fetch_add(1); }
+    ~AnalysisCount() { g_analyses.fetch_sub(1); }
+};
+
+// body(lo, hi) over [0, n): in up to four contiguous chunks on threads when
+// the range is large and no other analysis runs, else in one call
+template <typename F>
+void row_chunks(int n, F &&body) {
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int parts = (n >= 32768 && g_analyses.load() == 1) ? std::min(4, hw) : 1;
+    if (parts <= 1) {
+        body(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int p = 1; p < parts; ++p)
+        th.emplace_back([&body, n, p, parts] { body((int)((int64_t)n * p / parts), (int)((int64_t)n * (p + 1) / parts)); });
+    body(0, (int)((int64_t)n / parts));
+    for (auto &t : th) t.join();
+}
 }  // namespace
 
 bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constrained, Symbolic &sym,
                     std::string &err, bool &singular, bool mesh_order) {
+    const AnalysisCount counted;
     singular = false;
     sym = Symbolic();
     const int V = topo.V;
@@ -450,19 +476,35 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         if (!constrained[v]) { fidx[v] = (int32_t)fvert.size(); fvert.push_back(v); }
     const int m = (int)fvert.size();
     sym.m = m;
-    // graph of L's off-diagonal pattern over free indices (arap.h:319-330)
+    // graph of L's off-diagonal pattern over free indices (arap.h:319-330):
+    // row lengths, offsets, then the rows
     std::vector<int32_t> grow(m + 1, 0), gcol;
     std::vector<uint8_t> touches_c(m, 0);
-    for (int a = 0; a < m; ++a) {
-        const int v = fvert[a];
-        for (int32_t q = topo.rowptr[v]; q < topo.rowptr[v + 1]; ++q) {
-            const int u = topo.col[q];
-            if (u == v) continue;
-            if (constrained[u]) { touches_c[a] = 1; continue; }
-            gcol.push_back(fidx[u]);
+    row_chunks(m, [&](int lo, int hi) {
+        for (int a = lo; a < hi; ++a) {
+            const int v = fvert[a];
+            int32_t c = 0;
+            for (int32_t q = topo.rowptr[v]; q < topo.rowptr[v + 1]; ++q) {
+                const int u = topo.col[q];
+                if (u == v) continue;
+                if (constrained[u]) { touches_c[a] = 1; continue; }
+                ++c;
+            }
+            grow[a + 1] = c;
         }
-        grow[a + 1] = (int32_t)gcol.size();
-    }
+    });
+    for (int a = 0; a < m; ++a) grow[a + 1] += grow[a];
+    gcol.resize(grow[m]);
+    row_chunks(m, [&](int lo, int hi) {
+        for (int a = lo; a < hi; ++a) {
+            const int v = fvert[a];
+            int32_t e = grow[a];
+            for (int32_t q = topo.rowptr[v]; q < topo.rowptr[v + 1]; ++q) {
+                const int u = topo.col[q];
+                if (u != v && !constrained[u]) gcol[e++] = fidx[u];
+            }
+        }
+    });
     if (!mesh_order) {
         nd_order(m, grow.data(), gcol.data(), sym.perm, sym.block_ptr);
     } else {
@@ -521,13 +563,15 @@ bool build_symbolic(const Topology &topo, const std::vector<uint8_t> &constraine
         }
     });
     // permuted free graph: adjacency of device index k < m (neighbours < m)
-    std::vector<int32_t> prow(m + 1, 0), pcol;
-    pcol.reserve(gcol.size());
-    for (int k = 0; k < m; ++k) {
-        const int a = sym.perm[k];
-        for (int32_t q = grow[a]; q < grow[a + 1]; ++q) pcol.push_back(iperm[gcol[q]]);
-        prow[k + 1] = (int32_t)pcol.size();
-    }
+    std::vector<int32_t> prow(m + 1, 0), pcol(gcol.size());
+    for (int k = 0; k < m; ++k) prow[k + 1] = prow[k] + (grow[sym.perm[k] + 1] - grow[sym.perm[k]]);
+    row_chunks(m, [&](int lo, int hi) {
+        for (int k = lo; k < hi; ++k) {
+            const int a = sym.perm[k];
+            int32_t e = prow[k];
+            for (int32_t q = grow[a]; q < grow[a + 1]; ++q) pcol[e++] = iperm[gcol[q]];
+        }
+    });
     // elimination tree (Liu, with path compression), on a helper thread while
     // the supernodes' rows are built (they follow from the dissection's blocks)
     JoinOnExit et;
