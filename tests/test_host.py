@@ -186,3 +186,26 @@ def test_dissection_of_a_mesh_batch_orders_each_mesh_as_alone(gpu):
     again = gpu.analyze_pattern(int(offs[-1]), faces, cidx)
     for key in ("perm", "etree", "block_ptr"):
         np.testing.assert_array_equal(union[key], again[key])
+
+
+def test_concurrent_analyses_match_a_lone_analysis(gpu):
+    """Several analyses at once (the library splits its row loops over threads
+    only when an analysis runs alone) give the ordering, elimination tree and
+    blocks of a lone analysis."""
+    import threading
+
+    w = W.cfg_twisted_bar(h=0.025)
+    alone = gpu.analyze_pattern(w.V, w.faces, w.cidx)
+    outs = [None] * 4
+
+    def run(i):
+        outs[i] = gpu.analyze_pattern(w.V, w.faces, w.cidx)
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(len(outs))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for o in outs:
+        for key in ("perm", "etree", "block_ptr"):
+            np.testing.assert_array_equal(o[key], alone[key])
